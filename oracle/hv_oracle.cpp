@@ -1,0 +1,1216 @@
+/*
+ * hv_oracle.cpp -- CPU oracle for the GB300 HighVoronoi hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (parity checker, smoke check, CPU baseline).  The
+ * product library never links this file.
+ *
+ * What it restates (reference = HighVoronoi.jl v1.4.2):
+ *  - kd-tree: leaf size 10, split on the dimension of maximal spread at the
+ *    balanced index of find_split  (src/NearestNeighborModified/kd_tree.jl:27-158,
+ *    tree_ops.jl:11-43).  Node boxes are tight bounding boxes.
+ *  - incircle raycast: from vertex r along u, the next generator is the
+ *    argmin over u.(x_j - x_0) > 0 of t_j = (|x_j - r|^2 - |x_0 - r|^2) /
+ *    (2 u.(x_j - x_0))  (src/raycast.jl:794-970, get_t src/raycast.jl:395-397).
+ *    The search is the fused shrinking-ball traversal of RCCombined
+ *    (src/raycast.jl:504-528, kd_tree.jl:269-336).
+ *  - boundary: cuboid planes enter as mirror generators N+p
+ *    (src/raycast.jl:354-375, src/boundary.jl:206-211,518-534).  The mirror of
+ *    the cell's generator across plane p has t equal to the plane crossing of
+ *    the ray, which is what is evaluated here.
+ *  - ray direction: unit vector orthogonal to the edge's generator span,
+ *    pointing away from the dropped generator (u_qr, src/tools.jl:773-790).
+ *  - descent: d successive raycasts from x_i along random directions
+ *    orthogonal to the current span (src/raycast.jl:45-109, randray :211-239).
+ *  - per-cell exploration: LIFO queue over the cell's vertices with an edge
+ *    registry that closes an edge once both end points are known
+ *    (src/sysvoronoi.jl:384-442,490-525; src/edgehashing.jl:49-111).
+ *    Mode 1 walks only edges whose minimal generator is the current cell and
+ *    seeds a cell from vertices found by lower cells (sysvoronoi.jl:496).
+ *  - neighbours: sorted union of the generators of a cell's vertices
+ *    (src/neighbors.jl:219-258).
+ *  - VI_POLYGON: flag decomposition facet > ... > edge with face midpoints,
+ *    cone volume sum |det| / d!, area = V_ik d / h_ik, interfaces computed by
+ *    the lower cell and copied (src/polyintegrator.jl:174-468,
+ *    src/cleanup_cell.jl:174-204, src/Leibnitzrule.jl).
+ *  - VI_HEURISTIC_MC: t = min over neighbours, V = pi^(d/2)/Gamma(1+d/2)
+ *    mean(t^d), A_j = d * const * mean(t^(d-1)/|n_j.u|), two-sided averaging
+ *    with volume correction (src/mcintegrator.jl:98-226, src/heuristic_mc.jl).
+ *    Directions are i.i.d. Philox4x32-10 Gaussians (the reference's
+ *    new_directions! reuses one vector, src/mcintegrator.jl:82-95).
+ *
+ * Exactness: FP64 decisions carry a forward error bound (scaled by a condition
+ * estimate of the vertex system); a decision that is not certified is redone
+ * in binary128 (__float128 on x86-64, long double on AArch64).  Ties that
+ * survive binary128 are counted as degenerate.
+ */
+#include "hv_oracle.h"
+
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#if defined(__x86_64__) || defined(__i386__)
+typedef __float128 qreal;
+#else
+typedef long double qreal;
+#endif
+static_assert(sizeof(qreal) == 16, "binary128 required");
+
+namespace {
+
+constexpr int MAXD = 8;
+constexpr double EPS = 1.1102230246251565e-16;  // 2^-53
+
+std::mutex g_err_mu;
+std::string g_last_err;
+void set_err(const std::string& s) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_last_err = s;
+}
+
+/* ---------------- Philox4x32-10 (Salmon et al., SC'11) ---------------- */
+struct U4 { uint32_t v[4]; };
+inline U4 philox(U4 c, uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c.v[0];
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c.v[2];
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        U4 o;
+        o.v[0] = hi1 ^ c.v[1] ^ k0;
+        o.v[1] = lo1;
+        o.v[2] = hi0 ^ c.v[3] ^ k1;
+        o.v[3] = lo0;
+        c = o;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+/* d Gaussian numbers for (stream, a, b) with key seed: counter (a, b_lo, b_hi, blk). */
+void philox_gauss(uint64_t seed, uint32_t a, uint64_t b, int d, double* g) {
+    int got = 0;
+    for (uint32_t blk = 0; got < d; ++blk) {
+        U4 c{{a, (uint32_t)b, (uint32_t)(b >> 32), blk}};
+        U4 o = philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+        for (int p = 0; p < 2 && got < d; ++p) {
+            double u1 = ((double)o.v[2 * p] + 0.5) * 2.3283064365386963e-10;
+            double u2 = ((double)o.v[2 * p + 1] + 0.5) * 2.3283064365386963e-10;
+            double rr = std::sqrt(-2.0 * std::log(u1));
+            g[got++] = rr * std::cos(6.283185307179586 * u2);
+            if (got < d) g[got++] = rr * std::sin(6.283185307179586 * u2);
+        }
+    }
+}
+
+/* ---------------- problem + kd-tree ---------------- */
+struct KdNode {
+    double lo[MAXD], hi[MAXD];
+    int left, right;  // -1 for leaves
+    int start, end;   // range in perm
+};
+
+struct Problem {
+    int d = 0;
+    int n = 0;
+    std::vector<double> X;  // n*d
+    double blo[MAXD], bhi[MAXD];
+    std::vector<KdNode> nodes;
+    std::vector<int> perm;
+    uint64_t seed = 0;
+    const double* x(int i) const { return &X[(size_t)i * d]; }
+    bool is_plane(int item) const { return item >= n; }
+};
+
+/* Balanced split index of the reference kd-tree (tree_ops.jl:11-43), 0-based offsets. */
+int find_split(int low, int leafsize, int n_p) {
+    int n_leafs = (n_p + leafsize - 1) / leafsize;
+    int k = 0;
+    while ((1 << (k + 1)) <= n_leafs) ++k;
+    int rest = n_leafs - (1 << k);
+    int mid;
+    if (n_p <= 2 * leafsize) mid = leafsize;
+    else if (k >= 1 && rest > (1 << (k - 1))) mid = (1 << k) * leafsize;
+    else if (rest == 0) mid = (1 << (k - 1)) * leafsize;
+    else mid = n_p - (1 << (k - 1)) * leafsize;
+    return mid + low;
+}
+
+int build_node(Problem& P, int start, int end) {
+    const int d = P.d;
+    KdNode nd;
+    for (int k = 0; k < d; ++k) { nd.lo[k] = INFINITY; nd.hi[k] = -INFINITY; }
+    for (int s = start; s < end; ++s) {
+        const double* p = P.x(P.perm[s]);
+        for (int k = 0; k < d; ++k) { nd.lo[k] = std::min(nd.lo[k], p[k]); nd.hi[k] = std::max(nd.hi[k], p[k]); }
+    }
+    nd.start = start; nd.end = end; nd.left = nd.right = -1;
+    int id = (int)P.nodes.size();
+    P.nodes.push_back(nd);
+    const int leafsize = 10;
+    if (end - start <= leafsize) return id;
+    int dim = 0; double spread = -1;
+    for (int k = 0; k < d; ++k) if (nd.hi[k] - nd.lo[k] > spread) { spread = nd.hi[k] - nd.lo[k]; dim = k; }
+    int mid = find_split(start, leafsize, end - start);
+    std::nth_element(P.perm.begin() + start, P.perm.begin() + mid, P.perm.begin() + end,
+                     [&](int a, int b) { double xa = P.x(a)[dim], xb = P.x(b)[dim]; return xa < xb || (xa == xb && a < b); });
+    int l = build_node(P, start, mid);
+    int r = build_node(P, mid, end);
+    P.nodes[id].left = l; P.nodes[id].right = r;
+    return id;
+}
+
+void build_tree(Problem& P) {
+    P.perm.resize(P.n);
+    for (int i = 0; i < P.n; ++i) P.perm[i] = i;
+    P.nodes.clear();
+    if (P.n > 0) build_node(P, 0, P.n);
+}
+
+/* ---------------- small dense linear algebra ---------------- */
+template <class T>
+bool lu_factor(int d, T A[MAXD][MAXD], int piv[MAXD]) {
+    for (int c = 0; c < d; ++c) {
+        int p = c; T best = A[c][c] < 0 ? -A[c][c] : A[c][c];
+        for (int r = c + 1; r < d; ++r) { T v = A[r][c] < 0 ? -A[r][c] : A[r][c]; if (v > best) { best = v; p = r; } }
+        if (best == 0) return false;
+        piv[c] = p;
+        if (p != c) for (int k = 0; k < d; ++k) std::swap(A[c][k], A[p][k]);
+        for (int r = c + 1; r < d; ++r) {
+            T f = A[r][c] / A[c][c];
+            A[r][c] = f;
+            for (int k = c + 1; k < d; ++k) A[r][k] -= f * A[c][k];
+        }
+    }
+    return true;
+}
+template <class T>
+void lu_solve(int d, T A[MAXD][MAXD], const int piv[MAXD], T* b) {
+    for (int c = 0; c < d; ++c) { if (piv[c] != c) std::swap(b[c], b[piv[c]]); }
+    for (int r = 0; r < d; ++r) for (int k = 0; k < r; ++k) b[r] -= A[r][k] * b[k];
+    for (int r = d - 1; r >= 0; --r) { for (int k = r + 1; k < d; ++k) b[r] -= A[r][k] * b[k]; b[r] /= A[r][r]; }
+}
+
+/* Constraint row of item `it` relative to anchor a (real): bisector rows are
+ * x_g - x_a with rhs |x_g - x_a|^2/2; plane rows are +-e_k with rhs the signed
+ * offset of the plane from x_a. */
+template <class T>
+void constraint_row(const Problem& P, int a, int it, T* row, T& rhs) {
+    const int d = P.d;
+    const double* xa = P.x(a);
+    if (!P.is_plane(it)) {
+        const double* xg = P.x(it);
+        T s = 0;
+        for (int k = 0; k < d; ++k) { row[k] = (T)xg[k] - (T)xa[k]; s += row[k] * row[k]; }
+        rhs = s / 2;
+    } else {
+        int p = it - P.n, k = p / 2;
+        for (int q = 0; q < d; ++q) row[q] = 0;
+        if (p % 2 == 0) { row[k] = 1; rhs = (T)P.bhi[k] - (T)xa[k]; }
+        else { row[k] = -1; rhs = (T)xa[k] - (T)P.blo[k]; }
+    }
+}
+
+struct VertexSys {
+    double rho[MAXD];          // center - x_a
+    double Minv[MAXD][MAXD];   // inverse of the constraint matrix
+    double cond;
+    bool ok;
+};
+
+/* FP64 circumcentre of the sorted signature S (d+1 items, S[0] real). */
+VertexSys solve_vertex(const Problem& P, const int* S) {
+    const int d = P.d;
+    VertexSys V; V.ok = false;
+    double M[MAXD][MAXD], A[MAXD][MAXD], rhs[MAXD];
+    int a = S[0];
+    for (int r = 0; r < d; ++r) constraint_row<double>(P, a, S[r + 1], M[r], rhs[r]);
+    double nrm = 0;
+    for (int r = 0; r < d; ++r) { double s = 0; for (int k = 0; k < d; ++k) { A[r][k] = M[r][k]; s += std::fabs(M[r][k]); } nrm = std::max(nrm, s); }
+    int piv[MAXD] = {0};
+    if (!lu_factor<double>(d, A, piv)) return V;
+    for (int k = 0; k < d; ++k) V.rho[k] = rhs[k];
+    lu_solve<double>(d, A, piv, V.rho);
+    for (int c = 0; c < d; ++c) {
+        double col[MAXD];
+        for (int k = 0; k < d; ++k) col[k] = (k == c) ? 1.0 : 0.0;
+        lu_solve<double>(d, A, piv, col);
+        for (int k = 0; k < d; ++k) V.Minv[k][c] = col[k];
+    }
+    double ninv = 0;
+    for (int r = 0; r < d; ++r) { double s = 0; for (int k = 0; k < d; ++k) s += std::fabs(V.Minv[r][k]); ninv = std::max(ninv, s); }
+    V.cond = nrm * ninv;
+    V.ok = std::isfinite(V.cond);
+    return V;
+}
+
+/* Direction of the edge S \ {S[m]} leaving vertex S.  Returns false if the edge
+ * holds no real generator.  lam = u.(x_b - x_a) for the kept real b used as
+ * the reference point of the t formula, db = x_b - x_a. */
+bool edge_direction(const Problem& P, const int* S, const VertexSys& V, int m, double* u, double& lam, double* db) {
+    const int d = P.d;
+    for (int k = 0; k < d; ++k) { u[k] = 0; db[k] = 0; }
+    lam = 0;
+    if (m >= 1) {
+        for (int k = 0; k < d; ++k) u[k] = -V.Minv[k][m - 1];
+    } else {
+        int b = -1;
+        for (int r = 0; r < d; ++r) {
+            if (!P.is_plane(S[r + 1])) {
+                if (b < 0) b = S[r + 1];
+                for (int k = 0; k < d; ++k) u[k] += V.Minv[k][r];
+            }
+        }
+        if (b < 0) return false;
+        const double* xa = P.x(S[0]); const double* xb = P.x(b);
+        for (int k = 0; k < d; ++k) db[k] = xb[k] - xa[k];
+    }
+    double nu = 0;
+    for (int k = 0; k < d; ++k) nu += u[k] * u[k];
+    nu = std::sqrt(nu);
+    if (!(nu > 0)) return false;
+    for (int k = 0; k < d; ++k) u[k] /= nu;
+    for (int k = 0; k < d; ++k) lam += u[k] * db[k];
+    return true;
+}
+
+/* ---------------- the incircle search ---------------- */
+struct Cand { int item; double t, lo, hi; };
+
+struct RayQuery {
+    int a;
+    double rho[MAXD], u[MAXD], db[MAXD];
+    double lam;
+    const int* excl; int nexcl;  // sorted excluded items
+    double erho, eu;             // absolute error bounds of rho and u components
+};
+
+struct RayResult {
+    Cand best;
+    double second_lo;
+    std::vector<Cand> amb;
+    bool certified;
+};
+
+inline bool excluded(const RayQuery& q, int it) {
+    for (int s = 0; s < q.nexcl; ++s) if (q.excl[s] == it) return true;
+    return false;
+}
+
+struct Searcher {
+    const Problem& P;
+    explicit Searcher(const Problem& p) : P(p) {}
+
+    static void consider(RayResult& R, const Cand& c) {
+        if (c.lo < R.best.lo) {
+            if (R.best.item >= 0) R.second_lo = R.best.lo;
+            if (R.best.item >= 0 && R.best.lo <= c.hi) R.amb.push_back(R.best);
+            R.best = c;
+        } else {
+            if (c.lo < R.second_lo) R.second_lo = c.lo;
+            if (c.lo <= R.best.hi) R.amb.push_back(c);
+        }
+        if (R.amb.size() > 256) {
+            std::vector<Cand> keep;
+            for (auto& x : R.amb) if (x.lo <= R.best.hi) keep.push_back(x);
+            R.amb.swap(keep);
+        }
+    }
+
+    void eval_point(const RayQuery& q, int j, RayResult& R) const {
+        const int d = P.d;
+        const double* xa = P.x(q.a); const double* xj = P.x(j);
+        double nd = 0, dr = 0, du = 0, sdr = 0, sdu = 0, l1 = 0;
+        for (int k = 0; k < d; ++k) {
+            double dl = xj[k] - xa[k];
+            nd += dl * dl; dr += dl * q.rho[k]; du += dl * q.u[k];
+            sdr += std::fabs(dl * q.rho[k]); sdu += std::fabs(dl * q.u[k]); l1 += std::fabs(dl);
+        }
+        double num = nd - 2.0 * dr;
+        double den = 2.0 * (du - q.lam);
+        double e_num = (4.0 * d + 8.0) * EPS * (nd + 2.0 * sdr) + 2.0 * l1 * q.erho;
+        double e_den = (2.0 * d + 8.0) * EPS * 2.0 * (sdu + std::fabs(q.lam)) + 4.0 * l1 * q.eu;
+        Cand c; c.item = j;
+        if (den > e_den) {
+            c.t = num / den;
+            double et = (e_num + std::fabs(c.t) * e_den) / (den - e_den) + 4.0 * EPS * std::fabs(c.t);
+            c.lo = c.t - et; c.hi = c.t + et;
+        } else if (den < -e_den) {
+            return;
+        } else {
+            if (num - e_num > 0) {
+                if (!(den + e_den > 0)) return;
+                c.lo = (num - e_num) / (den + e_den); c.hi = INFINITY; c.t = c.lo;
+            } else {
+                c.lo = -INFINITY; c.hi = INFINITY; c.t = 0;
+            }
+        }
+        if (c.lo < R.best.hi || c.lo < R.second_lo) consider(R, c);
+    }
+
+    void eval_planes(const RayQuery& q, RayResult& R) const {
+        const int d = P.d;
+        const double* xa = P.x(q.a);
+        for (int p = 0; p < 2 * d; ++p) {
+            int it = P.n + p;
+            if (excluded(q, it)) continue;
+            int k = p / 2; bool upper = (p % 2 == 0);
+            double uk = upper ? q.u[k] : -q.u[k];
+            double ck = xa[k] + q.rho[k];
+            double num = upper ? (P.bhi[k] - ck) : (ck - P.blo[k]);
+            double e_num = 4.0 * EPS * (std::fabs(P.bhi[k]) + std::fabs(P.blo[k]) + std::fabs(xa[k]) + std::fabs(q.rho[k])) + q.erho;
+            double e_den = q.eu + 2.0 * EPS * std::fabs(uk);
+            Cand c; c.item = it;
+            if (uk > e_den) {
+                c.t = num / uk;
+                double et = (e_num + std::fabs(c.t) * e_den) / (uk - e_den) + 4.0 * EPS * std::fabs(c.t);
+                c.lo = c.t - et; c.hi = c.t + et;
+            } else if (uk < -e_den) {
+                continue;
+            } else {
+                if (num - e_num > 0) { c.lo = (num - e_num) / (std::fabs(uk) + e_den); c.hi = INFINITY; c.t = c.lo; }
+                else { c.lo = -INFINITY; c.hi = INFINITY; c.t = 0; }
+            }
+            consider(R, c);
+        }
+    }
+
+    /* Shrinking-ball kd-tree search for argmin t. */
+    RayResult search(const RayQuery& q) const {
+        const int d = P.d;
+        RayResult R;
+        R.best = Cand{-1, INFINITY, INFINITY, INFINITY};
+        R.second_lo = INFINITY;
+        eval_planes(q, R);
+        const double* xa = P.x(q.a);
+        int stack[128]; int sp = 0;
+        if (!P.nodes.empty()) stack[sp++] = 0;
+        while (sp > 0) {
+            int ni = stack[--sp];
+            const KdNode& nd = P.nodes[ni];
+            double tp = R.best.hi;
+            if (std::isfinite(tp)) {
+                double tpp = tp * (1.0 + 1e-9) + 1e-300;
+                double c[MAXD], r2 = 0, dist2 = 0;
+                for (int k = 0; k < d; ++k) {
+                    double off = q.rho[k] + tpp * q.u[k];
+                    c[k] = xa[k] + off;
+                    double w = q.db[k] - off; r2 += w * w;
+                    double e = 0;
+                    if (c[k] < nd.lo[k]) e = nd.lo[k] - c[k]; else if (c[k] > nd.hi[k]) e = c[k] - nd.hi[k];
+                    dist2 += e * e;
+                }
+                if (dist2 > r2 * (1.0 + 1e-9) + 1e-280) continue;
+            }
+            if (nd.left < 0) {
+                for (int s = nd.start; s < nd.end; ++s) {
+                    int j = P.perm[s];
+                    if (excluded(q, j)) continue;
+                    eval_point(q, j, R);
+                }
+            } else {
+                // visit the child nearer to the current ball centre first
+                double tp2 = std::isfinite(R.best.hi) ? R.best.hi : 0.0;
+                double dl = 0, dr = 0;
+                const KdNode& L = P.nodes[nd.left]; const KdNode& Rr = P.nodes[nd.right];
+                for (int k = 0; k < d; ++k) {
+                    double ck = xa[k] + q.rho[k] + tp2 * q.u[k];
+                    double e1 = ck < L.lo[k] ? L.lo[k] - ck : (ck > L.hi[k] ? ck - L.hi[k] : 0);
+                    double e2 = ck < Rr.lo[k] ? Rr.lo[k] - ck : (ck > Rr.hi[k] ? ck - Rr.hi[k] : 0);
+                    dl += e1 * e1; dr += e2 * e2;
+                }
+                if (sp + 2 > 128) { set_err("kd stack overflow"); break; }
+                if (dl <= dr) { stack[sp++] = nd.right; stack[sp++] = nd.left; }
+                else { stack[sp++] = nd.left; stack[sp++] = nd.right; }
+            }
+        }
+        std::vector<Cand> keep;
+        for (auto& c : R.amb) if (c.item != R.best.item && c.lo <= R.best.hi) keep.push_back(c);
+        R.amb.swap(keep);
+        R.certified = R.best.item >= 0 && R.best.hi < R.second_lo;
+        return R;
+    }
+
+    /* Ball query: is any real generator (not in S) strictly inside the sphere
+     * around c with squared radius r2 (relative tolerance tol)? */
+    bool any_inside(const double* c, double r2, const int* S, int nS, double tol) const {
+        const int d = P.d;
+        int stack[128]; int sp = 0;
+        if (!P.nodes.empty()) stack[sp++] = 0;
+        while (sp > 0) {
+            const KdNode& nd = P.nodes[stack[--sp]];
+            double dist2 = 0;
+            for (int k = 0; k < d; ++k) {
+                double e = c[k] < nd.lo[k] ? nd.lo[k] - c[k] : (c[k] > nd.hi[k] ? c[k] - nd.hi[k] : 0);
+                dist2 += e * e;
+            }
+            if (dist2 >= r2) continue;
+            if (nd.left < 0) {
+                for (int s = nd.start; s < nd.end; ++s) {
+                    int j = P.perm[s];
+                    bool ex = false;
+                    for (int t = 0; t < nS; ++t) if (S[t] == j) ex = true;
+                    if (ex) continue;
+                    const double* xj = P.x(j);
+                    double dd = 0;
+                    for (int k = 0; k < d; ++k) { double e = xj[k] - c[k]; dd += e * e; }
+                    if (dd < r2 * (1.0 - tol)) return true;
+                }
+            } else {
+                if (sp + 2 > 128) return true;
+                stack[sp++] = nd.left; stack[sp++] = nd.right;
+            }
+        }
+        return false;
+    }
+};
+
+/* ---------------- binary128 re-scoring ---------------- */
+inline qreal qabs(qreal v) { return v < 0 ? -v : v; }
+
+/* Re-decide a walk ray from vertex S (dropped position m) among candidate items
+ * in binary128.  Returns the winning item; sets degenerate if the two best
+ * survive as a tie. */
+int quad_rescore_walk(const Problem& P, const int* S, int m, const std::vector<int>& items, bool& degenerate) {
+    const int d = P.d;
+    qreal M[MAXD][MAXD], rhs[MAXD];
+    int a = S[0];
+    for (int r = 0; r < d; ++r) constraint_row<qreal>(P, a, S[r + 1], M[r], rhs[r]);
+    int piv[MAXD] = {0};
+    degenerate = false;
+    if (!lu_factor<qreal>(d, M, piv)) { degenerate = true; return items.empty() ? -1 : items[0]; }
+    qreal rho[MAXD];
+    for (int k = 0; k < d; ++k) rho[k] = rhs[k];
+    lu_solve<qreal>(d, M, piv, rho);
+    qreal u[MAXD], db[MAXD];
+    for (int k = 0; k < d; ++k) { u[k] = 0; db[k] = 0; }
+    const double* xa = P.x(a);
+    if (m >= 1) {
+        qreal col[MAXD];
+        for (int k = 0; k < d; ++k) col[k] = (k == m - 1) ? 1 : 0;
+        lu_solve<qreal>(d, M, piv, col);
+        for (int k = 0; k < d; ++k) u[k] = -col[k];
+    } else {
+        int b = -1;
+        qreal e[MAXD];
+        for (int r = 0; r < d; ++r) { e[r] = P.is_plane(S[r + 1]) ? 0 : 1; if (!P.is_plane(S[r + 1]) && b < 0) b = S[r + 1]; }
+        lu_solve<qreal>(d, M, piv, e);
+        for (int k = 0; k < d; ++k) u[k] = e[k];
+        const double* xb = P.x(b);
+        for (int k = 0; k < d; ++k) db[k] = (qreal)xb[k] - (qreal)xa[k];
+    }
+    qreal lam = 0;
+    for (int k = 0; k < d; ++k) lam += u[k] * db[k];
+    struct QC { int item; qreal t; };
+    std::vector<QC> ts;
+    for (int it : items) {
+        if (!P.is_plane(it)) {
+            const double* xj = P.x(it);
+            qreal nd = 0, dr = 0, du = 0;
+            for (int k = 0; k < d; ++k) { qreal dl = (qreal)xj[k] - (qreal)xa[k]; nd += dl * dl; dr += dl * rho[k]; du += dl * u[k]; }
+            qreal den = 2 * (du - lam);
+            if (!(den > 0)) continue;
+            ts.push_back({it, (nd - 2 * dr) / den});
+        } else {
+            int p = it - P.n, k = p / 2; bool upper = (p % 2 == 0);
+            qreal uk = upper ? u[k] : -u[k];
+            if (!(uk > 0)) continue;
+            qreal ck = (qreal)xa[k] + rho[k];
+            qreal num = upper ? ((qreal)P.bhi[k] - ck) : (ck - (qreal)P.blo[k]);
+            ts.push_back({it, num / uk});
+        }
+    }
+    if (ts.empty()) { degenerate = true; return -1; }
+    std::sort(ts.begin(), ts.end(), [](const QC& x, const QC& y) { return x.t < y.t || (x.t == y.t && x.item < y.item); });
+    if (ts.size() >= 2) {
+        qreal scale = qabs(ts[0].t) + 1e-3;
+        if (ts[1].t - ts[0].t <= (qreal)1e-26 * scale) degenerate = true;
+    }
+    return ts[0].item;
+}
+
+/* Re-evaluate a descent step in binary128 from the FP64 state. */
+int quad_rescore_point(const Problem& P, const RayQuery& q, const std::vector<int>& items) {
+    const int d = P.d;
+    const double* xa = P.x(q.a);
+    int best = -1; qreal bt = 0;
+    for (int it : items) {
+        qreal t;
+        if (!P.is_plane(it)) {
+            const double* xj = P.x(it);
+            qreal nd = 0, dr = 0, du = 0;
+            for (int k = 0; k < d; ++k) { qreal dl = (qreal)xj[k] - (qreal)xa[k]; nd += dl * dl; dr += dl * (qreal)q.rho[k]; du += dl * (qreal)q.u[k]; }
+            qreal den = 2 * (du - (qreal)q.lam);
+            if (!(den > 0)) continue;
+            t = (nd - 2 * dr) / den;
+        } else {
+            int p = it - P.n, k = p / 2; bool upper = (p % 2 == 0);
+            qreal uk = upper ? (qreal)q.u[k] : -(qreal)q.u[k];
+            if (!(uk > 0)) continue;
+            qreal ck = (qreal)xa[k] + (qreal)q.rho[k];
+            t = (upper ? ((qreal)P.bhi[k] - ck) : (ck - (qreal)P.blo[k])) / uk;
+        }
+        if (best < 0 || t < bt || (t == bt && it < best)) { best = it; bt = t; }
+    }
+    return best;
+}
+
+/* ---------------- per-cell exploration ---------------- */
+struct SigHash {
+    size_t operator()(const std::vector<int>& v) const {
+        uint64_t h = 1469598103934665603ull;
+        for (int x : v) { h ^= (uint32_t)x; h *= 1099511628211ull; }
+        return (size_t)h;
+    }
+};
+
+struct Counters {
+    int64_t rays = 0, descents = 0, descent_retries = 0, quad = 0, degenerate = 0, cell_vertices = 0, chains = 0;
+    void add(const Counters& o) {
+        rays += o.rays; descents += o.descents; descent_retries += o.descent_retries; quad += o.quad;
+        degenerate += o.degenerate; cell_vertices += o.cell_vertices; chains += o.chains;
+    }
+};
+
+struct CellVertex { std::vector<int> sig; double c[MAXD]; };
+
+struct Explorer {
+    const Problem& P;
+    Searcher S;
+    Counters cnt;
+    explicit Explorer(const Problem& p) : P(p), S(p) {}
+
+    /* Walk ray from vertex sig (sorted) dropping position m.  Returns the new
+     * sorted signature, or empty on failure. */
+    std::vector<int> walk(const std::vector<int>& sig, const VertexSys& V, int m) {
+        const int d = P.d;
+        RayQuery q;
+        q.a = sig[0];
+        if (!edge_direction(P, sig.data(), V, m, q.u, q.lam, q.db)) return {};
+        for (int k = 0; k < d; ++k) q.rho[k] = V.rho[k];
+        double nr = 0, nu = 0;
+        for (int k = 0; k < d; ++k) { nr = std::max(nr, std::fabs(q.rho[k])); nu = std::max(nu, std::fabs(q.u[k])); }
+        double kap = 8.0 * d * std::max(V.cond, 1.0) * EPS;
+        q.erho = kap * (nr + 1e-3);
+        q.eu = kap * (nu + 1e-3);
+        q.excl = sig.data(); q.nexcl = d + 1;
+        cnt.rays++;
+        RayResult R = S.search(q);
+        if (R.best.item < 0) return {};
+        int win = R.best.item;
+        if (!R.certified) {
+            cnt.quad++;
+            std::vector<int> items{R.best.item};
+            for (auto& c : R.amb) items.push_back(c.item);
+            bool degen = false;
+            win = quad_rescore_walk(P, sig.data(), m, items, degen);
+            if (degen) cnt.degenerate++;
+            if (win < 0) return {};
+        }
+        std::vector<int> ns;
+        for (int s = 0; s <= d; ++s) if (s != m) ns.push_back(sig[s]);
+        ns.push_back(win);
+        std::sort(ns.begin(), ns.end());
+        return ns;
+    }
+
+    /* Descent from generator i to one vertex of its cell (src/raycast.jl:45-109). */
+    std::vector<int> descent(int i) {
+        const int d = P.d;
+        for (int attempt = 0; attempt < 24; ++attempt) {
+            cnt.descents++;
+            std::vector<int> T{i};
+            double rho[MAXD] = {0};
+            bool fail = false;
+            for (int step = 1; step <= d && !fail; ++step) {
+                double g[MAXD];
+                philox_gauss(P.seed ^ 0x5DEECE66Dull, (uint32_t)(attempt * 16 + step), (uint64_t)i, d, g);
+                // orthonormal basis of the current constraint rows (Gram-Schmidt)
+                double B[MAXD][MAXD]; int nb = 0;
+                for (size_t s = 1; s < T.size(); ++s) {
+                    double row[MAXD], rh;
+                    constraint_row<double>(P, i, T[s], row, rh);
+                    for (int t = 0; t < nb; ++t) { double pr = 0; for (int k = 0; k < d; ++k) pr += row[k] * B[t][k]; for (int k = 0; k < d; ++k) row[k] -= pr * B[t][k]; }
+                    double nn = 0; for (int k = 0; k < d; ++k) nn += row[k] * row[k];
+                    nn = std::sqrt(nn);
+                    if (!(nn > 1e-300)) { fail = true; break; }
+                    for (int k = 0; k < d; ++k) B[nb][k] = row[k] / nn;
+                    ++nb;
+                }
+                if (fail) break;
+                for (int rep = 0; rep < 2; ++rep)
+                    for (int t = 0; t < nb; ++t) { double pr = 0; for (int k = 0; k < d; ++k) pr += g[k] * B[t][k]; for (int k = 0; k < d; ++k) g[k] -= pr * B[t][k]; }
+                double nn = 0; for (int k = 0; k < d; ++k) nn += g[k] * g[k];
+                nn = std::sqrt(nn);
+                if (!(nn > 1e-12)) { fail = true; break; }
+                RayQuery q;
+                q.a = i;
+                for (int k = 0; k < d; ++k) { q.u[k] = g[k] / nn; q.rho[k] = rho[k]; q.db[k] = 0; }
+                q.lam = 0;
+                std::vector<int> ex = T; std::sort(ex.begin(), ex.end());
+                q.excl = ex.data(); q.nexcl = (int)ex.size();
+                q.erho = 1e-12; q.eu = 1e-13;
+                cnt.rays++;
+                RayResult R = S.search(q);
+                if (R.best.item < 0) { fail = true; break; }
+                int win = R.best.item;
+                double t = R.best.t;
+                if (!R.certified) {
+                    cnt.quad++;
+                    std::vector<int> items{R.best.item};
+                    for (auto& c : R.amb) items.push_back(c.item);
+                    win = quad_rescore_point(P, q, items);
+                    if (win < 0) { fail = true; break; }
+                    if (win != R.best.item) {
+                        for (auto& c : R.amb) if (c.item == win) t = c.t;
+                    }
+                }
+                if (!(t > 0) || !std::isfinite(t)) { fail = true; break; }
+                for (int k = 0; k < d; ++k) rho[k] += t * q.u[k];
+                T.push_back(win);
+            }
+            if (fail) { cnt.descent_retries++; continue; }
+            std::sort(T.begin(), T.end());
+            if (verify(T)) return T;
+            cnt.descent_retries++;
+        }
+        return {};
+    }
+
+    /* Empty-sphere + in-box check of a signature (used for descent results). */
+    bool verify(const std::vector<int>& sig) {
+        const int d = P.d;
+        VertexSys V = solve_vertex(P, sig.data());
+        if (!V.ok) return false;
+        const double* xa = P.x(sig[0]);
+        double c[MAXD], r2 = 0;
+        for (int k = 0; k < d; ++k) { c[k] = xa[k] + V.rho[k]; r2 += V.rho[k] * V.rho[k]; }
+        for (int k = 0; k < d; ++k) {
+            double tol = 1e-12 * (1.0 + std::fabs(P.bhi[k]) + std::fabs(P.blo[k]));
+            if (c[k] < P.blo[k] - tol || c[k] > P.bhi[k] + tol) return false;
+        }
+        std::vector<int> reals;
+        for (int s : sig) if (!P.is_plane(s)) reals.push_back(s);
+        return !S.any_inside(c, r2, reals.data(), (int)reals.size(), 1e-10);
+    }
+
+    /* Enumerate all vertices of cell i.  If `walk_only_min` (mode 1), edges
+     * whose minimal generator is below i are not walked and the exploration
+     * starts from `known` (vertices of lower cells containing i). */
+    void explore_cell(int i, std::vector<CellVertex>& out, bool walk_only_min, const std::vector<std::vector<int>>* known) {
+        const int d = P.d;
+        std::unordered_map<std::vector<int>, int, SigHash> vmap;
+        std::unordered_map<std::vector<int>, int, SigHash> ecount;
+        std::vector<std::vector<int>> verts;
+        std::vector<int> stack;
+        auto reg = [&](const std::vector<int>& sig) {
+            for (int m = 0; m <= d; ++m) {
+                if (sig[m] == i) continue;
+                std::vector<int> e; e.reserve(d);
+                for (int s = 0; s <= d; ++s) if (s != m) e.push_back(sig[s]);
+                ecount[e]++;
+            }
+        };
+        auto add = [&](const std::vector<int>& sig) -> bool {
+            auto it = vmap.find(sig);
+            if (it != vmap.end()) return false;
+            vmap.emplace(sig, (int)verts.size());
+            verts.push_back(sig);
+            reg(sig);
+            return true;
+        };
+        if (known && !known->empty()) {
+            for (auto& s : *known) add(s);
+            for (int v = 0; v < (int)verts.size(); ++v) stack.push_back(v);
+        } else {
+            std::vector<int> s0 = descent(i);
+            if (s0.empty()) { set_err("descent failed at cell " + std::to_string(i)); return; }
+            add(s0);
+            stack.push_back(0);
+        }
+        while (!stack.empty()) {
+            int v = stack.back(); stack.pop_back();
+            std::vector<int> sig = verts[v];
+            VertexSys V = solve_vertex(P, sig.data());
+            if (!V.ok) { cnt.degenerate++; continue; }
+            for (int m = 0; m <= d; ++m) {
+                if (sig[m] == i) continue;
+                std::vector<int> e;
+                for (int s = 0; s <= d; ++s) if (s != m) e.push_back(sig[s]);
+                if (walk_only_min && e[0] != i) continue;
+                auto ec = ecount.find(e);
+                if (ec != ecount.end() && ec->second >= 2) continue;
+                std::vector<int> ns = walk(sig, V, m);
+                if (ns.empty()) continue;
+                if (add(ns)) stack.push_back((int)verts.size() - 1);
+            }
+        }
+        cnt.cell_vertices += (int64_t)verts.size();
+        out.clear();
+        out.reserve(verts.size());
+        for (auto& s : verts) {
+            CellVertex cv; cv.sig = s;
+            VertexSys V = solve_vertex(P, s.data());
+            const double* xa = P.x(s[0]);
+            for (int k = 0; k < d; ++k) cv.c[k] = xa[k] + (V.ok ? V.rho[k] : NAN);
+            out.push_back(std::move(cv));
+        }
+    }
+};
+
+/* ---------------- polygon integration (flag decomposition) ---------------- */
+struct PolyCell {
+    const Problem& P;
+    int i;
+    const std::vector<CellVertex>& V;
+    int64_t chains = 0;
+    int64_t bad = 0;
+    std::vector<const double*> centers;
+
+    double det_cols(double cols[MAXD][MAXD]) {
+        const int d = P.d;
+        double A[MAXD][MAXD]; int piv[MAXD] = {0};
+        for (int r = 0; r < d; ++r) for (int c = 0; c < d; ++c) A[r][c] = cols[c][r];
+        if (!lu_factor<double>(d, A, piv)) return 0.0;
+        double det = 1;
+        for (int r = 0; r < d; ++r) { det *= A[r][r]; if (piv[r] != r) det = -det; }
+        return det;
+    }
+
+    double chain_sum(const std::vector<int>& L, std::vector<int>& K) {
+        const int d = P.d;
+        const double* xi = P.x(i);
+        int depth = (int)K.size();
+        if (depth == d - 1) {
+            if (L.size() != 2) { bad++; return 0.0; }
+            double cols[MAXD][MAXD];
+            int c = 0;
+            for (const double* ce : centers) { for (int k = 0; k < d; ++k) cols[c][k] = ce[k] - xi[k]; ++c; }
+            for (int v : L) { for (int k = 0; k < d; ++k) cols[c][k] = V[v].c[k] - xi[k]; ++c; }
+            chains++;
+            return std::fabs(det_cols(cols));
+        }
+        std::vector<double> cen(d, 0.0);
+        for (int v : L) for (int k = 0; k < d; ++k) cen[k] += V[v].c[k];
+        for (int k = 0; k < d; ++k) cen[k] /= (double)L.size();
+        centers.push_back(cen.data());
+        std::vector<int> items;
+        for (int v : L) for (int s : V[v].sig) {
+            if (s == i) continue;
+            if (std::find(K.begin(), K.end(), s) != K.end()) continue;
+            items.push_back(s);
+        }
+        std::sort(items.begin(), items.end());
+        items.erase(std::unique(items.begin(), items.end()), items.end());
+        double sum = 0;
+        for (int l : items) {
+            std::vector<int> L2;
+            for (int v : L) if (std::find(V[v].sig.begin(), V[v].sig.end(), l) != V[v].sig.end()) L2.push_back(v);
+            if (L2.size() < 2) continue;
+            K.push_back(l);
+            sum += chain_sum(L2, K);
+            K.pop_back();
+        }
+        centers.pop_back();
+        return sum;
+    }
+};
+
+double height(const Problem& P, int i, int k) {
+    const double* xi = P.x(i);
+    if (!P.is_plane(k)) {
+        const double* xk = P.x(k);
+        double s = 0;
+        for (int q = 0; q < P.d; ++q) { double e = xk[q] - xi[q]; s += e * e; }
+        return 0.5 * std::sqrt(s);
+    }
+    int p = k - P.n, q = p / 2;
+    return (p % 2 == 0) ? (P.bhi[q] - xi[q]) : (xi[q] - P.blo[q]);
+}
+
+}  // namespace
+
+/* ---------------- mesh object ---------------- */
+struct hvo_mesh {
+    Problem P;
+    std::vector<std::vector<int>> vsig;  // owned vertices (internal ids, sorted)
+    std::vector<double> vc;              // centers
+    std::vector<int64_t> offs;           // neighbour CSR (items, internal ids)
+    std::vector<int> nbr;
+    std::vector<double> area;            // aligned with nbr (after symmetrisation)
+    std::vector<double> vol;
+    bool integrated = false;
+    Counters cnt;
+    std::vector<int64_t> order;          // sorted vertex order
+};
+
+namespace {
+
+int64_t out_item(const Problem& P, int it) { return (int64_t)it + 1; }
+
+void finish_mesh(hvo_mesh* M) {
+    const Problem& P = M->P;
+    const int d = P.d;
+    int64_t V = (int64_t)M->vsig.size();
+    M->order.resize(V);
+    for (int64_t v = 0; v < V; ++v) M->order[v] = v;
+    std::sort(M->order.begin(), M->order.end(), [&](int64_t a, int64_t b) { return M->vsig[a] < M->vsig[b]; });
+    (void)d;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* hvo_last_error(void) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    return g_last_err.c_str();
+}
+
+int hvo_build(int d, int64_t n, const double* pts, const double* lo, const double* hi,
+              uint64_t seed, int nthreads, int mode, int integrate, hvo_mesh** out) {
+    if (d < 2 || d > MAXD || n < 0 || n > (1ll << 30) || !out) { set_err("invalid argument"); return -1; }
+    hvo_mesh* M = new hvo_mesh();
+    Problem& P = M->P;
+    P.d = d; P.n = (int)n; P.seed = seed;
+    P.X.assign(pts, pts + (size_t)n * d);
+    for (int k = 0; k < d; ++k) { P.blo[k] = lo[k]; P.bhi[k] = hi[k]; }
+    for (int64_t i = 0; i < n; ++i) for (int k = 0; k < d; ++k) {
+        double v = pts[i * d + k];
+        if (!(v > lo[k] && v < hi[k])) { set_err("point outside the open box"); delete M; return -2; }
+    }
+    build_tree(P);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    std::vector<std::vector<int>> nb(n);
+    std::vector<std::vector<double>> ar(n);
+    std::vector<std::vector<CellVertex>> owned(n);
+    std::atomic<int> fail{0};
+    auto per_cell = [&](Explorer& ex, int i, const std::vector<CellVertex>& cv, Counters& cnt) {
+        std::vector<int> items;
+        for (auto& v : cv) for (int s : v.sig) if (s != i) items.push_back(s);
+        std::sort(items.begin(), items.end());
+        items.erase(std::unique(items.begin(), items.end()), items.end());
+        nb[i] = items;
+        for (auto& v : cv) if (v.sig[0] == i) owned[i].push_back(v);
+        if (integrate) {
+            PolyCell pc{P, i, cv};
+            std::vector<double> a(items.size(), 0.0);
+            double fact = 1; for (int q = 2; q <= d; ++q) fact *= q;
+            for (size_t t = 0; t < items.size(); ++t) {
+                int k = items[t];
+                if (!P.is_plane(k) && k < i) continue;
+                std::vector<int> L;
+                for (int v = 0; v < (int)cv.size(); ++v)
+                    if (std::find(cv[v].sig.begin(), cv[v].sig.end(), k) != cv[v].sig.end()) L.push_back(v);
+                std::vector<int> K{k};
+                double s = pc.chain_sum(L, K);
+                double Vik = s / fact;
+                a[t] = Vik * d / height(P, i, k);
+            }
+            ar[i] = a;
+            cnt.chains += pc.chains;
+            cnt.degenerate += pc.bad;
+        }
+        (void)ex;
+    };
+    if (mode == 0) {
+#pragma omp parallel
+        {
+            Explorer ex(P);
+            std::vector<CellVertex> cv;
+#pragma omp for schedule(dynamic, 16)
+            for (int64_t i = 0; i < n; ++i) {
+                ex.explore_cell((int)i, cv, false, nullptr);
+                if (cv.empty()) { fail = 1; continue; }
+                per_cell(ex, (int)i, cv, ex.cnt);
+            }
+#pragma omp critical
+            M->cnt.add(ex.cnt);
+        }
+    } else {
+        // reference order: cells 1..N, vertices of lower cells seed higher cells
+        Explorer ex(P);
+        std::vector<std::vector<std::vector<int>>> known(n);
+        std::vector<CellVertex> cv;
+        for (int64_t i = 0; i < n; ++i) {
+            ex.explore_cell((int)i, cv, true, &known[i]);
+            if (cv.empty()) { fail = 1; break; }
+            for (auto& v : cv) {
+                bool seen_before = false;
+                for (int s : v.sig) if (!P.is_plane(s) && s < i) seen_before = true;
+                if (seen_before) continue;  // already distributed by a lower cell
+                for (int s : v.sig) if (!P.is_plane(s) && s > i) known[s].push_back(v.sig);
+            }
+            per_cell(ex, (int)i, cv, ex.cnt);
+            std::vector<std::vector<int>>().swap(known[i]);
+        }
+        M->cnt.add(ex.cnt);
+    }
+    if (fail) { set_err("cell exploration failed: " + std::string(hvo_last_error())); delete M; return -3; }
+    // collect owned vertices
+    for (int64_t i = 0; i < n; ++i) for (auto& v : owned[i]) {
+        M->vsig.push_back(v.sig);
+        for (int k = 0; k < d; ++k) M->vc.push_back(v.c[k]);
+    }
+    // neighbour CSR
+    M->offs.assign(n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) M->offs[i + 1] = M->offs[i] + (int64_t)nb[i].size();
+    M->nbr.resize(M->offs[n]);
+    for (int64_t i = 0; i < n; ++i) std::copy(nb[i].begin(), nb[i].end(), M->nbr.begin() + M->offs[i]);
+    if (integrate) {
+        M->area.assign(M->offs[n], 0.0);
+        M->vol.assign(n, 0.0);
+        for (int64_t i = 0; i < n; ++i) std::copy(ar[i].begin(), ar[i].end(), M->area.begin() + M->offs[i]);
+        // copy interfaces from the lower cell (src/polyintegrator.jl:338-343)
+        for (int64_t i = 0; i < n; ++i) {
+            for (int64_t t = M->offs[i]; t < M->offs[i + 1]; ++t) {
+                int k = M->nbr[t];
+                if (P.is_plane(k) || k > i) continue;
+                auto b = M->nbr.begin() + M->offs[k], e = M->nbr.begin() + M->offs[k + 1];
+                auto it = std::lower_bound(b, e, (int)i);
+                if (it != e && *it == (int)i) M->area[t] = M->area[M->offs[k] + (it - b)];
+            }
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            double v = 0;
+            for (int64_t t = M->offs[i]; t < M->offs[i + 1]; ++t) v += M->area[t] * height(P, (int)i, M->nbr[t]) / d;
+            M->vol[i] = v;
+        }
+        M->integrated = true;
+    }
+    finish_mesh(M);
+    *out = M;
+    return 0;
+}
+
+int64_t hvo_num_vertices(const hvo_mesh* m) { return (int64_t)m->vsig.size(); }
+int64_t hvo_num_neighbors(const hvo_mesh* m) { return (int64_t)m->nbr.size(); }
+
+void hvo_vertices(const hvo_mesh* m, int64_t* sig, double* r) {
+    const int d = m->P.d;
+    for (size_t o = 0; o < m->order.size(); ++o) {
+        int64_t v = m->order[o];
+        for (int s = 0; s <= d; ++s) sig[o * (d + 1) + s] = out_item(m->P, m->vsig[v][s]);
+        for (int k = 0; k < d; ++k) r[o * d + k] = m->vc[v * d + k];
+    }
+}
+
+void hvo_neighbors(const hvo_mesh* m, int64_t* offs, int64_t* nbr) {
+    for (size_t i = 0; i < m->offs.size(); ++i) offs[i] = m->offs[i];
+    for (size_t t = 0; t < m->nbr.size(); ++t) nbr[t] = out_item(m->P, m->nbr[t]);
+}
+
+int hvo_polygon(const hvo_mesh* m, double* vol, double* area) {
+    if (!m->integrated) { set_err("mesh built without integrate=1"); return -1; }
+    std::copy(m->vol.begin(), m->vol.end(), vol);
+    std::copy(m->area.begin(), m->area.end(), area);
+    return 0;
+}
+
+void hvo_mc_directions(int d, int64_t cell, int ndir, uint64_t seed, double* dirs) {
+    for (int s = 0; s < ndir; ++s) {
+        double g[MAXD];
+        philox_gauss(seed, (uint32_t)s, (uint64_t)cell, d, g);
+        double nn = 0;
+        for (int k = 0; k < d; ++k) nn += g[k] * g[k];
+        nn = std::sqrt(nn);
+        for (int k = 0; k < d; ++k) dirs[(int64_t)s * d + k] = g[k] / nn;
+    }
+}
+
+int hvo_heuristic_mc(const hvo_mesh* m, int ndir, uint64_t seed, int nthreads,
+                     double* vol, double* area, double* vol_var, double* area_var) {
+    const Problem& P = m->P;
+    const int d = P.d;
+    const int64_t n = P.n;
+    if (ndir <= 0) { set_err("ndir must be positive"); return -1; }
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    const double c_vol = std::pow(M_PI, d / 2.0) / std::tgamma(1.0 + d / 2.0);
+    const double c_area = d * c_vol;
+    std::vector<double> raw_area(m->nbr.size(), 0.0), raw_vol(n, 0.0);
+    std::vector<double> var_v(n, 0.0), var_a(m->nbr.size(), 0.0);
+#pragma omp parallel for schedule(dynamic, 32)
+    for (int64_t i = 0; i < n; ++i) {
+        const double* xi = P.x((int)i);
+        int64_t b = m->offs[i], e = m->offs[i + 1];
+        int deg = (int)(e - b);
+        std::vector<double> nrm((size_t)deg * d);
+        for (int t = 0; t < deg; ++t) {
+            int k = m->nbr[b + t];
+            if (!P.is_plane(k)) {
+                const double* xk = P.x(k);
+                double s = 0;
+                for (int q = 0; q < d; ++q) { nrm[t * d + q] = xk[q] - xi[q]; s += nrm[t * d + q] * nrm[t * d + q]; }
+                s = std::sqrt(s);
+                for (int q = 0; q < d; ++q) nrm[t * d + q] /= s;
+            } else {
+                int p = k - P.n;
+                for (int q = 0; q < d; ++q) nrm[t * d + q] = 0;
+                nrm[t * d + p / 2] = (p % 2 == 0) ? 1.0 : -1.0;
+            }
+        }
+        double sv = 0, sv2 = 0;
+        std::vector<double> sa(deg, 0.0), sa2(deg, 0.0);
+        for (int s = 0; s < ndir; ++s) {
+            double g[MAXD];
+            philox_gauss(seed, (uint32_t)s, (uint64_t)i, d, g);
+            double nn = 0;
+            for (int q = 0; q < d; ++q) nn += g[q] * g[q];
+            nn = std::sqrt(nn);
+            for (int q = 0; q < d; ++q) g[q] /= nn;
+            // mc_raycast (src/mcintegrator.jl:207-226): t = min over neighbours
+            double tb = INFINITY; int jb = -1;
+            for (int t = 0; t < deg; ++t) {
+                int k = m->nbr[b + t];
+                double tt;
+                if (!P.is_plane(k)) {
+                    const double* xk = P.x(k);
+                    double nd = 0, du = 0;
+                    for (int q = 0; q < d; ++q) { double dl = xk[q] - xi[q]; nd += dl * dl; du += dl * g[q]; }
+                    if (!(du > 0)) continue;
+                    tt = nd / (2.0 * du);
+                } else {
+                    int p = k - P.n, q = p / 2; bool upper = (p % 2 == 0);
+                    double uk = upper ? g[q] : -g[q];
+                    if (!(uk > 0)) continue;
+                    tt = (upper ? (P.bhi[q] - xi[q]) : (xi[q] - P.blo[q])) / uk;
+                }
+                if (tt > 0 && tt < tb) { tb = tt; jb = t; }
+            }
+            if (jb < 0) continue;
+            double td = std::pow(tb, d);
+            sv += td; sv2 += td * td;
+            double cosv = 0;
+            for (int q = 0; q < d; ++q) cosv += nrm[jb * d + q] * g[q];
+            double dA = std::pow(tb, d - 1) / std::fabs(cosv);
+            sa[jb] += dA; sa2[jb] += dA * dA;
+        }
+        raw_vol[i] = sv * c_vol / ndir;
+        double mv = sv / ndir;
+        var_v[i] = c_vol * c_vol * std::max(sv2 / ndir - mv * mv, 0.0) / ndir;
+        for (int t = 0; t < deg; ++t) {
+            raw_area[b + t] = sa[t] * c_area / ndir;
+            double ma = sa[t] / ndir;
+            var_a[b + t] = c_area * c_area * std::max(sa2[t] / ndir - ma * ma, 0.0) / ndir;
+        }
+    }
+    // two-sided averaging with volume correction (src/mcintegrator.jl:172-201)
+    std::vector<double> A = raw_area, Vv = raw_vol;
+    for (int64_t i = 0; i < n; ++i) {
+        for (int64_t t = m->offs[i]; t < m->offs[i + 1]; ++t) {
+            int k = m->nbr[t];
+            if (P.is_plane(k) || k >= i) continue;
+            auto b = m->nbr.begin() + m->offs[k], e = m->nbr.begin() + m->offs[k + 1];
+            auto it = std::lower_bound(b, e, (int)i);
+            if (it == e || *it != (int)i) continue;
+            int64_t tk = m->offs[k] + (it - b);
+            double old_area = raw_area[t], neigh_area = raw_area[tk];
+            double na = std::fabs(neigh_area) < old_area * 1.0e-10 ? old_area : 0.5 * (old_area + neigh_area);
+            double factor = height(P, (int)i, k) / d;
+            Vv[k] += (na - neigh_area) * factor;
+            Vv[i] += (na - old_area) * factor;
+            A[t] = na; A[tk] = na;
+        }
+    }
+    std::copy(Vv.begin(), Vv.end(), vol);
+    std::copy(A.begin(), A.end(), area);
+    if (vol_var) std::copy(var_v.begin(), var_v.end(), vol_var);
+    if (area_var) std::copy(var_a.begin(), var_a.end(), area_var);
+    return 0;
+}
+
+void hvo_get_stats(const hvo_mesh* m, hvo_stats* st) {
+    st->rays = m->cnt.rays; st->descents = m->cnt.descents; st->descent_retries = m->cnt.descent_retries;
+    st->quad_rescores = m->cnt.quad; st->degenerate = m->cnt.degenerate;
+    st->cell_vertices = m->cnt.cell_vertices; st->chains = m->cnt.chains;
+}
+
+void hvo_free(hvo_mesh* m) { delete m; }
+
+int hvo_sample_cells(int d, int64_t n, const double* pts, const double* lo, const double* hi,
+                     uint64_t seed, int nthreads, int64_t ncells, const int64_t* cells,
+                     int64_t* owned_vertices, int64_t* rays, double* seconds) {
+    if (d < 2 || d > MAXD || n <= 0) { set_err("invalid argument"); return -1; }
+    auto t0 = std::chrono::steady_clock::now();
+    Problem P;
+    P.d = d; P.n = (int)n; P.seed = seed;
+    P.X.assign(pts, pts + (size_t)n * d);
+    for (int k = 0; k < d; ++k) { P.blo[k] = lo[k]; P.bhi[k] = hi[k]; }
+    build_tree(P);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    int64_t own = 0, nr = 0;
+    int fail = 0;
+#pragma omp parallel reduction(+ : own, nr, fail)
+    {
+        Explorer ex(P);
+        std::vector<CellVertex> cv;
+#pragma omp for schedule(dynamic, 4)
+        for (int64_t c = 0; c < ncells; ++c) {
+            int i = (int)cells[c];
+            ex.explore_cell(i, cv, false, nullptr);
+            if (cv.empty()) { fail++; continue; }
+            for (auto& v : cv) if (v.sig[0] == i) own++;
+        }
+        nr += ex.cnt.rays;
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    *owned_vertices = own;
+    *rays = nr;
+    *seconds = std::chrono::duration<double>(t1 - t0).count();
+    return fail ? -3 : 0;
+}
+
+int64_t hvo_verify_vertices(int d, int64_t n, const double* pts, const double* lo, const double* hi,
+                            int64_t nv, const int64_t* sig, const double* r, double rel_tol) {
+    int64_t bad = 0;
+#pragma omp parallel for reduction(+ : bad) schedule(static)
+    for (int64_t v = 0; v < nv; ++v) {
+        const int64_t* s = sig + v * (d + 1);
+        const double* c = r + v * d;
+        double rmin = INFINITY, rmax = 0;
+        bool ok = true;
+        for (int q = 0; q <= d; ++q) {
+            int64_t it = s[q] - 1;
+            if (it < n) {
+                double dd = 0;
+                for (int k = 0; k < d; ++k) { double e = pts[it * d + k] - c[k]; dd += e * e; }
+                rmin = std::min(rmin, dd); rmax = std::max(rmax, dd);
+            } else {
+                int p = (int)(it - n), k = p / 2;
+                double off = (p % 2 == 0) ? hi[k] - c[k] : c[k] - lo[k];
+                if (std::fabs(off) > 1e-9) ok = false;
+            }
+        }
+        if (!(rmax - rmin <= rel_tol * rmax + 1e-300)) ok = false;
+        for (int k = 0; k < d && ok; ++k) if (c[k] < lo[k] - 1e-9 || c[k] > hi[k] + 1e-9) ok = false;
+        for (int64_t j = 0; j < n && ok; ++j) {
+            bool in_sig = false;
+            for (int q = 0; q <= d; ++q) if (s[q] - 1 == j) in_sig = true;
+            if (in_sig) continue;
+            double dd = 0;
+            for (int k = 0; k < d; ++k) { double e = pts[j * d + k] - c[k]; dd += e * e; }
+            if (dd < rmin * (1.0 - rel_tol)) ok = false;
+        }
+        if (!ok) bad++;
+    }
+    return bad;
+}
+
+}  // extern "C"

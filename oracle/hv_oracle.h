@@ -1,0 +1,78 @@
+/*
+ * hv_oracle.h -- C API of the CPU oracle.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is a CPU restatement of
+ * HighVoronoi.jl's mesh-generation hot path (vertex search by raycasting,
+ * neighbour extraction, VI_POLYGON and VI_HEURISTIC_MC integration).  It is
+ * used by tests/ as the parity checker, by __graft_entry__.smoke() and by the
+ * CPU-baseline leg of bench.py.  The product (libhvgpu) never links or calls it.
+ *
+ * Index conventions follow the reference: generators are 1-based, boundary
+ * plane p (1-based, cuboid order of src/boundary.jl:518-534: plane 2k-1 is the
+ * upper face x_k = hi_k, plane 2k the lower face x_k = lo_k) is generator N+p.
+ * Point arrays are d x n column-major (Julia layout), i.e. point i occupies
+ * pts[d*i .. d*i+d-1].
+ */
+#ifndef HV_ORACLE_H
+#define HV_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct hvo_mesh hvo_mesh;
+
+/* Counters of rare events and work (rays, quad-precision re-scores, ...). */
+typedef struct {
+    int64_t rays;            /* incircle searches issued (descent + edge walks) */
+    int64_t descents;        /* descent attempts */
+    int64_t descent_retries; /* descents rejected by the empty-sphere check */
+    int64_t quad_rescores;   /* rays whose FP64 decision was not certified */
+    int64_t degenerate;      /* ties that survived quad precision */
+    int64_t cell_vertices;   /* sum over cells of vertices found */
+    int64_t chains;          /* polyintegrator simplices evaluated */
+} hvo_stats;
+
+/* Build the mesh.  mode 0: every cell enumerates its own polytope (OpenMP over
+ * cells); mode 1: the reference's sequential rule (cells in index order, edges
+ * walked only from their minimal generator).  integrate: 0 none, 1 polygon.
+ * Returns 0 on success, <0 on error. */
+int hvo_build(int d, int64_t n, const double* pts, const double* lo, const double* hi,
+              uint64_t seed, int nthreads, int mode, int integrate, hvo_mesh** out);
+
+int64_t hvo_num_vertices(const hvo_mesh* m);
+int64_t hvo_num_neighbors(const hvo_mesh* m);
+/* Vertices sorted lexicographically by their 1-based signature. */
+void hvo_vertices(const hvo_mesh* m, int64_t* sig, double* r);
+void hvo_neighbors(const hvo_mesh* m, int64_t* offs, int64_t* nbr);
+/* Volumes (n) and interface areas aligned with hvo_neighbors.  Needs integrate=1. */
+int hvo_polygon(const hvo_mesh* m, double* vol, double* area);
+/* Heuristic Monte-Carlo volumes/areas with ndir Philox directions per cell.
+ * vol_var / area_var (optional, may be NULL) receive the variance of the
+ * per-cell estimators (sample variance / ndir) before two-sided averaging. */
+int hvo_heuristic_mc(const hvo_mesh* m, int ndir, uint64_t seed, int nthreads,
+                     double* vol, double* area, double* vol_var, double* area_var);
+void hvo_get_stats(const hvo_mesh* m, hvo_stats* st);
+const char* hvo_last_error(void);
+void hvo_free(hvo_mesh* m);
+
+/* CPU-baseline sample: run the per-cell search for the listed cells (0-based)
+ * and report the number of vertices they own (minimal generator) and the
+ * wall time.  Returns 0 on success. */
+int hvo_sample_cells(int d, int64_t n, const double* pts, const double* lo, const double* hi,
+                     uint64_t seed, int nthreads, int64_t ncells, const int64_t* cells,
+                     int64_t* owned_vertices, int64_t* rays, double* seconds);
+
+/* Brute-force verification of a vertex list: empty open circumsphere w.r.t.
+ * every generator and equidistance to the signature.  Returns the number of
+ * violating vertices (0 = all verified). */
+int64_t hvo_verify_vertices(int d, int64_t n, const double* pts, const double* lo, const double* hi,
+                            int64_t nv, const int64_t* sig, const double* r, double rel_tol);
+
+/* Philox4x32-10 unit directions shared with the GPU MC kernel (for tests). */
+void hvo_mc_directions(int d, int64_t cell, int ndir, uint64_t seed, double* dirs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,177 @@
+"""ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module.  It restates HighVoronoi.jl's hot path on the CPU (see
+hv_oracle.cpp for the reference file:line of every step) and is the checker
+the CUDA library is compared against; it is never the thing measured for the
+GPU numbers and never a fallback of the product.
+
+Parity pin: HighVoronoi.jl holds no golden vertex sets, neighbour lists or
+volumes.  The oracle is pinned against the reference's own property tests
+(sum of volumes = domain volume, test/rcmethods.jl:3-13, test/basics.jl:42-46,
+test/jld.jl:15-20), against analytic known-answer meshes and against a
+brute-force empty-circumsphere check of every vertex (the model of
+verify_mesh, src/abstractmesh.jl:221-254).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libhvoracle.so")
+_lock = threading.Lock()
+_lib = None
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in (
+        "rays", "descents", "descent_retries", "quad_rescores", "degenerate", "cell_vertices", "chains")]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (g++ -O3 -fopenmp)."""
+    src = os.path.join(_HERE, "hv_oracle.cpp")
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-C", _HERE, "-s"], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = ctypes.CDLL(_LIB_PATH)
+            P, I64, D, I, U64 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_int, ctypes.c_uint64
+            dp = ctypes.POINTER(ctypes.c_double)
+            ip = ctypes.POINTER(ctypes.c_int64)
+            L.hvo_build.argtypes = [I, I64, dp, dp, dp, U64, I, I, I, ctypes.POINTER(P)]
+            L.hvo_build.restype = I
+            L.hvo_num_vertices.argtypes = [P]; L.hvo_num_vertices.restype = I64
+            L.hvo_num_neighbors.argtypes = [P]; L.hvo_num_neighbors.restype = I64
+            L.hvo_vertices.argtypes = [P, ip, dp]; L.hvo_vertices.restype = None
+            L.hvo_neighbors.argtypes = [P, ip, ip]; L.hvo_neighbors.restype = None
+            L.hvo_polygon.argtypes = [P, dp, dp]; L.hvo_polygon.restype = I
+            L.hvo_heuristic_mc.argtypes = [P, I, U64, I, dp, dp, dp, dp]; L.hvo_heuristic_mc.restype = I
+            L.hvo_get_stats.argtypes = [P, ctypes.POINTER(Stats)]; L.hvo_get_stats.restype = None
+            L.hvo_last_error.argtypes = []; L.hvo_last_error.restype = ctypes.c_char_p
+            L.hvo_free.argtypes = [P]; L.hvo_free.restype = None
+            L.hvo_sample_cells.argtypes = [I, I64, dp, dp, dp, U64, I, I64, ip, ip, ip, dp]
+            L.hvo_sample_cells.restype = I
+            L.hvo_verify_vertices.argtypes = [I, I64, dp, dp, dp, I64, ip, dp, D]
+            L.hvo_verify_vertices.restype = I64
+            L.hvo_mc_directions.argtypes = [I, I64, I, U64, dp]; L.hvo_mc_directions.restype = None
+            _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+
+class OracleMesh:
+    """Result of one oracle mesh build (1-based reference index conventions)."""
+
+    def __init__(self, pts, lo=None, hi=None, seed=0, nthreads=0, mode=0, integrate=False):
+        L = lib()
+        pts = np.ascontiguousarray(pts, dtype=np.float64)
+        self.n, self.d = pts.shape
+        self.pts = pts
+        self.lo = np.ascontiguousarray(np.zeros(self.d) if lo is None else lo, dtype=np.float64)
+        self.hi = np.ascontiguousarray(np.ones(self.d) if hi is None else hi, dtype=np.float64)
+        h = ctypes.c_void_p()
+        rc = L.hvo_build(self.d, self.n, _dp(pts), _dp(self.lo), _dp(self.hi), seed, nthreads, mode,
+                         1 if integrate else 0, ctypes.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"oracle build failed ({rc}): {L.hvo_last_error().decode()}")
+        self._h = h
+        self.integrated = integrate
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib().hvo_free(h)
+            self._h = None
+
+    def vertices(self):
+        L = lib()
+        V = L.hvo_num_vertices(self._h)
+        sig = np.zeros((V, self.d + 1), dtype=np.int64)
+        r = np.zeros((V, self.d), dtype=np.float64)
+        if V:
+            L.hvo_vertices(self._h, _ip(sig), _dp(r))
+        return sig, r
+
+    def neighbors(self):
+        L = lib()
+        E = L.hvo_num_neighbors(self._h)
+        offs = np.zeros(self.n + 1, dtype=np.int64)
+        nbr = np.zeros(max(E, 1), dtype=np.int64)
+        L.hvo_neighbors(self._h, _ip(offs), _ip(nbr))
+        return offs, nbr[:E]
+
+    def polygon(self):
+        L = lib()
+        E = L.hvo_num_neighbors(self._h)
+        vol = np.zeros(self.n)
+        area = np.zeros(max(E, 1))
+        if L.hvo_polygon(self._h, _dp(vol), _dp(area)) != 0:
+            raise RuntimeError(L.hvo_last_error().decode())
+        return vol, area[:E]
+
+    def heuristic_mc(self, ndir, seed, nthreads=0):
+        L = lib()
+        E = L.hvo_num_neighbors(self._h)
+        vol = np.zeros(self.n)
+        area = np.zeros(max(E, 1))
+        vv = np.zeros(self.n)
+        av = np.zeros(max(E, 1))
+        if L.hvo_heuristic_mc(self._h, ndir, seed, nthreads, _dp(vol), _dp(area), _dp(vv), _dp(av)) != 0:
+            raise RuntimeError(L.hvo_last_error().decode())
+        return vol, area[:E], vv, av[:E]
+
+    def stats(self):
+        st = Stats()
+        lib().hvo_get_stats(self._h, ctypes.byref(st))
+        return {n: getattr(st, n) for n, _ in Stats._fields_}
+
+
+def verify_vertices(pts, sig, r, lo=None, hi=None, rel_tol=1e-9):
+    """Brute-force empty-sphere check; returns the number of bad vertices."""
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    n, d = pts.shape
+    lo = np.ascontiguousarray(np.zeros(d) if lo is None else lo, dtype=np.float64)
+    hi = np.ascontiguousarray(np.ones(d) if hi is None else hi, dtype=np.float64)
+    sig = np.ascontiguousarray(sig, dtype=np.int64)
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    return lib().hvo_verify_vertices(d, n, _dp(pts), _dp(lo), _dp(hi), sig.shape[0], _ip(sig), _dp(r), rel_tol)
+
+
+def sample_cells(pts, cells, seed=0, nthreads=0, lo=None, hi=None):
+    """CPU-baseline sample: (owned vertices, rays, seconds) for the listed cells."""
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    n, d = pts.shape
+    lo = np.ascontiguousarray(np.zeros(d) if lo is None else lo, dtype=np.float64)
+    hi = np.ascontiguousarray(np.ones(d) if hi is None else hi, dtype=np.float64)
+    cells = np.ascontiguousarray(cells, dtype=np.int64)
+    own = ctypes.c_int64(); rays = ctypes.c_int64(); sec = ctypes.c_double()
+    rc = lib().hvo_sample_cells(d, n, _dp(pts), _dp(lo), _dp(hi), seed, nthreads, cells.shape[0], _ip(cells),
+                                ctypes.byref(own), ctypes.byref(rays), ctypes.byref(sec))
+    if rc != 0:
+        raise RuntimeError(lib().hvo_last_error().decode())
+    return own.value, rays.value, sec.value
+
+
+def mc_directions(d, cell, ndir, seed):
+    out = np.zeros((ndir, d))
+    lib().hvo_mc_directions(d, cell, ndir, seed, _dp(out))
+    return out
