@@ -1,0 +1,724 @@
+// hv_api.cu -- host orchestration and the C ABI of libhvgpu (include/hvgpu.h).
+//
+// hv_mesh_build replaces voronoi(mesh; searcher) (src/sysvoronoi.jl:21-39):
+//   prepare   Morton sort, tree, candidate lists
+//   seeds     descent from every seed_stride-th generator (src/raycast.jl:45-109)
+//   wavefront level k expands the vertices found at level k-1; every level is
+//             one expansion launch (+ the exact fallback and the FP64 centres);
+//             the reference repeats its cell loop until nothing new is found
+//             (src/sysvoronoi.jl:152-215), here until a level finds nothing new
+//   canonical vertices renumbered in lexicographic signature order
+// All device memory comes from the device's stream-ordered pool; the pool
+// keeps freed blocks cached so repeated builds do not return to the driver.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "hv_host.h"
+#include "hv_integrate.h"
+#include "hv_internal.cuh"
+#include "hvgpu.h"
+
+struct hv_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int nsm = 1;
+    std::string err;
+    unsigned* h_stat = nullptr;  // pinned: vcount, status, nfq, pad
+    std::vector<cudaEvent_t> evpool;  // timing events, reused across builds
+};
+
+struct hv_mesh {
+    hv_ctx* ctx = nullptr;
+    int d = 0;
+    int n = 0;
+    double lo[HV_MAXD], hi[HV_MAXD];
+    hv_params prm;
+    double* d_in = nullptr;  // points in original order (n x d)
+    unsigned V = 0;
+    int* osig = nullptr;     // V x (d+1) original 0-based items, canonical order
+    double* oc = nullptr;    // V x d
+    long long* inc_off = nullptr;
+    int* inc = nullptr;
+    long long* nbr_off = nullptr;
+    int* nbr = nullptr;
+    long long nnbr = -1;
+    hv_stats st;
+};
+
+namespace {
+
+struct HvError : std::runtime_error {
+    int code;
+    HvError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CK(x)                                                                                      \
+    do {                                                                                           \
+        cudaError_t e_ = (x);                                                                      \
+        if (e_ != cudaSuccess) {                                                                   \
+            throw HvError(e_ == cudaErrorMemoryAllocation ? HV_E_OOM : HV_E_CUDA,                  \
+                          std::string(#x) + ": " + cudaGetErrorString(e_));                        \
+        }                                                                                          \
+    } while (0)
+
+// Stream-ordered scratch allocations released when the scope ends.
+struct Scratch {
+    cudaStream_t st;
+    std::vector<void*> ptrs;
+    explicit Scratch(cudaStream_t s) : st(s) {}
+    template <class T>
+    T* get(size_t count) {
+        void* p = nullptr;
+        CK(cudaMallocAsync(&p, std::max<size_t>(count * sizeof(T), 16), st));
+        ptrs.push_back(p);
+        return (T*)p;
+    }
+    void release_all() {
+        for (void* p : ptrs) cudaFreeAsync(p, st);
+        ptrs.clear();
+    }
+    ~Scratch() { release_all(); }
+};
+
+template <class T>
+T* dalloc(cudaStream_t st, size_t count) {
+    void* p = nullptr;
+    CK(cudaMallocAsync(&p, std::max<size_t>(count * sizeof(T), 16), st));
+    return (T*)p;
+}
+
+void dfree(cudaStream_t st, void* p) {
+    if (p) cudaFreeAsync(p, st);
+}
+
+__global__ void k_iota(int* a, unsigned n) {
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = (int)i;
+}
+
+unsigned next_pow2(unsigned long long x) {
+    unsigned long long p = 1;
+    while (p < x) p <<= 1;
+    return (unsigned)p;
+}
+
+int default_knn(int d) {
+    static const int k[7] = {0, 0, 24, 48, 96, 192, 384};
+    return k[d];
+}
+
+// Expected vertices per generator for uniform points in the cube (the
+// reference's own counts, docs/src/index.md:93-96, extrapolated to 2, 3, 6).
+double vertices_per_point(int d) {
+    static const double c[7] = {0, 0, 2.2, 7.0, 30.0, 150.0, 1400.0};
+    return c[d];
+}
+
+double ms_between(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+struct Events {
+    cudaEvent_t e[4];
+    Events() { for (auto& x : e) cudaEventCreate(&x); }
+    ~Events() { for (auto& x : e) cudaEventDestroy(x); }
+};
+
+// Device time per kernel family: events recorded on the context's stream
+// around every launch, summed once the build has synchronised.
+enum Fam { F_KNN, F_DESCENT, F_EXPAND, F_FALLBACK, F_CENTERS, F_CANON, F_OTHER, F_N };
+struct KTimer {
+    hv_ctx* ctx;
+    std::vector<std::pair<int, int>> spans;  // (family, first event index)
+    size_t used = 0;
+    long long launches = 0;
+    explicit KTimer(hv_ctx* c) : ctx(c) {}
+    cudaEvent_t next() {
+        if (used == ctx->evpool.size()) {
+            cudaEvent_t e;
+            CK(cudaEventCreate(&e));
+            ctx->evpool.push_back(e);
+        }
+        return ctx->evpool[used++];
+    }
+    template <class F>
+    void run(int fam, int nlaunch, F&& f) {
+        const int i0 = (int)used;
+        CK(cudaEventRecord(next(), ctx->stream));
+        f();
+        CK(cudaEventRecord(next(), ctx->stream));
+        spans.emplace_back(fam, i0);
+        launches += nlaunch;
+    }
+    void totals(double* ms) const {  // after synchronisation
+        for (int f = 0; f < F_N; ++f) ms[f] = 0;
+        for (auto& sp : spans) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, ctx->evpool[sp.second], ctx->evpool[sp.second + 1]);
+            ms[sp.first] += t;
+        }
+    }
+};
+
+void read_stat(hv_ctx* ctx, const unsigned* dstat) {
+    CK(cudaMemcpyAsync(ctx->h_stat, dstat, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+}
+
+void check_fatal(unsigned status) {
+    using namespace hv;
+    if (status & ST_BADINPUT) throw HvError(HV_E_INVALID_ARG, "points must lie strictly inside the box and be finite");
+    if (status & ST_TIMEOUT) throw HvError(HV_E_TIMEOUT, "a bounded device wait gave up");
+    if (status & (ST_NUMERIC | ST_STACK | ST_AMB | ST_DESCENT))
+        throw HvError(HV_E_INTERNAL, "device search failed (status " + std::to_string(status) + ")");
+}
+
+void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_device, const double* h_src) {
+    using namespace hv;
+    const int d = mesh->d, n = mesh->n;
+    const int DP = d <= 4 ? 4 : 8;
+    cudaStream_t st = ctx->stream;
+    Events ev;
+    auto t0 = std::chrono::steady_clock::now();
+    CK(cudaEventRecord(ev.e[0], st));
+    mesh->d_in = dalloc<double>(st, (size_t)n * d);
+    if (n > 0) {
+        if (src_on_device)
+            CK(cudaMemcpyAsync(mesh->d_in, d_src, sizeof(double) * n * d, cudaMemcpyDeviceToDevice, st));
+        else
+            CK(cudaMemcpyAsync(mesh->d_in, h_src, sizeof(double) * n * d, cudaMemcpyHostToDevice, st));
+    }
+    hv_stats& S = mesh->st;
+    std::memset(&S, 0, sizeof(S));
+    if (n == 0) {
+        mesh->V = 0;
+        CK(cudaStreamSynchronize(st));
+        return;
+    }
+    Scratch prep(st);
+    unsigned* dstat = prep.get<unsigned>(4);
+    unsigned long long* dcnt = prep.get<unsigned long long>(C_NCOUNT);
+    CK(cudaMemsetAsync(dstat, 0, 4 * sizeof(unsigned), st));
+    CK(cudaMemsetAsync(dcnt, 0, C_NCOUNT * sizeof(unsigned long long), st));
+    // ---- Morton order
+    unsigned long long* codes = prep.get<unsigned long long>(n);
+    unsigned long long* codes2 = prep.get<unsigned long long>(n);
+    int* idx = prep.get<int>(n);
+    int* perm = prep.get<int>(n);
+    KTimer kt(ctx);
+    kt.run(F_OTHER, 1, [&] { launch_morton(d, mesh->d_in, n, mesh->lo, mesh->hi, codes, idx, dstat + 1, st); });
+    {
+        size_t tb = sort_pairs_u64_i32_temp(n);
+        void* tmp = prep.get<char>(tb);
+        sort_pairs_u64_i32(tmp, tb, codes, codes2, idx, perm, n, 64, st);
+    }
+    double* pts = prep.get<double>((size_t)n * d);
+    float* pts32 = prep.get<float>((size_t)n * DP);
+    kt.run(F_OTHER, 1, [&] { launch_gather(d, mesh->d_in, perm, n, pts, pts32, st); });
+    // ---- tree
+    DevMesh M;
+    std::memset(&M, 0, sizeof(M));
+    M.d = d; M.n = n; M.dp = DP;
+    double xs = 0;
+    for (int k = 0; k < d; ++k) {
+        M.lo[k] = mesh->lo[k]; M.hi[k] = mesh->hi[k];
+        xs = std::max(xs, std::max(std::fabs(mesh->lo[k]), std::fabs(mesh->hi[k])));
+    }
+    M.xscale = xs;
+    M.leaf = mesh->prm.leaf_size > 0 ? mesh->prm.leaf_size : 16;
+    M.nleaves = (n + M.leaf - 1) / M.leaf;
+    M.P = (int)next_pow2((unsigned long long)M.nleaves);
+    M.pts = pts; M.pts32 = pts32; M.perm = perm;
+    float* blo = prep.get<float>((size_t)2 * M.P * DP);
+    float* bhi = prep.get<float>((size_t)2 * M.P * DP);
+    unsigned* flags = prep.get<unsigned>((size_t)2 * M.P);
+    CK(cudaMemsetAsync(flags, 0, sizeof(unsigned) * 2 * M.P, st));
+    M.blo = blo; M.bhi = bhi;
+    M.status = dstat + 1;
+    M.cnt = dcnt;
+    kt.run(F_OTHER, 1, [&] { launch_bvh(M, blo, bhi, flags, st); });
+    // ---- candidate lists
+    const bool fast = mesh->prm.method == HV_METHOD_FAST;
+    int K = mesh->prm.knn > 0 ? mesh->prm.knn : default_knn(d);
+    K = std::min(K, std::max(n - 1, 0));
+    K = std::min(K, 480);
+    M.K = fast ? K : 0;
+    if (fast) {
+        int* knn = prep.get<int>((size_t)n * std::max(K, 1));
+        float* sec = prep.get<float>(n);
+        M.knn = knn; M.sec = sec;
+        kt.run(F_KNN, 1, [&] { launch_knn(M, knn, sec, st); });
+    }
+    CK(cudaGetLastError());
+    read_stat(ctx, dstat);
+    check_fatal(ctx->h_stat[1]);
+    CK(cudaEventRecord(ev.e[1], st));
+    // ---- search with capacity retry
+    double factor = mesh->prm.capacity_factor > 0 ? mesh->prm.capacity_factor : 1.3;
+    unsigned long long est = (unsigned long long)(vertices_per_point(d) * n) + (1ull << d) + 1024;
+    int stride = mesh->prm.seed_stride > 0 ? mesh->prm.seed_stride : (n <= 4096 ? 1 : 4);
+    const int nseeds = (n + stride - 1) / stride;
+    std::unique_ptr<Scratch> srch;
+    unsigned V = 0;
+    for (int attempt = 0;; ++attempt) {
+        if (attempt > 4) throw HvError(HV_E_CAPACITY, "vertex capacity retries exhausted");
+        unsigned long long vcap64 = (unsigned long long)(est * factor * (double)(1ull << attempt));
+        if (vcap64 > 0xFFFFFFF0ull / 8) throw HvError(HV_E_CAPACITY, "vertex count beyond 32-bit ids");
+        const unsigned vcap = (unsigned)vcap64;
+        srch.reset();
+        srch.reset(new Scratch(st));
+        M.vcap = vcap;
+        M.vsig = srch->get<int>((size_t)vcap * (d + 1));
+        M.vc = srch->get<double>((size_t)vcap * d);
+        M.vrho32 = srch->get<float>((size_t)vcap * DP);
+        M.vnew = srch->get<int>(vcap);
+        const unsigned hsize = next_pow2(2ull * vcap);
+        M.vhmask = hsize - 1;
+        M.vhash = srch->get<unsigned long long>(hsize);
+        CK(cudaMemsetAsync(M.vhash, 0, sizeof(unsigned long long) * hsize, st));
+        const unsigned fqcap = std::max(65536u, vcap / 2);
+        unsigned long long* fq = fast ? srch->get<unsigned long long>(fqcap) : nullptr;
+        M.vcount = dstat;
+        CK(cudaMemsetAsync(dstat, 0, 4 * sizeof(unsigned), st));
+        CK(cudaMemsetAsync(dcnt, 0, C_NCOUNT * sizeof(unsigned long long), st));
+        kt.run(F_DESCENT, 1, [&] { launch_descent(M, stride, nseeds, mesh->prm.seed ? mesh->prm.seed : 0x5EEDull, st); });
+        CK(cudaGetLastError());
+        read_stat(ctx, dstat);
+        const unsigned overflow_bits = ST_VCAP | ST_HASH | ST_QUEUE | ST_ECAP;
+        bool overflow = (ctx->h_stat[1] & overflow_bits) != 0;
+        if (!overflow) check_fatal(ctx->h_stat[1]);
+        unsigned f0 = 0, f1 = std::min(ctx->h_stat[0], vcap);
+        if (!overflow) kt.run(F_CENTERS, 1, [&] { launch_centers(M, 0, f1, ctx->nsm, st); });
+        long long levels = 0;
+        while (!overflow && f1 > f0) {
+            if (fast) {
+                CK(cudaMemsetAsync(dstat + 2, 0, sizeof(unsigned), st));
+                kt.run(F_EXPAND, 1, [&] { launch_expand_fast(M, f0, f1, fq, dstat + 2, fqcap, ctx->nsm, st); });
+                const unsigned long long maxq = std::min<unsigned long long>(fqcap, (unsigned long long)(f1 - f0) * (d + 1));
+                kt.run(F_FALLBACK, 1, [&] { launch_fallback(M, fq, dstat + 2, (unsigned)maxq, ctx->nsm, st); });
+            } else {
+                kt.run(F_EXPAND, 1, [&] { launch_expand_plain(M, f0, f1, ctx->nsm, st); });
+            }
+            CK(cudaGetLastError());
+            read_stat(ctx, dstat);
+            if (ctx->h_stat[1] & overflow_bits) { overflow = true; break; }
+            check_fatal(ctx->h_stat[1]);
+            const unsigned f2 = std::min(ctx->h_stat[0], vcap);
+            kt.run(F_CENTERS, 1, [&] { launch_centers(M, f1, f2, ctx->nsm, st); });
+            f0 = f1; f1 = f2;
+            ++levels;
+        }
+        if (overflow) { S.capacity_retries++; continue; }
+        V = f1;
+        S.levels = levels;
+        break;
+    }
+    CK(cudaEventRecord(ev.e[2], st));
+    // ---- canonical order
+    mesh->V = V;
+    CK(cudaEventRecord(kt.next(), st));
+    const int canon_ev = (int)kt.used - 1;
+    {
+        Scratch cs(st);
+        unsigned* keys = cs.get<unsigned>((size_t)V * (d + 1));
+        unsigned* kt = cs.get<unsigned>(V);
+        unsigned* kt2 = cs.get<unsigned>(V);
+        int* order = cs.get<int>(V);
+        int* order2 = cs.get<int>(V);
+        launch_canon_keys(M, V, keys, st);
+        if (V) k_iota<<<std::min<unsigned>((V + 255) / 256, 65535u), 256, 0, st>>>(order, V);
+        int end_bit = 1;
+        while ((1ull << end_bit) < (unsigned long long)(n + 2 * d + 1)) ++end_bit;
+        size_t tb = sort_pairs_u32_i32_temp((int)std::max(V, 1u));
+        void* tmp = cs.get<char>(tb);
+        for (int pos = d; pos >= 0; --pos) {
+            launch_gather_keys(keys + (size_t)pos * V, order, V, kt, st);
+            if (V) sort_pairs_u32_i32(tmp, tb, kt, kt2, order, order2, (int)V, end_bit, st);
+            std::swap(order, order2);
+        }
+        mesh->osig = dalloc<int>(st, (size_t)V * (d + 1));
+        mesh->oc = dalloc<double>(st, (size_t)V * d);
+        launch_canon_gather(M, V, keys, order, mesh->osig, mesh->oc, st);
+        CK(cudaGetLastError());
+    }
+    CK(cudaEventRecord(kt.next(), st));
+    kt.spans.emplace_back(F_CANON, canon_ev);
+    kt.launches += 3 + 2 * (d + 1);
+    CK(cudaEventRecord(ev.e[3], st));
+    unsigned long long hc[C_NCOUNT];
+    CK(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    srch.reset();
+    S.vertices = V;
+    S.rays = (int64_t)hc[C_RAYS];
+    S.fallback_rays = (int64_t)hc[C_FALLBACK];
+    S.uncertified = (int64_t)hc[C_UNCERT];
+    S.insecure = (int64_t)hc[C_INSECURE];
+    S.dd_rescores = (int64_t)hc[C_DD];
+    S.degenerate = (int64_t)hc[C_DEGEN];
+    S.descents = (int64_t)hc[C_DESCENT];
+    S.descent_retries = (int64_t)hc[C_DRETRY];
+    S.edges_closed = (int64_t)hc[C_EDGECLOSED];
+    double fam[F_N];
+    kt.totals(fam);
+    S.ms_knn = fam[F_KNN];
+    S.ms_descent = fam[F_DESCENT];
+    S.ms_expand = fam[F_EXPAND];
+    S.ms_fallback = fam[F_FALLBACK];
+    S.ms_centers = fam[F_CENTERS];
+    S.ms_canonical = fam[F_CANON];
+    S.launches = kt.launches;
+    S.ms_prepare = ms_between(ev.e[0], ev.e[1]);
+    S.ms_search = ms_between(ev.e[1], ev.e[2]);
+    S.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void ensure_neighbors(hv_mesh* m) {
+    using namespace hv;
+    if (m->nnbr >= 0) return;
+    hv_ctx* ctx = m->ctx;
+    cudaStream_t st = ctx->stream;
+    const int d = m->d, n = m->n;
+    const unsigned V = m->V;
+    m->inc_off = dalloc<long long>(st, (size_t)n + 1);
+    m->nbr_off = dalloc<long long>(st, (size_t)n + 1);
+    if (n == 0) {
+        CK(cudaMemsetAsync(m->inc_off, 0, sizeof(long long), st));
+        CK(cudaMemsetAsync(m->nbr_off, 0, sizeof(long long), st));
+        m->inc = dalloc<int>(st, 1);
+        m->nbr = dalloc<int>(st, 1);
+        m->nnbr = 0;
+        return;
+    }
+    Scratch s(st);
+    const unsigned long long np = (unsigned long long)V * (d + 1);
+    unsigned long long* pairs = s.get<unsigned long long>(np);
+    unsigned long long* pairs2 = s.get<unsigned long long>(np);
+    long long* cnt = s.get<long long>((size_t)n + 1);
+    CK(cudaMemsetAsync(cnt, 0, sizeof(long long) * (n + 1), st));
+    launch_inc_pairs(d, n, V, m->osig, pairs, cnt, st);
+    if (np) {
+        size_t tb = sort_keys_u64_temp((long long)np);
+        void* tmp = s.get<char>(tb);
+        sort_keys_u64(tmp, tb, pairs, pairs2, (long long)np, st);
+    }
+    {
+        size_t tb = scan_temp(n + 1);
+        void* tmp = s.get<char>(tb);
+        exclusive_scan_i64(tmp, tb, cnt, m->inc_off, n + 1, st);
+    }
+    long long ninc = 0;
+    CK(cudaMemcpyAsync(&ninc, m->inc_off + n, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    m->inc = dalloc<int>(st, (size_t)std::max(ninc, 1ll));
+    launch_inc_split((unsigned long long)ninc, pairs2, m->inc, st);
+    long long* nn = s.get<long long>((size_t)n + 1);
+    unsigned* dstat = s.get<unsigned>(1);
+    CK(cudaMemsetAsync(nn, 0, sizeof(long long) * (n + 1), st));
+    CK(cudaMemsetAsync(dstat, 0, sizeof(unsigned), st));
+    launch_nbr_count(d, n, m->inc_off, m->inc, m->osig, nn, dstat, st);
+    {
+        size_t tb = scan_temp(n + 1);
+        void* tmp = s.get<char>(tb);
+        exclusive_scan_i64(tmp, tb, nn, m->nbr_off, n + 1, st);
+    }
+    long long tot = 0;
+    unsigned hst = 0;
+    CK(cudaMemcpyAsync(&tot, m->nbr_off + n, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&hst, dstat, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (hst) throw HvError(HV_E_CAPACITY, "a cell has more neighbours than the neighbour table holds");
+    m->nbr = dalloc<int>(st, (size_t)std::max(tot, 1ll));
+    launch_nbr_fill(d, n, m->inc_off, m->inc, m->osig, m->nbr_off, m->nbr, st);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    m->nnbr = tot;
+}
+
+int fail(hv_ctx* ctx, const HvError& e) {
+    if (ctx) ctx->err = e.what();
+    return e.code;
+}
+
+int validate_common(hv_ctx* ctx, int d, int64_t n, const double* lo, const double* hi, hv_mesh** out) {
+    if (!ctx || !out || !lo || !hi) return HV_E_INVALID_ARG;
+    if (d < 2 || d > HV_MAXD) { ctx->err = "dimension must be between 2 and 6"; return HV_E_INVALID_ARG; }
+    if (n < 0 || n > (1ll << 30)) { ctx->err = "point count out of range"; return HV_E_INVALID_ARG; }
+    for (int k = 0; k < d; ++k)
+        if (!(lo[k] < hi[k]) || !std::isfinite(lo[k]) || !std::isfinite(hi[k])) {
+            ctx->err = "box bounds must be finite with lo < hi";
+            return HV_E_INVALID_ARG;
+        }
+    return HV_OK;
+}
+
+int build_entry(hv_ctx* ctx, int d, int64_t n, const double* src, bool on_device, const double* lo,
+                const double* hi, const hv_params* params, hv_mesh** out) {
+    int rc = validate_common(ctx, d, n, lo, hi, out);
+    if (rc != HV_OK) return rc;
+    if (n > 0 && !src) { ctx->err = "null point array"; return HV_E_INVALID_ARG; }
+    hv_mesh* m = new hv_mesh();
+    m->ctx = ctx; m->d = d; m->n = (int)n;
+    for (int k = 0; k < d; ++k) { m->lo[k] = lo[k]; m->hi[k] = hi[k]; }
+    if (params) m->prm = *params; else hv_params_default(&m->prm);
+    if (m->prm.method != HV_METHOD_FAST && m->prm.method != HV_METHOD_PLAIN) {
+        delete m;
+        ctx->err = "unknown method";
+        return HV_E_INVALID_ARG;
+    }
+    try {
+        CK(cudaSetDevice(ctx->device));
+        build_impl(ctx, m, src, on_device, src);
+    } catch (const HvError& e) {
+        hv_mesh_free(m);
+        return fail(ctx, e);
+    } catch (const std::bad_alloc&) {
+        hv_mesh_free(m);
+        ctx->err = "host allocation failed";
+        return HV_E_OOM;
+    }
+    *out = m;
+    return HV_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hv_version(void) { return HV_VERSION; }
+
+void hv_params_default(hv_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->method = HV_METHOD_FAST;
+    p->seed = 0x5EEDull;
+}
+
+int hv_ctx_create(int device, hv_ctx** out) {
+    if (!out) return HV_E_INVALID_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return HV_E_CUDA;
+    hv_ctx* c = new hv_ctx();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) { delete c; return HV_E_CUDA; }
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return HV_E_CUDA; }
+    cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
+    if (cudaMallocHost((void**)&c->h_stat, 4 * sizeof(unsigned)) != cudaSuccess) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return HV_E_CUDA;
+    }
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    *out = c;
+    return HV_OK;
+}
+
+int hv_ctx_destroy(hv_ctx* ctx) {
+    if (!ctx) return HV_E_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFreeHost(ctx->h_stat);
+    for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return HV_OK;
+}
+
+const char* hv_last_error(hv_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+void* hv_ctx_stream(hv_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int hv_mesh_build(hv_ctx* ctx, int d, int64_t n, const double* pts, const double* lo, const double* hi,
+                  const hv_params* params, hv_mesh** out) {
+    return build_entry(ctx, d, n, pts, false, lo, hi, params, out);
+}
+
+int hv_mesh_build_device(hv_ctx* ctx, int d, int64_t n, const double* d_pts, const double* lo, const double* hi,
+                         const hv_params* params, hv_mesh** out) {
+    return build_entry(ctx, d, n, d_pts, true, lo, hi, params, out);
+}
+
+int hv_mesh_counts(hv_mesh* m, int64_t* nverts, int64_t* nnbr_total) {
+    if (!m) return HV_E_INVALID_ARG;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        if (nnbr_total) { ensure_neighbors(m); *nnbr_total = m->nnbr; }
+        if (nverts) *nverts = m->V;
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
+int hv_mesh_vertices(hv_mesh* m, int64_t* sig, double* r) {
+    if (!m || (m->V && (!sig || !r))) return HV_E_INVALID_ARG;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        cudaStream_t st = m->ctx->stream;
+        if (m->V) {
+            Scratch s(st);
+            const size_t ns = (size_t)m->V * (m->d + 1);
+            int64_t* dsig = s.get<int64_t>(ns);
+            hv::launch_out_vertices(m->d, m->V, m->osig, dsig, st);
+            CK(cudaMemcpyAsync(sig, dsig, ns * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(r, m->oc, (size_t)m->V * m->d * sizeof(double), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+        }
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
+int hv_mesh_neighbors(hv_mesh* m, int64_t* offs, int64_t* nbr) {
+    if (!m || !offs) return HV_E_INVALID_ARG;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        ensure_neighbors(m);
+        if (m->nnbr > 0 && !nbr) return HV_E_INVALID_ARG;
+        cudaStream_t st = m->ctx->stream;
+        CK(cudaMemcpyAsync(offs, m->nbr_off, sizeof(int64_t) * (m->n + 1), cudaMemcpyDeviceToHost, st));
+        if (m->nnbr > 0) {
+            Scratch s(st);
+            int64_t* dn = s.get<int64_t>((size_t)m->nnbr);
+            hv::launch_out_nbr(m->nnbr, m->nbr, dn, st);
+            CK(cudaMemcpyAsync(nbr, dn, sizeof(int64_t) * m->nnbr, cudaMemcpyDeviceToHost, st));
+        }
+        CK(cudaStreamSynchronize(st));
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
+int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) {
+    if (!m || (m->n > 0 && !vol)) return HV_E_INVALID_ARG;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        ensure_neighbors(m);
+        if (m->nnbr > 0 && !area) return HV_E_INVALID_ARG;
+        if (m->n == 0) return HV_OK;
+        cudaStream_t st = m->ctx->stream;
+        const int d = m->d, n = m->n;
+        std::vector<long long> io(n + 1);
+        CK(cudaMemcpyAsync(io.data(), m->inc_off, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        long long maxc = 1;
+        for (int i = 0; i < n; ++i) maxc = std::max(maxc, io[i + 1] - io[i]);
+        int smax = 0;
+        cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, m->ctx->device);
+        Scratch s(st);
+        double* dvol = s.get<double>(n);
+        double* darea = s.get<double>((size_t)std::max(m->nnbr, 1ll));
+        unsigned* dstat = s.get<unsigned>(1);
+        hv::IntegrateInput in{d, n, m->lo, m->hi, m->d_in, m->osig, m->oc, m->inc_off, m->inc, m->nbr_off, m->nbr, dstat};
+        const int capC = (int)next_pow2((unsigned long long)maxc);
+        int capV = (int)std::min<long long>(capC, std::max(64, capC / 4));
+        for (int attempt = 0;; ++attempt) {
+            const int capF = 2 * capV;
+            const int capE = (int)next_pow2((unsigned long long)capV * (d - 1) / 2 + 2);
+            const size_t sm = hv::poly_smem_bytes(d, capC, capV, capF, capE);
+            if ((long long)sm > smax) throw HvError(HV_E_CAPACITY, "cell too large for the polygon integrator (" +
+                                                      std::to_string(maxc) + " vertices)");
+            CK(cudaMemsetAsync(dstat, 0, sizeof(unsigned), st));
+            CK(cudaMemsetAsync(darea, 0, sizeof(double) * std::max(m->nnbr, 1ll), st));
+            if (hv::launch_polygon(in, capC, capV, capF, capE, darea, dvol, m->ctx->nsm, st) != 0)
+                throw HvError(HV_E_CUDA, "polygon integrator launch failed");
+            CK(cudaGetLastError());
+            unsigned hs = 0;
+            CK(cudaMemcpyAsync(&hs, dstat, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (hs == 0) break;
+            if ((hs & 1u) || capV >= capC || attempt > 6)
+                throw HvError(HV_E_CAPACITY, "facet structure beyond the polygon integrator's capacity");
+            capV = std::min(capC, capV * 2);
+        }
+        CK(cudaMemcpyAsync(vol, dvol, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        if (m->nnbr > 0) CK(cudaMemcpyAsync(area, darea, sizeof(double) * m->nnbr, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
+int hv_integrate_heuristic_mc(hv_mesh* m, int ndir, uint64_t seed, double* vol, double* area) {
+    if (!m || ndir <= 0 || (m->n > 0 && !vol)) return HV_E_INVALID_ARG;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        ensure_neighbors(m);
+        if (m->nnbr > 0 && !area) return HV_E_INVALID_ARG;
+        if (m->n == 0) return HV_OK;
+        cudaStream_t st = m->ctx->stream;
+        const int d = m->d, n = m->n;
+        std::vector<long long> no(n + 1);
+        CK(cudaMemcpyAsync(no.data(), m->nbr_off, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        long long maxdeg = 1;
+        for (int i = 0; i < n; ++i) maxdeg = std::max(maxdeg, no[i + 1] - no[i]);
+        const int capN = (int)((maxdeg + 7) / 8 * 8);
+        int smax = 0;
+        cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, m->ctx->device);
+        const size_t sm = (size_t)2 * capN * (d + 2) * sizeof(float) + (size_t)2 * 32 * capN * sizeof(double) + 16;
+        if ((long long)sm > smax) throw HvError(HV_E_CAPACITY, "cell degree too large for the MC integrator");
+        Scratch s(st);
+        const size_t E = (size_t)std::max(m->nnbr, 1ll);
+        double* rawV = s.get<double>(n);
+        double* varV = s.get<double>(n);
+        double* dvol = s.get<double>(n);
+        double* rawA = s.get<double>(E);
+        double* outA = s.get<double>(E);
+        unsigned* dstat = s.get<unsigned>(1);
+        CK(cudaMemsetAsync(dstat, 0, sizeof(unsigned), st));
+        hv::IntegrateInput in{d, n, m->lo, m->hi, m->d_in, m->osig, m->oc, m->inc_off, m->inc, m->nbr_off, m->nbr, dstat};
+        const double cvol = std::pow(M_PI, d / 2.0) / std::tgamma(1.0 + d / 2.0);
+        if (hv::launch_heuristic_mc(in, ndir, seed, capN, cvol, rawV, rawA, varV, outA, dvol, m->ctx->nsm, st) != 0)
+            throw HvError(HV_E_CUDA, "MC integrator launch failed");
+        CK(cudaGetLastError());
+        unsigned hs = 0;
+        CK(cudaMemcpyAsync(&hs, dstat, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(vol, dvol, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        if (m->nnbr > 0) CK(cudaMemcpyAsync(area, outA, sizeof(double) * m->nnbr, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (hs) throw HvError(HV_E_CAPACITY, "cell degree beyond the MC integrator's capacity");
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
+int hv_mesh_stats(hv_mesh* m, hv_stats* s) {
+    if (!m || !s) return HV_E_INVALID_ARG;
+    *s = m->st;
+    return HV_OK;
+}
+
+int hv_mesh_free(hv_mesh* m) {
+    if (!m) return HV_E_INVALID_ARG;
+    cudaStream_t st = m->ctx->stream;
+    cudaSetDevice(m->ctx->device);
+    dfree(st, m->d_in);
+    dfree(st, m->osig);
+    dfree(st, m->oc);
+    dfree(st, m->inc_off);
+    dfree(st, m->inc);
+    dfree(st, m->nbr_off);
+    dfree(st, m->nbr);
+    cudaStreamSynchronize(st);
+    delete m;
+    return HV_OK;
+}
+
+}  // extern "C"

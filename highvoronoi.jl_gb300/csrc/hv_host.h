@@ -1,0 +1,51 @@
+// hv_host.h -- launchers shared between the libhvgpu translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hv {
+struct DevMesh;
+
+// hv_prep.cu
+void launch_morton(int d, const double* in, int n, const double* lo, const double* hi,
+                   unsigned long long* codes, int* idx, unsigned* status, cudaStream_t st);
+void launch_gather(int d, const double* in, const int* perm, int n, double* pts, float* pts32, cudaStream_t st);
+void launch_bvh(const DevMesh& M, float* blo, float* bhi, unsigned* flags, cudaStream_t st);
+void launch_knn(const DevMesh& M, int* knn, float* sec, cudaStream_t st);
+size_t sort_pairs_u64_i32_temp(int n);
+void sort_pairs_u64_i32(void* temp, size_t temp_bytes, const unsigned long long* kin, unsigned long long* kout,
+                        const int* vin, int* vout, int n, int end_bit, cudaStream_t st);
+size_t sort_pairs_u32_i32_temp(int n);
+void sort_pairs_u32_i32(void* temp, size_t temp_bytes, const unsigned* kin, unsigned* kout, const int* vin,
+                        int* vout, int n, int end_bit, cudaStream_t st);
+size_t sort_keys_u64_temp(long long n);
+void sort_keys_u64(void* temp, size_t temp_bytes, const unsigned long long* kin, unsigned long long* kout,
+                   long long n, cudaStream_t st);
+size_t scan_temp(int n);
+void exclusive_scan_i64(void* temp, size_t temp_bytes, const long long* in, long long* out, int n, cudaStream_t st);
+
+// hv_search.cu
+void launch_descent(const DevMesh& M, int stride, int nseeds, unsigned long long seed, cudaStream_t st);
+void launch_centers(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+void launch_expand_plain(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cudaStream_t st);
+void launch_expand_fast(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq,
+                        unsigned fqcap, int nsm, cudaStream_t st);
+void launch_fallback(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm,
+                     cudaStream_t st);
+
+// hv_post.cu
+// canonical keys: original 0-based items of each vertex, sorted, SoA by position
+void launch_canon_keys(const DevMesh& M, unsigned V, unsigned* keys, cudaStream_t st);
+void launch_gather_keys(const unsigned* keys_pos, const int* order, unsigned V, unsigned* out, cudaStream_t st);
+void launch_canon_gather(const DevMesh& M, unsigned V, const unsigned* keys, const int* order, int* osig,
+                         double* oc, cudaStream_t st);
+void launch_inc_pairs(int d, int n, unsigned V, const int* osig, unsigned long long* pairs, long long* cnt,
+                      cudaStream_t st);
+void launch_inc_split(unsigned long long npairs, const unsigned long long* pairs, int* inc, cudaStream_t st);
+void launch_nbr_count(int d, int n, const long long* inc_off, const int* inc, const int* osig, long long* nnbr,
+                      unsigned* status, cudaStream_t st);
+void launch_nbr_fill(int d, int n, const long long* inc_off, const int* inc, const int* osig,
+                     const long long* nbr_off, int* nbr, cudaStream_t st);
+void launch_out_vertices(int d, unsigned V, const int* osig, int64_t* sig_out, cudaStream_t st);
+void launch_out_nbr(long long total, const int* nbr, int64_t* out, cudaStream_t st);
+}  // namespace hv

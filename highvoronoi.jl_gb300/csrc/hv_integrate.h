@@ -1,0 +1,29 @@
+// hv_integrate.h -- launchers of the per-cell integrators (hv_integrate.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace hv {
+
+struct IntegrateInput {
+    int d, n;
+    const double* lo;
+    const double* hi;
+    const double* pts;        // original order, n x d
+    const int* osig;          // V x (d+1), original 0-based items
+    const double* oc;         // V x d
+    const long long* inc_off; // cell -> vertex CSR
+    const int* inc;
+    const long long* nbr_off; // cell -> neighbour CSR (sorted items, planes n+p)
+    const int* nbr;
+    unsigned* status;         // 1: cell over capacity, 2: facet over capacity, 4: degree over capacity
+};
+
+size_t poly_smem_bytes(int d, int capC, int capV, int capF, int capE);
+int launch_polygon(const IntegrateInput& in, int capC, int capV, int capF, int capE, double* area, double* vol,
+                   int nsm, cudaStream_t st);
+int launch_heuristic_mc(const IntegrateInput& in, int ndir, unsigned long long seed, int capN, double cvol,
+                        double* rawV, double* rawA, double* varV, double* outA, double* vol, int nsm,
+                        cudaStream_t st);
+
+}  // namespace hv

@@ -1,0 +1,222 @@
+// hv_post.cu -- canonical vertex order, cell incidence and neighbour lists.
+//
+// After the search every vertex is renumbered in the lexicographic order of
+// its signature written with original generator ids (planes as n+p).  The
+// order is a pure function of the vertex set, so every later result (lists,
+// integrals, sums) is bitwise reproducible regardless of the scheduling of
+// the wavefront.
+//
+// Neighbours of cell i are the sorted union of the generators of its
+// vertices, planes included (neighbors_of_cell_new, src/neighbors.jl:219-258).
+#include "hv_internal.cuh"
+#include "hv_host.h"
+
+namespace hv {
+
+template <int D>
+__global__ void k_canon_keys(DevMesh M, unsigned V, unsigned* keys) {
+    for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        unsigned s[D + 1];
+#pragma unroll
+        for (int k = 0; k <= D; ++k) {
+            const int it = M.vsig[(size_t)v * (D + 1) + k];
+            s[k] = it < M.n ? (unsigned)__ldg(M.perm + it) : (unsigned)it;
+        }
+#pragma unroll
+        for (int a = 1; a <= D; ++a) {
+#pragma unroll
+            for (int b = a; b > 0; --b) {
+                if (s[b] < s[b - 1]) { unsigned x = s[b]; s[b] = s[b - 1]; s[b - 1] = x; }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k <= D; ++k) keys[(size_t)k * V + v] = s[k];
+    }
+}
+
+__global__ void k_gather_keys(const unsigned* __restrict__ keys_pos, const int* __restrict__ order, unsigned V,
+                              unsigned* out) {
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < V; i += gridDim.x * blockDim.x)
+        out[i] = keys_pos[order[i]];
+}
+
+template <int D>
+__global__ void k_canon_gather(DevMesh M, unsigned V, const unsigned* __restrict__ keys,
+                               const int* __restrict__ order, int* osig, double* oc) {
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < V; i += gridDim.x * blockDim.x) {
+        const int v = order[i];
+#pragma unroll
+        for (int k = 0; k <= D; ++k) osig[(size_t)i * (D + 1) + k] = (int)keys[(size_t)k * V + v];
+#pragma unroll
+        for (int k = 0; k < D; ++k) oc[(size_t)i * D + k] = M.vc[(size_t)v * D + k];
+    }
+}
+
+template <int D>
+__global__ void k_inc_pairs(int n, unsigned V, const int* __restrict__ osig, unsigned long long* pairs,
+                            long long* cnt) {
+    for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int k = 0; k <= D; ++k) {
+            const int it = osig[(size_t)v * (D + 1) + k];
+            if (it < n) {
+                pairs[(size_t)v * (D + 1) + k] = ((unsigned long long)(unsigned)it << 32) | v;
+                atomicAdd((unsigned long long*)(cnt + it), 1ull);
+            } else {
+                pairs[(size_t)v * (D + 1) + k] = ~0ull;
+            }
+        }
+    }
+}
+
+__global__ void k_inc_split(unsigned long long npairs, const unsigned long long* __restrict__ pairs, int* inc) {
+    for (unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; t < npairs;
+         t += (unsigned long long)gridDim.x * blockDim.x)
+        inc[t] = (int)(unsigned)(pairs[t] & 0xFFFFFFFFull);
+}
+
+// One warp per cell: shared-memory hash set of the generators met.
+constexpr int NB_WPB = 4;
+constexpr int NB_HS = 1024;
+
+template <int D>
+__device__ int nbr_collect(int i, const long long* inc_off, const int* inc, const int* osig, int* hs, int lane) {
+    for (int k = lane; k < NB_HS; k += 32) hs[k] = 0x7FFFFFFF;
+    __syncwarp();
+    int fresh = 0;
+    for (long long t = inc_off[i] + lane; t < inc_off[i + 1]; t += 32) {
+        const int v = inc[t];
+#pragma unroll
+        for (int k = 0; k <= D; ++k) {
+            const int it = osig[(size_t)v * (D + 1) + k];
+            if (it == i) continue;
+            unsigned h = ((unsigned)it * 2654435761u) & (NB_HS - 1);
+            for (int probe = 0; probe < NB_HS; ++probe) {
+                const int prev = atomicCAS(&hs[h], 0x7FFFFFFF, it);
+                if (prev == 0x7FFFFFFF) { ++fresh; break; }
+                if (prev == it) break;
+                h = (h + 1) & (NB_HS - 1);
+            }
+        }
+    }
+    __syncwarp();
+    return __reduce_add_sync(0xFFFFFFFFu, fresh);
+}
+
+template <int D>
+__global__ void __launch_bounds__(NB_WPB * 32) k_nbr_count(int n, const long long* inc_off, const int* inc,
+                                                           const int* osig, long long* nnbr, unsigned* status) {
+    __shared__ int shs[NB_WPB][NB_HS];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = blockIdx.x * NB_WPB + wib; i < n; i += gridDim.x * NB_WPB) {
+        const int c = nbr_collect<D>(i, inc_off, inc, osig, shs[wib], lane);
+        if (lane == 0) {
+            nnbr[i] = c;
+            if (c > NB_HS / 2) atomicOr(status, ST_HASH);
+        }
+        __syncwarp();
+    }
+}
+
+template <int D>
+__global__ void __launch_bounds__(NB_WPB * 32) k_nbr_fill(int n, const long long* inc_off, const int* inc,
+                                                          const int* osig, const long long* nbr_off, int* nbr) {
+    __shared__ int shs[NB_WPB][NB_HS];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = blockIdx.x * NB_WPB + wib; i < n; i += gridDim.x * NB_WPB) {
+        int* hs = shs[wib];
+        const int c = nbr_collect<D>(i, inc_off, inc, osig, hs, lane);
+        // bitonic sort of the whole table (empty slots hold INT_MAX)
+#pragma unroll 1
+        for (int k = 2; k <= NB_HS; k <<= 1) {
+#pragma unroll 1
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int a = lane; a < NB_HS; a += 32) {
+                    const int b = a ^ j;
+                    if (b > a) {
+                        const bool up = (a & k) == 0;
+                        const int x = hs[a], y = hs[b];
+                        if ((x > y) == up) { hs[a] = y; hs[b] = x; }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        const long long o = nbr_off[i];
+        for (int k = lane; k < c; k += 32) nbr[o + k] = hs[k];
+        __syncwarp();
+    }
+}
+
+template <int D>
+__global__ void k_out_vertices(unsigned V, const int* __restrict__ osig, int64_t* out) {
+    const unsigned long long total = (unsigned long long)V * (D + 1);
+    for (unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; t < total;
+         t += (unsigned long long)gridDim.x * blockDim.x)
+        out[t] = (int64_t)osig[t] + 1;
+}
+
+__global__ void k_out_nbr(long long total, const int* __restrict__ nbr, int64_t* out) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x)
+        out[t] = (int64_t)nbr[t] + 1;
+}
+
+// ---------------------------------------------------------------------------
+#define HV_DISPATCH(d, CALL)                           \
+    switch (d) {                                       \
+        case 2: { constexpr int DD = 2; CALL; } break; \
+        case 3: { constexpr int DD = 3; CALL; } break; \
+        case 4: { constexpr int DD = 4; CALL; } break; \
+        case 5: { constexpr int DD = 5; CALL; } break; \
+        case 6: { constexpr int DD = 6; CALL; } break; \
+        default: break;                                \
+    }
+
+static unsigned grid_for(unsigned long long n, int bs) {
+    unsigned long long b = (n + bs - 1) / bs;
+    if (b > 65535ull * 16) b = 65535ull * 16;
+    return (unsigned)(b ? b : 1);
+}
+
+void launch_canon_keys(const DevMesh& M, unsigned V, unsigned* keys, cudaStream_t st) {
+    if (!V) return;
+    HV_DISPATCH(M.d, (k_canon_keys<DD><<<grid_for(V, 256), 256, 0, st>>>(M, V, keys)));
+}
+void launch_gather_keys(const unsigned* keys_pos, const int* order, unsigned V, unsigned* out, cudaStream_t st) {
+    if (!V) return;
+    k_gather_keys<<<grid_for(V, 256), 256, 0, st>>>(keys_pos, order, V, out);
+}
+void launch_canon_gather(const DevMesh& M, unsigned V, const unsigned* keys, const int* order, int* osig,
+                         double* oc, cudaStream_t st) {
+    if (!V) return;
+    HV_DISPATCH(M.d, (k_canon_gather<DD><<<grid_for(V, 256), 256, 0, st>>>(M, V, keys, order, osig, oc)));
+}
+void launch_inc_pairs(int d, int n, unsigned V, const int* osig, unsigned long long* pairs, long long* cnt,
+                      cudaStream_t st) {
+    if (!V) return;
+    HV_DISPATCH(d, (k_inc_pairs<DD><<<grid_for(V, 256), 256, 0, st>>>(n, V, osig, pairs, cnt)));
+}
+void launch_inc_split(unsigned long long npairs, const unsigned long long* pairs, int* inc, cudaStream_t st) {
+    if (!npairs) return;
+    k_inc_split<<<grid_for(npairs, 256), 256, 0, st>>>(npairs, pairs, inc);
+}
+void launch_nbr_count(int d, int n, const long long* inc_off, const int* inc, const int* osig, long long* nnbr,
+                      unsigned* status, cudaStream_t st) {
+    if (n <= 0) return;
+    HV_DISPATCH(d, (k_nbr_count<DD><<<grid_for(n, NB_WPB), NB_WPB * 32, 0, st>>>(n, inc_off, inc, osig, nnbr, status)));
+}
+void launch_nbr_fill(int d, int n, const long long* inc_off, const int* inc, const int* osig,
+                     const long long* nbr_off, int* nbr, cudaStream_t st) {
+    if (n <= 0) return;
+    HV_DISPATCH(d, (k_nbr_fill<DD><<<grid_for(n, NB_WPB), NB_WPB * 32, 0, st>>>(n, inc_off, inc, osig, nbr_off, nbr)));
+}
+void launch_out_vertices(int d, unsigned V, const int* osig, int64_t* out, cudaStream_t st) {
+    if (!V) return;
+    HV_DISPATCH(d, (k_out_vertices<DD><<<grid_for((unsigned long long)V * (DD + 1), 256), 256, 0, st>>>(V, osig, out)));
+}
+void launch_out_nbr(long long total, const int* nbr, int64_t* out, cudaStream_t st) {
+    if (total <= 0) return;
+    k_out_nbr<<<grid_for(total, 256), 256, 0, st>>>(total, nbr, out);
+}
+
+}  // namespace hv

@@ -1,0 +1,346 @@
+// hv_prep.cu -- point ordering, search tree and candidate lists.
+//
+// The reference builds a kd-tree with leaf size 10 split at the balanced index
+// of the widest dimension (src/NearestNeighborModified/kd_tree.jl:27-158).  On
+// the GPU the same role is played by an implicit complete binary tree over a
+// Morton-ordered point array: leaves hold `leaf` consecutive points, node boxes
+// are unions of their children and are built bottom-up in one pass.  Morton
+// order adapts to clustered inputs the way the balanced kd split does (every
+// leaf holds the same number of points) and keeps every later access to a
+// generator's neighbourhood local in memory.
+//
+// Candidate lists: for every generator the K nearest other generators (FP32
+// distances) and a radius `sec` such that every generator closer than `sec`
+// is in the list.  The fast ray kernel accepts a decision only if the new
+// empty sphere lies inside that radius (the security test).
+#include <cub/cub.cuh>
+
+#include "hv_internal.cuh"
+#include "hv_host.h"
+
+namespace hv {
+
+template <int D>
+__global__ void k_morton(const double* __restrict__ in, int n, DevBox box, unsigned long long* codes, int* idx,
+                         unsigned* status) {
+    constexpr int B = (63 / D) > 21 ? 21 : (63 / D);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        unsigned q[D];
+        bool ok = true;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const double x = in[(size_t)i * D + k];
+            if (!(x > box.lo[k] && x < box.hi[k])) ok = false;
+            double f = (x - box.lo[k]) / (box.hi[k] - box.lo[k]) * (double)(1u << B);
+            f = fmin(fmax(f, 0.0), (double)((1u << B) - 1));
+            q[k] = ok ? (unsigned)f : 0u;
+        }
+        if (!ok) atomicOr(status, ST_BADINPUT);
+        unsigned long long code = 0;
+        for (int b = B - 1; b >= 0; --b) {
+#pragma unroll
+            for (int k = 0; k < D; ++k) code = (code << 1) | ((q[k] >> b) & 1u);
+        }
+        codes[i] = code;
+        idx[i] = i;
+    }
+}
+
+template <int D>
+__global__ void k_gather(const double* __restrict__ in, const int* __restrict__ perm, int n, double* pts,
+                         float* pts32) {
+    constexpr int DP = (D <= 4) ? 4 : 8;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const int o = perm[s];
+        float f[DP];
+#pragma unroll
+        for (int k = 0; k < DP; ++k) f[k] = 0.f;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const double x = in[(size_t)o * D + k];
+            pts[(size_t)s * D + k] = x;
+            f[k] = (float)x;
+        }
+        float4* dst = reinterpret_cast<float4*>(pts32 + (size_t)s * DP);
+#pragma unroll
+        for (int h = 0; h < DP / 4; ++h) dst[h] = make_float4(f[4 * h], f[4 * h + 1], f[4 * h + 2], f[4 * h + 3]);
+    }
+}
+
+// Bottom-up box construction: every leaf thread climbs while it is the second
+// child to arrive at a node (the first arrival stops).
+template <int D>
+__global__ void k_bvh(DevMesh M, float* blo, float* bhi, unsigned* flags) {
+    const int dp = M.dp;
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= M.P) return;
+    float lo[D], hi[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) { lo[k] = INFINITY; hi[k] = -INFINITY; }
+    if (l < M.nleaves) {
+        const int s0 = l * M.leaf, s1 = min(s0 + M.leaf, M.n);
+        for (int s = s0; s < s1; ++s) {
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                const double x = M.pts[(size_t)s * D + k];
+                lo[k] = fminf(lo[k], __double2float_rd(x));
+                hi[k] = fmaxf(hi[k], __double2float_ru(x));
+            }
+        }
+    }
+    int node = M.P + l;
+#pragma unroll
+    for (int k = 0; k < D; ++k) { blo[(size_t)node * dp + k] = lo[k]; bhi[(size_t)node * dp + k] = hi[k]; }
+    __threadfence();
+    while (node > 1) {
+        const int parent = node >> 1;
+        if (atomicAdd(&flags[parent], 1u) == 0u) return;
+        __threadfence();
+        const int c0 = 2 * parent, c1 = 2 * parent + 1;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            lo[k] = fminf(__ldcg(blo + (size_t)c0 * dp + k), __ldcg(blo + (size_t)c1 * dp + k));
+            hi[k] = fmaxf(__ldcg(bhi + (size_t)c0 * dp + k), __ldcg(bhi + (size_t)c1 * dp + k));
+            blo[(size_t)parent * dp + k] = lo[k];
+            bhi[(size_t)parent * dp + k] = hi[k];
+        }
+        __threadfence();
+        node = parent;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// candidate lists: one warp per generator, shared-memory top-(K+1) buffer
+// ---------------------------------------------------------------------------
+constexpr int KNN_WPB = 4;
+
+__device__ __forceinline__ bool pair_less(float da, int ia, float db, int ib) {
+    return da < db || (da == db && ia < ib);
+}
+
+template <int CAP>
+__device__ __forceinline__ void warp_bitonic(float* sd, int* si, int lane) {
+#pragma unroll 1
+    for (int k = 2; k <= CAP; k <<= 1) {
+#pragma unroll 1
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < CAP; i += 32) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const bool up = (i & k) == 0;
+                    const float da = sd[i], db = sd[ixj];
+                    const int ia = si[i], ib = si[ixj];
+                    if (pair_less(db, ib, da, ia) == up) { sd[i] = db; sd[ixj] = da; si[i] = ib; si[ixj] = ia; }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+template <int D, int CAP>
+__global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float* sec) {
+    constexpr int DP = (D <= 4) ? 4 : 8;
+    __shared__ float sd[KNN_WPB][CAP];
+    __shared__ int si[KNN_WPB][CAP];
+    __shared__ int sstack[KNN_WPB][64];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int K = M.K;
+    const unsigned FULL = 0xFFFFFFFFu;
+    const float ex = (float)(M.xscale * 5.9604645e-08);
+    float* d = sd[wib];
+    int* ix = si[wib];
+    int* stk = sstack[wib];
+    for (int q = blockIdx.x * KNN_WPB + wib; q < M.n; q += gridDim.x * KNN_WPB) {
+        float xq[DP];
+        {
+            const float4* p = reinterpret_cast<const float4*>(M.pts32 + (size_t)q * DP);
+#pragma unroll
+            for (int h = 0; h < DP / 4; ++h) {
+                float4 f = __ldg(p + h);
+                xq[4 * h] = f.x; xq[4 * h + 1] = f.y; xq[4 * h + 2] = f.z; xq[4 * h + 3] = f.w;
+            }
+        }
+        int cnt = 0;
+        float thr = INFINITY;
+        int sp = 1;
+        if (lane == 0) stk[0] = 1;
+        __syncwarp();
+        while (sp > 0) {
+            const int node = stk[--sp];
+            __syncwarp();
+            float bd = 0.f;
+            {
+                const float* lo = M.blo + (size_t)node * DP;
+                const float* hi = M.bhi + (size_t)node * DP;
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    const float l = __ldg(lo + k), h = __ldg(hi + k);
+                    const float e = xq[k] < l ? l - xq[k] : (xq[k] > h ? xq[k] - h : 0.f);
+                    bd = fmaf(e, e, bd);
+                }
+            }
+            if (bd > thr * 1.00001f) continue;
+            if (node >= M.P) {
+                const int l = node - M.P;
+                if (l >= M.nleaves) continue;
+                const int s0 = l * M.leaf, s1 = min(s0 + M.leaf, M.n);
+                for (int base = s0; base < s1; base += 32) {
+                    const int s = base + lane;
+                    float d2 = INFINITY;
+                    if (s < s1 && s != q) {
+                        float xs[DP];
+                        const float4* p = reinterpret_cast<const float4*>(M.pts32 + (size_t)s * DP);
+#pragma unroll
+                        for (int h = 0; h < DP / 4; ++h) {
+                            float4 f = __ldg(p + h);
+                            xs[4 * h] = f.x; xs[4 * h + 1] = f.y; xs[4 * h + 2] = f.z; xs[4 * h + 3] = f.w;
+                        }
+                        d2 = 0.f;
+#pragma unroll
+                        for (int k = 0; k < D; ++k) { const float e = xs[k] - xq[k]; d2 = fmaf(e, e, d2); }
+                    }
+                    const bool take = d2 < thr;
+                    const unsigned bal = __ballot_sync(FULL, take);
+                    if (take) {
+                        const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+                        d[pos] = d2; ix[pos] = s;
+                    }
+                    cnt += __popc(bal);
+                    __syncwarp();
+                    if (cnt > CAP - 32) {
+                        for (int i = cnt + lane; i < CAP; i += 32) { d[i] = INFINITY; ix[i] = 0x7FFFFFFF; }
+                        __syncwarp();
+                        warp_bitonic<CAP>(d, ix, lane);
+                        cnt = min(cnt, K + 1);
+                        if (cnt == K + 1) thr = d[K];
+                        __syncwarp();
+                    }
+                }
+            } else {
+                const int c0 = 2 * node, c1 = 2 * node + 1;
+                float b0 = 0.f, b1 = 0.f;
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    const float l0 = __ldg(M.blo + (size_t)c0 * DP + k), h0 = __ldg(M.bhi + (size_t)c0 * DP + k);
+                    const float l1 = __ldg(M.blo + (size_t)c1 * DP + k), h1 = __ldg(M.bhi + (size_t)c1 * DP + k);
+                    const float e0 = xq[k] < l0 ? l0 - xq[k] : (xq[k] > h0 ? xq[k] - h0 : 0.f);
+                    const float e1 = xq[k] < l1 ? l1 - xq[k] : (xq[k] > h1 ? xq[k] - h1 : 0.f);
+                    b0 = fmaf(e0, e0, b0); b1 = fmaf(e1, e1, b1);
+                }
+                if (sp + 2 > 64) {
+                    if (lane == 0) atomicOr(M.status, ST_STACK);
+                    break;
+                }
+                if (lane == 0) {
+                    if (b0 <= b1) { stk[sp] = c1; stk[sp + 1] = c0; }
+                    else { stk[sp] = c0; stk[sp + 1] = c1; }
+                }
+                sp += 2;
+                __syncwarp();
+            }
+        }
+        for (int i = cnt + lane; i < CAP; i += 32) { d[i] = INFINITY; ix[i] = 0x7FFFFFFF; }
+        __syncwarp();
+        warp_bitonic<CAP>(d, ix, lane);
+        for (int c = lane; c < K; c += 32) knn[(size_t)q * K + c] = (c < cnt) ? ix[c] : -1;
+        if (lane == 0) {
+            float r = INFINITY;
+            if (cnt >= K + 1) {
+                r = sqrtf(d[K]) * (1.f - 4e-6f) - 3.f * sqrtf((float)D) * ex;
+                r = fmaxf(r, 0.f);
+            }
+            sec[q] = r;
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+#define HV_DISPATCH(d, CALL)                           \
+    switch (d) {                                       \
+        case 2: { constexpr int DD = 2; CALL; } break; \
+        case 3: { constexpr int DD = 3; CALL; } break; \
+        case 4: { constexpr int DD = 4; CALL; } break; \
+        case 5: { constexpr int DD = 5; CALL; } break; \
+        case 6: { constexpr int DD = 6; CALL; } break; \
+        default: break;                                \
+    }
+
+void launch_morton(int d, const double* in, int n, const double* lo, const double* hi, unsigned long long* codes,
+                   int* idx, unsigned* status, cudaStream_t st) {
+    if (n <= 0) return;
+    DevBox box;
+    for (int k = 0; k < d; ++k) { box.lo[k] = lo[k]; box.hi[k] = hi[k]; }
+    const int blocks = (n + 255) / 256;
+    HV_DISPATCH(d, (k_morton<DD><<<blocks, 256, 0, st>>>(in, n, box, codes, idx, status)));
+}
+
+void launch_gather(int d, const double* in, const int* perm, int n, double* pts, float* pts32, cudaStream_t st) {
+    if (n <= 0) return;
+    const int blocks = (n + 255) / 256;
+    HV_DISPATCH(d, (k_gather<DD><<<blocks, 256, 0, st>>>(in, perm, n, pts, pts32)));
+}
+
+void launch_bvh(const DevMesh& M, float* blo, float* bhi, unsigned* flags, cudaStream_t st) {
+    if (M.n <= 0) return;
+    const int blocks = (M.P + 127) / 128;
+    HV_DISPATCH(M.d, (k_bvh<DD><<<blocks, 128, 0, st>>>(M, blo, bhi, flags)));
+}
+
+template <int D>
+static void launch_knn_t(const DevMesh& M, int* knn, float* sec, cudaStream_t st) {
+    const int blocks = (M.n + KNN_WPB - 1) / KNN_WPB;
+    const int need = 2 * M.K + 64;
+    if (need <= 128) k_knn<D, 128><<<blocks, KNN_WPB * 32, 0, st>>>(M, knn, sec);
+    else if (need <= 256) k_knn<D, 256><<<blocks, KNN_WPB * 32, 0, st>>>(M, knn, sec);
+    else if (need <= 512) k_knn<D, 512><<<blocks, KNN_WPB * 32, 0, st>>>(M, knn, sec);
+    else k_knn<D, 1024><<<blocks, KNN_WPB * 32, 0, st>>>(M, knn, sec);
+}
+
+void launch_knn(const DevMesh& M, int* knn, float* sec, cudaStream_t st) {
+    if (M.n <= 0) return;
+    HV_DISPATCH(M.d, (launch_knn_t<DD>(M, knn, sec, st)));
+}
+
+size_t sort_pairs_u64_i32_temp(int n) {
+    size_t b = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, b, (const unsigned long long*)nullptr, (unsigned long long*)nullptr,
+                                    (const int*)nullptr, (int*)nullptr, n);
+    return b;
+}
+void sort_pairs_u64_i32(void* temp, size_t temp_bytes, const unsigned long long* kin, unsigned long long* kout,
+                        const int* vin, int* vout, int n, int end_bit, cudaStream_t st) {
+    cub::DeviceRadixSort::SortPairs(temp, temp_bytes, kin, kout, vin, vout, n, 0, end_bit, st);
+}
+size_t sort_pairs_u32_i32_temp(int n) {
+    size_t b = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, b, (const unsigned*)nullptr, (unsigned*)nullptr, (const int*)nullptr,
+                                    (int*)nullptr, n);
+    return b;
+}
+void sort_pairs_u32_i32(void* temp, size_t temp_bytes, const unsigned* kin, unsigned* kout, const int* vin,
+                        int* vout, int n, int end_bit, cudaStream_t st) {
+    cub::DeviceRadixSort::SortPairs(temp, temp_bytes, kin, kout, vin, vout, n, 0, end_bit, st);
+}
+size_t sort_keys_u64_temp(long long n) {
+    size_t b = 0;
+    cub::DeviceRadixSort::SortKeys(nullptr, b, (const unsigned long long*)nullptr, (unsigned long long*)nullptr, n);
+    return b;
+}
+void sort_keys_u64(void* temp, size_t temp_bytes, const unsigned long long* kin, unsigned long long* kout,
+                   long long n, cudaStream_t st) {
+    cub::DeviceRadixSort::SortKeys(temp, temp_bytes, kin, kout, n, 0, 64, st);
+}
+size_t scan_temp(int n) {
+    size_t b = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, b, (const long long*)nullptr, (long long*)nullptr, n);
+    return b;
+}
+void exclusive_scan_i64(void* temp, size_t temp_bytes, const long long* in, long long* out, int n, cudaStream_t st) {
+    cub::DeviceScan::ExclusiveSum(temp, temp_bytes, in, out, n, st);
+}
+
+}  // namespace hv

@@ -1,0 +1,232 @@
+"""ctypes binding of libhvgpu (include/hvgpu.h).
+
+The library is the only compute path: if it cannot be loaded, or no CUDA
+device is present, every call raises.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(_PKG, "_build", "libhvgpu.so")
+
+HV_OK = 0
+HV_E_INVALID_ARG = -1
+HV_E_OOM = -2
+HV_E_CAPACITY = -3
+HV_E_DEGENERATE = -4
+HV_E_TIMEOUT = -5
+HV_E_CUDA = -6
+HV_E_INTERNAL = -7
+HV_METHOD_FAST = 0
+HV_METHOD_PLAIN = 1
+
+_ERRNAMES = {
+    HV_E_INVALID_ARG: "HV_E_INVALID_ARG", HV_E_OOM: "HV_E_OOM", HV_E_CAPACITY: "HV_E_CAPACITY",
+    HV_E_DEGENERATE: "HV_E_DEGENERATE", HV_E_TIMEOUT: "HV_E_TIMEOUT", HV_E_CUDA: "HV_E_CUDA",
+    HV_E_INTERNAL: "HV_E_INTERNAL",
+}
+
+
+class HVError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_ERRNAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int), ("knn", ctypes.c_int), ("leaf_size", ctypes.c_int),
+                ("rays_per_warp", ctypes.c_int), ("seed_stride", ctypes.c_int), ("edge_dedup", ctypes.c_int),
+                ("seed", ctypes.c_uint64), ("capacity_factor", ctypes.c_double)]
+
+
+STAT_FIELDS = ("vertices", "rays", "fallback_rays", "uncertified", "insecure", "dd_rescores", "degenerate",
+               "descents", "descent_retries", "levels", "edges_closed", "capacity_retries", "launches")
+TIME_FIELDS = ("ms_prepare", "ms_search", "ms_total", "ms_knn", "ms_descent", "ms_expand", "ms_fallback",
+               "ms_centers", "ms_canonical")
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in STAT_FIELDS] + [(n, ctypes.c_double) for n in TIME_FIELDS]
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load(path: str | None = None):
+    """Loads libhvgpu.so from the package's build folder (raises if absent)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise HVError(HV_E_INTERNAL, f"libhvgpu.so not built ({p}); run highvoronoi.jl_gb300/build.py")
+        L = ctypes.CDLL(p)
+        I, I64, U64, P = ctypes.c_int, ctypes.c_int64, ctypes.c_uint64, ctypes.c_void_p
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int64)
+        L.hv_version.argtypes = []; L.hv_version.restype = I
+        L.hv_params_default.argtypes = [ctypes.POINTER(Params)]; L.hv_params_default.restype = None
+        L.hv_ctx_create.argtypes = [I, ctypes.POINTER(P)]; L.hv_ctx_create.restype = I
+        L.hv_ctx_destroy.argtypes = [P]; L.hv_ctx_destroy.restype = I
+        L.hv_last_error.argtypes = [P]; L.hv_last_error.restype = ctypes.c_char_p
+        L.hv_ctx_stream.argtypes = [P]; L.hv_ctx_stream.restype = P
+        L.hv_mesh_build.argtypes = [P, I, I64, P, dp, dp, ctypes.POINTER(Params), ctypes.POINTER(P)]
+        L.hv_mesh_build.restype = I
+        L.hv_mesh_build_device.argtypes = [P, I, I64, P, dp, dp, ctypes.POINTER(Params), ctypes.POINTER(P)]
+        L.hv_mesh_build_device.restype = I
+        L.hv_mesh_counts.argtypes = [P, ip, ip]; L.hv_mesh_counts.restype = I
+        L.hv_mesh_vertices.argtypes = [P, ip, dp]; L.hv_mesh_vertices.restype = I
+        L.hv_mesh_neighbors.argtypes = [P, ip, ip]; L.hv_mesh_neighbors.restype = I
+        L.hv_integrate_polygon.argtypes = [P, dp, dp]; L.hv_integrate_polygon.restype = I
+        L.hv_integrate_heuristic_mc.argtypes = [P, I, U64, dp, dp]; L.hv_integrate_heuristic_mc.restype = I
+        L.hv_mesh_stats.argtypes = [P, ctypes.POINTER(Stats)]; L.hv_mesh_stats.restype = I
+        L.hv_mesh_free.argtypes = [P]; L.hv_mesh_free.restype = I
+        _lib = L
+        return L
+
+
+def dptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def iptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+
+class Context:
+    """One CUDA device + one stream (hv_ctx)."""
+
+    def __init__(self, device: int = 0):
+        L = load()
+        h = ctypes.c_void_p()
+        rc = L.hv_ctx_create(device, ctypes.byref(h))
+        if rc != HV_OK:
+            raise HVError(rc, f"hv_ctx_create(device={device}) failed: no usable CUDA device")
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def stream(self) -> int:
+        """cudaStream_t of this context (as an integer handle)."""
+        return load().hv_ctx_stream(self._h) or 0
+
+    def error(self) -> str:
+        return load().hv_last_error(self._h).decode()
+
+    def check(self, rc: int, what: str):
+        if rc != HV_OK:
+            raise HVError(rc, f"{what}: {self.error()}")
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load().hv_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(int(os.environ.get("HV_DEVICE", "0")))
+    return _default_ctx
+
+
+def make_params(method: int = HV_METHOD_FAST, **kw) -> Params:
+    p = Params()
+    load().hv_params_default(ctypes.byref(p))
+    p.method = method
+    for k, v in kw.items():
+        if v is not None:
+            setattr(p, k, v)
+    return p
+
+
+class Mesh:
+    """A mesh built on the device (hv_mesh).  Results are copied out on demand."""
+
+    def __init__(self, ctx: Context, pts: np.ndarray, lo, hi, params: Params, device_ptr: int | None = None):
+        L = load()
+        self.ctx = ctx
+        pts = np.ascontiguousarray(pts, dtype=np.float64)
+        self.n, self.d = pts.shape if device_ptr is None else (int(pts[0]), int(pts[1]))
+        self.lo = np.ascontiguousarray(lo, dtype=np.float64)
+        self.hi = np.ascontiguousarray(hi, dtype=np.float64)
+        h = ctypes.c_void_p()
+        if device_ptr is None:
+            rc = L.hv_mesh_build(ctx.handle, self.d, self.n, pts.ctypes.data_as(ctypes.c_void_p), dptr(self.lo),
+                                 dptr(self.hi), ctypes.byref(params), ctypes.byref(h))
+        else:
+            rc = L.hv_mesh_build_device(ctx.handle, self.d, self.n, ctypes.c_void_p(device_ptr), dptr(self.lo),
+                                        dptr(self.hi), ctypes.byref(params), ctypes.byref(h))
+        ctx.check(rc, "hv_mesh_build")
+        self._h = h
+
+    def counts(self, neighbors: bool = False):
+        nv = ctypes.c_int64()
+        nn = ctypes.c_int64()
+        rc = load().hv_mesh_counts(self._h, ctypes.byref(nv), ctypes.byref(nn) if neighbors else None)
+        self.ctx.check(rc, "hv_mesh_counts")
+        return nv.value, (nn.value if neighbors else None)
+
+    def vertices(self):
+        V, _ = self.counts()
+        sig = np.zeros((V, self.d + 1), dtype=np.int64)
+        r = np.zeros((V, self.d), dtype=np.float64)
+        self.ctx.check(load().hv_mesh_vertices(self._h, iptr(sig), dptr(r)), "hv_mesh_vertices")
+        return sig, r
+
+    def neighbors(self):
+        _, E = self.counts(neighbors=True)
+        offs = np.zeros(self.n + 1, dtype=np.int64)
+        nbr = np.zeros(max(E, 1), dtype=np.int64)
+        self.ctx.check(load().hv_mesh_neighbors(self._h, iptr(offs), iptr(nbr)), "hv_mesh_neighbors")
+        return offs, nbr[:E]
+
+    def polygon(self):
+        _, E = self.counts(neighbors=True)
+        vol = np.zeros(self.n)
+        area = np.zeros(max(E, 1))
+        self.ctx.check(load().hv_integrate_polygon(self._h, dptr(vol), dptr(area)), "hv_integrate_polygon")
+        return vol, area[:E]
+
+    def heuristic_mc(self, ndir: int, seed: int):
+        _, E = self.counts(neighbors=True)
+        vol = np.zeros(self.n)
+        area = np.zeros(max(E, 1))
+        rc = load().hv_integrate_heuristic_mc(self._h, ndir, seed, dptr(vol), dptr(area))
+        self.ctx.check(rc, "hv_integrate_heuristic_mc")
+        return vol, area[:E]
+
+    def stats(self) -> dict:
+        s = Stats()
+        self.ctx.check(load().hv_mesh_stats(self._h, ctypes.byref(s)), "hv_mesh_stats")
+        return {n: getattr(s, n) for n, _ in Stats._fields_}
+
+    def free(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load().hv_mesh_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

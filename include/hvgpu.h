@@ -1,0 +1,137 @@
+/*
+ * hvgpu.h -- C ABI of libhvgpu, the GB300 (sm_103a) implementation of
+ * HighVoronoi.jl's mesh-generation hot path.
+ *
+ * The library replaces, behind a `search_settings=(method=RCGPU,)` switch,
+ * the whole-mesh vertex search and the per-cell integrators of HighVoronoi.jl:
+ *
+ *   hv_mesh_build          voronoi(mesh; searcher)                src/sysvoronoi.jl:21-39
+ *                          (_voronoi / __voronoi / systematic_explore_cell /
+ *                          walkray / raycast_des2, src/sysvoronoi.jl:41-552,
+ *                          src/raycast.jl:45-1049), called from
+ *                          VoronoiGeometry, src/geometry.jl:153-156
+ *   hv_mesh_vertices       the vertex database the search fills    src/abstractmesh.jl:111-127
+ *                          (push!(mesh, sig=>r)); read back as VoronoiData
+ *                          vertices, src/voronoidata.jl:545-700
+ *   hv_mesh_neighbors      neighbors_of_cell                       src/neighbors.jl:219-258
+ *   hv_integrate_polygon   integrate_geo with VI_POLYGON           src/geometry.jl:203-263,
+ *                          src/polyintegrator.jl:80-468, src/cleanup_cell.jl:174-204
+ *   hv_integrate_heuristic_mc  integrate_geo with VI_HEURISTIC_MC  src/heuristic_mc.jl:1-56,
+ *                          src/mcintegrator.jl:98-226
+ *   hv_mesh_stats          the rare-event counters SRI_*          src/raycast-types.jl:497-539
+ *
+ * Conventions (identical to the reference): generators are 1-based; the
+ * domain is the non-periodic cuboid [lo, hi] (cuboid(d, dimensions=hi-lo,
+ * offset=lo, periodic=[]), src/boundary.jl:518-534) whose plane p (1-based,
+ * 2k-1 = upper face of axis k, 2k = lower face) is generator n+p; every vertex
+ * signature is sorted ascending.  Point arrays are d x n column-major doubles
+ * (Julia layout): point i occupies pts[d*i .. d*i+d-1].
+ *
+ * Ownership: the caller owns all host arrays; device memory belongs to the
+ * library and is released by hv_mesh_free / hv_ctx_destroy.
+ * Errors: every call returns HV_OK (0) or a negative HV_E_* code; the text of
+ * the last error of a context is returned by hv_last_error.
+ * Threading: one hv_ctx per host thread (each context owns one CUDA stream).
+ */
+#ifndef HVGPU_H
+#define HVGPU_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HV_VERSION 10000 /* 1.0.0 */
+
+#define HV_OK 0
+#define HV_E_INVALID_ARG (-1)
+#define HV_E_OOM (-2)
+#define HV_E_CAPACITY (-3)
+#define HV_E_DEGENERATE (-4)
+#define HV_E_TIMEOUT (-5)
+#define HV_E_CUDA (-6)
+#define HV_E_INTERNAL (-7)
+
+/* Raycast method, the GPU counterpart of the reference's method singletons
+ * (src/raycast-types.jl:244-285). */
+#define HV_METHOD_FAST 0  /* batched split-precision raycast (FP32 filter, FP64 verify) */
+#define HV_METHOD_PLAIN 1 /* one ray per thread, FP64, exact tree search */
+
+typedef struct hv_ctx hv_ctx;
+typedef struct hv_mesh hv_mesh;
+
+/* Search settings (the GPU part of the reference's RaycastParameter,
+ * src/raycast-types.jl:312-349).  Zero means "choose automatically". */
+typedef struct {
+    int method;           /* HV_METHOD_FAST or HV_METHOD_PLAIN */
+    int knn;              /* candidate-list length per generator */
+    int leaf_size;        /* points per tree leaf */
+    int rays_per_warp;    /* vertices expanded per warp in the fast kernel (1 or 2) */
+    int seed_stride;      /* run a descent from every k-th generator */
+    int edge_dedup;       /* 1: close edges whose both end points are known (edge hash) */
+    uint64_t seed;        /* seed of the descent directions */
+    double capacity_factor; /* vertex capacity headroom over the per-dimension estimate */
+} hv_params;
+
+typedef struct {
+    int64_t vertices;       /* unique Voronoi vertices */
+    int64_t rays;           /* incircle searches issued (edge walks) */
+    int64_t fallback_rays;  /* rays redone by the exact FP64 tree search */
+    int64_t uncertified;    /* FP32 decisions that needed FP64 */
+    int64_t insecure;       /* candidate list did not cover the new sphere */
+    int64_t dd_rescores;    /* FP64 decisions redone in double-double */
+    int64_t degenerate;     /* ties that survived double-double */
+    int64_t descents;       /* descent seeds */
+    int64_t descent_retries;
+    int64_t levels;         /* wavefront levels */
+    int64_t edges_closed;   /* edges skipped because both end points were known */
+    int64_t capacity_retries;
+    int64_t launches;       /* kernels launched by this build */
+    double ms_prepare;      /* upload, sort, tree, candidate lists */
+    double ms_search;       /* descent + wavefront */
+    double ms_total;        /* whole hv_mesh_build (host wall clock) */
+    /* device time per kernel family, CUDA events on the context's stream */
+    double ms_knn;          /* candidate lists */
+    double ms_descent;      /* seed vertices */
+    double ms_expand;       /* wavefront expansion (fast or plain kernel) */
+    double ms_fallback;     /* exact re-walks of uncertified/insecure rays */
+    double ms_centers;      /* FP64 circumcentres of new vertices */
+    double ms_canonical;    /* canonical renumbering */
+} hv_stats;
+
+int hv_version(void);
+void hv_params_default(hv_params* p);
+
+int hv_ctx_create(int device, hv_ctx** out);
+int hv_ctx_destroy(hv_ctx* ctx);
+const char* hv_last_error(hv_ctx* ctx);
+/* The CUDA stream (cudaStream_t) on which the context runs all its work, for
+ * callers that order their own work or timing events against it. */
+void* hv_ctx_stream(hv_ctx* ctx);
+
+/* Vertex search of the Voronoi mesh of n points (host array, d x n) inside the
+ * cuboid [lo, hi] (host arrays of length d).  2 <= d <= 6. */
+int hv_mesh_build(hv_ctx* ctx, int d, int64_t n, const double* pts, const double* lo, const double* hi,
+                  const hv_params* params, hv_mesh** out);
+/* Same with pts already in device memory (d x n doubles on the context's device). */
+int hv_mesh_build_device(hv_ctx* ctx, int d, int64_t n, const double* d_pts, const double* lo,
+                         const double* hi, const hv_params* params, hv_mesh** out);
+
+/* Sizes of the caller's buffers: vertices, and the total neighbour count. */
+int hv_mesh_counts(hv_mesh* mesh, int64_t* nverts, int64_t* nnbr_total);
+/* Vertex records sorted lexicographically by signature: sig is (d+1) x V
+ * (1-based, sorted), r is d x V. */
+int hv_mesh_vertices(hv_mesh* mesh, int64_t* sig, double* r);
+/* Neighbour CSR: offs[n+1] (0-based offsets), nbr (1-based, sorted per cell,
+ * planes as n+p). */
+int hv_mesh_neighbors(hv_mesh* mesh, int64_t* offs, int64_t* nbr);
+/* Exact cell volumes (n) and interface areas aligned with hv_mesh_neighbors. */
+int hv_integrate_polygon(hv_mesh* mesh, double* vol, double* area);
+/* Monte-Carlo volumes and areas, ndir Philox directions per cell. */
+int hv_integrate_heuristic_mc(hv_mesh* mesh, int ndir, uint64_t seed, double* vol, double* area);
+int hv_mesh_stats(hv_mesh* mesh, hv_stats* stats);
+int hv_mesh_free(hv_mesh* mesh);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1020,6 +1020,12 @@ int hvo_polygon(const hvo_mesh* m, double* vol, double* area) {
     return 0;
 }
 
+void hvo_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    U4 c{{ctr[0], ctr[1], ctr[2], ctr[3]}};
+    U4 o = philox(c, key[0], key[1]);
+    for (int k = 0; k < 4; ++k) out[k] = o.v[k];
+}
+
 void hvo_mc_directions(int d, int64_t cell, int ndir, uint64_t seed, double* dirs) {
     for (int s = 0; s < ndir; ++s) {
         double g[MAXD];

@@ -69,6 +69,9 @@ int hvo_sample_cells(int d, int64_t n, const double* pts, const double* lo, cons
 int64_t hvo_verify_vertices(int d, int64_t n, const double* pts, const double* lo, const double* hi,
                             int64_t nv, const int64_t* sig, const double* r, double rel_tol);
 
+/* Raw Philox4x32-10 block (for known-answer tests of the generator). */
+void hvo_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
 /* Philox4x32-10 unit directions shared with the GPU MC kernel (for tests). */
 void hvo_mc_directions(int d, int64_t cell, int ndir, uint64_t seed, double* dirs);
 

@@ -65,6 +65,8 @@ def lib():
             L.hvo_sample_cells.restype = I
             L.hvo_verify_vertices.argtypes = [I, I64, dp, dp, dp, I64, ip, dp, D]
             L.hvo_verify_vertices.restype = I64
+            u32p = ctypes.POINTER(ctypes.c_uint32)
+            L.hvo_philox4x32.argtypes = [u32p, u32p, u32p]; L.hvo_philox4x32.restype = None
             L.hvo_mc_directions.argtypes = [I, I64, I, U64, dp]; L.hvo_mc_directions.restype = None
             _lib = L
     return _lib
@@ -169,6 +171,14 @@ def sample_cells(pts, cells, seed=0, nthreads=0, lo=None, hi=None):
     if rc != 0:
         raise RuntimeError(lib().hvo_last_error().decode())
     return own.value, rays.value, sec.value
+
+
+def philox4x32(ctr, key):
+    c = (ctypes.c_uint32 * 4)(*ctr)
+    k = (ctypes.c_uint32 * 2)(*key)
+    o = (ctypes.c_uint32 * 4)()
+    lib().hvo_philox4x32(c, k, o)
+    return list(o)
 
 
 def mc_directions(d, cell, ndir, seed):

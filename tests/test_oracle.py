@@ -1,0 +1,168 @@
+"""Pins of the CPU oracle (no GPU needed).
+
+HighVoronoi.jl holds no golden vertex sets, neighbour lists or per-cell
+volumes; its own tests only assert the sum of volumes (test/rcmethods.jl:3-13,
+test/database.jl:3-12, test/basics.jl:42-46, test/jld.jl:15-20).  The oracle is
+pinned here by those property tests, by analytic known-answer meshes, by a
+brute-force empty-circumsphere check of every vertex (verify_mesh,
+src/abstractmesh.jl:221-254) and by the agreement of its two exploration
+orders (per-cell and the reference's lower-cell-first rule).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+from hvgpu import datasets as D
+
+
+@pytest.mark.parametrize("d", [2, 3, 4, 5])
+def test_single_generator_is_the_whole_cube(d):
+    m = O.OracleMesh(np.full((1, d), 0.3), integrate=True)
+    sig, r = m.vertices()
+    assert sig.shape == (2 ** d, d + 1)
+    # every corner: the generator plus one plane per axis
+    assert np.all(sig[:, 0] == 1)
+    corners = {tuple(np.round(x).astype(int)) for x in r}
+    assert len(corners) == 2 ** d
+    vol, area = m.polygon()
+    assert vol[0] == pytest.approx(1.0, abs=1e-14)
+    offs, nbr = m.neighbors()
+    assert list(nbr) == [1 + p for p in range(1, 2 * d + 1)]
+    np.testing.assert_allclose(area, np.ones(2 * d), atol=1e-14)
+
+
+def test_two_generators_split_the_square_at_the_bisector():
+    a, b = 0.2, 0.7
+    pts = np.array([[a, 0.5], [b, 0.5]])
+    m = O.OracleMesh(pts, integrate=True)
+    sig, r = m.vertices()
+    # vertices: 4 corners + 2 points where the bisector x=(a+b)/2 meets y=0,1
+    assert len(sig) == 6
+    xm = 0.5 * (a + b)
+    on_bisector = r[np.isclose(r[:, 0], xm, atol=1e-15)]
+    assert len(on_bisector) == 2
+    vol, area = m.polygon()
+    np.testing.assert_allclose(vol, [xm, 1 - xm], atol=1e-15)
+    offs, nbr = m.neighbors()
+    # cell 1 (left): neighbour 2 (interface length 1) and the faces x=0 (plane 2),
+    # y=1 (plane 3), y=0 (plane 4) as generators N+p = 4, 5, 6
+    assert list(nbr[offs[0]:offs[1]]) == [2, 4, 5, 6]
+    assert list(nbr[offs[1]:offs[2]]) == [1, 3, 5, 6]
+    a1 = area[offs[0]:offs[1]]
+    assert a1[0] == pytest.approx(1.0)
+
+
+def test_box_offset_and_scale():
+    pts = np.array([[1.5, -2.0, 3.2]])
+    lo = np.array([1.0, -3.0, 3.0]); hi = np.array([2.0, -1.0, 4.0])
+    m = O.OracleMesh(pts, lo=lo, hi=hi, integrate=True)
+    vol, _ = m.polygon()
+    assert vol[0] == pytest.approx(2.0, rel=1e-14)
+
+
+@pytest.mark.parametrize("d,n", [(2, 1000), (3, 400), (4, 300), (5, 80)])
+def test_vertices_pass_brute_force_empty_sphere(d, n):
+    pts = D.uniform_points(d, n, 7 + d)
+    m = O.OracleMesh(pts)
+    sig, r = m.vertices()
+    assert O.verify_vertices(pts, sig, r) == 0
+    # each vertex: d+1 distinct sorted items, at least one generator
+    assert np.all(np.diff(sig, axis=1) > 0)
+    assert np.all(sig[:, 0] <= n)
+    assert len({tuple(s) for s in sig}) == len(sig)
+
+
+@pytest.mark.parametrize("d,n,tol", [(4, 1000, 1e-3), (4, 500, 1e-2), (5, 100, 1e-2)])
+def test_reference_volume_sum_property(d, n, tol):
+    """test/rcmethods.jl:3-13 (4D, 1000), test/basics.jl:42-46 (4D, 500), test/jld.jl:15-20 (5D, 100)."""
+    pts = D.uniform_points(d, n, 100 + n)
+    m = O.OracleMesh(pts, integrate=True)
+    vol, area = m.polygon()
+    assert abs(vol.sum() - 1.0) < tol
+    assert abs(vol.sum() - 1.0) < 1e-11  # the exact integrator is exact up to rounding
+    assert np.all(vol > 0)
+
+
+@pytest.mark.parametrize("d,n", [(2, 500), (3, 300), (4, 150)])
+def test_two_exploration_orders_agree(d, n):
+    pts = D.uniform_points(d, n, 3)
+    a = O.OracleMesh(pts, mode=0, integrate=True)
+    b = O.OracleMesh(pts, mode=1, integrate=True)
+    sa, ra = a.vertices()
+    sb, rb = b.vertices()
+    np.testing.assert_array_equal(sa, sb)
+    np.testing.assert_array_equal(ra, rb)
+    va, aa = a.polygon()
+    vb, ab = b.polygon()
+    np.testing.assert_allclose(va, vb, rtol=1e-12)
+    # the reference's rule uses about one raycast per vertex (docs/src/index.md:93)
+    st = b.stats()
+    assert st["rays"] < 1.3 * len(sb)
+
+
+def test_neighbours_and_areas_are_symmetric():
+    pts = D.uniform_points(3, 300, 11)
+    m = O.OracleMesh(pts, integrate=True)
+    offs, nbr = m.neighbors()
+    vol, area = m.polygon()
+    n = len(pts)
+    table = {}
+    for i in range(n):
+        for t in range(offs[i], offs[i + 1]):
+            table[(i + 1, int(nbr[t]))] = area[t]
+    for (i, k), a in table.items():
+        if k <= n:
+            assert (k, i) in table
+            assert table[(k, i)] == a
+    # sum of boundary facet areas = surface of the unit cube
+    bsum = sum(a for (i, k), a in table.items() if k > n)
+    assert bsum == pytest.approx(6.0, rel=1e-12)
+
+
+def test_clustered_points_volume_sum():
+    pts = D.clustered_points(5, 400, 2)
+    m = O.OracleMesh(pts, integrate=True)
+    sig, r = m.vertices()
+    assert O.verify_vertices(pts, sig, r) == 0
+    vol, _ = m.polygon()
+    assert vol.sum() == pytest.approx(1.0, abs=1e-11)
+
+
+def test_mc_matches_polygon_within_statistics():
+    pts = D.uniform_points(3, 200, 5)
+    m = O.OracleMesh(pts, integrate=True)
+    vol, area = m.polygon()
+    mvol, marea, vvar, avar = m.heuristic_mc(4000, 9)
+    # raw per-cell estimator error within 5 sigma on nearly all cells
+    z = np.abs(mvol - vol) / np.sqrt(np.maximum(vvar, 1e-300))
+    assert np.mean(z < 5.0) > 0.97
+    assert abs(mvol.sum() - 1.0) < 0.02
+
+
+def test_philox_known_answers():
+    """Random123 known-answer vectors of Philox4x32-10."""
+    assert O.philox4x32([0, 0, 0, 0], [0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert O.philox4x32([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
+    assert O.philox4x32([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0]) == [
+        0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+def test_mc_directions_are_unit_and_deterministic():
+    a = O.mc_directions(6, 17, 64, 3)
+    b = O.mc_directions(6, 17, 64, 3)
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_allclose(np.linalg.norm(a, axis=1), 1.0, rtol=1e-14)
+    c = O.mc_directions(6, 18, 64, 3)
+    assert not np.allclose(a, c)
+
+
+def test_sample_cells_counts_owned_vertices():
+    pts = D.uniform_points(3, 400, 1)
+    m = O.OracleMesh(pts)
+    sig, _ = m.vertices()
+    own, rays, sec = O.sample_cells(pts, np.arange(400))
+    assert own == len(sig)
+    assert rays > own and sec > 0
+    assert math.isfinite(sec)
