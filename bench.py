@@ -50,6 +50,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-cells", type=int, default=0, help="cells per CPU sample (0 = all)")
+    ap.add_argument("--serve", action="store_true", help="only the served-stream measurement")
+    ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-slots", type=int, default=8)
+    ap.add_argument("--no-serve", action="store_true")
     return ap.parse_args()
 
 
@@ -146,6 +151,56 @@ def cpu_baseline(pts, cells, threads):
     import oracle as O
     own, rays, sec = O.sample_cells(pts, cells, nthreads=threads)
     return own, rays, sec
+
+
+def serve_requests(count, seed=2000):
+    """The served stream: request r has d uniform in {2,3,4,5}, N log-uniform in
+    [200, 20000] and points uniform in the unit cube drawn with seed r; arrival
+    gaps are exponential with the requested mean rate."""
+    from hvgpu import datasets as D
+    u = D.uniform01(seed, 0, 3 * count).reshape(count, 3)
+    reqs = []
+    for r in range(count):
+        d = 2 + min(int(u[r, 0] * 4), 3)
+        n = int(round(np.exp(np.log(200) + u[r, 1] * (np.log(20000) - np.log(200)))))
+        reqs.append((d, n, r))
+    gaps = -np.log(u[:, 2])
+    return reqs, gaps
+
+
+def run_serve(args, device):
+    import hvgpu
+    from hvgpu import datasets as D
+    from hvgpu.serve import Server
+    reqs, gaps = serve_requests(args.serve_requests)
+    pts = [D.uniform_points(d, n, r) for d, n, r in reqs]
+    arrivals = np.cumsum(gaps / args.serve_rate)
+    with Server(device=device, slots=args.serve_slots) as srv:
+        # warm-up: one request per dimension
+        for d in (2, 3, 4, 5):
+            srv.result(srv.submit(D.uniform_points(d, 500, 10 ** 6 + d), integrator="polygon"))
+        t0 = time.perf_counter()
+        tickets = []
+        for k, (p, ta) in enumerate(zip(pts, arrivals)):
+            now = time.perf_counter() - t0
+            if ta > now:
+                time.sleep(ta - now)
+            tickets.append(srv.submit(p, integrator="polygon"))
+        lat, fails, verts = [], 0, 0
+        for t in tickets:
+            r = srv.result(t)
+            if r["status"] != 0:
+                fails += 1
+                continue
+            lat.append(r["latency_ms"])
+            verts += r["sig"].shape[0]
+        t_end = time.perf_counter() - t0
+    lat = np.array(lat)
+    return {"requests": len(reqs), "rate_per_s": args.serve_rate, "slots": args.serve_slots, "failures": fails,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "meshes_per_s": len(lat) / t_end, "vertices": int(verts),
+            "config": "d uniform {2,3,4,5}, N log-uniform [200,20000], uniform points seed=request id, "
+                      "cuboid(d, periodic=[]), VI_POLYGON, Poisson arrivals"}
 
 
 def run_reference(args):
@@ -286,6 +341,12 @@ def run_ours(args):
         cpu = {"value": own / sec, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"per-cell search of {len(cells)} of the {n} cells, vertices owned per second "
                          f"(C++ restatement of the reference algorithm, OpenMP)"}
+    serving = None
+    if not args.no_serve and ws == 1:
+        try:
+            serving = run_serve(args, local)
+        except Exception as e:  # the headline line must still print
+            serving = {"error": str(e)}
     cfg.update({"method": args.method, "l2": "flushed (256 MiB write) before every timed step",
                 "vertices_per_step": Vs, "levels": st0["levels"], "parallelism": f"replicas x{ws}"})
     breakdown = {k: statistics.mean(s[k] for s in stats) for k in
@@ -298,12 +359,17 @@ def run_ours(args):
             "gpu_launches": int(sum(s["launches"] for s in stats)),
             "stats": {k: st0[k] for k in ("rays", "fallback_rays", "uncertified", "insecure", "dd_rescores",
                                           "degenerate", "descents", "levels")},
-            "breakdown_ms": breakdown}
+            "breakdown_ms": breakdown, "serving": serving}
     print(json.dumps(line), flush=True)
 
 
 def main():
     args = parse()
+    if args.serve:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"serving": run_serve(args, 0)}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -13,7 +13,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libhvgpu.so")
-SOURCES = ["hv_prep.cu", "hv_search.cu", "hv_post.cu", "hv_integrate.cu", "hv_api.cu"]
+SOURCES = ["hv_prep.cu", "hv_search.cu", "hv_post.cu", "hv_integrate.cu", "hv_api.cu", "hv_server.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
 
@@ -42,7 +42,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     nvcc = _nvcc()
     jobs = []
     for s in srcs:
-        obj = os.path.join(OUT, s.replace(".cu", ".o"))
+        obj = os.path.join(OUT, os.path.splitext(s)[0] + ".o")
         if force or _stale(obj, [os.path.join(CSRC, s)] + hdrs):
             cmd = [nvcc, *FLAGS, *ARCH, *extra_flags, "-c", os.path.join(CSRC, s), "-o", obj]
             jobs.append((s, cmd))
@@ -58,9 +58,9 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
                 sys.stderr.write(r.stderr)
             if r.returncode != 0:
                 raise RuntimeError(f"nvcc failed for {name}:\n{r.stderr}")
-    objs = [os.path.join(OUT, s.replace(".cu", ".o")) for s in srcs]
+    objs = [os.path.join(OUT, os.path.splitext(s)[0] + ".o") for s in srcs]
     if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc, "-shared", *ARCH, "-o", LIB, *objs]
+        cmd = [nvcc, "-shared", *ARCH, "-o", LIB, *objs, "-Xcompiler", "-pthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")

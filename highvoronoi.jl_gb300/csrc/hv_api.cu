@@ -109,7 +109,7 @@ unsigned next_pow2(unsigned long long x) {
 }
 
 int default_knn(int d) {
-    static const int k[7] = {0, 0, 24, 48, 96, 192, 384};
+    static const int k[7] = {0, 0, 32, 96, 256, 384, 480};
     return k[d];
 }
 
@@ -222,7 +222,8 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     }
     double* pts = prep.get<double>((size_t)n * d);
     float* pts32 = prep.get<float>((size_t)n * DP);
-    kt.run(F_OTHER, 1, [&] { launch_gather(d, mesh->d_in, perm, n, pts, pts32, st); });
+    float* pts32lo = prep.get<float>((size_t)n * DP);
+    kt.run(F_OTHER, 1, [&] { launch_gather(d, mesh->d_in, perm, n, pts, pts32, pts32lo, st); });
     // ---- tree
     DevMesh M;
     std::memset(&M, 0, sizeof(M));
@@ -236,7 +237,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     M.leaf = mesh->prm.leaf_size > 0 ? mesh->prm.leaf_size : 16;
     M.nleaves = (n + M.leaf - 1) / M.leaf;
     M.P = (int)next_pow2((unsigned long long)M.nleaves);
-    M.pts = pts; M.pts32 = pts32; M.perm = perm;
+    M.pts = pts; M.pts32 = pts32; M.pts32lo = pts32lo; M.perm = perm;
     float* blo = prep.get<float>((size_t)2 * M.P * DP);
     float* bhi = prep.get<float>((size_t)2 * M.P * DP);
     unsigned* flags = prep.get<unsigned>((size_t)2 * M.P);
@@ -279,13 +280,26 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         M.vsig = srch->get<int>((size_t)vcap * (d + 1));
         M.vc = srch->get<double>((size_t)vcap * d);
         M.vrho32 = srch->get<float>((size_t)vcap * DP);
+        M.vinv32 = fast ? srch->get<float>((size_t)vcap * d * d) : nullptr;
+        M.vcond = fast ? srch->get<float>(vcap) : nullptr;
         M.vnew = srch->get<int>(vcap);
         const unsigned hsize = next_pow2(2ull * vcap);
         M.vhmask = hsize - 1;
         M.vhash = srch->get<unsigned long long>(hsize);
         CK(cudaMemsetAsync(M.vhash, 0, sizeof(unsigned long long) * hsize, st));
+        const bool dedup = mesh->prm.edge_dedup >= 0;
+        M.ecnt = nullptr; M.ehash = nullptr; M.ehmask = 0;
+        if (dedup) {
+            M.ecnt = srch->get<unsigned>(vcap);
+            CK(cudaMemsetAsync(M.ecnt, 0, sizeof(unsigned) * vcap, st));
+            const unsigned esize = next_pow2((unsigned long long)vcap * (d + 1));
+            M.ehmask = esize - 1;
+            M.ehash = srch->get<unsigned long long>(esize);
+            CK(cudaMemsetAsync(M.ehash, 0, sizeof(unsigned long long) * esize, st));
+        }
         const unsigned fqcap = std::max(65536u, vcap / 2);
-        unsigned long long* fq = fast ? srch->get<unsigned long long>(fqcap) : nullptr;
+        unsigned long long* fq = fast ? srch->get<unsigned long long>(fqcap) : nullptr;  // insecure rays
+        unsigned long long* fx = fast ? srch->get<unsigned long long>(fqcap) : nullptr;  // uncertified rays
         M.vcount = dstat;
         CK(cudaMemsetAsync(dstat, 0, 4 * sizeof(unsigned), st));
         CK(cudaMemsetAsync(dcnt, 0, C_NCOUNT * sizeof(unsigned long long), st));
@@ -299,11 +313,17 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         if (!overflow) kt.run(F_CENTERS, 1, [&] { launch_centers(M, 0, f1, ctx->nsm, st); });
         long long levels = 0;
         while (!overflow && f1 > f0) {
+            if (dedup) kt.run(F_OTHER, 1, [&] { launch_register_edges(M, f0, f1, ctx->nsm, st); });
             if (fast) {
-                CK(cudaMemsetAsync(dstat + 2, 0, sizeof(unsigned), st));
-                kt.run(F_EXPAND, 1, [&] { launch_expand_fast(M, f0, f1, fq, dstat + 2, fqcap, ctx->nsm, st); });
+                CK(cudaMemsetAsync(dstat + 2, 0, 2 * sizeof(unsigned), st));
+                kt.run(F_EXPAND, 1, [&] {
+                    launch_expand_fast(M, f0, f1, fq, dstat + 2, fqcap, fx, dstat + 3, fqcap, ctx->nsm, st);
+                });
                 const unsigned long long maxq = std::min<unsigned long long>(fqcap, (unsigned long long)(f1 - f0) * (d + 1));
-                kt.run(F_FALLBACK, 1, [&] { launch_fallback(M, fq, dstat + 2, (unsigned)maxq, ctx->nsm, st); });
+                kt.run(F_FALLBACK, 2, [&] {
+                    launch_fallback_warp(M, fq, dstat + 2, fqcap, (unsigned)maxq, fx, dstat + 3, fqcap, ctx->nsm, st);
+                    launch_fallback(M, fx, dstat + 3, (unsigned)maxq, ctx->nsm, st);
+                });
             } else {
                 kt.run(F_EXPAND, 1, [&] { launch_expand_plain(M, f0, f1, ctx->nsm, st); });
             }
@@ -622,29 +642,55 @@ int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) {
         Scratch s(st);
         double* dvol = s.get<double>(n);
         double* darea = s.get<double>((size_t)std::max(m->nnbr, 1ll));
-        unsigned* dstat = s.get<unsigned>(1);
+        unsigned* dstat = s.get<unsigned>(2);  // status, number of big cells
+        int* big = s.get<int>(n);
         hv::IntegrateInput in{d, n, m->lo, m->hi, m->d_in, m->osig, m->oc, m->inc_off, m->inc, m->nbr_off, m->nbr, dstat};
-        const int capC = (int)next_pow2((unsigned long long)maxc);
-        int capV = (int)std::min<long long>(capC, std::max(64, capC / 4));
+        auto caps_for = [&](int capC, int capV) {
+            hv::PolyCaps c;
+            c.capC = capC; c.capV = capV; c.capF = 2 * capV;
+            c.capE = (int)next_pow2((unsigned long long)capV * (d - 1) / 2 + 2);
+            return c;
+        };
+        // shared-memory pass: the largest power-of-two cell size that fits
+        int capC = (int)std::min<unsigned long long>(next_pow2((unsigned long long)maxc), 1024ull);
+        int capV = std::min(capC, std::max(64, capC / 4));
+        while (capC > 16 && (long long)hv::poly_smem_bytes(d, capC, capV, 2 * capV, caps_for(capC, capV).capE) > smax) {
+            capC /= 2;
+            capV = std::min(capC, std::max(64, capC / 4));
+        }
+        const int capCg = (int)next_pow2((unsigned long long)maxc);
+        int capVg = capCg;
         for (int attempt = 0;; ++attempt) {
-            const int capF = 2 * capV;
-            const int capE = (int)next_pow2((unsigned long long)capV * (d - 1) / 2 + 2);
-            const size_t sm = hv::poly_smem_bytes(d, capC, capV, capF, capE);
-            if ((long long)sm > smax) throw HvError(HV_E_CAPACITY, "cell too large for the polygon integrator (" +
-                                                      std::to_string(maxc) + " vertices)");
-            CK(cudaMemsetAsync(dstat, 0, sizeof(unsigned), st));
+            hv::PolyCaps cs = caps_for(capC, capV), cg = caps_for(capCg, capVg);
+            CK(cudaMemsetAsync(dstat, 0, 2 * sizeof(unsigned), st));
             CK(cudaMemsetAsync(darea, 0, sizeof(double) * std::max(m->nnbr, 1ll), st));
-            if (hv::launch_polygon(in, capC, capV, capF, capE, darea, dvol, m->ctx->nsm, st) != 0)
+            if (hv::launch_polygon(in, cs, cg, big, dstat + 1, 0, nullptr, 0, darea, dvol, 0, m->ctx->nsm, st) != 0)
                 throw HvError(HV_E_CUDA, "polygon integrator launch failed");
             CK(cudaGetLastError());
-            unsigned hs = 0;
-            CK(cudaMemcpyAsync(&hs, dstat, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+            unsigned hs[2] = {0, 0};
+            CK(cudaMemcpyAsync(hs, dstat, sizeof(hs), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
-            if (hs == 0) break;
-            if ((hs & 1u) || capV >= capC || attempt > 6)
+            if (hs[1] > 0 && !(hs[0] & 2u)) {
+                const size_t bytes = (hv::poly_smem_bytes(d, cg.capC, cg.capV, cg.capF, cg.capE) + 255) / 256 * 256;
+                const int gblocks = (int)std::min<unsigned>(hs[1], (unsigned)(2 * m->ctx->nsm));
+                Scratch gs(st);
+                unsigned char* gbase = gs.get<unsigned char>(bytes * gblocks);
+                hv::launch_polygon(in, cs, cg, big, dstat + 1, hs[1], gbase, gblocks, darea, dvol, 1, m->ctx->nsm, st);
+                CK(cudaGetLastError());
+                CK(cudaMemcpyAsync(hs, dstat, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+            }
+            if (hs[0] == 0) break;
+            if ((hs[0] & 1u) || attempt > 6)
                 throw HvError(HV_E_CAPACITY, "facet structure beyond the polygon integrator's capacity");
-            capV = std::min(capC, capV * 2);
+            capV = std::min(capC, capV * 2);   // facet over capacity: widen and redo
+            capVg = std::min(capCg, capVg * 2);
+            if (capV == capC && capVg == capCg && attempt > 2)
+                throw HvError(HV_E_CAPACITY, "facet structure beyond the polygon integrator's capacity");
         }
+        hv::launch_polygon(in, caps_for(capC, capV), caps_for(capCg, capVg), big, dstat + 1, 0, nullptr, 0, darea,
+                           dvol, 2, m->ctx->nsm, st);
+        CK(cudaGetLastError());
         CK(cudaMemcpyAsync(vol, dvol, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
         if (m->nnbr > 0) CK(cudaMemcpyAsync(area, darea, sizeof(double) * m->nnbr, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));

@@ -9,7 +9,8 @@ struct DevMesh;
 // hv_prep.cu
 void launch_morton(int d, const double* in, int n, const double* lo, const double* hi,
                    unsigned long long* codes, int* idx, unsigned* status, cudaStream_t st);
-void launch_gather(int d, const double* in, const int* perm, int n, double* pts, float* pts32, cudaStream_t st);
+void launch_gather(int d, const double* in, const int* perm, int n, double* pts, float* pts32, float* pts32lo,
+                   cudaStream_t st);
 void launch_bvh(const DevMesh& M, float* blo, float* bhi, unsigned* flags, cudaStream_t st);
 void launch_knn(const DevMesh& M, int* knn, float* sec, cudaStream_t st);
 size_t sort_pairs_u64_i32_temp(int n);
@@ -27,9 +28,14 @@ void exclusive_scan_i64(void* temp, size_t temp_bytes, const long long* in, long
 // hv_search.cu
 void launch_descent(const DevMesh& M, int stride, int nseeds, unsigned long long seed, cudaStream_t st);
 void launch_centers(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+void launch_register_edges(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
 void launch_expand_plain(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cudaStream_t st);
 void launch_expand_fast(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq,
-                        unsigned fqcap, int nsm, cudaStream_t st);
+                        unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm,
+                        cudaStream_t st);
+void launch_fallback_warp(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap,
+                          unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm,
+                          cudaStream_t st);
 void launch_fallback(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm,
                      cudaStream_t st);
 

@@ -114,11 +114,16 @@ __device__ __forceinline__ void lehmer(int w, int m, int* ord) {
     }
 }
 
-template <int D>
-__global__ void __launch_bounds__(128) k_poly_cells(PolyArgs A) {
+// GLOBAL = false: work area in shared memory, all cells; cells with more than
+// capC vertices are appended to `big` for the GLOBAL = true pass, whose work
+// area is a per-block slab of global memory sized for the largest cell.
+template <int D, bool GLOBAL>
+__global__ void __launch_bounds__(128) k_poly_cells(PolyArgs A, const int* cells, int ncells, unsigned char* gbase,
+                                                    size_t area_bytes, int* big, unsigned* nbig) {
     extern __shared__ __align__(16) unsigned char smem[];
+    unsigned char* base = GLOBAL ? gbase + (size_t)blockIdx.x * area_bytes : smem;
     const int capC = A.capC, capV = A.capV, capF = A.capF, capE = A.capE;
-    double* cx = (double*)smem;                       // capC x D   cell vertex coords - x_i
+    double* cx = (double*)base;                       // capC x D   cell vertex coords - x_i
     double* fcen = cx + (size_t)capC * D;             // capF x D   face centroids
     double* cF = fcen + (size_t)capF * D;             // D          facet centroid
     double* red = cF + D;                             // blockDim
@@ -136,14 +141,19 @@ __global__ void __launch_bounds__(128) k_poly_cells(PolyArgs A) {
     double fact = 1.0;
     for (int q = 2; q <= D; ++q) fact *= q;
 
-    for (int i = blockIdx.x; i < A.n; i += gridDim.x) {
+    const int nwork = GLOBAL ? ncells : A.n;
+    for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
+        const int i = GLOBAL ? cells[wi] : wi;
         double xi[D];
 #pragma unroll
         for (int c = 0; c < D; ++c) xi[c] = A.pts[(size_t)i * D + c];
         const long long vb = A.inc_off[i], ve = A.inc_off[i + 1];
         const int nc = (int)(ve - vb);
         if (nc > capC) {
-            if (threadIdx.x == 0) atomicOr(A.status, 1u);
+            if (threadIdx.x == 0) {
+                if (GLOBAL) atomicOr(A.status, 1u);
+                else big[atomicAdd(nbig, 1u)] = i;
+            }
             continue;
         }
         // ---- stage the cell's vertices
@@ -603,26 +613,37 @@ size_t poly_smem_bytes(int d, int capC, int capV, int capF, int capE) {
 }
 
 template <int D>
-static int poly_t(const IntegrateInput& in, int capC, int capV, int capF, int capE, double* area, double* vol,
+static int poly_t(const IntegrateInput& in, const PolyCaps& cs, const PolyCaps& cg, int* big, unsigned* nbig,
+                  unsigned nbig_host, unsigned char* gbase, int gblocks, double* area, double* vol, int pass,
                   int nsm, cudaStream_t st) {
     PolyArgs A = make_args(in);
     A.area = area;
-    A.capC = capC; A.capV = capV; A.capF = capF; A.capE = capE;
-    const size_t sm = poly_smem_bytes(D, capC, capV, capF, capE);
-    if (cudaFuncSetAttribute(k_poly_cells<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
-        return -1;
-    int blocks = nsm * 4;
-    if (blocks > in.n) blocks = in.n;
-    if (blocks < 1) blocks = 1;
-    k_poly_cells<D><<<blocks, 128, sm, st>>>(A);
-    k_poly_volumes<D><<<(in.n + 255) / 256, 256, 0, st>>>(A, vol);
+    if (pass == 0) {
+        A.capC = cs.capC; A.capV = cs.capV; A.capF = cs.capF; A.capE = cs.capE;
+        const size_t sm = poly_smem_bytes(D, cs.capC, cs.capV, cs.capF, cs.capE);
+        if (cudaFuncSetAttribute(k_poly_cells<D, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+            cudaSuccess)
+            return -1;
+        int blocks = nsm * 4;
+        if (blocks > in.n) blocks = in.n;
+        if (blocks < 1) blocks = 1;
+        k_poly_cells<D, false><<<blocks, 128, sm, st>>>(A, nullptr, 0, nullptr, 0, big, nbig);
+    } else if (pass == 1) {
+        A.capC = cg.capC; A.capV = cg.capV; A.capF = cg.capF; A.capE = cg.capE;
+        const size_t bytes = poly_smem_bytes(D, cg.capC, cg.capV, cg.capF, cg.capE);
+        k_poly_cells<D, true><<<gblocks, 128, 0, st>>>(A, big, (int)nbig_host, gbase, (bytes + 255) / 256 * 256,
+                                                        nullptr, nullptr);
+    } else {
+        k_poly_volumes<D><<<(in.n + 255) / 256, 256, 0, st>>>(A, vol);
+    }
     return 0;
 }
 
-int launch_polygon(const IntegrateInput& in, int capC, int capV, int capF, int capE, double* area, double* vol,
+int launch_polygon(const IntegrateInput& in, const PolyCaps& cs, const PolyCaps& cg, int* big, unsigned* nbig,
+                   unsigned nbig_host, unsigned char* gbase, int gblocks, double* area, double* vol, int pass,
                    int nsm, cudaStream_t st) {
     int rc = -1;
-    HV_DISPATCH(in.d, (rc = poly_t<DD>(in, capC, capV, capF, capE, area, vol, nsm, st)));
+    HV_DISPATCH(in.d, (rc = poly_t<DD>(in, cs, cg, big, nbig, nbig_host, gbase, gblocks, area, vol, pass, nsm, st)));
     return rc;
 }
 

@@ -19,8 +19,15 @@ struct IntegrateInput {
     unsigned* status;         // 1: cell over capacity, 2: facet over capacity, 4: degree over capacity
 };
 
+struct PolyCaps {
+    int capC, capV, capF, capE;  // cell vertices, facet vertices, faces, edges (powers of two)
+};
+
 size_t poly_smem_bytes(int d, int capC, int capV, int capF, int capE);
-int launch_polygon(const IntegrateInput& in, int capC, int capV, int capF, int capE, double* area, double* vol,
+// pass 0: shared-memory kernel over all cells (big cells appended to `big`),
+// pass 1: global-memory kernel over the big cells, pass 2: volumes.
+int launch_polygon(const IntegrateInput& in, const PolyCaps& cs, const PolyCaps& cg, int* big, unsigned* nbig,
+                   unsigned nbig_host, unsigned char* gbase, int gblocks, double* area, double* vol, int pass,
                    int nsm, cudaStream_t st);
 int launch_heuristic_mc(const IntegrateInput& in, int ndir, unsigned long long seed, int capN, double cvol,
                         double* rawV, double* rawA, double* varV, double* outA, double* vol, int nsm,

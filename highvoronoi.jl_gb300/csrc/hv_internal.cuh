@@ -4,6 +4,7 @@
 // Data layout in HBM (one mesh):
 //   pts      n x d doubles, points in Morton order ("internal" ids)
 //   pts32    n x DP floats (DP = 4 for d <= 4, 8 otherwise), same order
+//   pts32lo  n x DP floats: x - (float)x (double-float coordinates)
 //   perm     internal id -> original 0-based id
 //   blo/bhi  (2P) x DP floats: boxes of an implicit complete binary tree over
 //            leaves of `leaf` consecutive points (node 1 = root, leaves P..2P-1),
@@ -14,6 +15,8 @@
 //            are boundary planes n+p (p = 2k upper face, 2k+1 lower face)
 //   vc       vcap x d doubles: FP64 circumcentre
 //   vrho32   vcap x DP floats: rounded FP64 (centre - x_anchor), anchor = sig[0]
+//   vinv32   vcap x d x d floats: rounded FP64 inverse of the vertex's constraint
+//            matrix (columns give every ray direction of the vertex)
 //   vnew     vcap ints: generator added by the ray that found the vertex
 //   vhash    open-addressing table of 64-bit entries (fingerprint << 32 | id)
 #pragma once
@@ -64,6 +67,7 @@ struct DevMesh {
     double xscale;  // bound on |coordinate|
     const double* pts;
     const float* pts32;
+    const float* pts32lo;  // residual x - (float)x, so that x = hi + lo to ~2^-48
     const int* perm;
     const float* blo;
     const float* bhi;
@@ -72,6 +76,8 @@ struct DevMesh {
     int* vsig;
     double* vc;
     float* vrho32;  // vcap x DP: FP32 (centre - anchor)
+    float* vinv32;  // vcap x D x D: rounded FP64 inverse of the constraint matrix (row-major)
+    float* vcond;   // vcap: condition estimate |M| |M^-1|
     int* vnew;
     unsigned* vcount;
     unsigned long long* vhash;

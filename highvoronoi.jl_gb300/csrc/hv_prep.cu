@@ -48,22 +48,27 @@ __global__ void k_morton(const double* __restrict__ in, int n, DevBox box, unsig
 
 template <int D>
 __global__ void k_gather(const double* __restrict__ in, const int* __restrict__ perm, int n, double* pts,
-                         float* pts32) {
+                         float* pts32, float* pts32lo) {
     constexpr int DP = (D <= 4) ? 4 : 8;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
         const int o = perm[s];
-        float f[DP];
+        float f[DP], g[DP];
 #pragma unroll
-        for (int k = 0; k < DP; ++k) f[k] = 0.f;
+        for (int k = 0; k < DP; ++k) { f[k] = 0.f; g[k] = 0.f; }
 #pragma unroll
         for (int k = 0; k < D; ++k) {
             const double x = in[(size_t)o * D + k];
             pts[(size_t)s * D + k] = x;
             f[k] = (float)x;
+            g[k] = (float)(x - (double)f[k]);
         }
         float4* dst = reinterpret_cast<float4*>(pts32 + (size_t)s * DP);
+        float4* dlo = reinterpret_cast<float4*>(pts32lo + (size_t)s * DP);
 #pragma unroll
-        for (int h = 0; h < DP / 4; ++h) dst[h] = make_float4(f[4 * h], f[4 * h + 1], f[4 * h + 2], f[4 * h + 3]);
+        for (int h = 0; h < DP / 4; ++h) {
+            dst[h] = make_float4(f[4 * h], f[4 * h + 1], f[4 * h + 2], f[4 * h + 3]);
+            dlo[h] = make_float4(g[4 * h], g[4 * h + 1], g[4 * h + 2], g[4 * h + 3]);
+        }
     }
 }
 
@@ -278,10 +283,11 @@ void launch_morton(int d, const double* in, int n, const double* lo, const doubl
     HV_DISPATCH(d, (k_morton<DD><<<blocks, 256, 0, st>>>(in, n, box, codes, idx, status)));
 }
 
-void launch_gather(int d, const double* in, const int* perm, int n, double* pts, float* pts32, cudaStream_t st) {
+void launch_gather(int d, const double* in, const int* perm, int n, double* pts, float* pts32, float* pts32lo,
+                   cudaStream_t st) {
     if (n <= 0) return;
     const int blocks = (n + 255) / 256;
-    HV_DISPATCH(d, (k_gather<DD><<<blocks, 256, 0, st>>>(in, perm, n, pts, pts32)));
+    HV_DISPATCH(d, (k_gather<DD><<<blocks, 256, 0, st>>>(in, perm, n, pts, pts32, pts32lo)));
 }
 
 void launch_bvh(const DevMesh& M, float* blo, float* bhi, unsigned* flags, cudaStream_t st) {

@@ -121,6 +121,9 @@ struct Query {
 };
 
 __device__ __forceinline__ void consider(SearchOut& R, const Cand& c) {
+    // a candidate may be met twice (seed set and tree): keep one copy
+    if (c.item == R.best.item) return;
+    for (int k = 0; k < R.namb; ++k) if (R.amb[k].item == c.item) return;
     if (c.lo < R.best.lo) {
         if (R.best.item >= 0) {
             R.second_lo = R.best.lo;
@@ -232,6 +235,18 @@ __device__ void exact_search(const DevMesh& M, const Query<D>& q, SearchOut& R) 
     R.namb = 0;
     R.overflow = false;
     eval_planes<D>(M, q, R);
+    // start from the anchor's neighbourhood so that the ball is small before
+    // the tree is entered: its leaf, then the head of its candidate list
+    {
+        const int la = q.a / M.leaf;
+        const int s0 = la * M.leaf, s1 = min(s0 + M.leaf, M.n);
+        for (int j = s0; j < s1; ++j) if (!q_excluded<D>(q, j)) eval_point<D>(M, q, j, R);
+        const int kh = min(M.K, 32);
+        for (int c = 0; c < kh; ++c) {
+            const int j = __ldg(M.knn + (size_t)q.a * M.K + c);
+            if (j >= 0 && !q_excluded<D>(q, j)) eval_point<D>(M, q, j, R);
+        }
+    }
     int stack[64];
     int sp = 0;
     stack[sp++] = 1;
@@ -553,6 +568,7 @@ __global__ void __launch_bounds__(128) k_expand_plain(DevMesh M, unsigned f0, un
 #pragma unroll
         for (int k = 0; k <= D; ++k) sig[k] = M.vsig[(size_t)v * (D + 1) + k];
         if (!walkable<D>(M, sig, M.vnew[v], m)) continue;
+        if (M.ecnt && ((__ldg(M.ecnt + v) >> m) & 1u)) continue;  // both end points known
         count_add(M.cnt + C_RAYS);
         exact_walk<D>(M, v, m);
     }
@@ -728,6 +744,62 @@ __global__ void __launch_bounds__(128) k_descent(DevMesh M, int stride, int nsee
 }
 
 // ---------------------------------------------------------------------------
+// edge registry (src/edgehashing.jl:49-111): an edge is the sorted d-tuple
+// sig \ {sig[m]}; the table entry references (vertex, slot) so the key is read
+// back from the vertex record.  The second end point to register an edge
+// closes it for both: neither walks it (both end points are known).
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(256) k_register_edges(DevMesh M, unsigned v0, unsigned v1) {
+    const unsigned long long total = (unsigned long long)(v1 - v0) * (D + 1);
+    for (unsigned long long r = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; r < total;
+         r += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned v = v0 + (unsigned)(r / (D + 1));
+        const int m = (int)(r % (D + 1));
+        int sig[D + 1];
+#pragma unroll
+        for (int k = 0; k <= D; ++k) sig[k] = M.vsig[(size_t)v * (D + 1) + k];
+        if (m == 0 && sig[1] >= M.n) continue;  // the edge holds only planes
+        int e[D];
+        int o = 0;
+#pragma unroll
+        for (int k = 0; k <= D; ++k) if (k != m) e[o++] = sig[k];
+        const unsigned long long h = hash_items(e, D);
+        const unsigned fp = ((unsigned)(h >> 32) & 0x7FFFFFFFu) | 1u;
+        const unsigned long long mine = ((unsigned long long)fp << 32) | ((unsigned long long)v * 8u + (unsigned)m);
+        unsigned long long slot = h & M.ehmask;
+        bool done = false;
+        for (unsigned long long probe = 0; probe <= M.ehmask && !done; ++probe) {
+            const unsigned long long prev = atomicCAS(&M.ehash[slot], HASH_EMPTY, mine);
+            if (prev == HASH_EMPTY) { done = true; break; }
+            if ((unsigned)(prev >> 32) == fp) {
+                const unsigned ref = (unsigned)prev;
+                const unsigned ov = ref >> 3, om = ref & 7u;
+                int q = 0;
+                bool eq = true;
+#pragma unroll
+                for (int k = 0; k <= D; ++k) {
+                    if (k == (int)om) continue;
+                    const int x = M.vsig[(size_t)ov * (D + 1) + k];
+#pragma unroll
+                    for (int z = 0; z < D; ++z) if (z == q) eq &= (x == e[z]);
+                    ++q;
+                }
+                if (eq) {
+                    atomicOr(M.ecnt + ov, 1u << om);
+                    atomicOr(M.ecnt + v, 1u << m);
+                    count_add(M.cnt + C_EDGECLOSED);
+                    done = true;
+                    break;
+                }
+            }
+            slot = (slot + 1) & M.ehmask;
+        }
+        if (!done) set_status(M, ST_ECAP);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // FP64 circumcentres of new vertices, one thread per vertex (full-warp FP64)
 // ---------------------------------------------------------------------------
 template <int D>
@@ -737,24 +809,62 @@ __global__ void __launch_bounds__(128) k_centers(DevMesh M, unsigned v0, unsigne
         int s[D + 1];
 #pragma unroll
         for (int k = 0; k <= D; ++k) s[k] = M.vsig[(size_t)v * (D + 1) + k];
-        double c[D];
+        double xa[D], A[D][D], rho[D];
         const double* pa = M.pts + (size_t)s[0] * D;
-        if (!vertex_center<D>(M, s, c)) {
+#pragma unroll
+        for (int k = 0; k < D; ++k) xa[k] = __ldg(pa + k);
+#pragma unroll
+        for (int r = 0; r < D; ++r) con_row<D, double>(M, xa, s[r + 1], A[r], rho[r]);
+        double nrm = 0;
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+            double sr = 0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) sr += fabs(A[r][k]);
+            nrm = fmax(nrm, sr);
+        }
+        int piv[D];
+        const bool ok = lu_factor<D, double>(A, piv);
+        if (!ok) {
             set_status(M, ST_NUMERIC);
 #pragma unroll
-            for (int k = 0; k < D; ++k) c[k] = __ldg(pa + k);
+            for (int k = 0; k < D; ++k) rho[k] = 0.0;
+        } else {
+            lu_solve<D, double>(A, piv, rho);
         }
         float r32[DP];
 #pragma unroll
         for (int k = 0; k < DP; ++k) r32[k] = 0.f;
 #pragma unroll
         for (int k = 0; k < D; ++k) {
-            M.vc[(size_t)v * D + k] = c[k];
-            r32[k] = (float)(c[k] - __ldg(pa + k));
+            M.vc[(size_t)v * D + k] = xa[k] + rho[k];
+            r32[k] = (float)rho[k];
         }
         float4* dst = reinterpret_cast<float4*>(M.vrho32 + (size_t)v * DP);
 #pragma unroll
         for (int h = 0; h < DP / 4; ++h) dst[h] = make_float4(r32[4 * h], r32[4 * h + 1], r32[4 * h + 2], r32[4 * h + 3]);
+        if (M.vinv32) {
+            // FP64 inverse, rounded once to FP32: every ray direction of the vertex
+            double rows[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) rows[k] = 0.0;
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                double col[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) col[k] = (k == c) ? 1.0 : 0.0;
+                if (ok) lu_solve<D, double>(A, piv, col);
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    M.vinv32[(size_t)v * D * D + k * D + c] = (float)col[k];
+                    rows[k] += fabs(col[k]);
+                }
+            }
+            double ninv = 0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) ninv = fmax(ninv, rows[k]);
+            M.vcond[v] = ok ? (float)(nrm * ninv) : INFINITY;
+        }
     }
 }
 
@@ -775,9 +885,21 @@ __device__ __forceinline__ void load_pt32(const DevMesh& M, int j, float (&x)[(D
 }
 
 template <int D>
+__device__ __forceinline__ void load_pt32lo(const DevMesh& M, int j, float (&x)[(D <= 4) ? 4 : 8]) {
+    constexpr int DP = (D <= 4) ? 4 : 8;
+    const float4* p = reinterpret_cast<const float4*>(M.pts32lo + (size_t)j * DP);
+#pragma unroll
+    for (int h = 0; h < DP / 4; ++h) {
+        float4 f = __ldg(p + h);
+        x[4 * h] = f.x; x[4 * h + 1] = f.y; x[4 * h + 2] = f.z; x[4 * h + 3] = f.w;
+    }
+}
+
+template <int D>
 __global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsigned f0, unsigned f1,
                                                                unsigned long long* fq, unsigned* nfq,
-                                                               unsigned fqcap) {
+                                                               unsigned fqcap, unsigned long long* fx,
+                                                               unsigned* nfx, unsigned fxcap) {
     constexpr int R = D + 1;
     constexpr int DP = (D <= 4) ? 4 : 8;
     __shared__ float sInv[FAST_WPB][D][D];
@@ -789,7 +911,6 @@ __global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsign
     const unsigned FULL = 0xFFFFFFFFu;
     const unsigned nf = f1 - f0;
     const float S32 = 5.9604645e-08f;                          // 2^-24
-    const float EX = (float)(2.0 * M.xscale * 5.9604645e-08);  // rounding of a coordinate difference
     for (unsigned w = blockIdx.x * FAST_WPB + wib; w < nf; w += gridDim.x * FAST_WPB) {
         const unsigned v = f0 + w;
         int sig[R];
@@ -797,8 +918,9 @@ __global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsign
         for (int k = 0; k < R; ++k) sig[k] = M.vsig[(size_t)v * R + k];
         const int vnew = M.vnew[v];
         const int a = sig[0];
-        float xa[DP], rho[DP];
+        float xa[DP], xal[DP], rho[DP];
         load_pt32<D>(M, a, xa);
+        load_pt32lo<D>(M, a, xal);
         {
             const float4* pr = reinterpret_cast<const float4*>(M.vrho32 + (size_t)v * DP);
 #pragma unroll
@@ -807,62 +929,16 @@ __global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsign
                 rho[4 * h] = f.x; rho[4 * h + 1] = f.y; rho[4 * h + 2] = f.z; rho[4 * h + 3] = f.w;
             }
         }
-        // ---- FP32 constraint system; lanes 0..D-1 each produce one column of the inverse
-        float A[D][D];
-        float nrm = 0.f;
-#pragma unroll
-        for (int r = 0; r < D; ++r) {
-            const int it = sig[r + 1];
-            if (it < M.n) {
-                float xg[DP];
-                load_pt32<D>(M, it, xg);
-#pragma unroll
-                for (int k = 0; k < D; ++k) A[r][k] = xg[k] - xa[k];
-            } else {
-                const int p = it - M.n;
-#pragma unroll
-                for (int k = 0; k < D; ++k) A[r][k] = (k == (p >> 1)) ? (((p & 1) == 0) ? 1.f : -1.f) : 0.f;
-            }
-            float s = 0.f;
-#pragma unroll
-            for (int k = 0; k < D; ++k) s += fabsf(A[r][k]);
-            nrm = fmaxf(nrm, s);
-        }
-        int okv = 1;
-        if (lane < D) {
-            int piv[D];
-            okv = lu_factor<D, float>(A, piv) ? 1 : 0;
-            if (okv) {
-                float col[D];
-#pragma unroll
-                for (int k = 0; k < D; ++k) col[k] = (k == lane) ? 1.f : 0.f;
-                lu_solve<D, float>(A, piv, col);
-#pragma unroll
-                for (int k = 0; k < D; ++k) sInv[wib][k][lane] = col[k];
-            }
-        }
-        okv = __shfl_sync(FULL, okv, 0);
+        // ---- the vertex's inverse (FP64 solve rounded to FP32, written by k_centers)
+        for (int x = lane; x < D * D; x += 32) (&sInv[wib][0][0])[x] = M.vinv32[(size_t)v * D * D + x];
+        if (lane == 0) sCond[wib] = M.vcond[v];
         __syncwarp();
-        if (!okv) {
-            if (lane == 0) set_status(M, ST_NUMERIC);
-            continue;
-        }
-        if (lane == 0) {
-            float ninv = 0.f;
-#pragma unroll
-            for (int r = 0; r < D; ++r) {
-                float s = 0.f;
-#pragma unroll
-                for (int k = 0; k < D; ++k) s += fabsf(sInv[wib][r][k]);
-                ninv = fmaxf(ninv, s);
-            }
-            sCond[wib] = nrm * ninv;
-        }
         // ---- ray directions (lane m < R)
         int active = 0;
         if (lane < R) {
             const int m = lane;
             active = walkable<D>(M, sig, vnew, m) ? 1 : 0;
+            if (active && M.ecnt && ((M.ecnt[v] >> m) & 1u)) active = 0;  // both end points known
             if (active) {
                 float u[D], db[D];
 #pragma unroll
@@ -880,10 +956,11 @@ __global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsign
                             if (b < 0) b = sig[c + 1];
                         }
                     }
-                    float xb[DP];
+                    float xb[DP], xbl[DP];
                     load_pt32<D>(M, b, xb);
+                    load_pt32lo<D>(M, b, xbl);
 #pragma unroll
-                    for (int k = 0; k < D; ++k) db[k] = xb[k] - xa[k];
+                    for (int k = 0; k < D; ++k) db[k] = (xb[k] - xa[k]) + (xbl[k] - xal[k]);
                 }
                 float nu = 0.f;
 #pragma unroll
@@ -898,14 +975,16 @@ __global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsign
         }
         const unsigned rmask = __ballot_sync(FULL, active) & ((1u << R) - 1u);
         __syncwarp();
-        // relative error of the FP32 directions: conditioning x (input rounding + LU rounding)
         const float cond = sCond[wib];
-        const float relu = 4.f * cond * (D * EX / fmaxf(nrm, 1e-30f) + (D + 2) * S32) + 2.f * S32;
-        if (!(relu < 1e-3f)) {  // too ill-conditioned for an FP32 decision: all rays exact
+        // directions come from the FP64 inverse rounded to FP32: relative error
+        // (2D+6) 2^-24 from the rounding and normalisation, plus the FP64
+        // solve's own error ~ D cond 2^-53
+        const float relu = (2.f * D + 6.f) * S32 + 8.f * D * cond * 1.1102230e-16f;
+        if (!(cond < 1e7f)) {  // too ill-conditioned for an FP32 decision: all rays exact
             if (lane < R && active) {
                 count_add(M.cnt + C_RAYS);
-                const unsigned slot = atomicAdd(nfq, 1u);
-                if (slot < fqcap) fq[slot] = ((unsigned long long)v << 3) | (unsigned)lane;
+                const unsigned slot = atomicAdd(nfx, 1u);
+                if (slot < fxcap) fx[slot] = ((unsigned long long)v << 3) | (unsigned)lane;
                 else set_status(M, ST_QUEUE);
             }
             continue;
@@ -930,7 +1009,8 @@ __global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsign
             }
             lo1[m] = INFINITY; hi1[m] = INFINITY; lo2[m] = INFINITY; j1[m] = -1;
         }
-        const float CN = (4.f * D + 8.f) * S32, CD = (4.f * D + 16.f) * S32;
+        const float CN = (4.f * D + 20.f) * S32, CD = (4.f * D + 16.f) * S32;
+        const float TINY = (float)(4e-14 * M.xscale);
         const int K = M.K;
         // candidate list: the real generator of the vertex with the largest
         // complete radius (every generator is on the current sphere, so any
@@ -959,19 +1039,20 @@ __global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsign
 #pragma unroll
             for (int s = 0; s < R; ++s) insig |= (j == sig[s]);
             if (insig) continue;
-            float xj[DP];
+            float xj[DP], xjl[DP];
             load_pt32<D>(M, j, xj);
+            load_pt32lo<D>(M, j, xjl);
             float dl[D], A1 = 0.f, A2 = 0.f, A3 = 0.f, dr = 0.f;
 #pragma unroll
             for (int k = 0; k < D; ++k) {
-                dl[k] = xj[k] - xa[k];
+                dl[k] = (xj[k] - xa[k]) + (xjl[k] - xal[k]);
                 A1 += fabsf(dl[k]);
                 A2 = fmaf(dl[k], dl[k], A2);
                 A3 = fmaf(fabsf(dl[k]), fabsf(rho[k]), A3);
                 dr = fmaf(dl[k], rho[k], dr);
             }
             const float num = fmaf(-2.f, dr, A2);
-            const float e_num = 4.f * EX * (A1 + R1) + CN * (A2 + 2.f * A3) + 2.f * A1 * erho;
+            const float e_num = CN * (A2 + 2.f * A3) + 2.f * A1 * erho + TINY * (A1 + R1);
 #pragma unroll
             for (int m = 0; m < R; ++m) {
                 if (!((rmask >> m) & 1u)) continue;
@@ -979,7 +1060,7 @@ __global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsign
 #pragma unroll
                 for (int k = 0; k < D; ++k) { du = fmaf(dl[k], u32[m][k], du); B = fmaf(fabsf(dl[k]), fabsf(u32[m][k]), B); }
                 const float den = 2.f * (du - lam32[m]);
-                const float e_den = 4.f * EX * U1[m] + CD * (B + fabsf(lam32[m])) + 2.f * relu * (A1 + LB[m]);
+                const float e_den = CD * (B + fabsf(lam32[m])) + 2.f * relu * (A1 + LB[m]) + TINY * U1[m];
                 float lo, hi;
                 if (den > e_den) {
                     const float r = __fdividef(1.f, den);
@@ -1044,9 +1125,9 @@ __global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsign
                 const bool upper = (p & 1) == 0;
                 const float uk = upper ? u[k] : -u[k];
                 const float hk = (float)M.hi[k], lk = (float)M.lo[k];
-                const float ck = xa[k] + rho[k];
+                const float ck = xa[k] + (xal[k] + rho[k]);
                 const float num = upper ? (hk - ck) : (ck - lk);
-                const float e_num = 4.f * S32 * (fabsf(hk) + fabsf(lk) + fabsf(xa[k]) + fabsf(rho[k])) + erho + EX;
+                const float e_num = 4.f * S32 * (fabsf(hk) + fabsf(lk) + fabsf(xa[k]) + fabsf(rho[k])) + erho + TINY;
                 const float e_den = relu + 2.f * S32 * fabsf(uk);
                 float lo, hi;
                 if (uk > e_den) {
@@ -1066,10 +1147,10 @@ __global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsign
             float blo, bhi, second;
             if (cj1 >= 0 && clo1 <= plo1) { win = cj1; blo = clo1; bhi = chi1; second = fminf(clo2, plo1); }
             else { win = pj1; blo = plo1; bhi = phi1; second = fminf(plo2, clo1); }
-            bool queue = false;
+            bool queue = false, exact = false;
             if (!(win >= 0 && bhi < second)) {
                 count_add(M.cnt + C_UNCERT);
-                queue = true;
+                exact = true;
             } else {
                 // security: the new empty sphere must lie inside the complete radius of the list
                 const float t = 0.5f * (blo + bhi), et = 0.5f * (bhi - blo);
@@ -1080,24 +1161,26 @@ __global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsign
                     int b = -1;
 #pragma unroll
                     for (int s = 1; s <= D; ++s) if (b < 0 && sig[s] < M.n) b = sig[s];
-                    float xb[DP];
+                    float xb[DP], xbl[DP];
                     load_pt32<D>(M, b, xb);
+                    load_pt32lo<D>(M, b, xbl);
 #pragma unroll
-                    for (int k = 0; k < D; ++k) db[k] = xb[k] - xa[k];
+                    for (int k = 0; k < D; ++k) db[k] = (xb[k] - xa[k]) + (xbl[k] - xal[k]);
                 }
-                float xo[DP];
+                float xo[DP], xol[DP];
                 load_pt32<D>(M, own, xo);
+                load_pt32lo<D>(M, own, xol);
                 float c2 = 0.f, r2 = 0.f, cm = 0.f;
 #pragma unroll
                 for (int k = 0; k < D; ++k) {
                     const float cc = fmaf(t, u[k], rho[k]);
-                    const float co = cc - (xo[k] - xa[k]);
+                    const float co = cc - ((xo[k] - xa[k]) + (xol[k] - xal[k]));
                     c2 = fmaf(co, co, c2);
                     const float wv = db[k] - cc;
                     r2 = fmaf(wv, wv, r2);
                     cm = fmaxf(cm, fabsf(cc));
                 }
-                const float ec = erho + fabsf(t) * relu + et + 4.f * S32 * (rmax + fabsf(t)) + 3.f * EX;
+                const float ec = erho + fabsf(t) * relu + et + 4.f * S32 * (rmax + fabsf(t)) + 3.f * TINY;
                 const float lhs = sqrtf(c2) + sqrtf(r2) + 4.f * sqrtf((float)D) * ec + 4.f * S32 * cm;
                 const float seco = sec_own;
                 if (!(t > 0.f) || !(lhs < seco * (1.f - 1e-5f))) {
@@ -1105,7 +1188,11 @@ __global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsign
                     queue = true;
                 }
             }
-            if (queue) {
+            if (exact) {
+                const unsigned slot = atomicAdd(nfx, 1u);
+                if (slot < fxcap) fx[slot] = ((unsigned long long)v << 3) | (unsigned)m;
+                else set_status(M, ST_QUEUE);
+            } else if (queue) {
                 const unsigned slot = atomicAdd(nfq, 1u);
                 if (slot < fqcap) fq[slot] = ((unsigned long long)v << 3) | (unsigned)m;
                 else set_status(M, ST_QUEUE);
@@ -1121,8 +1208,288 @@ __global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsign
 }
 
 // ---------------------------------------------------------------------------
+// warp fallback: one warp per ray whose new sphere left the list's complete
+// radius.  The ray is re-run in FP32 over the candidate list and then over
+// the whole tree (warp-uniform traversal, one leaf point per lane), with the
+// same per-candidate error bounds; the tree pass is exhaustive up to the
+// conservative box test, so no security test is needed.  Rays that remain
+// uncertified go to the FP64 kernel.
+// ---------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ void cand32(const DevMesh& M, int j, const float* xa, const float* xal, const float* rho,
+                                       float R1, float erho, const float* u, float lam, float U1, float LB,
+                                       float relu, float& lo, float& hi, bool& valid) {
+    constexpr int DP = (D <= 4) ? 4 : 8;
+    const float S32 = 5.9604645e-08f;
+    const float CN = (4.f * D + 20.f) * S32, CD = (4.f * D + 16.f) * S32;
+    const float TINY = (float)(4e-14 * M.xscale);
+    float xj[DP], xjl[DP];
+    load_pt32<D>(M, j, xj);
+    load_pt32lo<D>(M, j, xjl);
+    float A1 = 0.f, A2 = 0.f, A3 = 0.f, dr = 0.f, du = 0.f, B = 0.f;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const float dl = (xj[k] - xa[k]) + (xjl[k] - xal[k]);
+        A1 += fabsf(dl);
+        A2 = fmaf(dl, dl, A2);
+        A3 = fmaf(fabsf(dl), fabsf(rho[k]), A3);
+        dr = fmaf(dl, rho[k], dr);
+        du = fmaf(dl, u[k], du);
+        B = fmaf(fabsf(dl), fabsf(u[k]), B);
+    }
+    const float num = fmaf(-2.f, dr, A2);
+    const float e_num = CN * (A2 + 2.f * A3) + 2.f * A1 * erho + TINY * (A1 + R1);
+    const float den = 2.f * (du - lam);
+    const float e_den = CD * (B + fabsf(lam)) + 2.f * relu * (A1 + LB) + TINY * U1;
+    valid = true;
+    if (den > e_den) {
+        const float r = __fdividef(1.f, den);
+        const float t = num * r;
+        float et;
+        if (e_den < 1e-3f * den) et = (e_num + fabsf(t) * e_den) * r * 1.0021f;
+        else et = __fdividef(e_num + fabsf(t) * e_den, den - e_den) * 1.00001f;
+        et += 8.f * S32 * fabsf(t);
+        lo = t - et; hi = t + et;
+    } else if (den < -e_den) {
+        valid = false;
+    } else if (num - e_num > 0.f) {
+        if (!(den + e_den > 0.f)) { valid = false; return; }
+        lo = __fdividef(num - e_num, den + e_den) * 0.99999f; hi = INFINITY;
+    } else {
+        lo = -INFINITY; hi = INFINITY;
+    }
+}
+
+__device__ __forceinline__ void top2_merge(float& lo1, float& hi1, int& j1, float& lo2, float olo1, float ohi1,
+                                           int oj1, float olo2) {
+    const bool take = (olo1 < lo1) || (olo1 == lo1 && oj1 >= 0 && (j1 < 0 || oj1 < j1));
+    if (take) { lo2 = fminf(lo1, olo2); lo1 = olo1; hi1 = ohi1; j1 = oj1; }
+    else { lo2 = fminf(lo2, olo1); }
+}
+
+__device__ __forceinline__ void top2_warp(float& lo1, float& hi1, int& j1, float& lo2) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float a = __shfl_xor_sync(0xFFFFFFFFu, lo1, off);
+        const float b = __shfl_xor_sync(0xFFFFFFFFu, hi1, off);
+        const float c = __shfl_xor_sync(0xFFFFFFFFu, lo2, off);
+        const int e = __shfl_xor_sync(0xFFFFFFFFu, j1, off);
+        top2_merge(lo1, hi1, j1, lo2, a, b, e, c);
+    }
+}
+
+__device__ __forceinline__ void top2_add(float& lo1, float& hi1, int& j1, float& lo2, float lo, float hi, int j) {
+    if (j == j1) return;
+    if (lo < lo1 || (lo == lo1 && (j1 < 0 || j < j1))) { lo2 = lo1; lo1 = lo; hi1 = hi; j1 = j; }
+    else if (lo < lo2) lo2 = lo;
+}
+
+constexpr int FB_WPB = 4;
+
+template <int D>
+__global__ void __launch_bounds__(FB_WPB * 32) k_fallback_warp(DevMesh M, const unsigned long long* fq,
+                                                               const unsigned* nfq, unsigned fqcap,
+                                                               unsigned long long* fx, unsigned* nfx,
+                                                               unsigned fxcap) {
+    constexpr int R = D + 1;
+    constexpr int DP = (D <= 4) ? 4 : 8;
+    __shared__ int sstack[FB_WPB][64];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float S32 = 5.9604645e-08f;
+    const unsigned nq = min(*nfq, fqcap);
+    int* stk = sstack[wib];
+    for (unsigned w = blockIdx.x * FB_WPB + wib; w < nq; w += gridDim.x * FB_WPB) {
+        const unsigned long long e = fq[w];
+        const unsigned v = (unsigned)(e >> 3);
+        const int m = (int)(e & 7);
+        if (lane == 0) count_add(M.cnt + C_FALLBACK);
+        int sig[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) sig[k] = M.vsig[(size_t)v * R + k];
+        const int a = sig[0];
+        float xa[DP], xal[DP], rho[DP];
+        load_pt32<D>(M, a, xa);
+        load_pt32lo<D>(M, a, xal);
+        {
+            const float4* pr = reinterpret_cast<const float4*>(M.vrho32 + (size_t)v * DP);
+#pragma unroll
+            for (int h = 0; h < DP / 4; ++h) {
+                float4 f = pr[h];
+                rho[4 * h] = f.x; rho[4 * h + 1] = f.y; rho[4 * h + 2] = f.z; rho[4 * h + 3] = f.w;
+            }
+        }
+        const float* inv = M.vinv32 + (size_t)v * D * D;
+        float u[D], db[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) { u[k] = 0.f; db[k] = 0.f; }
+        if (m >= 1) {
+#pragma unroll
+            for (int k = 0; k < D; ++k) u[k] = -inv[k * D + (m - 1)];
+        } else {
+            int b = -1;
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                if (sig[c + 1] < M.n) {
+#pragma unroll
+                    for (int k = 0; k < D; ++k) u[k] += inv[k * D + c];
+                    if (b < 0) b = sig[c + 1];
+                }
+            }
+            float xb[DP], xbl[DP];
+            load_pt32<D>(M, b, xb);
+            load_pt32lo<D>(M, b, xbl);
+#pragma unroll
+            for (int k = 0; k < D; ++k) db[k] = (xb[k] - xa[k]) + (xbl[k] - xal[k]);
+        }
+        float nu = 0.f;
+#pragma unroll
+        for (int k = 0; k < D; ++k) nu = fmaf(u[k], u[k], nu);
+        nu = rsqrtf(nu);
+        float lam = 0.f, LB = 0.f, U1 = 0.f, R1 = 0.f, rmax = 0.f;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            u[k] *= nu;
+            lam = fmaf(u[k], db[k], lam);
+            LB += fabsf(db[k]);
+            U1 += fabsf(u[k]);
+            R1 += fabsf(rho[k]);
+            rmax = fmaxf(rmax, fabsf(rho[k]));
+        }
+        const float cond = M.vcond[v];
+        const float relu = (2.f * D + 6.f) * S32 + 8.f * D * cond * 1.1102230e-16f;
+        const float erho = 2.f * S32 * rmax;
+        float lo1 = INFINITY, hi1 = INFINITY, lo2 = INFINITY;
+        int j1 = -1;
+        // planes (lane 0)
+        if (lane == 0) {
+            const float TINY = (float)(4e-14 * M.xscale);
+#pragma unroll
+            for (int p = 0; p < 2 * D; ++p) {
+                const int it = M.n + p;
+                bool ex = false;
+#pragma unroll
+                for (int q = 0; q < R; ++q) ex |= (sig[q] == it);
+                if (ex) continue;
+                const int k = p >> 1;
+                const bool upper = (p & 1) == 0;
+                const float uk = upper ? u[k] : -u[k];
+                const float hk = (float)M.hi[k], lk = (float)M.lo[k];
+                const float ck = xa[k] + (xal[k] + rho[k]);
+                const float num = upper ? (hk - ck) : (ck - lk);
+                const float e_num = 4.f * S32 * (fabsf(hk) + fabsf(lk) + fabsf(xa[k]) + fabsf(rho[k])) + erho + TINY;
+                const float e_den = relu + 2.f * S32 * fabsf(uk);
+                float lo, hi;
+                if (uk > e_den) {
+                    const float t = __fdividef(num, uk);
+                    const float et = __fdividef(e_num + fabsf(t) * e_den, uk - e_den) * 1.00001f + 8.f * S32 * fabsf(t);
+                    lo = t - et; hi = t + et;
+                } else if (uk < -e_den) {
+                    continue;
+                } else {
+                    if (num - e_num > 0.f) { lo = __fdividef(num - e_num, fabsf(uk) + e_den) * 0.99999f; hi = INFINITY; }
+                    else { lo = -INFINITY; hi = INFINITY; }
+                }
+                top2_add(lo1, hi1, j1, lo2, lo, hi, it);
+            }
+        }
+        // candidate list of the anchor (good initial ball)
+        if (M.K > 0) {
+            const int* lst = M.knn + (size_t)a * M.K;
+            for (int c = lane; c < M.K; c += 32) {
+                const int j = __ldg(lst + c);
+                if (j < 0) continue;
+                bool insig = false;
+#pragma unroll
+                for (int q = 0; q < R; ++q) insig |= (j == sig[q]);
+                if (insig) continue;
+                float lo, hi;
+                bool ok;
+                cand32<D>(M, j, xa, xal, rho, R1, erho, u, lam, U1, LB, relu, lo, hi, ok);
+                if (ok) top2_add(lo1, hi1, j1, lo2, lo, hi, j);
+            }
+        }
+        top2_warp(lo1, hi1, j1, lo2);
+        // exhaustive tree pass with the shrinking ball
+        int sp = 1;
+        if (lane == 0) stk[0] = 1;
+        __syncwarp();
+        bool overflow = false;
+        while (sp > 0) {
+            const int node = stk[--sp];
+            __syncwarp();
+            // ball of the current upper bound, relative to x_a
+            const float tp = hi1;
+            if (isfinite(tp)) {
+                float r2 = 0.f, bd2 = 0.f;
+                const float* blo = M.blo + (size_t)node * DP;
+                const float* bhi = M.bhi + (size_t)node * DP;
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    const float off = fmaf(tp, u[k], rho[k]);
+                    const float w2 = db[k] - off;
+                    r2 = fmaf(w2, w2, r2);
+                    const float ck = xa[k] + (xal[k] + off);
+                    const float l = __ldg(blo + k), h = __ldg(bhi + k);
+                    const float ex = ck < l ? l - ck : (ck > h ? ck - h : 0.f);
+                    bd2 = fmaf(ex, ex, bd2);
+                }
+                const float rr = sqrtf(r2) * 1.0001f + 1e-6f * (float)M.xscale + 1e-4f * fabsf(tp);
+                if (bd2 > rr * rr) continue;
+            }
+            if (node >= M.P) {
+                const int l = node - M.P;
+                if (l >= M.nleaves) continue;
+                const int s0 = l * M.leaf, s1 = min(s0 + M.leaf, M.n);
+                for (int base = s0; base < s1; base += 32) {
+                    const int j = base + lane;
+                    if (j < s1) {
+                        bool insig = false;
+#pragma unroll
+                        for (int q = 0; q < R; ++q) insig |= (j == sig[q]);
+                        if (!insig) {
+                            float lo, hi;
+                            bool ok;
+                            cand32<D>(M, j, xa, xal, rho, R1, erho, u, lam, U1, LB, relu, lo, hi, ok);
+                            if (ok) top2_add(lo1, hi1, j1, lo2, lo, hi, j);
+                        }
+                    }
+                }
+                top2_warp(lo1, hi1, j1, lo2);
+            } else {
+                if (sp + 2 > 64) { overflow = true; break; }
+                if (lane == 0) { stk[sp] = 2 * node + 1; stk[sp + 1] = 2 * node; }
+                sp += 2;
+                __syncwarp();
+            }
+        }
+        if (lane == 0) {
+            if (!overflow && j1 >= 0 && hi1 < lo2) {
+                int ns[R];
+                make_sig<D>(sig, m, j1, ns);
+                bool is_new;
+                vertex_insert<D>(M, ns, j1, is_new);
+            } else {
+                count_add(M.cnt + C_UNCERT);
+                const unsigned slot = atomicAdd(nfx, 1u);
+                if (slot < fxcap) fx[slot] = e;
+                else set_status(M, ST_QUEUE);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
+template <int D>
+static void launch_register_t(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st) {
+    const unsigned long long total = (unsigned long long)(v1 - v0) * (D + 1);
+    if (!total) return;
+    unsigned long long blocks = (total + 255) / 256;
+    if (blocks > (unsigned long long)nsm * 32) blocks = (unsigned long long)nsm * 32;
+    k_register_edges<D><<<(unsigned)blocks, 256, 0, st>>>(M, v0, v1);
+}
 template <int D>
 static void launch_centers_t(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st) {
     if (v1 <= v0) return;
@@ -1145,12 +1512,22 @@ static void launch_plain_t(const DevMesh& M, unsigned f0, unsigned f1, int nsm, 
 }
 template <int D>
 static void launch_fast_t(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq,
-                          unsigned fqcap, int nsm, cudaStream_t st) {
+                          unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm,
+                          cudaStream_t st) {
     unsigned nf = f1 - f0;
     if (!nf) return;
     unsigned blocks = (nf + FAST_WPB - 1) / FAST_WPB;
     if (blocks > (unsigned)nsm * 32) blocks = (unsigned)nsm * 32;
-    k_expand_fast<D><<<blocks, FAST_WPB * 32, 0, st>>>(M, f0, f1, fq, nfq, fqcap);
+    k_expand_fast<D><<<blocks, FAST_WPB * 32, 0, st>>>(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap);
+}
+template <int D>
+static void launch_fallback_warp_t(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq,
+                                   unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx,
+                                   unsigned fxcap, int nsm, cudaStream_t st) {
+    if (!maxq) return;
+    unsigned blocks = (maxq + FB_WPB - 1) / FB_WPB;
+    if (blocks > (unsigned)nsm * 32) blocks = (unsigned)nsm * 32;
+    k_fallback_warp<D><<<blocks, FB_WPB * 32, 0, st>>>(M, fq, nfq, fqcap, fx, nfx, fxcap);
 }
 template <int D>
 static void launch_fallback_t(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq,
@@ -1171,6 +1548,9 @@ static void launch_fallback_t(const DevMesh& M, const unsigned long long* fq, co
         default: break;                           \
     }
 
+void launch_register_edges(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st) {
+    HV_DISPATCH(M.d, (launch_register_t<DD>(M, v0, v1, nsm, st)));
+}
 void launch_centers(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st) {
     HV_DISPATCH(M.d, (launch_centers_t<DD>(M, v0, v1, nsm, st)));
 }
@@ -1181,8 +1561,14 @@ void launch_expand_plain(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cu
     HV_DISPATCH(M.d, (launch_plain_t<DD>(M, f0, f1, nsm, st)));
 }
 void launch_expand_fast(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq,
-                        unsigned fqcap, int nsm, cudaStream_t st) {
-    HV_DISPATCH(M.d, (launch_fast_t<DD>(M, f0, f1, fq, nfq, fqcap, nsm, st)));
+                        unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm,
+                        cudaStream_t st) {
+    HV_DISPATCH(M.d, (launch_fast_t<DD>(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap, nsm, st)));
+}
+void launch_fallback_warp(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap,
+                          unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm,
+                          cudaStream_t st) {
+    HV_DISPATCH(M.d, (launch_fallback_warp_t<DD>(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, nsm, st)));
 }
 void launch_fallback(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm,
                      cudaStream_t st) {

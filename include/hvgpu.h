@@ -67,7 +67,7 @@ typedef struct {
     int leaf_size;        /* points per tree leaf */
     int rays_per_warp;    /* vertices expanded per warp in the fast kernel (1 or 2) */
     int seed_stride;      /* run a descent from every k-th generator */
-    int edge_dedup;       /* 1: close edges whose both end points are known (edge hash) */
+    int edge_dedup;       /* 0/1: skip edges whose both end points are known (edge table, default); -1: walk all */
     uint64_t seed;        /* seed of the descent directions */
     double capacity_factor; /* vertex capacity headroom over the per-dimension estimate */
 } hv_params;
@@ -130,6 +130,69 @@ int hv_integrate_polygon(hv_mesh* mesh, double* vol, double* area);
 int hv_integrate_heuristic_mc(hv_mesh* mesh, int ndir, uint64_t seed, double* vol, double* area);
 int hv_mesh_stats(hv_mesh* mesh, hv_stats* stats);
 int hv_mesh_free(hv_mesh* mesh);
+
+/* ------------------------------------------------------------------------
+ * Serving: continuous batching of mesh requests on one device.
+ *
+ * The server owns `slots` contexts (one CUDA stream and one worker thread
+ * each).  Requests are admitted in arrival order as soon as a slot is free and
+ * the HBM estimate of the request fits into the remaining budget next to the
+ * requests already running; the running requests' kernels overlap on the
+ * device.  Results do not depend on what else is running (every result is a
+ * pure function of its request).  There is no reference counterpart: the
+ * reference builds one mesh per call.
+ * ------------------------------------------------------------------------ */
+typedef struct hv_server hv_server;
+
+#define HV_INTEGRATOR_NONE 0
+#define HV_INTEGRATOR_POLYGON 1
+#define HV_INTEGRATOR_HEURISTIC_MC 2
+
+typedef struct {
+    int device;
+    int slots;               /* concurrent requests (worker threads / streams) */
+    double hbm_budget_bytes; /* admission budget; 0 = 80% of free device memory */
+} hv_server_config;
+
+typedef struct {
+    int d;
+    int64_t n;
+    const double* pts;       /* d x n, copied at submission */
+    const double* lo;
+    const double* hi;
+    int integrator;          /* HV_INTEGRATOR_* */
+    int ndir;                /* directions per cell for HV_INTEGRATOR_HEURISTIC_MC */
+    uint64_t mc_seed;
+    hv_params params;
+} hv_request;
+
+typedef struct {
+    int status;              /* HV_OK or the HV_E_* code of the failed request */
+    int d;
+    int64_t n, nverts, nnbr;
+    const int64_t* sig;      /* (d+1) x nverts, owned by the server until hv_server_release */
+    const double* r;         /* d x nverts */
+    const int64_t* offs;     /* n+1 */
+    const int64_t* nbr;      /* nnbr */
+    const double* vol;       /* n (NULL without integrator) */
+    const double* area;      /* nnbr (NULL without integrator) */
+    double queue_ms;         /* submission -> start of service */
+    double service_ms;       /* start of service -> result ready */
+    double latency_ms;       /* submission -> result ready */
+    hv_stats stats;
+} hv_result;
+
+int hv_server_start(const hv_server_config* cfg, hv_server** out);
+/* Copies the request and returns a ticket; HV_E_OOM if it can never fit the budget. */
+int hv_server_submit(hv_server* s, const hv_request* req, int64_t* ticket);
+/* done = 1 once the ticket's result is ready. */
+int hv_server_poll(hv_server* s, int64_t ticket, int* done);
+/* Blocks until the result is ready (timeout_ms < 0: no limit; HV_E_TIMEOUT on expiry). */
+int hv_server_wait(hv_server* s, int64_t ticket, double timeout_ms, hv_result* out);
+/* Frees the result buffers of a ticket. */
+int hv_server_release(hv_server* s, int64_t ticket);
+/* Drains running requests, stops the workers and frees the server. */
+int hv_server_stop(hv_server* s);
 
 #ifdef __cplusplus
 }

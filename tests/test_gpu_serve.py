@@ -1,0 +1,68 @@
+"""Serving loop (continuous batching) on the GPU, through the C ABI.
+
+Requests of mixed dimension and size are submitted while others run; each
+result must be bitwise identical to the same request served alone, and agree
+with the oracle.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from hvgpu import datasets as D
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests(k):
+    rng = np.random.default_rng(5)
+    out = []
+    for rid in range(k):
+        d = int(rng.integers(2, 6))
+        n = int(np.exp(rng.uniform(np.log(50), np.log(800))))
+        out.append((d, n, rid))
+    return out
+
+
+def test_results_identical_alone_and_in_the_mix(gpu_lib):
+    from hvgpu.serve import Server
+    reqs = _requests(12)
+    alone = []
+    with Server(slots=1) as s:
+        for d, n, rid in reqs:
+            t = s.submit(D.uniform_points(d, n, rid), integrator="polygon")
+            alone.append(s.result(t))
+    with Server(slots=4) as s:
+        tickets = [s.submit(D.uniform_points(d, n, rid), integrator="polygon") for d, n, rid in reqs]
+        mixed = [s.result(t) for t in tickets]
+    for a, b in zip(alone, mixed):
+        assert a["status"] == 0 and b["status"] == 0
+        for key in ("sig", "r", "offs", "nbr", "vol", "area"):
+            np.testing.assert_array_equal(a[key], b[key])
+    # and against the oracle on a few of them
+    for (d, n, rid), res in list(zip(reqs, mixed))[:4]:
+        ref = O.OracleMesh(D.uniform_points(d, n, rid), integrate=True)
+        np.testing.assert_array_equal(res["sig"], ref.vertices()[0])
+        rv, ra = ref.polygon()
+        np.testing.assert_allclose(res["vol"], rv, rtol=1e-10)
+
+
+def test_server_reports_latency_and_errors(gpu_lib):
+    from hvgpu.serve import Server
+    with Server(slots=2) as s:
+        bad = D.uniform_points(3, 40, 1)
+        bad[0, 0] = 2.0
+        t_bad = s.submit(bad)
+        t_ok = s.submit(D.uniform_points(3, 40, 2))
+        rb = s.result(t_bad)
+        ro = s.result(t_ok)
+        assert rb["status"] == -1
+        assert ro["status"] == 0
+        assert ro["latency_ms"] >= ro["service_ms"] >= 0.0
+
+
+def test_admission_budget_serialises_large_requests(gpu_lib):
+    from hvgpu.serve import Server
+    import hvgpu
+    with pytest.raises(hvgpu.HVError):
+        with Server(slots=2, hbm_budget_bytes=1e6) as s:
+            s.submit(D.uniform_points(4, 2000, 1))
