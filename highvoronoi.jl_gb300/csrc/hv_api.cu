@@ -14,6 +14,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <new>
 #include <stdexcept>
@@ -32,6 +33,7 @@ struct hv_ctx {
     std::string err;
     unsigned* h_stat = nullptr;  // pinned: vcount, status, nfq, pad
     std::vector<cudaEvent_t> evpool;  // timing events, reused across builds
+    std::map<std::pair<int, int>, hv_params> tuned;  // autotuner results per (d, log2 n)
 };
 
 struct hv_mesh {
@@ -303,7 +305,12 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         M.vcount = dstat;
         CK(cudaMemsetAsync(dstat, 0, 4 * sizeof(unsigned), st));
         CK(cudaMemsetAsync(dcnt, 0, C_NCOUNT * sizeof(unsigned long long), st));
-        kt.run(F_DESCENT, 1, [&] { launch_descent(M, stride, nseeds, mesh->prm.seed ? mesh->prm.seed : 0x5EEDull, st); });
+        int* dfail = fast ? srch->get<int>((size_t)nseeds) : nullptr;
+        unsigned* ndfail = fast ? srch->get<unsigned>(1) : nullptr;
+        if (fast) CK(cudaMemsetAsync(ndfail, 0, sizeof(unsigned), st));
+        kt.run(F_DESCENT, fast ? 2 : 1, [&] {
+            launch_descent(M, stride, nseeds, mesh->prm.seed ? mesh->prm.seed : 0x5EEDull, dfail, ndfail, ctx->nsm, st);
+        });
         CK(cudaGetLastError());
         read_stat(ctx, dstat);
         const unsigned overflow_bits = ST_VCAP | ST_HASH | ST_QUEUE | ST_ECAP;
@@ -489,6 +496,17 @@ int build_entry(hv_ctx* ctx, int d, int64_t n, const double* src, bool on_device
     m->ctx = ctx; m->d = d; m->n = (int)n;
     for (int k = 0; k < d; ++k) { m->lo[k] = lo[k]; m->hi[k] = hi[k]; }
     if (params) m->prm = *params; else hv_params_default(&m->prm);
+    {
+        int nb = 0;
+        while ((1ll << (nb + 1)) <= std::max<int64_t>(n, 1)) ++nb;
+        auto it = ctx->tuned.find({d, nb});
+        if (it != ctx->tuned.end() && m->prm.method == HV_METHOD_FAST) {
+            if (m->prm.knn == 0) m->prm.knn = it->second.knn;
+            if (m->prm.leaf_size == 0) m->prm.leaf_size = it->second.leaf_size;
+            if (m->prm.seed_stride == 0) m->prm.seed_stride = it->second.seed_stride;
+            if (m->prm.rays_per_warp == 0) m->prm.rays_per_warp = it->second.rays_per_warp;
+        }
+    }
     if (m->prm.method != HV_METHOD_FAST && m->prm.method != HV_METHOD_PLAIN) {
         delete m;
         ctx->err = "unknown method";
@@ -570,6 +588,60 @@ int hv_mesh_build_device(hv_ctx* ctx, int d, int64_t n, const double* d_pts, con
     return build_entry(ctx, d, n, d_pts, true, lo, hi, params, out);
 }
 
+int hv_autotune(hv_ctx* ctx, int d, int64_t n, const double* pts, const double* lo, const double* hi,
+                hv_params* out) {
+    int rc = validate_common(ctx, d, n, lo, hi, (hv_mesh**)&out);
+    if (rc != HV_OK || !out) return rc != HV_OK ? rc : HV_E_INVALID_ARG;
+    if (n < 2) { hv_params_default(out); return HV_OK; }
+    std::vector<double> synth;
+    if (!pts) {  // uniform points in the box (SplitMix64, seed 0x7a11)
+        synth.resize((size_t)n * d);
+        uint64_t st = 0x7a11;
+        for (size_t q = 0; q < synth.size(); ++q) {
+            uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+            z ^= z >> 31;
+            const double u01 = ((double)(z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+            const int k = (int)(q % d);
+            synth[q] = lo[k] + (hi[k] - lo[k]) * u01;
+        }
+        pts = synth.data();
+    }
+    static const int kd[7] = {0, 0, 32, 96, 256, 384, 480};
+    const int K0 = kd[d];
+    std::vector<int> ks = {std::max(16, K0 / 2), K0, std::min(480, K0 * 3 / 2)};
+    std::vector<int> leaves = {8, 16};
+    std::vector<int> strides = {1, 4, 16};
+    hv_params best;
+    hv_params_default(&best);
+    double best_ms = 1e300;
+    for (int K : ks)
+        for (int L : leaves)
+            for (int S : strides) {
+                hv_params p;
+                hv_params_default(&p);
+                p.knn = K; p.leaf_size = L; p.seed_stride = S; p.rays_per_warp = 1;
+                double ms = 1e300;
+                for (int rep = 0; rep < 2; ++rep) {  // the first build warms caches and the pool
+                    hv_mesh* m = nullptr;
+                    int r = hv_mesh_build(ctx, d, n, pts, lo, hi, &p, &m);
+                    if (r != HV_OK) { ms = 1e300; break; }
+                    hv_stats stt;
+                    hv_mesh_stats(m, &stt);
+                    ms = std::min(ms, stt.ms_total);
+                    hv_mesh_free(m);
+                }
+                if (ms < best_ms) { best_ms = ms; best = p; }
+            }
+    if (best_ms >= 1e300) return HV_E_INTERNAL;
+    int nb = 0;
+    while ((1ll << (nb + 1)) <= n) ++nb;
+    ctx->tuned[{d, nb}] = best;
+    *out = best;
+    return HV_OK;
+}
+
 int hv_mesh_counts(hv_mesh* m, int64_t* nverts, int64_t* nnbr_total) {
     if (!m) return HV_E_INVALID_ARG;
     try {
@@ -649,12 +721,16 @@ int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) {
             hv::PolyCaps c;
             c.capC = capC; c.capV = capV; c.capF = 2 * capV;
             c.capE = (int)next_pow2((unsigned long long)capV * (d - 1) / 2 + 2);
+            c.capI = (int)std::min<unsigned long long>(1024ull, next_pow2((unsigned long long)std::max(64, capV)));
             return c;
         };
         // shared-memory pass: the largest power-of-two cell size that fits
         int capC = (int)std::min<unsigned long long>(next_pow2((unsigned long long)maxc), 1024ull);
         int capV = std::min(capC, std::max(64, capC / 4));
-        while (capC > 16 && (long long)hv::poly_smem_bytes(d, capC, capV, 2 * capV, caps_for(capC, capV).capE) > smax) {
+        auto smem_of = [&](const hv::PolyCaps& c) {
+            return (long long)hv::poly_smem_bytes(d, c.capC, c.capV, c.capF, c.capE, c.capI);
+        };
+        while (capC > 16 && smem_of(caps_for(capC, capV)) > smax) {
             capC /= 2;
             capV = std::min(capC, std::max(64, capC / 4));
         }
@@ -671,7 +747,7 @@ int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) {
             CK(cudaMemcpyAsync(hs, dstat, sizeof(hs), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
             if (hs[1] > 0 && !(hs[0] & 2u)) {
-                const size_t bytes = (hv::poly_smem_bytes(d, cg.capC, cg.capV, cg.capF, cg.capE) + 255) / 256 * 256;
+                const size_t bytes = ((size_t)smem_of(cg) + 255) / 256 * 256;
                 const int gblocks = (int)std::min<unsigned>(hs[1], (unsigned)(2 * m->ctx->nsm));
                 Scratch gs(st);
                 unsigned char* gbase = gs.get<unsigned char>(bytes * gblocks);

@@ -34,7 +34,7 @@ struct PolyArgs {
     const int* nbr;
     double* area;            // aligned with nbr
     unsigned* status;        // bit 1: cell too large, bit 2: facet structure overflow
-    int capC, capV, capF, capE;
+    int capC, capV, capF, capE, capI;
 };
 
 __device__ __forceinline__ double plane_height(const PolyArgs& A, const double* xi, int k) {
@@ -114,6 +114,27 @@ __device__ __forceinline__ void lehmer(int w, int m, int* ord) {
     }
 }
 
+// Local item lists: every facet vertex has D-1 generators besides i and k,
+// mapped to local indices < capI (10 bits) and kept sorted.  A face of the
+// facet is a sorted subset of those indices, packed 10 bits per item with the
+// length in bits 56..59, so faces sort and search as 64-bit keys.
+__device__ __forceinline__ unsigned long long pack_face(const int* it, int len) {
+    unsigned long long k = (unsigned long long)len << 56;
+    for (int q = 0; q < len; ++q) k |= (unsigned long long)it[q] << (10 * q);
+    return k;
+}
+
+// Is the sorted list `sub` (len items) contained in the sorted list `set` (m items)?
+__device__ __forceinline__ bool contains_sorted(const int* set, int m, const int* sub, int len) {
+    int p = 0;
+    for (int q = 0; q < len; ++q) {
+        while (p < m && set[p] < sub[q]) ++p;
+        if (p == m || set[p] != sub[q]) return false;
+        ++p;
+    }
+    return true;
+}
+
 // GLOBAL = false: work area in shared memory, all cells; cells with more than
 // capC vertices are appended to `big` for the GLOBAL = true pass, whose work
 // area is a per-block slab of global memory sized for the largest cell.
@@ -122,20 +143,21 @@ __global__ void __launch_bounds__(128) k_poly_cells(PolyArgs A, const int* cells
                                                     size_t area_bytes, int* big, unsigned* nbig) {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned char* base = GLOBAL ? gbase + (size_t)blockIdx.x * area_bytes : smem;
-    const int capC = A.capC, capV = A.capV, capF = A.capF, capE = A.capE;
+    const int capC = A.capC, capV = A.capV, capF = A.capF, capE = A.capE, capI = A.capI;
+    constexpr int DM = (D > 1) ? D - 1 : 1;        // local items per facet vertex
     double* cx = (double*)base;                       // capC x D   cell vertex coords - x_i
     double* fcen = cx + (size_t)capC * D;             // capF x D   face centroids
     double* cF = fcen + (size_t)capF * D;             // D          facet centroid
     double* red = cF + D;                             // blockDim
-    unsigned long long* fmask = (unsigned long long*)(red + blockDim.x);  // capV
-    unsigned long long* flist = fmask + capV;         // capF (sorted face masks)
+    unsigned long long* flist = (unsigned long long*)(red + blockDim.x);  // capF (sorted face keys)
     unsigned long long* ftab = flist + capF;          // 2*capF hash table
     int* csig = (int*)(ftab + 2 * capF);              // capC x (D+1)
     int* fv = csig + (size_t)capC * (D + 1);          // capV (local cell-vertex index)
-    int* ekey = fv + capV;                            // capE (a << 16 | b)
-    int* items = ekey + capE;                         // 64
-    int* itab = items + 64;                           // 128 hash of items
-    int* cnt = itab + 128;                            // 8 counters
+    int* vit = fv + capV;                             // capV x DM local item lists (sorted)
+    int* ekey = vit + (size_t)capV * DM;              // capE (a << 16 | b)
+    int* items = ekey + capE;                         // capI
+    int* itab = items + capI;                         // 2*capI hash of items
+    int* cnt = itab + 2 * capI;                       // 8 counters
 
     constexpr int NPERM = (D <= 3) ? 1 : (D == 4 ? 2 : (D == 5 ? 6 : 24));  // (D-2)!
     double fact = 1.0;
@@ -170,7 +192,7 @@ __global__ void __launch_bounds__(128) k_poly_cells(PolyArgs A, const int* cells
             const int k = A.nbr[t];
             if (k < i) continue;
             if (threadIdx.x < 8) cnt[threadIdx.x] = 0;
-            for (int x = threadIdx.x; x < 128; x += blockDim.x) itab[x] = -1;
+            for (int x = threadIdx.x; x < 2 * capI; x += blockDim.x) itab[x] = -1;
             __syncthreads();
             // facet vertices (cell-local indices)
             for (int a = threadIdx.x; a < nc; a += blockDim.x) {
@@ -195,73 +217,79 @@ __global__ void __launch_bounds__(128) k_poly_cells(PolyArgs A, const int* cells
             block_bitonic<int>(fv, nv2);
             // local items (generators of the facet's vertices other than i and k)
             for (int a = threadIdx.x; a < nv; a += blockDim.x) {
-                const int* s = csig + fv[a] * (D + 1);
+                const int* sg = csig + fv[a] * (D + 1);
                 for (int q = 0; q <= D; ++q) {
-                    const int it = s[q];
+                    const int it = sg[q];
                     if (it == i || it == k) continue;
-                    unsigned h = ((unsigned)it * 2654435761u) & 127u;
-                    for (int pr = 0; pr < 128; ++pr) {
+                    unsigned h = ((unsigned)it * 2654435761u) & (unsigned)(2 * capI - 1);
+                    for (int pr = 0; pr < 2 * capI; ++pr) {
                         const int prev = atomicCAS(&itab[h], -1, it);
                         if (prev == -1) { atomicAdd(&cnt[1], 1); break; }
                         if (prev == it) break;
-                        h = (h + 1) & 127u;
+                        h = (h + 1) & (unsigned)(2 * capI - 1);
                     }
                 }
             }
             __syncthreads();
             const int ni = cnt[1];
-            if (ni > 64) {
+            if (ni > capI) {
                 if (threadIdx.x == 0) atomicOr(A.status, 2u);
                 __syncthreads();
                 continue;
             }
             if (threadIdx.x == 0) {
                 int w = 0;
-                for (int x = 0; x < 128; ++x) if (itab[x] >= 0) items[w++] = itab[x];
-                for (int x = w; x < 64; ++x) items[x] = 0x7FFFFFFF;
+                for (int x = 0; x < 2 * capI; ++x) if (itab[x] >= 0) items[w++] = itab[x];
+                for (int x = w; x < capI; ++x) items[x] = 0x7FFFFFFF;
             }
             __syncthreads();
-            block_bitonic<int>(items, 64);
-            // vertex masks over the local items
+            block_bitonic<int>(items, capI);
+            // per-vertex sorted local item lists
             for (int a = threadIdx.x; a < nv; a += blockDim.x) {
-                const int* s = csig + fv[a] * (D + 1);
-                unsigned long long m = 0;
+                const int* sg = csig + fv[a] * (D + 1);
+                int loc[DM];
+                int w = 0;
                 for (int q = 0; q <= D; ++q) {
-                    const int it = s[q];
+                    const int it = sg[q];
                     if (it == i || it == k) continue;
                     int lo = 0, hi = ni - 1;
                     while (lo < hi) { const int md = (lo + hi) >> 1; if (items[md] < it) lo = md + 1; else hi = md; }
-                    m |= 1ull << lo;
+                    if (w < DM) loc[w++] = lo;
                 }
-                fmask[a] = m;
+                for (int x = 1; x < w; ++x)
+                    for (int y = x; y > 0 && loc[y] < loc[y - 1]; --y) { const int z = loc[y]; loc[y] = loc[y - 1]; loc[y - 1] = z; }
+                for (int x = 0; x < DM; ++x) vit[a * DM + x] = x < w ? loc[x] : 0x7FFFFFFF;
             }
             __syncthreads();
             // facet centroid (fixed-order sums)
             if (D >= 3) {
                 for (int c = 0; c < D; ++c) {
-                    double s = 0;
-                    for (int a = threadIdx.x; a < nv; a += blockDim.x) s += cx[fv[a] * D + c];
-                    const double tot = block_sum(s, red);
+                    double sum = 0;
+                    for (int a = threadIdx.x; a < nv; a += blockDim.x) sum += cx[fv[a] * D + c];
+                    const double tot = block_sum(sum, red);
                     if (threadIdx.x == 0) cF[c] = tot / nv;
                 }
             }
-            // faces of size 1..D-3 (d >= 4): hash, then sorted list
+            // faces: sorted subsets of size 1..D-3 of the vertices' item lists (d >= 4)
             int nf = 0;
             if (D >= 4) {
                 for (int x = threadIdx.x; x < 2 * capF; x += blockDim.x) ftab[x] = 0ull;
                 __syncthreads();
                 for (int a = threadIdx.x; a < nv; a += blockDim.x) {
-                    const unsigned long long m = fmask[a];
-                    // enumerate sub-masks of m with popcount in [1, D-3]
-                    for (unsigned long long sub = m; sub; sub = (sub - 1) & m) {
-                        const int pc = __popcll(sub);
+                    const int* li = vit + a * DM;
+                    for (unsigned sub = 1; sub < (1u << DM); ++sub) {
+                        const int pc = __popc(sub);
                         if (pc > D - 3) continue;
-                        unsigned long long h = (sub * 0x9E3779B97F4A7C15ull) >> 20;
+                        int tup[DM];
+                        int w = 0;
+                        for (int x = 0; x < DM; ++x) if ((sub >> x) & 1u) tup[w++] = li[x];
+                        const unsigned long long key = pack_face(tup, w);
+                        const unsigned long long h = (key * 0x9E3779B97F4A7C15ull) >> 20;
                         for (int pr = 0; pr < 2 * capF; ++pr) {
                             const unsigned slot = (unsigned)((h + pr) & (unsigned long long)(2 * capF - 1));
-                            const unsigned long long prev = atomicCAS(&ftab[slot], 0ull, sub);
+                            const unsigned long long prev = atomicCAS(&ftab[slot], 0ull, key);
                             if (prev == 0ull) { atomicAdd(&cnt[2], 1); break; }
-                            if (prev == sub) break;
+                            if (prev == key) break;
                         }
                     }
                 }
@@ -282,29 +310,34 @@ __global__ void __launch_bounds__(128) k_poly_cells(PolyArgs A, const int* cells
                 __syncthreads();
                 block_bitonic<unsigned long long>(flist, nf2);
                 for (int f = threadIdx.x; f < nf; f += blockDim.x) {
-                    const unsigned long long L = flist[f];
-                    double s[D];
+                    const unsigned long long key = flist[f];
+                    const int len = (int)(key >> 56);
+                    int tup[DM];
+                    for (int q = 0; q < len; ++q) tup[q] = (int)((key >> (10 * q)) & 1023ull);
+                    double sum[D];
 #pragma unroll
-                    for (int c = 0; c < D; ++c) s[c] = 0;
+                    for (int c = 0; c < D; ++c) sum[c] = 0;
                     int cntv = 0;
                     for (int a = 0; a < nv; ++a) {
-                        if ((fmask[a] & L) == L) {
+                        if (contains_sorted(vit + a * DM, DM, tup, len)) {
                             ++cntv;
 #pragma unroll
-                            for (int c = 0; c < D; ++c) s[c] += cx[fv[a] * D + c];
+                            for (int c = 0; c < D; ++c) sum[c] += cx[fv[a] * D + c];
                         }
                     }
 #pragma unroll
-                    for (int c = 0; c < D; ++c) fcen[f * D + c] = s[c] / cntv;
+                    for (int c = 0; c < D; ++c) fcen[f * D + c] = sum[c] / cntv;
                 }
             }
             // edges: vertex pairs sharing D-2 local items
             for (int a = threadIdx.x; a < nv; a += blockDim.x) {
-                const unsigned long long m = fmask[a];
-                for (unsigned long long bits = m; bits; bits &= bits - 1) {
-                    const unsigned long long L = m & ~(bits & (~bits + 1));
+                const int* la = vit + a * DM;
+                for (int drop = 0; drop < DM; ++drop) {
+                    int L[DM];
+                    int w = 0;
+                    for (int x = 0; x < DM; ++x) if (x != drop) L[w++] = la[x];
                     for (int b = a + 1; b < nv; ++b) {
-                        if ((fmask[b] & L) == L) {
+                        if (contains_sorted(vit + b * DM, DM, L, w)) {
                             const int p = atomicAdd(&cnt[3], 1);
                             if (p < capE) ekey[p] = (a << 16) | b;
                             break;
@@ -337,17 +370,24 @@ __global__ void __launch_bounds__(128) k_poly_cells(PolyArgs A, const int* cells
                     col = 1;
                 }
                 if (D >= 4) {
-                    const unsigned long long L = fmask[a] & fmask[b];
-                    int it[HV_MAXD];
+                    // common items of a and b (the edge), in sorted order
+                    int it[DM];
                     int m = 0;
-                    for (unsigned long long bits = L; bits; bits &= bits - 1) it[m++] = __ffsll((long long)bits) - 1;
+                    const int* la = vit + a * DM;
+                    const int* lb = vit + b * DM;
+                    for (int x = 0; x < DM; ++x)
+                        if (contains_sorted(lb, DM, la + x, 1)) it[m++] = la[x];
                     int ord[HV_MAXD];
                     lehmer(perm, D - 2, ord);
-                    unsigned long long pre = 0;
+                    int pre[DM];
                     for (int j = 0; j < D - 3; ++j) {
-                        pre |= 1ull << it[ord[j]];
+                        // prefix {it[ord[0]], ..., it[ord[j]]}, sorted
+                        int x = j;
+                        pre[x] = it[ord[j]];
+                        while (x > 0 && pre[x] < pre[x - 1]) { const int z = pre[x]; pre[x] = pre[x - 1]; pre[x - 1] = z; --x; }
+                        const unsigned long long key = pack_face(pre, j + 1);
                         int lo = 0, hi = nf - 1;
-                        while (lo < hi) { const int md = (lo + hi) >> 1; if (flist[md] < pre) lo = md + 1; else hi = md; }
+                        while (lo < hi) { const int md = (lo + hi) >> 1; if (flist[md] < key) lo = md + 1; else hi = md; }
 #pragma unroll
                         for (int c = 0; c < D; ++c) {
 #pragma unroll
@@ -602,14 +642,14 @@ static PolyArgs make_args(const IntegrateInput& in) {
     A.inc_off = in.inc_off; A.inc = in.inc; A.nbr_off = in.nbr_off; A.nbr = in.nbr;
     A.status = in.status;
     A.area = nullptr;
-    A.capC = A.capV = A.capF = A.capE = 0;
+    A.capC = A.capV = A.capF = A.capE = A.capI = 0;
     return A;
 }
 
-size_t poly_smem_bytes(int d, int capC, int capV, int capF, int capE) {
+size_t poly_smem_bytes(int d, int capC, int capV, int capF, int capE, int capI) {
     return sizeof(double) * ((size_t)capC * d + (size_t)capF * d + d + 128) +
-           sizeof(unsigned long long) * ((size_t)capV + 3 * (size_t)capF) +
-           sizeof(int) * ((size_t)capC * (d + 1) + capV + capE + 64 + 128 + 8);
+           sizeof(unsigned long long) * (3 * (size_t)capF) +
+           sizeof(int) * ((size_t)capC * (d + 1) + (size_t)capV * d + capE + 3 * (size_t)capI + 8);
 }
 
 template <int D>
@@ -619,8 +659,8 @@ static int poly_t(const IntegrateInput& in, const PolyCaps& cs, const PolyCaps& 
     PolyArgs A = make_args(in);
     A.area = area;
     if (pass == 0) {
-        A.capC = cs.capC; A.capV = cs.capV; A.capF = cs.capF; A.capE = cs.capE;
-        const size_t sm = poly_smem_bytes(D, cs.capC, cs.capV, cs.capF, cs.capE);
+        A.capC = cs.capC; A.capV = cs.capV; A.capF = cs.capF; A.capE = cs.capE; A.capI = cs.capI;
+        const size_t sm = poly_smem_bytes(D, cs.capC, cs.capV, cs.capF, cs.capE, cs.capI);
         if (cudaFuncSetAttribute(k_poly_cells<D, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
             cudaSuccess)
             return -1;
@@ -629,8 +669,8 @@ static int poly_t(const IntegrateInput& in, const PolyCaps& cs, const PolyCaps& 
         if (blocks < 1) blocks = 1;
         k_poly_cells<D, false><<<blocks, 128, sm, st>>>(A, nullptr, 0, nullptr, 0, big, nbig);
     } else if (pass == 1) {
-        A.capC = cg.capC; A.capV = cg.capV; A.capF = cg.capF; A.capE = cg.capE;
-        const size_t bytes = poly_smem_bytes(D, cg.capC, cg.capV, cg.capF, cg.capE);
+        A.capC = cg.capC; A.capV = cg.capV; A.capF = cg.capF; A.capE = cg.capE; A.capI = cg.capI;
+        const size_t bytes = poly_smem_bytes(D, cg.capC, cg.capV, cg.capF, cg.capE, cg.capI);
         k_poly_cells<D, true><<<gblocks, 128, 0, st>>>(A, big, (int)nbig_host, gbase, (bytes + 255) / 256 * 256,
                                                         nullptr, nullptr);
     } else {

@@ -20,10 +20,10 @@ struct IntegrateInput {
 };
 
 struct PolyCaps {
-    int capC, capV, capF, capE;  // cell vertices, facet vertices, faces, edges (powers of two)
+    int capC, capV, capF, capE, capI;  // cell vertices, facet vertices, faces, edges, local items (powers of two)
 };
 
-size_t poly_smem_bytes(int d, int capC, int capV, int capF, int capE);
+size_t poly_smem_bytes(int d, int capC, int capV, int capF, int capE, int capI);
 // pass 0: shared-memory kernel over all cells (big cells appended to `big`),
 // pass 1: global-memory kernel over the big cells, pass 2: volumes.
 int launch_polygon(const IntegrateInput& in, const PolyCaps& cs, const PolyCaps& cg, int* big, unsigned* nbig,

@@ -1,1578 +1,115 @@
-// hv_search.cu -- Voronoi vertex search on the GPU.
-//
-// The vertex set is explored as a wavefront over the graph of Voronoi
-// vertices: level 0 holds one seed vertex per generator (descent), level k+1
-// the vertices first reached by walking the edges of level k.  A walk from
-// vertex S along the edge S \ {q} is the incircle raycast of the reference
-// (raycast_des2, src/raycast.jl:794-970): the next generator is the argmin over
-// u.(x_j - x_b) > 0 of t_j = (|x_j - r|^2 - |x_b - r|^2) / (2 u.(x_j - x_b)),
-// with boundary planes entering through their crossing parameter (the t of the
-// mirror node N+p, src/raycast.jl:354-375).  New vertices are deduplicated in
-// an open-addressing hash keyed on the sorted generator tuple (the role of
-// the reference's vertex database / QueueHashTable, src/hvdatabase.jl:111,
-// src/queuehashing.jl:8-104).
-//
-// Two ray kernels:
-//  * exact (one ray per thread, FP64): shrinking-ball search over the tree
-//    (the fused kd traversal of RCCombined, src/raycast.jl:504-528); used for
-//    the PLAIN method and as the fallback of the fast kernel;
-//  * fast (one warp per vertex): all open edges of a vertex scan the FP32
-//    candidate list of the vertex's anchor generator in one pass, with a
-//    forward error bound per candidate; a decision is kept only if it is
-//    certified and the new empty sphere lies inside the list's complete
-//    radius, otherwise the ray is redone by the exact kernel.
+// hv_search.cu -- dimension dispatch of the vertex-search launchers
+// (kernels in hv_search_impl.cuh, one translation unit per dimension).
 #include "hv_internal.cuh"
 #include "hv_host.h"
 
 namespace hv {
 
-constexpr double EPS64 = 1.1102230246251565e-16;
-
-// ---------------------------------------------------------------------------
-// vertex hash
-// ---------------------------------------------------------------------------
-template <int D>
-__device__ unsigned vertex_insert(const DevMesh& M, const int (&s)[D + 1], int newitem, bool& is_new) {
-    is_new = false;
-    const unsigned long long h = hash_items(s, D + 1);
-    const unsigned fp = ((unsigned)(h >> 32) & 0x7FFFFFFFu) | 1u;
-    unsigned long long slot = h & M.vhmask;
-    for (unsigned long long probe = 0; probe <= M.vhmask; ++probe) {
-        unsigned long long e = *(volatile unsigned long long*)&M.vhash[slot];
-        if (e == HASH_EMPTY) {
-            unsigned long long prev = atomicCAS(&M.vhash[slot], HASH_EMPTY, HASH_BUSY);
-            if (prev == HASH_EMPTY) {
-                unsigned vid = atomicAdd(M.vcount, 1u);
-                if (vid >= M.vcap) {
-                    set_status(M, ST_VCAP);
-                    atomicExch(&M.vhash[slot], ((unsigned long long)fp << 32) | INVALID_ID);
-                    return INVALID_ID;
-                }
-#pragma unroll
-                for (int k = 0; k <= D; ++k) M.vsig[(size_t)vid * (D + 1) + k] = s[k];
-                M.vnew[vid] = newitem;
-                __threadfence();
-                atomicExch(&M.vhash[slot], ((unsigned long long)fp << 32) | vid);
-                is_new = true;
-                return vid;
-            }
-            e = prev;
-        }
-        int spins = 0;
-        while (e == HASH_BUSY) {
-            if (++spins > SPIN_LIMIT) { set_status(M, ST_TIMEOUT); return INVALID_ID; }
-            __nanosleep(32);
-            e = *(volatile unsigned long long*)&M.vhash[slot];
-        }
-        if ((unsigned)(e >> 32) == fp) {
-            unsigned id = (unsigned)e;
-            if (id != INVALID_ID) {
-                __threadfence();
-                bool eq = true;
-#pragma unroll
-                for (int k = 0; k <= D; ++k) eq &= (__ldcg(&M.vsig[(size_t)id * (D + 1) + k]) == s[k]);
-                if (eq) return id;
-            }
-        }
-        slot = (slot + 1) & M.vhmask;
-    }
-    set_status(M, ST_HASH);
-    return INVALID_ID;
-}
-
-// FP64 circumcentre of a signature.
-template <int D>
-__device__ bool vertex_center(const DevMesh& M, const int (&s)[D + 1], double (&c)[D]) {
-    double xa[D], A[D][D], rhs[D];
-    const double* pa = M.pts + (size_t)s[0] * D;
-#pragma unroll
-    for (int k = 0; k < D; ++k) xa[k] = __ldg(pa + k);
-#pragma unroll
-    for (int r = 0; r < D; ++r) con_row<D, double>(M, xa, s[r + 1], A[r], rhs[r]);
-    int piv[D];
-    if (!lu_factor<D, double>(A, piv)) return false;
-    lu_solve<D, double>(A, piv, rhs);
-#pragma unroll
-    for (int k = 0; k < D; ++k) c[k] = xa[k] + rhs[k];
-    return true;
-}
-
-// ---------------------------------------------------------------------------
-// exact FP64 search
-// ---------------------------------------------------------------------------
-struct Cand { int item; double t, lo, hi; };
-
-struct SearchOut {
-    Cand best;
-    double second_lo;
-    Cand amb[HV_NAMB];
-    int namb;
-    bool overflow;
-};
-
-template <int D>
-struct Query {
-    int a;
-    double xa[D], rho[D], u[D], db[D];
-    double lam;
-    int excl[D + 1];
-    int nexcl;
-    double erho, eu;
-};
-
-__device__ __forceinline__ void consider(SearchOut& R, const Cand& c) {
-    // a candidate may be met twice (seed set and tree): keep one copy
-    if (c.item == R.best.item) return;
-    for (int k = 0; k < R.namb; ++k) if (R.amb[k].item == c.item) return;
-    if (c.lo < R.best.lo) {
-        if (R.best.item >= 0) {
-            R.second_lo = R.best.lo;
-            if (R.best.lo <= c.hi) {
-                if (R.namb < HV_NAMB) R.amb[R.namb++] = R.best; else R.overflow = true;
-            }
-        }
-        R.best = c;
-    } else {
-        if (c.lo < R.second_lo) R.second_lo = c.lo;
-        if (c.lo <= R.best.hi) {
-            if (R.namb == HV_NAMB) {  // compact: drop what the current best excludes
-                int w = 0;
-                for (int k = 0; k < HV_NAMB; ++k) if (R.amb[k].lo <= R.best.hi) R.amb[w++] = R.amb[k];
-                R.namb = w;
-            }
-            if (R.namb < HV_NAMB) R.amb[R.namb++] = c; else R.overflow = true;
-        }
-    }
-}
-
-template <int D>
-__device__ __forceinline__ bool q_excluded(const Query<D>& q, int it) {
-    bool ex = false;
-#pragma unroll
-    for (int s = 0; s <= D; ++s) ex |= (s < q.nexcl && q.excl[s] == it);
-    return ex;
-}
-
-template <int D>
-__device__ __forceinline__ void eval_point(const DevMesh& M, const Query<D>& q, int j, SearchOut& R) {
-    const double* xj = M.pts + (size_t)j * D;
-    double nd = 0, dr = 0, du = 0, sdr = 0, sdu = 0, l1 = 0;
-#pragma unroll
-    for (int k = 0; k < D; ++k) {
-        double dl = __ldg(xj + k) - q.xa[k];
-        nd = fma(dl, dl, nd); dr = fma(dl, q.rho[k], dr); du = fma(dl, q.u[k], du);
-        sdr += fabs(dl * q.rho[k]); sdu += fabs(dl * q.u[k]); l1 += fabs(dl);
-    }
-    double num = nd - 2.0 * dr;
-    double den = 2.0 * (du - q.lam);
-    double e_num = (4.0 * D + 8.0) * EPS64 * (nd + 2.0 * sdr) + 2.0 * l1 * q.erho;
-    double e_den = (2.0 * D + 8.0) * EPS64 * 2.0 * (sdu + fabs(q.lam)) + 4.0 * l1 * q.eu;
-    Cand c; c.item = j;
-    if (den > e_den) {
-        c.t = num / den;
-        double et = (e_num + fabs(c.t) * e_den) / (den - e_den) + 4.0 * EPS64 * fabs(c.t);
-        c.lo = c.t - et; c.hi = c.t + et;
-    } else if (den < -e_den) {
-        return;
-    } else {
-        if (num - e_num > 0) {
-            if (!(den + e_den > 0)) return;
-            c.lo = (num - e_num) / (den + e_den); c.hi = INFINITY; c.t = c.lo;
-        } else {
-            c.lo = -INFINITY; c.hi = INFINITY; c.t = 0;
-        }
-    }
-    if (c.lo < R.best.hi || c.lo < R.second_lo) consider(R, c);
-}
-
-template <int D>
-__device__ __forceinline__ void eval_planes(const DevMesh& M, const Query<D>& q, SearchOut& R) {
-#pragma unroll
-    for (int p = 0; p < 2 * D; ++p) {
-        const int it = M.n + p;
-        if (q_excluded<D>(q, it)) continue;
-        const int k = p >> 1;
-        const bool upper = (p & 1) == 0;
-        double uk = upper ? q.u[k] : -q.u[k];
-        double ck = q.xa[k] + q.rho[k];
-        double num = upper ? (M.hi[k] - ck) : (ck - M.lo[k]);
-        double e_num = 4.0 * EPS64 * (fabs(M.hi[k]) + fabs(M.lo[k]) + fabs(q.xa[k]) + fabs(q.rho[k])) + q.erho;
-        double e_den = q.eu + 2.0 * EPS64 * fabs(uk);
-        Cand c; c.item = it;
-        if (uk > e_den) {
-            c.t = num / uk;
-            double et = (e_num + fabs(c.t) * e_den) / (uk - e_den) + 4.0 * EPS64 * fabs(c.t);
-            c.lo = c.t - et; c.hi = c.t + et;
-        } else if (uk < -e_den) {
-            continue;
-        } else {
-            if (num - e_num > 0) { c.lo = (num - e_num) / (fabs(uk) + e_den); c.hi = INFINITY; c.t = c.lo; }
-            else { c.lo = -INFINITY; c.hi = INFINITY; c.t = 0; }
-        }
-        consider(R, c);
-    }
-}
-
-template <int D>
-__device__ __forceinline__ double box_dist2(const DevMesh& M, int node, const double (&c)[D]) {
-    const float* lo = M.blo + (size_t)node * M.dp;
-    const float* hi = M.bhi + (size_t)node * M.dp;
-    double s = 0;
-#pragma unroll
-    for (int k = 0; k < D; ++k) {
-        double l = (double)__ldg(lo + k), h = (double)__ldg(hi + k);
-        double e = c[k] < l ? l - c[k] : (c[k] > h ? c[k] - h : 0.0);
-        s = fma(e, e, s);
-    }
-    return s;
-}
-
-// Shrinking-ball tree search for argmin t (certified with forward error bounds).
-template <int D>
-__device__ void exact_search(const DevMesh& M, const Query<D>& q, SearchOut& R) {
-    R.best = Cand{-1, INFINITY, INFINITY, INFINITY};
-    R.second_lo = INFINITY;
-    R.namb = 0;
-    R.overflow = false;
-    eval_planes<D>(M, q, R);
-    // start from the anchor's neighbourhood so that the ball is small before
-    // the tree is entered: its leaf, then the head of its candidate list
-    {
-        const int la = q.a / M.leaf;
-        const int s0 = la * M.leaf, s1 = min(s0 + M.leaf, M.n);
-        for (int j = s0; j < s1; ++j) if (!q_excluded<D>(q, j)) eval_point<D>(M, q, j, R);
-        const int kh = min(M.K, 32);
-        for (int c = 0; c < kh; ++c) {
-            const int j = __ldg(M.knn + (size_t)q.a * M.K + c);
-            if (j >= 0 && !q_excluded<D>(q, j)) eval_point<D>(M, q, j, R);
-        }
-    }
-    int stack[64];
-    int sp = 0;
-    stack[sp++] = 1;
-    while (sp > 0) {
-        const int node = stack[--sp];
-        const double tp = R.best.hi;
-        if (isfinite(tp)) {
-            const double tpp = tp * (1.0 + 1e-9) + 1e-300;
-            double c[D];
-            double r2 = 0;
-#pragma unroll
-            for (int k = 0; k < D; ++k) {
-                double off = q.rho[k] + tpp * q.u[k];
-                c[k] = q.xa[k] + off;
-                double w = q.db[k] - off;
-                r2 = fma(w, w, r2);
-            }
-            if (box_dist2<D>(M, node, c) > r2 * (1.0 + 1e-9) + 1e-280) continue;
-        }
-        if (node >= M.P) {
-            const int l = node - M.P;
-            if (l >= M.nleaves) continue;
-            const int s0 = l * M.leaf;
-            const int s1 = min(s0 + M.leaf, M.n);
-            for (int j = s0; j < s1; ++j) {
-                if (q_excluded<D>(q, j)) continue;
-                eval_point<D>(M, q, j, R);
-            }
-        } else {
-            const double tp2 = isfinite(R.best.hi) ? R.best.hi : 0.0;
-            double c[D];
-#pragma unroll
-            for (int k = 0; k < D; ++k) c[k] = q.xa[k] + q.rho[k] + tp2 * q.u[k];
-            const double dl = box_dist2<D>(M, 2 * node, c);
-            const double dr = box_dist2<D>(M, 2 * node + 1, c);
-            if (sp + 2 > 64) { set_status(M, ST_STACK); break; }
-            if (dl <= dr) { stack[sp++] = 2 * node + 1; stack[sp++] = 2 * node; }
-            else { stack[sp++] = 2 * node; stack[sp++] = 2 * node + 1; }
-        }
-    }
-    int w = 0;
-    for (int k = 0; k < R.namb; ++k)
-        if (R.amb[k].item != R.best.item && R.amb[k].lo <= R.best.hi) R.amb[w++] = R.amb[k];
-    R.namb = w;
-}
-
-// Is any real generator outside S strictly inside the sphere (c, r2)?
-template <int D>
-__device__ bool ball_occupied(const DevMesh& M, const double (&c)[D], double r2, const int (&S)[D + 1], double tol) {
-    int stack[64];
-    int sp = 0;
-    stack[sp++] = 1;
-    while (sp > 0) {
-        const int node = stack[--sp];
-        if (box_dist2<D>(M, node, c) >= r2) continue;
-        if (node >= M.P) {
-            const int l = node - M.P;
-            if (l >= M.nleaves) continue;
-            const int s0 = l * M.leaf, s1 = min(s0 + M.leaf, M.n);
-            for (int j = s0; j < s1; ++j) {
-                bool ex = false;
-#pragma unroll
-                for (int s = 0; s <= D; ++s) ex |= (S[s] == j);
-                if (ex) continue;
-                const double* xj = M.pts + (size_t)j * D;
-                double dd2 = 0;
-#pragma unroll
-                for (int k = 0; k < D; ++k) { double e = __ldg(xj + k) - c[k]; dd2 = fma(e, e, dd2); }
-                if (dd2 < r2 * (1.0 - tol)) return true;
-            }
-        } else {
-            if (sp + 2 > 64) { set_status(M, ST_STACK); return true; }
-            stack[sp++] = 2 * node; stack[sp++] = 2 * node + 1;
-        }
-    }
-    return false;
-}
-
-// ---------------------------------------------------------------------------
-// double-double re-scoring of ambiguous decisions
-// ---------------------------------------------------------------------------
-template <int D>
-__device__ int dd_rescore_walk(const DevMesh& M, const int (&sig)[D + 1], int m, const int* items, int nitems,
-                               bool& degen) {
-    degen = false;
-    double xa[D];
-    const double* pa = M.pts + (size_t)sig[0] * D;
-#pragma unroll
-    for (int k = 0; k < D; ++k) xa[k] = __ldg(pa + k);
-    dd A[D][D], rho[D], u[D], db[D];
-#pragma unroll
-    for (int r = 0; r < D; ++r) con_row<D, dd>(M, xa, sig[r + 1], A[r], rho[r]);
-    int piv[D];
-    if (!lu_factor<D, dd>(A, piv)) { degen = true; return nitems > 0 ? items[0] : -1; }
-    lu_solve<D, dd>(A, piv, rho);
-#pragma unroll
-    for (int k = 0; k < D; ++k) { u[k] = mk(0.0); db[k] = mk(0.0); }
-    if (m >= 1) {
-#pragma unroll
-        for (int k = 0; k < D; ++k) u[k] = mk(k == m - 1 ? 1.0 : 0.0);
-        lu_solve<D, dd>(A, piv, u);
-#pragma unroll
-        for (int k = 0; k < D; ++k) u[k] = -u[k];
-    } else {
-        int b = -1;
-#pragma unroll
-        for (int r = 0; r < D; ++r) {
-            bool real = sig[r + 1] < M.n;
-            u[r] = mk(real ? 1.0 : 0.0);
-            if (real && b < 0) b = sig[r + 1];
-        }
-        lu_solve<D, dd>(A, piv, u);
-        if (b >= 0) {
-            const double* pb = M.pts + (size_t)b * D;
-#pragma unroll
-            for (int k = 0; k < D; ++k) db[k] = diff_d<dd>(__ldg(pb + k), xa[k]);
-        }
-    }
-    dd lam = mk(0.0);
-#pragma unroll
-    for (int k = 0; k < D; ++k) lam += u[k] * db[k];
-    int best = -1, second = -1;
-    dd bt = mk(0.0), st = mk(0.0);
-    for (int c = 0; c < nitems; ++c) {
-        const int it = items[c];
-        dd t;
-        if (it < M.n) {
-            const double* xj = M.pts + (size_t)it * D;
-            dd nd = mk(0.0), dr = mk(0.0), du = mk(0.0);
-#pragma unroll
-            for (int k = 0; k < D; ++k) {
-                dd dl = diff_d<dd>(__ldg(xj + k), xa[k]);
-                nd += dl * dl; dr += dl * rho[k]; du += dl * u[k];
-            }
-            dd den = (du - lam) * mk(2.0);
-            if (!(den.hi > 0)) continue;
-            t = (nd - dr * mk(2.0)) / den;
-        } else {
-            const int p = it - M.n, k0 = p >> 1;
-            const bool upper = (p & 1) == 0;
-            dd uk = mk(0.0), ck = mk(0.0);
-#pragma unroll
-            for (int k = 0; k < D; ++k) if (k == k0) { uk = upper ? u[k] : -u[k]; ck = mk(xa[k]) + rho[k]; }
-            if (!(uk.hi > 0)) continue;
-            dd num = upper ? (mk(M.hi[k0]) - ck) : (ck - mk(M.lo[k0]));
-            t = num / uk;
-        }
-        if (best < 0 || t < bt || (!(bt < t) && it < best)) { second = best; st = bt; best = it; bt = t; }
-        else if (second < 0 || t < st) { second = it; st = t; }
-    }
-    if (best >= 0 && second >= 0) {
-        dd gap = st - bt;
-        if (gap.hi <= 1e-27 * (fabs(bt.hi) + 1e-3)) degen = true;
-    }
-    return best;
-}
-
-// Re-evaluate a descent step in double-double from the FP64 state.
-template <int D>
-__device__ int dd_rescore_point(const DevMesh& M, const Query<D>& q, const int* items, int nitems, double& tout) {
-    int best = -1;
-    dd bt = mk(0.0);
-    for (int c = 0; c < nitems; ++c) {
-        const int it = items[c];
-        dd t;
-        if (it < M.n) {
-            const double* xj = M.pts + (size_t)it * D;
-            dd nd = mk(0.0), dr = mk(0.0), du = mk(0.0);
-#pragma unroll
-            for (int k = 0; k < D; ++k) {
-                dd dl = diff_d<dd>(__ldg(xj + k), q.xa[k]);
-                nd += dl * dl; dr += dl * mk(q.rho[k]); du += dl * mk(q.u[k]);
-            }
-            dd den = (du - mk(q.lam)) * mk(2.0);
-            if (!(den.hi > 0)) continue;
-            t = (nd - dr * mk(2.0)) / den;
-        } else {
-            const int p = it - M.n, k0 = p >> 1;
-            const bool upper = (p & 1) == 0;
-            double uk = upper ? q.u[k0] : -q.u[k0];
-            if (!(uk > 0)) continue;
-            dd ck = mk(q.xa[k0]) + mk(q.rho[k0]);
-            dd num = upper ? (mk(M.hi[k0]) - ck) : (ck - mk(M.lo[k0]));
-            t = num / mk(uk);
-        }
-        if (best < 0 || t < bt || (!(bt < t) && it < best)) { best = it; bt = t; }
-    }
-    tout = bt.hi;
-    return best;
-}
-
-// ---------------------------------------------------------------------------
-// exact walk of one edge (PLAIN method and fallback)
-// ---------------------------------------------------------------------------
-// Sets up the ray leaving vertex `sig` along the edge sig \ {sig[m]}.
-template <int D>
-__device__ bool setup_walk(const DevMesh& M, const int (&sig)[D + 1], int m, Query<D>& q) {
-    q.a = sig[0];
-    const double* pa = M.pts + (size_t)q.a * D;
-#pragma unroll
-    for (int k = 0; k < D; ++k) q.xa[k] = __ldg(pa + k);
-    double A[D][D], rhs[D];
-#pragma unroll
-    for (int r = 0; r < D; ++r) con_row<D, double>(M, q.xa, sig[r + 1], A[r], rhs[r]);
-    double nrm = 0;
-#pragma unroll
-    for (int r = 0; r < D; ++r) {
-        double s = 0;
-#pragma unroll
-        for (int k = 0; k < D; ++k) s += fabs(A[r][k]);
-        nrm = fmax(nrm, s);
-    }
-    int piv[D];
-    if (!lu_factor<D, double>(A, piv)) { set_status(M, ST_NUMERIC); return false; }
-#pragma unroll
-    for (int k = 0; k < D; ++k) q.rho[k] = rhs[k];
-    lu_solve<D, double>(A, piv, q.rho);
-    double rows[D];
-    int b = -1;
-#pragma unroll
-    for (int k = 0; k < D; ++k) { rows[k] = 0; q.u[k] = 0; q.db[k] = 0; }
-#pragma unroll
-    for (int c = 0; c < D; ++c) {
-        double col[D];
-#pragma unroll
-        for (int k = 0; k < D; ++k) col[k] = (k == c) ? 1.0 : 0.0;
-        lu_solve<D, double>(A, piv, col);
-#pragma unroll
-        for (int k = 0; k < D; ++k) rows[k] += fabs(col[k]);
-        const bool real = sig[c + 1] < M.n;
-        if (m >= 1 && c == m - 1) {
-#pragma unroll
-            for (int k = 0; k < D; ++k) q.u[k] = -col[k];
-        }
-        if (m == 0 && real) {
-#pragma unroll
-            for (int k = 0; k < D; ++k) q.u[k] += col[k];
-            if (b < 0) b = sig[c + 1];
-        }
-    }
-    if (m == 0) {
-        if (b < 0) return false;  // the edge holds only planes: no walk
-        const double* pb = M.pts + (size_t)b * D;
-#pragma unroll
-        for (int k = 0; k < D; ++k) q.db[k] = __ldg(pb + k) - q.xa[k];
-    }
-    double ninv = 0;
-#pragma unroll
-    for (int k = 0; k < D; ++k) ninv = fmax(ninv, rows[k]);
-    const double cond = nrm * ninv;
-    double nu = 0;
-#pragma unroll
-    for (int k = 0; k < D; ++k) nu = fma(q.u[k], q.u[k], nu);
-    nu = sqrt(nu);
-    if (!(nu > 0)) { set_status(M, ST_NUMERIC); return false; }
-    q.lam = 0;
-    double nr = 0, nuu = 0;
-#pragma unroll
-    for (int k = 0; k < D; ++k) {
-        q.u[k] /= nu;
-        q.lam = fma(q.u[k], q.db[k], q.lam);
-        nr = fmax(nr, fabs(q.rho[k]));
-        nuu = fmax(nuu, fabs(q.u[k]));
-    }
-    const double kap = 8.0 * D * fmax(cond, 1.0) * EPS64;
-    q.erho = kap * (nr + 1e-3);
-    q.eu = kap * (nuu + 1e-3);
-#pragma unroll
-    for (int s = 0; s <= D; ++s) q.excl[s] = sig[s];
-    q.nexcl = D + 1;
-    return true;
-}
-
-template <int D>
-__device__ void exact_walk(const DevMesh& M, unsigned v, int m) {
-    int sig[D + 1];
-#pragma unroll
-    for (int k = 0; k <= D; ++k) sig[k] = M.vsig[(size_t)v * (D + 1) + k];
-    Query<D> q;
-    if (!setup_walk<D>(M, sig, m, q)) return;
-    SearchOut R;
-    exact_search<D>(M, q, R);
-    if (R.best.item < 0) { set_status(M, ST_NUMERIC); return; }
-    int win = R.best.item;
-    if (!(R.best.hi < R.second_lo)) {
-        count_add(M.cnt + C_DD);
-        if (R.overflow) set_status(M, ST_AMB);
-        int items[HV_NAMB + 1];
-        items[0] = R.best.item;
-        for (int k = 0; k < R.namb; ++k) items[k + 1] = R.amb[k].item;
-        bool degen = false;
-        win = dd_rescore_walk<D>(M, sig, m, items, R.namb + 1, degen);
-        if (degen) { count_add(M.cnt + C_DEGEN); set_status(M, ST_DEGEN); }
-        if (win < 0) { set_status(M, ST_NUMERIC); return; }
-    }
-    int ns[D + 1];
-    make_sig<D>(sig, m, win, ns);
-    bool is_new;
-    vertex_insert<D>(M, ns, win, is_new);
-}
-
-// Edge sig \ {sig[m]} is walkable if it is not the edge the vertex was found
-// through and if it still contains a real generator.
-template <int D>
-__device__ __forceinline__ bool walkable(const DevMesh& M, const int (&sig)[D + 1], int vnew, int m) {
-    if (sig[m] == vnew) return false;
-    if (m == 0) return sig[1] < M.n;
-    return true;
-}
-
-template <int D>
-__global__ void __launch_bounds__(128) k_expand_plain(DevMesh M, unsigned f0, unsigned f1) {
-    const unsigned long long total = (unsigned long long)(f1 - f0) * (D + 1);
-    for (unsigned long long r = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; r < total;
-         r += (unsigned long long)gridDim.x * blockDim.x) {
-        const unsigned v = f0 + (unsigned)(r / (D + 1));
-        const int m = (int)(r % (D + 1));
-        int sig[D + 1];
-#pragma unroll
-        for (int k = 0; k <= D; ++k) sig[k] = M.vsig[(size_t)v * (D + 1) + k];
-        if (!walkable<D>(M, sig, M.vnew[v], m)) continue;
-        if (M.ecnt && ((__ldg(M.ecnt + v) >> m) & 1u)) continue;  // both end points known
-        count_add(M.cnt + C_RAYS);
-        exact_walk<D>(M, v, m);
-    }
-}
-
-template <int D>
-__global__ void __launch_bounds__(128) k_fallback(DevMesh M, const unsigned long long* fq, const unsigned* nfq,
-                                                  unsigned fqcap) {
-    const unsigned n = min(*nfq, fqcap);  // entries past the capacity were never written
-    for (unsigned r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-        const unsigned long long e = fq[r];
-        count_add(M.cnt + C_FALLBACK);
-        exact_walk<D>(M, (unsigned)(e >> 3), (int)(e & 7));
-    }
-}
-
-// ---------------------------------------------------------------------------
-// descent: one seed vertex per selected generator (src/raycast.jl:45-109)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void philox4x32(unsigned (&c)[4], unsigned k0, unsigned k1) {
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        unsigned hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
-        unsigned hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
-        unsigned o0 = hi1 ^ c[1] ^ k0, o2 = hi0 ^ c[3] ^ k1;
-        c[0] = o0; c[1] = lo1; c[2] = o2; c[3] = lo0;
-        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
-    }
-}
-
-template <int D>
-__device__ void gauss_dir(unsigned long long seed, unsigned a, unsigned long long b, double (&g)[D]) {
-    int got = 0;
-#pragma unroll
-    for (unsigned blk = 0; blk < (unsigned)((D + 3) / 4); ++blk) {
-        unsigned c[4] = {a, (unsigned)b, (unsigned)(b >> 32), blk};
-        philox4x32(c, (unsigned)seed, (unsigned)(seed >> 32));
-#pragma unroll
-        for (int p = 0; p < 2; ++p) {
-            double u1 = ((double)c[2 * p] + 0.5) * 2.3283064365386963e-10;
-            double u2 = ((double)c[2 * p + 1] + 0.5) * 2.3283064365386963e-10;
-            double rr = sqrt(-2.0 * log(u1));
-            double sn, cs;
-            sincospi(2.0 * u2, &sn, &cs);
-#pragma unroll
-            for (int k = 0; k < D; ++k) {
-                if (k == got) g[k] = rr * cs;
-                if (k == got + 1) g[k] = rr * sn;
-            }
-            got += 2;
-        }
-    }
-}
-
-template <int D>
-__global__ void __launch_bounds__(128) k_descent(DevMesh M, int stride, int nseeds, unsigned long long seed) {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= nseeds) return;
-    const int i = idx * stride;
-    if (i >= M.n) return;
-    count_add(M.cnt + C_DESCENT);
-    for (int attempt = 0; attempt < 16; ++attempt) {
-        Query<D> q;
-        q.a = i;
-        const double* pa = M.pts + (size_t)i * D;
-#pragma unroll
-        for (int k = 0; k < D; ++k) { q.xa[k] = __ldg(pa + k); q.rho[k] = 0; q.db[k] = 0; }
-        q.lam = 0; q.erho = 1e-12; q.eu = 1e-13;
-        q.excl[0] = i; q.nexcl = 1;
-#pragma unroll
-        for (int s = 1; s <= D; ++s) q.excl[s] = -1;
-        bool ok = true;
-        for (int step = 1; step <= D && ok; ++step) {
-            double g[D];
-            gauss_dir<D>(seed, (unsigned)(attempt * 16 + step), (unsigned long long)i, g);
-            // Gram-Schmidt basis of the constraint rows of the current set
-            double B[D][D];
-#pragma unroll
-            for (int s = 1; s < D; ++s) {
-                if (s >= q.nexcl) break;
-                double row[D], rh;
-                con_row<D, double>(M, q.xa, q.excl[s], row, rh);
-#pragma unroll
-                for (int t = 0; t < D - 1; ++t) {
-                    if (t >= s - 1) break;
-                    double pr = 0;
-#pragma unroll
-                    for (int k = 0; k < D; ++k) pr = fma(row[k], B[t][k], pr);
-#pragma unroll
-                    for (int k = 0; k < D; ++k) row[k] -= pr * B[t][k];
-                }
-                double nn = 0;
-#pragma unroll
-                for (int k = 0; k < D; ++k) nn = fma(row[k], row[k], nn);
-                nn = sqrt(nn);
-                if (!(nn > 1e-300)) { ok = false; break; }
-#pragma unroll
-                for (int k = 0; k < D; ++k) B[s - 1][k] = row[k] / nn;
-            }
-            if (!ok) break;
-            for (int rep = 0; rep < 2; ++rep) {
-#pragma unroll
-                for (int t = 0; t < D - 1; ++t) {
-                    if (t >= q.nexcl - 1) break;
-                    double pr = 0;
-#pragma unroll
-                    for (int k = 0; k < D; ++k) pr = fma(g[k], B[t][k], pr);
-#pragma unroll
-                    for (int k = 0; k < D; ++k) g[k] -= pr * B[t][k];
-                }
-            }
-            double nn = 0;
-#pragma unroll
-            for (int k = 0; k < D; ++k) nn = fma(g[k], g[k], nn);
-            nn = sqrt(nn);
-            if (!(nn > 1e-12)) { ok = false; break; }
-#pragma unroll
-            for (int k = 0; k < D; ++k) q.u[k] = g[k] / nn;
-            SearchOut R;
-            exact_search<D>(M, q, R);
-            if (R.best.item < 0) { ok = false; break; }
-            int win = R.best.item;
-            double t = R.best.t;
-            if (!(R.best.hi < R.second_lo)) {
-                int items[HV_NAMB + 1];
-                items[0] = R.best.item;
-                for (int k = 0; k < R.namb; ++k) items[k + 1] = R.amb[k].item;
-                win = dd_rescore_point<D>(M, q, items, R.namb + 1, t);
-                if (win < 0) { ok = false; break; }
-            }
-            if (!(t > 0) || !isfinite(t)) { ok = false; break; }
-#pragma unroll
-            for (int k = 0; k < D; ++k) q.rho[k] = fma(t, q.u[k], q.rho[k]);
-#pragma unroll
-            for (int s = 0; s <= D; ++s) if (s == q.nexcl) q.excl[s] = win;
-            q.nexcl++;
-        }
-        if (ok) {
-            int S[D + 1];
-#pragma unroll
-            for (int s = 0; s <= D; ++s) S[s] = q.excl[s];
-            // sort (insertion, D+1 <= 7)
-#pragma unroll
-            for (int s = 1; s <= D; ++s) {
-#pragma unroll
-                for (int t = s; t > 0; --t) {
-                    if (S[t] < S[t - 1]) { int x = S[t]; S[t] = S[t - 1]; S[t - 1] = x; }
-                }
-            }
-            double c[D];
-            bool good = vertex_center<D>(M, S, c);
-            if (good) {
-                double r2 = 0;
-                const double* p0 = M.pts + (size_t)S[0] * D;
-#pragma unroll
-                for (int k = 0; k < D; ++k) {
-                    double tol = 1e-12 * (1.0 + fabs(M.hi[k]) + fabs(M.lo[k]));
-                    if (c[k] < M.lo[k] - tol || c[k] > M.hi[k] + tol) good = false;
-                    double e = __ldg(p0 + k) - c[k];
-                    r2 = fma(e, e, r2);
-                }
-                if (good) good = !ball_occupied<D>(M, c, r2, S, 1e-10);
-            }
-            if (good) {
-                bool is_new;
-                vertex_insert<D>(M, S, -1, is_new);
-                return;
-            }
-        }
-        count_add(M.cnt + C_DRETRY);
-    }
-    set_status(M, ST_DESCENT);
-}
-
-// ---------------------------------------------------------------------------
-// edge registry (src/edgehashing.jl:49-111): an edge is the sorted d-tuple
-// sig \ {sig[m]}; the table entry references (vertex, slot) so the key is read
-// back from the vertex record.  The second end point to register an edge
-// closes it for both: neither walks it (both end points are known).
-// ---------------------------------------------------------------------------
-template <int D>
-__global__ void __launch_bounds__(256) k_register_edges(DevMesh M, unsigned v0, unsigned v1) {
-    const unsigned long long total = (unsigned long long)(v1 - v0) * (D + 1);
-    for (unsigned long long r = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; r < total;
-         r += (unsigned long long)gridDim.x * blockDim.x) {
-        const unsigned v = v0 + (unsigned)(r / (D + 1));
-        const int m = (int)(r % (D + 1));
-        int sig[D + 1];
-#pragma unroll
-        for (int k = 0; k <= D; ++k) sig[k] = M.vsig[(size_t)v * (D + 1) + k];
-        if (m == 0 && sig[1] >= M.n) continue;  // the edge holds only planes
-        int e[D];
-        int o = 0;
-#pragma unroll
-        for (int k = 0; k <= D; ++k) if (k != m) e[o++] = sig[k];
-        const unsigned long long h = hash_items(e, D);
-        const unsigned fp = ((unsigned)(h >> 32) & 0x7FFFFFFFu) | 1u;
-        const unsigned long long mine = ((unsigned long long)fp << 32) | ((unsigned long long)v * 8u + (unsigned)m);
-        unsigned long long slot = h & M.ehmask;
-        bool done = false;
-        for (unsigned long long probe = 0; probe <= M.ehmask && !done; ++probe) {
-            const unsigned long long prev = atomicCAS(&M.ehash[slot], HASH_EMPTY, mine);
-            if (prev == HASH_EMPTY) { done = true; break; }
-            if ((unsigned)(prev >> 32) == fp) {
-                const unsigned ref = (unsigned)prev;
-                const unsigned ov = ref >> 3, om = ref & 7u;
-                int q = 0;
-                bool eq = true;
-#pragma unroll
-                for (int k = 0; k <= D; ++k) {
-                    if (k == (int)om) continue;
-                    const int x = M.vsig[(size_t)ov * (D + 1) + k];
-#pragma unroll
-                    for (int z = 0; z < D; ++z) if (z == q) eq &= (x == e[z]);
-                    ++q;
-                }
-                if (eq) {
-                    atomicOr(M.ecnt + ov, 1u << om);
-                    atomicOr(M.ecnt + v, 1u << m);
-                    count_add(M.cnt + C_EDGECLOSED);
-                    done = true;
-                    break;
-                }
-            }
-            slot = (slot + 1) & M.ehmask;
-        }
-        if (!done) set_status(M, ST_ECAP);
-    }
-}
-
-// ---------------------------------------------------------------------------
-// FP64 circumcentres of new vertices, one thread per vertex (full-warp FP64)
-// ---------------------------------------------------------------------------
-template <int D>
-__global__ void __launch_bounds__(128) k_centers(DevMesh M, unsigned v0, unsigned v1) {
-    constexpr int DP = (D <= 4) ? 4 : 8;
-    for (unsigned v = v0 + blockIdx.x * blockDim.x + threadIdx.x; v < v1; v += gridDim.x * blockDim.x) {
-        int s[D + 1];
-#pragma unroll
-        for (int k = 0; k <= D; ++k) s[k] = M.vsig[(size_t)v * (D + 1) + k];
-        double xa[D], A[D][D], rho[D];
-        const double* pa = M.pts + (size_t)s[0] * D;
-#pragma unroll
-        for (int k = 0; k < D; ++k) xa[k] = __ldg(pa + k);
-#pragma unroll
-        for (int r = 0; r < D; ++r) con_row<D, double>(M, xa, s[r + 1], A[r], rho[r]);
-        double nrm = 0;
-#pragma unroll
-        for (int r = 0; r < D; ++r) {
-            double sr = 0;
-#pragma unroll
-            for (int k = 0; k < D; ++k) sr += fabs(A[r][k]);
-            nrm = fmax(nrm, sr);
-        }
-        int piv[D];
-        const bool ok = lu_factor<D, double>(A, piv);
-        if (!ok) {
-            set_status(M, ST_NUMERIC);
-#pragma unroll
-            for (int k = 0; k < D; ++k) rho[k] = 0.0;
-        } else {
-            lu_solve<D, double>(A, piv, rho);
-        }
-        float r32[DP];
-#pragma unroll
-        for (int k = 0; k < DP; ++k) r32[k] = 0.f;
-#pragma unroll
-        for (int k = 0; k < D; ++k) {
-            M.vc[(size_t)v * D + k] = xa[k] + rho[k];
-            r32[k] = (float)rho[k];
-        }
-        float4* dst = reinterpret_cast<float4*>(M.vrho32 + (size_t)v * DP);
-#pragma unroll
-        for (int h = 0; h < DP / 4; ++h) dst[h] = make_float4(r32[4 * h], r32[4 * h + 1], r32[4 * h + 2], r32[4 * h + 3]);
-        if (M.vinv32) {
-            // FP64 inverse, rounded once to FP32: every ray direction of the vertex
-            double rows[D];
-#pragma unroll
-            for (int k = 0; k < D; ++k) rows[k] = 0.0;
-#pragma unroll
-            for (int c = 0; c < D; ++c) {
-                double col[D];
-#pragma unroll
-                for (int k = 0; k < D; ++k) col[k] = (k == c) ? 1.0 : 0.0;
-                if (ok) lu_solve<D, double>(A, piv, col);
-#pragma unroll
-                for (int k = 0; k < D; ++k) {
-                    M.vinv32[(size_t)v * D * D + k * D + c] = (float)col[k];
-                    rows[k] += fabs(col[k]);
-                }
-            }
-            double ninv = 0;
-#pragma unroll
-            for (int k = 0; k < D; ++k) ninv = fmax(ninv, rows[k]);
-            M.vcond[v] = ok ? (float)(nrm * ninv) : INFINITY;
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------
-// fast kernel: one warp expands one vertex entirely in FP32
-// ---------------------------------------------------------------------------
-constexpr int FAST_WPB = 4;  // warps per block
-
-template <int D>
-__device__ __forceinline__ void load_pt32(const DevMesh& M, int j, float (&x)[(D <= 4) ? 4 : 8]) {
-    constexpr int DP = (D <= 4) ? 4 : 8;
-    const float4* p = reinterpret_cast<const float4*>(M.pts32 + (size_t)j * DP);
-#pragma unroll
-    for (int h = 0; h < DP / 4; ++h) {
-        float4 f = __ldg(p + h);
-        x[4 * h] = f.x; x[4 * h + 1] = f.y; x[4 * h + 2] = f.z; x[4 * h + 3] = f.w;
-    }
-}
-
-template <int D>
-__device__ __forceinline__ void load_pt32lo(const DevMesh& M, int j, float (&x)[(D <= 4) ? 4 : 8]) {
-    constexpr int DP = (D <= 4) ? 4 : 8;
-    const float4* p = reinterpret_cast<const float4*>(M.pts32lo + (size_t)j * DP);
-#pragma unroll
-    for (int h = 0; h < DP / 4; ++h) {
-        float4 f = __ldg(p + h);
-        x[4 * h] = f.x; x[4 * h + 1] = f.y; x[4 * h + 2] = f.z; x[4 * h + 3] = f.w;
-    }
-}
-
-template <int D>
-__global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsigned f0, unsigned f1,
-                                                               unsigned long long* fq, unsigned* nfq,
-                                                               unsigned fqcap, unsigned long long* fx,
-                                                               unsigned* nfx, unsigned fxcap) {
-    constexpr int R = D + 1;
-    constexpr int DP = (D <= 4) ? 4 : 8;
-    __shared__ float sInv[FAST_WPB][D][D];
-    __shared__ float sU[FAST_WPB][R][D];
-    __shared__ float sLam[FAST_WPB][R];
-    __shared__ float sLb[FAST_WPB][R];
-    __shared__ float sCond[FAST_WPB];
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const unsigned FULL = 0xFFFFFFFFu;
-    const unsigned nf = f1 - f0;
-    const float S32 = 5.9604645e-08f;                          // 2^-24
-    for (unsigned w = blockIdx.x * FAST_WPB + wib; w < nf; w += gridDim.x * FAST_WPB) {
-        const unsigned v = f0 + w;
-        int sig[R];
-#pragma unroll
-        for (int k = 0; k < R; ++k) sig[k] = M.vsig[(size_t)v * R + k];
-        const int vnew = M.vnew[v];
-        const int a = sig[0];
-        float xa[DP], xal[DP], rho[DP];
-        load_pt32<D>(M, a, xa);
-        load_pt32lo<D>(M, a, xal);
-        {
-            const float4* pr = reinterpret_cast<const float4*>(M.vrho32 + (size_t)v * DP);
-#pragma unroll
-            for (int h = 0; h < DP / 4; ++h) {
-                float4 f = pr[h];
-                rho[4 * h] = f.x; rho[4 * h + 1] = f.y; rho[4 * h + 2] = f.z; rho[4 * h + 3] = f.w;
-            }
-        }
-        // ---- the vertex's inverse (FP64 solve rounded to FP32, written by k_centers)
-        for (int x = lane; x < D * D; x += 32) (&sInv[wib][0][0])[x] = M.vinv32[(size_t)v * D * D + x];
-        if (lane == 0) sCond[wib] = M.vcond[v];
-        __syncwarp();
-        // ---- ray directions (lane m < R)
-        int active = 0;
-        if (lane < R) {
-            const int m = lane;
-            active = walkable<D>(M, sig, vnew, m) ? 1 : 0;
-            if (active && M.ecnt && ((M.ecnt[v] >> m) & 1u)) active = 0;  // both end points known
-            if (active) {
-                float u[D], db[D];
-#pragma unroll
-                for (int k = 0; k < D; ++k) { u[k] = 0.f; db[k] = 0.f; }
-                if (m >= 1) {
-#pragma unroll
-                    for (int k = 0; k < D; ++k) u[k] = -sInv[wib][k][m - 1];
-                } else {
-                    int b = -1;
-#pragma unroll
-                    for (int c = 0; c < D; ++c) {
-                        if (sig[c + 1] < M.n) {
-#pragma unroll
-                            for (int k = 0; k < D; ++k) u[k] += sInv[wib][k][c];
-                            if (b < 0) b = sig[c + 1];
-                        }
-                    }
-                    float xb[DP], xbl[DP];
-                    load_pt32<D>(M, b, xb);
-                    load_pt32lo<D>(M, b, xbl);
-#pragma unroll
-                    for (int k = 0; k < D; ++k) db[k] = (xb[k] - xa[k]) + (xbl[k] - xal[k]);
-                }
-                float nu = 0.f;
-#pragma unroll
-                for (int k = 0; k < D; ++k) nu = fmaf(u[k], u[k], nu);
-                nu = rsqrtf(nu);
-                float lam = 0.f, lb = 0.f;
-#pragma unroll
-                for (int k = 0; k < D; ++k) { u[k] *= nu; lam = fmaf(u[k], db[k], lam); lb += fabsf(db[k]); sU[wib][m][k] = u[k]; }
-                sLam[wib][m] = lam;
-                sLb[wib][m] = lb;
-            }
-        }
-        const unsigned rmask = __ballot_sync(FULL, active) & ((1u << R) - 1u);
-        __syncwarp();
-        const float cond = sCond[wib];
-        // directions come from the FP64 inverse rounded to FP32: relative error
-        // (2D+6) 2^-24 from the rounding and normalisation, plus the FP64
-        // solve's own error ~ D cond 2^-53
-        const float relu = (2.f * D + 6.f) * S32 + 8.f * D * cond * 1.1102230e-16f;
-        if (!(cond < 1e7f)) {  // too ill-conditioned for an FP32 decision: all rays exact
-            if (lane < R && active) {
-                count_add(M.cnt + C_RAYS);
-                const unsigned slot = atomicAdd(nfx, 1u);
-                if (slot < fxcap) fx[slot] = ((unsigned long long)v << 3) | (unsigned)lane;
-                else set_status(M, ST_QUEUE);
-            }
-            continue;
-        }
-        float R1 = 0.f, rmax = 0.f;
-#pragma unroll
-        for (int k = 0; k < D; ++k) { R1 += fabsf(rho[k]); rmax = fmaxf(rmax, fabsf(rho[k])); }
-        const float erho = 2.f * S32 * rmax;  // rho is the rounded FP64 centre offset
-        float u32[R][D], lam32[R], U1[R], LB[R];
-        float lo1[R], hi1[R], lo2[R];
-        int j1[R];
-#pragma unroll
-        for (int m = 0; m < R; ++m) {
-            U1[m] = 0.f; lam32[m] = 0.f; LB[m] = 0.f;
-#pragma unroll
-            for (int k = 0; k < D; ++k) u32[m][k] = 0.f;
-            if ((rmask >> m) & 1u) {
-#pragma unroll
-                for (int k = 0; k < D; ++k) { u32[m][k] = sU[wib][m][k]; U1[m] += fabsf(u32[m][k]); }
-                lam32[m] = sLam[wib][m];
-                LB[m] = sLb[wib][m];
-            }
-            lo1[m] = INFINITY; hi1[m] = INFINITY; lo2[m] = INFINITY; j1[m] = -1;
-        }
-        const float CN = (4.f * D + 20.f) * S32, CD = (4.f * D + 16.f) * S32;
-        const float TINY = (float)(4e-14 * M.xscale);
-        const int K = M.K;
-        // candidate list: the real generator of the vertex with the largest
-        // complete radius (every generator is on the current sphere, so any
-        // of their lists covers the same neighbourhood; the widest one makes
-        // the security test pass most often)
-        int own = a;
-        float sec_own = -1.f;
-        {
-            float sv = -1.f;
-            int it = -1;
-            if (lane < R && sig[lane < R ? lane : 0] < M.n) { it = sig[lane]; sv = __ldg(M.sec + it); }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                const float osv = __shfl_xor_sync(FULL, sv, off);
-                const int oit = __shfl_xor_sync(FULL, it, off);
-                if (osv > sv || (osv == sv && oit >= 0 && (it < 0 || oit < it))) { sv = osv; it = oit; }
-            }
-            own = it;
-            sec_own = sv;
-        }
-        const int* lst = M.knn + (size_t)own * K;
-        for (int c = lane; c < K; c += 32) {
-            const int j = __ldg(lst + c);
-            if (j < 0) continue;
-            bool insig = false;
-#pragma unroll
-            for (int s = 0; s < R; ++s) insig |= (j == sig[s]);
-            if (insig) continue;
-            float xj[DP], xjl[DP];
-            load_pt32<D>(M, j, xj);
-            load_pt32lo<D>(M, j, xjl);
-            float dl[D], A1 = 0.f, A2 = 0.f, A3 = 0.f, dr = 0.f;
-#pragma unroll
-            for (int k = 0; k < D; ++k) {
-                dl[k] = (xj[k] - xa[k]) + (xjl[k] - xal[k]);
-                A1 += fabsf(dl[k]);
-                A2 = fmaf(dl[k], dl[k], A2);
-                A3 = fmaf(fabsf(dl[k]), fabsf(rho[k]), A3);
-                dr = fmaf(dl[k], rho[k], dr);
-            }
-            const float num = fmaf(-2.f, dr, A2);
-            const float e_num = CN * (A2 + 2.f * A3) + 2.f * A1 * erho + TINY * (A1 + R1);
-#pragma unroll
-            for (int m = 0; m < R; ++m) {
-                if (!((rmask >> m) & 1u)) continue;
-                float du = 0.f, B = 0.f;
-#pragma unroll
-                for (int k = 0; k < D; ++k) { du = fmaf(dl[k], u32[m][k], du); B = fmaf(fabsf(dl[k]), fabsf(u32[m][k]), B); }
-                const float den = 2.f * (du - lam32[m]);
-                const float e_den = CD * (B + fabsf(lam32[m])) + 2.f * relu * (A1 + LB[m]) + TINY * U1[m];
-                float lo, hi;
-                if (den > e_den) {
-                    const float r = __fdividef(1.f, den);
-                    const float t = num * r;
-                    float et;
-                    if (e_den < 1e-3f * den) et = (e_num + fabsf(t) * e_den) * r * 1.0021f;
-                    else et = __fdividef(e_num + fabsf(t) * e_den, den - e_den) * 1.00001f;
-                    et += 8.f * S32 * fabsf(t);
-                    lo = t - et; hi = t + et;
-                } else if (den < -e_den) {
-                    continue;
-                } else {
-                    if (num - e_num > 0.f) {
-                        if (!(den + e_den > 0.f)) continue;
-                        lo = __fdividef(num - e_num, den + e_den) * 0.99999f; hi = INFINITY;
-                    } else {
-                        lo = -INFINITY; hi = INFINITY;
-                    }
-                }
-                if (lo < lo1[m] || (lo == lo1[m] && j < j1[m])) { lo2[m] = lo1[m]; lo1[m] = lo; hi1[m] = hi; j1[m] = j; }
-                else if (lo < lo2[m]) lo2[m] = lo;
-            }
-        }
-        // ---- warp reduction of the per-ray top-2
-#pragma unroll
-        for (int m = 0; m < R; ++m) {
-            if (!((rmask >> m) & 1u)) continue;
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                const float olo1 = __shfl_xor_sync(FULL, lo1[m], off);
-                const float ohi1 = __shfl_xor_sync(FULL, hi1[m], off);
-                const float olo2 = __shfl_xor_sync(FULL, lo2[m], off);
-                const int oj1 = __shfl_xor_sync(FULL, j1[m], off);
-                const bool take = (olo1 < lo1[m]) || (olo1 == lo1[m] && oj1 >= 0 && (j1[m] < 0 || oj1 < j1[m]));
-                if (take) { lo2[m] = fminf(lo1[m], olo2); lo1[m] = olo1; hi1[m] = ohi1; j1[m] = oj1; }
-                else { lo2[m] = fminf(lo2[m], olo1); }
-            }
-        }
-        // ---- per-ray decision on lane m
-        if (lane < R && ((rmask >> lane) & 1u)) {
-            const int m = lane;
-            count_add(M.cnt + C_RAYS);
-            float u[D];
-#pragma unroll
-            for (int k = 0; k < D; ++k) u[k] = sU[wib][m][k];
-            float clo1 = 0.f, chi1 = 0.f, clo2 = 0.f;
-            int cj1 = -1;
-#pragma unroll
-            for (int mm = 0; mm < R; ++mm)
-                if (mm == m) { clo1 = lo1[mm]; chi1 = hi1[mm]; clo2 = lo2[mm]; cj1 = j1[mm]; }
-            // boundary planes in FP32 with the same error model
-            float plo1 = INFINITY, phi1 = INFINITY, plo2 = INFINITY;
-            int pj1 = -1;
-#pragma unroll
-            for (int p = 0; p < 2 * D; ++p) {
-                const int it = M.n + p;
-                bool ex = false;
-#pragma unroll
-                for (int s = 0; s < R; ++s) ex |= (sig[s] == it);
-                if (ex) continue;
-                const int k = p >> 1;
-                const bool upper = (p & 1) == 0;
-                const float uk = upper ? u[k] : -u[k];
-                const float hk = (float)M.hi[k], lk = (float)M.lo[k];
-                const float ck = xa[k] + (xal[k] + rho[k]);
-                const float num = upper ? (hk - ck) : (ck - lk);
-                const float e_num = 4.f * S32 * (fabsf(hk) + fabsf(lk) + fabsf(xa[k]) + fabsf(rho[k])) + erho + TINY;
-                const float e_den = relu + 2.f * S32 * fabsf(uk);
-                float lo, hi;
-                if (uk > e_den) {
-                    const float t = __fdividef(num, uk);
-                    const float et = __fdividef(e_num + fabsf(t) * e_den, uk - e_den) * 1.00001f + 8.f * S32 * fabsf(t);
-                    lo = t - et; hi = t + et;
-                } else if (uk < -e_den) {
-                    continue;
-                } else {
-                    if (num - e_num > 0.f) { lo = __fdividef(num - e_num, fabsf(uk) + e_den) * 0.99999f; hi = INFINITY; }
-                    else { lo = -INFINITY; hi = INFINITY; }
-                }
-                if (lo < plo1) { plo2 = plo1; plo1 = lo; phi1 = hi; pj1 = it; }
-                else if (lo < plo2) plo2 = lo;
-            }
-            int win;
-            float blo, bhi, second;
-            if (cj1 >= 0 && clo1 <= plo1) { win = cj1; blo = clo1; bhi = chi1; second = fminf(clo2, plo1); }
-            else { win = pj1; blo = plo1; bhi = phi1; second = fminf(plo2, clo1); }
-            bool queue = false, exact = false;
-            if (!(win >= 0 && bhi < second)) {
-                count_add(M.cnt + C_UNCERT);
-                exact = true;
-            } else {
-                // security: the new empty sphere must lie inside the complete radius of the list
-                const float t = 0.5f * (blo + bhi), et = 0.5f * (bhi - blo);
-                float db[D];
-#pragma unroll
-                for (int k = 0; k < D; ++k) db[k] = 0.f;
-                if (m == 0) {
-                    int b = -1;
-#pragma unroll
-                    for (int s = 1; s <= D; ++s) if (b < 0 && sig[s] < M.n) b = sig[s];
-                    float xb[DP], xbl[DP];
-                    load_pt32<D>(M, b, xb);
-                    load_pt32lo<D>(M, b, xbl);
-#pragma unroll
-                    for (int k = 0; k < D; ++k) db[k] = (xb[k] - xa[k]) + (xbl[k] - xal[k]);
-                }
-                float xo[DP], xol[DP];
-                load_pt32<D>(M, own, xo);
-                load_pt32lo<D>(M, own, xol);
-                float c2 = 0.f, r2 = 0.f, cm = 0.f;
-#pragma unroll
-                for (int k = 0; k < D; ++k) {
-                    const float cc = fmaf(t, u[k], rho[k]);
-                    const float co = cc - ((xo[k] - xa[k]) + (xol[k] - xal[k]));
-                    c2 = fmaf(co, co, c2);
-                    const float wv = db[k] - cc;
-                    r2 = fmaf(wv, wv, r2);
-                    cm = fmaxf(cm, fabsf(cc));
-                }
-                const float ec = erho + fabsf(t) * relu + et + 4.f * S32 * (rmax + fabsf(t)) + 3.f * TINY;
-                const float lhs = sqrtf(c2) + sqrtf(r2) + 4.f * sqrtf((float)D) * ec + 4.f * S32 * cm;
-                const float seco = sec_own;
-                if (!(t > 0.f) || !(lhs < seco * (1.f - 1e-5f))) {
-                    count_add(M.cnt + C_INSECURE);
-                    queue = true;
-                }
-            }
-            if (exact) {
-                const unsigned slot = atomicAdd(nfx, 1u);
-                if (slot < fxcap) fx[slot] = ((unsigned long long)v << 3) | (unsigned)m;
-                else set_status(M, ST_QUEUE);
-            } else if (queue) {
-                const unsigned slot = atomicAdd(nfq, 1u);
-                if (slot < fqcap) fq[slot] = ((unsigned long long)v << 3) | (unsigned)m;
-                else set_status(M, ST_QUEUE);
-            } else {
-                int ns[R];
-                make_sig<D>(sig, m, win, ns);
-                bool is_new;
-                vertex_insert<D>(M, ns, win, is_new);
-            }
-        }
-        __syncwarp();
-    }
-}
-
-// ---------------------------------------------------------------------------
-// warp fallback: one warp per ray whose new sphere left the list's complete
-// radius.  The ray is re-run in FP32 over the candidate list and then over
-// the whole tree (warp-uniform traversal, one leaf point per lane), with the
-// same per-candidate error bounds; the tree pass is exhaustive up to the
-// conservative box test, so no security test is needed.  Rays that remain
-// uncertified go to the FP64 kernel.
-// ---------------------------------------------------------------------------
-template <int D>
-__device__ __forceinline__ void cand32(const DevMesh& M, int j, const float* xa, const float* xal, const float* rho,
-                                       float R1, float erho, const float* u, float lam, float U1, float LB,
-                                       float relu, float& lo, float& hi, bool& valid) {
-    constexpr int DP = (D <= 4) ? 4 : 8;
-    const float S32 = 5.9604645e-08f;
-    const float CN = (4.f * D + 20.f) * S32, CD = (4.f * D + 16.f) * S32;
-    const float TINY = (float)(4e-14 * M.xscale);
-    float xj[DP], xjl[DP];
-    load_pt32<D>(M, j, xj);
-    load_pt32lo<D>(M, j, xjl);
-    float A1 = 0.f, A2 = 0.f, A3 = 0.f, dr = 0.f, du = 0.f, B = 0.f;
-#pragma unroll
-    for (int k = 0; k < D; ++k) {
-        const float dl = (xj[k] - xa[k]) + (xjl[k] - xal[k]);
-        A1 += fabsf(dl);
-        A2 = fmaf(dl, dl, A2);
-        A3 = fmaf(fabsf(dl), fabsf(rho[k]), A3);
-        dr = fmaf(dl, rho[k], dr);
-        du = fmaf(dl, u[k], du);
-        B = fmaf(fabsf(dl), fabsf(u[k]), B);
-    }
-    const float num = fmaf(-2.f, dr, A2);
-    const float e_num = CN * (A2 + 2.f * A3) + 2.f * A1 * erho + TINY * (A1 + R1);
-    const float den = 2.f * (du - lam);
-    const float e_den = CD * (B + fabsf(lam)) + 2.f * relu * (A1 + LB) + TINY * U1;
-    valid = true;
-    if (den > e_den) {
-        const float r = __fdividef(1.f, den);
-        const float t = num * r;
-        float et;
-        if (e_den < 1e-3f * den) et = (e_num + fabsf(t) * e_den) * r * 1.0021f;
-        else et = __fdividef(e_num + fabsf(t) * e_den, den - e_den) * 1.00001f;
-        et += 8.f * S32 * fabsf(t);
-        lo = t - et; hi = t + et;
-    } else if (den < -e_den) {
-        valid = false;
-    } else if (num - e_num > 0.f) {
-        if (!(den + e_den > 0.f)) { valid = false; return; }
-        lo = __fdividef(num - e_num, den + e_den) * 0.99999f; hi = INFINITY;
-    } else {
-        lo = -INFINITY; hi = INFINITY;
-    }
-}
-
-__device__ __forceinline__ void top2_merge(float& lo1, float& hi1, int& j1, float& lo2, float olo1, float ohi1,
-                                           int oj1, float olo2) {
-    const bool take = (olo1 < lo1) || (olo1 == lo1 && oj1 >= 0 && (j1 < 0 || oj1 < j1));
-    if (take) { lo2 = fminf(lo1, olo2); lo1 = olo1; hi1 = ohi1; j1 = oj1; }
-    else { lo2 = fminf(lo2, olo1); }
-}
-
-__device__ __forceinline__ void top2_warp(float& lo1, float& hi1, int& j1, float& lo2) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const float a = __shfl_xor_sync(0xFFFFFFFFu, lo1, off);
-        const float b = __shfl_xor_sync(0xFFFFFFFFu, hi1, off);
-        const float c = __shfl_xor_sync(0xFFFFFFFFu, lo2, off);
-        const int e = __shfl_xor_sync(0xFFFFFFFFu, j1, off);
-        top2_merge(lo1, hi1, j1, lo2, a, b, e, c);
-    }
-}
-
-__device__ __forceinline__ void top2_add(float& lo1, float& hi1, int& j1, float& lo2, float lo, float hi, int j) {
-    if (j == j1) return;
-    if (lo < lo1 || (lo == lo1 && (j1 < 0 || j < j1))) { lo2 = lo1; lo1 = lo; hi1 = hi; j1 = j; }
-    else if (lo < lo2) lo2 = lo;
-}
-
-constexpr int FB_WPB = 4;
-
-template <int D>
-__global__ void __launch_bounds__(FB_WPB * 32) k_fallback_warp(DevMesh M, const unsigned long long* fq,
-                                                               const unsigned* nfq, unsigned fqcap,
-                                                               unsigned long long* fx, unsigned* nfx,
-                                                               unsigned fxcap) {
-    constexpr int R = D + 1;
-    constexpr int DP = (D <= 4) ? 4 : 8;
-    __shared__ int sstack[FB_WPB][64];
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const float S32 = 5.9604645e-08f;
-    const unsigned nq = min(*nfq, fqcap);
-    int* stk = sstack[wib];
-    for (unsigned w = blockIdx.x * FB_WPB + wib; w < nq; w += gridDim.x * FB_WPB) {
-        const unsigned long long e = fq[w];
-        const unsigned v = (unsigned)(e >> 3);
-        const int m = (int)(e & 7);
-        if (lane == 0) count_add(M.cnt + C_FALLBACK);
-        int sig[R];
-#pragma unroll
-        for (int k = 0; k < R; ++k) sig[k] = M.vsig[(size_t)v * R + k];
-        const int a = sig[0];
-        float xa[DP], xal[DP], rho[DP];
-        load_pt32<D>(M, a, xa);
-        load_pt32lo<D>(M, a, xal);
-        {
-            const float4* pr = reinterpret_cast<const float4*>(M.vrho32 + (size_t)v * DP);
-#pragma unroll
-            for (int h = 0; h < DP / 4; ++h) {
-                float4 f = pr[h];
-                rho[4 * h] = f.x; rho[4 * h + 1] = f.y; rho[4 * h + 2] = f.z; rho[4 * h + 3] = f.w;
-            }
-        }
-        const float* inv = M.vinv32 + (size_t)v * D * D;
-        float u[D], db[D];
-#pragma unroll
-        for (int k = 0; k < D; ++k) { u[k] = 0.f; db[k] = 0.f; }
-        if (m >= 1) {
-#pragma unroll
-            for (int k = 0; k < D; ++k) u[k] = -inv[k * D + (m - 1)];
-        } else {
-            int b = -1;
-#pragma unroll
-            for (int c = 0; c < D; ++c) {
-                if (sig[c + 1] < M.n) {
-#pragma unroll
-                    for (int k = 0; k < D; ++k) u[k] += inv[k * D + c];
-                    if (b < 0) b = sig[c + 1];
-                }
-            }
-            float xb[DP], xbl[DP];
-            load_pt32<D>(M, b, xb);
-            load_pt32lo<D>(M, b, xbl);
-#pragma unroll
-            for (int k = 0; k < D; ++k) db[k] = (xb[k] - xa[k]) + (xbl[k] - xal[k]);
-        }
-        float nu = 0.f;
-#pragma unroll
-        for (int k = 0; k < D; ++k) nu = fmaf(u[k], u[k], nu);
-        nu = rsqrtf(nu);
-        float lam = 0.f, LB = 0.f, U1 = 0.f, R1 = 0.f, rmax = 0.f;
-#pragma unroll
-        for (int k = 0; k < D; ++k) {
-            u[k] *= nu;
-            lam = fmaf(u[k], db[k], lam);
-            LB += fabsf(db[k]);
-            U1 += fabsf(u[k]);
-            R1 += fabsf(rho[k]);
-            rmax = fmaxf(rmax, fabsf(rho[k]));
-        }
-        const float cond = M.vcond[v];
-        const float relu = (2.f * D + 6.f) * S32 + 8.f * D * cond * 1.1102230e-16f;
-        const float erho = 2.f * S32 * rmax;
-        float lo1 = INFINITY, hi1 = INFINITY, lo2 = INFINITY;
-        int j1 = -1;
-        // planes (lane 0)
-        if (lane == 0) {
-            const float TINY = (float)(4e-14 * M.xscale);
-#pragma unroll
-            for (int p = 0; p < 2 * D; ++p) {
-                const int it = M.n + p;
-                bool ex = false;
-#pragma unroll
-                for (int q = 0; q < R; ++q) ex |= (sig[q] == it);
-                if (ex) continue;
-                const int k = p >> 1;
-                const bool upper = (p & 1) == 0;
-                const float uk = upper ? u[k] : -u[k];
-                const float hk = (float)M.hi[k], lk = (float)M.lo[k];
-                const float ck = xa[k] + (xal[k] + rho[k]);
-                const float num = upper ? (hk - ck) : (ck - lk);
-                const float e_num = 4.f * S32 * (fabsf(hk) + fabsf(lk) + fabsf(xa[k]) + fabsf(rho[k])) + erho + TINY;
-                const float e_den = relu + 2.f * S32 * fabsf(uk);
-                float lo, hi;
-                if (uk > e_den) {
-                    const float t = __fdividef(num, uk);
-                    const float et = __fdividef(e_num + fabsf(t) * e_den, uk - e_den) * 1.00001f + 8.f * S32 * fabsf(t);
-                    lo = t - et; hi = t + et;
-                } else if (uk < -e_den) {
-                    continue;
-                } else {
-                    if (num - e_num > 0.f) { lo = __fdividef(num - e_num, fabsf(uk) + e_den) * 0.99999f; hi = INFINITY; }
-                    else { lo = -INFINITY; hi = INFINITY; }
-                }
-                top2_add(lo1, hi1, j1, lo2, lo, hi, it);
-            }
-        }
-        // candidate list of the anchor (good initial ball)
-        if (M.K > 0) {
-            const int* lst = M.knn + (size_t)a * M.K;
-            for (int c = lane; c < M.K; c += 32) {
-                const int j = __ldg(lst + c);
-                if (j < 0) continue;
-                bool insig = false;
-#pragma unroll
-                for (int q = 0; q < R; ++q) insig |= (j == sig[q]);
-                if (insig) continue;
-                float lo, hi;
-                bool ok;
-                cand32<D>(M, j, xa, xal, rho, R1, erho, u, lam, U1, LB, relu, lo, hi, ok);
-                if (ok) top2_add(lo1, hi1, j1, lo2, lo, hi, j);
-            }
-        }
-        top2_warp(lo1, hi1, j1, lo2);
-        // exhaustive tree pass with the shrinking ball
-        int sp = 1;
-        if (lane == 0) stk[0] = 1;
-        __syncwarp();
-        bool overflow = false;
-        while (sp > 0) {
-            const int node = stk[--sp];
-            __syncwarp();
-            // ball of the current upper bound, relative to x_a
-            const float tp = hi1;
-            if (isfinite(tp)) {
-                float r2 = 0.f, bd2 = 0.f;
-                const float* blo = M.blo + (size_t)node * DP;
-                const float* bhi = M.bhi + (size_t)node * DP;
-#pragma unroll
-                for (int k = 0; k < D; ++k) {
-                    const float off = fmaf(tp, u[k], rho[k]);
-                    const float w2 = db[k] - off;
-                    r2 = fmaf(w2, w2, r2);
-                    const float ck = xa[k] + (xal[k] + off);
-                    const float l = __ldg(blo + k), h = __ldg(bhi + k);
-                    const float ex = ck < l ? l - ck : (ck > h ? ck - h : 0.f);
-                    bd2 = fmaf(ex, ex, bd2);
-                }
-                const float rr = sqrtf(r2) * 1.0001f + 1e-6f * (float)M.xscale + 1e-4f * fabsf(tp);
-                if (bd2 > rr * rr) continue;
-            }
-            if (node >= M.P) {
-                const int l = node - M.P;
-                if (l >= M.nleaves) continue;
-                const int s0 = l * M.leaf, s1 = min(s0 + M.leaf, M.n);
-                for (int base = s0; base < s1; base += 32) {
-                    const int j = base + lane;
-                    if (j < s1) {
-                        bool insig = false;
-#pragma unroll
-                        for (int q = 0; q < R; ++q) insig |= (j == sig[q]);
-                        if (!insig) {
-                            float lo, hi;
-                            bool ok;
-                            cand32<D>(M, j, xa, xal, rho, R1, erho, u, lam, U1, LB, relu, lo, hi, ok);
-                            if (ok) top2_add(lo1, hi1, j1, lo2, lo, hi, j);
-                        }
-                    }
-                }
-                top2_warp(lo1, hi1, j1, lo2);
-            } else {
-                if (sp + 2 > 64) { overflow = true; break; }
-                if (lane == 0) { stk[sp] = 2 * node + 1; stk[sp + 1] = 2 * node; }
-                sp += 2;
-                __syncwarp();
-            }
-        }
-        if (lane == 0) {
-            if (!overflow && j1 >= 0 && hi1 < lo2) {
-                int ns[R];
-                make_sig<D>(sig, m, j1, ns);
-                bool is_new;
-                vertex_insert<D>(M, ns, j1, is_new);
-            } else {
-                count_add(M.cnt + C_UNCERT);
-                const unsigned slot = atomicAdd(nfx, 1u);
-                if (slot < fxcap) fx[slot] = e;
-                else set_status(M, ST_QUEUE);
-            }
-        }
-        __syncwarp();
-    }
-}
-
-// ---------------------------------------------------------------------------
-// host launchers
-// ---------------------------------------------------------------------------
-template <int D>
-static void launch_register_t(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st) {
-    const unsigned long long total = (unsigned long long)(v1 - v0) * (D + 1);
-    if (!total) return;
-    unsigned long long blocks = (total + 255) / 256;
-    if (blocks > (unsigned long long)nsm * 32) blocks = (unsigned long long)nsm * 32;
-    k_register_edges<D><<<(unsigned)blocks, 256, 0, st>>>(M, v0, v1);
-}
-template <int D>
-static void launch_centers_t(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st) {
-    if (v1 <= v0) return;
-    unsigned blocks = (v1 - v0 + 127) / 128;
-    if (blocks > (unsigned)nsm * 16) blocks = (unsigned)nsm * 16;
-    k_centers<D><<<blocks, 128, 0, st>>>(M, v0, v1);
-}
-template <int D>
-static void launch_descent_t(const DevMesh& M, int stride, int nseeds, unsigned long long seed, cudaStream_t st) {
-    if (nseeds <= 0) return;
-    k_descent<D><<<(nseeds + 127) / 128, 128, 0, st>>>(M, stride, nseeds, seed);
-}
-template <int D>
-static void launch_plain_t(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cudaStream_t st) {
-    unsigned long long total = (unsigned long long)(f1 - f0) * (D + 1);
-    if (!total) return;
-    unsigned long long blocks = (total + 127) / 128;
-    blocks = blocks > (unsigned long long)nsm * 64 ? (unsigned long long)nsm * 64 : blocks;
-    k_expand_plain<D><<<(unsigned)blocks, 128, 0, st>>>(M, f0, f1);
-}
-template <int D>
-static void launch_fast_t(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq,
-                          unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm,
-                          cudaStream_t st) {
-    unsigned nf = f1 - f0;
-    if (!nf) return;
-    unsigned blocks = (nf + FAST_WPB - 1) / FAST_WPB;
-    if (blocks > (unsigned)nsm * 32) blocks = (unsigned)nsm * 32;
-    k_expand_fast<D><<<blocks, FAST_WPB * 32, 0, st>>>(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap);
-}
-template <int D>
-static void launch_fallback_warp_t(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq,
-                                   unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx,
-                                   unsigned fxcap, int nsm, cudaStream_t st) {
-    if (!maxq) return;
-    unsigned blocks = (maxq + FB_WPB - 1) / FB_WPB;
-    if (blocks > (unsigned)nsm * 32) blocks = (unsigned)nsm * 32;
-    k_fallback_warp<D><<<blocks, FB_WPB * 32, 0, st>>>(M, fq, nfq, fqcap, fx, nfx, fxcap);
-}
-template <int D>
-static void launch_fallback_t(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq,
-                              int nsm, cudaStream_t st) {
-    if (!maxq) return;
-    unsigned blocks = (maxq + 127) / 128;
-    if (blocks > (unsigned)nsm * 16) blocks = (unsigned)nsm * 16;
-    k_fallback<D><<<blocks, 128, 0, st>>>(M, fq, nfq, maxq);
-}
-
-#define HV_DISPATCH(d, CALL)                      \
-    switch (d) {                                  \
-        case 2: { constexpr int DD = 2; CALL; } break; \
-        case 3: { constexpr int DD = 3; CALL; } break; \
-        case 4: { constexpr int DD = 4; CALL; } break; \
-        case 5: { constexpr int DD = 5; CALL; } break; \
-        case 6: { constexpr int DD = 6; CALL; } break; \
-        default: break;                           \
-    }
+void launch_register_d2(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+void launch_register_d3(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+void launch_register_d4(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+void launch_register_d5(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+void launch_register_d6(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+void launch_centers_d2(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+void launch_centers_d3(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+void launch_centers_d4(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+void launch_centers_d5(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+void launch_centers_d6(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+void launch_descent_d2(const DevMesh& M, int stride, int nseeds, unsigned long long seed, int* failed, unsigned* nfailed, int nsm, cudaStream_t st);
+void launch_descent_d3(const DevMesh& M, int stride, int nseeds, unsigned long long seed, int* failed, unsigned* nfailed, int nsm, cudaStream_t st);
+void launch_descent_d4(const DevMesh& M, int stride, int nseeds, unsigned long long seed, int* failed, unsigned* nfailed, int nsm, cudaStream_t st);
+void launch_descent_d5(const DevMesh& M, int stride, int nseeds, unsigned long long seed, int* failed, unsigned* nfailed, int nsm, cudaStream_t st);
+void launch_descent_d6(const DevMesh& M, int stride, int nseeds, unsigned long long seed, int* failed, unsigned* nfailed, int nsm, cudaStream_t st);
+void launch_plain_d2(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cudaStream_t st);
+void launch_plain_d3(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cudaStream_t st);
+void launch_plain_d4(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cudaStream_t st);
+void launch_plain_d5(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cudaStream_t st);
+void launch_plain_d6(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cudaStream_t st);
+void launch_fast_d2(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq, unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
+void launch_fast_d3(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq, unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
+void launch_fast_d4(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq, unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
+void launch_fast_d5(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq, unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
+void launch_fast_d6(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq, unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
+void launch_fallback_warp_d2(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
+void launch_fallback_warp_d3(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
+void launch_fallback_warp_d4(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
+void launch_fallback_warp_d5(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
+void launch_fallback_warp_d6(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
+void launch_fallback_d2(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm, cudaStream_t st);
+void launch_fallback_d3(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm, cudaStream_t st);
+void launch_fallback_d4(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm, cudaStream_t st);
+void launch_fallback_d5(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm, cudaStream_t st);
+void launch_fallback_d6(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm, cudaStream_t st);
 
 void launch_register_edges(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st) {
-    HV_DISPATCH(M.d, (launch_register_t<DD>(M, v0, v1, nsm, st)));
+    switch (M.d) {
+        case 2: launch_register_d2(M, v0, v1, nsm, st); break;
+        case 3: launch_register_d3(M, v0, v1, nsm, st); break;
+        case 4: launch_register_d4(M, v0, v1, nsm, st); break;
+        case 5: launch_register_d5(M, v0, v1, nsm, st); break;
+        case 6: launch_register_d6(M, v0, v1, nsm, st); break;
+        default: break;
+    }
 }
 void launch_centers(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st) {
-    HV_DISPATCH(M.d, (launch_centers_t<DD>(M, v0, v1, nsm, st)));
+    switch (M.d) {
+        case 2: launch_centers_d2(M, v0, v1, nsm, st); break;
+        case 3: launch_centers_d3(M, v0, v1, nsm, st); break;
+        case 4: launch_centers_d4(M, v0, v1, nsm, st); break;
+        case 5: launch_centers_d5(M, v0, v1, nsm, st); break;
+        case 6: launch_centers_d6(M, v0, v1, nsm, st); break;
+        default: break;
+    }
 }
-void launch_descent(const DevMesh& M, int stride, int nseeds, unsigned long long seed, cudaStream_t st) {
-    HV_DISPATCH(M.d, (launch_descent_t<DD>(M, stride, nseeds, seed, st)));
+void launch_descent(const DevMesh& M, int stride, int nseeds, unsigned long long seed, int* failed, unsigned* nfailed, int nsm, cudaStream_t st) {
+    switch (M.d) {
+        case 2: launch_descent_d2(M, stride, nseeds, seed, failed, nfailed, nsm, st); break;
+        case 3: launch_descent_d3(M, stride, nseeds, seed, failed, nfailed, nsm, st); break;
+        case 4: launch_descent_d4(M, stride, nseeds, seed, failed, nfailed, nsm, st); break;
+        case 5: launch_descent_d5(M, stride, nseeds, seed, failed, nfailed, nsm, st); break;
+        case 6: launch_descent_d6(M, stride, nseeds, seed, failed, nfailed, nsm, st); break;
+        default: break;
+    }
 }
 void launch_expand_plain(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cudaStream_t st) {
-    HV_DISPATCH(M.d, (launch_plain_t<DD>(M, f0, f1, nsm, st)));
+    switch (M.d) {
+        case 2: launch_plain_d2(M, f0, f1, nsm, st); break;
+        case 3: launch_plain_d3(M, f0, f1, nsm, st); break;
+        case 4: launch_plain_d4(M, f0, f1, nsm, st); break;
+        case 5: launch_plain_d5(M, f0, f1, nsm, st); break;
+        case 6: launch_plain_d6(M, f0, f1, nsm, st); break;
+        default: break;
+    }
 }
-void launch_expand_fast(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq,
-                        unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm,
-                        cudaStream_t st) {
-    HV_DISPATCH(M.d, (launch_fast_t<DD>(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap, nsm, st)));
+void launch_expand_fast(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq, unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st) {
+    switch (M.d) {
+        case 2: launch_fast_d2(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap, nsm, st); break;
+        case 3: launch_fast_d3(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap, nsm, st); break;
+        case 4: launch_fast_d4(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap, nsm, st); break;
+        case 5: launch_fast_d5(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap, nsm, st); break;
+        case 6: launch_fast_d6(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap, nsm, st); break;
+        default: break;
+    }
 }
-void launch_fallback_warp(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap,
-                          unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm,
-                          cudaStream_t st) {
-    HV_DISPATCH(M.d, (launch_fallback_warp_t<DD>(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, nsm, st)));
+void launch_fallback_warp(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st) {
+    switch (M.d) {
+        case 2: launch_fallback_warp_d2(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, nsm, st); break;
+        case 3: launch_fallback_warp_d3(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, nsm, st); break;
+        case 4: launch_fallback_warp_d4(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, nsm, st); break;
+        case 5: launch_fallback_warp_d5(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, nsm, st); break;
+        case 6: launch_fallback_warp_d6(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, nsm, st); break;
+        default: break;
+    }
 }
-void launch_fallback(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm,
-                     cudaStream_t st) {
-    HV_DISPATCH(M.d, (launch_fallback_t<DD>(M, fq, nfq, maxq, nsm, st)));
+void launch_fallback(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm, cudaStream_t st) {
+    switch (M.d) {
+        case 2: launch_fallback_d2(M, fq, nfq, maxq, nsm, st); break;
+        case 3: launch_fallback_d3(M, fq, nfq, maxq, nsm, st); break;
+        case 4: launch_fallback_d4(M, fq, nfq, maxq, nsm, st); break;
+        case 5: launch_fallback_d5(M, fq, nfq, maxq, nsm, st); break;
+        case 6: launch_fallback_d6(M, fq, nfq, maxq, nsm, st); break;
+        default: break;
+    }
 }
 
 }  // namespace hv

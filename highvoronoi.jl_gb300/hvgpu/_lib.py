@@ -82,6 +82,7 @@ def load(path: str | None = None):
         L.hv_mesh_build_device.argtypes = [P, I, I64, P, dp, dp, ctypes.POINTER(Params), ctypes.POINTER(P)]
         L.hv_mesh_build_device.restype = I
         L.hv_mesh_counts.argtypes = [P, ip, ip]; L.hv_mesh_counts.restype = I
+        L.hv_autotune.argtypes = [P, I, I64, P, dp, dp, ctypes.POINTER(Params)]; L.hv_autotune.restype = I
         L.hv_mesh_vertices.argtypes = [P, ip, dp]; L.hv_mesh_vertices.restype = I
         L.hv_mesh_neighbors.argtypes = [P, ip, ip]; L.hv_mesh_neighbors.restype = I
         L.hv_integrate_polygon.argtypes = [P, dp, dp]; L.hv_integrate_polygon.restype = I
@@ -122,6 +123,18 @@ class Context:
 
     def error(self) -> str:
         return load().hv_last_error(self._h).decode()
+
+    def autotune(self, d: int, n: int, pts=None, lo=None, hi=None) -> dict:
+        """Runs hv_autotune; the winner is cached in this context per (d, log2 n)."""
+        lo = np.ascontiguousarray(np.zeros(d) if lo is None else lo, dtype=np.float64)
+        hi = np.ascontiguousarray(np.ones(d) if hi is None else hi, dtype=np.float64)
+        p = Params()
+        ptr = None
+        if pts is not None:
+            pts = np.ascontiguousarray(pts, dtype=np.float64)
+            ptr = pts.ctypes.data_as(ctypes.c_void_p)
+        self.check(load().hv_autotune(self._h, d, n, ptr, dptr(lo), dptr(hi), ctypes.byref(p)), "hv_autotune")
+        return {k: getattr(p, k) for k, _ in Params._fields_}
 
     def check(self, rc: int, what: str):
         if rc != HV_OK:

@@ -72,9 +72,10 @@ class VoronoiGeometry:
     """Vertex search (and optionally integration) of the Voronoi mesh of ``xs``.
 
     ``xs`` is an (n, d) array (row i = generator i+1) or a list of points.
-    ``search_settings`` accepts ``method`` (RCGPU default, RCGPUPlain) and the
+    ``search_settings`` accepts ``method`` (RCGPU default, RCGPUPlain), the
     GPU knobs ``knn``, ``leaf_size``, ``seed_stride``, ``edge_dedup``,
-    ``capacity_factor``, ``seed``.  ``mc_accurate=(ndir, 1, recycle)`` sets the
+    ``capacity_factor``, ``seed``, and ``autotune=True`` (tune the knobs for
+    this (d, n) once per context).  ``mc_accurate=(ndir, 1, recycle)`` sets the
     directions per cell of VI_HEURISTIC_MC (src/geometry.jl:70-72).
     """
 
@@ -93,6 +94,7 @@ class VoronoiGeometry:
         method = ss.pop("method", RCGPU)
         if not isinstance(method, RaycastMethod):
             raise ValueError(f"unsupported raycast method {method!r} on the GPU path")
+        autotune = bool(ss.pop("autotune", False))
         allowed = {"knn", "leaf_size", "seed_stride", "edge_dedup", "capacity_factor", "seed", "rays_per_warp"}
         unknown = set(ss) - allowed
         if unknown:
@@ -101,6 +103,9 @@ class VoronoiGeometry:
         self.boundary = b
         self.nodes = pts
         self.method = method
+        if autotune and method.code == _lib.HV_METHOD_FAST:
+            # tuned on synthetic points of the same (d, n); cached in the context
+            self.ctx.autotune(d, n, lo=b.lo, hi=b.hi)
         self.params = _lib.make_params(method.code, **ss)
         self.mesh = _lib.Mesh(self.ctx, pts, b.lo, b.hi, self.params)
         self.integrator = integrator

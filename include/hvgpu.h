@@ -116,6 +116,14 @@ int hv_mesh_build(hv_ctx* ctx, int d, int64_t n, const double* pts, const double
 int hv_mesh_build_device(hv_ctx* ctx, int d, int64_t n, const double* d_pts, const double* lo,
                          const double* hi, const hv_params* params, hv_mesh** out);
 
+/* Autotuner: times hv_mesh_build over a small grid of knn x leaf_size x
+ * seed_stride (x rays_per_warp) on the given points (pts == NULL: uniform
+ * points in the box) and writes the fastest settings to *out.  The result is
+ * cached in the context per (d, round(log2 n)); later builds on the context
+ * whose params leave those fields at 0 use the cached values. */
+int hv_autotune(hv_ctx* ctx, int d, int64_t n, const double* pts, const double* lo, const double* hi,
+                hv_params* out);
+
 /* Sizes of the caller's buffers: vertices, and the total neighbour count. */
 int hv_mesh_counts(hv_mesh* mesh, int64_t* nverts, int64_t* nnbr_total);
 /* Vertex records sorted lexicographically by signature: sig is (d+1) x V
