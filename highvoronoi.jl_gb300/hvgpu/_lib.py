@@ -89,6 +89,8 @@ def load(path: str | None = None):
         L.hv_integrate_heuristic_mc.argtypes = [P, I, U64, dp, dp]; L.hv_integrate_heuristic_mc.restype = I
         L.hv_mesh_stats.argtypes = [P, ctypes.POINTER(Stats)]; L.hv_mesh_stats.restype = I
         L.hv_mesh_free.argtypes = [P]; L.hv_mesh_free.restype = I
+        L.hv_integrate_heuristic_mc_noalloc.argtypes = [I, I64, P, dp, dp, P, P, I64, I, I, U64, P, P, P]
+        L.hv_integrate_heuristic_mc_noalloc.restype = I
         _lib = L
         return L
 
@@ -99,6 +101,20 @@ def dptr(a: np.ndarray):
 
 def iptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+
+def heuristic_mc_noalloc(d, n, d_pts, lo, hi, d_nbr_off, d_nbr, nnbr, max_degree, ndir, seed, d_vol, d_area,
+                        stream=0):
+    """hv_integrate_heuristic_mc_noalloc on caller-owned device buffers (raw
+    pointers); raises HVError on a non-zero return code."""
+    lo = np.ascontiguousarray(lo, dtype=np.float64)
+    hi = np.ascontiguousarray(hi, dtype=np.float64)
+    rc = load().hv_integrate_heuristic_mc_noalloc(d, n, d_pts, dptr(lo), dptr(hi), d_nbr_off, d_nbr, nnbr,
+                                                  max_degree, ndir, seed, d_vol, d_area, stream)
+    if rc != HV_OK:
+        msg = {HV_E_CAPACITY: "2n + nnbr doubles exceed the static scratch",
+               HV_E_INVALID_ARG: "invalid argument or a row longer than max_degree"}.get(rc, "CUDA error")
+        raise HVError(rc, "hv_integrate_heuristic_mc_noalloc: " + msg)
 
 
 class Context:

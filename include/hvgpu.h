@@ -139,6 +139,28 @@ int hv_integrate_heuristic_mc(hv_mesh* mesh, int ndir, uint64_t seed, double* vo
 int hv_mesh_stats(hv_mesh* mesh, hv_stats* stats);
 int hv_mesh_free(hv_mesh* mesh);
 
+/* Heuristic Monte-Carlo volumes and areas for callers that cannot allocate
+ * device memory: an application that has already committed the whole device
+ * memory budget, a loop where allocator calls are not allowed, or a framework
+ * that hands out fixed buffers.  It computes what hv_integrate_heuristic_mc
+ * computes, but every input and output is a caller-owned device buffer and the
+ * scratch lives in a static device array of HV_NOALLOC_SCRATCH_BYTES that this
+ * library holds on every GPU that loads it.  No counterpart in the reference.
+ *   d_pts      n x d doubles (device), d_nbr_off n+1 int64 and d_nbr nnbr int32
+ *              (device): neighbour CSR with 0-based generators, plane p as n+p
+ *              (hv_mesh_neighbors' lists minus one), max_degree >= every row
+ *   d_vol      n doubles (device), d_area nnbr doubles (device), stream a
+ *              cudaStream_t (NULL: legacy default stream); returns synchronised
+ * Limits: 256 + 8 (2 n + nnbr) bytes must fit the scratch (else
+ * HV_E_CAPACITY); HV_E_INVALID_ARG if a row is longer than max_degree.
+ * The first call on a device looks up the scratch address on that device
+ * (call it once before any stream capture).  Calls share the scratch: calls
+ * that overlap on the GPU race. */
+#define HV_NOALLOC_SCRATCH_BYTES (16u << 20)
+int hv_integrate_heuristic_mc_noalloc(int d, int64_t n, const double* d_pts, const double* lo, const double* hi,
+                                      const int64_t* d_nbr_off, const int32_t* d_nbr, int64_t nnbr, int max_degree,
+                                      int ndir, uint64_t seed, double* d_vol, double* d_area, void* stream);
+
 /* ------------------------------------------------------------------------
  * Serving: continuous batching of mesh requests on one device.
  *
