@@ -308,11 +308,16 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         int* dfail = fast ? srch->get<int>((size_t)nseeds) : nullptr;
         unsigned* ndfail = fast ? srch->get<unsigned>(1) : nullptr;
         if (fast) CK(cudaMemsetAsync(ndfail, 0, sizeof(unsigned), st));
-        kt.run(F_DESCENT, fast ? 2 : 1, [&] {
-            launch_descent(M, stride, nseeds, mesh->prm.seed ? mesh->prm.seed : 0x5EEDull, dfail, ndfail, ctx->nsm, st);
-        });
+        const unsigned long long dseed = mesh->prm.seed ? mesh->prm.seed : 0x5EEDull;
+        kt.run(F_DESCENT, 1, [&] { launch_descent(M, stride, nseeds, dseed, dfail, ndfail, ctx->nsm, st); });
         CK(cudaGetLastError());
         read_stat(ctx, dstat);
+        if (fast && ctx->h_stat[0] == 0 && !(ctx->h_stat[1] & (ST_VCAP | ST_HASH))) {
+            // no FP32 seed was decided: the exact descent on the undecided ones
+            kt.run(F_DESCENT, 1, [&] { launch_descent_exact(M, nseeds, dseed, dfail, ndfail, ctx->nsm, st); });
+            CK(cudaGetLastError());
+            read_stat(ctx, dstat);
+        }
         const unsigned overflow_bits = ST_VCAP | ST_HASH | ST_QUEUE | ST_ECAP;
         bool overflow = (ctx->h_stat[1] & overflow_bits) != 0;
         if (!overflow) check_fatal(ctx->h_stat[1]);

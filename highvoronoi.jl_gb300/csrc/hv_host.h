@@ -28,6 +28,8 @@ void exclusive_scan_i64(void* temp, size_t temp_bytes, const long long* in, long
 // hv_search.cu
 void launch_descent(const DevMesh& M, int stride, int nseeds, unsigned long long seed, int* failed,
                     unsigned* nfailed, int nsm, cudaStream_t st);
+void launch_descent_exact(const DevMesh& M, int maxn, unsigned long long seed, int* failed, unsigned* nfailed,
+                          int nsm, cudaStream_t st);
 void launch_centers(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
 void launch_register_edges(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
 void launch_expand_plain(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cudaStream_t st);

@@ -41,6 +41,12 @@ void launch_fallback_d4(const DevMesh& M, const unsigned long long* fq, const un
 void launch_fallback_d5(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm, cudaStream_t st);
 void launch_fallback_d6(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm, cudaStream_t st);
 
+void launch_descent_exact_d2(const DevMesh& M, int maxn, unsigned long long seed, int* failed, unsigned* nfailed, int nsm, cudaStream_t st);
+void launch_descent_exact_d3(const DevMesh& M, int maxn, unsigned long long seed, int* failed, unsigned* nfailed, int nsm, cudaStream_t st);
+void launch_descent_exact_d4(const DevMesh& M, int maxn, unsigned long long seed, int* failed, unsigned* nfailed, int nsm, cudaStream_t st);
+void launch_descent_exact_d5(const DevMesh& M, int maxn, unsigned long long seed, int* failed, unsigned* nfailed, int nsm, cudaStream_t st);
+void launch_descent_exact_d6(const DevMesh& M, int maxn, unsigned long long seed, int* failed, unsigned* nfailed, int nsm, cudaStream_t st);
+
 void launch_register_edges(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st) {
     switch (M.d) {
         case 2: launch_register_d2(M, v0, v1, nsm, st); break;
@@ -108,6 +114,17 @@ void launch_fallback(const DevMesh& M, const unsigned long long* fq, const unsig
         case 4: launch_fallback_d4(M, fq, nfq, maxq, nsm, st); break;
         case 5: launch_fallback_d5(M, fq, nfq, maxq, nsm, st); break;
         case 6: launch_fallback_d6(M, fq, nfq, maxq, nsm, st); break;
+        default: break;
+    }
+}
+
+void launch_descent_exact(const DevMesh& M, int maxn, unsigned long long seed, int* failed, unsigned* nfailed, int nsm, cudaStream_t st) {
+    switch (M.d) {
+        case 2: launch_descent_exact_d2(M, maxn, seed, failed, nfailed, nsm, st); break;
+        case 3: launch_descent_exact_d3(M, maxn, seed, failed, nfailed, nsm, st); break;
+        case 4: launch_descent_exact_d4(M, maxn, seed, failed, nfailed, nsm, st); break;
+        case 5: launch_descent_exact_d5(M, maxn, seed, failed, nfailed, nsm, st); break;
+        case 6: launch_descent_exact_d6(M, maxn, seed, failed, nfailed, nsm, st); break;
         default: break;
     }
 }

@@ -1815,13 +1815,22 @@ static void launch_descent_t(const DevMesh& M, int stride, int nseeds, unsigned 
                              unsigned* nfailed, int nsm, cudaStream_t st) {
     if (nseeds <= 0) return;
     if (M.K > 0 && failed) {
+        // FP32 warp descent; seeds whose step cannot be decided are only listed:
+        // any seed reaches the whole (connected) vertex graph, so the exact
+        // descent runs on that list only when no seed at all succeeded
+        // (launch_descent_exact)
         int blocks = (nseeds + FB_WPB - 1) / FB_WPB;
         if (blocks > nsm * 32) blocks = nsm * 32;
         k_descent_warp<D><<<blocks, FB_WPB * 32, 0, st>>>(M, stride, nseeds, seed, failed, nfailed);
-        k_descent<D><<<(nseeds + 127) / 128, 128, 0, st>>>(M, stride, nseeds, seed, failed, nfailed);
     } else {
         k_descent<D><<<(nseeds + 127) / 128, 128, 0, st>>>(M, stride, nseeds, seed, nullptr, nullptr);
     }
+}
+template <int D>
+static void launch_descent_exact_t(const DevMesh& M, int maxn, unsigned long long seed, int* failed,
+                                   unsigned* nfailed, int nsm, cudaStream_t st) {
+    if (maxn <= 0) return;
+    k_descent<D><<<(maxn + 127) / 128, 128, 0, st>>>(M, 1, maxn, seed, failed, nfailed);
 }
 template <int D>
 static void launch_plain_t(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cudaStream_t st) {
