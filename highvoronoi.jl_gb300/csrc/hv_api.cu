@@ -707,74 +707,90 @@ int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) {
         ensure_neighbors(m);
         if (m->nnbr > 0 && !area) return HV_E_INVALID_ARG;
         if (m->n == 0) return HV_OK;
-        cudaStream_t st = m->ctx->stream;
+        hv_ctx* ctx = m->ctx;
+        cudaStream_t st = ctx->stream;
         const int d = m->d, n = m->n;
-        std::vector<long long> io(n + 1);
-        CK(cudaMemcpyAsync(io.data(), m->inc_off, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        long long maxc = 1;
-        for (int i = 0; i < n; ++i) maxc = std::max(maxc, io[i + 1] - io[i]);
-        int smax = 0;
-        cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, m->ctx->device);
+        const long long ns = m->nnbr;
+        const auto t0 = std::chrono::steady_clock::now();
+        KTimer kt(ctx);
         Scratch s(st);
-        double* dvol = s.get<double>(n);
-        double* darea = s.get<double>((size_t)std::max(m->nnbr, 1ll));
-        unsigned* dstat = s.get<unsigned>(2);  // status, number of big cells
-        int* big = s.get<int>(n);
-        hv::IntegrateInput in{d, n, m->lo, m->hi, m->d_in, m->osig, m->oc, m->inc_off, m->inc, m->nbr_off, m->nbr, dstat};
-        auto caps_for = [&](int capC, int capV) {
-            hv::PolyCaps c;
-            c.capC = capC; c.capV = capV; c.capF = 2 * capV;
-            c.capE = (int)next_pow2((unsigned long long)capV * (d - 1) / 2 + 2);
-            c.capI = (int)std::min<unsigned long long>(1024ull, next_pow2((unsigned long long)std::max(64, capV)));
-            return c;
-        };
-        // shared-memory pass: the largest power-of-two cell size that fits
-        int capC = (int)std::min<unsigned long long>(next_pow2((unsigned long long)maxc), 1024ull);
-        int capV = std::min(capC, std::max(64, capC / 4));
-        auto smem_of = [&](const hv::PolyCaps& c) {
-            return (long long)hv::poly_smem_bytes(d, c.capC, c.capV, c.capF, c.capE, c.capI);
-        };
-        while (capC > 16 && smem_of(caps_for(capC, capV)) > smax) {
-            capC /= 2;
-            capV = std::min(capC, std::max(64, capC / 4));
-        }
-        const int capCg = (int)next_pow2((unsigned long long)maxc);
-        int capVg = capCg;
-        for (int attempt = 0;; ++attempt) {
-            hv::PolyCaps cs = caps_for(capC, capV), cg = caps_for(capCg, capVg);
-            CK(cudaMemsetAsync(dstat, 0, 2 * sizeof(unsigned), st));
-            CK(cudaMemsetAsync(darea, 0, sizeof(double) * std::max(m->nnbr, 1ll), st));
-            if (hv::launch_polygon(in, cs, cg, big, dstat + 1, 0, nullptr, 0, darea, dvol, 0, m->ctx->nsm, st) != 0)
-                throw HvError(HV_E_CUDA, "polygon integrator launch failed");
+        hv::PolyRun R{};
+        R.d = d; R.n = n; R.V = m->V; R.lo = m->lo; R.hi = m->hi;
+        R.pts = m->d_in; R.osig = m->osig; R.oc = m->oc; R.nbr_off = m->nbr_off; R.nbr = m->nbr;
+        R.nslots = ns; R.nsm = ctx->nsm; R.stream = st;
+        R.cnt = s.get<unsigned long long>((size_t)ns + 1);
+        long long* foff = s.get<long long>((size_t)ns + 1);
+        R.foff = foff;
+        R.slot_cell = s.get<int>((size_t)std::max(ns, 1ll));
+        R.area = s.get<double>((size_t)std::max(ns, 1ll));
+        R.vol = s.get<double>(n);
+        unsigned* dstat = s.get<unsigned>(4);  // status, number of big facets, their largest vertex count
+        R.status = dstat; R.nbig = dstat + 1; R.maxnv = dstat + 2;
+        R.next = s.get<unsigned long long>(1);
+        R.big = s.get<long long>((size_t)std::max(ns, 1ll));
+        CK(cudaMemsetAsync(R.cnt, 0, sizeof(unsigned long long) * (ns + 1), st));
+        CK(cudaMemsetAsync(dstat, 0, 4 * sizeof(unsigned), st));
+        CK(cudaMemsetAsync(R.next, 0, sizeof(unsigned long long), st));
+        CK(cudaMemsetAsync(R.area, 0, sizeof(double) * std::max(ns, 1ll), st));
+        auto run = [&](int pass) {
+            R.pass = pass;
+            if (hv::launch_poly(R) != 0) throw HvError(HV_E_CUDA, "polygon integrator launch failed");
             CK(cudaGetLastError());
-            unsigned hs[2] = {0, 0};
-            CK(cudaMemcpyAsync(hs, dstat, sizeof(hs), cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
-            if (hs[1] > 0 && !(hs[0] & 2u)) {
-                const size_t bytes = ((size_t)smem_of(cg) + 255) / 256 * 256;
-                const int gblocks = (int)std::min<unsigned>(hs[1], (unsigned)(2 * m->ctx->nsm));
+        };
+        // facet -> vertex incidences
+        size_t scan_tb = hv::scan_temp((int)(ns + 1));
+        void* scan_tmp = s.get<char>(scan_tb);
+        kt.run(0, 2, [&] {
+            run(0);
+            hv::exclusive_scan_i64(scan_tmp, scan_tb, (const long long*)R.cnt, foff, (int)(ns + 1), st);
+        });
+        long long ninc = 0;
+        CK(cudaMemcpyAsync(&ninc, foff + ns, sizeof(long long), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        R.fvert = s.get<unsigned>((size_t)std::max(ninc, 1ll));
+        CK(cudaMemsetAsync(R.cnt, 0, sizeof(unsigned long long) * (ns + 1), st));
+        kt.run(0, 1, [&] { run(1); });
+        // tier A: shared-memory work areas
+        static const int capA[7] = {0, 0, 2, 32, 64, 128, 256};
+        int smax = 0;
+        cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+        R.capV = capA[d];
+        while (R.capV > 4 && hv::poly_area_bytes(d, R.capV, 1, false) > (size_t)smax) R.capV /= 2;
+        kt.run(1, 1, [&] { run(2); });
+        unsigned hs[3] = {0, 0, 0};
+        CK(cudaMemcpyAsync(hs, dstat, sizeof(hs), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (hs[0] & 8u) throw HvError(HV_E_INTERNAL, "a facet is not a simple polytope (degenerate vertex)");
+        const unsigned nbig = hs[1];
+        if (hs[1] > 0) {  // tier B: facets over the tier-A caps, global-memory work areas
+            R.nbig_host = hs[1];
+            R.capV = (int)next_pow2(hs[2]);
+            R.blocks = (int)std::min<long long>(hs[1], 2ll * ctx->nsm);
+            for (R.widen = 1;; R.widen *= 2) {
                 Scratch gs(st);
-                unsigned char* gbase = gs.get<unsigned char>(bytes * gblocks);
-                hv::launch_polygon(in, cs, cg, big, dstat + 1, hs[1], gbase, gblocks, darea, dvol, 1, m->ctx->nsm, st);
-                CK(cudaGetLastError());
+                R.slab = gs.get<unsigned char>(hv::poly_area_bytes(d, R.capV, R.widen, true) * R.blocks);
+                CK(cudaMemsetAsync(R.next, 0, sizeof(unsigned long long), st));
+                CK(cudaMemsetAsync(dstat, 0, sizeof(unsigned), st));
+                kt.run(2, 1, [&] { run(3); });
                 CK(cudaMemcpyAsync(hs, dstat, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
                 CK(cudaStreamSynchronize(st));
+                if (hs[0] & 8u) throw HvError(HV_E_INTERNAL, "a facet is not a simple polytope (degenerate vertex)");
+                if (hs[0] == 0) break;
+                if (R.widen >= 8) throw HvError(HV_E_CAPACITY, "facet structure beyond the polygon integrator's capacity");
             }
-            if (hs[0] == 0) break;
-            if ((hs[0] & 1u) || attempt > 6)
-                throw HvError(HV_E_CAPACITY, "facet structure beyond the polygon integrator's capacity");
-            capV = std::min(capC, capV * 2);   // facet over capacity: widen and redo
-            capVg = std::min(capCg, capVg * 2);
-            if (capV == capC && capVg == capCg && attempt > 2)
-                throw HvError(HV_E_CAPACITY, "facet structure beyond the polygon integrator's capacity");
         }
-        hv::launch_polygon(in, caps_for(capC, capV), caps_for(capCg, capVg), big, dstat + 1, 0, nullptr, 0, darea,
-                           dvol, 2, m->ctx->nsm, st);
-        CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(vol, dvol, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
-        if (m->nnbr > 0) CK(cudaMemcpyAsync(area, darea, sizeof(double) * m->nnbr, cudaMemcpyDeviceToHost, st));
+        run(4);
+        CK(cudaMemcpyAsync(vol, R.vol, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        if (ns > 0) CK(cudaMemcpyAsync(area, R.area, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
+        double fam[F_N];
+        kt.totals(fam);
+        m->st.poly_big_facets = nbig;
+        m->st.ms_poly_incidence = fam[0];
+        m->st.ms_poly_facets = fam[1];
+        m->st.ms_poly_big = fam[2];
+        m->st.ms_poly_total =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     } catch (const HvError& e) {
         return fail(m->ctx, e);
     }

@@ -19,16 +19,42 @@ struct IntegrateInput {
     unsigned* status;         // 1: cell over capacity, 2: facet over capacity, 4: degree over capacity
 };
 
-struct PolyCaps {
-    int capC, capV, capF, capE, capI;  // cell vertices, facet vertices, faces, edges, local items (powers of two)
+// VI_POLYGON (hv_poly.cu).  pass 0: count facet-vertex incidences per
+// neighbour slot and fill slot_cell; pass 1: fill fvert (cnt re-zeroed, foff
+// = exclusive scan of the counts); pass 2: tier-A facet kernel (shared-memory
+// work areas, facets of up to capV vertices; the others are listed in big);
+// pass 3: tier-B facet kernel over the nbig_host listed facets (global-memory
+// work areas, caps from capV and widen); pass 4: cell volumes.
+struct PolyRun {
+    int d, n, pass;
+    unsigned V;
+    const double* lo;          // host arrays
+    const double* hi;
+    const double* pts;
+    const int* osig;
+    const double* oc;
+    const long long* nbr_off;
+    const int* nbr;
+    long long nslots;
+    unsigned long long* cnt;   // nslots + 1
+    const long long* foff;
+    unsigned* fvert;
+    int* slot_cell;
+    double* area;
+    double* vol;
+    unsigned* status;
+    unsigned long long* next;  // work counter
+    long long* big;
+    unsigned* nbig;
+    unsigned* maxnv;
+    long long nbig_host;
+    int capV, widen, blocks, nsm;
+    unsigned char* slab;
+    cudaStream_t stream;
 };
-
-size_t poly_smem_bytes(int d, int capC, int capV, int capF, int capE, int capI);
-// pass 0: shared-memory kernel over all cells (big cells appended to `big`),
-// pass 1: global-memory kernel over the big cells, pass 2: volumes.
-int launch_polygon(const IntegrateInput& in, const PolyCaps& cs, const PolyCaps& cg, int* big, unsigned* nbig,
-                   unsigned nbig_host, unsigned char* gbase, int gblocks, double* area, double* vol, int pass,
-                   int nsm, cudaStream_t st);
+int launch_poly(const PolyRun& R);
+// Work-area bytes: per block for tier A, per block (one group) for tier B.
+size_t poly_area_bytes(int d, int capV, int widen, bool tier_b);
 int launch_heuristic_mc(const IntegrateInput& in, int ndir, unsigned long long seed, int capN, double cvol,
                         double* rawV, double* rawA, double* varV, double* outA, double* vol, int nsm,
                         cudaStream_t st);

@@ -48,10 +48,12 @@ STAT_FIELDS = ("vertices", "rays", "fallback_rays", "uncertified", "insecure", "
                "descents", "descent_retries", "levels", "edges_closed", "capacity_retries", "launches")
 TIME_FIELDS = ("ms_prepare", "ms_search", "ms_total", "ms_knn", "ms_descent", "ms_expand", "ms_fallback",
                "ms_centers", "ms_canonical")
+POLY_FIELDS = ("ms_poly_incidence", "ms_poly_facets", "ms_poly_big", "ms_poly_total")
 
 
 class Stats(ctypes.Structure):
-    _fields_ = [(n, ctypes.c_int64) for n in STAT_FIELDS] + [(n, ctypes.c_double) for n in TIME_FIELDS]
+    _fields_ = ([(n, ctypes.c_int64) for n in STAT_FIELDS] + [(n, ctypes.c_double) for n in TIME_FIELDS] +
+                [("poly_big_facets", ctypes.c_int64)] + [(n, ctypes.c_double) for n in POLY_FIELDS])
 
 
 _lock = threading.Lock()

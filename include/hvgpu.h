@@ -96,6 +96,12 @@ typedef struct {
     double ms_fallback;     /* exact re-walks of uncertified/insecure rays */
     double ms_centers;      /* FP64 circumcentres of new vertices */
     double ms_canonical;    /* canonical renumbering */
+    /* last hv_integrate_polygon on this mesh */
+    int64_t poly_big_facets;   /* facets redone with global-memory work areas */
+    double ms_poly_incidence;  /* facet -> vertex lists (device) */
+    double ms_poly_facets;     /* shared-memory facet kernel (device) */
+    double ms_poly_big;        /* global-memory facet kernel (device) */
+    double ms_poly_total;      /* whole call (host wall clock) */
 } hv_stats;
 
 int hv_version(void);
