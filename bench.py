@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-integrators", action="store_true")
+    ap.add_argument("--mc-dirs", type=int, default=1000, help="directions per cell of VI_HEURISTIC_MC")
     return ap.parse_args()
 
 
@@ -286,6 +288,29 @@ def run_ours(args):
         torch.distributed.all_reduce(v)
         verts = int(v.item())
     value = verts / (tot_ms / 1e3)
+    # ---- the two integrators on the same mesh (host wall clock through the C ABI, outputs copied back)
+    integ = None
+    if not args.no_integrators and ws == 1:
+        m = build_dev()
+        integ = {}
+        for name, fn in (("polygon", lambda: m.polygon()),
+                         ("heuristic_mc", lambda: m.heuristic_mc(args.mc_dirs, 7))):
+            for _ in range(max(args.warmup, 3)):
+                fn()
+            ts = []
+            for _ in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                fn()
+                ts.append(time.perf_counter() - t0)
+            t = statistics.mean(ts)
+            integ[name] = {"ms": 1e3 * t, "cells_per_s": n / t}
+        st = m.stats()
+        integ["polygon"].update({k: st[k] for k in ("poly_big_facets", "ms_poly_incidence", "ms_poly_facets",
+                                                    "ms_poly_big")})
+        integ["heuristic_mc"]["directions_per_cell"] = args.mc_dirs
+        m.free()
     # ---- end to end through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
@@ -329,8 +354,26 @@ def run_ours(args):
     roof = {"bound": "hbm", "kernel": "k_expand_fast" if method == hvgpu.HV_METHOD_FAST else "k_expand_plain",
             "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
             "traffic": traffic, "peak_source": peak_kind,
+            "traffic_note": "ncu DRAM bytes with its default cache flush before every launch: the candidate lists "
+                            "are re-read from DRAM at every wavefront level, which L2 holds in an unprofiled run",
             "alg_bytes_per_launch": alg_bytes / launches, "ms_per_launch": exp_ms / launches,
             "launches_per_step": launches}
+    # FP32 view (the binding pipe of the candidate scan): n_bar (5d+3) flops per vertex, n_bar = mean
+    # neighbour count of the mesh; peak = SMs x 128 FP32 lanes x 2 x max SM clock (nominal)
+    try:
+        mm = build_dev()
+        _, nnbr = mm.counts(neighbors=True)
+        mm.free()
+        nbar = nnbr / n
+        prop = torch.cuda.get_device_properties(local)
+        fmax = (clocks or {}).get("sm_max_mhz") or 2070.0
+        fp32_peak = prop.multi_processor_count * 128 * 2 * fmax * 1e6 / 1e12
+        fl = Vs * nbar * (5 * d + 3)
+        ach = fl / (exp_ms / 1e3) / 1e12
+        roof["fp32"] = {"algorithmic_flops_per_vertex": nbar * (5 * d + 3), "mean_neighbours": nbar,
+                        "achieved_tflops": ach, "peak_tflops_nominal": fp32_peak, "frac": ach / fp32_peak}
+    except Exception as ex:  # noqa: BLE001
+        roof["fp32"] = {"error": str(ex)}
     # ---- CPU baseline on the host cores
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
@@ -355,7 +398,7 @@ def run_ours(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "config": cfg,
-            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks, "integrators": integ,
             "gpu_launches": int(sum(s["launches"] for s in stats)),
             "stats": {k: st0[k] for k in ("rays", "fallback_rays", "uncertified", "insecure", "dd_rescores",
                                           "degenerate", "descents", "levels")},

@@ -12,6 +12,8 @@
 // keeps freed blocks cached so repeated builds do not return to the driver.
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -724,12 +726,14 @@ int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) {
         R.slot_cell = s.get<int>((size_t)std::max(ns, 1ll));
         R.area = s.get<double>((size_t)std::max(ns, 1ll));
         R.vol = s.get<double>(n);
-        unsigned* dstat = s.get<unsigned>(4);  // status, number of big facets, their largest vertex count
-        R.status = dstat; R.nbig = dstat + 1; R.maxnv = dstat + 2;
+        // status, big facets (count, largest vertex count), huge facets (count, largest vertex count)
+        unsigned* dstat = s.get<unsigned>(8);
+        R.status = dstat; R.nbig = dstat + 1; R.maxnv = dstat + 2; R.nbig2 = dstat + 3; R.maxnv2 = dstat + 4;
         R.next = s.get<unsigned long long>(1);
         R.big = s.get<long long>((size_t)std::max(ns, 1ll));
+        R.big2 = s.get<long long>((size_t)std::max(ns, 1ll));
         CK(cudaMemsetAsync(R.cnt, 0, sizeof(unsigned long long) * (ns + 1), st));
-        CK(cudaMemsetAsync(dstat, 0, 4 * sizeof(unsigned), st));
+        CK(cudaMemsetAsync(dstat, 0, 8 * sizeof(unsigned), st));
         CK(cudaMemsetAsync(R.next, 0, sizeof(unsigned long long), st));
         CK(cudaMemsetAsync(R.area, 0, sizeof(double) * std::max(ns, 1ll), st));
         auto run = [&](int pass) {
@@ -754,7 +758,17 @@ int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) {
         static const int capA[7] = {0, 0, 2, 32, 64, 128, 256};
         int smax = 0;
         cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
-        R.capV = capA[d];
+        // HV_POLY_CAPS="a,b" lowers the tier-A and shared-memory tier-B vertex caps
+        // (powers of two) so that small meshes exercise every tier
+        int cap_a = capA[d], cap_b = 1 << 30;
+        if (const char* e = std::getenv("HV_POLY_CAPS")) {
+            int a = 0, b = 0;
+            if (std::sscanf(e, "%d,%d", &a, &b) == 2 && a >= 2 && b >= 2) {
+                cap_a = std::min(cap_a, (int)next_pow2((unsigned)a));
+                cap_b = (int)next_pow2((unsigned)b);
+            }
+        }
+        R.capV = cap_a;
         while (R.capV > 4 && hv::poly_area_bytes(d, R.capV, 1, false) > (size_t)smax) R.capV /= 2;
         kt.run(1, 1, [&] { run(2); });
         unsigned hs[3] = {0, 0, 0};
@@ -762,21 +776,33 @@ int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) {
         CK(cudaStreamSynchronize(st));
         if (hs[0] & 8u) throw HvError(HV_E_INTERNAL, "a facet is not a simple polytope (degenerate vertex)");
         const unsigned nbig = hs[1];
-        if (hs[1] > 0) {  // tier B: facets over the tier-A caps, global-memory work areas
+        if (hs[1] > 0) {  // tier B: facets over the tier-A caps, one block each, shared memory
             R.nbig_host = hs[1];
-            R.capV = (int)next_pow2(hs[2]);
-            R.blocks = (int)std::min<long long>(hs[1], 2ll * ctx->nsm);
-            for (R.widen = 1;; R.widen *= 2) {
-                Scratch gs(st);
-                R.slab = gs.get<unsigned char>(hv::poly_area_bytes(d, R.capV, R.widen, true) * R.blocks);
-                CK(cudaMemsetAsync(R.next, 0, sizeof(unsigned long long), st));
-                CK(cudaMemsetAsync(dstat, 0, sizeof(unsigned), st));
-                kt.run(2, 1, [&] { run(3); });
-                CK(cudaMemcpyAsync(hs, dstat, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-                CK(cudaStreamSynchronize(st));
-                if (hs[0] & 8u) throw HvError(HV_E_INTERNAL, "a facet is not a simple polytope (degenerate vertex)");
-                if (hs[0] == 0) break;
-                if (R.widen >= 8) throw HvError(HV_E_CAPACITY, "facet structure beyond the polygon integrator's capacity");
+            R.capV = 16;
+            while (R.capV * 2 <= cap_b && hv::poly_area_bytes(d, R.capV * 2, 1, true) <= (size_t)smax) R.capV *= 2;
+            CK(cudaMemsetAsync(R.next, 0, sizeof(unsigned long long), st));
+            kt.run(2, 1, [&] { run(3); });
+            unsigned h2[5] = {0, 0, 0, 0, 0};
+            CK(cudaMemcpyAsync(h2, dstat, sizeof(h2), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (h2[0] & 8u) throw HvError(HV_E_INTERNAL, "a facet is not a simple polytope (degenerate vertex)");
+            if (h2[3] > 0) {  // the largest facets: global-memory work areas
+                R.nbig_host = h2[3];
+                R.capV = (int)next_pow2(h2[4]);
+                R.blocks = (int)std::min<long long>(h2[3], 2ll * ctx->nsm);
+                for (R.widen = 1;; R.widen *= 2) {
+                    Scratch gs(st);
+                    R.slab = gs.get<unsigned char>(hv::poly_area_bytes(d, R.capV, R.widen, true) * R.blocks);
+                    CK(cudaMemsetAsync(R.next, 0, sizeof(unsigned long long), st));
+                    CK(cudaMemsetAsync(dstat, 0, sizeof(unsigned), st));
+                    kt.run(2, 1, [&] { run(5); });
+                    CK(cudaMemcpyAsync(hs, dstat, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+                    CK(cudaStreamSynchronize(st));
+                    if (hs[0] & 8u) throw HvError(HV_E_INTERNAL, "a facet is not a simple polytope (degenerate vertex)");
+                    if (hs[0] == 0) break;
+                    if (R.widen >= 8)
+                        throw HvError(HV_E_CAPACITY, "facet structure beyond the polygon integrator's capacity");
+                }
             }
         }
         run(4);

@@ -23,8 +23,10 @@ struct IntegrateInput {
 // neighbour slot and fill slot_cell; pass 1: fill fvert (cnt re-zeroed, foff
 // = exclusive scan of the counts); pass 2: tier-A facet kernel (shared-memory
 // work areas, facets of up to capV vertices; the others are listed in big);
-// pass 3: tier-B facet kernel over the nbig_host listed facets (global-memory
-// work areas, caps from capV and widen); pass 4: cell volumes.
+// pass 3: tier-B facet kernel with a shared-memory work area over the
+// nbig_host facets in big (over its caps: listed in big2); pass 5: tier-B
+// kernel with global-memory work areas over the nbig_host facets in big2
+// (caps from capV and widen); pass 4: cell volumes.
 struct PolyRun {
     int d, n, pass;
     unsigned V;
@@ -47,6 +49,9 @@ struct PolyRun {
     long long* big;
     unsigned* nbig;
     unsigned* maxnv;
+    long long* big2;
+    unsigned* nbig2;
+    unsigned* maxnv2;
     long long nbig_host;
     int capV, widen, blocks, nsm;
     unsigned char* slab;

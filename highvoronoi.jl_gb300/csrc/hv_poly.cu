@@ -624,23 +624,32 @@ __global__ void __launch_bounds__(NW * 32 * GPB) k_poly_facets(PolyIn P, FCaps c
     }
 }
 
-// Tier B: one group of NW warps per block, 64-bit keys, global-memory work
-// areas (one per block), over the listed facets.
-template <int D, int NW>
-__global__ void __launch_bounds__(NW * 32) k_poly_big(PolyIn P, FCaps c, const long long* big, long long nbig,
-                                                      unsigned long long* next, unsigned char* slab) {
+// Tier B: one group of NW warps per block, 64-bit keys, over a list of facets.
+// SMEM: work area in shared memory; facets over its caps go to `out`.
+// Otherwise: one global-memory work area per block; over the caps is fatal.
+template <int D, int NW, bool SMEM>
+__global__ void __launch_bounds__(NW * 32) k_poly_big(PolyIn P, FCaps c, const long long* in, long long nin,
+                                                      unsigned long long* next, unsigned char* slab, long long* out,
+                                                      unsigned* nout, unsigned* maxnv) {
+    extern __shared__ __align__(16) unsigned char smem[];
     const Grp<NW> g(threadIdx.x, 0);
-    const FArea<D, unsigned long long> W(slab + (size_t)blockIdx.x * farea_bytes<D, unsigned long long>(c), c);
+    unsigned char* base = SMEM ? smem : slab + (size_t)blockIdx.x * farea_bytes<D, unsigned long long>(c);
+    const FArea<D, unsigned long long> W(base, c);
     for (;;) {
         const long long f = g_claim(g, next, W.ll + 1);
-        if (f >= nbig) break;
-        const long long t = big[f];
+        if (f >= nin) break;
+        const long long t = in[f];
         const int i = P.slot_cell[t], k = P.nbr[t];
         double ar = 0.0;
         const int r = poly_facet<D, NW, unsigned long long>(P, i, k, t, W, c, g, ar);
         if (g.rank == 0) {
             if (r == F_OK) write_area<D>(P, i, k, t, ar);
-            else atomicOr(P.status, r == F_CAP ? 1u : 8u);
+            else if (r == F_CAP && SMEM) {
+                out[atomicAdd(nout, 1u)] = t;
+                atomicMax(maxnv, (unsigned)(P.foff[t + 1] - P.foff[t]));
+            } else {
+                atomicOr(P.status, r == F_CAP ? 1u : 8u);
+            }
         }
         g.sync();
     }
@@ -785,9 +794,23 @@ static int poly_run(const PolyRun& R) {
             return -1;
         k_poly_facets<D, NW, GPB><<<R.nsm * per, NW * 32 * GPB, sm, st>>>(P, c, R.nslots, R.next, R.big, R.nbig,
                                                                          R.maxnv);
-    } else if (R.pass == 3) {  // tier B
+    } else if (R.pass == 3) {  // tier B, shared memory
+        const FCaps c = caps_for(D, R.capV, 1);
+        const size_t sm = bytes_b<D>(c);
+        if (cudaFuncSetAttribute(k_poly_big<D, 8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+            cudaSuccess)
+            return -1;
+        int per = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_poly_big<D, 8, true>, 256, sm) != cudaSuccess ||
+            per < 1)
+            return -1;
+        const long long blocks = std::min<long long>(R.nbig_host, (long long)R.nsm * per);
+        k_poly_big<D, 8, true><<<(int)blocks, 256, sm, st>>>(P, c, R.big, R.nbig_host, R.next, nullptr, R.big2,
+                                                             R.nbig2, R.maxnv2);
+    } else if (R.pass == 5) {  // tier B, global memory
         const FCaps c = caps_for(D, R.capV, R.widen);
-        k_poly_big<D, 8><<<R.blocks, 256, 0, st>>>(P, c, R.big, R.nbig_host, R.next, R.slab);
+        k_poly_big<D, 8, false><<<R.blocks, 256, 0, st>>>(P, c, R.big2, R.nbig_host, R.next, R.slab, nullptr,
+                                                          nullptr, nullptr);
     } else {
         k_cell_volumes<D><<<grid_of(R.n, 256), 256, 0, st>>>(P, R.vol);
     }

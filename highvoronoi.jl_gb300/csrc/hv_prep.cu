@@ -123,24 +123,61 @@ __device__ __forceinline__ bool pair_less(float da, int ia, float db, int ib) {
     return da < db || (da == db && ia < ib);
 }
 
-template <int CAP>
-__device__ __forceinline__ void warp_bitonic(float* sd, int* si, int lane) {
+// Bitonic sort of n2 (power of two) (distance, index) pairs by a warp.
+__device__ __forceinline__ void warp_bitonic_n(float* sd, int* si, int n2, int lane) {
 #pragma unroll 1
-    for (int k = 2; k <= CAP; k <<= 1) {
+    for (int k = 2; k <= n2; k <<= 1) {
 #pragma unroll 1
         for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = lane; i < CAP; i += 32) {
-                const int ixj = i ^ j;
-                if (ixj > i) {
-                    const bool up = (i & k) == 0;
-                    const float da = sd[i], db = sd[ixj];
-                    const int ia = si[i], ib = si[ixj];
-                    if (pair_less(db, ib, da, ia) == up) { sd[i] = db; sd[ixj] = da; si[i] = ib; si[ixj] = ia; }
-                }
+            for (int q = lane; q < (n2 >> 1); q += 32) {
+                const int i = ((q & ~(j - 1)) << 1) | (q & (j - 1));
+                const int ixj = i | j;
+                const bool up = (i & k) == 0;
+                const float da = sd[i], db = sd[ixj];
+                const int ia = si[i], ib = si[ixj];
+                if (pair_less(db, ib, da, ia) == up) { sd[i] = db; sd[ixj] = da; si[i] = ib; si[ixj] = ia; }
             }
             __syncwarp();
         }
     }
+}
+
+// Keeps exactly the `need` smallest of the n buffered distances (n >= need):
+// bisection over the bit patterns of the non-negative distances for the
+// need-th smallest value t, then one ordered compaction keeping every entry
+// below t and the first entries equal to t.  Returns t.
+__device__ float warp_keep_smallest(float* sd, int* si, int n, int need, int lane) {
+    const unsigned FULL = 0xFFFFFFFFu;
+    unsigned lo = 0, hi = 0x7F800000u;
+    while (lo < hi) {
+        const unsigned mid = lo + ((hi - lo) >> 1);
+        int c = 0;
+        for (int x = lane; x < n; x += 32) c += (__float_as_uint(sd[x]) <= mid);
+        c = __reduce_add_sync(FULL, c);
+        if (c >= need) hi = mid; else lo = mid + 1;
+    }
+    const unsigned tb = lo;
+    int clt = 0;
+    for (int x = lane; x < n; x += 32) clt += (__float_as_uint(sd[x]) < tb);
+    clt = __reduce_add_sync(FULL, clt);
+    const int eq_budget = need - clt;
+    int w = 0, eqseen = 0;
+    for (int base = 0; base < n; base += 32) {
+        const int x = base + lane;
+        float dv = 0.f;
+        int iv = 0;
+        unsigned b = 0xFFFFFFFFu;
+        if (x < n) { dv = sd[x]; iv = si[x]; b = __float_as_uint(dv); }
+        const unsigned beq = __ballot_sync(FULL, x < n && b == tb);
+        const unsigned lm = (1u << lane) - 1u;
+        const bool keep = (x < n) && (b < tb || (b == tb && eqseen + __popc(beq & lm) < eq_budget));
+        const unsigned bk = __ballot_sync(FULL, keep);
+        if (keep) { sd[w + __popc(bk & lm)] = dv; si[w + __popc(bk & lm)] = iv; }
+        w += __popc(bk);
+        eqseen += __popc(beq);
+    }
+    __syncwarp();
+    return __uint_as_float(tb);
 }
 
 template <int D, int CAP>
@@ -213,13 +250,9 @@ __global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float
                     }
                     cnt += __popc(bal);
                     __syncwarp();
-                    if (cnt > CAP - 32) {
-                        for (int i = cnt + lane; i < CAP; i += 32) { d[i] = INFINITY; ix[i] = 0x7FFFFFFF; }
-                        __syncwarp();
-                        warp_bitonic<CAP>(d, ix, lane);
-                        cnt = min(cnt, K + 1);
-                        if (cnt == K + 1) thr = d[K];
-                        __syncwarp();
+                    if (cnt > CAP - 32) {  // keep the K+1 nearest so far; their largest bounds the rest
+                        thr = warp_keep_smallest(d, ix, cnt, K + 1, lane);
+                        cnt = K + 1;
                     }
                 }
             } else {
@@ -245,9 +278,15 @@ __global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float
                 __syncwarp();
             }
         }
-        for (int i = cnt + lane; i < CAP; i += 32) { d[i] = INFINITY; ix[i] = 0x7FFFFFFF; }
+        if (cnt > K + 1) {
+            warp_keep_smallest(d, ix, cnt, K + 1, lane);
+            cnt = K + 1;
+        }
+        int n2 = 32;
+        while (n2 < cnt) n2 <<= 1;
+        for (int i = cnt + lane; i < n2; i += 32) { d[i] = INFINITY; ix[i] = 0x7FFFFFFF; }
         __syncwarp();
-        warp_bitonic<CAP>(d, ix, lane);
+        warp_bitonic_n(d, ix, n2, lane);
         for (int c = lane; c < K; c += 32) knn[(size_t)q * K + c] = (c < cnt) ? ix[c] : -1;
         if (lane == 0) {
             float r = INFINITY;

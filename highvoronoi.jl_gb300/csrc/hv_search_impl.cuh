@@ -900,7 +900,7 @@ __device__ __forceinline__ void load_pt32lo(const DevMesh& M, int j, float (&x)[
 }
 
 template <int D>
-__global__ void __launch_bounds__(FAST_WPB * 32) k_expand_fast(DevMesh M, unsigned f0, unsigned f1,
+__global__ void __launch_bounds__(FAST_WPB * 32, (D <= 4 ? 16 / FAST_WPB : 1)) k_expand_fast(DevMesh M, unsigned f0, unsigned f1,
                                                                unsigned long long* fq, unsigned* nfq,
                                                                unsigned fqcap, unsigned long long* fx,
                                                                unsigned* nfx, unsigned fxcap) {

@@ -82,3 +82,18 @@ def test_heuristic_mc_against_exact_volumes(gpu_lib):
     v, _ = m.heuristic_mc(4000, 5)
     assert abs(v.sum() - 1.0) < 0.02
     assert np.median(np.abs(v - ev) / ev) < 0.05
+
+
+@pytest.mark.parametrize("d,n,seed", [(3, 300, 11), (4, 300, 12), (5, 150, 13), (6, 60, 14)])
+def test_polygon_tiers_agree(gpu_lib, d, n, seed, monkeypatch):
+    """Tiny vertex caps push facets through the shared-memory and the global-memory
+    tier-B kernels; every tier must give the same areas as the default run."""
+    pts = D.uniform_points(d, n, seed)
+    v0, a0 = _mesh(gpu_lib, pts).polygon()
+    monkeypatch.setenv("HV_POLY_CAPS", "4,8")
+    m = _mesh(gpu_lib, pts)
+    v1, a1 = m.polygon()
+    st = m.stats()
+    assert st["poly_big_facets"] > 0 and st["ms_poly_big"] > 0
+    np.testing.assert_allclose(v1, v0, rtol=1e-13, atol=0)
+    np.testing.assert_allclose(a1, a0, rtol=1e-12, atol=1e-15 * max(1.0, a0.max()))
