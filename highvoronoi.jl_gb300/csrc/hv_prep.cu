@@ -180,19 +180,30 @@ __device__ float warp_keep_smallest(float* sd, int* si, int n, int need, int lan
     return __uint_as_float(tb);
 }
 
+constexpr int KNN_STK = 768;  // traversal stack entries per warp (bounded by 32 x tree depth + 64)
+constexpr int KNN_LQ = 64;     // queued leaves per warp
+
+// One warp per generator.  Phase 1 inserts the generator's smallest ancestor
+// subtree holding at least K+1+leaf points (a contiguous Morton range, read
+// coalesced) and keeps the K+1 nearest, which bounds the K+1-th distance.
+// Phase 2 walks the rest of the tree 32 nodes per step (one box test per
+// lane), queues the surviving leaves and scans them 32 points at a time.
 template <int D, int CAP>
 __global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float* sec) {
     constexpr int DP = (D <= 4) ? 4 : 8;
     __shared__ float sd[KNN_WPB][CAP];
     __shared__ int si[KNN_WPB][CAP];
-    __shared__ int sstack[KNN_WPB][64];
+    __shared__ int sstack[KNN_WPB][KNN_STK];
+    __shared__ int sleaf[KNN_WPB][KNN_LQ];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int K = M.K;
     const unsigned FULL = 0xFFFFFFFFu;
+    const unsigned lt = (1u << lane) - 1u;
     const float ex = (float)(M.xscale * 5.9604645e-08);
     float* d = sd[wib];
     int* ix = si[wib];
     int* stk = sstack[wib];
+    int* lq = sleaf[wib];
     for (int q = blockIdx.x * KNN_WPB + wib; q < M.n; q += gridDim.x * KNN_WPB) {
         float xq[DP];
         {
@@ -205,76 +216,105 @@ __global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float
         }
         int cnt = 0;
         float thr = INFINITY;
-        int sp = 1;
-        if (lane == 0) stk[0] = 1;
-        __syncwarp();
-        while (sp > 0) {
-            const int node = stk[--sp];
-            __syncwarp();
-            float bd = 0.f;
-            {
-                const float* lo = M.blo + (size_t)node * DP;
-                const float* hi = M.bhi + (size_t)node * DP;
+        // the points pt(0..np-1) (except q) with d2 < thr into the buffer
+        auto scan = [&](int np, auto pt) {
+            for (int base = 0; base < np; base += 32) {
+                const int s = base + lane < np ? pt(base + lane) : -1;
+                float d2 = INFINITY;
+                if (s >= 0 && s < M.n && s != q) {
+                    float xs[DP];
+                    const float4* p = reinterpret_cast<const float4*>(M.pts32 + (size_t)s * DP);
 #pragma unroll
-                for (int k = 0; k < D; ++k) {
-                    const float l = __ldg(lo + k), h = __ldg(hi + k);
-                    const float e = xq[k] < l ? l - xq[k] : (xq[k] > h ? xq[k] - h : 0.f);
-                    bd = fmaf(e, e, bd);
+                    for (int h = 0; h < DP / 4; ++h) {
+                        float4 f = __ldg(p + h);
+                        xs[4 * h] = f.x; xs[4 * h + 1] = f.y; xs[4 * h + 2] = f.z; xs[4 * h + 3] = f.w;
+                    }
+                    d2 = 0.f;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) { const float e = xs[k] - xq[k]; d2 = fmaf(e, e, d2); }
+                }
+                const bool take = d2 < thr;
+                const unsigned bal = __ballot_sync(FULL, take);
+                if (take) { const int pos = cnt + __popc(bal & lt); d[pos] = d2; ix[pos] = s; }
+                cnt += __popc(bal);
+                __syncwarp();
+                if (cnt > CAP - 32) {  // keep the K+1 nearest so far; their largest bounds the rest
+                    thr = warp_keep_smallest(d, ix, cnt, K + 1, lane);
+                    cnt = K + 1;
                 }
             }
-            if (bd > thr * 1.00001f) continue;
-            if (node >= M.P) {
-                const int l = node - M.P;
-                if (l >= M.nleaves) continue;
-                const int s0 = l * M.leaf, s1 = min(s0 + M.leaf, M.n);
-                for (int base = s0; base < s1; base += 32) {
-                    const int s = base + lane;
-                    float d2 = INFINITY;
-                    if (s < s1 && s != q) {
-                        float xs[DP];
-                        const float4* p = reinterpret_cast<const float4*>(M.pts32 + (size_t)s * DP);
-#pragma unroll
-                        for (int h = 0; h < DP / 4; ++h) {
-                            float4 f = __ldg(p + h);
-                            xs[4 * h] = f.x; xs[4 * h + 1] = f.y; xs[4 * h + 2] = f.z; xs[4 * h + 3] = f.w;
-                        }
-                        d2 = 0.f;
-#pragma unroll
-                        for (int k = 0; k < D; ++k) { const float e = xs[k] - xq[k]; d2 = fmaf(e, e, d2); }
-                    }
-                    const bool take = d2 < thr;
-                    const unsigned bal = __ballot_sync(FULL, take);
-                    if (take) {
-                        const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
-                        d[pos] = d2; ix[pos] = s;
-                    }
-                    cnt += __popc(bal);
-                    __syncwarp();
-                    if (cnt > CAP - 32) {  // keep the K+1 nearest so far; their largest bounds the rest
-                        thr = warp_keep_smallest(d, ix, cnt, K + 1, lane);
-                        cnt = K + 1;
-                    }
+        };
+        // ---- phase 1: the smallest ancestor subtree with at least K+1+leaf points
+        const int lq0 = q / M.leaf;
+        int A = M.P + lq0, depthA = 0;  // node id and levels above the leaf
+        int la0 = lq0, la1 = lq0 + 1;
+        while (A > 1 && (min(la1 * M.leaf, M.n) - la0 * M.leaf) < K + 1 + M.leaf) {
+            A >>= 1;
+            ++depthA;
+            la0 = (A << depthA) - M.P;
+            la1 = ((A + 1) << depthA) - M.P;
+            la0 = max(la0, 0);
+            la1 = min(la1, M.nleaves);
+        }
+        {
+            const int s0 = la0 * M.leaf;
+            scan(min(la1 * M.leaf, M.n) - s0, [&](int x) { return s0 + x; });
+        }
+        if (cnt >= K + 1) {
+            thr = warp_keep_smallest(d, ix, cnt, K + 1, lane);
+            cnt = K + 1;
+        }
+        // ---- phase 2: the rest of the tree
+        if (A > 1) {
+            const int lvA = 31 - __clz(A);
+            int sp = 1, nl = 0;
+            if (lane == 0) stk[0] = 1;
+            __syncwarp();
+            while (sp > 0 || nl > 0) {
+                if (nl >= 2 || (sp == 0 && nl > 0)) {
+                    const int L = M.leaf;
+                    scan(nl * L, [&](int x) { return lq[x / L] * L + x % L; });
+                    nl = 0;
+                    continue;
                 }
-            } else {
-                const int c0 = 2 * node, c1 = 2 * node + 1;
-                float b0 = 0.f, b1 = 0.f;
-#pragma unroll
-                for (int k = 0; k < D; ++k) {
-                    const float l0 = __ldg(M.blo + (size_t)c0 * DP + k), h0 = __ldg(M.bhi + (size_t)c0 * DP + k);
-                    const float l1 = __ldg(M.blo + (size_t)c1 * DP + k), h1 = __ldg(M.bhi + (size_t)c1 * DP + k);
-                    const float e0 = xq[k] < l0 ? l0 - xq[k] : (xq[k] > h0 ? xq[k] - h0 : 0.f);
-                    const float e1 = xq[k] < l1 ? l1 - xq[k] : (xq[k] > h1 ? xq[k] - h1 : 0.f);
-                    b0 = fmaf(e0, e0, b0); b1 = fmaf(e1, e1, b1);
+                const int nt = min(sp, 32);
+                const int node = lane < nt ? stk[sp - nt + lane] : 1;
+                sp -= nt;
+                __syncwarp();
+                bool keep = lane < nt;
+                if (keep) {
+                    // already scanned: the phase-1 subtree
+                    const int lv = 31 - __clz(node);
+                    if (lv >= lvA && (node >> (lv - lvA)) == A) keep = false;
                 }
-                if (sp + 2 > 64) {
+                if (keep && isfinite(thr)) {
+                    float bd = 0.f;
+                    const float* lo = M.blo + (size_t)node * DP;
+                    const float* hi = M.bhi + (size_t)node * DP;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        const float l = __ldg(lo + k), h = __ldg(hi + k);
+                        const float e = xq[k] < l ? l - xq[k] : (xq[k] > h ? xq[k] - h : 0.f);
+                        bd = fmaf(e, e, bd);
+                    }
+                    keep = !(bd > thr * 1.00001f);
+                }
+                const bool isleaf = node >= M.P;
+                const bool lvf = keep && isleaf && (node - M.P) < M.nleaves;
+                const bool in = keep && !isleaf;
+                const unsigned bl = __ballot_sync(FULL, lvf), bi = __ballot_sync(FULL, in);
+                if (sp + 2 * __popc(bi) > KNN_STK) {
                     if (lane == 0) atomicOr(M.status, ST_STACK);
                     break;
                 }
-                if (lane == 0) {
-                    if (b0 <= b1) { stk[sp] = c1; stk[sp + 1] = c0; }
-                    else { stk[sp] = c0; stk[sp + 1] = c1; }
+                if (lvf) lq[nl + __popc(bl & lt)] = node - M.P;
+                if (in) {
+                    const int p = sp + 2 * __popc(bi & lt);
+                    stk[p] = 2 * node + 1;
+                    stk[p + 1] = 2 * node;
                 }
-                sp += 2;
+                nl += __popc(bl);
+                sp += 2 * __popc(bi);
                 __syncwarp();
             }
         }

@@ -1036,16 +1036,26 @@ __global__ void __launch_bounds__(FAST_WPB * 32, (D <= 4 ? 16 / FAST_WPB : 1)) k
             sec_own = sv;
         }
         const int* lst = M.knn + (size_t)own * K;
+        // software pipeline: list entries two iterations ahead, coordinates one ahead
+        int jn = lane < K ? __ldg(lst + lane) : -1;
+        int jnn = lane + 32 < K ? __ldg(lst + lane + 32) : -1;
+        float xn[DP], xnl[DP];
+#pragma unroll
+        for (int k = 0; k < DP; ++k) { xn[k] = 0.f; xnl[k] = 0.f; }
+        if (jn >= 0) { load_pt32<D>(M, jn, xn); load_pt32lo<D>(M, jn, xnl); }
         for (int c = lane; c < K; c += 32) {
-            const int j = __ldg(lst + c);
+            const int j = jn;
+            float xj[DP], xjl[DP];
+#pragma unroll
+            for (int k = 0; k < DP; ++k) { xj[k] = xn[k]; xjl[k] = xnl[k]; }
+            jn = jnn;
+            jnn = c + 64 < K ? __ldg(lst + c + 64) : -1;
+            if (jn >= 0) { load_pt32<D>(M, jn, xn); load_pt32lo<D>(M, jn, xnl); }
             if (j < 0) continue;
             bool insig = false;
 #pragma unroll
             for (int s = 0; s < R; ++s) insig |= (j == sig[s]);
             if (insig) continue;
-            float xj[DP], xjl[DP];
-            load_pt32<D>(M, j, xj);
-            load_pt32lo<D>(M, j, xjl);
             float dl[D], A1 = 0.f, A2 = 0.f, A3 = 0.f, dr = 0.f;
 #pragma unroll
             for (int k = 0; k < D; ++k) {
@@ -1293,6 +1303,8 @@ __device__ __forceinline__ void top2_add(float& lo1, float& hi1, int& j1, float&
 constexpr int FB_WPB = 4;
 constexpr int FB_AMB = 4;      // ambiguous candidates kept per lane
 constexpr int FB_AMB_MAX = 32; // ambiguous set re-scored in FP64
+constexpr int FB_STK = 1024;   // tree stack entries per warp
+constexpr int FB_LQ = 64;      // queued leaves per warp
 
 // FP64 decision of a walk restricted to the candidate set `items` (every
 // possible winner is in it): forward-bounded FP64 first, double-double if the
@@ -1334,13 +1346,15 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_fallback_warp(DevMesh M, const 
                                                                unsigned fxcap) {
     constexpr int R = D + 1;
     constexpr int DP = (D <= 4) ? 4 : 8;
-    __shared__ int sstack[FB_WPB][64];
+    __shared__ int sstack[FB_WPB][FB_STK];
+    __shared__ int sleaf[FB_WPB][FB_LQ];
     __shared__ int samb[FB_WPB][FB_AMB_MAX];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned FULL = 0xFFFFFFFFu;
     const float S32 = 5.9604645e-08f;
     const unsigned nq = min(*nfq, fqcap);
     int* stk = sstack[wib];
+    int* lq = sleaf[wib];
     for (unsigned w = blockIdx.x * FB_WPB + wib; w < nq; w += gridDim.x * FB_WPB) {
         const unsigned long long e = fq[w];
         const unsigned v = (unsigned)(e >> 4);
@@ -1489,17 +1503,49 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_fallback_warp(DevMesh M, const 
         top2_warp(lo1, hi1, j1, lo2);
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) H = fminf(H, __shfl_xor_sync(FULL, H, off));
-        // exhaustive tree pass with the shrinking ball (only if the list may miss a winner)
+        // exhaustive tree pass with the shrinking ball (only if the list may miss a winner):
+        // up to 32 stack nodes are tested per step, one per lane; surviving leaves are
+        // queued and evaluated 32 points at a time, after which the bound H shrinks
         bool overflow = false;
         if (!complete || M.K == 0) {
-            int sp = 1;
+            int sp = 1, nl = 0;
             if (lane == 0) stk[0] = 1;
             __syncwarp();
-            while (sp > 0) {
-                const int node = stk[--sp];
+            while (sp > 0 || nl > 0) {
+                if (nl >= 2 || (sp == 0 && nl > 0)) {
+                    const int L = M.leaf;
+                    const int tot = nl * L;
+                    for (int base = 0; base < tot; base += 32) {
+                        const int qq = base + lane;
+                        if (qq < tot) {
+                            const int j = lq[qq / L] * L + (qq % L);
+                            if (j < M.n) {
+                                bool insig = false;
+#pragma unroll
+                                for (int q = 0; q < R; ++q) insig |= (j == sig[q]);
+                                if (!insig) {
+                                    float lo, hi;
+                                    bool ok;
+                                    cand32<D>(M, j, xa, xal, rho, R1, erho, u, lam, U1, LB, relu, lo, hi, ok);
+                                    if (ok) take(j, lo, hi);
+                                }
+                            }
+                        }
+                    }
+                    top2_warp(lo1, hi1, j1, lo2);
+#pragma unroll
+                    for (int off = 16; off > 0; off >>= 1) H = fminf(H, __shfl_xor_sync(FULL, H, off));
+                    nl = 0;
+                    __syncwarp();
+                    continue;
+                }
+                const int nt = min(sp, 32);
+                const int node = lane < nt ? stk[sp - nt + lane] : 0;
+                sp -= nt;
                 __syncwarp();
+                bool keep = lane < nt;
                 const float tp = H;
-                if (isfinite(tp)) {
+                if (keep && isfinite(tp)) {
                     float r2 = 0.f, bd2 = 0.f;
                     const float* blo = M.blo + (size_t)node * DP;
                     const float* bhi = M.bhi + (size_t)node * DP;
@@ -1514,35 +1560,23 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_fallback_warp(DevMesh M, const 
                         bd2 = fmaf(ex, ex, bd2);
                     }
                     const float rr = sqrtf(r2) * 1.0001f + 1e-6f * (float)M.xscale + 1e-4f * fabsf(tp);
-                    if (bd2 > rr * rr) continue;
+                    keep = !(bd2 > rr * rr);
                 }
-                if (node >= M.P) {
-                    const int l = node - M.P;
-                    if (l >= M.nleaves) continue;
-                    const int s0 = l * M.leaf, s1 = min(s0 + M.leaf, M.n);
-                    for (int base = s0; base < s1; base += 32) {
-                        const int j = base + lane;
-                        if (j < s1) {
-                            bool insig = false;
-#pragma unroll
-                            for (int q = 0; q < R; ++q) insig |= (j == sig[q]);
-                            if (!insig) {
-                                float lo, hi;
-                                bool ok;
-                                cand32<D>(M, j, xa, xal, rho, R1, erho, u, lam, U1, LB, relu, lo, hi, ok);
-                                if (ok) take(j, lo, hi);
-                            }
-                        }
-                    }
-                    top2_warp(lo1, hi1, j1, lo2);
-#pragma unroll
-                    for (int off = 16; off > 0; off >>= 1) H = fminf(H, __shfl_xor_sync(FULL, H, off));
-                } else {
-                    if (sp + 2 > 64) { overflow = true; break; }
-                    if (lane == 0) { stk[sp] = 2 * node + 1; stk[sp + 1] = 2 * node; }
-                    sp += 2;
-                    __syncwarp();
+                const bool isleaf = node >= M.P;
+                const bool lv = keep && isleaf && (node - M.P) < M.nleaves;
+                const bool in = keep && !isleaf;
+                const unsigned bl = __ballot_sync(FULL, lv), bi = __ballot_sync(FULL, in);
+                const unsigned lt = (1u << lane) - 1u;
+                if (sp + 2 * __popc(bi) > FB_STK) { overflow = true; break; }
+                if (lv) lq[nl + __popc(bl & lt)] = node - M.P;
+                if (in) {
+                    const int p = sp + 2 * __popc(bi & lt);
+                    stk[p] = 2 * node + 1;
+                    stk[p + 1] = 2 * node;
                 }
+                nl += __popc(bl);
+                sp += 2 * __popc(bi);
+                __syncwarp();
             }
         }
         const bool certified = !overflow && j1 >= 0 && hi1 < lo2;
