@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-integrators", action="store_true")
+    ap.add_argument("--knn", type=int, default=0, help="candidate list length (0 = library default)")
+    ap.add_argument("--leaf-size", type=int, default=0, help="tree leaf size (0 = library default)")
     ap.add_argument("--mc-dirs", type=int, default=1000, help="directions per cell of VI_HEURISTIC_MC")
     return ap.parse_args()
 
@@ -247,7 +249,10 @@ def run_ours(args):
     n, d = pts.shape
     lo, hi = np.zeros(d), np.ones(d)
     method = hvgpu.HV_METHOD_FAST if args.method == "fast" else hvgpu.HV_METHOD_PLAIN
-    params = hvgpu.make_params(method)
+    knobs = {k: v for k, v in (("knn", args.knn), ("leaf_size", args.leaf_size)) if v}
+    params = hvgpu.make_params(method, **knobs)
+    if knobs:
+        cfg["params"] = knobs
     dev_pts = torch.from_numpy(np.ascontiguousarray(pts)).cuda()
     stream = torch.cuda.ExternalStream(ctx.stream())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -401,7 +406,9 @@ def run_ours(args):
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks, "integrators": integ,
             "gpu_launches": int(sum(s["launches"] for s in stats)),
             "stats": {k: st0[k] for k in ("rays", "fallback_rays", "uncertified", "insecure", "dd_rescores",
-                                          "degenerate", "descents", "levels")},
+                                          "degenerate", "descents", "levels", "fallback_tree_rays",
+                                          "fallback_nodes", "fallback_leaves", "fallback_points",
+                                          "ambiguous_sets")},
             "breakdown_ms": breakdown, "serving": serving}
     print(json.dumps(line), flush=True)
 

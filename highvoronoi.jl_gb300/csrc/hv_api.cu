@@ -208,9 +208,9 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         return;
     }
     Scratch prep(st);
-    unsigned* dstat = prep.get<unsigned>(4);
+    unsigned* dstat = prep.get<unsigned>(8);  // vcount, status, insecure queue, exact queue, ambiguous sets
     unsigned long long* dcnt = prep.get<unsigned long long>(C_NCOUNT);
-    CK(cudaMemsetAsync(dstat, 0, 4 * sizeof(unsigned), st));
+    CK(cudaMemsetAsync(dstat, 0, 8 * sizeof(unsigned), st));
     CK(cudaMemsetAsync(dcnt, 0, C_NCOUNT * sizeof(unsigned long long), st));
     // ---- Morton order
     unsigned long long* codes = prep.get<unsigned long long>(n);
@@ -304,8 +304,16 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         const unsigned fqcap = std::max(65536u, vcap / 2);
         unsigned long long* fq = fast ? srch->get<unsigned long long>(fqcap) : nullptr;  // insecure rays
         unsigned long long* fx = fast ? srch->get<unsigned long long>(fqcap) : nullptr;  // uncertified rays
+        hv::AmbQueue aq{};  // ambiguous candidate sets of the FP32 tree search
+        if (fast) {
+            aq.cap = fqcap;
+            aq.e = srch->get<unsigned long long>(aq.cap);
+            aq.n = srch->get<int>(aq.cap);
+            aq.ids = srch->get<int>((size_t)aq.cap * hv::AMB_SET);
+            aq.count = dstat + 4;
+        }
         M.vcount = dstat;
-        CK(cudaMemsetAsync(dstat, 0, 4 * sizeof(unsigned), st));
+        CK(cudaMemsetAsync(dstat, 0, 8 * sizeof(unsigned), st));
         CK(cudaMemsetAsync(dcnt, 0, C_NCOUNT * sizeof(unsigned long long), st));
         int* dfail = fast ? srch->get<int>((size_t)nseeds) : nullptr;
         unsigned* ndfail = fast ? srch->get<unsigned>(1) : nullptr;
@@ -329,13 +337,13 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         while (!overflow && f1 > f0) {
             if (dedup) kt.run(F_OTHER, 1, [&] { launch_register_edges(M, f0, f1, ctx->nsm, st); });
             if (fast) {
-                CK(cudaMemsetAsync(dstat + 2, 0, 2 * sizeof(unsigned), st));
+                CK(cudaMemsetAsync(dstat + 2, 0, 3 * sizeof(unsigned), st));
                 kt.run(F_EXPAND, 1, [&] {
                     launch_expand_fast(M, f0, f1, fq, dstat + 2, fqcap, fx, dstat + 3, fqcap, ctx->nsm, st);
                 });
                 const unsigned long long maxq = std::min<unsigned long long>(fqcap, (unsigned long long)(f1 - f0) * (d + 1));
-                kt.run(F_FALLBACK, 2, [&] {
-                    launch_fallback_warp(M, fq, dstat + 2, fqcap, (unsigned)maxq, fx, dstat + 3, fqcap, ctx->nsm, st);
+                kt.run(F_FALLBACK, 3, [&] {
+                    launch_fallback_warp(M, fq, dstat + 2, fqcap, (unsigned)maxq, fx, dstat + 3, fqcap, aq, ctx->nsm, st);
                     launch_fallback(M, fx, dstat + 3, (unsigned)maxq, ctx->nsm, st);
                 });
             } else {
@@ -401,6 +409,11 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     S.descents = (int64_t)hc[C_DESCENT];
     S.descent_retries = (int64_t)hc[C_DRETRY];
     S.edges_closed = (int64_t)hc[C_EDGECLOSED];
+    S.fallback_tree_rays = (int64_t)hc[C_FBTREE];
+    S.fallback_nodes = (int64_t)hc[C_FBNODES];
+    S.fallback_leaves = (int64_t)hc[C_FBLEAVES];
+    S.fallback_points = (int64_t)hc[C_FBPOINTS];
+    S.ambiguous_sets = (int64_t)hc[C_AMBSET];
     double fam[F_N];
     kt.totals(fam);
     S.ms_knn = fam[F_KNN];
@@ -778,8 +791,10 @@ int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) {
         const unsigned nbig = hs[1];
         if (hs[1] > 0) {  // tier B: facets over the tier-A caps, one block each, shared memory
             R.nbig_host = hs[1];
+            // the largest vertex cap that keeps two blocks per SM
             R.capV = 16;
-            while (R.capV * 2 <= cap_b && hv::poly_area_bytes(d, R.capV * 2, 1, true) <= (size_t)smax) R.capV *= 2;
+            while (R.capV * 2 <= cap_b && hv::poly_area_bytes(d, R.capV * 2, 1, true) <= (size_t)smax / 2)
+                R.capV *= 2;
             CK(cudaMemsetAsync(R.next, 0, sizeof(unsigned long long), st));
             kt.run(2, 1, [&] { run(3); });
             unsigned h2[5] = {0, 0, 0, 0, 0};

@@ -6,6 +6,18 @@
 namespace hv {
 struct DevMesh;
 
+// Rays whose FP32 decision left a small ambiguous candidate set: the queue
+// entry (vertex << 4 | flags | slot), the set size and up to AMB_SET ids each.
+constexpr int AMB_SET = 32;
+struct AmbQueue {
+    unsigned long long* e;
+    int* n;
+    int* ids;
+    unsigned* count;
+    unsigned cap;
+};
+
+
 // hv_prep.cu
 void launch_morton(int d, const double* in, int n, const double* lo, const double* hi,
                    unsigned long long* codes, int* idx, unsigned* status, cudaStream_t st);
@@ -36,9 +48,11 @@ void launch_expand_plain(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cu
 void launch_expand_fast(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq,
                         unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm,
                         cudaStream_t st);
+// FP32 warp tree search of the queued rays, then the FP64 decision of their
+// ambiguous candidate sets (queued in aq); the rest goes to fx.
 void launch_fallback_warp(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap,
-                          unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm,
-                          cudaStream_t st);
+                          unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, const AmbQueue& aq,
+                          int nsm, cudaStream_t st);
 void launch_fallback(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm,
                      cudaStream_t st);
 

@@ -44,6 +44,7 @@ enum : unsigned {
 
 enum {
     C_RAYS = 0, C_FALLBACK, C_UNCERT, C_INSECURE, C_DD, C_DEGEN, C_DESCENT, C_DRETRY, C_EDGECLOSED,
+    C_FBTREE, C_FBNODES, C_FBLEAVES, C_FBPOINTS, C_AMBSET,
     C_NCOUNT
 };
 

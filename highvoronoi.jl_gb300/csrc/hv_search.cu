@@ -30,11 +30,11 @@ void launch_fast_d3(const DevMesh& M, unsigned f0, unsigned f1, unsigned long lo
 void launch_fast_d4(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq, unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
 void launch_fast_d5(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq, unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
 void launch_fast_d6(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq, unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
-void launch_fallback_warp_d2(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
-void launch_fallback_warp_d3(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
-void launch_fallback_warp_d4(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
-void launch_fallback_warp_d5(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
-void launch_fallback_warp_d6(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st);
+void launch_fallback_warp_d2(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, const AmbQueue& aq, int nsm, cudaStream_t st);
+void launch_fallback_warp_d3(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, const AmbQueue& aq, int nsm, cudaStream_t st);
+void launch_fallback_warp_d4(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, const AmbQueue& aq, int nsm, cudaStream_t st);
+void launch_fallback_warp_d5(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, const AmbQueue& aq, int nsm, cudaStream_t st);
+void launch_fallback_warp_d6(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, const AmbQueue& aq, int nsm, cudaStream_t st);
 void launch_fallback_d2(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm, cudaStream_t st);
 void launch_fallback_d3(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm, cudaStream_t st);
 void launch_fallback_d4(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq, int nsm, cudaStream_t st);
@@ -97,13 +97,13 @@ void launch_expand_fast(const DevMesh& M, unsigned f0, unsigned f1, unsigned lon
         default: break;
     }
 }
-void launch_fallback_warp(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm, cudaStream_t st) {
+void launch_fallback_warp(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx, unsigned fxcap, const AmbQueue& aq, int nsm, cudaStream_t st) {
     switch (M.d) {
-        case 2: launch_fallback_warp_d2(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, nsm, st); break;
-        case 3: launch_fallback_warp_d3(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, nsm, st); break;
-        case 4: launch_fallback_warp_d4(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, nsm, st); break;
-        case 5: launch_fallback_warp_d5(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, nsm, st); break;
-        case 6: launch_fallback_warp_d6(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, nsm, st); break;
+        case 2: launch_fallback_warp_d2(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, aq, nsm, st); break;
+        case 3: launch_fallback_warp_d3(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, aq, nsm, st); break;
+        case 4: launch_fallback_warp_d4(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, aq, nsm, st); break;
+        case 5: launch_fallback_warp_d5(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, aq, nsm, st); break;
+        case 6: launch_fallback_warp_d6(M, fq, nfq, fqcap, maxq, fx, nfx, fxcap, aq, nsm, st); break;
         default: break;
     }
 }

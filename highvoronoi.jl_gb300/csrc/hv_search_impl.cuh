@@ -1302,7 +1302,7 @@ __device__ __forceinline__ void top2_add(float& lo1, float& hi1, int& j1, float&
 
 constexpr int FB_WPB = 4;
 constexpr int FB_AMB = 4;      // ambiguous candidates kept per lane
-constexpr int FB_AMB_MAX = 32; // ambiguous set re-scored in FP64
+constexpr int FB_AMB_MAX = AMB_SET; // ambiguous set re-scored in FP64
 constexpr int FB_STK = 1024;   // tree stack entries per warp
 constexpr int FB_LQ = 64;      // queued leaves per warp
 
@@ -1340,14 +1340,15 @@ __device__ int exact_decide_set(const DevMesh& M, const int (&sig)[D + 1], int m
 }
 
 template <int D>
-__global__ void __launch_bounds__(FB_WPB * 32) k_fallback_warp(DevMesh M, const unsigned long long* fq,
+__global__ void __launch_bounds__(FB_WPB * 32, 4) k_fallback_warp(DevMesh M, const unsigned long long* fq,
                                                                const unsigned* nfq, unsigned fqcap,
                                                                unsigned long long* fx, unsigned* nfx,
-                                                               unsigned fxcap) {
+                                                               unsigned fxcap, AmbQueue aq) {
     constexpr int R = D + 1;
     constexpr int DP = (D <= 4) ? 4 : 8;
     __shared__ int sstack[FB_WPB][FB_STK];
     __shared__ int sleaf[FB_WPB][FB_LQ];
+    __shared__ int scq[FB_WPB][64];
     __shared__ int samb[FB_WPB][FB_AMB_MAX];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned FULL = 0xFFFFFFFFu;
@@ -1355,6 +1356,7 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_fallback_warp(DevMesh M, const 
     const unsigned nq = min(*nfq, fqcap);
     int* stk = sstack[wib];
     int* lq = sleaf[wib];
+    int* cq = scq[wib];
     for (unsigned w = blockIdx.x * FB_WPB + wib; w < nq; w += gridDim.x * FB_WPB) {
         const unsigned long long e = fq[w];
         const unsigned v = (unsigned)(e >> 4);
@@ -1508,6 +1510,7 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_fallback_warp(DevMesh M, const 
         // queued and evaluated 32 points at a time, after which the bound H shrinks
         bool overflow = false;
         if (!complete || M.K == 0) {
+            long long nnodes = 0, nleaves_seen = 0, npoints_in = 0;
             int sp = 1, nl = 0;
             if (lane == 0) stk[0] = 1;
             __syncwarp();
@@ -1515,21 +1518,62 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_fallback_warp(DevMesh M, const 
                 if (nl >= 2 || (sp == 0 && nl > 0)) {
                     const int L = M.leaf;
                     const int tot = nl * L;
+                    nleaves_seen += nl;
+                    // a point can beat the bound H only inside the ball of parameter H (the
+                    // node test for a single point, same margins); the survivors, compacted
+                    // into full warps, get the interval evaluation
+                    const float tp = H;
+                    float cH[D];
+                    float rr2 = INFINITY;
+                    if (isfinite(tp)) {
+                        float r2 = 0.f;
+#pragma unroll
+                        for (int k = 0; k < D; ++k) {
+                            const float off = fmaf(tp, u[k], rho[k]);
+                            const float w2 = db[k] - off;
+                            r2 = fmaf(w2, w2, r2);
+                            cH[k] = xa[k] + (xal[k] + off);
+                        }
+                        const float rr = sqrtf(r2) * 1.0001f + 1e-6f * (float)M.xscale + 1e-4f * fabsf(tp);
+                        rr2 = rr * rr;
+                    }
+                    int nc = 0;
                     for (int base = 0; base < tot; base += 32) {
                         const int qq = base + lane;
+                        int j = -1;
                         if (qq < tot) {
-                            const int j = lq[qq / L] * L + (qq % L);
-                            if (j < M.n) {
-                                bool insig = false;
+                            j = lq[qq / L] * L + (qq % L);
+                            if (j >= M.n) j = -1;
+                        }
+                        if (j >= 0) {
 #pragma unroll
-                                for (int q = 0; q < R; ++q) insig |= (j == sig[q]);
-                                if (!insig) {
+                            for (int q = 0; q < R; ++q) if (j == sig[q]) j = -1;
+                        }
+                        if (j >= 0 && rr2 < INFINITY) {
+                            float xj[DP];
+                            load_pt32<D>(M, j, xj);
+                            float d2 = 0.f;
+#pragma unroll
+                            for (int k = 0; k < D; ++k) { const float e = xj[k] - cH[k]; d2 = fmaf(e, e, d2); }
+                            if (d2 > rr2) j = -1;
+                        }
+                        const unsigned bj = __ballot_sync(FULL, j >= 0);
+                        if (j >= 0) cq[nc + __popc(bj & ((1u << lane) - 1u))] = j;
+                        nc += __popc(bj);
+                        npoints_in += __popc(bj);
+                        __syncwarp();
+                        if (nc >= 32 || (base + 32 >= tot && nc > 0)) {
+                            for (int b2 = 0; b2 < nc; b2 += 32) {
+                                if (b2 + lane < nc) {
+                                    const int jj = cq[b2 + lane];
                                     float lo, hi;
                                     bool ok;
-                                    cand32<D>(M, j, xa, xal, rho, R1, erho, u, lam, U1, LB, relu, lo, hi, ok);
-                                    if (ok) take(j, lo, hi);
+                                    cand32<D>(M, jj, xa, xal, rho, R1, erho, u, lam, U1, LB, relu, lo, hi, ok);
+                                    if (ok) take(jj, lo, hi);
                                 }
                             }
+                            nc = 0;
+                            __syncwarp();
                         }
                     }
                     top2_warp(lo1, hi1, j1, lo2);
@@ -1542,6 +1586,7 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_fallback_warp(DevMesh M, const 
                 const int nt = min(sp, 32);
                 const int node = lane < nt ? stk[sp - nt + lane] : 0;
                 sp -= nt;
+                nnodes += nt;
                 __syncwarp();
                 bool keep = lane < nt;
                 const float tp = H;
@@ -1578,6 +1623,12 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_fallback_warp(DevMesh M, const 
                 sp += 2 * __popc(bi);
                 __syncwarp();
             }
+            if (lane == 0) {
+                count_add(M.cnt + C_FBTREE);
+                atomicAdd(M.cnt + C_FBNODES, (unsigned long long)nnodes);
+                atomicAdd(M.cnt + C_FBLEAVES, (unsigned long long)nleaves_seen);
+                atomicAdd(M.cnt + C_FBPOINTS, (unsigned long long)npoints_in);
+            }
         }
         const bool certified = !overflow && j1 >= 0 && hi1 < lo2;
         if (certified) {
@@ -1605,24 +1656,53 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_fallback_warp(DevMesh M, const 
                     if (amb_lo[q] <= H) samb[wib][pos++] = amb_j[q];
             }
             __syncwarp();
-            if (lane == 0) {
-                int win = -1;
-                if (!over && total <= FB_AMB_MAX && total > 0) {
-                    win = exact_decide_set<D>(M, sig, m, samb[wib], total);
-                }
-                if (win >= 0) {
-                    int ns[R];
-                    make_sig<D>(sig, m, win, ns);
-                    bool is_new;
-                    vertex_insert<D>(M, ns, win, is_new);
-                } else {
-                    const unsigned slot = atomicAdd(nfx, 1u);
-                    if (slot < fxcap) fx[slot] = e;
-                    else set_status(M, ST_QUEUE);
-                }
+            // the set goes to the FP64 decision kernel (k_decide_sets); without a usable
+            // set, or with its queue full, the ray is redone by the exact tree search
+            unsigned slot = 0xFFFFFFFFu;
+            if (lane == 0 && !over && total <= FB_AMB_MAX && total > 0) {
+                slot = atomicAdd(aq.count, 1u);
+                if (slot >= aq.cap) slot = 0xFFFFFFFFu;
+            }
+            slot = __shfl_sync(FULL, slot, 0);
+            if (slot != 0xFFFFFFFFu) {
+                if (lane < total) aq.ids[(size_t)slot * AMB_SET + lane] = samb[wib][lane];
+                if (lane == 0) { aq.e[slot] = e; aq.n[slot] = total; }
+            } else if (lane == 0) {
+                const unsigned fs = atomicAdd(nfx, 1u);
+                if (fs < fxcap) fx[fs] = e;
+                else set_status(M, ST_QUEUE);
             }
         }
         __syncwarp();
+    }
+}
+
+// FP64 (then double-double) decision of the queued ambiguous sets, one ray per
+// thread; an undecided ray is redone by the exact tree search (k_fallback).
+template <int D>
+__global__ void __launch_bounds__(128) k_decide_sets(DevMesh M, AmbQueue aq, unsigned long long* fx, unsigned* nfx,
+                                                     unsigned fxcap) {
+    constexpr int R = D + 1;
+    const unsigned nq = min(*aq.count, aq.cap);
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nq; w += gridDim.x * blockDim.x) {
+        count_add(M.cnt + C_AMBSET);
+        const unsigned long long e = aq.e[w];
+        const unsigned v = (unsigned)(e >> 4);
+        const int m = (int)(e & 7);
+        int sig[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) sig[k] = M.vsig[(size_t)v * R + k];
+        const int win = exact_decide_set<D>(M, sig, m, aq.ids + (size_t)w * AMB_SET, aq.n[w]);
+        if (win >= 0) {
+            int ns[R];
+            make_sig<D>(sig, m, win, ns);
+            bool is_new;
+            vertex_insert<D>(M, ns, win, is_new);
+        } else {
+            const unsigned fs = atomicAdd(nfx, 1u);
+            if (fs < fxcap) fx[fs] = e;
+            else set_status(M, ST_QUEUE);
+        }
     }
 }
 
@@ -1887,18 +1967,23 @@ static void launch_fast_t(const DevMesh& M, unsigned f0, unsigned f1, unsigned l
 template <int D>
 static void launch_fallback_warp_t(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq,
                                    unsigned fqcap, unsigned maxq, unsigned long long* fx, unsigned* nfx,
-                                   unsigned fxcap, int nsm, cudaStream_t st) {
+                                   unsigned fxcap, const AmbQueue& aq, int nsm, cudaStream_t st) {
     if (!maxq) return;
+    // grid-stride over the queue: a few resident waves, so empty levels cost little
     unsigned blocks = (maxq + FB_WPB - 1) / FB_WPB;
-    if (blocks > (unsigned)nsm * 32) blocks = (unsigned)nsm * 32;
-    k_fallback_warp<D><<<blocks, FB_WPB * 32, 0, st>>>(M, fq, nfq, fqcap, fx, nfx, fxcap);
+    if (blocks > (unsigned)nsm * 8) blocks = (unsigned)nsm * 8;
+    k_fallback_warp<D><<<blocks, FB_WPB * 32, 0, st>>>(M, fq, nfq, fqcap, fx, nfx, fxcap, aq);
+    unsigned b2 = (min(maxq, aq.cap) + 127) / 128;
+    if (b2 > (unsigned)nsm * 2) b2 = (unsigned)nsm * 2;
+    if (b2 < 1) b2 = 1;
+    k_decide_sets<D><<<b2, 128, 0, st>>>(M, aq, fx, nfx, fxcap);
 }
 template <int D>
 static void launch_fallback_t(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq,
                               int nsm, cudaStream_t st) {
     if (!maxq) return;
     unsigned blocks = (maxq + 127) / 128;
-    if (blocks > (unsigned)nsm * 16) blocks = (unsigned)nsm * 16;
+    if (blocks > (unsigned)nsm * 4) blocks = (unsigned)nsm * 4;
     k_fallback<D><<<blocks, 128, 0, st>>>(M, fq, nfq, maxq);
 }
 

@@ -49,11 +49,13 @@ STAT_FIELDS = ("vertices", "rays", "fallback_rays", "uncertified", "insecure", "
 TIME_FIELDS = ("ms_prepare", "ms_search", "ms_total", "ms_knn", "ms_descent", "ms_expand", "ms_fallback",
                "ms_centers", "ms_canonical")
 POLY_FIELDS = ("ms_poly_incidence", "ms_poly_facets", "ms_poly_big", "ms_poly_total")
+FALLBACK_FIELDS = ("fallback_tree_rays", "fallback_nodes", "fallback_leaves", "fallback_points", "ambiguous_sets")
 
 
 class Stats(ctypes.Structure):
     _fields_ = ([(n, ctypes.c_int64) for n in STAT_FIELDS] + [(n, ctypes.c_double) for n in TIME_FIELDS] +
-                [("poly_big_facets", ctypes.c_int64)] + [(n, ctypes.c_double) for n in POLY_FIELDS])
+                [("poly_big_facets", ctypes.c_int64)] + [(n, ctypes.c_double) for n in POLY_FIELDS] +
+                [(n, ctypes.c_int64) for n in FALLBACK_FIELDS])
 
 
 _lock = threading.Lock()

@@ -102,6 +102,12 @@ typedef struct {
     double ms_poly_facets;     /* shared-memory facet kernel (device) */
     double ms_poly_big;        /* global-memory facet kernel (device) */
     double ms_poly_total;      /* whole call (host wall clock) */
+    /* tree pass of the FP32 fallback (rays whose candidate list may miss the winner) */
+    int64_t fallback_tree_rays;
+    int64_t fallback_nodes;    /* tree nodes tested */
+    int64_t fallback_leaves;   /* leaves scanned */
+    int64_t fallback_points;   /* points inside the bounding ball (interval-evaluated) */
+    int64_t ambiguous_sets;    /* candidate sets decided in FP64 after the FP32 tree search */
 } hv_stats;
 
 int hv_version(void);
