@@ -900,7 +900,7 @@ __device__ __forceinline__ void load_pt32lo(const DevMesh& M, int j, float (&x)[
 }
 
 template <int D>
-__global__ void __launch_bounds__(FAST_WPB * 32, (D <= 4 ? 16 / FAST_WPB : 1)) k_expand_fast(DevMesh M, unsigned f0, unsigned f1,
+__global__ void __launch_bounds__(FAST_WPB * 32, 16 / FAST_WPB) k_expand_fast(DevMesh M, unsigned f0, unsigned f1,
                                                                unsigned long long* fq, unsigned* nfq,
                                                                unsigned fqcap, unsigned long long* fx,
                                                                unsigned* nfx, unsigned fxcap) {
@@ -910,6 +910,7 @@ __global__ void __launch_bounds__(FAST_WPB * 32, (D <= 4 ? 16 / FAST_WPB : 1)) k
     __shared__ float sU[FAST_WPB][R][D];
     __shared__ float sLam[FAST_WPB][R];
     __shared__ float sLb[FAST_WPB][R];
+    __shared__ float sU1[FAST_WPB][R];
     __shared__ float sCond[FAST_WPB];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned FULL = 0xFFFFFFFFu;
@@ -997,19 +998,34 @@ __global__ void __launch_bounds__(FAST_WPB * 32, (D <= 4 ? 16 / FAST_WPB : 1)) k
 #pragma unroll
         for (int k = 0; k < D; ++k) { R1 += fabsf(rho[k]); rmax = fmaxf(rmax, fabsf(rho[k])); }
         const float erho = 2.f * S32 * rmax;  // rho is the rounded FP64 centre offset
-        float u32[R][D], lam32[R], U1[R], LB[R];
+        // d >= 5: the rays' directions stay in shared memory (broadcast reads in the
+        // candidate loop) instead of (d+1) x (d+3) registers, for occupancy
+        constexpr bool RAYS_SMEM = D >= 5;
+        constexpr int RR = RAYS_SMEM ? 1 : R;
+        float u32[RR][D], lam32[RR], U1[RR], LB[RR];
         float lo1[R], hi1[R], lo2[R];
         int j1[R];
+        if (RAYS_SMEM) {
+            if (lane < R && ((rmask >> lane) & 1u)) {
+                float a1 = 0.f;
+#pragma unroll
+                for (int k = 0; k < D; ++k) a1 += fabsf(sU[wib][lane][k]);
+                sU1[wib][lane] = a1;
+            }
+            __syncwarp();
+        }
 #pragma unroll
         for (int m = 0; m < R; ++m) {
-            U1[m] = 0.f; lam32[m] = 0.f; LB[m] = 0.f;
+            if (!RAYS_SMEM) {
+                U1[m % RR] = 0.f; lam32[m % RR] = 0.f; LB[m % RR] = 0.f;
 #pragma unroll
-            for (int k = 0; k < D; ++k) u32[m][k] = 0.f;
-            if ((rmask >> m) & 1u) {
+                for (int k = 0; k < D; ++k) u32[m % RR][k] = 0.f;
+                if ((rmask >> m) & 1u) {
 #pragma unroll
-                for (int k = 0; k < D; ++k) { u32[m][k] = sU[wib][m][k]; U1[m] += fabsf(u32[m][k]); }
-                lam32[m] = sLam[wib][m];
-                LB[m] = sLb[wib][m];
+                    for (int k = 0; k < D; ++k) { u32[m % RR][k] = sU[wib][m][k]; U1[m % RR] += fabsf(u32[m % RR][k]); }
+                    lam32[m % RR] = sLam[wib][m];
+                    LB[m % RR] = sLb[wib][m];
+                }
             }
             lo1[m] = INFINITY; hi1[m] = INFINITY; lo2[m] = INFINITY; j1[m] = -1;
         }
@@ -1072,9 +1088,16 @@ __global__ void __launch_bounds__(FAST_WPB * 32, (D <= 4 ? 16 / FAST_WPB : 1)) k
                 if (!((rmask >> m) & 1u)) continue;
                 float du = 0.f, B = 0.f;
 #pragma unroll
-                for (int k = 0; k < D; ++k) { du = fmaf(dl[k], u32[m][k], du); B = fmaf(fabsf(dl[k]), fabsf(u32[m][k]), B); }
-                const float den = 2.f * (du - lam32[m]);
-                const float e_den = CD * (B + fabsf(lam32[m])) + 2.f * relu * (A1 + LB[m]) + TINY * U1[m];
+                for (int k = 0; k < D; ++k) {
+                    const float uk = RAYS_SMEM ? sU[wib][m][k] : u32[m % RR][k];
+                    du = fmaf(dl[k], uk, du);
+                    B = fmaf(fabsf(dl[k]), fabsf(uk), B);
+                }
+                const float lm = RAYS_SMEM ? sLam[wib][m] : lam32[m % RR];
+                const float lbm = RAYS_SMEM ? sLb[wib][m] : LB[m % RR];
+                const float u1m = RAYS_SMEM ? sU1[wib][m] : U1[m % RR];
+                const float den = 2.f * (du - lm);
+                const float e_den = CD * (B + fabsf(lm)) + 2.f * relu * (A1 + lbm) + TINY * u1m;
                 float lo, hi;
                 if (den > e_den) {
                     const float r = __fdividef(1.f, den);
@@ -1677,32 +1700,119 @@ __global__ void __launch_bounds__(FB_WPB * 32, 4) k_fallback_warp(DevMesh M, con
     }
 }
 
-// FP64 (then double-double) decision of the queued ambiguous sets, one ray per
-// thread; an undecided ray is redone by the exact tree search (k_fallback).
+// FP64 (then double-double) decision of the queued ambiguous sets.  Many sets:
+// one per thread.  Few sets (latency-bound): one per warp -- lane 0 sets the ray
+// up, every lane evaluates one candidate in FP64, lane 0 folds them in the order
+// of the set (the same decisions as the serial pass) and re-scores the rest in
+// double-double if needed.  An undecided ray is redone by the exact tree search
+// (k_fallback).
+constexpr int DS_WPB = 4;
+
 template <int D>
-__global__ void __launch_bounds__(128) k_decide_sets(DevMesh M, AmbQueue aq, unsigned long long* fx, unsigned* nfx,
-                                                     unsigned fxcap) {
+__global__ void __launch_bounds__(DS_WPB * 32) k_decide_sets(DevMesh M, AmbQueue aq, unsigned long long* fx,
+                                                             unsigned* nfx, unsigned fxcap) {
     constexpr int R = D + 1;
+    __shared__ Query<D> sq[DS_WPB];
+    __shared__ Cand sc[DS_WPB][AMB_SET];
+    __shared__ int sok[DS_WPB];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned FULL = 0xFFFFFFFFu;
     const unsigned nq = min(*aq.count, aq.cap);
-    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nq; w += gridDim.x * blockDim.x) {
-        count_add(M.cnt + C_AMBSET);
+    if (nq > 2u * gridDim.x * DS_WPB) {  // many sets: one per thread (throughput)
+        for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nq; w += gridDim.x * blockDim.x) {
+            count_add(M.cnt + C_AMBSET);
+            const unsigned long long e = aq.e[w];
+            const unsigned v = (unsigned)(e >> 4);
+            const int m = (int)(e & 7);
+            int sig[R];
+#pragma unroll
+            for (int k = 0; k < R; ++k) sig[k] = M.vsig[(size_t)v * R + k];
+            const int win = exact_decide_set<D>(M, sig, m, aq.ids + (size_t)w * AMB_SET, aq.n[w]);
+            if (win >= 0) {
+                int ns[R];
+                make_sig<D>(sig, m, win, ns);
+                bool is_new;
+                vertex_insert<D>(M, ns, win, is_new);
+            } else {
+                const unsigned fs = atomicAdd(nfx, 1u);
+                if (fs < fxcap) fx[fs] = e;
+                else set_status(M, ST_QUEUE);
+            }
+        }
+        return;
+    }
+    for (unsigned w = blockIdx.x * DS_WPB + wib; w < nq; w += gridDim.x * DS_WPB) {  // few sets: one per warp
         const unsigned long long e = aq.e[w];
         const unsigned v = (unsigned)(e >> 4);
         const int m = (int)(e & 7);
+        const int nitems = aq.n[w];
+        const int* items = aq.ids + (size_t)w * AMB_SET;
         int sig[R];
 #pragma unroll
         for (int k = 0; k < R; ++k) sig[k] = M.vsig[(size_t)v * R + k];
-        const int win = exact_decide_set<D>(M, sig, m, aq.ids + (size_t)w * AMB_SET, aq.n[w]);
-        if (win >= 0) {
-            int ns[R];
-            make_sig<D>(sig, m, win, ns);
-            bool is_new;
-            vertex_insert<D>(M, ns, win, is_new);
-        } else {
-            const unsigned fs = atomicAdd(nfx, 1u);
-            if (fs < fxcap) fx[fs] = e;
-            else set_status(M, ST_QUEUE);
+        if (lane == 0) {
+            count_add(M.cnt + C_AMBSET);
+            sok[wib] = setup_walk<D>(M, sig, m, sq[wib]) ? 1 : 0;
         }
+        __syncwarp();
+        int win = -1;
+        if (sok[wib]) {
+            const Query<D>& q = sq[wib];
+            Cand c;
+            c.item = -1;
+            c.t = c.lo = c.hi = INFINITY;
+            if (lane < nitems && items[lane] < M.n) {
+                SearchOut Rl;
+                Rl.best = Cand{-1, INFINITY, INFINITY, INFINITY};
+                Rl.second_lo = INFINITY;
+                Rl.namb = 0;
+                Rl.overflow = false;
+                eval_point<D>(M, q, items[lane], Rl);
+                c = Rl.best;
+            }
+            sc[wib][lane] = c;
+            const bool planes = __any_sync(FULL, lane < nitems && items[lane] >= M.n);
+            __syncwarp();
+            if (lane == 0) {
+                SearchOut Rs;
+                Rs.best = Cand{-1, INFINITY, INFINITY, INFINITY};
+                Rs.second_lo = INFINITY;
+                Rs.namb = 0;
+                Rs.overflow = false;
+                for (int k = 0; k < nitems; ++k)
+                    if (sc[wib][k].item >= 0) consider(Rs, sc[wib][k]);
+                if (planes) eval_planes<D>(M, q, Rs);
+                if (Rs.best.item >= 0) {
+                    if (Rs.best.hi < Rs.second_lo) {
+                        win = Rs.best.item;
+                    } else {
+                        count_add(M.cnt + C_DD);
+                        if (Rs.overflow) set_status(M, ST_AMB);
+                        int its[HV_NAMB + 1];
+                        its[0] = Rs.best.item;
+                        int n2 = 1;
+                        for (int k = 0; k < Rs.namb; ++k)
+                            if (Rs.amb[k].lo <= Rs.best.hi) its[n2++] = Rs.amb[k].item;
+                        bool degen = false;
+                        win = dd_rescore_walk<D>(M, sig, m, its, n2, degen);
+                        if (degen) { count_add(M.cnt + C_DEGEN); set_status(M, ST_DEGEN); }
+                    }
+                }
+            }
+        }
+        if (lane == 0) {
+            if (win >= 0) {
+                int ns[R];
+                make_sig<D>(sig, m, win, ns);
+                bool is_new;
+                vertex_insert<D>(M, ns, win, is_new);
+            } else {
+                const unsigned fs = atomicAdd(nfx, 1u);
+                if (fs < fxcap) fx[fs] = e;
+                else set_status(M, ST_QUEUE);
+            }
+        }
+        __syncwarp();
     }
 }
 
@@ -1973,10 +2083,10 @@ static void launch_fallback_warp_t(const DevMesh& M, const unsigned long long* f
     unsigned blocks = (maxq + FB_WPB - 1) / FB_WPB;
     if (blocks > (unsigned)nsm * 8) blocks = (unsigned)nsm * 8;
     k_fallback_warp<D><<<blocks, FB_WPB * 32, 0, st>>>(M, fq, nfq, fqcap, fx, nfx, fxcap, aq);
-    unsigned b2 = (min(maxq, aq.cap) + 127) / 128;
-    if (b2 > (unsigned)nsm * 2) b2 = (unsigned)nsm * 2;
+    unsigned b2 = (min(maxq, aq.cap) + DS_WPB - 1) / DS_WPB;
+    if (b2 > (unsigned)nsm * 4) b2 = (unsigned)nsm * 4;
     if (b2 < 1) b2 = 1;
-    k_decide_sets<D><<<b2, 128, 0, st>>>(M, aq, fx, nfx, fxcap);
+    k_decide_sets<D><<<b2, DS_WPB * 32, 0, st>>>(M, aq, fx, nfx, fxcap);
 }
 template <int D>
 static void launch_fallback_t(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq, unsigned maxq,
