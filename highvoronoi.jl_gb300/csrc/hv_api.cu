@@ -238,6 +238,12 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         xs = std::max(xs, std::max(std::fabs(mesh->lo[k]), std::fabs(mesh->hi[k])));
     }
     M.xscale = xs;
+    for (int k = 0; k < d; ++k) { M.lo32[k] = (float)M.lo[k]; M.hi32[k] = (float)M.hi[k]; }
+    M.xs32 = (float)xs;
+    M.tiny32 = (float)(4e-14 * xs);
+    M.e13_32 = (float)(1e-13 * xs);
+    M.e12_32 = (float)(1e-12 * xs);
+    M.ulp32 = (float)(xs * 5.9604645e-08);
     M.leaf = mesh->prm.leaf_size > 0 ? mesh->prm.leaf_size : 16;
     M.nleaves = (n + M.leaf - 1) / M.leaf;
     M.P = (int)next_pow2((unsigned long long)M.nleaves);

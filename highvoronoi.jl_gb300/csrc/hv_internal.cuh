@@ -66,6 +66,13 @@ struct DevMesh {
     unsigned long long ehmask;
     double lo[HV_MAXD], hi[HV_MAXD];
     double xscale;  // bound on |coordinate|
+    // FP32 copies for the FP32 kernels (rounded once on the host)
+    float lo32[HV_MAXD], hi32[HV_MAXD];
+    float xs32;      // (float)xscale
+    float tiny32;    // (float)(4e-14 xscale)
+    float e13_32;    // (float)(1e-13 xscale)
+    float e12_32;    // (float)(1e-12 xscale)
+    float ulp32;     // (float)(xscale 2^-24)
     const double* pts;
     const float* pts32;
     const float* pts32lo;  // residual x - (float)x, so that x = hi + lo to ~2^-48

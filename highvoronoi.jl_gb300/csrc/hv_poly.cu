@@ -82,13 +82,14 @@ __host__ __device__ inline size_t farea_bytes(const FCaps& c) {
     b += 4 * (size_t)c.capI;          // its
     b += 4 * ((size_t)c.capF + 1);    // seg
     b += 4 * 16;                      // wsum
+    b += (size_t)c.capF;              // fneed
     return (b + 255) / 256 * 256;
 }
 
 template <int D, class K>
 struct FArea {
     double* fvol; double* dred; long long* ll; K* buf; K* fcode; K* faux;
-    unsigned* fv; unsigned* vit; unsigned* its; unsigned* seg; int* wsum;
+    unsigned* fv; unsigned* vit; unsigned* its; unsigned* seg; int* wsum; unsigned char* fneed;
     __device__ FArea(unsigned char* base, const FCaps& c) {
         constexpr int DM = D > 1 ? D - 1 : 1;
         fvol = (double*)base;
@@ -102,6 +103,7 @@ struct FArea {
         its = vit + (size_t)c.capV * DM;
         seg = its + c.capI;
         wsum = (int*)(seg + c.capF + 1);
+        fneed = (unsigned char*)(wsum + 16);
     }
 };
 
@@ -445,7 +447,53 @@ __device__ int poly_facet(const PolyIn& P, int i, int k, long long t, const FAre
         if (g_or(g, bad, W.wsum)) return F_BAD;
         if (j + 1 < D) off[j + 1] = off[j] + m;
     }
-    // ---- volumes of the faces, bottom-up (levels D-3 .. 1)
+    // ---- faces whose volume is used: the level-1 faces off facet vertex 0, then
+    // every sub-face of a used face that misses that face's reference vertex
+    if (D >= 4) {
+        for (int f = g.rank; f < nf[1]; f += g.size) {
+            bool through = false;
+#pragma unroll
+            for (int x = 0; x < DM; ++x) through |= (W.vit[x] == (unsigned)f);
+            W.fneed[off[1] + f] = through ? 0 : 1;
+        }
+        g.sync();
+        int bad = 0;
+        for (int j = 1; j <= D - 3; ++j) {
+            for (int ch = g.rank; ch < nf[j + 1]; ch += g.size) {
+                unsigned T[DM];
+                items_of(j + 1, ch, T);
+                const K cc = W.fcode[off[j + 1] + ch];
+                unsigned char nd = 0;
+                for (int q = 0; q <= j && !nd; ++q) {
+                    int pidx;
+                    if (q == j) {
+                        pidx = (int)(cc >> B);
+                    } else {
+                        unsigned Pt[DM];
+                        int w = 0;
+                        for (int x = 0; x <= j; ++x) if (x != q) Pt[w++] = T[x];
+                        K pc = 0;
+                        if (!code_of(Pt, j, pc)) { bad = 1; break; }
+                        if (j == 1) pidx = (int)pc;
+                        else {
+                            pidx = lower_bound_k<K>(W.fcode + off[j], nf[j], pc);
+                            if (pidx >= nf[j] || W.fcode[off[j] + pidx] != pc) { bad = 1; break; }
+                        }
+                    }
+                    if (!W.fneed[off[j] + pidx]) continue;
+                    const unsigned rep = (unsigned)W.faux[off[j] + pidx];
+                    bool through = false;
+#pragma unroll
+                    for (int x = 0; x < DM; ++x) through |= (W.vit[rep * DM + x] == T[q]);
+                    if (!through) nd = 1;
+                }
+                W.fneed[off[j + 1] + ch] = nd;
+            }
+            g.sync();
+        }
+        if (g_or(g, bad, W.wsum)) return F_BAD;
+    }
+    // ---- volumes of the used faces, bottom-up (levels D-3 .. 1)
     for (int j = D - 3; j >= 1; --j) {
         const int nc = nf[j + 1], mm = j + 1;
         const int np = nc * mm, n2 = pow2_ge(np);
@@ -471,9 +519,9 @@ __device__ int poly_facet(const PolyIn& P, int i, int k, long long t, const FAre
                         if (pidx >= nf[j] || W.fcode[off[j] + pidx] != pc) { bad = 1; pidx = 0; }
                     }
                 }
-                // skip sub-faces through the parent's reference vertex
+                // skip unused parents and sub-faces through the parent's reference vertex
                 const unsigned rep = (unsigned)W.faux[off[j] + pidx];
-                bool through = false;
+                bool through = !W.fneed[off[j] + pidx];
 #pragma unroll
                 for (int x = 0; x < DM; ++x) through |= (W.vit[rep * DM + x] == T[q]);
                 W.buf[ch * mm + q] = through ? SENT : (((K)pidx << B) | (K)ch);

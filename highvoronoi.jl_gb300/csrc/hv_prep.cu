@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float
     const int K = M.K;
     const unsigned FULL = 0xFFFFFFFFu;
     const unsigned lt = (1u << lane) - 1u;
-    const float ex = (float)(M.xscale * 5.9604645e-08);
+    const float ex = M.ulp32;
     float* d = sd[wib];
     int* ix = si[wib];
     int* stk = sstack[wib];

@@ -1030,7 +1030,7 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 16 / FAST_WPB) k_expand_fast(De
             lo1[m] = INFINITY; hi1[m] = INFINITY; lo2[m] = INFINITY; j1[m] = -1;
         }
         const float CN = (4.f * D + 20.f) * S32, CD = (4.f * D + 16.f) * S32;
-        const float TINY = (float)(4e-14 * M.xscale);
+        const float TINY = M.tiny32;
         const int K = M.K;
         // candidate list: the real generator of the vertex with the largest
         // complete radius (every generator is on the current sphere, so any
@@ -1151,7 +1151,7 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 16 / FAST_WPB) k_expand_fast(De
             // boundary planes in FP32 with the same error model
             float plo1 = INFINITY, phi1 = INFINITY, plo2 = INFINITY;
             int pj1 = -1;
-#pragma unroll
+#pragma unroll 1
             for (int p = 0; p < 2 * D; ++p) {
                 const int it = M.n + p;
                 bool ex = false;
@@ -1161,7 +1161,7 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 16 / FAST_WPB) k_expand_fast(De
                 const int k = p >> 1;
                 const bool upper = (p & 1) == 0;
                 const float uk = upper ? u[k] : -u[k];
-                const float hk = (float)M.hi[k], lk = (float)M.lo[k];
+                const float hk = M.hi32[k], lk = M.lo32[k];
                 const float ck = xa[k] + (xal[k] + rho[k]);
                 const float num = upper ? (hk - ck) : (ck - lk);
                 const float e_num = 4.f * S32 * (fabsf(hk) + fabsf(lk) + fabsf(xa[k]) + fabsf(rho[k])) + erho + TINY;
@@ -1261,7 +1261,7 @@ __device__ __forceinline__ void cand32(const DevMesh& M, int j, const float* xa,
     constexpr int DP = (D <= 4) ? 4 : 8;
     const float S32 = 5.9604645e-08f;
     const float CN = (4.f * D + 20.f) * S32, CD = (4.f * D + 16.f) * S32;
-    const float TINY = (float)(4e-14 * M.xscale);
+    const float TINY = M.tiny32;
     float xj[DP], xjl[DP];
     load_pt32<D>(M, j, xj);
     load_pt32lo<D>(M, j, xjl);
@@ -1479,7 +1479,7 @@ __global__ void __launch_bounds__(FB_WPB * 32, 4) k_fallback_warp(DevMesh M, con
         };
         // planes (lane 0)
         if (lane == 0) {
-            const float TINY = (float)(4e-14 * M.xscale);
+            const float TINY = M.tiny32;
 #pragma unroll
             for (int p = 0; p < 2 * D; ++p) {
                 const int it = M.n + p;
@@ -1490,7 +1490,7 @@ __global__ void __launch_bounds__(FB_WPB * 32, 4) k_fallback_warp(DevMesh M, con
                 const int k = p >> 1;
                 const bool upper = (p & 1) == 0;
                 const float uk = upper ? u[k] : -u[k];
-                const float hk = (float)M.hi[k], lk = (float)M.lo[k];
+                const float hk = M.hi32[k], lk = M.lo32[k];
                 const float ck = xa[k] + (xal[k] + rho[k]);
                 const float num = upper ? (hk - ck) : (ck - lk);
                 const float e_num = 4.f * S32 * (fabsf(hk) + fabsf(lk) + fabsf(xa[k]) + fabsf(rho[k])) + erho + TINY;
@@ -1557,7 +1557,7 @@ __global__ void __launch_bounds__(FB_WPB * 32, 4) k_fallback_warp(DevMesh M, con
                             r2 = fmaf(w2, w2, r2);
                             cH[k] = xa[k] + (xal[k] + off);
                         }
-                        const float rr = sqrtf(r2) * 1.0001f + 1e-6f * (float)M.xscale + 1e-4f * fabsf(tp);
+                        const float rr = sqrtf(r2) * 1.0001f + 1e-6f * M.xs32 + 1e-4f * fabsf(tp);
                         rr2 = rr * rr;
                     }
                     int nc = 0;
@@ -1627,7 +1627,7 @@ __global__ void __launch_bounds__(FB_WPB * 32, 4) k_fallback_warp(DevMesh M, con
                         const float ex = ck < l ? l - ck : (ck > h ? ck - h : 0.f);
                         bd2 = fmaf(ex, ex, bd2);
                     }
-                    const float rr = sqrtf(r2) * 1.0001f + 1e-6f * (float)M.xscale + 1e-4f * fabsf(tp);
+                    const float rr = sqrtf(r2) * 1.0001f + 1e-6f * M.xs32 + 1e-4f * fabsf(tp);
                     keep = !(bd2 > rr * rr);
                 }
                 const bool isleaf = node >= M.P;
@@ -1908,12 +1908,12 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_descent_warp(DevMesh M, int str
                 rmax = fmaxf(rmax, fabsf(rho[k]));
             }
             const float relu = 4.f * S32;
-            const float erho = 2.f * S32 * rmax + (float)(1e-13 * M.xscale);
+            const float erho = 2.f * S32 * rmax + M.e13_32;
             float lo1 = INFINITY, hi1 = INFINITY, lo2 = INFINITY, H = INFINITY;
             int j1 = -1;
             // planes (lane 0)
             if (lane == 0) {
-                const float TINY = (float)(4e-14 * M.xscale);
+                const float TINY = M.tiny32;
 #pragma unroll
                 for (int p = 0; p < 2 * D; ++p) {
                     const int it = M.n + p;
@@ -1924,7 +1924,7 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_descent_warp(DevMesh M, int str
                     const int k = p >> 1;
                     const bool upper = (p & 1) == 0;
                     const float uk = upper ? u[k] : -u[k];
-                    const float hk = (float)M.hi[k], lk = (float)M.lo[k];
+                    const float hk = M.hi32[k], lk = M.lo32[k];
                     const float ck = xa[k] + (xal[k] + rho[k]);
                     const float num = upper ? (hk - ck) : (ck - lk);
                     const float e_num = 4.f * S32 * (fabsf(hk) + fabsf(lk) + fabsf(xa[k]) + fabsf(rho[k])) + erho + TINY;
@@ -1966,7 +1966,7 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_descent_warp(DevMesh M, int str
                 float c2 = 0.f;
 #pragma unroll
                 for (int k = 0; k < D; ++k) { const float cc = fmaf(hi1, u[k], rho[k]); c2 = fmaf(cc, cc, c2); }
-                const float ec = erho + hi1 * relu + 4.f * S32 * (rmax + hi1) + (float)(1e-12 * M.xscale);
+                const float ec = erho + hi1 * relu + 4.f * S32 * (rmax + hi1) + M.e12_32;
                 good = 2.f * sqrtf(c2) + 4.f * sqrtf((float)D) * ec < seci * (1.f - 1e-5f);
             }
             if (!good) { ok = false; break; }
