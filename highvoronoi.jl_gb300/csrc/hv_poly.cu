@@ -60,6 +60,7 @@ struct PolyIn {
 
 struct FCaps {
     int capV, capI, capB, capF;  // vertices (pow2), items, sort buffer (pow2), faces of all levels
+    int capT;                    // edge-term slots (groups of more than one warp; 0 for one warp)
 };
 
 template <int D>
@@ -74,6 +75,7 @@ __host__ __device__ inline size_t farea_bytes(const FCaps& c) {
     constexpr int DM = D > 1 ? D - 1 : 1;
     size_t b = 0;
     b += 8 * (size_t)c.capF;          // fvol
+    b += 8 * (size_t)c.capT;          // dterm
     b += 8 * 16;                      // dred + ll
     b += sizeof(K) * (size_t)c.capB;  // buf
     b += sizeof(K) * 2 * (size_t)c.capF;  // fcode, faux
@@ -88,12 +90,13 @@ __host__ __device__ inline size_t farea_bytes(const FCaps& c) {
 
 template <int D, class K>
 struct FArea {
-    double* fvol; double* dred; long long* ll; K* buf; K* fcode; K* faux;
+    double* fvol; double* dterm; double* dred; long long* ll; K* buf; K* fcode; K* faux;
     unsigned* fv; unsigned* vit; unsigned* its; unsigned* seg; int* wsum; unsigned char* fneed;
     __device__ FArea(unsigned char* base, const FCaps& c) {
         constexpr int DM = D > 1 ? D - 1 : 1;
         fvol = (double*)base;
-        dred = fvol + c.capF;
+        dterm = fvol + c.capF;
+        dred = dterm + c.capT;
         ll = (long long*)(dred + 8);
         buf = (K*)(ll + 8);
         fcode = buf + c.capB;
@@ -229,17 +232,23 @@ __device__ __forceinline__ void vload(const PolyIn& P, unsigned v, double* x) {
     for (int q = 0; q < D; ++q) x[q] = P.oc[(size_t)v * D + q];
 }
 
-// Distance from p to the line through a and b.
+// |(p - a) ^ (b - a)| = dist(p, line ab) * |b - a| (twice the triangle's area),
+// by Lagrange's identity as the root of the sum of the squared 2x2 minors; each
+// minor is formed with one rounding (FMA), so there is no cancellation beyond it.
 template <int D>
-__device__ __forceinline__ double line_dist(const double* p, const double* a, const double* b) {
-    double w[D], u[D], wu = 0, uu = 0;
+__device__ __forceinline__ double tri_area2(const double* p, const double* a, const double* b) {
+    double w[D], u[D];
 #pragma unroll
-    for (int q = 0; q < D; ++q) { w[q] = p[q] - a[q]; u[q] = b[q] - a[q]; wu = fma(w[q], u[q], wu); uu = fma(u[q], u[q], uu); }
-    const double s = wu / uu;
-    double r2 = 0;
+    for (int q = 0; q < D; ++q) { w[q] = p[q] - a[q]; u[q] = b[q] - a[q]; }
+    double s2 = 0;
 #pragma unroll
-    for (int q = 0; q < D; ++q) { const double r = fma(-s, u[q], w[q]); r2 = fma(r, r, r2); }
-    return sqrt(r2);
+    for (int x = 0; x < D; ++x)
+#pragma unroll
+        for (int y = x + 1; y < D; ++y) {
+            const double m = fma(w[x], u[y], -(w[y] * u[x]));
+            s2 = fma(m, m, s2);
+        }
+    return sqrt(s2);
 }
 
 // Orthonormal basis (modified Gram-Schmidt) of the normals of a face's
@@ -259,7 +268,7 @@ __device__ __forceinline__ int mgs_add(double (&Q)[D][D], int m, const double* n
     double nn = 0;
 #pragma unroll
     for (int q = 0; q < D; ++q) nn = fma(r[q], r[q], nn);
-    const double inv = 1.0 / sqrt(nn);
+    const double inv = rsqrt(nn);
 #pragma unroll
     for (int q = 0; q < D; ++q) Q[m][q] = r[q] * inv;
     return m + 1;
@@ -283,7 +292,7 @@ __device__ __forceinline__ double plane_dist(const double (&Q)[D][D], int m, con
     double nn = 0;
 #pragma unroll
     for (int q = 0; q < D; ++q) nn = fma(r[q], r[q], nn);
-    return fabs(num) / sqrt(nn);
+    return fabs(num) * rsqrt(nn);
 }
 
 enum { F_OK = 0, F_CAP = 1, F_BAD = 2 };
@@ -432,13 +441,7 @@ __device__ int poly_facet(const PolyIn& P, int i, int k, long long t, const FAre
                 if (x1 - x0 != 2) { bad = 1; continue; }
                 const K b = W.buf[x0 + 1] & (K)MASK;
                 W.faux[off[j] + s] = a | (b << B);
-                double va[D], vb[D];
-                vload<D>(P, W.fv[(int)a], va);
-                vload<D>(P, W.fv[(int)b], vb);
-                double d2 = 0;
-#pragma unroll
-                for (int q = 0; q < D; ++q) d2 = fma(va[q] - vb[q], va[q] - vb[q], d2);
-                W.fvol[off[j] + s] = sqrt(d2);
+                W.fvol[off[j] + s] = 0.0;  // edge terms use |(p - a) ^ (b - a)| directly
             } else {
                 W.faux[off[j] + s] = a;
                 W.fvol[off[j] + s] = 0.0;
@@ -536,6 +539,61 @@ __device__ int poly_facet(const PolyIn& P, int i, int k, long long t, const FAre
         const int m = g_compact(g, np, [&](int x) { return bb[x] != SENT && (x == 0 || (bb[x] >> B) != (bb[x - 1] >> B)); },
                                 [&](int x, int pos) { if (pos < room) seg[pos] = (unsigned)x; }, W.wsum);
         if (m > room) return F_CAP;
+        if (j + 1 == D - 2) {
+            // edge children: one term per lane over the whole sorted pair list (the
+            // terms of a parent vary 1..6 in number), then each parent's sum in order
+            const int nvalid = g_compact(g, np, [&](int x) { return bb[x] != SENT; }, [&](int, int) {}, W.wsum);
+            auto edge_term = [&](int x, int& pidx) -> double {
+                pidx = (int)(W.buf[x] >> B);
+                const int ch = (int)(W.buf[x] & (K)MASK);
+                double p[D], va[D], vb[D];
+                vload<D>(P, W.fv[(int)W.faux[off[j] + pidx]], p);
+                const K ab = W.faux[off[j + 1] + ch];
+                vload<D>(P, W.fv[(int)(ab & (K)MASK)], va);
+                vload<D>(P, W.fv[(int)(ab >> B)], vb);
+                return tri_area2<D>(p, va, vb);
+            };
+            if (NW == 1) {
+                // one warp: segmented scan of each 32-pair chunk, the last lane of a
+                // parent's run adds the chunk's partial (chunks in order)
+                const int lane = g.rank;
+                for (int f = lane; f < nf[j]; f += 32) W.fvol[off[j] + f] = 0.0;
+                __syncwarp();
+                for (int base = 0; base < nvalid; base += 32) {
+                    const int x = base + lane;
+                    int key = -1 - lane;
+                    double v = 0.0;
+                    if (x < nvalid) v = edge_term(x, key);
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const double vu = __shfl_up_sync(0xFFFFFFFFu, v, o);
+                        const int ku = __shfl_up_sync(0xFFFFFFFFu, key, o);
+                        if (lane >= o && ku == key) v += vu;
+                    }
+                    const int kn = __shfl_down_sync(0xFFFFFFFFu, key, 1);
+                    if (x < nvalid && (lane == 31 || kn != key)) W.fvol[off[j] + key] += v;
+                    __syncwarp();
+                }
+                for (int f = lane; f < nf[j]; f += 32) W.fvol[off[j] + f] /= (double)(D - 1 - j);
+                __syncwarp();
+            } else {
+                if (nvalid > c.capT) return F_CAP;
+                for (int x = g.rank; x < nvalid; x += g.size) {
+                    int pidx;
+                    W.dterm[x] = edge_term(x, pidx);
+                }
+                g.sync();
+                for (int s = g.rank; s < m; s += g.size) {
+                    int x = (int)W.seg[s];
+                    const int pidx = (int)(W.buf[x] >> B);
+                    double sum = 0.0;
+                    for (; x < nvalid && (int)(W.buf[x] >> B) == pidx; ++x) sum += W.dterm[x];
+                    W.fvol[off[j] + pidx] = sum / (double)(D - 1 - j);
+                }
+                g.sync();
+            }
+            continue;
+        }
         for (int s = g.rank; s < m; s += g.size) {
             int x = (int)W.seg[s];
             const int pidx = (int)(W.buf[x] >> B);
@@ -557,13 +615,14 @@ __device__ int poly_facet(const PolyIn& P, int i, int k, long long t, const FAre
             double sum = 0.0;
             for (; x < n2 && W.buf[x] != SENT && (int)(W.buf[x] >> B) == pidx; ++x) {
                 const int ch = (int)(W.buf[x] & (K)MASK);
-                double h;
-                if (j + 1 == D - 2) {
+                double h, cv;
+                if (j + 1 == D - 2) {  // an edge: height times length in one
                     const K ab = W.faux[off[j + 1] + ch];
                     double va[D], vb[D];
                     vload<D>(P, W.fv[(int)(ab & (K)MASK)], va);
                     vload<D>(P, W.fv[(int)(ab >> B)], vb);
-                    h = line_dist<D>(p, va, vb);
+                    h = tri_area2<D>(p, va, vb);
+                    cv = 1.0;
                 } else {
                     unsigned T[DM];
                     items_of(j + 1, ch, T);
@@ -577,8 +636,9 @@ __device__ int poly_facet(const PolyIn& P, int i, int k, long long t, const FAre
                     normal_of<D>(P, (int)W.its[xit], xi, nx);
                     vload<D>(P, W.fv[(int)W.faux[off[j + 1] + ch]], vc);
                     h = plane_dist<D>(Q, qm, nx, vc, p);
+                    cv = W.fvol[off[j + 1] + ch];
                 }
-                sum += h * W.fvol[off[j + 1] + ch];
+                sum += h * cv;
             }
             W.fvol[off[j] + pidx] = sum / (double)(D - 1 - j);
         }
@@ -600,20 +660,18 @@ __device__ int poly_facet(const PolyIn& P, int i, int k, long long t, const FAre
 #pragma unroll
         for (int x = 0; x < DM; ++x) through |= (W.vit[x] == (unsigned)f);
         if (through) continue;
-        double h;
-        if (D == 3) {
+        if (D == 3) {  // edges: height times length in one
             const K ab = W.faux[off[1] + f];
             double va[D], vb[D];
             vload<D>(P, W.fv[(int)(ab & (K)MASK)], va);
             vload<D>(P, W.fv[(int)(ab >> B)], vb);
-            h = line_dist<D>(p, va, vb);
+            part += tri_area2<D>(p, va, vb);
         } else {
             double nx[D], vc[D];
             normal_of<D>(P, (int)W.its[f], xi, nx);
             vload<D>(P, W.fv[(int)W.faux[off[1] + f]], vc);
-            h = plane_dist<D>(Q, qm, nx, vc, p);
+            part += plane_dist<D>(Q, qm, nx, vc, p) * W.fvol[off[1] + f];
         }
-        part += h * W.fvol[off[1] + f];
     }
     area = g_sum(g, part, W.dred) / (double)(D - 1);
     return F_OK;
@@ -800,6 +858,7 @@ static FCaps caps_for(int d, int capV, int widen) {
     while (b < (long long)capV * bmul * widen) b <<= 1;
     c.capB = (int)std::max(64ll, b);
     c.capF = std::max(32, capV * fmul * widen);
+    c.capT = c.capB;
     return c;
 }
 
@@ -810,7 +869,10 @@ struct TierA {
 };
 
 template <int D>
-static size_t bytes_a(const FCaps& c) { return farea_bytes<D, unsigned>(c); }
+static size_t bytes_a(FCaps c) {
+    if (TierA<D>::NW == 1) c.capT = 0;
+    return farea_bytes<D, unsigned>(c);
+}
 template <int D>
 static size_t bytes_b(const FCaps& c) { return farea_bytes<D, unsigned long long>(c); }
 
@@ -831,7 +893,8 @@ static int poly_run(const PolyRun& R) {
                                                                         R.foff, R.fvert);
     } else if (R.pass == 2) {  // tier A
         constexpr int NW = TierA<D>::NW, GPB = TierA<D>::GPB;
-        const FCaps c = caps_for(D, R.capV, 1);
+        FCaps c = caps_for(D, R.capV, 1);
+        if (NW == 1) c.capT = 0;
         const size_t sm = GPB * bytes_a<D>(c);
         if (cudaFuncSetAttribute(k_poly_facets<D, NW, GPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
             cudaSuccess)
