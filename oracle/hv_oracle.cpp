@@ -38,6 +38,15 @@
  *    Directions are i.i.d. Philox4x32-10 Gaussians (the reference's
  *    new_directions! reuses one vector, src/mcintegrator.jl:82-95).
  *
+ * Parity pin: parity unpinned against the reference's own outputs -- the
+ * reference holds no golden vertex sets, neighbour lists or volumes for this
+ * path and its Julia code cannot run here.  The restatement is pinned against
+ * the reference's property tests (sum of cell volumes = domain volume,
+ * test/rcmethods.jl:3-13, test/basics.jl:42-46, test/jld.jl:15-20), analytic
+ * known-answer meshes (one and two generators) and a brute-force
+ * empty-circumsphere check of every vertex (verify_mesh,
+ * src/abstractmesh.jl:221-254).
+ *
  * Exactness: FP64 decisions carry a forward error bound (scaled by a condition
  * estimate of the vertex system); a decision that is not certified is redone
  * in binary128 (__float128 on x86-64, long double on AArch64).  Ties that

@@ -6,8 +6,9 @@ hv_oracle.cpp for the reference file:line of every step) and is the checker
 the CUDA library is compared against; it is never the thing measured for the
 GPU numbers and never a fallback of the product.
 
-Parity pin: HighVoronoi.jl holds no golden vertex sets, neighbour lists or
-volumes.  The oracle is pinned against the reference's own property tests
+Parity pin: parity unpinned against the reference's own outputs --
+HighVoronoi.jl holds no golden vertex sets, neighbour lists or volumes and its
+Julia code cannot run here.  The oracle is pinned against the reference's own property tests
 (sum of volumes = domain volume, test/rcmethods.jl:3-13, test/basics.jl:42-46,
 test/jld.jl:15-20), against analytic known-answer meshes and against a
 brute-force empty-circumsphere check of every vertex (the model of
