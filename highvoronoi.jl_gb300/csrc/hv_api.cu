@@ -9,7 +9,7 @@
 //             (src/sysvoronoi.jl:152-215), here until a level finds nothing new
 //   canonical vertices renumbered in lexicographic signature order
 // All device memory comes from the device's stream-ordered pool; the pool
-// keeps freed blocks cached so repeated builds do not return to the driver.
+// keeps freed blocks cached so repeated builds make no CUDA allocation calls.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>

@@ -85,7 +85,7 @@ typedef struct {
     int64_t levels;         /* wavefront levels */
     int64_t edges_closed;   /* edges skipped because both end points were known */
     int64_t capacity_retries;
-    int64_t launches;       /* kernels launched by this build */
+    int64_t launches;       /* kernels launched by this mesh build */
     double ms_prepare;      /* upload, sort, tree, candidate lists */
     double ms_search;       /* descent + wavefront */
     double ms_total;        /* whole hv_mesh_build (host wall clock) */
