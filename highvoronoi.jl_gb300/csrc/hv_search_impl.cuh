@@ -922,6 +922,13 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 16 / FAST_WPB) k_expand_fast(De
 #pragma unroll
         for (int k = 0; k < R; ++k) sig[k] = M.vsig[(size_t)v * R + k];
         const int vnew = M.vnew[v];
+        // ---- open rays first: a vertex whose edges are all walked or closed costs no more
+        int active = 0;
+        if (lane < R) {
+            active = walkable<D>(M, sig, vnew, lane) ? 1 : 0;
+            if (active && M.ecnt && ((M.ecnt[v] >> lane) & 1u)) active = 0;  // both end points known
+        }
+        if (__ballot_sync(FULL, active) == 0u) continue;
         const int a = sig[0];
         float xa[DP], xal[DP], rho[DP];
         load_pt32<D>(M, a, xa);
@@ -939,11 +946,8 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 16 / FAST_WPB) k_expand_fast(De
         if (lane == 0) sCond[wib] = M.vcond[v];
         __syncwarp();
         // ---- ray directions (lane m < R)
-        int active = 0;
         if (lane < R) {
             const int m = lane;
-            active = walkable<D>(M, sig, vnew, m) ? 1 : 0;
-            if (active && M.ecnt && ((M.ecnt[v] >> m) & 1u)) active = 0;  // both end points known
             if (active) {
                 float u[D], db[D];
 #pragma unroll
