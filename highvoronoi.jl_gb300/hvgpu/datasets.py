@@ -83,6 +83,9 @@ WORKLOADS = {
     "4d_uniform_20k": dict(d=4, n=20000, seed=1, kind="uniform", integrator=None),
     "5d_clustered_50k": dict(d=5, n=50000, seed=2, kind="clustered", integrator="polygon"),
     "6d_uniform_10k_mc": dict(d=6, n=10000, seed=3, kind="uniform", integrator="heuristic_mc", ndir=1000),
+    # larger cases for throughput sweeps
+    "3d_uniform_100k": dict(d=3, n=100000, seed=4, kind="uniform", integrator="polygon"),
+    "5d_uniform_20k": dict(d=5, n=20000, seed=5, kind="uniform", integrator="polygon"),
 }
 
 
