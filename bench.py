@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-integrators", action="store_true")
     ap.add_argument("--knn", type=int, default=0, help="candidate list length (0 = library default)")
     ap.add_argument("--leaf-size", type=int, default=0, help="tree leaf size (0 = library default)")
+    ap.add_argument("--seed-stride", type=int, default=0, help="one descent seed per this many generators (0 = default)")
     ap.add_argument("--mc-dirs", type=int, default=1000, help="directions per cell of VI_HEURISTIC_MC")
     return ap.parse_args()
 
@@ -249,7 +250,7 @@ def run_ours(args):
     n, d = pts.shape
     lo, hi = np.zeros(d), np.ones(d)
     method = hvgpu.HV_METHOD_FAST if args.method == "fast" else hvgpu.HV_METHOD_PLAIN
-    knobs = {k: v for k, v in (("knn", args.knn), ("leaf_size", args.leaf_size)) if v}
+    knobs = {k: v for k, v in (("knn", args.knn), ("leaf_size", args.leaf_size), ("seed_stride", args.seed_stride)) if v}
     params = hvgpu.make_params(method, **knobs)
     if knobs:
         cfg["params"] = knobs
