@@ -900,7 +900,7 @@ __device__ __forceinline__ void load_pt32lo(const DevMesh& M, int j, float (&x)[
 }
 
 template <int D>
-__global__ void __launch_bounds__(FAST_WPB * 32, 16 / FAST_WPB) k_expand_fast(DevMesh M, unsigned f0, unsigned f1,
+__global__ void __launch_bounds__(FAST_WPB * 32, 6) k_expand_fast(DevMesh M, unsigned f0, unsigned f1,
                                                                unsigned long long* fq, unsigned* nfq,
                                                                unsigned fqcap, unsigned long long* fx,
                                                                unsigned* nfx, unsigned fxcap) {
@@ -911,6 +911,8 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 16 / FAST_WPB) k_expand_fast(De
     __shared__ float sLam[FAST_WPB][R];
     __shared__ float sLb[FAST_WPB][R];
     __shared__ float sU1[FAST_WPB][R];
+    __shared__ float sRlo1[FAST_WPB][R], sRhi1[FAST_WPB][R], sRlo2[FAST_WPB][R];
+    __shared__ int sRj1[FAST_WPB][R];
     __shared__ float sCond[FAST_WPB];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned FULL = 0xFFFFFFFFu;
@@ -1002,37 +1004,15 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 16 / FAST_WPB) k_expand_fast(De
 #pragma unroll
         for (int k = 0; k < D; ++k) { R1 += fabsf(rho[k]); rmax = fmaxf(rmax, fabsf(rho[k])); }
         const float erho = 2.f * S32 * rmax;  // rho is the rounded FP64 centre offset
-        // d >= 5: the rays' directions stay in shared memory (broadcast reads in the
-        // candidate loop) instead of (d+1) x (d+3) registers, for occupancy
-        constexpr bool RAYS_SMEM = D >= 5;
-        constexpr int RR = RAYS_SMEM ? 1 : R;
-        float u32[RR][D], lam32[RR], U1[RR], LB[RR];
-        float lo1[R], hi1[R], lo2[R];
-        int j1[R];
-        if (RAYS_SMEM) {
-            if (lane < R && ((rmask >> lane) & 1u)) {
-                float a1 = 0.f;
+        // one pass over the candidate list per open ray: small per-lane state (more
+        // resident warps), the rays' directions read from shared memory
+        if (lane < R && ((rmask >> lane) & 1u)) {
+            float a1 = 0.f;
 #pragma unroll
-                for (int k = 0; k < D; ++k) a1 += fabsf(sU[wib][lane][k]);
-                sU1[wib][lane] = a1;
-            }
-            __syncwarp();
+            for (int k = 0; k < D; ++k) a1 += fabsf(sU[wib][lane][k]);
+            sU1[wib][lane] = a1;
         }
-#pragma unroll
-        for (int m = 0; m < R; ++m) {
-            if (!RAYS_SMEM) {
-                U1[m % RR] = 0.f; lam32[m % RR] = 0.f; LB[m % RR] = 0.f;
-#pragma unroll
-                for (int k = 0; k < D; ++k) u32[m % RR][k] = 0.f;
-                if ((rmask >> m) & 1u) {
-#pragma unroll
-                    for (int k = 0; k < D; ++k) { u32[m % RR][k] = sU[wib][m][k]; U1[m % RR] += fabsf(u32[m % RR][k]); }
-                    lam32[m % RR] = sLam[wib][m];
-                    LB[m % RR] = sLb[wib][m];
-                }
-            }
-            lo1[m] = INFINITY; hi1[m] = INFINITY; lo2[m] = INFINITY; j1[m] = -1;
-        }
+        __syncwarp();
         const float CN = (4.f * D + 20.f) * S32, CD = (4.f * D + 16.f) * S32;
         const float TINY = M.tiny32;
         const int K = M.K;
@@ -1056,50 +1036,49 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 16 / FAST_WPB) k_expand_fast(De
             sec_own = sv;
         }
         const int* lst = M.knn + (size_t)own * K;
-        // software pipeline: list entries two iterations ahead, coordinates one ahead
-        int jn = lane < K ? __ldg(lst + lane) : -1;
-        int jnn = lane + 32 < K ? __ldg(lst + lane + 32) : -1;
-        float xn[DP], xnl[DP];
+        unsigned todo = rmask;
+        while (todo) {
+            const int m = __ffs(todo) - 1;
+            todo &= todo - 1;
+            float um[D];
 #pragma unroll
-        for (int k = 0; k < DP; ++k) { xn[k] = 0.f; xnl[k] = 0.f; }
-        if (jn >= 0) { load_pt32<D>(M, jn, xn); load_pt32lo<D>(M, jn, xnl); }
-        for (int c = lane; c < K; c += 32) {
-            const int j = jn;
-            float xj[DP], xjl[DP];
+            for (int k = 0; k < D; ++k) um[k] = sU[wib][m][k];
+            const float lm = sLam[wib][m], lbm = sLb[wib][m], u1m = sU1[wib][m];
+            float lo1 = INFINITY, hi1 = INFINITY, lo2 = INFINITY;
+            int j1 = -1;
+            // software pipeline: list entries two iterations ahead, coordinates one ahead
+            int jn = lane < K ? __ldg(lst + lane) : -1;
+            int jnn = lane + 32 < K ? __ldg(lst + lane + 32) : -1;
+            float xn[DP], xnl[DP];
 #pragma unroll
-            for (int k = 0; k < DP; ++k) { xj[k] = xn[k]; xjl[k] = xnl[k]; }
-            jn = jnn;
-            jnn = c + 64 < K ? __ldg(lst + c + 64) : -1;
+            for (int k = 0; k < DP; ++k) { xn[k] = 0.f; xnl[k] = 0.f; }
             if (jn >= 0) { load_pt32<D>(M, jn, xn); load_pt32lo<D>(M, jn, xnl); }
-            if (j < 0) continue;
-            bool insig = false;
+            for (int c = lane; c < K; c += 32) {
+                const int j = jn;
+                float xj[DP], xjl[DP];
 #pragma unroll
-            for (int s = 0; s < R; ++s) insig |= (j == sig[s]);
-            if (insig) continue;
-            float dl[D], A1 = 0.f, A2 = 0.f, A3 = 0.f, dr = 0.f;
+                for (int k = 0; k < DP; ++k) { xj[k] = xn[k]; xjl[k] = xnl[k]; }
+                jn = jnn;
+                jnn = c + 64 < K ? __ldg(lst + c + 64) : -1;
+                if (jn >= 0) { load_pt32<D>(M, jn, xn); load_pt32lo<D>(M, jn, xnl); }
+                if (j < 0) continue;
+                bool insig = false;
 #pragma unroll
-            for (int k = 0; k < D; ++k) {
-                dl[k] = (xj[k] - xa[k]) + (xjl[k] - xal[k]);
-                A1 += fabsf(dl[k]);
-                A2 = fmaf(dl[k], dl[k], A2);
-                A3 = fmaf(fabsf(dl[k]), fabsf(rho[k]), A3);
-                dr = fmaf(dl[k], rho[k], dr);
-            }
-            const float num = fmaf(-2.f, dr, A2);
-            const float e_num = CN * (A2 + 2.f * A3) + 2.f * A1 * erho + TINY * (A1 + R1);
-#pragma unroll
-            for (int m = 0; m < R; ++m) {
-                if (!((rmask >> m) & 1u)) continue;
-                float du = 0.f, B = 0.f;
+                for (int q = 0; q < R; ++q) insig |= (j == sig[q]);
+                if (insig) continue;
+                float A1 = 0.f, A2 = 0.f, A3 = 0.f, dr = 0.f, du = 0.f, B = 0.f;
 #pragma unroll
                 for (int k = 0; k < D; ++k) {
-                    const float uk = RAYS_SMEM ? sU[wib][m][k] : u32[m % RR][k];
-                    du = fmaf(dl[k], uk, du);
-                    B = fmaf(fabsf(dl[k]), fabsf(uk), B);
+                    const float dl = (xj[k] - xa[k]) + (xjl[k] - xal[k]);
+                    A1 += fabsf(dl);
+                    A2 = fmaf(dl, dl, A2);
+                    A3 = fmaf(fabsf(dl), fabsf(rho[k]), A3);
+                    dr = fmaf(dl, rho[k], dr);
+                    du = fmaf(dl, um[k], du);
+                    B = fmaf(fabsf(dl), fabsf(um[k]), B);
                 }
-                const float lm = RAYS_SMEM ? sLam[wib][m] : lam32[m % RR];
-                const float lbm = RAYS_SMEM ? sLb[wib][m] : LB[m % RR];
-                const float u1m = RAYS_SMEM ? sU1[wib][m] : U1[m % RR];
+                const float num = fmaf(-2.f, dr, A2);
+                const float e_num = CN * (A2 + 2.f * A3) + 2.f * A1 * erho + TINY * (A1 + R1);
                 const float den = 2.f * (du - lm);
                 const float e_den = CD * (B + fabsf(lm)) + 2.f * relu * (A1 + lbm) + TINY * u1m;
                 float lo, hi;
@@ -1121,25 +1100,23 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 16 / FAST_WPB) k_expand_fast(De
                         lo = -INFINITY; hi = INFINITY;
                     }
                 }
-                if (lo < lo1[m] || (lo == lo1[m] && j < j1[m])) { lo2[m] = lo1[m]; lo1[m] = lo; hi1[m] = hi; j1[m] = j; }
-                else if (lo < lo2[m]) lo2[m] = lo;
+                if (lo < lo1 || (lo == lo1 && j < j1)) { lo2 = lo1; lo1 = lo; hi1 = hi; j1 = j; }
+                else if (lo < lo2) lo2 = lo;
             }
-        }
-        // ---- warp reduction of the per-ray top-2
-#pragma unroll
-        for (int m = 0; m < R; ++m) {
-            if (!((rmask >> m) & 1u)) continue;
+            // warp reduction of the ray's top-2
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
-                const float olo1 = __shfl_xor_sync(FULL, lo1[m], off);
-                const float ohi1 = __shfl_xor_sync(FULL, hi1[m], off);
-                const float olo2 = __shfl_xor_sync(FULL, lo2[m], off);
-                const int oj1 = __shfl_xor_sync(FULL, j1[m], off);
-                const bool take = (olo1 < lo1[m]) || (olo1 == lo1[m] && oj1 >= 0 && (j1[m] < 0 || oj1 < j1[m]));
-                if (take) { lo2[m] = fminf(lo1[m], olo2); lo1[m] = olo1; hi1[m] = ohi1; j1[m] = oj1; }
-                else { lo2[m] = fminf(lo2[m], olo1); }
+                const float olo1 = __shfl_xor_sync(FULL, lo1, off);
+                const float ohi1 = __shfl_xor_sync(FULL, hi1, off);
+                const float olo2 = __shfl_xor_sync(FULL, lo2, off);
+                const int oj1 = __shfl_xor_sync(FULL, j1, off);
+                const bool take = (olo1 < lo1) || (olo1 == lo1 && oj1 >= 0 && (j1 < 0 || oj1 < j1));
+                if (take) { lo2 = fminf(lo1, olo2); lo1 = olo1; hi1 = ohi1; j1 = oj1; }
+                else { lo2 = fminf(lo2, olo1); }
             }
+            if (lane == 0) { sRlo1[wib][m] = lo1; sRhi1[wib][m] = hi1; sRlo2[wib][m] = lo2; sRj1[wib][m] = j1; }
         }
+        __syncwarp();
         // ---- per-ray decision on lane m
         if (lane < R && ((rmask >> lane) & 1u)) {
             const int m = lane;
@@ -1147,11 +1124,8 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 16 / FAST_WPB) k_expand_fast(De
             float u[D];
 #pragma unroll
             for (int k = 0; k < D; ++k) u[k] = sU[wib][m][k];
-            float clo1 = 0.f, chi1 = 0.f, clo2 = 0.f;
-            int cj1 = -1;
-#pragma unroll
-            for (int mm = 0; mm < R; ++mm)
-                if (mm == m) { clo1 = lo1[mm]; chi1 = hi1[mm]; clo2 = lo2[mm]; cj1 = j1[mm]; }
+            const float clo1 = sRlo1[wib][m], chi1 = sRhi1[wib][m], clo2 = sRlo2[wib][m];
+            const int cj1 = sRj1[wib][m];
             // boundary planes in FP32 with the same error model
             float plo1 = INFINITY, phi1 = INFINITY, plo2 = INFINITY;
             int pj1 = -1;
