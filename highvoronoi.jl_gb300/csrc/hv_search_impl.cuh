@@ -1279,6 +1279,8 @@ __device__ __forceinline__ void cand32(const DevMesh& M, int j, const float* xa,
 
 __device__ __forceinline__ void top2_merge(float& lo1, float& hi1, int& j1, float& lo2, float olo1, float ohi1,
                                            int oj1, float olo2) {
+    // the same candidate met by two lanes (list and tree): one entry, not a rival
+    if (oj1 >= 0 && oj1 == j1) { lo2 = fminf(lo2, olo2); return; }
     const bool take = (olo1 < lo1) || (olo1 == lo1 && oj1 >= 0 && (j1 < 0 || oj1 < j1));
     if (take) { lo2 = fminf(lo1, olo2); lo1 = olo1; hi1 = ohi1; j1 = oj1; }
     else { lo2 = fminf(lo2, olo1); }
