@@ -806,6 +806,63 @@ __global__ void __launch_bounds__(256) k_register_edges(DevMesh M, unsigned v0, 
 // ---------------------------------------------------------------------------
 // FP64 circumcentres of new vertices, one thread per vertex (full-warp FP64)
 // ---------------------------------------------------------------------------
+// LU with partial pivoting keeping the reciprocals of the pivots: one FP64
+// division per pivot instead of one per eliminated entry and per solve step
+// (the centres and the inverse below need d + 1 solves per vertex).
+template <int D>
+__device__ __forceinline__ bool lu_factor_rcp(double (&A)[D][D], int (&piv)[D], double (&rd)[D]) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+        int p = c;
+        double best = fabs(A[c][c]);
+#pragma unroll
+        for (int r = c + 1; r < D; ++r) { const double v = fabs(A[r][c]); if (v > best) { best = v; p = r; } }
+        piv[c] = p;
+        if (best == 0.0) return false;
+        if (p != c) {
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+#pragma unroll
+                for (int r = c + 1; r < D; ++r) {
+                    if (r == p) { const double t = A[c][k]; A[c][k] = A[r][k]; A[r][k] = t; }
+                }
+            }
+        }
+        rd[c] = 1.0 / A[c][c];
+#pragma unroll
+        for (int r = c + 1; r < D; ++r) {
+            const double f = A[r][c] * rd[c];
+            A[r][c] = f;
+#pragma unroll
+            for (int k = c + 1; k < D; ++k) A[r][k] = fma(-f, A[c][k], A[r][k]);
+        }
+    }
+    return true;
+}
+
+template <int D>
+__device__ __forceinline__ void lu_solve_rcp(const double (&A)[D][D], const int (&piv)[D], const double (&rd)[D],
+                                             double (&b)[D]) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+#pragma unroll
+        for (int r = c + 1; r < D; ++r) {
+            if (piv[c] == r) { const double t = b[c]; b[c] = b[r]; b[r] = t; }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+#pragma unroll
+        for (int k = 0; k < r; ++k) b[r] = fma(-A[r][k], b[k], b[r]);
+    }
+#pragma unroll
+    for (int r = D - 1; r >= 0; --r) {
+#pragma unroll
+        for (int k = r + 1; k < D; ++k) b[r] = fma(-A[r][k], b[k], b[r]);
+        b[r] *= rd[r];
+    }
+}
+
 template <int D>
 __global__ void __launch_bounds__(128) k_centers(DevMesh M, unsigned v0, unsigned v1) {
     constexpr int DP = (D <= 4) ? 4 : 8;
@@ -828,13 +885,14 @@ __global__ void __launch_bounds__(128) k_centers(DevMesh M, unsigned v0, unsigne
             nrm = fmax(nrm, sr);
         }
         int piv[D];
-        const bool ok = lu_factor<D, double>(A, piv);
+        double rd[D];
+        const bool ok = lu_factor_rcp<D>(A, piv, rd);
         if (!ok) {
             set_status(M, ST_NUMERIC);
 #pragma unroll
             for (int k = 0; k < D; ++k) rho[k] = 0.0;
         } else {
-            lu_solve<D, double>(A, piv, rho);
+            lu_solve_rcp<D>(A, piv, rd, rho);
         }
         float r32[DP];
 #pragma unroll
@@ -857,7 +915,7 @@ __global__ void __launch_bounds__(128) k_centers(DevMesh M, unsigned v0, unsigne
                 double col[D];
 #pragma unroll
                 for (int k = 0; k < D; ++k) col[k] = (k == c) ? 1.0 : 0.0;
-                if (ok) lu_solve<D, double>(A, piv, col);
+                if (ok) lu_solve_rcp<D>(A, piv, rd, col);
 #pragma unroll
                 for (int k = 0; k < D; ++k) {
                     M.vinv32[(size_t)v * D * D + k * D + c] = (float)col[k];
