@@ -65,6 +65,9 @@ RCGPUPlain = RaycastMethod("RCGPUPlain", _lib.HV_METHOD_PLAIN)
 
 VI_GEOMETRY = "VI_GEOMETRY"
 VI_POLYGON = "VI_POLYGON"
+# The reference's memoised exact integrator (src/fastpolyintegrator.jl:4-476): the same cell
+# volumes and interface areas as VI_POLYGON, which the GPU computes the same way for both.
+VI_FAST_POLYGON = "VI_FAST_POLYGON"
 VI_HEURISTIC_MC = "VI_HEURISTIC_MC"
 
 
@@ -111,7 +114,7 @@ class VoronoiGeometry:
         self.integrator = integrator
         self._volumes = None
         self._areas = None
-        if integrator == VI_POLYGON:
+        if integrator in (VI_POLYGON, VI_FAST_POLYGON):
             self._volumes, self._areas = self.mesh.polygon()
         elif integrator == VI_HEURISTIC_MC:
             self._volumes, self._areas = self.mesh.heuristic_mc(int(mc_accurate[0]), int(mc_seed))

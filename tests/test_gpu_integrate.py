@@ -97,3 +97,18 @@ def test_polygon_tiers_agree(gpu_lib, d, n, seed, monkeypatch):
     assert st["poly_big_facets"] > 0 and st["ms_poly_big"] > 0
     np.testing.assert_allclose(v1, v0, rtol=1e-13, atol=0)
     np.testing.assert_allclose(a1, a0, rtol=1e-12, atol=1e-15 * max(1.0, a0.max()))
+
+
+def test_fast_polygon_integrator_is_the_polygon_integrator(gpu_lib):
+    """VI_FAST_POLYGON (the reference's memoised exact integrator) gives the exact
+    volumes and areas of VI_POLYGON."""
+    hv = gpu_lib
+    pts = D.uniform_points(4, 400, 41)
+    a = hv.VoronoiData(hv.VoronoiGeometry(pts, hv.cuboid(4, periodic=[]), integrator=hv.VI_POLYGON))
+    b = hv.VoronoiData(hv.VoronoiGeometry(pts, hv.cuboid(4, periodic=[]), integrator=hv.VI_FAST_POLYGON))
+    np.testing.assert_array_equal(a.volume, b.volume)
+    for x, y in zip(a.area, b.area):
+        np.testing.assert_array_equal(x, y)
+    ref = O.OracleMesh(pts, integrate=True)
+    rv, _ = ref.polygon()
+    np.testing.assert_allclose(b.volume, rv, rtol=POLY_RTOL, atol=1e-15)
