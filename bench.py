@@ -380,6 +380,13 @@ def run_ours(args):
                         "achieved_tflops": ach, "peak_tflops_nominal": fp32_peak, "frac": ach / fp32_peak}
     except Exception as ex:  # noqa: BLE001
         roof["fp32"] = {"error": str(ex)}
+    # FP64 view of the circumcentre solves: (2/3)d^3 + 4d^2 flops per vertex against the nominal
+    # GB300 FP64 rate (1.25 TFLOP/s; no measured FP64 peak exists for this machine)
+    cen_ms = statistics.mean(s["ms_centers"] for s in stats)
+    f64 = Vs * ((2.0 / 3.0) * d ** 3 + 4 * d * d)
+    roof["fp64"] = {"kernel": "k_centers", "algorithmic_flops_per_vertex": (2.0 / 3.0) * d ** 3 + 4 * d * d,
+                    "achieved_tflops": f64 / (cen_ms / 1e3) / 1e12, "peak_tflops_nominal": 1.25,
+                    "frac": f64 / (cen_ms / 1e3) / 1e12 / 1.25}
     # ---- CPU baseline on the host cores
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
@@ -410,6 +417,7 @@ def run_ours(args):
                                           "degenerate", "descents", "levels", "fallback_tree_rays",
                                           "fallback_nodes", "fallback_leaves", "fallback_points",
                                           "ambiguous_sets")},
+            "rays_per_s": st0["rays"] / (tot_ms / 1e3 / args.steps),
             "breakdown_ms": breakdown, "serving": serving}
     print(json.dumps(line), flush=True)
 
