@@ -42,7 +42,10 @@ struct hv_mesh {
     hv_ctx* ctx = nullptr;
     int d = 0;
     int n = 0;
-    double lo[HV_MAXD], hi[HV_MAXD];
+    double lo[HV_MAXD], hi[HV_MAXD];  // bounding box of the domain
+    int np = 0;                       // boundary planes, generator ids n .. n+np-1
+    hv::DevPlane planes[hv::HV_MAXP];
+    hv::DevPlane* d_planes = nullptr;
     hv_params prm;
     double* d_in = nullptr;  // points in original order (n x d)
     unsigned V = 0;
@@ -182,7 +185,7 @@ void read_stat(hv_ctx* ctx, const unsigned* dstat) {
 
 void check_fatal(unsigned status) {
     using namespace hv;
-    if (status & ST_BADINPUT) throw HvError(HV_E_INVALID_ARG, "points must lie strictly inside the box and be finite");
+    if (status & ST_BADINPUT) throw HvError(HV_E_INVALID_ARG, "points must lie strictly inside the domain and be finite");
     if (status & ST_TIMEOUT) throw HvError(HV_E_TIMEOUT, "a bounded device wait gave up");
     if (status & (ST_NUMERIC | ST_STACK | ST_AMB | ST_DESCENT))
         throw HvError(HV_E_INTERNAL, "device search failed (status " + std::to_string(status) + ")");
@@ -197,6 +200,8 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     auto t0 = std::chrono::steady_clock::now();
     CK(cudaEventRecord(ev.e[0], st));
     mesh->d_in = dalloc<double>(st, (size_t)n * d);
+    mesh->d_planes = dalloc<DevPlane>(st, (size_t)mesh->np);
+    CK(cudaMemcpyAsync(mesh->d_planes, mesh->planes, sizeof(DevPlane) * mesh->np, cudaMemcpyHostToDevice, st));
     if (n > 0) {
         if (src_on_device)
             CK(cudaMemcpyAsync(mesh->d_in, d_src, sizeof(double) * n * d, cudaMemcpyDeviceToDevice, st));
@@ -221,7 +226,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     int* idx = prep.get<int>(n);
     int* perm = prep.get<int>(n);
     KTimer kt(ctx);
-    kt.run(F_OTHER, 1, [&] { launch_morton(d, mesh->d_in, n, mesh->lo, mesh->hi, codes, idx, dstat + 1, st); });
+    kt.run(F_OTHER, 1, [&] { launch_morton(d, mesh->d_in, n, mesh->lo, mesh->hi, mesh->d_planes, mesh->np, codes, idx, dstat + 1, st); });
     {
         size_t tb = sort_pairs_u64_i32_temp(n);
         void* tmp = prep.get<char>(tb);
@@ -241,7 +246,8 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         xs = std::max(xs, std::max(std::fabs(mesh->lo[k]), std::fabs(mesh->hi[k])));
     }
     M.xscale = xs;
-    for (int k = 0; k < d; ++k) { M.lo32[k] = (float)M.lo[k]; M.hi32[k] = (float)M.hi[k]; }
+    M.np = mesh->np;
+    M.planes = mesh->d_planes;
     M.xs32 = (float)xs;
     M.tiny32 = (float)(4e-14 * xs);
     M.e13_32 = (float)(1e-13 * xs);
@@ -387,7 +393,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         launch_canon_keys(M, V, keys, st);
         if (V) k_iota<<<std::min<unsigned>((V + 255) / 256, 65535u), 256, 0, st>>>(order, V);
         int end_bit = 1;
-        while ((1ull << end_bit) < (unsigned long long)(n + 2 * d + 1)) ++end_bit;
+        while ((1ull << end_bit) < (unsigned long long)(n + mesh->np + 1)) ++end_bit;
         size_t tb = sort_pairs_u32_i32_temp((int)std::max(V, 1u));
         void* tmp = cs.get<char>(tb);
         for (int pos = d; pos >= 0; --pos) {
@@ -504,11 +510,12 @@ int fail(hv_ctx* ctx, const HvError& e) {
     return e.code;
 }
 
-int validate_common(hv_ctx* ctx, int d, int64_t n, const double* lo, const double* hi, hv_mesh** out) {
-    if (!ctx || !out || !lo || !hi) return HV_E_INVALID_ARG;
+int validate_common(hv_ctx* ctx, int d, int64_t n, const double* lo, const double* hi, hv_mesh** out,
+                    bool box = true) {
+    if (!ctx || !out || (box && (!lo || !hi))) return HV_E_INVALID_ARG;
     if (d < 2 || d > HV_MAXD) { ctx->err = "dimension must be between 2 and 6"; return HV_E_INVALID_ARG; }
     if (n < 0 || n > (1ll << 30)) { ctx->err = "point count out of range"; return HV_E_INVALID_ARG; }
-    for (int k = 0; k < d; ++k)
+    for (int k = 0; box && k < d; ++k)
         if (!(lo[k] < hi[k]) || !std::isfinite(lo[k]) || !std::isfinite(hi[k])) {
             ctx->err = "box bounds must be finite with lo < hi";
             return HV_E_INVALID_ARG;
@@ -516,14 +523,50 @@ int validate_common(hv_ctx* ctx, int d, int64_t n, const double* lo, const doubl
     return HV_OK;
 }
 
-int build_entry(hv_ctx* ctx, int d, int64_t n, const double* src, bool on_device, const double* lo,
-                const double* hi, const hv_params* params, hv_mesh** out) {
-    int rc = validate_common(ctx, d, n, lo, hi, out);
+// The domain: a box [lo, hi] (cuboid planes), or np planes given by base
+// points and normals (P x d each) with optional boundary conditions.
+struct DomainSpec {
+    const double* lo = nullptr;
+    const double* hi = nullptr;
+    int np = 0;
+    const double* base = nullptr;
+    const double* normal = nullptr;
+    const int16_t* bc = nullptr;
+};
+
+int build_entry(hv_ctx* ctx, int d, int64_t n, const double* src, bool on_device, const DomainSpec& dom,
+                const hv_params* params, hv_mesh** out) {
+    if (!ctx || !out) return HV_E_INVALID_ARG;
+    int rc = HV_OK;
+    if (dom.lo || dom.hi) {
+        rc = validate_common(ctx, d, n, dom.lo, dom.hi, out);
+    } else {
+        rc = validate_common(ctx, d, n, nullptr, nullptr, out, false);
+        if (rc == HV_OK && (!dom.base || !dom.normal)) { ctx->err = "null plane array"; rc = HV_E_INVALID_ARG; }
+        if (rc == HV_OK && dom.bc)
+            for (int p = 0; p < dom.np; ++p)
+                if (dom.bc[p] > 0) {
+                    ctx->err = "periodic boundary planes are not supported";
+                    rc = HV_E_INVALID_ARG;
+                    break;
+                }
+    }
     if (rc != HV_OK) return rc;
     if (n > 0 && !src) { ctx->err = "null point array"; return HV_E_INVALID_ARG; }
-    hv_mesh* m = new hv_mesh();
+    std::unique_ptr<hv_mesh> mp(new hv_mesh());
+    hv_mesh* m = mp.get();
     m->ctx = ctx; m->d = d; m->n = (int)n;
-    for (int k = 0; k < d; ++k) { m->lo[k] = lo[k]; m->hi[k] = hi[k]; }
+    if (dom.lo) {
+        for (int k = 0; k < d; ++k) { m->lo[k] = dom.lo[k]; m->hi[k] = dom.hi[k]; }
+        m->np = 2 * d;
+        hv::box_planes(d, dom.lo, dom.hi, m->planes);
+    } else {
+        std::string e = hv::make_planes(d, dom.np, dom.base, dom.normal, m->planes);
+        if (e.empty()) e = hv::planes_bbox(d, dom.np, m->planes, m->lo, m->hi);
+        if (!e.empty()) { ctx->err = e; return HV_E_INVALID_ARG; }
+        m->np = dom.np;
+    }
+    mp.release();
     if (params) m->prm = *params; else hv_params_default(&m->prm);
     {
         int nb = 0;
@@ -609,12 +652,33 @@ void* hv_ctx_stream(hv_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
 int hv_mesh_build(hv_ctx* ctx, int d, int64_t n, const double* pts, const double* lo, const double* hi,
                   const hv_params* params, hv_mesh** out) {
-    return build_entry(ctx, d, n, pts, false, lo, hi, params, out);
+    DomainSpec dom;
+    dom.lo = lo; dom.hi = hi;
+    if (!lo || !hi) return HV_E_INVALID_ARG;
+    return build_entry(ctx, d, n, pts, false, dom, params, out);
 }
 
 int hv_mesh_build_device(hv_ctx* ctx, int d, int64_t n, const double* d_pts, const double* lo, const double* hi,
                          const hv_params* params, hv_mesh** out) {
-    return build_entry(ctx, d, n, d_pts, true, lo, hi, params, out);
+    DomainSpec dom;
+    dom.lo = lo; dom.hi = hi;
+    if (!lo || !hi) return HV_E_INVALID_ARG;
+    return build_entry(ctx, d, n, d_pts, true, dom, params, out);
+}
+
+int hv_mesh_build_planes(hv_ctx* ctx, int d, int64_t n, const double* pts, int nplanes, const double* base,
+                         const double* normal, const int16_t* bc, const hv_params* params, hv_mesh** out) {
+    DomainSpec dom;
+    dom.np = nplanes; dom.base = base; dom.normal = normal; dom.bc = bc;
+    return build_entry(ctx, d, n, pts, false, dom, params, out);
+}
+
+int hv_mesh_build_planes_device(hv_ctx* ctx, int d, int64_t n, const double* d_pts, int nplanes,
+                                const double* base, const double* normal, const int16_t* bc,
+                                const hv_params* params, hv_mesh** out) {
+    DomainSpec dom;
+    dom.np = nplanes; dom.base = base; dom.normal = normal; dom.bc = bc;
+    return build_entry(ctx, d, n, d_pts, true, dom, params, out);
 }
 
 int hv_autotune(hv_ctx* ctx, int d, int64_t n, const double* pts, const double* lo, const double* hi,
@@ -739,7 +803,7 @@ int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) {
         KTimer kt(ctx);
         Scratch s(st);
         hv::PolyRun R{};
-        R.d = d; R.n = n; R.V = m->V; R.lo = m->lo; R.hi = m->hi;
+        R.d = d; R.n = n; R.V = m->V; R.planes = m->d_planes;
         R.pts = m->d_in; R.osig = m->osig; R.oc = m->oc; R.nbr_off = m->nbr_off; R.nbr = m->nbr;
         R.nslots = ns; R.nsm = ctx->nsm; R.stream = st;
         R.cnt = s.get<unsigned long long>((size_t)ns + 1);
@@ -875,7 +939,7 @@ int hv_integrate_heuristic_mc(hv_mesh* m, int ndir, uint64_t seed, double* vol, 
         double* outA = s.get<double>(E);
         unsigned* dstat = s.get<unsigned>(1);
         CK(cudaMemsetAsync(dstat, 0, sizeof(unsigned), st));
-        hv::IntegrateInput in{d, n, m->lo, m->hi, m->d_in, m->osig, m->oc, m->inc_off, m->inc, m->nbr_off, m->nbr, dstat};
+        hv::IntegrateInput in{d, n, m->lo, m->hi, m->np, m->d_planes, m->d_in, m->osig, m->oc, m->inc_off, m->inc, m->nbr_off, m->nbr, dstat};
         const double cvol = std::pow(M_PI, d / 2.0) / std::tgamma(1.0 + d / 2.0);
         if (hv::launch_heuristic_mc(in, ndir, seed, capN, cvol, rawV, rawA, varV, outA, dvol, m->ctx->nsm, st) != 0)
             throw HvError(HV_E_CUDA, "MC integrator launch failed");
@@ -903,6 +967,7 @@ int hv_mesh_free(hv_mesh* m) {
     cudaStream_t st = m->ctx->stream;
     cudaSetDevice(m->ctx->device);
     dfree(st, m->d_in);
+    dfree(st, m->d_planes);
     dfree(st, m->osig);
     dfree(st, m->oc);
     dfree(st, m->inc_off);

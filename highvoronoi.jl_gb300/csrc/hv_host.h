@@ -3,8 +3,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 namespace hv {
 struct DevMesh;
+struct DevPlane;
 
 // Rays whose FP32 decision left a small ambiguous candidate set: the queue
 // entry (vertex << 4 | flags | slot), the set size and up to AMB_SET ids each.
@@ -19,8 +22,15 @@ struct AmbQueue {
 
 
 // hv_prep.cu
-void launch_morton(int d, const double* in, int n, const double* lo, const double* hi,
-                   unsigned long long* codes, int* idx, unsigned* status, cudaStream_t st);
+// hv_domain.cu: boundary planes (cuboid faces 2k upper, 2k+1 lower; or from
+// base points and normals, normals scaled to unit length) and the domain's
+// bounding box; the strings are empty on success, else the error text.
+void box_planes(int d, const double* lo, const double* hi, DevPlane* out);
+std::string make_planes(int d, int np, const double* base, const double* normal, DevPlane* out);
+std::string planes_bbox(int d, int np, const DevPlane* P, double* lo, double* hi);
+
+void launch_morton(int d, const double* in, int n, const double* lo, const double* hi, const DevPlane* planes,
+                   int np, unsigned long long* codes, int* idx, unsigned* status, cudaStream_t st);
 void launch_gather(int d, const double* in, const int* perm, int n, double* pts, float* pts32, float* pts32lo,
                    cudaStream_t st);
 void launch_bvh(const DevMesh& M, float* blo, float* bhi, unsigned* flags, cudaStream_t st);

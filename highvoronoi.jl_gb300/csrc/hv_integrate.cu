@@ -15,7 +15,7 @@ namespace hv {
 
 struct PolyArgs {
     int d, n;
-    double lo[HV_MAXD], hi[HV_MAXD];
+    const DevPlane* planes;  // boundary planes, generator ids n + p
     const double* pts;       // original order, n x d
     const int* osig;         // V x (d+1), original 0-based items
     const double* oc;        // V x d
@@ -28,14 +28,9 @@ struct PolyArgs {
     int capC, capV, capF, capE, capI;
 };
 
-__device__ __forceinline__ double plane_height(const PolyArgs& A, const double* xi, int k) {
-    const int p = k - A.n, q = p >> 1;
-    return (p & 1) == 0 ? A.hi[q] - xi[q] : xi[q] - A.lo[q];
-}
-
 template <int D>
 __device__ __forceinline__ double facet_height(const PolyArgs& A, const double* xi, int k) {
-    if (k >= A.n) return plane_height(A, xi, k);
+    if (k >= A.n) return plane_height<D>(A.planes[k - A.n], xi);
     double s = 0;
 #pragma unroll
     for (int c = 0; c < D; ++c) { const double e = A.pts[(size_t)k * D + c] - xi[c]; s = fma(e, e, s); }
@@ -122,12 +117,12 @@ __global__ void __launch_bounds__(MC_WPB * 32) k_mc_cells(PolyArgs A, int ndir, 
                 e[D] = s;
                 e[D + 1] = rsqrtf(s);  // 1/|delta| for the normal
             } else {
-                const int p = k - A.n, q = p >> 1;
+                const DevPlane& B = A.planes[k - A.n];
+                double xd[D];
 #pragma unroll
-                for (int c = 0; c < D; ++c) e[c] = 0.f;
-                e[D] = (float)(-1 - p);  // plane marker
-                e[D + 1] = (float)((p & 1) == 0 ? A.hi[q] - A.pts[(size_t)i * D + q]
-                                                 : A.pts[(size_t)i * D + q] - A.lo[q]);
+                for (int c = 0; c < D; ++c) { e[c] = B.n32[c]; xd[c] = A.pts[(size_t)i * D + c]; }
+                e[D] = -1.f;  // plane marker
+                e[D + 1] = (float)plane_height<D>(B, xd);
             }
             for (int l = 0; l < 32; ++l) slab[l * capN + t] = 0.0;
         }
@@ -149,11 +144,9 @@ __global__ void __launch_bounds__(MC_WPB * 32) k_mc_cells(PolyArgs A, int ndir, 
                     tt = e[D] / (2.f * du);
                     cs = du * e[D + 1];
                 } else {
-                    const int p = -1 - (int)e[D], q = p >> 1;
-                    float uk = 0.f;
+                    float uk = 0.f;  // n.u, exactly +-u[axis] for axis planes
 #pragma unroll
-                    for (int c = 0; c < D; ++c) if (c == q) uk = u[c];
-                    if ((p & 1) != 0) uk = -uk;
+                    for (int c = 0; c < D; ++c) uk = fmaf(e[c], u[c], uk);
                     if (!(uk > 0.f)) continue;
                     tt = e[D + 1] / uk;
                     cs = uk;
@@ -243,7 +236,7 @@ __global__ void k_mc_volumes(PolyArgs A, const double* rawV, const double* rawA,
 static PolyArgs make_args(const IntegrateInput& in) {
     PolyArgs A;
     A.d = in.d; A.n = in.n;
-    for (int k = 0; k < in.d; ++k) { A.lo[k] = in.lo[k]; A.hi[k] = in.hi[k]; }
+    A.planes = in.planes;
     A.pts = in.pts; A.osig = in.osig; A.oc = in.oc;
     A.inc_off = in.inc_off; A.inc = in.inc; A.nbr_off = in.nbr_off; A.nbr = in.nbr;
     A.status = in.status;

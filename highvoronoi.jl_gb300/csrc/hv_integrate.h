@@ -5,10 +5,14 @@
 
 namespace hv {
 
+struct DevPlane;
+
 struct IntegrateInput {
     int d, n;
-    const double* lo;
+    const double* lo;         // host arrays: bounding box of the domain
     const double* hi;
+    int np;                   // boundary planes (device array), generator ids n + p
+    const DevPlane* planes;
     const double* pts;        // original order, n x d
     const int* osig;          // V x (d+1), original 0-based items
     const double* oc;         // V x d
@@ -30,8 +34,7 @@ struct IntegrateInput {
 struct PolyRun {
     int d, n, pass;
     unsigned V;
-    const double* lo;          // host arrays
-    const double* hi;
+    const DevPlane* planes;    // device array of boundary planes
     const double* pts;
     const int* osig;
     const double* oc;

@@ -20,6 +20,7 @@
 //   vnew     vcap ints: generator added by the ray that found the vertex
 //   vhash    open-addressing table of 64-bit entries (fingerprint << 32 | id)
 #pragma once
+#include <type_traits>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -53,6 +54,28 @@ constexpr unsigned long long HASH_BUSY = ~0ull;
 constexpr unsigned INVALID_ID = 0xFFFFFFFFu;
 constexpr int SPIN_LIMIT = 1 << 22;
 
+// A boundary plane {x : n.x = off} with outer unit normal n (the domain is n.x <= off).
+// axis >= 0 marks n = sgn e_axis exactly (cuboid faces): those keep the exact
+// single-coordinate arithmetic.
+constexpr int HV_MAXP = 64;
+struct DevPlane {
+    double n[HV_MAXD];
+    double off;
+    float n32[HV_MAXD];
+    float off32;
+    int axis, sgn;
+};
+
+// Distance off - n.x of x below plane B (exact single subtraction for axis planes).
+template <int D>
+__device__ __forceinline__ double plane_height(const DevPlane& B, const double* x) {
+    if (B.axis >= 0) return B.sgn > 0 ? B.off - x[B.axis] : B.off + x[B.axis];
+    double h = B.off;
+#pragma unroll
+    for (int q = 0; q < D; ++q) h = fma(-B.n[q], x[q], h);
+    return h;
+}
+
 struct DevBox {
     double lo[HV_MAXD], hi[HV_MAXD];
 };
@@ -64,10 +87,11 @@ struct DevMesh {
     unsigned vcap;
     unsigned long long vhmask;
     unsigned long long ehmask;
-    double lo[HV_MAXD], hi[HV_MAXD];
+    double lo[HV_MAXD], hi[HV_MAXD];  // bounding box of the domain
     double xscale;  // bound on |coordinate|
+    int np;                   // boundary planes, generator ids n .. n+np-1
+    const DevPlane* planes;   // np entries
     // FP32 copies for the FP32 kernels (rounded once on the host)
-    float lo32[HV_MAXD], hi32[HV_MAXD];
     float xs32;      // (float)xscale
     float tiny32;    // (float)(4e-14 xscale)
     float e13_32;    // (float)(1e-13 xscale)
@@ -222,9 +246,35 @@ __device__ __forceinline__ void lu_solve(const T (&A)[D][D], const int (&piv)[D]
     }
 }
 
+// off - n . xa in double-double (one rounding for the double result).
+template <int D>
+__device__ __forceinline__ dd plane_rhs_dd(const DevPlane& P, const double* xa) {
+    dd s = mk(P.off);
+#pragma unroll
+    for (int q = 0; q < D; ++q) s = s - mk(P.n[q]) * mk(xa[q]);
+    return s;
+}
+// For axis planes (n = +-e_k) the FMA chain adds exact zeros and rounds
+// off -+ xa_k once, so it equals the double-double result rounded.
+template <int D, class T>
+__device__ __forceinline__ T plane_rhs(const DevPlane& P, const double* xa) {
+    if constexpr (std::is_same<T, dd>::value) {
+        return plane_rhs_dd<D>(P, xa);
+    } else {
+        if (P.axis >= 0) {
+            double h = P.off;
+#pragma unroll
+            for (int q = 0; q < D; ++q) h = fma(-P.n[q], xa[q], h);
+            return h;
+        }
+        const dd s = plane_rhs_dd<D>(P, xa);
+        return s.hi + s.lo;
+    }
+}
+
 // Constraint row of item `it` relative to the real anchor xa:
 //   generator g : (x_g - x_a) . rho = |x_g - x_a|^2 / 2
-//   plane p     : +-e_k . rho = signed offset of the plane from x_a
+//   plane p     : n_p . rho = off_p - n_p . x_a
 template <int D, class T>
 __device__ __forceinline__ void con_row(const DevMesh& M, const double* xa, int it, T (&row)[D], T& rhs) {
     if (it < M.n) {
@@ -234,16 +284,11 @@ __device__ __forceinline__ void con_row(const DevMesh& M, const double* xa, int 
         for (int k = 0; k < D; ++k) { row[k] = diff_d<T>(__ldg(xg + k), xa[k]); s += row[k] * row[k]; }
         rhs = s * from_d<T>(0.5);
     } else {
-        int p = it - M.n, k = p >> 1;
+        // n . rho = off - n . xa: one rounding (exact for T = dd)
+        const DevPlane& P = M.planes[it - M.n];
 #pragma unroll
-        for (int q = 0; q < D; ++q) row[q] = from_d<T>(0.0);
-#pragma unroll
-        for (int q = 0; q < D; ++q) {
-            if (q == k) {
-                if ((p & 1) == 0) { row[q] = from_d<T>(1.0); rhs = diff_d<T>(M.hi[q], xa[q]); }
-                else { row[q] = from_d<T>(-1.0); rhs = diff_d<T>(xa[q], M.lo[q]); }
-            }
-        }
+        for (int q = 0; q < D; ++q) row[q] = from_d<T>(P.n[q]);
+        rhs = plane_rhs<D, T>(P, xa);
     }
 }
 

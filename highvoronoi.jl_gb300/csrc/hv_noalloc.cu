@@ -4,8 +4,8 @@
 // that owns the whole device memory budget, a real-time loop that forbids
 // allocator calls, or code handed fixed buffers by a framework).  The caller
 // passes every input and output in device memory; the integrator's scratch
-// (raw per-cell volumes and variances, raw interface areas, a status word)
-// lives in one file-scope static device array of HV_NOALLOC_SCRATCH_BYTES
+// (raw per-cell volumes and variances, raw interface areas, the cuboid's
+// boundary planes, a status word) lives in one file-scope static device array of HV_NOALLOC_SCRATCH_BYTES
 // (16 MiB), which every GPU that loads this library holds until exit.
 //
 // The array's name is only a host-side stand-in for the symbol, so its device
@@ -19,13 +19,16 @@
 
 #include <cuda_runtime.h>
 
+#include "hv_host.h"
 #include "hv_integrate.h"
+#include "hv_internal.cuh"
 #include "hvgpu.h"
 
 namespace {
 
 constexpr size_t kScratchBytes = HV_NOALLOC_SCRATCH_BYTES;
 constexpr size_t kStatusBytes = 256;
+constexpr size_t kPlaneBytes = 2 * HV_MAXD * sizeof(hv::DevPlane) + 256 - (2 * HV_MAXD * sizeof(hv::DevPlane)) % 256;
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_mc_scratch[kScratchBytes];
@@ -57,8 +60,8 @@ extern "C" int hv_integrate_heuristic_mc_noalloc(int d, int64_t n, const double*
         return HV_E_INVALID_ARG;
     for (int k = 0; k < d; ++k)
         if (!(lo[k] < hi[k])) return HV_E_INVALID_ARG;
-    // scratch: status | raw volume (n) | variance (n) | raw area (nnbr), in doubles
-    const double need = (double)kStatusBytes + 8.0 * (2.0 * (double)n + (double)nnbr);
+    // scratch: status | planes | raw volume (n) | variance (n) | raw area (nnbr), in doubles
+    const double need = (double)(kStatusBytes + kPlaneBytes) + 8.0 * (2.0 * (double)n + (double)nnbr);
     if (need > (double)kScratchBytes) return HV_E_CAPACITY;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return HV_E_CUDA;
@@ -73,11 +76,17 @@ extern "C" int hv_integrate_heuristic_mc_noalloc(int d, int64_t n, const double*
     if ((long long)sm > smax) return HV_E_CAPACITY;
     cudaStream_t st = (cudaStream_t)stream;
     unsigned* status = (unsigned*)base;
-    double* rawV = (double*)(base + kStatusBytes);
+    hv::DevPlane* planes = (hv::DevPlane*)(base + kStatusBytes);
+    double* rawV = (double*)(base + kStatusBytes + kPlaneBytes);
     double* varV = rawV + n;
     double* rawA = varV + n;
     if (cudaMemsetAsync(status, 0, sizeof(unsigned), st) != cudaSuccess) return HV_E_CUDA;
-    hv::IntegrateInput in{d, (int)n, lo, hi, d_pts, nullptr, nullptr, nullptr, nullptr,
+    hv::DevPlane hp[2 * HV_MAXD];
+    hv::box_planes(d, lo, hi, hp);
+    // pageable source: the copy has read hp when the call returns
+    if (cudaMemcpyAsync(planes, hp, sizeof(hv::DevPlane) * 2 * d, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return HV_E_CUDA;
+    hv::IntegrateInput in{d, (int)n, lo, hi, 2 * d, planes, d_pts, nullptr, nullptr, nullptr, nullptr,
                           (const long long*)d_nbr_off, d_nbr, status};
     const double cvol = std::pow(M_PI, d / 2.0) / std::tgamma(1.0 + d / 2.0);  // unit-ball volume
     if (hv::launch_heuristic_mc(in, ndir, seed, capN, cvol, rawV, rawA, varV, d_area, d_vol, nsm, st) != 0)

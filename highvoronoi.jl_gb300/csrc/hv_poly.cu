@@ -45,7 +45,7 @@ template <> struct KeyBits<unsigned long long> { static constexpr int B = 20; };
 
 struct PolyIn {
     int n;
-    double lo[HV_MAXD], hi[HV_MAXD];
+    const DevPlane* planes;   // boundary planes, generator ids n + p
     const double* pts;        // n x d, original order
     const int* osig;          // V x (d+1), sorted 0-based items, planes n+p
     const double* oc;         // V x d
@@ -220,9 +220,9 @@ __device__ __forceinline__ void normal_of(const PolyIn& P, int g, const double* 
 #pragma unroll
         for (int q = 0; q < D; ++q) nv[q] = P.pts[(size_t)g * D + q] - xi[q];
     } else {
-        const int ax = (g - P.n) >> 1;
+        const DevPlane& B = P.planes[g - P.n];
 #pragma unroll
-        for (int q = 0; q < D; ++q) nv[q] = q == ax ? 1.0 : 0.0;
+        for (int q = 0; q < D; ++q) nv[q] = B.n[q];
     }
 }
 
@@ -807,8 +807,7 @@ __global__ void k_cell_volumes(PolyIn P, double* vol) {
             const int k = P.nbr[t];
             double h;
             if (k >= P.n) {
-                const int p = k - P.n, q = p >> 1;
-                h = (p & 1) == 0 ? P.hi[q] - xi[q] : xi[q] - P.lo[q];
+                h = plane_height<D>(P.planes[k - P.n], xi);
             } else {
                 double s2 = 0;
 #pragma unroll
@@ -880,7 +879,7 @@ template <int D>
 static int poly_run(const PolyRun& R) {
     PolyIn P;
     P.n = R.n;
-    for (int q = 0; q < D; ++q) { P.lo[q] = R.lo[q]; P.hi[q] = R.hi[q]; }
+    P.planes = R.planes;
     P.pts = R.pts; P.osig = R.osig; P.oc = R.oc; P.nbr_off = R.nbr_off; P.nbr = R.nbr;
     P.foff = R.foff; P.fvert = R.fvert; P.slot_cell = R.slot_cell; P.area = R.area; P.status = R.status;
     cudaStream_t st = R.stream;

@@ -21,8 +21,8 @@
 namespace hv {
 
 template <int D>
-__global__ void k_morton(const double* __restrict__ in, int n, DevBox box, unsigned long long* codes, int* idx,
-                         unsigned* status) {
+__global__ void k_morton(const double* __restrict__ in, int n, DevBox box, const DevPlane* __restrict__ planes, int np,
+                         unsigned long long* codes, int* idx, unsigned* status) {
     constexpr int B = (63 / D) > 21 ? 21 : (63 / D);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         unsigned q[D];
@@ -34,6 +34,13 @@ __global__ void k_morton(const double* __restrict__ in, int n, DevBox box, unsig
             double f = (x - box.lo[k]) / (box.hi[k] - box.lo[k]) * (double)(1u << B);
             f = fmin(fmax(f, 0.0), (double)((1u << B) - 1));
             q[k] = ok ? (unsigned)f : 0u;
+        }
+        // strictly inside every boundary plane
+        for (int p = 0; p < np && ok; ++p) {
+            double nx = 0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) nx = fma(planes[p].n[k], in[(size_t)i * D + k], nx);
+            if (!(nx < planes[p].off)) ok = false;
         }
         if (!ok) atomicOr(status, ST_BADINPUT);
         unsigned long long code = 0;
@@ -353,13 +360,13 @@ __global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float
         default: break;                                \
     }
 
-void launch_morton(int d, const double* in, int n, const double* lo, const double* hi, unsigned long long* codes,
-                   int* idx, unsigned* status, cudaStream_t st) {
+void launch_morton(int d, const double* in, int n, const double* lo, const double* hi, const DevPlane* planes, int np,
+                   unsigned long long* codes, int* idx, unsigned* status, cudaStream_t st) {
     if (n <= 0) return;
     DevBox box;
     for (int k = 0; k < d; ++k) { box.lo[k] = lo[k]; box.hi[k] = hi[k]; }
     const int blocks = (n + 255) / 256;
-    HV_DISPATCH(d, (k_morton<DD><<<blocks, 256, 0, st>>>(in, n, box, codes, idx, status)));
+    HV_DISPATCH(d, (k_morton<DD><<<blocks, 256, 0, st>>>(in, n, box, planes, np, codes, idx, status)));
 }
 
 void launch_gather(int d, const double* in, const int* perm, int n, double* pts, float* pts32, float* pts32lo,

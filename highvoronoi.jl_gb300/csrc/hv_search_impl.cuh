@@ -190,16 +190,39 @@ __device__ __forceinline__ void eval_point(const DevMesh& M, const Query<D>& q, 
 template <int D>
 __device__ __forceinline__ void eval_planes(const DevMesh& M, const Query<D>& q, SearchOut& R) {
 #pragma unroll
-    for (int p = 0; p < 2 * D; ++p) {
+    for (int p = 0; p < M.np; ++p) {
         const int it = M.n + p;
         if (q_excluded<D>(q, it)) continue;
-        const int k = p >> 1;
-        const bool upper = (p & 1) == 0;
-        double uk = upper ? q.u[k] : -q.u[k];
-        double ck = q.xa[k] + q.rho[k];
-        double num = upper ? (M.hi[k] - ck) : (ck - M.lo[k]);
-        double e_num = 4.0 * EPS64 * (fabs(M.hi[k]) + fabs(M.lo[k]) + fabs(q.xa[k]) + fabs(q.rho[k])) + q.erho;
-        double e_den = q.eu + 2.0 * EPS64 * fabs(uk);
+        const DevPlane& P = M.planes[p];
+        double uk, num, e_num, e_den;
+        if (P.axis >= 0) {  // cuboid face: n = +-e_k, every product below is exact
+            double nc = 0, ac = 0;
+            uk = 0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                nc = fma(P.n[k], q.xa[k] + q.rho[k], nc);
+                uk = fma(P.n[k], q.u[k], uk);
+                ac += fabs(P.n[k]) * (fabs(q.xa[k]) + fabs(q.rho[k]));
+            }
+            num = P.off - nc;
+            e_num = 4.0 * EPS64 * (fabs(P.off) + ac) + q.erho;
+            e_den = q.eu + 2.0 * EPS64 * fabs(uk);
+        } else {  // off - n.(xa + rho): the xa part in double-double
+            const dd sx = plane_rhs_dd<D>(P, q.xa);
+            double nr = 0, nu = 0, an = 0, anr = 0, anu = 0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                nr = fma(P.n[k], q.rho[k], nr);
+                nu = fma(P.n[k], q.u[k], nu);
+                an += fabs(P.n[k]);
+                anr += fabs(P.n[k] * q.rho[k]);
+                anu += fabs(P.n[k] * q.u[k]);
+            }
+            num = (sx.hi + sx.lo) - nr;
+            uk = nu;
+            e_num = 4.0 * EPS64 * fabs(num) + (D + 4.0) * EPS64 * anr + q.erho * an;
+            e_den = q.eu * an + (D + 2.0) * EPS64 * anu;
+        }
         Cand c; c.item = it;
         if (uk > e_den) {
             c.t = num / uk;
@@ -387,13 +410,16 @@ __device__ int dd_rescore_walk(const DevMesh& M, const int (&sig)[D + 1], int m,
             if (!(den.hi > 0)) continue;
             t = (nd - dr * mk(2.0)) / den;
         } else {
-            const int p = it - M.n, k0 = p >> 1;
-            const bool upper = (p & 1) == 0;
-            dd uk = mk(0.0), ck = mk(0.0);
+            // off - n.(xa + rho) over n.u; for axis planes the zero terms and
+            // the +-1 products are exact
+            const DevPlane& P = M.planes[it - M.n];
+            dd uk = mk(0.0), num = mk(P.off);
 #pragma unroll
-            for (int k = 0; k < D; ++k) if (k == k0) { uk = upper ? u[k] : -u[k]; ck = mk(xa[k]) + rho[k]; }
+            for (int k = 0; k < D; ++k) {
+                uk += mk(P.n[k]) * u[k];
+                num -= mk(P.n[k]) * (mk(xa[k]) + rho[k]);
+            }
             if (!(uk.hi > 0)) continue;
-            dd num = upper ? (mk(M.hi[k0]) - ck) : (ck - mk(M.lo[k0]));
             t = num / uk;
         }
         if (best < 0 || t < bt || (!(bt < t) && it < best)) { second = best; st = bt; best = it; bt = t; }
@@ -426,13 +452,28 @@ __device__ int dd_rescore_point(const DevMesh& M, const Query<D>& q, const int* 
             if (!(den.hi > 0)) continue;
             t = (nd - dr * mk(2.0)) / den;
         } else {
-            const int p = it - M.n, k0 = p >> 1;
-            const bool upper = (p & 1) == 0;
-            double uk = upper ? q.u[k0] : -q.u[k0];
-            if (!(uk > 0)) continue;
-            dd ck = mk(q.xa[k0]) + mk(q.rho[k0]);
-            dd num = upper ? (mk(M.hi[k0]) - ck) : (ck - mk(M.lo[k0]));
-            t = num / mk(uk);
+            const DevPlane& P = M.planes[it - M.n];
+            if (P.axis >= 0) {  // n = +-e_k: the three dot products are exact
+                double uk = 0, xk = 0, rk = 0;
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    uk = fma(P.n[k], q.u[k], uk);
+                    xk = fma(P.n[k], q.xa[k], xk);
+                    rk = fma(P.n[k], q.rho[k], rk);
+                }
+                if (!(uk > 0)) continue;
+                t = (mk(P.off) - (mk(xk) + mk(rk))) / mk(uk);
+            } else {
+                dd uk = mk(0.0);
+                dd num = plane_rhs_dd<D>(P, q.xa);
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    uk += mk(P.n[k]) * mk(q.u[k]);
+                    num -= mk(P.n[k]) * mk(q.rho[k]);
+                }
+                if (!(uk.hi > 0)) continue;
+                t = num / uk;
+            }
         }
         if (best < 0 || t < bt || (!(bt < t) && it < best)) { best = it; bt = t; }
     }
@@ -729,10 +770,16 @@ __global__ void __launch_bounds__(128) k_descent(DevMesh M, int stride, int nsee
                 const double* p0 = M.pts + (size_t)S[0] * D;
 #pragma unroll
                 for (int k = 0; k < D; ++k) {
-                    double tol = 1e-12 * (1.0 + fabs(M.hi[k]) + fabs(M.lo[k]));
-                    if (c[k] < M.lo[k] - tol || c[k] > M.hi[k] + tol) good = false;
                     double e = __ldg(p0 + k) - c[k];
                     r2 = fma(e, e, r2);
+                }
+                // inside the domain (every plane, with a small tolerance)
+                for (int p = 0; p < M.np && good; ++p) {
+                    const DevPlane& P = M.planes[p];
+                    double nc = 0, anc = 0;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) { nc = fma(P.n[k], c[k], nc); anc += fabs(P.n[k] * c[k]); }
+                    if (nc > P.off + 1e-12 * (1.0 + fabs(P.off) + anc)) good = false;
                 }
                 if (good) good = !ball_occupied<D>(M, c, r2, S, 1e-10);
             }
@@ -933,6 +980,57 @@ __global__ void __launch_bounds__(128) k_centers(DevMesh M, unsigned v0, unsigne
 // ---------------------------------------------------------------------------
 // fast kernel: one warp expands one vertex entirely in FP32
 // ---------------------------------------------------------------------------
+// FP32 crossing of boundary plane P by the ray from c0 = xa + (xal + rho) along
+// u, as the interval [lo, hi] of its parameter; false if the ray moves away
+// from the plane.  Cuboid faces use the single coordinate; other planes bound
+// the rounding of the split coordinates, of the FP32 copies of n and off and of
+// the dot products.
+template <int D>
+__device__ __forceinline__ bool plane32(const DevPlane& P, const float* xa, const float* xal, const float* rho,
+                                        const float* u, float erho, float relu, float TINY, float& lo, float& hi) {
+    const float S32 = 5.9604645e-08f;
+    float num, e_num, uk, e_den;
+    if (P.axis >= 0) {  // n = +-e_k: the dot products are exact
+        float nc = 0.f, ac = 0.f;
+        uk = 0.f;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            nc = fmaf(P.n32[k], xa[k] + (xal[k] + rho[k]), nc);
+            uk = fmaf(P.n32[k], u[k], uk);
+            ac += fabsf(P.n32[k]) * (fabsf(xa[k]) + fabsf(rho[k]));
+        }
+        num = P.off32 - nc;
+        e_num = 4.f * S32 * (fabsf(P.off32) + ac) + erho + TINY;
+        e_den = relu + 2.f * S32 * fabsf(uk);
+    } else {
+        float nc = 0.f, nu = 0.f, an = 0.f, anc = 0.f, anu = 0.f;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const float ck = xa[k] + (xal[k] + rho[k]);
+            nc = fmaf(P.n32[k], ck, nc);
+            nu = fmaf(P.n32[k], u[k], nu);
+            an += fabsf(P.n32[k]);
+            anc += fabsf(P.n32[k]) * (fabsf(xa[k]) + fabsf(rho[k]));
+            anu += fabsf(P.n32[k] * u[k]);
+        }
+        num = P.off32 - nc;
+        uk = nu;
+        e_num = (2.f * D + 8.f) * S32 * (fabsf(P.off32) + anc) + erho * an + TINY;
+        e_den = relu * an + (D + 4.f) * S32 * anu;
+    }
+    if (uk > e_den) {
+        const float t = __fdividef(num, uk);
+        const float et = __fdividef(e_num + fabsf(t) * e_den, uk - e_den) * 1.00001f + 8.f * S32 * fabsf(t);
+        lo = t - et; hi = t + et;
+    } else if (uk < -e_den) {
+        return false;
+    } else {
+        if (num - e_num > 0.f) { lo = __fdividef(num - e_num, fabsf(uk) + e_den) * 0.99999f; hi = INFINITY; }
+        else { lo = -INFINITY; hi = INFINITY; }
+    }
+    return true;
+}
+
 constexpr int FAST_WPB = 4;  // warps per block
 
 template <int D>
@@ -1188,31 +1286,14 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 6) k_expand_fast(DevMesh M, uns
             float plo1 = INFINITY, phi1 = INFINITY, plo2 = INFINITY;
             int pj1 = -1;
 #pragma unroll 1
-            for (int p = 0; p < 2 * D; ++p) {
+            for (int p = 0; p < M.np; ++p) {
                 const int it = M.n + p;
                 bool ex = false;
 #pragma unroll
                 for (int s = 0; s < R; ++s) ex |= (sig[s] == it);
                 if (ex) continue;
-                const int k = p >> 1;
-                const bool upper = (p & 1) == 0;
-                const float uk = upper ? u[k] : -u[k];
-                const float hk = M.hi32[k], lk = M.lo32[k];
-                const float ck = xa[k] + (xal[k] + rho[k]);
-                const float num = upper ? (hk - ck) : (ck - lk);
-                const float e_num = 4.f * S32 * (fabsf(hk) + fabsf(lk) + fabsf(xa[k]) + fabsf(rho[k])) + erho + TINY;
-                const float e_den = relu + 2.f * S32 * fabsf(uk);
                 float lo, hi;
-                if (uk > e_den) {
-                    const float t = __fdividef(num, uk);
-                    const float et = __fdividef(e_num + fabsf(t) * e_den, uk - e_den) * 1.00001f + 8.f * S32 * fabsf(t);
-                    lo = t - et; hi = t + et;
-                } else if (uk < -e_den) {
-                    continue;
-                } else {
-                    if (num - e_num > 0.f) { lo = __fdividef(num - e_num, fabsf(uk) + e_den) * 0.99999f; hi = INFINITY; }
-                    else { lo = -INFINITY; hi = INFINITY; }
-                }
+                if (!plane32<D>(M.planes[p], xa, xal, rho, u, erho, relu, TINY, lo, hi)) continue;
                 if (lo < plo1) { plo2 = plo1; plo1 = lo; phi1 = hi; pj1 = it; }
                 else if (lo < plo2) plo2 = lo;
             }
@@ -1519,31 +1600,14 @@ __global__ void __launch_bounds__(FB_WPB * 32, 4) k_fallback_warp(DevMesh M, con
         if (lane == 0) {
             const float TINY = M.tiny32;
 #pragma unroll
-            for (int p = 0; p < 2 * D; ++p) {
+            for (int p = 0; p < M.np; ++p) {
                 const int it = M.n + p;
                 bool ex = false;
 #pragma unroll
                 for (int q = 0; q < R; ++q) ex |= (sig[q] == it);
                 if (ex) continue;
-                const int k = p >> 1;
-                const bool upper = (p & 1) == 0;
-                const float uk = upper ? u[k] : -u[k];
-                const float hk = M.hi32[k], lk = M.lo32[k];
-                const float ck = xa[k] + (xal[k] + rho[k]);
-                const float num = upper ? (hk - ck) : (ck - lk);
-                const float e_num = 4.f * S32 * (fabsf(hk) + fabsf(lk) + fabsf(xa[k]) + fabsf(rho[k])) + erho + TINY;
-                const float e_den = relu + 2.f * S32 * fabsf(uk);
                 float lo, hi;
-                if (uk > e_den) {
-                    const float t = __fdividef(num, uk);
-                    const float et = __fdividef(e_num + fabsf(t) * e_den, uk - e_den) * 1.00001f + 8.f * S32 * fabsf(t);
-                    lo = t - et; hi = t + et;
-                } else if (uk < -e_den) {
-                    continue;
-                } else {
-                    if (num - e_num > 0.f) { lo = __fdividef(num - e_num, fabsf(uk) + e_den) * 0.99999f; hi = INFINITY; }
-                    else { lo = -INFINITY; hi = INFINITY; }
-                }
+                if (!plane32<D>(M.planes[p], xa, xal, rho, u, erho, relu, TINY, lo, hi)) continue;
                 take(it, lo, hi);
             }
         }
@@ -1953,31 +2017,14 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_descent_warp(DevMesh M, int str
             if (lane == 0) {
                 const float TINY = M.tiny32;
 #pragma unroll
-                for (int p = 0; p < 2 * D; ++p) {
+                for (int p = 0; p < M.np; ++p) {
                     const int it = M.n + p;
                     bool ex = false;
 #pragma unroll
                     for (int q = 0; q <= D; ++q) ex |= (T[q] == it);
                     if (ex) continue;
-                    const int k = p >> 1;
-                    const bool upper = (p & 1) == 0;
-                    const float uk = upper ? u[k] : -u[k];
-                    const float hk = M.hi32[k], lk = M.lo32[k];
-                    const float ck = xa[k] + (xal[k] + rho[k]);
-                    const float num = upper ? (hk - ck) : (ck - lk);
-                    const float e_num = 4.f * S32 * (fabsf(hk) + fabsf(lk) + fabsf(xa[k]) + fabsf(rho[k])) + erho + TINY;
-                    const float e_den = relu + 2.f * S32 * fabsf(uk);
                     float lo, hi;
-                    if (uk > e_den) {
-                        const float t = __fdividef(num, uk);
-                        const float et = __fdividef(e_num + fabsf(t) * e_den, uk - e_den) * 1.00001f + 8.f * S32 * fabsf(t);
-                        lo = t - et; hi = t + et;
-                    } else if (uk < -e_den) {
-                        continue;
-                    } else {
-                        if (num - e_num > 0.f) { lo = __fdividef(num - e_num, fabsf(uk) + e_den) * 0.99999f; hi = INFINITY; }
-                        else { lo = -INFINITY; hi = INFINITY; }
-                    }
+                    if (!plane32<D>(M.planes[p], xa, xal, rho, u, erho, relu, TINY, lo, hi)) continue;
                     H = fminf(H, hi);
                     top2_add(lo1, hi1, j1, lo2, lo, hi, it);
                 }
@@ -2020,10 +2067,22 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_descent_warp(DevMesh M, int str
                     }
                     tt = (nd - 2.0 * dr) / (2.0 * du);
                 } else {
-                    const int p = j1 - M.n, k0 = p >> 1;
-                    const bool upper = (p & 1) == 0;
-                    const double ck = xi[k0] + sRho[wib][k0];
-                    tt = (upper ? (M.hi[k0] - ck) : (ck - M.lo[k0])) / (upper ? sU[wib][k0] : -sU[wib][k0]);
+                    const DevPlane& P = M.planes[j1 - M.n];
+                    if (P.axis >= 0) {  // n = +-e_k: exact dot products
+                        double nc = 0, nu = 0;
+#pragma unroll
+                        for (int k = 0; k < D; ++k) {
+                            nc = fma(P.n[k], xi[k] + sRho[wib][k], nc);
+                            nu = fma(P.n[k], sU[wib][k], nu);
+                        }
+                        tt = (P.off - nc) / nu;
+                    } else {
+                        const dd sx = plane_rhs_dd<D>(P, xi);
+                        double nr = 0, nu = 0;
+#pragma unroll
+                        for (int k = 0; k < D; ++k) { nr = fma(P.n[k], sRho[wib][k], nr); nu = fma(P.n[k], sU[wib][k], nu); }
+                        tt = ((sx.hi + sx.lo) - nr) / nu;
+                    }
                 }
 #pragma unroll
                 for (int k = 0; k < D; ++k) sRho[wib][k] = fma(tt, sU[wib][k], sRho[wib][k]);

@@ -6,7 +6,8 @@ Python host side that mirrors the reference's VoronoiGeometry / VoronoiData API.
 from ._lib import (HV_METHOD_FAST, HV_METHOD_PLAIN, Context, HVError, Mesh, default_context, load,  # noqa: F401
                    make_params)
 from .geometry import (RCGPU, RCGPUPlain, VI_FAST_POLYGON, VI_GEOMETRY, VI_HEURISTIC_MC, VI_POLYGON,  # noqa: F401
-                       Boundary, RaycastMethod, VoronoiData, VoronoiGeometry, cuboid)
+                       BC_Dirichlet, BC_Neumann, BC_Periodic, Boundary, Dirichlet, Neumann, Plane, RaycastMethod,
+                       VoronoiData, VoronoiGeometry, cuboid)
 from . import datasets  # noqa: F401
 
 __version__ = "1.0.0"

@@ -85,6 +85,12 @@ def load(path: str | None = None):
         L.hv_mesh_build.restype = I
         L.hv_mesh_build_device.argtypes = [P, I, I64, P, dp, dp, ctypes.POINTER(Params), ctypes.POINTER(P)]
         L.hv_mesh_build_device.restype = I
+        i16p = ctypes.POINTER(ctypes.c_int16)
+        L.hv_mesh_build_planes.argtypes = [P, I, I64, P, I, dp, dp, i16p, ctypes.POINTER(Params), ctypes.POINTER(P)]
+        L.hv_mesh_build_planes.restype = I
+        L.hv_mesh_build_planes_device.argtypes = [P, I, I64, P, I, dp, dp, i16p, ctypes.POINTER(Params),
+                                                  ctypes.POINTER(P)]
+        L.hv_mesh_build_planes_device.restype = I
         L.hv_mesh_counts.argtypes = [P, ip, ip]; L.hv_mesh_counts.restype = I
         L.hv_autotune.argtypes = [P, I, I64, P, dp, dp, ctypes.POINTER(Params)]; L.hv_autotune.restype = I
         L.hv_mesh_vertices.argtypes = [P, ip, dp]; L.hv_mesh_vertices.restype = I
@@ -195,14 +201,39 @@ def make_params(method: int = HV_METHOD_FAST, **kw) -> Params:
 class Mesh:
     """A mesh built on the device (hv_mesh).  Results are copied out on demand."""
 
-    def __init__(self, ctx: Context, pts: np.ndarray, lo, hi, params: Params, device_ptr: int | None = None):
+    def __init__(self, ctx: Context, pts: np.ndarray, lo, hi, params: Params, device_ptr: int | None = None,
+                 planes=None):
+        """Box domain [lo, hi], or (lo = hi = None) the convex domain of
+        ``planes = (base, normal, bc)``: (P, d) base points, (P, d) outer
+        normals and P boundary-condition codes (or None)."""
         L = load()
         self.ctx = ctx
         pts = np.ascontiguousarray(pts, dtype=np.float64)
         self.n, self.d = pts.shape if device_ptr is None else (int(pts[0]), int(pts[1]))
+        h = ctypes.c_void_p()
+        if planes is not None:
+            base = np.ascontiguousarray(planes[0], dtype=np.float64)
+            normal = np.ascontiguousarray(planes[1], dtype=np.float64)
+            if base.shape != normal.shape or base.ndim != 2 or base.shape[1] != self.d:
+                raise ValueError("plane bases and normals must be (P, d) arrays")
+            bc = None if planes[2] is None else np.ascontiguousarray(planes[2], dtype=np.int16)
+            bcp = None if bc is None else bc.ctypes.data_as(ctypes.POINTER(ctypes.c_int16))
+            self.lo = self.hi = None
+            self.planes = (base, normal, bc)
+            if device_ptr is None:
+                rc = L.hv_mesh_build_planes(ctx.handle, self.d, self.n, pts.ctypes.data_as(ctypes.c_void_p),
+                                            base.shape[0], dptr(base), dptr(normal), bcp, ctypes.byref(params),
+                                            ctypes.byref(h))
+            else:
+                rc = L.hv_mesh_build_planes_device(ctx.handle, self.d, self.n, ctypes.c_void_p(device_ptr),
+                                                   base.shape[0], dptr(base), dptr(normal), bcp,
+                                                   ctypes.byref(params), ctypes.byref(h))
+            ctx.check(rc, "hv_mesh_build_planes")
+            self._h = h
+            return
+        self.planes = None
         self.lo = np.ascontiguousarray(lo, dtype=np.float64)
         self.hi = np.ascontiguousarray(hi, dtype=np.float64)
-        h = ctypes.c_void_p()
         if device_ptr is None:
             rc = L.hv_mesh_build(ctx.handle, self.d, self.n, pts.ctypes.data_as(ctypes.c_void_p), dptr(self.lo),
                                  dptr(self.hi), ctypes.byref(params), ctypes.byref(h))

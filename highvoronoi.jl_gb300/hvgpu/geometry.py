@@ -3,7 +3,8 @@
     VoronoiGeometry(xs, cuboid(d, periodic=[]); search_settings=dict(method=RCGPU),
                     integrator=VI_POLYGON)           src/geometry.jl:139-201
     VoronoiData(geometry)                            src/voronoidata.jl:545-700
-    cuboid(dim; dimensions, periodic, offset)        src/boundary.jl:518-534
+    cuboid(dim; dimensions, periodic, offset)        src/boundary.jl:510-534
+    Boundary(planes...), BC_Dirichlet, BC_Neumann    src/boundary.jl:22-45,94-131
 
 The names, argument meanings and conventions (1-based generators, boundary
 plane p as generator N+p, sorted signatures, neighbour lists with the planes
@@ -18,36 +19,99 @@ import numpy as np
 from . import _lib
 
 
+# Boundary-condition codes of a plane (src/boundary.jl:2-3); a positive code
+# names the periodic partner plane.
+Dirichlet = 0
+Neumann = -1
+
+
 @dataclass
+class Plane:
+    """A boundary plane through ``base`` with outer normal ``normal``
+    (src/boundary.jl:22-29); the domain side is (x - base) . normal < 0."""
+    base: np.ndarray
+    normal: np.ndarray
+    BC: int = Dirichlet
+
+
+def BC_Dirichlet(b, n) -> Plane:
+    return Plane(np.asarray(b, dtype=np.float64), np.asarray(n, dtype=np.float64), Dirichlet)
+
+
+def BC_Neumann(b, n) -> Plane:
+    return Plane(np.asarray(b, dtype=np.float64), np.asarray(n, dtype=np.float64), Neumann)
+
+
+def BC_Periodic(base1, base2, normal1):
+    """Periodic plane pairs (src/boundary.jl:47-57) are not part of the GPU mesh path."""
+    raise NotImplementedError("periodic boundaries are not part of the GPU mesh path")
+
+
 class Boundary:
-    """Axis-aligned box [offset, offset + dimensions] with Dirichlet planes."""
-    lo: np.ndarray
-    hi: np.ndarray
-    periodic: list = field(default_factory=list)
+    """A convex domain: the intersection of the half-spaces of its planes
+    (src/boundary.jl:78-131).  ``Boundary(p1, p2, ...)`` takes Plane objects
+    in the reference's order: plane p (1-based) is generator N+p.  A box made
+    by ``cuboid`` also carries ``lo`` and ``hi`` and runs through the box
+    entry point (exact single-coordinate plane arithmetic); any other domain
+    runs through the plane entry point, where normals are scaled to unit length.
+    Domains must be bounded with a non-empty interior; at most 64 planes."""
+
+    def __init__(self, *planes: Plane, lo=None, hi=None):
+        for p in planes:
+            if not isinstance(p, Plane):
+                raise TypeError("Boundary takes Plane objects (BC_Dirichlet / BC_Neumann)")
+            if p.BC > 0:
+                raise NotImplementedError("periodic boundaries are not part of the GPU mesh path")
+        self.planes = list(planes)
+        self.lo = None if lo is None else np.asarray(lo, dtype=np.float64)
+        self.hi = None if hi is None else np.asarray(hi, dtype=np.float64)
+        self.periodic: list = []
 
     @property
     def dim(self) -> int:
-        return int(self.lo.shape[0])
+        return int(self.planes[0].normal.shape[0]) if self.planes else 0
 
     @property
     def nplanes(self) -> int:
-        return 2 * self.dim
+        return len(self.planes)
+
+    @property
+    def is_box(self) -> bool:
+        return self.lo is not None
+
+    def arrays(self):
+        """(base (P, d), normal (P, d), BC (P,) int16) in plane order."""
+        base = np.array([p.base for p in self.planes], dtype=np.float64)
+        normal = np.array([p.normal for p in self.planes], dtype=np.float64)
+        bc = np.array([p.BC for p in self.planes], dtype=np.int16)
+        return base, normal, bc
+
+    def __contains__(self, x) -> bool:
+        """Membership as the reference tests it (src/boundary.jl:427-435)."""
+        x = np.asarray(x, dtype=np.float64)
+        return all(float(np.dot(p.base - x, p.normal)) >= 0.0 for p in self.planes)
 
 
 def cuboid(dim: int, dimensions=None, periodic=None, neumann=(), offset=None) -> Boundary:
-    """The reference's cuboid (src/boundary.jl:518-534).  Its default is fully
+    """The reference's cuboid (src/boundary.jl:510-534).  Its default is fully
     periodic (periodic=1:dim); only non-periodic boxes run on the GPU path, so
     pass ``periodic=[]`` as the reference's own tests and benchmarks do
     (test/rcmethods.jl:4, src/statistics.jl:107).  Plane 2k-1 is the upper face
-    of axis k and plane 2k the lower face, as in the reference."""
+    of axis k and plane 2k the lower face, as in the reference; ``neumann``
+    lists k for a Neumann upper face and -k for a Neumann lower face."""
     dims = np.ones(dim) if dimensions is None else np.asarray(dimensions, dtype=np.float64)
     off = np.zeros(dim) if offset is None else np.asarray(offset, dtype=np.float64)
     per = list(range(1, dim + 1)) if periodic is None else list(periodic)
     if per:
         raise NotImplementedError("periodic boundaries are not part of the GPU mesh path; use periodic=[]")
-    # Neumann and Dirichlet planes give the same mesh; the flag only matters to the FV layer.
-    del neumann
-    return Boundary(lo=off.copy(), hi=off + dims, periodic=per)
+    neu = set(int(k) for k in neumann)
+    planes = []
+    for k in range(dim):
+        unit = np.zeros(dim)
+        unit[k] = 1.0
+        planes.append(Plane(off + dims * unit, unit.copy(), Neumann if (k + 1) in neu else Dirichlet))
+        planes.append(Plane(off.copy(), -unit, Neumann if -(k + 1) in neu else Dirichlet))
+    return Boundary(*planes, lo=off.copy(), hi=off + dims)
 
 
 @dataclass(frozen=True)
@@ -90,7 +154,7 @@ class VoronoiGeometry:
             raise ValueError("xs must be an (n, d) array")
         n, d = pts.shape
         if b is None:
-            raise ValueError("a bounded domain is required: pass cuboid(d, periodic=[])")
+            raise ValueError("a bounded domain is required: pass cuboid(d, periodic=[]) or Boundary(planes...)")
         if b.dim != d:
             raise ValueError("dimension of the boundary and of the points differ")
         ss = dict(search_settings or {})
@@ -107,10 +171,16 @@ class VoronoiGeometry:
         self.nodes = pts
         self.method = method
         if autotune and method.code == _lib.HV_METHOD_FAST:
-            # tuned on synthetic points of the same (d, n); cached in the context
-            self.ctx.autotune(d, n, lo=b.lo, hi=b.hi)
+            # tuned on synthetic points of the same (d, n) in the domain's box; cached in the context
+            if b.is_box:
+                self.ctx.autotune(d, n, lo=b.lo, hi=b.hi)
+            else:
+                self.ctx.autotune(d, n, pts=pts, lo=pts.min(axis=0) - 1.0, hi=pts.max(axis=0) + 1.0)
         self.params = _lib.make_params(method.code, **ss)
-        self.mesh = _lib.Mesh(self.ctx, pts, b.lo, b.hi, self.params)
+        if b.is_box:
+            self.mesh = _lib.Mesh(self.ctx, pts, b.lo, b.hi, self.params)
+        else:
+            self.mesh = _lib.Mesh(self.ctx, pts, None, None, self.params, planes=b.arrays())
         self.integrator = integrator
         self._volumes = None
         self._areas = None

@@ -23,8 +23,10 @@
  * Conventions (identical to the reference): generators are 1-based; the
  * domain is the non-periodic cuboid [lo, hi] (cuboid(d, dimensions=hi-lo,
  * offset=lo, periodic=[]), src/boundary.jl:518-534) whose plane p (1-based,
- * 2k-1 = upper face of axis k, 2k = lower face) is generator n+p; every vertex
- * signature is sorted ascending.  Point arrays are d x n column-major doubles
+ * 2k-1 = upper face of axis k, 2k = lower face) is generator n+p, or (the
+ * *_planes builds) a convex domain of Dirichlet/Neumann planes given by base
+ * points and normals (Boundary(planes...), src/boundary.jl:94-131) whose plane
+ * p is generator n+p; every vertex signature is sorted ascending.  Point arrays are d x n column-major doubles
  * (Julia layout): point i occupies pts[d*i .. d*i+d-1].
  *
  * Ownership: the caller owns all host arrays; device memory belongs to the
@@ -127,6 +129,22 @@ int hv_mesh_build(hv_ctx* ctx, int d, int64_t n, const double* pts, const double
 /* Same with pts already in device memory (d x n doubles on the context's device). */
 int hv_mesh_build_device(hv_ctx* ctx, int d, int64_t n, const double* d_pts, const double* lo,
                          const double* hi, const hv_params* params, hv_mesh** out);
+/* Vertex search inside the convex domain {x : (x - base_p) . normal_p <= 0
+ * for every p} of nplanes (1..64) boundary planes (Plane(base, normal, BC),
+ * src/boundary.jl:22-29; membership test src/boundary.jl:427-435).  base and
+ * normal are d x nplanes column-major host arrays (plane p at [d*p .. d*p+d-1]);
+ * normals are scaled to unit length (the reference's reflection,
+ * src/boundary.jl:206-211, assumes unit normals).  bc (nplanes entries, may be
+ * NULL) takes the reference's codes: Dirichlet and Neumann planes are accepted,
+ * periodic ones (bc > 0) are HV_E_INVALID_ARG.  An unbounded domain or one
+ * with an empty interior is HV_E_INVALID_ARG.  Plane p (0-based) is generator
+ * n+p+1 in the 1-based output. */
+int hv_mesh_build_planes(hv_ctx* ctx, int d, int64_t n, const double* pts, int nplanes, const double* base,
+                         const double* normal, const int16_t* bc, const hv_params* params, hv_mesh** out);
+/* Same with pts already in device memory (base, normal and bc stay host arrays). */
+int hv_mesh_build_planes_device(hv_ctx* ctx, int d, int64_t n, const double* d_pts, int nplanes,
+                                const double* base, const double* normal, const int16_t* bc,
+                                const hv_params* params, hv_mesh** out);
 
 /* Autotuner: times hv_mesh_build over a small grid of knn x leaf_size x
  * seed_stride (x rays_per_warp) on the given points (pts == NULL: uniform

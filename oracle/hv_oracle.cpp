@@ -13,10 +13,13 @@
  *    (2 u.(x_j - x_0))  (src/raycast.jl:794-970, get_t src/raycast.jl:395-397).
  *    The search is the fused shrinking-ball traversal of RCCombined
  *    (src/raycast.jl:504-528, kd_tree.jl:269-336).
- *  - boundary: cuboid planes enter as mirror generators N+p
- *    (src/raycast.jl:354-375, src/boundary.jl:206-211,518-534).  The mirror of
- *    the cell's generator across plane p has t equal to the plane crossing of
- *    the ray, which is what is evaluated here.
+ *  - boundary: the planes of a convex domain (cuboid(d, periodic=[]) or
+ *    Boundary(planes...), src/boundary.jl:94-131,510-534) enter as mirror
+ *    generators N+p (src/raycast.jl:354-375, reflect src/boundary.jl:206-211).
+ *    The mirror of the cell's generator across plane p has t equal to the
+ *    plane crossing of the ray, which is what is evaluated here.  A plane is
+ *    n.x <= off with n the unit outer normal and off = n.base rounded once;
+ *    axis planes (n = +-e_k) keep their exact single-coordinate arithmetic.
  *  - ray direction: unit vector orthogonal to the edge's generator span,
  *    pointing away from the dropped generator (u_qr, src/tools.jl:773-790).
  *  - descent: d successive raycasts from x_i along random directions
@@ -79,6 +82,7 @@ static_assert(sizeof(qreal) == 16, "binary128 required");
 namespace {
 
 constexpr int MAXD = 8;
+constexpr int MAXP = 64;
 constexpr double EPS = 1.1102230246251565e-16;  // 2^-53
 
 std::mutex g_err_mu;
@@ -134,7 +138,11 @@ struct Problem {
     int d = 0;
     int n = 0;
     std::vector<double> X;  // n*d
-    double blo[MAXD], bhi[MAXD];
+    int np = 0;                   // boundary planes n.x <= off, generator ids n + p
+    double pn[MAXP][MAXD] = {};
+    double poff[MAXP] = {};
+    int pax[MAXP] = {};           // axis k for n = sgn e_k, else -1
+    int psg[MAXP] = {};
     std::vector<KdNode> nodes;
     std::vector<int> perm;
     uint64_t seed = 0;
@@ -224,10 +232,16 @@ void constraint_row(const Problem& P, int a, int it, T* row, T& rhs) {
         for (int k = 0; k < d; ++k) { row[k] = (T)xg[k] - (T)xa[k]; s += row[k] * row[k]; }
         rhs = s / 2;
     } else {
-        int p = it - P.n, k = p / 2;
-        for (int q = 0; q < d; ++q) row[q] = 0;
-        if (p % 2 == 0) { row[k] = 1; rhs = (T)P.bhi[k] - (T)xa[k]; }
-        else { row[k] = -1; rhs = (T)xa[k] - (T)P.blo[k]; }
+        const int p = it - P.n;
+        for (int q = 0; q < d; ++q) row[q] = (T)P.pn[p][q];
+        if (P.pax[p] >= 0) {
+            const int k = P.pax[p];
+            rhs = P.psg[p] > 0 ? (T)P.poff[p] - (T)xa[k] : (T)P.poff[p] + (T)xa[k];
+        } else {  // off - n.xa evaluated in binary128, rounded once to T
+            qreal s = (qreal)P.poff[p];
+            for (int q = 0; q < d; ++q) s -= (qreal)P.pn[p][q] * (qreal)xa[q];
+            rhs = (T)s;
+        }
     }
 }
 
@@ -371,15 +385,33 @@ struct Searcher {
     void eval_planes(const RayQuery& q, RayResult& R) const {
         const int d = P.d;
         const double* xa = P.x(q.a);
-        for (int p = 0; p < 2 * d; ++p) {
+        for (int p = 0; p < P.np; ++p) {
             int it = P.n + p;
             if (excluded(q, it)) continue;
-            int k = p / 2; bool upper = (p % 2 == 0);
-            double uk = upper ? q.u[k] : -q.u[k];
-            double ck = xa[k] + q.rho[k];
-            double num = upper ? (P.bhi[k] - ck) : (ck - P.blo[k]);
-            double e_num = 4.0 * EPS * (std::fabs(P.bhi[k]) + std::fabs(P.blo[k]) + std::fabs(xa[k]) + std::fabs(q.rho[k])) + q.erho;
-            double e_den = q.eu + 2.0 * EPS * std::fabs(uk);
+            double uk, num, e_num, e_den;
+            if (P.pax[p] >= 0) {
+                const int k = P.pax[p];
+                const double ck = xa[k] + q.rho[k];
+                uk = P.psg[p] > 0 ? q.u[k] : -q.u[k];
+                num = P.psg[p] > 0 ? P.poff[p] - ck : P.poff[p] + ck;
+                e_num = 4.0 * EPS * (std::fabs(P.poff[p]) + std::fabs(xa[k]) + std::fabs(q.rho[k])) + q.erho;
+                e_den = q.eu + 2.0 * EPS * std::fabs(uk);
+            } else {  // off - n.xa in binary128, then - n.rho over n.u in FP64
+                qreal sx = (qreal)P.poff[p];
+                double nr = 0, nu = 0, an = 0, anr = 0, anu = 0;
+                for (int k = 0; k < d; ++k) {
+                    sx -= (qreal)P.pn[p][k] * (qreal)xa[k];
+                    nr += P.pn[p][k] * q.rho[k];
+                    nu += P.pn[p][k] * q.u[k];
+                    an += std::fabs(P.pn[p][k]);
+                    anr += std::fabs(P.pn[p][k] * q.rho[k]);
+                    anu += std::fabs(P.pn[p][k] * q.u[k]);
+                }
+                num = (double)sx - nr;
+                uk = nu;
+                e_num = 4.0 * EPS * std::fabs(num) + (d + 4.0) * EPS * anr + q.erho * an;
+                e_den = q.eu * an + (d + 2.0) * EPS * anu;
+            }
             Cand c; c.item = it;
             if (uk > e_den) {
                 c.t = num / uk;
@@ -532,11 +564,13 @@ int quad_rescore_walk(const Problem& P, const int* S, int m, const std::vector<i
             if (!(den > 0)) continue;
             ts.push_back({it, (nd - 2 * dr) / den});
         } else {
-            int p = it - P.n, k = p / 2; bool upper = (p % 2 == 0);
-            qreal uk = upper ? u[k] : -u[k];
+            const int p = it - P.n;
+            qreal uk = 0, num = (qreal)P.poff[p];
+            for (int k = 0; k < d; ++k) {
+                uk += (qreal)P.pn[p][k] * u[k];
+                num -= (qreal)P.pn[p][k] * ((qreal)xa[k] + rho[k]);
+            }
             if (!(uk > 0)) continue;
-            qreal ck = (qreal)xa[k] + rho[k];
-            qreal num = upper ? ((qreal)P.bhi[k] - ck) : (ck - (qreal)P.blo[k]);
             ts.push_back({it, num / uk});
         }
     }
@@ -564,11 +598,14 @@ int quad_rescore_point(const Problem& P, const RayQuery& q, const std::vector<in
             if (!(den > 0)) continue;
             t = (nd - 2 * dr) / den;
         } else {
-            int p = it - P.n, k = p / 2; bool upper = (p % 2 == 0);
-            qreal uk = upper ? (qreal)q.u[k] : -(qreal)q.u[k];
+            const int p = it - P.n;
+            qreal uk = 0, num = (qreal)P.poff[p];
+            for (int k = 0; k < d; ++k) {
+                uk += (qreal)P.pn[p][k] * (qreal)q.u[k];
+                num -= (qreal)P.pn[p][k] * ((qreal)xa[k] + (qreal)q.rho[k]);
+            }
             if (!(uk > 0)) continue;
-            qreal ck = (qreal)xa[k] + (qreal)q.rho[k];
-            t = (upper ? ((qreal)P.bhi[k] - ck) : (ck - (qreal)P.blo[k])) / uk;
+            t = num / uk;
         }
         if (best < 0 || t < bt || (t == bt && it < best)) { best = it; bt = t; }
     }
@@ -705,9 +742,10 @@ struct Explorer {
         const double* xa = P.x(sig[0]);
         double c[MAXD], r2 = 0;
         for (int k = 0; k < d; ++k) { c[k] = xa[k] + V.rho[k]; r2 += V.rho[k] * V.rho[k]; }
-        for (int k = 0; k < d; ++k) {
-            double tol = 1e-12 * (1.0 + std::fabs(P.bhi[k]) + std::fabs(P.blo[k]));
-            if (c[k] < P.blo[k] - tol || c[k] > P.bhi[k] + tol) return false;
+        for (int p = 0; p < P.np; ++p) {  // inside every plane, with a small tolerance
+            double nc = 0, anc = 0;
+            for (int k = 0; k < d; ++k) { nc += P.pn[p][k] * c[k]; anc += std::fabs(P.pn[p][k] * c[k]); }
+            if (nc > P.poff[p] + 1e-12 * (1.0 + std::fabs(P.poff[p]) + anc)) return false;
         }
         std::vector<int> reals;
         for (int s : sig) if (!P.is_plane(s)) reals.push_back(s);
@@ -836,6 +874,89 @@ struct PolyCell {
     }
 };
 
+/* Cuboid planes: 2k upper face (n = +e_k, off = hi_k), 2k+1 lower face
+ * (n = -e_k, off = -lo_k), the order of cuboid (src/boundary.jl:510-534). */
+void set_box_planes(Problem& P, const double* lo, const double* hi) {
+    P.np = 2 * P.d;
+    for (int k = 0; k < P.d; ++k)
+        for (int s = 0; s < 2; ++s) {
+            const int p = 2 * k + s;
+            for (int q = 0; q < MAXD; ++q) P.pn[p][q] = 0;
+            P.pn[p][k] = s == 0 ? 1.0 : -1.0;
+            P.poff[p] = s == 0 ? hi[k] : -lo[k];
+            P.pax[p] = k;
+            P.psg[p] = s == 0 ? 1 : -1;
+        }
+}
+
+/* Planes from base points and normals (Plane(base, normal, BC),
+ * src/boundary.jl:22-29): normals scaled to unit length (the reflection of
+ * src/boundary.jl:206-211 assumes |n| = 1), off = n.base as a double-double
+ * dot product rounded once; a normal with one non-zero entry is the exact
+ * axis plane +-e_k with off = +-base_k. */
+bool set_planes(Problem& P, int np, const double* base, const double* normal) {
+    if (np < 1 || np > MAXP) return false;
+    P.np = np;
+    const int d = P.d;
+    for (int p = 0; p < np; ++p) {
+        const double* b = base + (size_t)p * d;
+        const double* nv = normal + (size_t)p * d;
+        double s = 0;
+        int nz = 0, ax = -1;
+        for (int k = 0; k < d; ++k) {
+            if (!std::isfinite(b[k]) || !std::isfinite(nv[k])) return false;
+            s += nv[k] * nv[k];
+            if (nv[k] != 0) { ++nz; ax = k; }
+        }
+        if (!(s > 0)) return false;
+        for (int q = 0; q < MAXD; ++q) P.pn[p][q] = 0;
+        if (nz == 1) {
+            P.pax[p] = ax;
+            P.psg[p] = nv[ax] > 0 ? 1 : -1;
+            P.pn[p][ax] = (double)P.psg[p];
+            P.poff[p] = P.psg[p] > 0 ? b[ax] : -b[ax];
+        } else {
+            const double inv = 1.0 / std::sqrt(s);
+            for (int k = 0; k < d; ++k) P.pn[p][k] = nv[k] * inv;
+            double hi = 0, lo = 0;  // two-product / two-sum chain
+            for (int k = 0; k < d; ++k) {
+                const double pr = P.pn[p][k] * b[k];
+                const double pe = std::fma(P.pn[p][k], b[k], -pr);
+                const double sm = hi + pr;
+                const double bb = sm - hi;
+                const double se = (hi - (sm - bb)) + (pr - bb);
+                hi = sm;
+                lo += se + pe;
+            }
+            P.poff[p] = hi + lo;
+            P.pax[p] = -1;
+            P.psg[p] = 0;
+        }
+    }
+    return true;
+}
+
+/* Strictly inside every plane: n.x < off with the FMA chain of the GPU check. */
+bool inside_planes(const Problem& P, const double* x) {
+    for (int p = 0; p < P.np; ++p) {
+        double nx = 0;
+        for (int k = 0; k < P.d; ++k) nx = std::fma(P.pn[p][k], x[k], nx);
+        if (!(nx < P.poff[p])) return false;
+    }
+    return true;
+}
+
+/* off - n.x: exact single subtraction for axis planes, binary128 otherwise. */
+double plane_height(const Problem& P, int p, const double* x) {
+    if (P.pax[p] >= 0) {
+        const int k = P.pax[p];
+        return P.psg[p] > 0 ? P.poff[p] - x[k] : P.poff[p] + x[k];
+    }
+    qreal s = (qreal)P.poff[p];
+    for (int q = 0; q < P.d; ++q) s -= (qreal)P.pn[p][q] * (qreal)x[q];
+    return (double)s;
+}
+
 double height(const Problem& P, int i, int k) {
     const double* xi = P.x(i);
     if (!P.is_plane(k)) {
@@ -844,8 +965,7 @@ double height(const Problem& P, int i, int k) {
         for (int q = 0; q < P.d; ++q) { double e = xk[q] - xi[q]; s += e * e; }
         return 0.5 * std::sqrt(s);
     }
-    int p = k - P.n, q = p / 2;
-    return (p % 2 == 0) ? (P.bhi[q] - xi[q]) : (xi[q] - P.blo[q]);
+    return plane_height(P, k - P.n, xi);
 }
 
 }  // namespace
@@ -887,18 +1007,39 @@ const char* hvo_last_error(void) {
     return g_last_err.c_str();
 }
 
+static int build_mesh(hvo_mesh* M, int64_t n, const double* pts, int nthreads, int mode, int integrate,
+                      hvo_mesh** out);
+
 int hvo_build(int d, int64_t n, const double* pts, const double* lo, const double* hi,
               uint64_t seed, int nthreads, int mode, int integrate, hvo_mesh** out) {
     if (d < 2 || d > MAXD || n < 0 || n > (1ll << 30) || !out) { set_err("invalid argument"); return -1; }
     hvo_mesh* M = new hvo_mesh();
     Problem& P = M->P;
     P.d = d; P.n = (int)n; P.seed = seed;
-    P.X.assign(pts, pts + (size_t)n * d);
-    for (int k = 0; k < d; ++k) { P.blo[k] = lo[k]; P.bhi[k] = hi[k]; }
-    for (int64_t i = 0; i < n; ++i) for (int k = 0; k < d; ++k) {
-        double v = pts[i * d + k];
-        if (!(v > lo[k] && v < hi[k])) { set_err("point outside the open box"); delete M; return -2; }
+    set_box_planes(P, lo, hi);
+    return build_mesh(M, n, pts, nthreads, mode, integrate, out);
+}
+
+int hvo_build_planes(int d, int64_t n, const double* pts, int np, const double* base, const double* normal,
+                     uint64_t seed, int nthreads, int mode, int integrate, hvo_mesh** out) {
+    if (d < 2 || d > MAXD || n < 0 || n > (1ll << 30) || !out || !base || !normal) {
+        set_err("invalid argument");
+        return -1;
     }
+    hvo_mesh* M = new hvo_mesh();
+    Problem& P = M->P;
+    P.d = d; P.n = (int)n; P.seed = seed;
+    if (!set_planes(P, np, base, normal)) { set_err("invalid planes"); delete M; return -1; }
+    return build_mesh(M, n, pts, nthreads, mode, integrate, out);
+}
+
+static int build_mesh(hvo_mesh* M, int64_t n, const double* pts, int nthreads, int mode, int integrate,
+                      hvo_mesh** out) {
+    Problem& P = M->P;
+    const int d = P.d;
+    P.X.assign(pts, pts + (size_t)n * d);
+    for (int64_t i = 0; i < n; ++i)
+        if (!inside_planes(P, pts + i * d)) { set_err("point outside the open domain"); delete M; return -2; }
     build_tree(P);
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -1074,9 +1215,8 @@ int hvo_heuristic_mc(const hvo_mesh* m, int ndir, uint64_t seed, int nthreads,
                 s = std::sqrt(s);
                 for (int q = 0; q < d; ++q) nrm[t * d + q] /= s;
             } else {
-                int p = k - P.n;
-                for (int q = 0; q < d; ++q) nrm[t * d + q] = 0;
-                nrm[t * d + p / 2] = (p % 2 == 0) ? 1.0 : -1.0;
+                const int p = k - P.n;
+                for (int q = 0; q < d; ++q) nrm[t * d + q] = P.pn[p][q];
             }
         }
         double sv = 0, sv2 = 0;
@@ -1100,10 +1240,11 @@ int hvo_heuristic_mc(const hvo_mesh* m, int ndir, uint64_t seed, int nthreads,
                     if (!(du > 0)) continue;
                     tt = nd / (2.0 * du);
                 } else {
-                    int p = k - P.n, q = p / 2; bool upper = (p % 2 == 0);
-                    double uk = upper ? g[q] : -g[q];
+                    const int p = k - P.n;
+                    double uk = 0;
+                    for (int q = 0; q < d; ++q) uk += P.pn[p][q] * g[q];
                     if (!(uk > 0)) continue;
-                    tt = (upper ? (P.bhi[q] - xi[q]) : (xi[q] - P.blo[q])) / uk;
+                    tt = plane_height(P, p, xi) / uk;
                 }
                 if (tt > 0 && tt < tb) { tb = tt; jb = t; }
             }
@@ -1165,7 +1306,7 @@ int hvo_sample_cells(int d, int64_t n, const double* pts, const double* lo, cons
     Problem P;
     P.d = d; P.n = (int)n; P.seed = seed;
     P.X.assign(pts, pts + (size_t)n * d);
-    for (int k = 0; k < d; ++k) { P.blo[k] = lo[k]; P.bhi[k] = hi[k]; }
+    set_box_planes(P, lo, hi);
     build_tree(P);
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -1192,8 +1333,30 @@ int hvo_sample_cells(int d, int64_t n, const double* pts, const double* lo, cons
     return fail ? -3 : 0;
 }
 
+static int64_t verify_vertices(const Problem& P, const double* pts, int64_t nv, const int64_t* sig,
+                               const double* r, double rel_tol);
+
 int64_t hvo_verify_vertices(int d, int64_t n, const double* pts, const double* lo, const double* hi,
                             int64_t nv, const int64_t* sig, const double* r, double rel_tol) {
+    Problem P;
+    P.d = d; P.n = (int)n;
+    set_box_planes(P, lo, hi);
+    return verify_vertices(P, pts, nv, sig, r, rel_tol);
+}
+
+int64_t hvo_verify_vertices_planes(int d, int64_t n, const double* pts, int np, const double* base,
+                                   const double* normal, int64_t nv, const int64_t* sig, const double* r,
+                                   double rel_tol) {
+    Problem P;
+    P.d = d; P.n = (int)n;
+    if (!set_planes(P, np, base, normal)) return -1;
+    return verify_vertices(P, pts, nv, sig, r, rel_tol);
+}
+
+static int64_t verify_vertices(const Problem& P, const double* pts, int64_t nv, const int64_t* sig,
+                               const double* r, double rel_tol) {
+    const int d = P.d;
+    const int64_t n = P.n;
     int64_t bad = 0;
 #pragma omp parallel for reduction(+ : bad) schedule(static)
     for (int64_t v = 0; v < nv; ++v) {
@@ -1207,14 +1370,14 @@ int64_t hvo_verify_vertices(int d, int64_t n, const double* pts, const double* l
                 double dd = 0;
                 for (int k = 0; k < d; ++k) { double e = pts[it * d + k] - c[k]; dd += e * e; }
                 rmin = std::min(rmin, dd); rmax = std::max(rmax, dd);
+            } else if (it - n < P.np) {
+                if (std::fabs(plane_height(P, (int)(it - n), c)) > 1e-9) ok = false;
             } else {
-                int p = (int)(it - n), k = p / 2;
-                double off = (p % 2 == 0) ? hi[k] - c[k] : c[k] - lo[k];
-                if (std::fabs(off) > 1e-9) ok = false;
+                ok = false;
             }
         }
         if (!(rmax - rmin <= rel_tol * rmax + 1e-300)) ok = false;
-        for (int k = 0; k < d && ok; ++k) if (c[k] < lo[k] - 1e-9 || c[k] > hi[k] + 1e-9) ok = false;
+        for (int p = 0; p < P.np && ok; ++p) if (plane_height(P, p, c) < -1e-9) ok = false;
         for (int64_t j = 0; j < n && ok; ++j) {
             bool in_sig = false;
             for (int q = 0; q <= d; ++q) if (s[q] - 1 == j) in_sig = true;

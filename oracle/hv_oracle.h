@@ -9,7 +9,8 @@
  *
  * Index conventions follow the reference: generators are 1-based, boundary
  * plane p (1-based, cuboid order of src/boundary.jl:518-534: plane 2k-1 is the
- * upper face x_k = hi_k, plane 2k the lower face x_k = lo_k) is generator N+p.
+ * upper face x_k = hi_k, plane 2k the lower face x_k = lo_k; or the p-th plane
+ * given to the *_planes entry points) is generator N+p.
  * Point arrays are d x n column-major (Julia layout), i.e. point i occupies
  * pts[d*i .. d*i+d-1].
  */
@@ -39,6 +40,11 @@ typedef struct {
  * Returns 0 on success, <0 on error. */
 int hvo_build(int d, int64_t n, const double* pts, const double* lo, const double* hi,
               uint64_t seed, int nthreads, int mode, int integrate, hvo_mesh** out);
+/* Same inside the convex domain of np planes (base, normal: d x np column-major;
+ * the domain is (x - base_p) . normal_p < 0 for every p, normals scaled to unit
+ * length). */
+int hvo_build_planes(int d, int64_t n, const double* pts, int np, const double* base, const double* normal,
+                     uint64_t seed, int nthreads, int mode, int integrate, hvo_mesh** out);
 
 int64_t hvo_num_vertices(const hvo_mesh* m);
 int64_t hvo_num_neighbors(const hvo_mesh* m);
@@ -68,6 +74,9 @@ int hvo_sample_cells(int d, int64_t n, const double* pts, const double* lo, cons
  * violating vertices (0 = all verified). */
 int64_t hvo_verify_vertices(int d, int64_t n, const double* pts, const double* lo, const double* hi,
                             int64_t nv, const int64_t* sig, const double* r, double rel_tol);
+int64_t hvo_verify_vertices_planes(int d, int64_t n, const double* pts, int np, const double* base,
+                                   const double* normal, int64_t nv, const int64_t* sig, const double* r,
+                                   double rel_tol);
 
 /* Raw Philox4x32-10 block (for known-answer tests of the generator). */
 void hvo_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

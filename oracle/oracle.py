@@ -53,6 +53,10 @@ def lib():
             ip = ctypes.POINTER(ctypes.c_int64)
             L.hvo_build.argtypes = [I, I64, dp, dp, dp, U64, I, I, I, ctypes.POINTER(P)]
             L.hvo_build.restype = I
+            L.hvo_build_planes.argtypes = [I, I64, dp, I, dp, dp, U64, I, I, I, ctypes.POINTER(P)]
+            L.hvo_build_planes.restype = I
+            L.hvo_verify_vertices_planes.argtypes = [I, I64, dp, I, dp, dp, I64, ip, dp, D]
+            L.hvo_verify_vertices_planes.restype = I64
             L.hvo_num_vertices.argtypes = [P]; L.hvo_num_vertices.restype = I64
             L.hvo_num_neighbors.argtypes = [P]; L.hvo_num_neighbors.restype = I64
             L.hvo_vertices.argtypes = [P, ip, dp]; L.hvo_vertices.restype = None
@@ -84,16 +88,25 @@ def _ip(a):
 class OracleMesh:
     """Result of one oracle mesh build (1-based reference index conventions)."""
 
-    def __init__(self, pts, lo=None, hi=None, seed=0, nthreads=0, mode=0, integrate=False):
+    def __init__(self, pts, lo=None, hi=None, seed=0, nthreads=0, mode=0, integrate=False, planes=None):
+        """Box [lo, hi] (default unit cube), or the convex domain of
+        ``planes = (base, normal)``, (P, d) arrays each."""
         L = lib()
         pts = np.ascontiguousarray(pts, dtype=np.float64)
         self.n, self.d = pts.shape
         self.pts = pts
-        self.lo = np.ascontiguousarray(np.zeros(self.d) if lo is None else lo, dtype=np.float64)
-        self.hi = np.ascontiguousarray(np.ones(self.d) if hi is None else hi, dtype=np.float64)
         h = ctypes.c_void_p()
-        rc = L.hvo_build(self.d, self.n, _dp(pts), _dp(self.lo), _dp(self.hi), seed, nthreads, mode,
-                         1 if integrate else 0, ctypes.byref(h))
+        if planes is not None:
+            base = np.ascontiguousarray(planes[0], dtype=np.float64)
+            normal = np.ascontiguousarray(planes[1], dtype=np.float64)
+            self.lo = self.hi = None
+            rc = L.hvo_build_planes(self.d, self.n, _dp(pts), base.shape[0], _dp(base), _dp(normal), seed,
+                                    nthreads, mode, 1 if integrate else 0, ctypes.byref(h))
+        else:
+            self.lo = np.ascontiguousarray(np.zeros(self.d) if lo is None else lo, dtype=np.float64)
+            self.hi = np.ascontiguousarray(np.ones(self.d) if hi is None else hi, dtype=np.float64)
+            rc = L.hvo_build(self.d, self.n, _dp(pts), _dp(self.lo), _dp(self.hi), seed, nthreads, mode,
+                             1 if integrate else 0, ctypes.byref(h))
         if rc != 0:
             raise RuntimeError(f"oracle build failed ({rc}): {L.hvo_last_error().decode()}")
         self._h = h
@@ -148,10 +161,17 @@ class OracleMesh:
         return {n: getattr(st, n) for n, _ in Stats._fields_}
 
 
-def verify_vertices(pts, sig, r, lo=None, hi=None, rel_tol=1e-9):
+def verify_vertices(pts, sig, r, lo=None, hi=None, rel_tol=1e-9, planes=None):
     """Brute-force empty-sphere check; returns the number of bad vertices."""
     pts = np.ascontiguousarray(pts, dtype=np.float64)
     n, d = pts.shape
+    sig = np.ascontiguousarray(sig, dtype=np.int64)
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    if planes is not None:
+        base = np.ascontiguousarray(planes[0], dtype=np.float64)
+        normal = np.ascontiguousarray(planes[1], dtype=np.float64)
+        return lib().hvo_verify_vertices_planes(d, n, _dp(pts), base.shape[0], _dp(base), _dp(normal),
+                                                sig.shape[0], _ip(sig), _dp(r), rel_tol)
     lo = np.ascontiguousarray(np.zeros(d) if lo is None else lo, dtype=np.float64)
     hi = np.ascontiguousarray(np.ones(d) if hi is None else hi, dtype=np.float64)
     sig = np.ascontiguousarray(sig, dtype=np.int64)

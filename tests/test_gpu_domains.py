@@ -1,0 +1,172 @@
+"""Convex domains given by boundary planes (hv_mesh_build_planes) on the GPU,
+against the CPU oracle and against the box path, through the C ABI.
+
+Bar: signatures and neighbour lists bit-exact against the oracle; coordinates
+within COORD_TOL; VI_POLYGON volumes and areas within POLY_RTOL relative.  A
+box given as axis planes through the plane entry point runs the same exact
+single-coordinate arithmetic as the box entry point, so its mesh is
+bit-identical (coordinates included).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from _domains import points_in_planes, regular_polygon, rotate_points, rotated_cube, simplex, simplex_points
+from hvgpu import datasets as D
+
+pytestmark = pytest.mark.gpu
+
+COORD_TOL = 1e-9
+POLY_RTOL = 1e-10
+
+
+def _planes_mesh(hv, pts, base, normal, bc=None, method=None, **kw):
+    method = hv.HV_METHOD_FAST if method is None else method
+    return hv.Mesh(hv.default_context(), pts, None, None, hv.make_params(method, **kw), planes=(base, normal, bc))
+
+
+def _compare(hv, pts, base, normal, method=None, integrate=False):
+    ref = O.OracleMesh(pts, planes=(base, normal), integrate=integrate)
+    m = _planes_mesh(hv, pts, base, normal, method=method)
+    rs, rr = ref.vertices()
+    s, r = m.vertices()
+    assert s.shape == rs.shape, f"{len(s)} vertices, oracle {len(rs)}"
+    np.testing.assert_array_equal(s, rs)
+    assert np.max(np.abs(r - rr)) < COORD_TOL
+    ro, rn = ref.neighbors()
+    o, nb = m.neighbors()
+    np.testing.assert_array_equal(o, ro)
+    np.testing.assert_array_equal(nb, rn)
+    assert m.stats()["degenerate"] == 0
+    if integrate:
+        rv, ra = ref.polygon()
+        v, a = m.polygon()
+        np.testing.assert_allclose(v, rv, rtol=POLY_RTOL, atol=1e-15)
+        np.testing.assert_allclose(a, ra, rtol=POLY_RTOL, atol=1e-15 * max(1.0, ra.max()))
+    return m
+
+
+@pytest.mark.parametrize("method", ["fast", "plain"])
+@pytest.mark.parametrize("d,n", [(2, 400), (3, 300), (4, 300), (5, 150), (6, 60)])
+def test_simplex_domain(gpu_lib, method, d, n):
+    hv = gpu_lib
+    base, normal, vol = simplex(d)
+    X = simplex_points(d, n, 20 + d)
+    code = hv.HV_METHOD_FAST if method == "fast" else hv.HV_METHOD_PLAIN
+    m = _compare(hv, X, base, normal, method=code, integrate=(method == "fast" and d <= 5))
+    if method == "fast":
+        v, _ = m.polygon()
+        assert abs(v.sum() - vol) < 1e-11 * vol
+
+
+@pytest.mark.parametrize("d,n", [(2, 500), (3, 400), (4, 300), (5, 150)])
+def test_rotated_cube(gpu_lib, d, n):
+    """Rotated points in the rotated cube: the oracle's mesh, and the box mesh
+    of the unrotated points (same signatures, rotated coordinates, volumes)."""
+    hv = gpu_lib
+    X = D.uniform_points(d, n, 30 + d)
+    Q, base, normal = rotated_cube(d, d)
+    Y = rotate_points(Q, X)
+    m = _compare(hv, Y, base, normal, integrate=True)
+    box = hv.Mesh(hv.default_context(), X, np.zeros(d), np.ones(d), hv.make_params(hv.HV_METHOD_FAST))
+    sb, rb = box.vertices()
+    s, r = m.vertices()
+    np.testing.assert_array_equal(s, sb)
+    np.testing.assert_allclose(rotate_points(Q, rb), r, atol=1e-11)
+    np.testing.assert_allclose(m.polygon()[0], box.polygon()[0], rtol=1e-10, atol=1e-15)
+
+
+def test_hexagon(gpu_lib):
+    base, normal, area = regular_polygon(6)
+    X = points_in_planes(base, normal, np.full(2, -1.0), np.full(2, 1.0), 2000, 5)
+    m = _compare(gpu_lib, X, base, normal, integrate=True)
+    assert abs(m.polygon()[0].sum() - area) < 1e-11
+
+
+@pytest.mark.parametrize("d,n", [(3, 2000), (4, 2000)])
+def test_axis_planes_match_the_box_path_bit_for_bit(gpu_lib, d, n):
+    """A box given as axis planes in a shuffled order: same mesh as the box
+    entry point up to the renumbering of the planes, identical coordinates."""
+    hv = gpu_lib
+    lo, hi = np.full(d, -0.5), np.linspace(1.0, 2.0, d)
+    X = lo + (hi - lo) * np.random.default_rng(d).random((n, d))
+    box = hv.Mesh(hv.default_context(), X, lo, hi, hv.make_params(hv.HV_METHOD_FAST))
+    order = np.random.default_rng(99).permutation(2 * d)   # new plane j = box plane order[j]
+    base, normal = [], []
+    for p in order:
+        k = p // 2
+        e = np.zeros(d); e[k] = 3.0                          # unnormalised normals are scaled
+        if p % 2 == 0:
+            b = lo.copy(); b[k] = hi[k]; base.append(b); normal.append(e)
+        else:
+            base.append(lo.copy()); normal.append(-e)
+    m = _planes_mesh(hv, X, np.array(base), np.array(normal), bc=np.zeros(2 * d, dtype=np.int16))
+    sb, rb = box.vertices()
+    s, r = m.vertices()
+    inv = np.empty(2 * d, dtype=np.int64); inv[order] = np.arange(2 * d)
+    sb2 = np.where(sb > n, n + 1 + inv[np.clip(sb - n - 1, 0, 2 * d - 1)], sb)
+    sb2.sort(axis=1)
+    key = np.lexsort(sb2.T[::-1])
+    np.testing.assert_array_equal(s, sb2[key])
+    np.testing.assert_array_equal(r, rb[key])
+
+
+def test_integrators_on_a_simplex(gpu_lib):
+    hv = gpu_lib
+    d = 4
+    base, normal, vol = simplex(d)
+    X = simplex_points(d, 400, 3)
+    m = _planes_mesh(hv, X, base, normal)
+    v, a = m.polygon()
+    assert abs(v.sum() - vol) < 1e-11 * vol
+    ref = O.OracleMesh(X, planes=(base, normal), integrate=True)
+    mv, ma = m.heuristic_mc(2000, 7)
+    rv, ra, vvar, avar = ref.heuristic_mc(2000, 7)
+    assert np.all(np.abs(mv - rv) <= 3 * np.sqrt(np.maximum(vvar, 1e-300)) + 1e-12)
+    np.testing.assert_allclose(mv, rv, rtol=1e-4)
+    close = np.abs(ma - ra) <= 1e-4 * np.abs(ra) + 1e-9
+    assert close.mean() > 0.995
+    assert np.all(np.abs(ma - ra)[~close] <= 3 * np.sqrt(avar[~close]) + 1e-9)
+    assert abs(mv.sum() - vol) < 0.05 * vol
+
+
+def test_plane_domain_errors(gpu_lib):
+    hv = gpu_lib
+    X = np.array([[0.2, 0.2], [0.3, 0.1]])
+    base, normal, _ = simplex(2)
+    with pytest.raises(hv.HVError):   # one plane: unbounded
+        _planes_mesh(hv, X, base[:1], normal[:1])
+    with pytest.raises(hv.HVError):   # x < 0.1 and x > 0.5: empty
+        _planes_mesh(hv, X, np.array([[0.1, 0], [0.5, 0], [0, 0], [0, 1]]),
+                     np.array([[1.0, 0], [-1.0, 0], [0, -1.0], [0, 1.0]]))
+    with pytest.raises(hv.HVError):   # periodic plane code
+        _planes_mesh(hv, X, base, normal, bc=np.array([0, 0, 2], dtype=np.int16))
+    with pytest.raises(hv.HVError):   # a point outside
+        _planes_mesh(hv, np.array([[0.2, 0.2], [0.9, 0.9]]), base, normal)
+    with pytest.raises(hv.HVError):   # zero normal
+        _planes_mesh(hv, X, base, np.array([[0.0, 0.0], [0, -1.0], [1.0, 1.0]]))
+
+
+def test_geometry_api_with_planes(gpu_lib):
+    hv = gpu_lib
+    base, normal, area = regular_polygon(5, r=2.0)
+    b = hv.Boundary(*[hv.BC_Dirichlet(base[j], normal[j]) for j in range(5)])
+    X = points_in_planes(base, normal, np.full(2, -2.0), np.full(2, 2.0), 500, 1)
+    g = hv.VoronoiGeometry(X, b, integrator=hv.VI_POLYGON)
+    vd = hv.VoronoiData(g)
+    assert abs(vd.volume.sum() - area) < 1e-10
+    assert all(x in b for x in X[:20])
+
+
+def test_device_points_with_planes(gpu_lib):
+    torch = pytest.importorskip("torch")
+    hv = gpu_lib
+    base, normal, _ = simplex(3)
+    X = simplex_points(3, 500, 9)
+    t = torch.from_numpy(X).to("cuda:0")
+    torch.cuda.synchronize()
+    m = hv.Mesh(hv.default_context(), np.array(X.shape), None, None, hv.make_params(hv.HV_METHOD_FAST),
+                device_ptr=t.data_ptr(), planes=(base, normal, None))
+    h = _planes_mesh(hv, X, base, normal)
+    np.testing.assert_array_equal(m.vertices()[0], h.vertices()[0])
+    np.testing.assert_array_equal(m.vertices()[1], h.vertices()[1])

@@ -166,3 +166,57 @@ def test_sample_cells_counts_owned_vertices():
     assert own == len(sig)
     assert rays > own and sec > 0
     assert math.isfinite(sec)
+
+
+# ---- convex domains given by planes (Boundary(planes...), src/boundary.jl:94-131)
+
+@pytest.mark.parametrize("d,n", [(2, 300), (3, 300), (4, 200), (5, 100)])
+def test_rotated_cube_has_the_box_mesh(d, n):
+    """A rigid motion of points and cube leaves the mesh unchanged: the same
+    signatures (plane 2k = image of the box's plane 2k), coordinates moved by
+    the rotation, the same volumes."""
+    from _domains import rotate_points, rotated_cube
+    X = D.uniform_points(d, n, 10 + d)
+    Q, base, normal = rotated_cube(d, d)
+    A = O.OracleMesh(X, integrate=True)
+    B = O.OracleMesh(rotate_points(Q, X), planes=(base, normal), integrate=True)
+    sa, ra = A.vertices()
+    sb, rb = B.vertices()
+    np.testing.assert_array_equal(sa, sb)
+    np.testing.assert_allclose(rotate_points(Q, ra), rb, atol=1e-12)
+    va, _ = A.polygon()
+    vb, _ = B.polygon()
+    np.testing.assert_allclose(va, vb, rtol=1e-10, atol=1e-15)
+    assert O.verify_vertices(B.pts, sb, rb, planes=(base, normal)) == 0
+
+
+@pytest.mark.parametrize("d,n", [(2, 200), (3, 200), (4, 200), (5, 100), (6, 40)])
+def test_simplex_domain_volume(d, n):
+    from _domains import simplex, simplex_points
+    base, normal, vol = simplex(d)
+    X = simplex_points(d, n, d)
+    m = O.OracleMesh(X, planes=(base, normal), integrate=True)
+    s, r = m.vertices()
+    assert O.verify_vertices(X, s, r, planes=(base, normal)) == 0
+    v, _ = m.polygon()
+    assert abs(v.sum() - vol) < 1e-12 * max(1.0, vol) + 1e-15
+    assert m.stats()["degenerate"] == 0
+
+
+def test_hexagon_area_and_plane_ids():
+    from _domains import points_in_planes, regular_polygon
+    base, normal, area = regular_polygon(6)
+    X = points_in_planes(base, normal, np.full(2, -1.0), np.full(2, 1.0), 400, 7)
+    m = O.OracleMesh(X, planes=(base, normal), integrate=True)
+    v, _ = m.polygon()
+    assert abs(v.sum() - area) < 1e-12
+    s, _ = m.vertices()
+    planes_used = np.unique(s[s > len(X)]) - len(X)
+    np.testing.assert_array_equal(planes_used, np.arange(1, 7))
+
+
+def test_points_outside_planes_are_rejected():
+    from _domains import simplex
+    base, normal, _ = simplex(3)
+    with pytest.raises(RuntimeError):
+        O.OracleMesh(np.array([[0.2, 0.2, 0.2], [0.5, 0.5, 0.5]]), planes=(base, normal))
