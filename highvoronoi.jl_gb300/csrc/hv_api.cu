@@ -248,6 +248,14 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     M.xscale = xs;
     M.np = mesh->np;
     M.planes = mesh->d_planes;
+    M.box = mesh->np == 2 * d;
+    for (int p = 0; p < mesh->np && M.box; ++p)
+        M.box = mesh->planes[p].axis == p / 2 && mesh->planes[p].sgn == ((p & 1) == 0 ? 1 : -1);
+    if (M.box)
+        for (int k = 0; k < d; ++k) {
+            M.lo32[k] = (float)(-mesh->planes[2 * k + 1].off);
+            M.hi32[k] = (float)mesh->planes[2 * k].off;
+        }
     M.xs32 = (float)xs;
     M.tiny32 = (float)(4e-14 * xs);
     M.e13_32 = (float)(1e-13 * xs);

@@ -91,7 +91,9 @@ struct DevMesh {
     double xscale;  // bound on |coordinate|
     int np;                   // boundary planes, generator ids n .. n+np-1
     const DevPlane* planes;   // np entries
+    int box;                  // planes are the cuboid faces 2k (x_k <= hi_k), 2k+1 (x_k >= lo_k)
     // FP32 copies for the FP32 kernels (rounded once on the host)
+    float lo32[HV_MAXD], hi32[HV_MAXD];  // the cuboid's bounds when box
     float xs32;      // (float)xscale
     float tiny32;    // (float)(4e-14 xscale)
     float e13_32;    // (float)(1e-13 xscale)

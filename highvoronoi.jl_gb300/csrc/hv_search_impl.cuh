@@ -985,6 +985,23 @@ __global__ void __launch_bounds__(128) k_centers(DevMesh M, unsigned v0, unsigne
 // from the plane.  Cuboid faces use the single coordinate; other planes bound
 // the rounding of the split coordinates, of the FP32 copies of n and off and of
 // the dot products.
+// Parameter interval [lo, hi] of the crossing num / uk given the absolute
+// error bounds of both; false if the ray moves away from the plane.
+__device__ __forceinline__ bool crossing32(float num, float e_num, float uk, float e_den, float& lo, float& hi) {
+    const float S32 = 5.9604645e-08f;
+    if (uk > e_den) {
+        const float t = __fdividef(num, uk);
+        const float et = __fdividef(e_num + fabsf(t) * e_den, uk - e_den) * 1.00001f + 8.f * S32 * fabsf(t);
+        lo = t - et; hi = t + et;
+    } else if (uk < -e_den) {
+        return false;
+    } else {
+        if (num - e_num > 0.f) { lo = __fdividef(num - e_num, fabsf(uk) + e_den) * 0.99999f; hi = INFINITY; }
+        else { lo = -INFINITY; hi = INFINITY; }
+    }
+    return true;
+}
+
 template <int D>
 __device__ __forceinline__ bool plane32(const DevPlane& P, const float* xa, const float* xal, const float* rho,
                                         const float* u, float erho, float relu, float TINY, float& lo, float& hi) {
@@ -1018,17 +1035,50 @@ __device__ __forceinline__ bool plane32(const DevPlane& P, const float* xa, cons
         e_num = (2.f * D + 8.f) * S32 * (fabsf(P.off32) + anc) + erho * an + TINY;
         e_den = relu * an + (D + 4.f) * S32 * anu;
     }
-    if (uk > e_den) {
-        const float t = __fdividef(num, uk);
-        const float et = __fdividef(e_num + fabsf(t) * e_den, uk - e_den) * 1.00001f + 8.f * S32 * fabsf(t);
-        lo = t - et; hi = t + et;
-    } else if (uk < -e_den) {
-        return false;
+    return crossing32(num, e_num, uk, e_den, lo, hi);
+}
+
+// Cuboid face p (2k upper, 2k+1 lower) with p known at compile time after
+// unrolling: one coordinate, bounds from the kernel parameters.
+template <int D>
+__device__ __forceinline__ bool box32(const DevMesh& M, int p, const float* xa, const float* xal, const float* rho,
+                                      const float* u, float erho, float relu, float TINY, float& lo, float& hi) {
+    const float S32 = 5.9604645e-08f;
+    const int k = p >> 1;
+    const bool upper = (p & 1) == 0;
+    const float uk = upper ? u[k] : -u[k];
+    const float hk = M.hi32[k], lk = M.lo32[k];
+    const float ck = xa[k] + (xal[k] + rho[k]);
+    const float num = upper ? (hk - ck) : (ck - lk);
+    const float e_num = 4.f * S32 * (fabsf(hk) + fabsf(lk) + fabsf(xa[k]) + fabsf(rho[k])) + erho + TINY;
+    const float e_den = relu + 2.f * S32 * fabsf(uk);
+    return crossing32(num, e_num, uk, e_den, lo, hi);
+}
+
+// Visits every boundary plane not excluded by excl(item) whose FP32 crossing
+// interval exists: f(item, lo, hi).  Cuboid domains unroll over their 2D faces.
+template <int D, class Excl, class F>
+__device__ __forceinline__ void planes32(const DevMesh& M, const float* xa, const float* xal, const float* rho,
+                                         const float* u, float erho, float relu, float TINY, Excl&& excl, F&& f) {
+    if (M.box) {
+#pragma unroll
+        for (int p = 0; p < 2 * D; ++p) {
+            const int it = M.n + p;
+            if (excl(it)) continue;
+            float lo, hi;
+            if (!box32<D>(M, p, xa, xal, rho, u, erho, relu, TINY, lo, hi)) continue;
+            f(it, lo, hi);
+        }
     } else {
-        if (num - e_num > 0.f) { lo = __fdividef(num - e_num, fabsf(uk) + e_den) * 0.99999f; hi = INFINITY; }
-        else { lo = -INFINITY; hi = INFINITY; }
+#pragma unroll 1
+        for (int p = 0; p < M.np; ++p) {
+            const int it = M.n + p;
+            if (excl(it)) continue;
+            float lo, hi;
+            if (!plane32<D>(M.planes[p], xa, xal, rho, u, erho, relu, TINY, lo, hi)) continue;
+            f(it, lo, hi);
+        }
     }
-    return true;
 }
 
 constexpr int FAST_WPB = 4;  // warps per block
@@ -1285,18 +1335,18 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 6) k_expand_fast(DevMesh M, uns
             // boundary planes in FP32 with the same error model
             float plo1 = INFINITY, phi1 = INFINITY, plo2 = INFINITY;
             int pj1 = -1;
-#pragma unroll 1
-            for (int p = 0; p < M.np; ++p) {
-                const int it = M.n + p;
-                bool ex = false;
+            planes32<D>(
+                M, xa, xal, rho, u, erho, relu, TINY,
+                [&](int it) {
+                    bool ex = false;
 #pragma unroll
-                for (int s = 0; s < R; ++s) ex |= (sig[s] == it);
-                if (ex) continue;
-                float lo, hi;
-                if (!plane32<D>(M.planes[p], xa, xal, rho, u, erho, relu, TINY, lo, hi)) continue;
-                if (lo < plo1) { plo2 = plo1; plo1 = lo; phi1 = hi; pj1 = it; }
-                else if (lo < plo2) plo2 = lo;
-            }
+                    for (int s = 0; s < R; ++s) ex |= (sig[s] == it);
+                    return ex;
+                },
+                [&](int it, float lo, float hi) {
+                    if (lo < plo1) { plo2 = plo1; plo1 = lo; phi1 = hi; pj1 = it; }
+                    else if (lo < plo2) plo2 = lo;
+                });
             int win;
             float blo, bhi, second;
             if (cj1 >= 0 && clo1 <= plo1) { win = cj1; blo = clo1; bhi = chi1; second = fminf(clo2, plo1); }
@@ -1599,17 +1649,15 @@ __global__ void __launch_bounds__(FB_WPB * 32, 4) k_fallback_warp(DevMesh M, con
         // planes (lane 0)
         if (lane == 0) {
             const float TINY = M.tiny32;
+            planes32<D>(
+                M, xa, xal, rho, u, erho, relu, TINY,
+                [&](int it) {
+                    bool ex = false;
 #pragma unroll
-            for (int p = 0; p < M.np; ++p) {
-                const int it = M.n + p;
-                bool ex = false;
-#pragma unroll
-                for (int q = 0; q < R; ++q) ex |= (sig[q] == it);
-                if (ex) continue;
-                float lo, hi;
-                if (!plane32<D>(M.planes[p], xa, xal, rho, u, erho, relu, TINY, lo, hi)) continue;
-                take(it, lo, hi);
-            }
+                    for (int q = 0; q < R; ++q) ex |= (sig[q] == it);
+                    return ex;
+                },
+                [&](int it, float lo, float hi) { take(it, lo, hi); });
         }
         // the candidate list
         if (M.K > 0) {
@@ -2016,18 +2064,18 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_descent_warp(DevMesh M, int str
             // planes (lane 0)
             if (lane == 0) {
                 const float TINY = M.tiny32;
+                planes32<D>(
+                    M, xa, xal, rho, u, erho, relu, TINY,
+                    [&](int it) {
+                        bool ex = false;
 #pragma unroll
-                for (int p = 0; p < M.np; ++p) {
-                    const int it = M.n + p;
-                    bool ex = false;
-#pragma unroll
-                    for (int q = 0; q <= D; ++q) ex |= (T[q] == it);
-                    if (ex) continue;
-                    float lo, hi;
-                    if (!plane32<D>(M.planes[p], xa, xal, rho, u, erho, relu, TINY, lo, hi)) continue;
-                    H = fminf(H, hi);
-                    top2_add(lo1, hi1, j1, lo2, lo, hi, it);
-                }
+                        for (int q = 0; q <= D; ++q) ex |= (T[q] == it);
+                        return ex;
+                    },
+                    [&](int it, float lo, float hi) {
+                        H = fminf(H, hi);
+                        top2_add(lo1, hi1, j1, lo2, lo, hi, it);
+                    });
             }
             const int* lst = M.knn + (size_t)i * M.K;
             for (int c = lane; c < M.K; c += 32) {
