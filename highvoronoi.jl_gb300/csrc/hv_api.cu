@@ -26,6 +26,7 @@
 #include "hv_host.h"
 #include "hv_integrate.h"
 #include "hv_internal.cuh"
+#include "hv_periodic.h"
 #include "hvgpu.h"
 
 struct hv_ctx {
@@ -57,6 +58,16 @@ struct hv_mesh {
     int* nbr = nullptr;
     long long nnbr = -1;
     hv_stats st;
+    // periodic cuboid: the public view above is reduced from the mesh of the
+    // generators and their images in the widened box
+    int pmask = 0;
+    hv_mesh* ext = nullptr;
+    int nimg = 0;
+    double delta[HV_MAXD] = {};
+    int* img_ref = nullptr;            // nimg originals
+    short* img_code = nullptr;         // nimg shift codes sum (s_k + 1) 3^k
+    signed char* pshift = nullptr;     // nnbr x d lattice shifts of the neighbours
+    int* pperm = nullptr;              // nnbr: position in the extended row
 };
 
 namespace {
@@ -607,6 +618,157 @@ int build_entry(hv_ctx* ctx, int d, int64_t n, const double* src, bool on_device
     return HV_OK;
 }
 
+// Periodic cuboid [lo, hi] with periodic axes pmask.  The margin starts at
+// 1.5 mean spacings and grows by 1.5 until every vertex of an original cell is
+// certified (at most 0.999 of a side).
+int periodic_entry(hv_ctx* ctx, int d, int64_t n, const double* src, bool on_device, const double* lo,
+                   const double* hi, int pmask, const hv_params* params, hv_mesh** out) {
+    using namespace hv;
+    int rc = validate_common(ctx, d, n, lo, hi, out);
+    if (rc != HV_OK) return rc;
+    if (n > 0 && !src) { ctx->err = "null point array"; return HV_E_INVALID_ARG; }
+    if (n < 1) { ctx->err = "a periodic mesh needs at least one generator"; return HV_E_INVALID_ARG; }
+    std::unique_ptr<hv_mesh> mp(new hv_mesh());
+    hv_mesh* m = mp.get();
+    m->ctx = ctx; m->d = d; m->n = (int)n; m->pmask = pmask;
+    for (int k = 0; k < d; ++k) { m->lo[k] = lo[k]; m->hi[k] = hi[k]; }
+    m->np = 2 * d;
+    box_planes(d, lo, hi, m->planes);
+    if (params) m->prm = *params; else hv_params_default(&m->prm);
+    try {
+        CK(cudaSetDevice(ctx->device));
+        cudaStream_t st = ctx->stream;
+        m->d_in = dalloc<double>(st, (size_t)n * d);
+        CK(cudaMemcpyAsync(m->d_in, src, sizeof(double) * n * d,
+                           on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+        m->d_planes = dalloc<DevPlane>(st, (size_t)m->np);
+        CK(cudaMemcpyAsync(m->d_planes, m->planes, sizeof(DevPlane) * m->np, cudaMemcpyHostToDevice, st));
+        PerBox B{};
+        B.d = d; B.pmask = pmask;
+        double vol = 1.0, scale = 0.0;
+        for (int k = 0; k < d; ++k) {
+            B.lo[k] = lo[k]; B.hi[k] = hi[k]; B.L[k] = hi[k] - lo[k];
+            vol *= B.L[k];
+        }
+        const double spacing = std::pow(vol / (double)n, 1.0 / d);
+        double grow = 1.5;
+        Scratch ps(st);
+        unsigned* dbad = ps.get<unsigned>(2);
+        CK(cudaMemsetAsync(dbad, 0, 2 * sizeof(unsigned), st));
+        launch_in_box(B, m->d_in, (int)n, dbad, st);
+        unsigned hb[2] = {0, 0};
+        CK(cudaMemcpyAsync(hb, dbad, sizeof(hb), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (hb[0]) throw HvError(HV_E_INVALID_ARG, "points must lie strictly inside the box and be finite");
+        long long* cnt = ps.get<long long>((size_t)n + 1);
+        long long* off = ps.get<long long>((size_t)n + 1);
+        size_t stb = scan_temp((int)n + 1);
+        void* stmp = ps.get<char>(stb);
+        for (int attempt = 0;; ++attempt) {
+            bool capped = true;
+            scale = 0.0;
+            for (int k = 0; k < d; ++k) {
+                B.delta[k] = 0.0;
+                if ((pmask >> k) & 1) {
+                    B.delta[k] = std::min(grow * spacing, 0.999 * B.L[k]);
+                    capped &= B.delta[k] >= 0.999 * B.L[k];
+                }
+                scale = std::max(scale, std::max(std::fabs(lo[k] - B.delta[k]), std::fabs(hi[k] + B.delta[k])));
+            }
+            B.scale = scale;
+            CK(cudaMemsetAsync(cnt, 0, sizeof(long long) * (n + 1), st));
+            launch_img_count(B, m->d_in, (int)n, cnt, st);
+            exclusive_scan_i64(stmp, stb, cnt, off, (int)n + 1, st);
+            long long nimg = 0;
+            CK(cudaMemcpyAsync(&nimg, off + n, sizeof(long long), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (n + nimg > (1ll << 30)) throw HvError(HV_E_CAPACITY, "too many periodic images");
+            const long long n_ext = n + nimg;
+            dfree(st, m->img_ref); dfree(st, m->img_code);
+            m->img_ref = dalloc<int>(st, (size_t)std::max(nimg, 1ll));
+            m->img_code = dalloc<short>(st, (size_t)std::max(nimg, 1ll));
+            Scratch es(st);
+            double* ext_pts = es.get<double>((size_t)n_ext * d);
+            CK(cudaMemcpyAsync(ext_pts, m->d_in, sizeof(double) * n * d, cudaMemcpyDeviceToDevice, st));
+            launch_img_fill(B, m->d_in, (int)n, off, ext_pts, m->img_ref, m->img_code, st);
+            CK(cudaGetLastError());
+            double elo[HV_MAXD], ehi[HV_MAXD];
+            for (int k = 0; k < d; ++k) { elo[k] = lo[k] - B.delta[k]; ehi[k] = hi[k] + B.delta[k]; }
+            DomainSpec dom;
+            dom.lo = elo; dom.hi = ehi;
+            hv_mesh* ext = nullptr;
+            int r = build_entry(ctx, d, n_ext, ext_pts, true, dom, &m->prm, &ext);
+            if (r != HV_OK) throw HvError(r, ctx->err);
+            ensure_neighbors(ext);
+            CK(cudaMemsetAsync(dbad, 0, sizeof(unsigned), st));
+            launch_per_validate(B, ext->osig, ext->oc, ext->V, (int)n, (int)n_ext, ext->d_in, dbad, st);
+            CK(cudaMemcpyAsync(hb, dbad, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (hb[0] == 0) {
+                m->ext = ext;
+                m->nimg = (int)nimg;
+                for (int k = 0; k < d; ++k) m->delta[k] = B.delta[k];
+                break;
+            }
+            hv_mesh_free(ext);
+            if (capped || attempt >= 12)
+                throw HvError(HV_E_CAPACITY, "too few generators for the periodic image margin");
+            grow *= 1.5;
+        }
+        // the public view
+        hv_mesh* e = m->ext;
+        const int n_ext = e->n;
+        const unsigned Ve = e->V;
+        {
+            Scratch vs(st);
+            long long* flag = vs.get<long long>((size_t)Ve + 1);
+            long long* pos = vs.get<long long>((size_t)Ve + 1);
+            int* ext2pub = vs.get<int>((size_t)std::max(Ve, 1u));
+            launch_pub_flag(d, e->osig, Ve, (int)n, flag, st);
+            size_t tb = scan_temp((int)Ve + 1);
+            void* tmp = vs.get<char>(tb);
+            exclusive_scan_i64(tmp, tb, flag, pos, (int)Ve + 1, st);
+            long long Vp = 0;
+            CK(cudaMemcpyAsync(&Vp, pos + Ve, sizeof(long long), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            m->V = (unsigned)Vp;
+            m->osig = dalloc<int>(st, (size_t)std::max(Vp, 1ll) * (d + 1));
+            m->oc = dalloc<double>(st, (size_t)std::max(Vp, 1ll) * d);
+            launch_pub_fill(d, e->osig, e->oc, Ve, (int)n, n_ext, m->img_ref, m->img_code, pos, m->osig, m->oc,
+                            ext2pub, st);
+            long long tot = 0, ninc = 0;
+            CK(cudaMemcpyAsync(&tot, e->nbr_off + n, sizeof(long long), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(&ninc, e->inc_off + n, sizeof(long long), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            m->nbr_off = dalloc<long long>(st, (size_t)n + 1);
+            m->inc_off = dalloc<long long>(st, (size_t)n + 1);
+            CK(cudaMemcpyAsync(m->nbr_off, e->nbr_off, sizeof(long long) * (n + 1), cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(m->inc_off, e->inc_off, sizeof(long long) * (n + 1), cudaMemcpyDeviceToDevice, st));
+            m->nbr = dalloc<int>(st, (size_t)std::max(tot, 1ll));
+            m->pshift = dalloc<signed char>(st, (size_t)std::max(tot, 1ll) * d);
+            m->pperm = dalloc<int>(st, (size_t)std::max(tot, 1ll));
+            launch_pub_nbr(d, (int)n, n_ext, e->nbr_off, e->nbr, m->img_ref, m->img_code, m->nbr, m->pshift,
+                           m->pperm, st);
+            m->inc = dalloc<int>(st, (size_t)std::max(ninc, 1ll));
+            launch_pub_inc(ninc, e->inc, ext2pub, m->inc, st);
+            CK(cudaGetLastError());
+            CK(cudaStreamSynchronize(st));
+            m->nnbr = tot;
+        }
+        m->st = e->st;
+        m->st.vertices = m->V;
+    } catch (const HvError& e) {
+        hv_mesh_free(mp.release());
+        return fail(ctx, e);
+    } catch (const std::bad_alloc&) {
+        hv_mesh_free(mp.release());
+        ctx->err = "host allocation failed";
+        return HV_E_OOM;
+    }
+    *out = mp.release();
+    return HV_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -796,8 +958,60 @@ int hv_mesh_neighbors(hv_mesh* m, int64_t* offs, int64_t* nbr) {
     return HV_OK;
 }
 
-int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) {
+}  // extern "C"
+
+namespace {
+
+// VI_POLYGON; vol/area are host arrays, or (dev_out) device arrays that receive
+// the results in place, stream-ordered on the context's stream.
+int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out);
+int mc_impl(hv_mesh* m, int ndir, uint64_t seed, double* vol, double* area, bool dev_out);
+
+// A periodic mesh integrates its extended mesh and gathers the original cells:
+// volumes are the first n, areas follow the public neighbour order.
+template <class F>
+int periodic_integrate(hv_mesh* m, double* vol, double* area, bool dev_out, F&& run_ext) {
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        cudaStream_t st = m->ctx->stream;
+        hv_mesh* e = m->ext;
+        long long ne = 0;
+        CK(cudaMemcpyAsync(&ne, e->nbr_off + e->n, sizeof(long long), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        Scratch s(st);
+        double* evol = s.get<double>((size_t)e->n);
+        double* earea = s.get<double>((size_t)std::max(ne, 1ll));
+        int r = run_ext(e, evol, earea);
+        if (r != HV_OK) { m->ctx->err = e->ctx->err; return r; }
+        double* pvol = dev_out ? vol : s.get<double>((size_t)m->n);
+        double* parea = dev_out ? area : s.get<double>((size_t)std::max(m->nnbr, 1ll));
+        CK(cudaMemcpyAsync(pvol, evol, sizeof(double) * m->n, cudaMemcpyDeviceToDevice, st));
+        if (m->nnbr > 0) hv::launch_pub_area(m->n, m->nbr_off, m->pperm, earea, parea, st);
+        if (!dev_out) {
+            CK(cudaMemcpyAsync(vol, pvol, sizeof(double) * m->n, cudaMemcpyDeviceToHost, st));
+            if (m->nnbr > 0) CK(cudaMemcpyAsync(area, parea, sizeof(double) * m->nnbr, cudaMemcpyDeviceToHost, st));
+        }
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(st));
+        m->st.poly_big_facets = e->st.poly_big_facets;
+        m->st.ms_poly_incidence = e->st.ms_poly_incidence;
+        m->st.ms_poly_facets = e->st.ms_poly_facets;
+        m->st.ms_poly_big = e->st.ms_poly_big;
+        m->st.ms_poly_total = e->st.ms_poly_total;
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
+int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out) {
     if (!m || (m->n > 0 && !vol)) return HV_E_INVALID_ARG;
+    if (m->ext) {
+        if (m->nnbr > 0 && !area) return HV_E_INVALID_ARG;
+        return periodic_integrate(m, vol, area, dev_out, [&](hv_mesh* e, double* ev, double* ea) {
+            return polygon_impl(e, ev, ea, true);
+        });
+    }
     try {
         CK(cudaSetDevice(m->ctx->device));
         ensure_neighbors(m);
@@ -818,8 +1032,8 @@ int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) {
         long long* foff = s.get<long long>((size_t)ns + 1);
         R.foff = foff;
         R.slot_cell = s.get<int>((size_t)std::max(ns, 1ll));
-        R.area = s.get<double>((size_t)std::max(ns, 1ll));
-        R.vol = s.get<double>(n);
+        R.area = dev_out && ns > 0 ? area : s.get<double>((size_t)std::max(ns, 1ll));
+        R.vol = dev_out ? vol : s.get<double>(n);
         // status, big facets (count, largest vertex count), huge facets (count, largest vertex count)
         unsigned* dstat = s.get<unsigned>(8);
         R.status = dstat; R.nbig = dstat + 1; R.maxnv = dstat + 2; R.nbig2 = dstat + 3; R.maxnv2 = dstat + 4;
@@ -902,8 +1116,10 @@ int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) {
             }
         }
         run(4);
-        CK(cudaMemcpyAsync(vol, R.vol, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
-        if (ns > 0) CK(cudaMemcpyAsync(area, R.area, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+        if (!dev_out) {
+            CK(cudaMemcpyAsync(vol, R.vol, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+            if (ns > 0) CK(cudaMemcpyAsync(area, R.area, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+        }
         CK(cudaStreamSynchronize(st));
         double fam[F_N];
         kt.totals(fam);
@@ -919,8 +1135,14 @@ int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) {
     return HV_OK;
 }
 
-int hv_integrate_heuristic_mc(hv_mesh* m, int ndir, uint64_t seed, double* vol, double* area) {
+int mc_impl(hv_mesh* m, int ndir, uint64_t seed, double* vol, double* area, bool dev_out) {
     if (!m || ndir <= 0 || (m->n > 0 && !vol)) return HV_E_INVALID_ARG;
+    if (m->ext) {
+        if (m->nnbr > 0 && !area) return HV_E_INVALID_ARG;
+        return periodic_integrate(m, vol, area, dev_out, [&](hv_mesh* e, double* ev, double* ea) {
+            return mc_impl(e, ndir, seed, ev, ea, true);
+        });
+    }
     try {
         CK(cudaSetDevice(m->ctx->device));
         ensure_neighbors(m);
@@ -942,9 +1164,9 @@ int hv_integrate_heuristic_mc(hv_mesh* m, int ndir, uint64_t seed, double* vol, 
         const size_t E = (size_t)std::max(m->nnbr, 1ll);
         double* rawV = s.get<double>(n);
         double* varV = s.get<double>(n);
-        double* dvol = s.get<double>(n);
+        double* dvol = dev_out ? vol : s.get<double>(n);
         double* rawA = s.get<double>(E);
-        double* outA = s.get<double>(E);
+        double* outA = dev_out && m->nnbr > 0 ? area : s.get<double>(E);
         unsigned* dstat = s.get<unsigned>(1);
         CK(cudaMemsetAsync(dstat, 0, sizeof(unsigned), st));
         hv::IntegrateInput in{d, n, m->lo, m->hi, m->np, m->d_planes, m->d_in, m->osig, m->oc, m->inc_off, m->inc, m->nbr_off, m->nbr, dstat};
@@ -954,10 +1176,143 @@ int hv_integrate_heuristic_mc(hv_mesh* m, int ndir, uint64_t seed, double* vol, 
         CK(cudaGetLastError());
         unsigned hs = 0;
         CK(cudaMemcpyAsync(&hs, dstat, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(vol, dvol, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
-        if (m->nnbr > 0) CK(cudaMemcpyAsync(area, outA, sizeof(double) * m->nnbr, cudaMemcpyDeviceToHost, st));
+        if (!dev_out) {
+            CK(cudaMemcpyAsync(vol, dvol, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+            if (m->nnbr > 0) CK(cudaMemcpyAsync(area, outA, sizeof(double) * m->nnbr, cudaMemcpyDeviceToHost, st));
+        }
         CK(cudaStreamSynchronize(st));
         if (hs) throw HvError(HV_E_CAPACITY, "cell degree beyond the MC integrator's capacity");
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) { return polygon_impl(m, vol, area, false); }
+
+int hv_integrate_polygon_device(hv_mesh* m, double* d_vol, double* d_area) {
+    return polygon_impl(m, d_vol, d_area, true);
+}
+
+int hv_integrate_heuristic_mc(hv_mesh* m, int ndir, uint64_t seed, double* vol, double* area) {
+    return mc_impl(m, ndir, seed, vol, area, false);
+}
+
+int hv_integrate_heuristic_mc_device(hv_mesh* m, int ndir, uint64_t seed, double* d_vol, double* d_area) {
+    return mc_impl(m, ndir, seed, d_vol, d_area, true);
+}
+
+int hv_mesh_build_periodic(hv_ctx* ctx, int d, int64_t n, const double* pts, const double* lo, const double* hi,
+                           const int* periodic, const hv_params* params, hv_mesh** out) {
+    if (!ctx || !periodic || d < 2 || d > HV_MAXD) return HV_E_INVALID_ARG;
+    int pmask = 0;
+    for (int k = 0; k < d; ++k) pmask |= (periodic[k] ? 1 : 0) << k;
+    if (!pmask) return hv_mesh_build(ctx, d, n, pts, lo, hi, params, out);
+    return periodic_entry(ctx, d, n, pts, false, lo, hi, pmask, params, out);
+}
+
+int hv_mesh_build_periodic_device(hv_ctx* ctx, int d, int64_t n, const double* d_pts, const double* lo,
+                                  const double* hi, const int* periodic, const hv_params* params, hv_mesh** out) {
+    if (!ctx || !periodic || d < 2 || d > HV_MAXD) return HV_E_INVALID_ARG;
+    int pmask = 0;
+    for (int k = 0; k < d; ++k) pmask |= (periodic[k] ? 1 : 0) << k;
+    if (!pmask) return hv_mesh_build_device(ctx, d, n, d_pts, lo, hi, params, out);
+    return periodic_entry(ctx, d, n, d_pts, true, lo, hi, pmask, params, out);
+}
+
+int hv_mesh_periodic_shifts(hv_mesh* m, int8_t* shift) {
+    if (!m || !shift) return HV_E_INVALID_ARG;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        ensure_neighbors(m);
+        if (m->nnbr <= 0) return HV_OK;
+        if (!m->pshift) {
+            std::memset(shift, 0, (size_t)m->nnbr * m->d);
+            return HV_OK;
+        }
+        CK(cudaMemcpyAsync(shift, m->pshift, (size_t)m->nnbr * m->d, cudaMemcpyDeviceToHost, m->ctx->stream));
+        CK(cudaStreamSynchronize(m->ctx->stream));
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
+int hv_mesh_periodic_images(hv_mesh* m, int64_t* nimages, double* delta, int64_t* ref, int8_t* shift) {
+    if (!m || !nimages) return HV_E_INVALID_ARG;
+    *nimages = m->nimg;
+    if (delta)
+        for (int k = 0; k < m->d; ++k) delta[k] = m->delta[k];
+    if (m->nimg == 0 || (!ref && !shift)) return HV_OK;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        std::vector<int> r(m->nimg);
+        std::vector<short> c(m->nimg);
+        CK(cudaMemcpyAsync(r.data(), m->img_ref, sizeof(int) * m->nimg, cudaMemcpyDeviceToHost, m->ctx->stream));
+        CK(cudaMemcpyAsync(c.data(), m->img_code, sizeof(short) * m->nimg, cudaMemcpyDeviceToHost, m->ctx->stream));
+        CK(cudaStreamSynchronize(m->ctx->stream));
+        for (int i = 0; i < m->nimg; ++i) {
+            if (ref) ref[i] = (int64_t)r[i] + 1;
+            int code = c[i];
+            for (int k = 0; k < m->d; ++k) {
+                if (shift) shift[(size_t)i * m->d + k] = (int8_t)(code % 3 - 1);
+                code /= 3;
+            }
+        }
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
+int hv_mesh_cell_vertices(hv_mesh* m, int64_t* offs, int64_t* vtx) {
+    if (!m || !offs) return HV_E_INVALID_ARG;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        ensure_neighbors(m);
+        cudaStream_t st = m->ctx->stream;
+        CK(cudaMemcpyAsync(offs, m->inc_off, sizeof(int64_t) * (m->n + 1), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        const long long tot = offs[m->n];
+        if (vtx && tot > 0) {
+            Scratch s(st);
+            int64_t* dv = s.get<int64_t>((size_t)tot);
+            hv::launch_out_nbr(tot, m->inc, dv, st);  // 1-based vertex rows
+            CK(cudaMemcpyAsync(vtx, dv, sizeof(int64_t) * tot, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+        }
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
+int hv_mesh_device_views(hv_mesh* m, hv_device_views* out) {
+    if (!m || !out) return HV_E_INVALID_ARG;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        ensure_neighbors(m);
+        cudaStream_t st = m->ctx->stream;
+        long long ninc = 0;
+        CK(cudaMemcpyAsync(&ninc, m->inc_off + m->n, sizeof(long long), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        out->d = m->d;
+        out->n = m->n;
+        out->nverts = m->V;
+        out->nnbr = m->nnbr;
+        out->ncell_vertices = ninc;
+        out->sig = m->osig;
+        out->r = m->oc;
+        out->nbr_off = (const int64_t*)m->nbr_off;
+        out->nbr = m->nbr;
+        out->vtx_off = (const int64_t*)m->inc_off;
+        out->vtx = m->inc;
+        out->pts = m->d_in;
+        out->stream = (void*)st;
     } catch (const HvError& e) {
         return fail(m->ctx, e);
     }
@@ -982,7 +1337,12 @@ int hv_mesh_free(hv_mesh* m) {
     dfree(st, m->inc);
     dfree(st, m->nbr_off);
     dfree(st, m->nbr);
+    dfree(st, m->img_ref);
+    dfree(st, m->img_code);
+    dfree(st, m->pshift);
+    dfree(st, m->pperm);
     cudaStreamSynchronize(st);
+    if (m->ext) hv_mesh_free(m->ext);
     delete m;
     return HV_OK;
 }

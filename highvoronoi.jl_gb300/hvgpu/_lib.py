@@ -58,6 +58,33 @@ class Stats(ctypes.Structure):
                 [(n, ctypes.c_int64) for n in FALLBACK_FIELDS])
 
 
+class DeviceViews(ctypes.Structure):
+    """hv_device_views: device pointers into a mesh's own arrays."""
+    _fields_ = [("d", ctypes.c_int), ("n", ctypes.c_int64), ("nverts", ctypes.c_int64), ("nnbr", ctypes.c_int64),
+                ("ncell_vertices", ctypes.c_int64), ("sig", ctypes.c_void_p), ("r", ctypes.c_void_p),
+                ("nbr_off", ctypes.c_void_p), ("nbr", ctypes.c_void_p), ("vtx_off", ctypes.c_void_p),
+                ("vtx", ctypes.c_void_p), ("pts", ctypes.c_void_p), ("stream", ctypes.c_void_p)]
+
+
+class CudaArray:
+    """A device array exposing ``__cuda_array_interface__`` (v3), so
+    torch.as_tensor / CuPy / Numba view it without a copy.  It keeps the owning
+    mesh alive.  The memory is the mesh's own: read it, do not write it (the
+    interface's read-only flag stays False because torch rejects it)."""
+
+    def __init__(self, ptr: int, shape, typestr: str, owner, stream: int | None = None):
+        self.ptr, self.shape, self.typestr, self.owner = int(ptr or 0), tuple(int(x) for x in shape), typestr, owner
+        self.stream = stream
+
+    @property
+    def __cuda_array_interface__(self):
+        iface = {"shape": self.shape, "typestr": self.typestr, "data": (self.ptr, False), "version": 3,
+                 "strides": None}
+        if self.stream:
+            iface["stream"] = int(self.stream)
+        return iface
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -99,6 +126,20 @@ def load(path: str | None = None):
         L.hv_integrate_heuristic_mc.argtypes = [P, I, U64, dp, dp]; L.hv_integrate_heuristic_mc.restype = I
         L.hv_mesh_stats.argtypes = [P, ctypes.POINTER(Stats)]; L.hv_mesh_stats.restype = I
         L.hv_mesh_free.argtypes = [P]; L.hv_mesh_free.restype = I
+        L.hv_mesh_cell_vertices.argtypes = [P, ip, ip]; L.hv_mesh_cell_vertices.restype = I
+        i32p = ctypes.POINTER(ctypes.c_int32)
+        i8p = ctypes.POINTER(ctypes.c_int8)
+        L.hv_mesh_build_periodic.argtypes = [P, I, I64, P, dp, dp, i32p, ctypes.POINTER(Params), ctypes.POINTER(P)]
+        L.hv_mesh_build_periodic.restype = I
+        L.hv_mesh_build_periodic_device.argtypes = [P, I, I64, P, dp, dp, i32p, ctypes.POINTER(Params),
+                                                    ctypes.POINTER(P)]
+        L.hv_mesh_build_periodic_device.restype = I
+        L.hv_mesh_periodic_shifts.argtypes = [P, i8p]; L.hv_mesh_periodic_shifts.restype = I
+        L.hv_mesh_periodic_images.argtypes = [P, ip, dp, ip, i8p]; L.hv_mesh_periodic_images.restype = I
+        L.hv_mesh_device_views.argtypes = [P, ctypes.POINTER(DeviceViews)]; L.hv_mesh_device_views.restype = I
+        L.hv_integrate_polygon_device.argtypes = [P, P, P]; L.hv_integrate_polygon_device.restype = I
+        L.hv_integrate_heuristic_mc_device.argtypes = [P, I, U64, P, P]
+        L.hv_integrate_heuristic_mc_device.restype = I
         L.hv_integrate_heuristic_mc_noalloc.argtypes = [I, I64, P, dp, dp, P, P, I64, I, I, U64, P, P, P]
         L.hv_integrate_heuristic_mc_noalloc.restype = I
         _lib = L
@@ -202,15 +243,36 @@ class Mesh:
     """A mesh built on the device (hv_mesh).  Results are copied out on demand."""
 
     def __init__(self, ctx: Context, pts: np.ndarray, lo, hi, params: Params, device_ptr: int | None = None,
-                 planes=None):
-        """Box domain [lo, hi], or (lo = hi = None) the convex domain of
-        ``planes = (base, normal, bc)``: (P, d) base points, (P, d) outer
-        normals and P boundary-condition codes (or None)."""
+                 planes=None, periodic=None):
+        """Box domain [lo, hi] (``periodic``: d flags of periodic axes), or
+        (lo = hi = None) the convex domain of ``planes = (base, normal, bc)``:
+        (P, d) base points, (P, d) outer normals and P boundary-condition codes
+        (or None)."""
         L = load()
         self.ctx = ctx
         pts = np.ascontiguousarray(pts, dtype=np.float64)
         self.n, self.d = pts.shape if device_ptr is None else (int(pts[0]), int(pts[1]))
         h = ctypes.c_void_p()
+        self.periodic = None
+        if periodic is not None and any(periodic):
+            flags = np.ascontiguousarray([1 if f else 0 for f in periodic], dtype=np.int32)
+            if flags.shape[0] != self.d:
+                raise ValueError("periodic needs one flag per axis")
+            self.periodic = flags.astype(bool)
+            self.lo = np.ascontiguousarray(lo, dtype=np.float64)
+            self.hi = np.ascontiguousarray(hi, dtype=np.float64)
+            self.planes = None
+            fp = flags.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+            if device_ptr is None:
+                rc = L.hv_mesh_build_periodic(ctx.handle, self.d, self.n, pts.ctypes.data_as(ctypes.c_void_p),
+                                              dptr(self.lo), dptr(self.hi), fp, ctypes.byref(params), ctypes.byref(h))
+            else:
+                rc = L.hv_mesh_build_periodic_device(ctx.handle, self.d, self.n, ctypes.c_void_p(device_ptr),
+                                                     dptr(self.lo), dptr(self.hi), fp, ctypes.byref(params),
+                                                     ctypes.byref(h))
+            ctx.check(rc, "hv_mesh_build_periodic")
+            self._h = h
+            return
         if planes is not None:
             base = np.ascontiguousarray(planes[0], dtype=np.float64)
             normal = np.ascontiguousarray(planes[1], dtype=np.float64)
@@ -278,6 +340,63 @@ class Mesh:
         rc = load().hv_integrate_heuristic_mc(self._h, ndir, seed, dptr(vol), dptr(area))
         self.ctx.check(rc, "hv_integrate_heuristic_mc")
         return vol, area[:E]
+
+    def periodic_shifts(self) -> np.ndarray:
+        """(nnbr, d) lattice shifts of the neighbour entries (zeros unless periodic)."""
+        _, E = self.counts(neighbors=True)
+        out = np.zeros((max(E, 1), self.d), dtype=np.int8)
+        rc = load().hv_mesh_periodic_shifts(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)))
+        self.ctx.check(rc, "hv_mesh_periodic_shifts")
+        return out[:E]
+
+    def periodic_images(self):
+        """(margin delta (d), 1-based originals, (nimg, d) lattice shifts) of the images."""
+        L = load()
+        ni = ctypes.c_int64()
+        delta = np.zeros(self.d)
+        self.ctx.check(L.hv_mesh_periodic_images(self._h, ctypes.byref(ni), dptr(delta), None, None),
+                       "hv_mesh_periodic_images")
+        ref = np.zeros(max(ni.value, 1), dtype=np.int64)
+        sh = np.zeros((max(ni.value, 1), self.d), dtype=np.int8)
+        self.ctx.check(L.hv_mesh_periodic_images(self._h, ctypes.byref(ni), dptr(delta), iptr(ref),
+                                                 sh.ctypes.data_as(ctypes.POINTER(ctypes.c_int8))),
+                       "hv_mesh_periodic_images")
+        return delta, ref[:ni.value], sh[:ni.value]
+
+    def cell_vertices(self):
+        """(offs (n+1), 1-based vertex rows) of every cell, ascending."""
+        offs = np.zeros(self.n + 1, dtype=np.int64)
+        L = load()
+        self.ctx.check(L.hv_mesh_cell_vertices(self._h, iptr(offs), None), "hv_mesh_cell_vertices")
+        vtx = np.zeros(max(int(offs[-1]), 1), dtype=np.int64)
+        self.ctx.check(L.hv_mesh_cell_vertices(self._h, iptr(offs), iptr(vtx)), "hv_mesh_cell_vertices")
+        return offs, vtx[:int(offs[-1])]
+
+    def device_views(self) -> dict:
+        """Zero-copy device arrays of the mesh (0-based ids, planes n+p):
+        sig, r, nbr_off, nbr, vtx_off, vtx, pts."""
+        v = DeviceViews()
+        self.ctx.check(load().hv_mesh_device_views(self._h, ctypes.byref(v)), "hv_mesh_device_views")
+        d, st = v.d, v.stream
+        return {
+            "sig": CudaArray(v.sig, (v.nverts, d + 1), "<i4", self, st),
+            "r": CudaArray(v.r, (v.nverts, d), "<f8", self, st),
+            "nbr_off": CudaArray(v.nbr_off, (v.n + 1,), "<i8", self, st),
+            "nbr": CudaArray(v.nbr, (v.nnbr,), "<i4", self, st),
+            "vtx_off": CudaArray(v.vtx_off, (v.n + 1,), "<i8", self, st),
+            "vtx": CudaArray(v.vtx, (v.ncell_vertices,), "<i4", self, st),
+            "pts": CudaArray(v.pts, (v.n, d), "<f8", self, st),
+        }
+
+    def polygon_device(self, d_vol: int, d_area: int):
+        """VI_POLYGON into caller device buffers (n and nnbr doubles)."""
+        self.ctx.check(load().hv_integrate_polygon_device(self._h, ctypes.c_void_p(d_vol), ctypes.c_void_p(d_area)),
+                       "hv_integrate_polygon_device")
+
+    def heuristic_mc_device(self, ndir: int, seed: int, d_vol: int, d_area: int):
+        rc = load().hv_integrate_heuristic_mc_device(self._h, ndir, seed, ctypes.c_void_p(d_vol),
+                                                     ctypes.c_void_p(d_area))
+        self.ctx.check(rc, "hv_integrate_heuristic_mc_device")
 
     def stats(self) -> dict:
         s = Stats()

@@ -43,8 +43,9 @@ def BC_Neumann(b, n) -> Plane:
 
 
 def BC_Periodic(base1, base2, normal1):
-    """Periodic plane pairs (src/boundary.jl:47-57) are not part of the GPU mesh path."""
-    raise NotImplementedError("periodic boundaries are not part of the GPU mesh path")
+    """Periodic plane pairs (src/boundary.jl:47-57) run on the GPU path only as
+    the faces of a periodic cuboid: use ``cuboid(d, periodic=[...])``."""
+    raise NotImplementedError("periodic planes are supported as cuboid(d, periodic=[...]) faces")
 
 
 class Boundary:
@@ -56,16 +57,16 @@ class Boundary:
     runs through the plane entry point, where normals are scaled to unit length.
     Domains must be bounded with a non-empty interior; at most 64 planes."""
 
-    def __init__(self, *planes: Plane, lo=None, hi=None):
+    def __init__(self, *planes: Plane, lo=None, hi=None, periodic=()):
         for p in planes:
             if not isinstance(p, Plane):
                 raise TypeError("Boundary takes Plane objects (BC_Dirichlet / BC_Neumann)")
-            if p.BC > 0:
-                raise NotImplementedError("periodic boundaries are not part of the GPU mesh path")
+            if p.BC > 0 and lo is None:
+                raise NotImplementedError("periodic planes are supported as cuboid(d, periodic=[...]) faces")
         self.planes = list(planes)
         self.lo = None if lo is None else np.asarray(lo, dtype=np.float64)
         self.hi = None if hi is None else np.asarray(hi, dtype=np.float64)
-        self.periodic: list = []
+        self.periodic: list = sorted(int(k) for k in periodic)  # 1-based periodic axes
 
     @property
     def dim(self) -> int:
@@ -78,6 +79,10 @@ class Boundary:
     @property
     def is_box(self) -> bool:
         return self.lo is not None
+
+    @property
+    def periodic_flags(self):
+        return [(k + 1) in self.periodic for k in range(self.dim)]
 
     def arrays(self):
         """(base (P, d), normal (P, d), BC (P,) int16) in plane order."""
@@ -93,25 +98,29 @@ class Boundary:
 
 
 def cuboid(dim: int, dimensions=None, periodic=None, neumann=(), offset=None) -> Boundary:
-    """The reference's cuboid (src/boundary.jl:510-534).  Its default is fully
-    periodic (periodic=1:dim); only non-periodic boxes run on the GPU path, so
-    pass ``periodic=[]`` as the reference's own tests and benchmarks do
+    """The reference's cuboid (src/boundary.jl:510-534), fully periodic by
+    default (periodic=1:dim) like the reference's; ``periodic=[]`` gives the
+    Dirichlet box the reference's own tests and benchmarks use
     (test/rcmethods.jl:4, src/statistics.jl:107).  Plane 2k-1 is the upper face
     of axis k and plane 2k the lower face, as in the reference; ``neumann``
     lists k for a Neumann upper face and -k for a Neumann lower face."""
     dims = np.ones(dim) if dimensions is None else np.asarray(dimensions, dtype=np.float64)
     off = np.zeros(dim) if offset is None else np.asarray(offset, dtype=np.float64)
-    per = list(range(1, dim + 1)) if periodic is None else list(periodic)
-    if per:
-        raise NotImplementedError("periodic boundaries are not part of the GPU mesh path; use periodic=[]")
+    per = list(range(1, dim + 1)) if periodic is None else [int(k) for k in periodic]
+    if any(not 1 <= k <= dim for k in per):
+        raise ValueError("periodic axes are 1-based axis numbers")
     neu = set(int(k) for k in neumann)
     planes = []
     for k in range(dim):
         unit = np.zeros(dim)
         unit[k] = 1.0
+        if (k + 1) in per:  # the partner plane's 1-based index (src/boundary.jl:517-520)
+            planes.append(Plane(off + dims * unit, unit.copy(), 2 * k + 2))
+            planes.append(Plane(off.copy(), -unit, 2 * k + 1))
+            continue
         planes.append(Plane(off + dims * unit, unit.copy(), Neumann if (k + 1) in neu else Dirichlet))
         planes.append(Plane(off.copy(), -unit, Neumann if -(k + 1) in neu else Dirichlet))
-    return Boundary(*planes, lo=off.copy(), hi=off + dims)
+    return Boundary(*planes, lo=off.copy(), hi=off + dims, periodic=per)
 
 
 @dataclass(frozen=True)
@@ -177,7 +186,9 @@ class VoronoiGeometry:
             else:
                 self.ctx.autotune(d, n, pts=pts, lo=pts.min(axis=0) - 1.0, hi=pts.max(axis=0) + 1.0)
         self.params = _lib.make_params(method.code, **ss)
-        if b.is_box:
+        if b.is_box and b.periodic:
+            self.mesh = _lib.Mesh(self.ctx, pts, b.lo, b.hi, self.params, periodic=b.periodic_flags)
+        elif b.is_box:
             self.mesh = _lib.Mesh(self.ctx, pts, b.lo, b.hi, self.params)
         else:
             self.mesh = _lib.Mesh(self.ctx, pts, None, None, self.params, planes=b.arrays())
@@ -201,16 +212,80 @@ class VoronoiGeometry:
         return self.mesh.stats()
 
 
+def _unit_planes(boundary: Boundary):
+    base, normal, _ = boundary.arrays()
+    normal = normal / np.linalg.norm(normal, axis=1, keepdims=True)
+    return normal, np.einsum("pk,pk->p", normal, base)
+
+
+def reflect(x, boundary: Boundary, plane: int):
+    """Mirror image of ``x`` across plane ``plane`` (1-based), as the
+    reference's reflect (src/boundary.jl:206-211) with the unit normal."""
+    normal, off = _unit_planes(boundary)
+    nrm = normal[plane - 1]
+    x = np.asarray(x, dtype=np.float64)
+    return x + 2.0 * nrm * (off[plane - 1] - float(np.dot(nrm, x)))
+
+
+def orientations(nodes, offs, nbr, boundary: Boundary, onboundary: bool = False, shifts=None):
+    """For every neighbour k of cell i the vector from x_i to x_k (to its
+    periodic image x_k + s*L with ``shifts`` s), or to the mirror image of x_i
+    across a boundary plane (half of it if ``onboundary``), aligned with the
+    neighbour CSR (the reference's Orientations, src/voronoidata.jl:265-283)."""
+    nodes = np.asarray(nodes, dtype=np.float64)
+    n = nodes.shape[0]
+    cell = np.repeat(np.arange(n), np.diff(offs))
+    nbr = np.asarray(nbr, dtype=np.int64)
+    out = np.empty((len(nbr), nodes.shape[1]))
+    gen = nbr <= n
+    out[gen] = nodes[nbr[gen] - 1] - nodes[cell[gen]]
+    if shifts is not None and boundary.is_box:
+        out[gen] += np.asarray(shifts, dtype=np.float64)[gen] * (boundary.hi - boundary.lo)
+    if (~gen).any():
+        normal, off = _unit_planes(boundary)
+        p = nbr[~gen] - n - 1
+        x = nodes[cell[~gen]]
+        h = off[p] - np.einsum("ek,ek->e", normal[p], x)
+        out[~gen] = (1.0 if onboundary else 2.0) * h[:, None] * normal[p]
+    return out
+
+
+def boundary_nodes(nodes, offs, nbr, boundary: Boundary, onboundary: bool = False, shifts=None) -> dict:
+    """{i: {N+p: mirror of x_i across plane p}} (1-based keys) for every cell
+    touching a boundary plane; the projection onto the plane if ``onboundary``
+    (the reference's BNodesDictDict, src/voronoidata.jl:354-420)."""
+    nodes = np.asarray(nodes, dtype=np.float64)
+    n = nodes.shape[0]
+    o = orientations(nodes, offs, nbr, boundary, onboundary, shifts)
+    res: dict = {}
+    for i in range(n):
+        for t in range(int(offs[i]), int(offs[i + 1])):
+            k = int(nbr[t])
+            if k > n:
+                res.setdefault(i + 1, {})[k] = nodes[i] + o[t]
+    return res
+
+
 class VoronoiData:
     """Read view of a VoronoiGeometry (src/voronoidata.jl:545-700).
 
-    ``vertices``: (V, d+1) sorted 1-based signatures and (V, d) coordinates;
-    ``neighbors[i]``: sorted 1-based neighbours of generator i+1 (planes as
-    N+p); ``volume[i]`` and ``area[i]`` (aligned with ``neighbors[i]``) when the
-    geometry was integrated.
+    ``vertices[i]``: the vertices of cell i+1 as (sorted 1-based signature,
+    coordinates) pairs; ``vertex_sigs`` / ``vertex_coords``: all vertices, rows
+    sorted by signature; ``neighbors[i]``: sorted 1-based neighbours of
+    generator i+1 (planes as N+p); ``orientations[i]``: vectors to the
+    neighbours (mirror images for planes); ``boundary_nodes``: mirror images of
+    the generators across the planes they touch; ``volume[i]`` and ``area[i]``
+    (aligned with ``neighbors[i]``) when the geometry was integrated.  On a
+    periodic cuboid the neighbour entries carry lattice shifts (``shifts[i]``,
+    used by ``orientations``), ``offset`` counts the periodic images the search
+    added, ``references`` (1-based originals) and ``reference_shifts`` (their
+    translation vectors) describe them; otherwise ``offset`` is 0.  There are
+    no infinite edges (``boundary_vertices``).  Integrands (``bulk_integral``,
+    ``interface_integral``) are not computed on the GPU path.
     """
 
-    def __init__(self, geo: VoronoiGeometry):
+    def __init__(self, geo: VoronoiGeometry, onboundary: bool = False):
+        self.geometry = geo
         self.nodes = geo.nodes
         self.boundary = geo.boundary
         self.vertex_sigs, self.vertex_coords = geo.mesh.vertices()
@@ -218,11 +293,28 @@ class VoronoiData:
         self.neighbor_offsets = offs
         self.neighbor_flat = nbr
         self.neighbors = [nbr[offs[i]:offs[i + 1]] for i in range(len(offs) - 1)]
+        voffs, vtx = geo.mesh.cell_vertices()
+        self.vertex_offsets, self.vertex_flat = voffs, vtx
+        self.vertices = [[(self.vertex_sigs[v - 1], self.vertex_coords[v - 1]) for v in vtx[voffs[i]:voffs[i + 1]]]
+                         for i in range(len(voffs) - 1)]
+        shifts = geo.mesh.periodic_shifts() if geo.mesh.periodic is not None else None
+        self.shifts = None if shifts is None else [shifts[offs[i]:offs[i + 1]] for i in range(len(offs) - 1)]
+        o = orientations(self.nodes, offs, nbr, self.boundary, onboundary, shifts)
+        self.orientations = [o[offs[i]:offs[i + 1]] for i in range(len(offs) - 1)]
+        self.boundary_nodes = boundary_nodes(self.nodes, offs, nbr, self.boundary, onboundary, shifts)
+        self.boundary_nodes_on_boundary = onboundary
+        self.boundary_vertices: dict = {}
+        self.offset = 0
+        self.references = np.zeros(0, dtype=np.int64)
+        self.reference_shifts = np.zeros((0, self.nodes.shape[1]))
+        if geo.mesh.periodic is not None:
+            _, ref, sh = geo.mesh.periodic_images()
+            self.offset = len(ref)
+            self.references = ref
+            self.reference_shifts = sh * (self.boundary.hi - self.boundary.lo)
+        self.bulk_integral = None
+        self.interface_integral = None
         self.volume = geo._volumes
         self.area = None
         if geo._areas is not None:
             self.area = [geo._areas[offs[i]:offs[i + 1]] for i in range(len(offs) - 1)]
-
-    @property
-    def vertices(self):
-        return self.vertex_sigs, self.vertex_coords

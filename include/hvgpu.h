@@ -166,6 +166,61 @@ int hv_mesh_neighbors(hv_mesh* mesh, int64_t* offs, int64_t* nbr);
 int hv_integrate_polygon(hv_mesh* mesh, double* vol, double* area);
 /* Monte-Carlo volumes and areas, ndir Philox directions per cell. */
 int hv_integrate_heuristic_mc(hv_mesh* mesh, int ndir, uint64_t seed, double* vol, double* area);
+/* Periodic cuboid [lo, hi] (cuboid(d, periodic=...), src/boundary.jl:510-534):
+ * periodic[k] != 0 makes axis k periodic, the other faces stay Dirichlet.
+ * The mesh of the generators and of their periodic images in a widened box is
+ * searched (the reference's periodize!, src/domain.jl:139-213) and reduced to
+ * the periodic tessellation: every accessor below then reports the n original
+ * cells, naming a neighbour image by its original (1-based) id and its lattice
+ * shift (hv_mesh_periodic_shifts); vertex signatures list original ids (a
+ * generator may appear twice through two of its images), coordinates are the
+ * true positions (a vertex on a periodic seam appears once per translate that
+ * touches an original cell); non-periodic faces keep the ids n+p.
+ * HV_E_CAPACITY when the generators are too few for any image margin. */
+int hv_mesh_build_periodic(hv_ctx* ctx, int d, int64_t n, const double* pts, const double* lo, const double* hi,
+                           const int* periodic, const hv_params* params, hv_mesh** out);
+int hv_mesh_build_periodic_device(hv_ctx* ctx, int d, int64_t n, const double* d_pts, const double* lo,
+                                  const double* hi, const int* periodic, const hv_params* params, hv_mesh** out);
+/* Lattice shift s (nnbr x d, entries -1, 0, 1) of every neighbour entry: the
+ * neighbour of cell i is the image x_j + s * (hi - lo).  Zeros for
+ * non-periodic meshes. */
+int hv_mesh_periodic_shifts(hv_mesh* m, int8_t* shift);
+/* The images the periodic search added (the reference's references /
+ * reference_shifts, src/voronoidata.jl:9-15): their count, the margin delta
+ * (d) of the widened box and, if the arrays are given, the 1-based original
+ * (nimages) and the lattice shift (nimages x d) of every image. */
+int hv_mesh_periodic_images(hv_mesh* m, int64_t* nimages, double* delta, int64_t* ref, int8_t* shift);
+
+/* Cell -> vertex incidences: offs (n+1) and, when vtx is not NULL, the
+ * 1-based row indices (into the hv_mesh_vertices order) of the vertices of
+ * every cell, ascending (the reference's VoronoiData.vertices,
+ * src/voronoidata.jl:545-700).  Call with vtx == NULL to size vtx by offs[n]. */
+int hv_mesh_cell_vertices(hv_mesh* m, int64_t* offs, int64_t* vtx);
+
+/* Zero-copy hand-off: device pointers into the mesh's own arrays (valid until
+ * hv_mesh_free; read-only; on the context's device).  Indices are 0-based,
+ * boundary plane p (0-based) is n+p; signature rows are sorted and the rows
+ * are in the hv_mesh_vertices order.  Julia can wrap them with
+ * unsafe_wrap(CuArray, ...), Python through __cuda_array_interface__. */
+typedef struct {
+    int d;
+    int64_t n, nverts, nnbr, ncell_vertices;
+    const int32_t* sig;       /* nverts x (d+1) */
+    const double* r;          /* nverts x d */
+    const int64_t* nbr_off;   /* n+1 */
+    const int32_t* nbr;       /* nnbr, sorted per cell, planes last */
+    const int64_t* vtx_off;   /* n+1 */
+    const int32_t* vtx;       /* ncell_vertices vertex rows, ascending per cell */
+    const double* pts;        /* n x d generators, original order */
+    void* stream;             /* cudaStream_t the arrays are ordered on */
+} hv_device_views;
+int hv_mesh_device_views(hv_mesh* m, hv_device_views* out);
+
+/* The integrators with outputs in caller device memory (vol: n doubles,
+ * area: nnbr doubles aligned with the neighbour CSR); complete on return. */
+int hv_integrate_polygon_device(hv_mesh* m, double* d_vol, double* d_area);
+int hv_integrate_heuristic_mc_device(hv_mesh* m, int ndir, uint64_t seed, double* d_vol, double* d_area);
+
 int hv_mesh_stats(hv_mesh* mesh, hv_stats* stats);
 int hv_mesh_free(hv_mesh* mesh);
 

@@ -206,3 +206,98 @@ def mc_directions(d, cell, ndir, seed):
     out = np.zeros((ndir, d))
     lib().hvo_mc_directions(d, cell, ndir, seed, _dp(out))
     return out
+
+
+# ---- periodic cuboids: the oracle's mesh of the generators and their periodic
+# images in the widened box, reduced to the original cells (the same
+# construction as the reference's periodize!, src/domain.jl:139-213)
+
+def _codes(d):
+    c = np.arange(3 ** d)
+    return np.stack([(c // 3 ** k) % 3 - 1 for k in range(d)], axis=1)  # (3^d, d) shifts
+
+
+def periodic_images(pts, lo, hi, periodic, delta):
+    """Images x + s*L strictly inside the box widened by delta on the periodic
+    axes, in (point, shift code) order: (images, 0-based originals, shifts)."""
+    pts = np.asarray(pts, dtype=np.float64)
+    n, d = pts.shape
+    lo, hi, delta = (np.asarray(a, dtype=np.float64) for a in (lo, hi, delta))
+    L = hi - lo
+    per = np.asarray(periodic, dtype=bool)
+    S = _codes(d)
+    S = S[np.all((S == 0) | per, axis=1) & np.any(S != 0, axis=1)]
+    Y = pts[:, None, :] + S[None, :, :] * L
+    moved = S[None, :, :] != 0
+    ok = np.all(~moved | ((Y > lo - delta) & (Y < hi + delta)), axis=2)
+    ii, cc = np.nonzero(ok)  # row-major: point-major, codes ascending
+    return Y[ii, cc], ii, S[cc]
+
+
+def periodic_margin_ok(ext_sig, ext_r, ext_pts, n, n_ext, lo, hi, periodic, delta):
+    """Every vertex of an original cell has its circumsphere inside the widened
+    box and holds no widened periodic face."""
+    pub = ext_sig[:, 0] <= n
+    s, r = ext_sig[pub], ext_r[pub]
+    per = np.asarray(periodic, dtype=bool)
+    planes = s > n_ext
+    if np.any(planes & per[np.clip((s - n_ext - 1) // 2, 0, len(per) - 1)]):
+        return False
+    R = np.linalg.norm(r - ext_pts[s[:, 0] - 1], axis=1)[:, None] * (1 + 1e-12) + 1e-12
+    lo, hi, delta = (np.asarray(a, dtype=np.float64) for a in (lo, hi, delta))
+    inside = (r - R > lo - delta) & (r + R < hi + delta)
+    return bool(np.all(inside[:, per]))
+
+
+def periodic_mesh(pts, lo, hi, periodic, delta=None, integrate=False, nthreads=0):
+    """The periodic tessellation of ``pts`` in the cuboid [lo, hi] (periodic
+    axes flagged) from the oracle's mesh of the extended generator set.  With
+    delta None the margin grows from 1.5 spacings by 1.5 until certified.
+    Returns a dict: delta, sig (V, d+1) 1-based original ids (rows sorted),
+    r, offs, nbr (1-based, sorted by (id, shift code)), shift (nnbr, d) and,
+    if integrate, vol and area."""
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    n, d = pts.shape
+    lo = np.asarray(lo, dtype=np.float64)
+    hi = np.asarray(hi, dtype=np.float64)
+    per = np.asarray(periodic, dtype=bool)
+    L = hi - lo
+    spacing = (np.prod(L) / n) ** (1.0 / d)
+    grow = 1.5
+    while True:
+        dl = np.where(per, np.minimum(grow * spacing, 0.999 * L), 0.0) if delta is None else np.asarray(delta)
+        img, ref, sh = periodic_images(pts, lo, hi, per, dl)
+        ext = np.vstack([pts, img])
+        n_ext = len(ext)
+        M = OracleMesh(ext, lo=lo - dl, hi=hi + dl, integrate=integrate, nthreads=nthreads)
+        es, er = M.vertices()
+        if delta is not None or periodic_margin_ok(es, er, ext, n, n_ext, lo, hi, per, dl):
+            break
+        if np.all(dl[per] >= 0.999 * L[per]):
+            raise RuntimeError("too few generators for the periodic image margin")
+        grow *= 1.5
+    center = (3 ** d - 1) // 2
+    codes = np.full(n_ext + 2 * d + 1, center, dtype=np.int64)
+    ids = np.arange(n_ext + 2 * d + 1, dtype=np.int64)   # 1-based ext id -> public id
+    weights = 3 ** np.arange(d)
+    codes[n + 1:n_ext + 1] = (sh + 1) @ weights
+    ids[n + 1:n_ext + 1] = ref + 1
+    ids[n_ext + 1:] = n + np.arange(1, 2 * d + 1)
+    pub = es[:, 0] <= n
+    psig = np.sort(ids[es[pub]], axis=1)
+    pr = er[pub]
+    eo, en = M.neighbors()
+    offs = eo[:n + 1].copy()
+    tot = int(offs[-1])
+    key = ids[en[:tot]] * 1024 + codes[en[:tot]]
+    row = np.repeat(np.arange(n), np.diff(offs))
+    order = np.lexsort((key, row))
+    nbr = ids[en[:tot]][order]
+    c = codes[en[:tot]][order]
+    shift = np.stack([(c // 3 ** k) % 3 - 1 for k in range(d)], axis=1).astype(np.int8)
+    out = dict(delta=dl, sig=psig, r=pr, offs=offs, nbr=nbr, shift=shift, nimages=len(img), ref=ref + 1, ref_shift=sh)
+    if integrate:
+        vol, area = M.polygon()
+        out["vol"] = vol[:n]
+        out["area"] = area[:tot][order]
+    return out

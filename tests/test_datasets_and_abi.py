@@ -87,8 +87,12 @@ def test_python_layer_fails_loudly_without_device(libhvgpu):
 
 def test_cuboid_mirrors_reference_defaults():
     import hvgpu
-    with pytest.raises(NotImplementedError):
-        hvgpu.cuboid(3)  # the reference's default is fully periodic
+    full = hvgpu.cuboid(3)  # the reference's default is fully periodic, partners named by 1-based index
+    assert full.periodic == [1, 2, 3]
+    assert [p.BC for p in full.planes] == [2, 1, 4, 3, 6, 5]
+    part = hvgpu.cuboid(2, periodic=[2], neumann=[1])
+    assert part.periodic_flags == [False, True]
+    assert [p.BC for p in part.planes] == [hvgpu.Neumann, hvgpu.Dirichlet, 4, 3]
     b = hvgpu.cuboid(3, periodic=[], dimensions=[2, 1, 1], offset=[-1, 0, 0])
     np.testing.assert_array_equal(b.lo, [-1, 0, 0])
     np.testing.assert_array_equal(b.hi, [1, 1, 1])

@@ -170,3 +170,38 @@ def test_device_points_with_planes(gpu_lib):
     h = _planes_mesh(hv, X, base, normal)
     np.testing.assert_array_equal(m.vertices()[0], h.vertices()[0])
     np.testing.assert_array_equal(m.vertices()[1], h.vertices()[1])
+
+
+def test_voronoi_data_views_and_device_handoff(gpu_lib):
+    """Per-cell vertices, the zero-copy device arrays and the device-output
+    integrators agree with the host outputs."""
+    torch = pytest.importorskip("torch")
+    hv = gpu_lib
+    X = D.uniform_points(3, 800, 77)
+    geo = hv.VoronoiGeometry(X, hv.cuboid(3, periodic=[]), integrator=hv.VI_POLYGON)
+    vd = hv.VoronoiData(geo)
+    for i in range(0, len(X), 13):
+        assert len(vd.vertices[i]) > 0
+        for s, _ in vd.vertices[i]:
+            assert i + 1 in s
+    # every vertex of the mesh appears in exactly d+1 cells counted over its generators
+    cnt = np.bincount(vd.vertex_flat - 1, minlength=len(vd.vertex_sigs))
+    np.testing.assert_array_equal(cnt, np.sum(vd.vertex_sigs <= len(X), axis=1))
+    m = geo.mesh
+    views = m.device_views()
+    sig = torch.as_tensor(views["sig"], device="cuda").cpu().numpy()
+    np.testing.assert_array_equal(sig + 1, vd.vertex_sigs)
+    np.testing.assert_array_equal(torch.as_tensor(views["r"], device="cuda").cpu().numpy(), vd.vertex_coords)
+    np.testing.assert_array_equal(torch.as_tensor(views["nbr"], device="cuda").cpu().numpy() + 1, vd.neighbor_flat)
+    np.testing.assert_array_equal(torch.as_tensor(views["nbr_off"], device="cuda").cpu().numpy(), vd.neighbor_offsets)
+    np.testing.assert_array_equal(torch.as_tensor(views["vtx"], device="cuda").cpu().numpy() + 1, vd.vertex_flat)
+    dv = torch.zeros(len(X), dtype=torch.float64, device="cuda")
+    da = torch.zeros(len(vd.neighbor_flat), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    m.polygon_device(dv.data_ptr(), da.data_ptr())
+    np.testing.assert_array_equal(dv.cpu().numpy(), vd.volume)
+    np.testing.assert_array_equal(da.cpu().numpy(), np.concatenate(vd.area))
+    mv, ma = m.heuristic_mc(500, 3)
+    m.heuristic_mc_device(500, 3, dv.data_ptr(), da.data_ptr())
+    np.testing.assert_array_equal(dv.cpu().numpy(), mv)
+    np.testing.assert_array_equal(da.cpu().numpy(), ma)

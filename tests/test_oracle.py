@@ -220,3 +220,78 @@ def test_points_outside_planes_are_rejected():
     base, normal, _ = simplex(3)
     with pytest.raises(RuntimeError):
         O.OracleMesh(np.array([[0.2, 0.2, 0.2], [0.5, 0.5, 0.5]]), planes=(base, normal))
+
+
+# ---- VoronoiData's derived views (orientations, boundary_nodes; src/voronoidata.jl:265-420)
+
+@pytest.mark.parametrize("domain", ["box", "simplex"])
+def test_orientations_are_facet_normals(domain):
+    """Every vertex of cell i on the facet towards neighbour k lies on the
+    bisector of x_i and x_i + o (o the orientation): (r - x_i - o/2) . o = 0.
+    For plane neighbours x_i + o is the mirror image of x_i."""
+    import hvgpu
+    from _domains import simplex, simplex_points
+    d = 3
+    if domain == "box":
+        X = D.uniform_points(d, 300, 5)
+        b = hvgpu.cuboid(d, periodic=[])
+        m = O.OracleMesh(X)
+    else:
+        base, normal, _ = simplex(d)
+        X = simplex_points(d, 300, 5)
+        b = hvgpu.Boundary(*[hvgpu.BC_Dirichlet(base[p], normal[p]) for p in range(len(base))])
+        m = O.OracleMesh(X, planes=(base, normal))
+    offs, nbr = m.neighbors()
+    sig, r = m.vertices()
+    o = hvgpu.orientations(X, offs, nbr, b)
+    n = len(X)
+    for i in range(0, n, 7):
+        mine = np.any(sig == i + 1, axis=1)
+        for t in range(offs[i], offs[i + 1]):
+            rows = mine & np.any(sig == nbr[t], axis=1)
+            assert rows.any()
+            res = (r[rows] - X[i] - 0.5 * o[t]) @ o[t]
+            assert np.max(np.abs(res)) < 1e-12
+    bn = hvgpu.boundary_nodes(X, offs, nbr, b)
+    for i, planes in list(bn.items())[:20]:
+        for k, y in planes.items():
+            np.testing.assert_allclose(y, hvgpu.reflect(X[i - 1], b, k - n), atol=1e-15)
+    half = hvgpu.boundary_nodes(X, offs, nbr, b, onboundary=True)
+    i, planes = next(iter(half.items()))
+    for k, y in planes.items():
+        np.testing.assert_allclose(y, 0.5 * (X[i - 1] + hvgpu.reflect(X[i - 1], b, k - n)), atol=1e-15)
+
+
+# ---- periodic cuboids (cuboid(d), fully periodic by default, src/boundary.jl:510-534)
+
+def _facet_pairs(P, n):
+    """{(i, j, shift): area} of the periodic facets between generators."""
+    out = {}
+    for i in range(n):
+        for t in range(P["offs"][i], P["offs"][i + 1]):
+            j = int(P["nbr"][t])
+            if j <= n:
+                out[(i + 1, j, tuple(int(x) for x in P["shift"][t]))] = P["area"][t]
+    return out
+
+
+@pytest.mark.parametrize("d,n,per", [(2, 300, [1, 1]), (3, 300, [1, 1, 1]), (3, 200, [0, 1, 0]), (4, 200, [1, 1, 1, 1])])
+def test_periodic_oracle_properties(d, n, per):
+    """Volumes tile the torus; every facet (i, j, s) has its partner (j, i, -s)
+    with the same area; the tessellation is invariant under translation mod L."""
+    X = D.uniform_points(d, n, 40 + d)
+    lo, hi = np.zeros(d), np.ones(d)
+    P = O.periodic_mesh(X, lo, hi, per, integrate=True)
+    assert abs(P["vol"].sum() - 1.0) < 1e-11
+    fp = _facet_pairs(P, n)
+    for (i, j, s), a in fp.items():
+        b = fp[(j, i, tuple(-x for x in s))]
+        assert abs(a - b) <= 1e-10 * max(a, 1e-300) + 1e-16
+    t = np.where(np.asarray(per, dtype=bool), 0.3719, 0.0)
+    Y = np.where(np.asarray(per, dtype=bool), (X + t) % 1.0, X)
+    Q = O.periodic_mesh(Y, lo, hi, per, integrate=True)
+    np.testing.assert_allclose(Q["vol"], P["vol"], rtol=1e-9, atol=1e-14)
+    for i in range(0, n, 17):
+        a = sorted(P["nbr"][P["offs"][i]:P["offs"][i + 1]])
+        b = sorted(Q["nbr"][Q["offs"][i]:Q["offs"][i + 1]])
+        assert a == b
