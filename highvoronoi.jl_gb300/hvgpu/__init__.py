@@ -7,7 +7,7 @@ from ._lib import (HV_METHOD_FAST, HV_METHOD_PLAIN, Context, HVError, Mesh, defa
                    make_params)
 from .geometry import (RCGPU, RCGPUPlain, VI_FAST_POLYGON, VI_GEOMETRY, VI_HEURISTIC_MC, VI_POLYGON,  # noqa: F401
                        BC_Dirichlet, BC_Neumann, BC_Periodic, Boundary, Dirichlet, Neumann, Plane, RaycastMethod,
-                       VoronoiData, VoronoiGeometry, boundary_nodes, cuboid, orientations, reflect)
+                       VoronoiData, VoronoiGeometry, boundary_nodes, cuboid, orientations, refine, reflect)
 from . import datasets  # noqa: F401
 
 __version__ = "1.0.0"

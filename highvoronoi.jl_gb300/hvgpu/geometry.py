@@ -186,23 +186,49 @@ class VoronoiGeometry:
             else:
                 self.ctx.autotune(d, n, pts=pts, lo=pts.min(axis=0) - 1.0, hi=pts.max(axis=0) + 1.0)
         self.params = _lib.make_params(method.code, **ss)
-        if b.is_box and b.periodic:
-            self.mesh = _lib.Mesh(self.ctx, pts, b.lo, b.hi, self.params, periodic=b.periodic_flags)
-        elif b.is_box:
-            self.mesh = _lib.Mesh(self.ctx, pts, b.lo, b.hi, self.params)
-        else:
-            self.mesh = _lib.Mesh(self.ctx, pts, None, None, self.params, planes=b.arrays())
+        self.mesh = self._build(pts)
         self.integrator = integrator
-        self._volumes = None
-        self._areas = None
-        if integrator in (VI_POLYGON, VI_FAST_POLYGON):
-            self._volumes, self._areas = self.mesh.polygon()
-        elif integrator == VI_HEURISTIC_MC:
-            self._volumes, self._areas = self.mesh.heuristic_mc(int(mc_accurate[0]), int(mc_seed))
-        elif integrator != VI_GEOMETRY:
+        self.mc_accurate = mc_accurate
+        self.mc_seed = mc_seed
+        if integrator not in (VI_GEOMETRY, VI_POLYGON, VI_FAST_POLYGON, VI_HEURISTIC_MC):
             raise ValueError(f"unsupported integrator {integrator!r} on the GPU path")
+        self._integrate()
         if not silence:
             print(f"VoronoiGeometry: {self.mesh.stats()['vertices']} vertices")
+
+    def _build(self, pts):
+        b = self.boundary
+        if b.is_box and b.periodic:
+            return _lib.Mesh(self.ctx, pts, b.lo, b.hi, self.params, periodic=b.periodic_flags)
+        if b.is_box:
+            return _lib.Mesh(self.ctx, pts, b.lo, b.hi, self.params)
+        return _lib.Mesh(self.ctx, pts, None, None, self.params, planes=b.arrays())
+
+    def _integrate(self):
+        self._volumes = None
+        self._areas = None
+        if self.integrator in (VI_POLYGON, VI_FAST_POLYGON):
+            self._volumes, self._areas = self.mesh.polygon()
+        elif self.integrator == VI_HEURISTIC_MC:
+            self._volumes, self._areas = self.mesh.heuristic_mc(int(self.mc_accurate[0]), int(self.mc_seed))
+
+    def refine(self, xs, update: bool = True) -> "VoronoiGeometry":
+        """refine!(VG, xs, update) (src/geometry.jl:404-433): appends the
+        generators ``xs`` (numbered after the existing ones) and recomputes the
+        mesh, and with ``update`` the integrals.  The GPU search rebuilds the
+        whole tessellation of the enlarged set; the result is the one the
+        reference's cell-by-cell update reaches, since the tessellation is
+        unique."""
+        xs = np.asarray(xs, dtype=np.float64).reshape(-1, self.dimension)
+        pts = np.ascontiguousarray(np.vstack([self.nodes, xs]))
+        mesh = self._build(pts)
+        self.mesh.free()
+        self.mesh, self.nodes = mesh, pts
+        if update:
+            self._integrate()
+        else:
+            self._volumes = self._areas = None
+        return self
 
     @property
     def dimension(self) -> int:
@@ -210,6 +236,14 @@ class VoronoiGeometry:
 
     def stats(self) -> dict:
         return self.mesh.stats()
+
+
+def refine(VG: "VoronoiGeometry", xs, update: bool = True) -> "VoronoiGeometry":
+    """refine(VG, xs, update) (src/geometry.jl:440-442): a refined copy; VG is unchanged."""
+    g = VoronoiGeometry(VG.nodes, VG.boundary, search_settings=None, integrator=VI_GEOMETRY, context=VG.ctx)
+    g.params, g.method = VG.params, VG.method
+    g.integrator, g.mc_accurate, g.mc_seed = VG.integrator, VG.mc_accurate, VG.mc_seed
+    return g.refine(xs, update)
 
 
 def _unit_planes(boundary: Boundary):

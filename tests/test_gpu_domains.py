@@ -205,3 +205,22 @@ def test_voronoi_data_views_and_device_handoff(gpu_lib):
     m.heuristic_mc_device(500, 3, dv.data_ptr(), da.data_ptr())
     np.testing.assert_array_equal(dv.cpu().numpy(), mv)
     np.testing.assert_array_equal(da.cpu().numpy(), ma)
+
+
+def test_refine_matches_a_fresh_build(gpu_lib):
+    """refine!(VG, xs) appends generators: the mesh and volumes equal those of
+    one build on all points, for a box, a periodic cuboid and a plane domain."""
+    hv = gpu_lib
+    X = D.uniform_points(3, 1200, 88)
+    base, normal, _ = simplex(3)
+    S = simplex_points(3, 1200, 89)
+    for b, pts in ((hv.cuboid(3, periodic=[]), X), (hv.cuboid(3), X),
+                   (hv.Boundary(*[hv.BC_Dirichlet(base[p], normal[p]) for p in range(4)]), S)):
+        g = hv.VoronoiGeometry(pts[:800], b, integrator=hv.VI_POLYGON)
+        h = hv.refine(g, pts[800:])
+        assert len(g.nodes) == 800
+        g.refine(pts[800:])
+        f = hv.VoronoiGeometry(pts, b, integrator=hv.VI_POLYGON)
+        for x in (g, h):
+            np.testing.assert_array_equal(x.mesh.vertices()[0], f.mesh.vertices()[0])
+            np.testing.assert_array_equal(hv.VoronoiData(x).volume, hv.VoronoiData(f).volume)
