@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-integrator", choices=["polygon", "none"], default="polygon")
     ap.add_argument("--no-integrators", action="store_true")
     ap.add_argument("--knn", type=int, default=0, help="candidate list length (0 = library default)")
     ap.add_argument("--leaf-size", type=int, default=0, help="tree leaf size (0 = library default)")
@@ -180,17 +181,18 @@ def run_serve(args, device):
     reqs, gaps = serve_requests(args.serve_requests)
     pts = [D.uniform_points(d, n, r) for d, n, r in reqs]
     arrivals = np.cumsum(gaps / args.serve_rate)
+    integ = None if args.serve_integrator == "none" else args.serve_integrator
     with Server(device=device, slots=args.serve_slots) as srv:
         # warm-up: one request per dimension
         for d in (2, 3, 4, 5):
-            srv.result(srv.submit(D.uniform_points(d, 500, 10 ** 6 + d), integrator="polygon"))
+            srv.result(srv.submit(D.uniform_points(d, 500, 10 ** 6 + d), integrator=integ))
         t0 = time.perf_counter()
         tickets = []
         for k, (p, ta) in enumerate(zip(pts, arrivals)):
             now = time.perf_counter() - t0
             if ta > now:
                 time.sleep(ta - now)
-            tickets.append(srv.submit(p, integrator="polygon"))
+            tickets.append(srv.submit(p, integrator=integ))
         lat, fails, verts = [], 0, 0
         for t in tickets:
             r = srv.result(t)
@@ -205,7 +207,8 @@ def run_serve(args, device):
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "mean_ms": float(lat.mean()), "meshes_per_s": len(lat) / t_end, "vertices": int(verts),
             "config": "d uniform {2,3,4,5}, N log-uniform [200,20000], uniform points seed=request id, "
-                      "cuboid(d, periodic=[]), VI_POLYGON, Poisson arrivals"}
+                      "cuboid(d, periodic=[]), " + ("VI_POLYGON" if integ else "no integrator") +
+                      ", Poisson arrivals"}
 
 
 def run_reference(args):

@@ -135,6 +135,19 @@ class RaycastMethod:
 # Beside the reference's RCOriginal / RCNonGeneral / RCCombined (src/raycast-types.jl:244-285).
 RCGPU = RaycastMethod("RCGPU", _lib.HV_METHOD_FAST)
 RCGPUPlain = RaycastMethod("RCGPUPlain", _lib.HV_METHOD_PLAIN)
+# The reference's CPU raycast variants (src/raycast-types.jl:244-310) differ in
+# speed, not in the tessellation they find (the unique Voronoi diagram of the
+# generators in general position); on this path they all run the GPU search.
+RCOriginal = RaycastMethod("RCOriginal", _lib.HV_METHOD_FAST)
+RCOriginalSafety = RaycastMethod("RCOriginalSafety", _lib.HV_METHOD_FAST)
+RCOriginalHP = RaycastMethod("RCOriginalHP", _lib.HV_METHOD_FAST)
+RCNonGeneralFast = RaycastMethod("RCNonGeneralFast", _lib.HV_METHOD_FAST)
+RCNonGeneralSkip = RaycastMethod("RCNonGeneralSkip", _lib.HV_METHOD_FAST)
+RCNonGeneralHP = RaycastMethod("RCNonGeneralHP", _lib.HV_METHOD_FAST)
+RCNonGeneralCutoff = RaycastMethod("RCNonGeneralCutoff", _lib.HV_METHOD_FAST)
+RCCombined = RaycastMethod("RCCombined", _lib.HV_METHOD_FAST)
+RCNonGeneral = RCNonGeneralHP
+RCStandard = RCNonGeneral
 
 VI_GEOMETRY = "VI_GEOMETRY"
 VI_POLYGON = "VI_POLYGON"
@@ -142,6 +155,10 @@ VI_POLYGON = "VI_POLYGON"
 # volumes and interface areas as VI_POLYGON, which the GPU computes the same way for both.
 VI_FAST_POLYGON = "VI_FAST_POLYGON"
 VI_HEURISTIC_MC = "VI_HEURISTIC_MC"
+# VI_HEURISTIC_MC takes its volumes and areas from VI_MONTECARLO without an
+# integrand (src/heuristic_mc.jl:10); without integrands the two give the same
+# quantities, computed here by the GPU Monte-Carlo integrator.
+VI_MONTECARLO = "VI_MONTECARLO"
 
 
 class VoronoiGeometry:
@@ -190,7 +207,7 @@ class VoronoiGeometry:
         self.integrator = integrator
         self.mc_accurate = mc_accurate
         self.mc_seed = mc_seed
-        if integrator not in (VI_GEOMETRY, VI_POLYGON, VI_FAST_POLYGON, VI_HEURISTIC_MC):
+        if integrator not in (VI_GEOMETRY, VI_POLYGON, VI_FAST_POLYGON, VI_HEURISTIC_MC, VI_MONTECARLO):
             raise ValueError(f"unsupported integrator {integrator!r} on the GPU path")
         self._integrate()
         if not silence:
@@ -209,7 +226,7 @@ class VoronoiGeometry:
         self._areas = None
         if self.integrator in (VI_POLYGON, VI_FAST_POLYGON):
             self._volumes, self._areas = self.mesh.polygon()
-        elif self.integrator == VI_HEURISTIC_MC:
+        elif self.integrator in (VI_HEURISTIC_MC, VI_MONTECARLO):
             self._volumes, self._areas = self.mesh.heuristic_mc(int(self.mc_accurate[0]), int(self.mc_seed))
 
     def refine(self, xs, update: bool = True) -> "VoronoiGeometry":

@@ -112,3 +112,18 @@ def test_fast_polygon_integrator_is_the_polygon_integrator(gpu_lib):
     ref = O.OracleMesh(pts, integrate=True)
     rv, _ = ref.polygon()
     np.testing.assert_allclose(b.volume, rv, rtol=POLY_RTOL, atol=1e-15)
+
+
+def test_reference_method_and_integrator_names(gpu_lib):
+    """The reference's raycast variants run the GPU search (same tessellation) and
+    VI_MONTECARLO gives the volumes and areas VI_HEURISTIC_MC is built from
+    (src/heuristic_mc.jl:10)."""
+    hv = gpu_lib
+    pts = D.uniform_points(3, 300, 44)
+    base = hv.VoronoiData(hv.VoronoiGeometry(pts, hv.cuboid(3, periodic=[]), integrator=hv.VI_HEURISTIC_MC))
+    for m in (hv.RCOriginal, hv.RCCombined, hv.RCNonGeneralHP, hv.RCStandard):
+        g = hv.VoronoiGeometry(pts, hv.cuboid(3, periodic=[]), search_settings=dict(method=m),
+                               integrator=hv.VI_MONTECARLO)
+        vd = hv.VoronoiData(g)
+        np.testing.assert_array_equal(vd.vertex_sigs, base.vertex_sigs)
+        np.testing.assert_array_equal(vd.volume, base.volume)
