@@ -126,13 +126,17 @@ unsigned next_pow2(unsigned long long x) {
     return (unsigned)p;
 }
 
-// Candidate list length per dimension: measured on GB300 (4D/20k uniform: K=160
-// is fastest; 5D clustered: 320; 6D: 480), shorter lists trade kNN and scan work
-// for more rays that leave the list's complete radius.
+// Candidate list length per dimension, measured on GB300 (sweeps over 2D/1k,
+// 3D/100k, 4D/20k, 5D/20k uniform and 50k clustered, 6D/10k): shorter lists
+// trade kNN and scan work for more rays that leave the list's complete radius.
 int default_knn(int d) {
-    static const int k[7] = {0, 0, 32, 96, 160, 320, 480};
+    static const int k[7] = {0, 0, 24, 64, 128, 256, 384};
     return k[d];
 }
+
+// One descent seed per `stride` generators (measured with the list lengths
+// above): every seed costs d dependent rays, fewer seeds cost wavefront levels.
+int default_seed_stride(long long n) { return n <= 4096 ? 1 : (n < 65536 ? 8 : 16); }
 
 // Expected vertices per generator for uniform points in the cube (the
 // reference's own counts, docs/src/index.md:93-96, extrapolated to 2, 3, 6).
@@ -303,7 +307,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     // ---- search with capacity retry
     double factor = mesh->prm.capacity_factor > 0 ? mesh->prm.capacity_factor : 1.3;
     unsigned long long est = (unsigned long long)(vertices_per_point(d) * n) + (1ull << d) + 1024;
-    int stride = mesh->prm.seed_stride > 0 ? mesh->prm.seed_stride : (n <= 4096 ? 1 : 4);
+    int stride = mesh->prm.seed_stride > 0 ? mesh->prm.seed_stride : default_seed_stride(n);
     const int nseeds = (n + stride - 1) / stride;
     std::unique_ptr<Scratch> srch;
     unsigned V = 0;
@@ -871,11 +875,10 @@ int hv_autotune(hv_ctx* ctx, int d, int64_t n, const double* pts, const double* 
         }
         pts = synth.data();
     }
-    static const int kd[7] = {0, 0, 32, 96, 160, 320, 480};
-    const int K0 = kd[d];
+    const int K0 = default_knn(d);
     std::vector<int> ks = {std::max(16, K0 / 2), K0, std::min(480, K0 * 3 / 2)};
     std::vector<int> leaves = {8, 16};
-    std::vector<int> strides = {1, 4, 16};
+    std::vector<int> strides = {1, 4, 8, 16};
     hv_params best;
     hv_params_default(&best);
     double best_ms = 1e300;

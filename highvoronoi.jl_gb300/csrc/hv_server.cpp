@@ -178,7 +178,7 @@ int hv_server_submit(hv_server* S, const hv_request* q, int64_t* ticket) {
     J->lo.assign(q->lo, q->lo + q->d);
     J->hi.assign(q->hi, q->hi + q->d);
     J->req.pts = nullptr; J->req.lo = nullptr; J->req.hi = nullptr;
-    static const int kd[7] = {0, 0, 32, 96, 256, 384, 480};
+    static const int kd[7] = {0, 0, 24, 64, 128, 256, 384};  // the library's default list lengths
     J->est = estimate_bytes(q->d, q->n, q->params.knn > 0 ? q->params.knn : kd[q->d]);
     if (J->est > S->budget) return HV_E_OOM;
     J->t_submit = clk::now();
