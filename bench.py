@@ -85,6 +85,19 @@ def dist_env():
     return ws, rank, local
 
 
+def aggregate_over_ranks(tot_ms, units, device):
+    """Whole-job numbers of the replicas: the MAX over ranks of the timed
+    milliseconds and the SUM of the units (vertices) they processed, over the
+    default process group (nccl on the GPUs, gloo in the CPU tests)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(tot_ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(u)
+    return float(t.item()), int(round(u.item()))
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -290,12 +303,8 @@ def run_ours(args):
         m.free()
     clocks = clk.stop()
     if ws > 1:
-        t = torch.tensor([tot_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        tot_ms = float(t.item())
-        v = torch.tensor([float(verts)], device="cuda")
-        torch.distributed.all_reduce(v)
-        verts = int(v.item())
+        torch.distributed.barrier()
+        tot_ms, verts = aggregate_over_ranks(tot_ms, verts, "cuda")
     value = verts / (tot_ms / 1e3)
     # ---- the two integrators on the same mesh (host wall clock through the C ABI, outputs copied back)
     integ = None

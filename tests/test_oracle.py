@@ -295,3 +295,33 @@ def test_periodic_oracle_properties(d, n, per):
         a = sorted(P["nbr"][P["offs"][i]:P["offs"][i + 1]])
         b = sorted(Q["nbr"][Q["offs"][i]:Q["offs"][i + 1]])
         assert a == b
+
+
+# ---- committed golden fixtures (tests/golden/make_golden.py)
+
+def _golden_names():
+    import glob
+    import os
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(here, "*.npz")))
+
+
+@pytest.mark.parametrize("name", _golden_names())
+def test_oracle_reproduces_golden(name):
+    """The oracle still produces the committed fixtures: signatures and
+    neighbours exactly, coordinates and integrals to rounding."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_golden as G
+    ref = np.load(os.path.join(os.path.dirname(G.__file__), name + ".npz"))
+    out = G.compute(name)
+    np.testing.assert_array_equal(out["pts"], ref["pts"])
+    np.testing.assert_array_equal(out["sig"], ref["sig"])
+    np.testing.assert_allclose(out["r"], ref["r"], atol=1e-12)
+    np.testing.assert_array_equal(out["offs"], ref["offs"])
+    np.testing.assert_array_equal(out["nbr"], ref["nbr"])
+    if "shift" in ref:
+        np.testing.assert_array_equal(out["shift"], ref["shift"])
+    np.testing.assert_allclose(out["vol"], ref["vol"], rtol=1e-12, atol=1e-16)
+    np.testing.assert_allclose(out["area"], ref["area"], rtol=1e-12, atol=1e-16)
