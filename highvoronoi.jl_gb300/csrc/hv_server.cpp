@@ -29,7 +29,10 @@ using clk = std::chrono::steady_clock;
 
 struct Job {
     hv_request req;
-    std::vector<double> pts, lo, hi;
+    std::vector<double> pts, lo, hi, base, normal;
+    std::vector<int> periodic;
+    std::vector<int16_t> bc;
+    std::vector<int8_t> shift;
     double est = 0;
     int state = 0;  // 0 queued, 1 running, 2 done
     int rc = HV_OK;
@@ -74,7 +77,15 @@ namespace {
 void run_job(hv_ctx* ctx, Job& J) {
     const hv_request& q = J.req;
     hv_mesh* m = nullptr;
-    int rc = hv_mesh_build(ctx, q.d, q.n, J.pts.data(), J.lo.data(), J.hi.data(), &q.params, &m);
+    int rc;
+    if (!J.periodic.empty())
+        rc = hv_mesh_build_periodic(ctx, q.d, q.n, J.pts.data(), J.lo.data(), J.hi.data(), J.periodic.data(),
+                                    &q.params, &m);
+    else if (q.nplanes > 0)
+        rc = hv_mesh_build_planes(ctx, q.d, q.n, J.pts.data(), q.nplanes, J.base.data(), J.normal.data(),
+                                  J.bc.empty() ? nullptr : J.bc.data(), &q.params, &m);
+    else
+        rc = hv_mesh_build(ctx, q.d, q.n, J.pts.data(), J.lo.data(), J.hi.data(), &q.params, &m);
     if (rc == HV_OK) {
         int64_t nv = 0, nn = 0;
         rc = hv_mesh_counts(m, &nv, &nn);
@@ -87,6 +98,10 @@ void run_job(hv_ctx* ctx, Job& J) {
             rc = hv_mesh_vertices(m, J.sig.data(), J.r.data());
         }
         if (rc == HV_OK) rc = hv_mesh_neighbors(m, J.offs.data(), J.nbr.data());
+        if (rc == HV_OK && !J.periodic.empty()) {
+            J.shift.resize((size_t)std::max<int64_t>(J.nnbr, 1) * q.d);
+            rc = hv_mesh_periodic_shifts(m, J.shift.data());
+        }
         if (rc == HV_OK && q.integrator != HV_INTEGRATOR_NONE) {
             J.vol.resize((size_t)std::max<int64_t>(q.n, 1));
             J.area.resize((size_t)std::max<int64_t>(J.nnbr, 1));
@@ -170,16 +185,37 @@ int hv_server_start(const hv_server_config* cfg, hv_server** out) {
 }
 
 int hv_server_submit(hv_server* S, const hv_request* q, int64_t* ticket) {
-    if (!S || !q || !ticket || q->d < 2 || q->d > 6 || q->n < 0 || (q->n > 0 && !q->pts) || !q->lo || !q->hi)
+    if (!S || !q || !ticket || q->d < 2 || q->d > 6 || q->n < 0 || (q->n > 0 && !q->pts))
         return HV_E_INVALID_ARG;
+    const bool planes = q->nplanes > 0;
+    if (planes && (q->nplanes > 64 || !q->base || !q->normal || q->periodic)) return HV_E_INVALID_ARG;
+    if (!planes && (!q->lo || !q->hi)) return HV_E_INVALID_ARG;
     std::unique_ptr<Job> J(new Job());
     J->req = *q;
     J->pts.assign(q->pts, q->pts + (size_t)q->n * q->d);
-    J->lo.assign(q->lo, q->lo + q->d);
-    J->hi.assign(q->hi, q->hi + q->d);
+    if (planes) {
+        J->base.assign(q->base, q->base + (size_t)q->nplanes * q->d);
+        J->normal.assign(q->normal, q->normal + (size_t)q->nplanes * q->d);
+        if (q->bc) J->bc.assign(q->bc, q->bc + q->nplanes);
+    } else {
+        J->lo.assign(q->lo, q->lo + q->d);
+        J->hi.assign(q->hi, q->hi + q->d);
+    }
+    double n_eff = (double)q->n;
+    if (q->periodic) {
+        bool any = false;
+        for (int k = 0; k < q->d; ++k) any |= q->periodic[k] != 0;
+        if (any) {
+            J->periodic.assign(q->periodic, q->periodic + q->d);
+            // images in a margin of a few spacings on each periodic face
+            const double grow = std::pow(1.0 + 6.0 / std::pow(std::max<double>((double)q->n, 1.0), 1.0 / q->d), q->d);
+            n_eff *= std::min(grow, std::pow(3.0, q->d));
+        }
+    }
     J->req.pts = nullptr; J->req.lo = nullptr; J->req.hi = nullptr;
+    J->req.periodic = nullptr; J->req.base = nullptr; J->req.normal = nullptr; J->req.bc = nullptr;
     static const int kd[7] = {0, 0, 24, 64, 128, 256, 384};  // the library's default list lengths
-    J->est = estimate_bytes(q->d, q->n, q->params.knn > 0 ? q->params.knn : kd[q->d]);
+    J->est = estimate_bytes(q->d, (int64_t)n_eff, q->params.knn > 0 ? q->params.knn : kd[q->d]);
     if (J->est > S->budget) return HV_E_OOM;
     J->t_submit = clk::now();
     {
@@ -225,6 +261,7 @@ int hv_server_wait(hv_server* S, int64_t ticket, double timeout_ms, hv_result* o
         out->vol = J->vol.empty() ? nullptr : J->vol.data();
         out->area = J->area.empty() ? nullptr : J->area.data();
         out->stats = J->stats;
+        out->shift = J->shift.empty() ? nullptr : J->shift.data();
     }
     out->queue_ms = ms(J->t_submit, J->t_start);
     out->service_ms = ms(J->t_start, J->t_end);

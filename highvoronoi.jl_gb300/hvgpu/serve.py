@@ -23,7 +23,9 @@ class _Config(ctypes.Structure):
 class _Request(ctypes.Structure):
     _fields_ = [("d", ctypes.c_int), ("n", ctypes.c_int64), ("pts", ctypes.c_void_p), ("lo", ctypes.c_void_p),
                 ("hi", ctypes.c_void_p), ("integrator", ctypes.c_int), ("ndir", ctypes.c_int),
-                ("mc_seed", ctypes.c_uint64), ("params", _lib.Params)]
+                ("mc_seed", ctypes.c_uint64), ("params", _lib.Params), ("periodic", ctypes.c_void_p),
+                ("nplanes", ctypes.c_int), ("base", ctypes.c_void_p), ("normal", ctypes.c_void_p),
+                ("bc", ctypes.c_void_p)]
 
 
 class _Result(ctypes.Structure):
@@ -32,7 +34,8 @@ class _Result(ctypes.Structure):
                 ("r", ctypes.POINTER(ctypes.c_double)), ("offs", ctypes.POINTER(ctypes.c_int64)),
                 ("nbr", ctypes.POINTER(ctypes.c_int64)), ("vol", ctypes.POINTER(ctypes.c_double)),
                 ("area", ctypes.POINTER(ctypes.c_double)), ("queue_ms", ctypes.c_double),
-                ("service_ms", ctypes.c_double), ("latency_ms", ctypes.c_double), ("stats", _lib.Stats)]
+                ("service_ms", ctypes.c_double), ("latency_ms", ctypes.c_double), ("stats", _lib.Stats),
+                ("shift", ctypes.POINTER(ctypes.c_int8))]
 
 
 def _bind():
@@ -69,13 +72,30 @@ class Server:
         self._h = h
 
     def submit(self, pts, lo=None, hi=None, integrator=None, ndir=1000, mc_seed=0, method=_lib.HV_METHOD_FAST,
-               **params) -> int:
+               periodic=None, planes=None, **params) -> int:
+        """Queues one mesh request: the box [lo, hi] (default unit cube), with
+        ``periodic`` (d flags) the periodic cuboid, or with ``planes = (base,
+        normal, bc)`` the convex domain of those planes.  The arrays are copied."""
         pts = np.ascontiguousarray(pts, dtype=np.float64)
         n, d = pts.shape
         lo = np.ascontiguousarray(np.zeros(d) if lo is None else lo, dtype=np.float64)
         hi = np.ascontiguousarray(np.ones(d) if hi is None else hi, dtype=np.float64)
         q = _Request(d, n, pts.ctypes.data, lo.ctypes.data, hi.ctypes.data, INTEGRATORS[integrator], ndir, mc_seed,
                      _lib.make_params(method, **params))
+        keep = []
+        if periodic is not None:
+            flags = np.ascontiguousarray([1 if f else 0 for f in periodic], dtype=np.int32)
+            keep.append(flags)
+            q.periodic = flags.ctypes.data
+        if planes is not None:
+            base = np.ascontiguousarray(planes[0], dtype=np.float64)
+            normal = np.ascontiguousarray(planes[1], dtype=np.float64)
+            keep += [base, normal]
+            q.nplanes, q.base, q.normal = base.shape[0], base.ctypes.data, normal.ctypes.data
+            if len(planes) > 2 and planes[2] is not None:
+                bc = np.ascontiguousarray(planes[2], dtype=np.int16)
+                keep.append(bc)
+                q.bc = bc.ctypes.data
         t = ctypes.c_int64()
         rc = _bind().hv_server_submit(self._h, ctypes.byref(q), ctypes.byref(t))
         if rc != _lib.HV_OK:
@@ -106,6 +126,7 @@ class Server:
                 "vol": _arr(r.vol, n, np.float64) if r.vol else None,
                 "area": _arr(r.area, E, np.float64) if r.area else None,
                 "stats": {k: getattr(r.stats, k) for k, _ in _lib.Stats._fields_},
+                "shift": _arr(r.shift, E * d, np.int8).reshape(E, d) if r.shift else None,
             })
         if release:
             L.hv_server_release(self._h, ticket)

@@ -279,6 +279,14 @@ typedef struct {
     int ndir;                /* directions per cell for HV_INTEGRATOR_HEURISTIC_MC */
     uint64_t mc_seed;
     hv_params params;
+    /* Domains beyond the box (a zero-initialised tail keeps the box [lo, hi]):
+     * periodic != NULL: d flags, the periodic cuboid of hv_mesh_build_periodic;
+     * nplanes > 0: the convex domain of hv_mesh_build_planes (lo, hi unused). */
+    const int* periodic;
+    int nplanes;
+    const double* base;      /* d x nplanes */
+    const double* normal;    /* d x nplanes */
+    const int16_t* bc;       /* nplanes boundary conditions, or NULL */
 } hv_request;
 
 typedef struct {
@@ -295,6 +303,7 @@ typedef struct {
     double service_ms;       /* start of service -> result ready */
     double latency_ms;       /* submission -> result ready */
     hv_stats stats;
+    const int8_t* shift;     /* d x nnbr lattice shifts of the neighbours (periodic requests), else NULL */
 } hv_result;
 
 int hv_server_start(const hv_server_config* cfg, hv_server** out);

@@ -66,3 +66,30 @@ def test_admission_budget_serialises_large_requests(gpu_lib):
     with pytest.raises(hvgpu.HVError):
         with Server(slots=2, hbm_budget_bytes=1e6) as s:
             s.submit(D.uniform_points(4, 2000, 1))
+
+
+def test_served_periodic_and_plane_domains(gpu_lib):
+    """Periodic cuboids and plane domains through the server equal the direct builds."""
+    from hvgpu.serve import Server
+    from _domains import simplex, simplex_points
+    hv = gpu_lib
+    X = D.uniform_points(3, 600, 91)
+    base, normal, _ = simplex(3)
+    S = simplex_points(3, 600, 92)
+    with Server(slots=4) as srv:
+        tp = srv.submit(X, integrator="polygon", periodic=[1, 1, 1])
+        ts = srv.submit(S, integrator="polygon", planes=(base, normal, np.zeros(4, dtype=np.int16)))
+        tb = srv.submit(X, integrator="polygon")
+        rp, rs, rb = srv.result(tp), srv.result(ts), srv.result(tb)
+    assert rp["status"] == rs["status"] == rb["status"] == 0
+    mp = hv.Mesh(hv.default_context(), X, np.zeros(3), np.ones(3), hv.make_params(hv.HV_METHOD_FAST),
+                 periodic=[1, 1, 1])
+    np.testing.assert_array_equal(rp["sig"], mp.vertices()[0])
+    np.testing.assert_array_equal(rp["nbr"], mp.neighbors()[1])
+    np.testing.assert_array_equal(rp["shift"], mp.periodic_shifts())
+    np.testing.assert_array_equal(rp["vol"], mp.polygon()[0])
+    assert abs(rp["vol"].sum() - 1.0) < 1e-11
+    ms = hv.Mesh(hv.default_context(), S, None, None, hv.make_params(hv.HV_METHOD_FAST), planes=(base, normal, None))
+    np.testing.assert_array_equal(rs["sig"], ms.vertices()[0])
+    np.testing.assert_array_equal(rs["vol"], ms.polygon()[0])
+    assert rs["shift"] is None and rb["shift"] is None
