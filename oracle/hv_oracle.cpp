@@ -1187,6 +1187,15 @@ void hvo_mc_directions(int d, int64_t cell, int ndir, uint64_t seed, double* dir
     }
 }
 
+// The reference's direction batches (new_directions!, src/mcintegrator.jl:82-95,
+// refreshed every `recycle` cells, :103-107): `abs` is set to 2 once before the
+// loop, so after the first accepted Gaussian vector (|v|^2 <= 1) the rejection
+// loop never runs again and every direction of the batch is that one vector.
+// Off (0) by default; for documenting that estimator only.
+static int g_mc_reference_recycle = 0;
+
+void hvo_set_mc_reference_directions(int recycle) { g_mc_reference_recycle = recycle > 0 ? recycle : 0; }
+
 int hvo_heuristic_mc(const hvo_mesh* m, int ndir, uint64_t seed, int nthreads,
                      double* vol, double* area, double* vol_var, double* area_var) {
     const Problem& P = m->P;
@@ -1221,13 +1230,31 @@ int hvo_heuristic_mc(const hvo_mesh* m, int ndir, uint64_t seed, int nthreads,
         }
         double sv = 0, sv2 = 0;
         std::vector<double> sa(deg, 0.0), sa2(deg, 0.0);
+        double gref[MAXD];
+        if (g_mc_reference_recycle > 0) {  // the batch's one direction
+            const uint64_t batch = (uint64_t)(i / g_mc_reference_recycle);
+            for (uint32_t att = 0;; ++att) {
+                philox_gauss(seed, att, batch, d, gref);
+                double a2 = 0;
+                for (int q = 0; q < d; ++q) a2 += gref[q] * gref[q];
+                if (a2 <= 1.0 && a2 > 0.0) {
+                    const double nn = std::sqrt(a2);
+                    for (int q = 0; q < d; ++q) gref[q] /= nn;
+                    break;
+                }
+            }
+        }
         for (int s = 0; s < ndir; ++s) {
             double g[MAXD];
-            philox_gauss(seed, (uint32_t)s, (uint64_t)i, d, g);
-            double nn = 0;
-            for (int q = 0; q < d; ++q) nn += g[q] * g[q];
-            nn = std::sqrt(nn);
-            for (int q = 0; q < d; ++q) g[q] /= nn;
+            if (g_mc_reference_recycle > 0) {
+                for (int q = 0; q < d; ++q) g[q] = gref[q];
+            } else {
+                philox_gauss(seed, (uint32_t)s, (uint64_t)i, d, g);
+                double nn = 0;
+                for (int q = 0; q < d; ++q) nn += g[q] * g[q];
+                nn = std::sqrt(nn);
+                for (int q = 0; q < d; ++q) g[q] /= nn;
+            }
             // mc_raycast (src/mcintegrator.jl:207-226): t = min over neighbours
             double tb = INFINITY; int jb = -1;
             for (int t = 0; t < deg; ++t) {

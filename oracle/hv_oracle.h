@@ -58,6 +58,11 @@ int hvo_polygon(const hvo_mesh* m, double* vol, double* area);
  * per-cell estimators (sample variance / ndir) before two-sided averaging. */
 int hvo_heuristic_mc(const hvo_mesh* m, int ndir, uint64_t seed, int nthreads,
                      double* vol, double* area, double* vol_var, double* area_var);
+/* recycle > 0: hvo_heuristic_mc uses the reference's direction batches instead
+ * of i.i.d. directions -- one vector for every sample of `recycle` consecutive
+ * cells (new_directions! never resets its rejection flag,
+ * src/mcintegrator.jl:82-95).  0 restores the i.i.d. estimator. */
+void hvo_set_mc_reference_directions(int recycle);
 void hvo_get_stats(const hvo_mesh* m, hvo_stats* st);
 const char* hvo_last_error(void);
 void hvo_free(hvo_mesh* m);

@@ -73,6 +73,7 @@ def lib():
             u32p = ctypes.POINTER(ctypes.c_uint32)
             L.hvo_philox4x32.argtypes = [u32p, u32p, u32p]; L.hvo_philox4x32.restype = None
             L.hvo_mc_directions.argtypes = [I, I64, I, U64, dp]; L.hvo_mc_directions.restype = None
+            L.hvo_set_mc_reference_directions.argtypes = [I]; L.hvo_set_mc_reference_directions.restype = None
             _lib = L
     return _lib
 
@@ -144,8 +145,19 @@ class OracleMesh:
             raise RuntimeError(L.hvo_last_error().decode())
         return vol, area[:E]
 
-    def heuristic_mc(self, ndir, seed, nthreads=0):
+    def heuristic_mc(self, ndir, seed, nthreads=0, reference_directions=0):
+        """i.i.d. directions per cell; ``reference_directions=r`` (> 0) instead
+        reproduces the reference's batches (one direction for every sample of r
+        consecutive cells, src/mcintegrator.jl:82-107), for documentation."""
         L = lib()
+        with _lock:
+            L.hvo_set_mc_reference_directions(int(reference_directions))
+            try:
+                return self._heuristic_mc(L, ndir, seed, nthreads)
+            finally:
+                L.hvo_set_mc_reference_directions(0)
+
+    def _heuristic_mc(self, L, ndir, seed, nthreads):
         E = L.hvo_num_neighbors(self._h)
         vol = np.zeros(self.n)
         area = np.zeros(max(E, 1))

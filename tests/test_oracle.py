@@ -325,3 +325,19 @@ def test_oracle_reproduces_golden(name):
         np.testing.assert_array_equal(out["shift"], ref["shift"])
     np.testing.assert_allclose(out["vol"], ref["vol"], rtol=1e-12, atol=1e-16)
     np.testing.assert_allclose(out["area"], ref["area"], rtol=1e-12, atol=1e-16)
+
+
+def test_reference_mc_directions_are_one_vector_per_batch():
+    """The reference's new_directions! (src/mcintegrator.jl:82-95) keeps one
+    direction for a whole batch of cells: every sample of a cell is the same,
+    so the per-cell variance is zero and the volumes no longer tile the cube,
+    while the i.i.d. estimator does to sampling accuracy."""
+    X = D.uniform_points(3, 400, 9)
+    m = O.OracleMesh(X)
+    v, _, vv, _ = m.heuristic_mc(400, 3)
+    r, _, rv, _ = m.heuristic_mc(400, 3, reference_directions=20)
+    assert abs(v.sum() - 1.0) < 0.02
+    assert np.all(rv <= 1e-12 * r ** 2) and np.all(vv > 1e-6 * v ** 2 / 400)
+    assert abs(r.sum() - 1.0) > 0.05
+    again, _, _, _ = m.heuristic_mc(400, 3)   # the switch is off again
+    np.testing.assert_array_equal(again, v)
