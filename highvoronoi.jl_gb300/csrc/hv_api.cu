@@ -399,6 +399,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         if (overflow) { S.capacity_retries++; continue; }
         V = f1;
         S.levels = levels;
+        if (fast) kt.run(F_CENTERS, 1, [&] { launch_refine_centers(M, V, ctx->nsm, st); });
         break;
     }
     CK(cudaEventRecord(ev.e[2], st));
@@ -464,6 +465,14 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     S.ms_prepare = ms_between(ev.e[0], ev.e[1]);
     S.ms_search = ms_between(ev.e[1], ev.e[2]);
     S.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    // A tie that double-double cannot break means generators in degenerate
+    // position (more than d+1 on one empty sphere, e.g. lattice points): the
+    // reference stores such a vertex with all of them; this search broke the tie
+    // by index, so the mesh is not the Voronoi diagram -- refuse it.
+    if (S.degenerate > 0)
+        throw HvError(HV_E_DEGENERATE, "generators in degenerate position (" + std::to_string(S.degenerate) +
+                                           " exact ties, e.g. more than d+1 points on one empty sphere); "
+                                           "the GPU search needs general position -- perturb the points");
 }
 
 void ensure_neighbors(hv_mesh* m) {

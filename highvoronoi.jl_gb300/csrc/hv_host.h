@@ -53,6 +53,8 @@ void launch_descent(const DevMesh& M, int stride, int nseeds, unsigned long long
 void launch_descent_exact(const DevMesh& M, int maxn, unsigned long long seed, int* failed, unsigned* nfailed,
                           int nsm, cudaStream_t st);
 void launch_centers(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+// residual correction of the ill-conditioned centres after the search (fast method)
+void launch_refine_centers(const DevMesh& M, unsigned V, int nsm, cudaStream_t st);
 void launch_register_edges(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
 void launch_expand_plain(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cudaStream_t st);
 void launch_expand_fast(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq,

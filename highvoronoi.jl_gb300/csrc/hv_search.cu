@@ -10,6 +10,11 @@ void launch_register_d3(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cud
 void launch_register_d4(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
 void launch_register_d5(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
 void launch_register_d6(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+void launch_refine_d2(const DevMesh& M, unsigned V, int nsm, cudaStream_t st);
+void launch_refine_d3(const DevMesh& M, unsigned V, int nsm, cudaStream_t st);
+void launch_refine_d4(const DevMesh& M, unsigned V, int nsm, cudaStream_t st);
+void launch_refine_d5(const DevMesh& M, unsigned V, int nsm, cudaStream_t st);
+void launch_refine_d6(const DevMesh& M, unsigned V, int nsm, cudaStream_t st);
 void launch_centers_d2(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
 void launch_centers_d3(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
 void launch_centers_d4(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
@@ -54,6 +59,16 @@ void launch_register_edges(const DevMesh& M, unsigned v0, unsigned v1, int nsm, 
         case 4: launch_register_d4(M, v0, v1, nsm, st); break;
         case 5: launch_register_d5(M, v0, v1, nsm, st); break;
         case 6: launch_register_d6(M, v0, v1, nsm, st); break;
+        default: break;
+    }
+}
+void launch_refine_centers(const DevMesh& M, unsigned V, int nsm, cudaStream_t st) {
+    switch (M.d) {
+        case 2: launch_refine_d2(M, V, nsm, st); break;
+        case 3: launch_refine_d3(M, V, nsm, st); break;
+        case 4: launch_refine_d4(M, V, nsm, st); break;
+        case 5: launch_refine_d5(M, V, nsm, st); break;
+        case 6: launch_refine_d6(M, V, nsm, st); break;
         default: break;
     }
 }

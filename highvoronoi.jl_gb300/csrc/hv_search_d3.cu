@@ -5,6 +5,7 @@ namespace hv {
 
 void launch_register_d3(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st) { launch_register_t<3>(M, v0, v1, nsm, st); }
 void launch_centers_d3(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st) { launch_centers_t<3>(M, v0, v1, nsm, st); }
+void launch_refine_d3(const DevMesh& M, unsigned V, int nsm, cudaStream_t st) { launch_refine_t<3>(M, V, nsm, st); }
 void launch_descent_d3(const DevMesh& M, int stride, int nseeds, unsigned long long seed, int* failed,                              unsigned* nfailed, int nsm, cudaStream_t st) { launch_descent_t<3>(M, stride, nseeds, seed, failed, nfailed, nsm, st); }
 void launch_plain_d3(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cudaStream_t st) { launch_plain_t<3>(M, f0, f1, nsm, st); }
 void launch_fast_d3(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq,                           unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm,                           cudaStream_t st) { launch_fast_t<3>(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap, nsm, st); }

@@ -155,8 +155,9 @@ __device__ __forceinline__ bool q_excluded(const Query<D>& q, int it) {
     return ex;
 }
 
+// FP64 interval of generator j's crossing parameter; false if the ray moves away from it.
 template <int D>
-__device__ __forceinline__ void eval_point(const DevMesh& M, const Query<D>& q, int j, SearchOut& R) {
+__device__ __forceinline__ bool cand_point(const DevMesh& M, const Query<D>& q, int j, Cand& c) {
     const double* xj = M.pts + (size_t)j * D;
     double nd = 0, dr = 0, du = 0, sdr = 0, sdu = 0, l1 = 0;
 #pragma unroll
@@ -169,26 +170,34 @@ __device__ __forceinline__ void eval_point(const DevMesh& M, const Query<D>& q, 
     double den = 2.0 * (du - q.lam);
     double e_num = (4.0 * D + 8.0) * EPS64 * (nd + 2.0 * sdr) + 2.0 * l1 * q.erho;
     double e_den = (2.0 * D + 8.0) * EPS64 * 2.0 * (sdu + fabs(q.lam)) + 4.0 * l1 * q.eu;
-    Cand c; c.item = j;
+    c.item = j;
     if (den > e_den) {
         c.t = num / den;
         double et = (e_num + fabs(c.t) * e_den) / (den - e_den) + 4.0 * EPS64 * fabs(c.t);
         c.lo = c.t - et; c.hi = c.t + et;
     } else if (den < -e_den) {
-        return;
+        return false;
     } else {
         if (num - e_num > 0) {
-            if (!(den + e_den > 0)) return;
+            if (!(den + e_den > 0)) return false;
             c.lo = (num - e_num) / (den + e_den); c.hi = INFINITY; c.t = c.lo;
         } else {
             c.lo = -INFINITY; c.hi = INFINITY; c.t = 0;
         }
     }
-    if (c.lo < R.best.hi || c.lo < R.second_lo) consider(R, c);
+    return true;
 }
 
 template <int D>
-__device__ __forceinline__ void eval_planes(const DevMesh& M, const Query<D>& q, SearchOut& R) {
+__device__ __forceinline__ void eval_point(const DevMesh& M, const Query<D>& q, int j, SearchOut& R) {
+    Cand c;
+    if (!cand_point<D>(M, q, j, c)) return;
+    if (c.lo < R.best.hi || c.lo < R.second_lo) consider(R, c);
+}
+
+// FP64 intervals of the boundary planes' crossings: sink(Cand) for each plane the ray approaches.
+template <int D, class Sink>
+__device__ __forceinline__ void cand_planes(const DevMesh& M, const Query<D>& q, Sink&& sink) {
 #pragma unroll
     for (int p = 0; p < M.np; ++p) {
         const int it = M.n + p;
@@ -234,8 +243,13 @@ __device__ __forceinline__ void eval_planes(const DevMesh& M, const Query<D>& q,
             if (num - e_num > 0) { c.lo = (num - e_num) / (fabs(uk) + e_den); c.hi = INFINITY; c.t = c.lo; }
             else { c.lo = -INFINITY; c.hi = INFINITY; c.t = 0; }
         }
-        consider(R, c);
+        sink(c);
     }
+}
+
+template <int D>
+__device__ __forceinline__ void eval_planes(const DevMesh& M, const Query<D>& q, SearchOut& R) {
+    cand_planes<D>(M, q, [&](const Cand& c) { consider(R, c); });
 }
 
 template <int D>
@@ -316,6 +330,46 @@ __device__ void exact_search(const DevMesh& M, const Query<D>& q, SearchOut& R) 
     for (int k = 0; k < R.namb; ++k)
         if (R.amb[k].item != R.best.item && R.amb[k].lo <= R.best.hi) R.amb[w++] = R.amb[k];
     R.namb = w;
+}
+
+// Every item whose FP64 interval starts at or below H (planes, then the tree
+// with the ball of parameter H): visit(item).  Used when more candidates than
+// HV_NAMB tie with the winner within FP64 (near-degenerate generators).
+template <int D, class Visit>
+__device__ void exact_visit(const DevMesh& M, const Query<D>& q, double H, Visit&& visit) {
+    cand_planes<D>(M, q, [&](const Cand& c) { if (c.lo <= H) visit(c.item); });
+    const double tpp = H * (1.0 + 1e-9) + 1e-300;
+    double c[D];
+    double r2 = 0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const double off = q.rho[k] + tpp * q.u[k];
+        c[k] = q.xa[k] + off;
+        const double w = q.db[k] - off;
+        r2 = fma(w, w, r2);
+    }
+    r2 = r2 * (1.0 + 1e-9) + 1e-280;
+    int stack[64];
+    int sp = 0;
+    stack[sp++] = 1;
+    while (sp > 0) {
+        const int node = stack[--sp];
+        if (box_dist2<D>(M, node, c) > r2) continue;
+        if (node >= M.P) {
+            const int l = node - M.P;
+            if (l >= M.nleaves) continue;
+            const int s0 = l * M.leaf, s1 = min(s0 + M.leaf, M.n);
+            for (int j = s0; j < s1; ++j) {
+                if (q_excluded<D>(q, j)) continue;
+                Cand cj;
+                if (cand_point<D>(M, q, j, cj) && cj.lo <= H) visit(j);
+            }
+        } else {
+            if (sp + 2 > 64) { set_status(M, ST_STACK); return; }
+            stack[sp++] = 2 * node + 1;
+            stack[sp++] = 2 * node;
+        }
+    }
 }
 
 // Is any real generator outside S strictly inside the sphere (c, r2)?
@@ -576,12 +630,34 @@ __device__ void exact_walk(const DevMesh& M, unsigned v, int m) {
     int win = R.best.item;
     if (!(R.best.hi < R.second_lo)) {
         count_add(M.cnt + C_DD);
-        if (R.overflow) set_status(M, ST_AMB);
         int items[HV_NAMB + 1];
-        items[0] = R.best.item;
-        for (int k = 0; k < R.namb; ++k) items[k + 1] = R.amb[k].item;
         bool degen = false;
-        win = dd_rescore_walk<D>(M, sig, m, items, R.namb + 1, degen);
+        if (!R.overflow) {
+            items[0] = R.best.item;
+            for (int k = 0; k < R.namb; ++k) items[k + 1] = R.amb[k].item;
+            win = dd_rescore_walk<D>(M, sig, m, items, R.namb + 1, degen);
+        } else {
+            // more near-ties than the set holds: every item whose interval reaches
+            // below the winner's upper bound is re-scored in double-double, HV_NAMB
+            // at a time against the running winner
+            int nb = 0;
+            auto flush = [&]() {
+                items[0] = win;
+                bool d2 = false;
+                const int w2 = dd_rescore_walk<D>(M, sig, m, items, nb + 1, d2);
+                if (w2 >= 0) {  // a tie counts while its winner stands
+                    degen = (w2 == win) ? (degen || d2) : d2;
+                    win = w2;
+                }
+                nb = 0;
+            };
+            exact_visit<D>(M, q, R.best.hi, [&](int it) {
+                if (it == win) return;
+                items[1 + nb++] = it;
+                if (nb == HV_NAMB) flush();
+            });
+            if (nb > 0) flush();
+        }
         if (degen) { count_add(M.cnt + C_DEGEN); set_status(M, ST_DEGEN); }
         if (win < 0) { set_status(M, ST_NUMERIC); return; }
     }
@@ -737,6 +813,7 @@ __global__ void __launch_bounds__(128) k_descent(DevMesh M, int stride, int nsee
             if (R.best.item < 0) { ok = false; break; }
             int win = R.best.item;
             double t = R.best.t;
+            if (!(R.best.hi < R.second_lo) && R.overflow) { ok = false; break; }  // near-degenerate step: retry
             if (!(R.best.hi < R.second_lo)) {
                 int items[HV_NAMB + 1];
                 items[0] = R.best.item;
@@ -907,6 +984,48 @@ __device__ __forceinline__ void lu_solve_rcp(const double (&A)[D][D], const int 
 #pragma unroll
         for (int k = r + 1; k < D; ++k) b[r] = fma(-A[r][k], b[k], b[r]);
         b[r] *= rd[r];
+    }
+}
+
+// Residual correction of the ill-conditioned centres (near-degenerate
+// generators; condition estimate above 1e6), after the search: r = b - A rho
+// with the exact rows and right-hand sides in double-double, then A delta = r
+// with the FP64 factors, twice -- the double-double residual step of the
+// reference's high-precision vertex correction (src/raycast.jl:633-707).  Only
+// the output coordinates need it: the search itself decides from the signature.
+template <int D>
+__global__ void __launch_bounds__(128) k_refine_centers(DevMesh M, unsigned V) {
+    for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        if (!(M.vcond[v] > 1e6f)) continue;
+        int s[D + 1];
+#pragma unroll
+        for (int k = 0; k <= D; ++k) s[k] = M.vsig[(size_t)v * (D + 1) + k];
+        double xa[D], A[D][D], rho[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) xa[k] = M.pts[(size_t)s[0] * D + k];
+#pragma unroll
+        for (int r = 0; r < D; ++r) con_row<D, double>(M, xa, s[r + 1], A[r], rho[r]);
+        int piv[D];
+        double rd[D];
+        if (!lu_factor_rcp<D>(A, piv, rd)) continue;
+        lu_solve_rcp<D>(A, piv, rd, rho);
+#pragma unroll 1
+        for (int it = 0; it < 2; ++it) {
+            double r[D];
+#pragma unroll
+            for (int row = 0; row < D; ++row) {
+                dd rw[D], rh;
+                con_row<D, dd>(M, xa, s[row + 1], rw, rh);
+#pragma unroll
+                for (int k = 0; k < D; ++k) rh = rh - rw[k] * mk(rho[k]);
+                r[row] = rh.hi + rh.lo;
+            }
+            lu_solve_rcp<D>(A, piv, rd, r);
+#pragma unroll
+            for (int k = 0; k < D; ++k) rho[k] += r[k];
+        }
+#pragma unroll
+        for (int k = 0; k < D; ++k) M.vc[(size_t)v * D + k] = xa[k] + rho[k];
     }
 }
 
@@ -1518,8 +1637,8 @@ __device__ int exact_decide_set(const DevMesh& M, const int (&sig)[D + 1], int m
     if (planes) eval_planes<D>(M, q, R);
     if (R.best.item < 0) return -1;
     if (R.best.hi < R.second_lo) return R.best.item;
+    if (R.overflow) return -1;  // more near-ties than the set holds: the exact tree search decides
     count_add(M.cnt + C_DD);
-    if (R.overflow) set_status(M, ST_AMB);
     int its[HV_NAMB + 1];
     its[0] = R.best.item;
     int w = 1;
@@ -1935,9 +2054,10 @@ __global__ void __launch_bounds__(DS_WPB * 32) k_decide_sets(DevMesh M, AmbQueue
                 if (Rs.best.item >= 0) {
                     if (Rs.best.hi < Rs.second_lo) {
                         win = Rs.best.item;
+                    } else if (Rs.overflow) {
+                        win = -1;  // more near-ties than the set holds: the exact tree search decides
                     } else {
                         count_add(M.cnt + C_DD);
-                        if (Rs.overflow) set_status(M, ST_AMB);
                         int its[HV_NAMB + 1];
                         its[0] = Rs.best.item;
                         int n2 = 1;
@@ -2171,6 +2291,13 @@ static void launch_register_t(const DevMesh& M, unsigned v0, unsigned v1, int ns
     unsigned long long blocks = (total + 255) / 256;
     if (blocks > (unsigned long long)nsm * 32) blocks = (unsigned long long)nsm * 32;
     k_register_edges<D><<<(unsigned)blocks, 256, 0, st>>>(M, v0, v1);
+}
+template <int D>
+static void launch_refine_t(const DevMesh& M, unsigned V, int nsm, cudaStream_t st) {
+    if (!V || !M.vcond) return;
+    unsigned blocks = (V + 127) / 128;
+    if (blocks > (unsigned)nsm * 16) blocks = (unsigned)nsm * 16;
+    k_refine_centers<D><<<blocks, 128, 0, st>>>(M, V);
 }
 template <int D>
 static void launch_centers_t(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st) {

@@ -275,6 +275,22 @@ VertexSys solve_vertex(const Problem& P, const int* S) {
     for (int r = 0; r < d; ++r) { double s = 0; for (int k = 0; k < d; ++k) s += std::fabs(V.Minv[r][k]); ninv = std::max(ninv, s); }
     V.cond = nrm * ninv;
     V.ok = std::isfinite(V.cond);
+    // ill-conditioned centre (near-degenerate generators): two residual
+    // corrections with the residual in binary128 (the reference corrects such
+    // vertices with a Double64 residual, src/raycast.jl:633-707)
+    if (V.ok && V.cond > 1e6) {
+        for (int it = 0; it < 2; ++it) {
+            double r[MAXD];
+            for (int row = 0; row < d; ++row) {
+                qreal rw[MAXD], rh;
+                constraint_row<qreal>(P, a, S[row + 1], rw, rh);
+                for (int k = 0; k < d; ++k) rh -= rw[k] * (qreal)V.rho[k];
+                r[row] = (double)rh;
+            }
+            lu_solve<double>(d, A, piv, r);
+            for (int k = 0; k < d; ++k) V.rho[k] += r[k];
+        }
+    }
     return V;
 }
 

@@ -176,3 +176,32 @@ def test_autotune_keeps_the_vertex_set(gpu_lib):
     geo = hv.VoronoiGeometry(pts, hv.cuboid(3, periodic=[]), search_settings=dict(method=hv.RCGPU, autotune=True),
                              context=ctx)
     np.testing.assert_array_equal(geo.mesh.vertices()[0], m.vertices()[0])
+
+
+def _grid(d, k):
+    g = (np.arange(k) + 0.5) / k
+    return np.array(np.meshgrid(*([g] * d), indexing="ij")).reshape(d, -1).T.copy()
+
+
+@pytest.mark.parametrize("d,k", [(2, 6), (3, 4)])
+def test_lattice_points_are_refused(gpu_lib, d, k):
+    """Lattice points put more than d+1 generators on one empty sphere; the
+    reference stores such vertices with all of them, this search would have to
+    break the ties by index -- it returns HV_E_DEGENERATE instead of a wrong mesh."""
+    hv = gpu_lib
+    with pytest.raises(hv.HVError) as e:
+        _build(hv, _grid(d, k), hv.HV_METHOD_FAST)
+    assert e.value.code == hv._lib.HV_E_DEGENERATE
+    _compare(hv, D.uniform_points(2, 30, 3), hv.HV_METHOD_FAST)  # the context stays usable
+
+
+@pytest.mark.parametrize("d,k,eps", [(2, 20, 1e-9), (3, 8, 1e-9), (4, 4, 1e-8), (3, 6, 1e-12)])
+def test_near_lattice_points(gpu_lib, d, k, eps):
+    """Lattice points moved by tiny amounts: many near-ties per ray, decided
+    exactly (double-double over every near-tied candidate); bit-exact against the
+    oracle (binary128) and the volumes tile the cube."""
+    hv = gpu_lib
+    X = _grid(d, k) + eps * np.random.default_rng(d).uniform(-1, 1, (k ** d, d))
+    m, st = _compare(hv, X, hv.HV_METHOD_FAST)
+    v, _ = m.polygon()
+    assert abs(v.sum() - 1.0) < 1e-11
