@@ -32,9 +32,11 @@
 struct hv_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;  // the fallback ladder of a level, beside the next level's expansion
+    cudaEvent_t ovl_ev[3] = {};      // expansion done, fallback done (two parities); no timing
     int nsm = 1;
     std::string err;
-    unsigned* h_stat = nullptr;  // pinned: vcount, status, nfq, pad
+    unsigned* h_stat = nullptr;  // pinned: vcount, status, queue length, pad
     std::vector<cudaEvent_t> evpool;  // timing events, reused across builds
     std::map<std::pair<int, int>, hv_params> tuned;  // autotuner results per (d, log2 n)
 };
@@ -175,11 +177,13 @@ struct KTimer {
         return ctx->evpool[used++];
     }
     template <class F>
-    void run(int fam, int nlaunch, F&& f) {
+    void run(int fam, int nlaunch, F&& f) { run_on(ctx->stream, fam, nlaunch, f); }
+    template <class F>
+    void run_on(cudaStream_t s, int fam, int nlaunch, F&& f) {
         const int i0 = (int)used;
-        CK(cudaEventRecord(next(), ctx->stream));
+        CK(cudaEventRecord(next(), s));
         f();
-        CK(cudaEventRecord(next(), ctx->stream));
+        CK(cudaEventRecord(next(), s));
         spans.emplace_back(fam, i0);
         launches += nlaunch;
     }
@@ -193,8 +197,20 @@ struct KTimer {
     }
 };
 
+// vertex count and status word into h_stat[0..1] (h_stat[2..3] are the caller's)
+// Queued rays per SM above which a level's fallback ladder is not overlapped with
+// the next expansion (HV_OVERLAP_RAYS_PER_SM overrides, for tuning).
+int overlap_rays_per_sm() {
+    static const int v = [] {
+        const char* e = std::getenv("HV_OVERLAP_RAYS_PER_SM");
+        const int x = e ? std::atoi(e) : 0;
+        return x > 0 ? x : 128;
+    }();
+    return v;
+}
+
 void read_stat(hv_ctx* ctx, const unsigned* dstat) {
-    CK(cudaMemcpyAsync(ctx->h_stat, dstat, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->h_stat, dstat, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
 }
 
@@ -310,6 +326,12 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     int stride = mesh->prm.seed_stride > 0 ? mesh->prm.seed_stride : default_seed_stride(n);
     const int nseeds = (n + stride - 1) / stride;
     std::unique_ptr<Scratch> srch;
+    // the second stream's kernels use the search scratch: drain it before that is freed
+    // (also when an error unwinds the build)
+    struct Drain {
+        cudaStream_t s;
+        ~Drain() { cudaStreamSynchronize(s); }
+    } drain{ctx->stream2};
     unsigned V = 0;
     for (int attempt = 0;; ++attempt) {
         if (attempt > 4) throw HvError(HV_E_CAPACITY, "vertex capacity retries exhausted");
@@ -340,8 +362,16 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
             CK(cudaMemsetAsync(M.ehash, 0, sizeof(unsigned long long) * esize, st));
         }
         const unsigned fqcap = std::max(65536u, vcap / 2);
-        unsigned long long* fq = fast ? srch->get<unsigned long long>(fqcap) : nullptr;  // insecure rays
-        unsigned long long* fx = fast ? srch->get<unsigned long long>(fqcap) : nullptr;  // uncertified rays
+        // insecure rays (fq) and rays for the exact search (fx), one pair per level
+        // parity: the ladder of level L drains its pair while level L+1 fills the other
+        unsigned long long* fqs[2] = {nullptr, nullptr};
+        unsigned long long* fxs[2] = {nullptr, nullptr};
+        if (fast)
+            for (int p = 0; p < 2; ++p) {
+                fqs[p] = srch->get<unsigned long long>(fqcap);
+                fxs[p] = srch->get<unsigned long long>(fqcap);
+            }
+        unsigned* qc = fast ? srch->get<unsigned>(4) : nullptr;  // nfq, nfx per parity
         hv::AmbQueue aq{};  // ambiguous candidate sets of the FP32 tree search
         if (fast) {
             aq.cap = fqcap;
@@ -372,21 +402,74 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         unsigned f0 = 0, f1 = std::min(ctx->h_stat[0], vcap);
         if (!overflow) kt.run(F_CENTERS, 1, [&] { launch_centers(M, 0, f1, ctx->nsm, st); });
         long long levels = 0;
-        while (!overflow && f1 > f0) {
-            if (dedup) kt.run(F_OTHER, 1, [&] { launch_register_edges(M, f0, f1, ctx->nsm, st); });
-            if (fast) {
-                CK(cudaMemsetAsync(dstat + 2, 0, 3 * sizeof(unsigned), st));
+        if (fast) {
+            // Level L expands [f0, f1) on the context's stream; its fallback ladder
+            // (tree search, set decisions, exact search) runs on the second stream
+            // beside the expansion of level L+1.  The vertices that ladder finds join
+            // the frontier of level L+2, whose range is read once it has finished.
+            // Overlap pays while a ladder is latency-bound (a few rays per SM); a
+            // ladder of more than 128 rays per SM (clustered data) is work-bound and
+            // would only contend with the expansion, so the next level waits for it.
+            cudaStream_t st2 = ctx->stream2;
+            cudaEvent_t ev_exp = ctx->ovl_ev[0];
+            bool pend = false;
+            int pend_par = 0;
+            for (int L = 0; !overflow; ++L) {
+                if (f1 == f0) {
+                    if (!pend) break;
+                    CK(cudaStreamWaitEvent(st, ctx->ovl_ev[1 + pend_par], 0));
+                    pend = false;
+                    read_stat(ctx, dstat);
+                    if (ctx->h_stat[1] & overflow_bits) { overflow = true; break; }
+                    check_fatal(ctx->h_stat[1]);
+                    const unsigned e = std::min(ctx->h_stat[0], vcap);
+                    if (e == f1) break;
+                    kt.run(F_CENTERS, 1, [&] { launch_centers(M, f1, e, ctx->nsm, st); });
+                    f0 = f1; f1 = e;
+                    continue;
+                }
+                const int p = L & 1;
+                if (dedup) kt.run(F_OTHER, 1, [&] { launch_register_edges(M, f0, f1, ctx->nsm, st); });
+                CK(cudaMemsetAsync(qc + 2 * p, 0, 2 * sizeof(unsigned), st));
                 kt.run(F_EXPAND, 1, [&] {
-                    launch_expand_fast(M, f0, f1, fq, dstat + 2, fqcap, fx, dstat + 3, fqcap, ctx->nsm, st);
+                    launch_expand_fast(M, f0, f1, fqs[p], qc + 2 * p, fqcap, fxs[p], qc + 2 * p + 1, fqcap,
+                                       ctx->nsm, st);
                 });
-                const unsigned long long maxq = std::min<unsigned long long>(fqcap, (unsigned long long)(f1 - f0) * (d + 1));
-                kt.run(F_FALLBACK, 3, [&] {
-                    launch_fallback_warp(M, fq, dstat + 2, fqcap, (unsigned)maxq, fx, dstat + 3, fqcap, aq, ctx->nsm, st);
-                    launch_fallback(M, fx, dstat + 3, (unsigned)maxq, ctx->nsm, st);
+                CK(cudaEventRecord(ev_exp, st));
+                CK(cudaStreamWaitEvent(st2, ev_exp, 0));
+                const unsigned long long maxq =
+                    std::min<unsigned long long>(fqcap, (unsigned long long)(f1 - f0) * (d + 1));
+                CK(cudaMemsetAsync(aq.count, 0, sizeof(unsigned), st2));
+                kt.run_on(st2, F_FALLBACK, 3, [&] {
+                    launch_fallback_warp(M, fqs[p], qc + 2 * p, fqcap, (unsigned)maxq, fxs[p], qc + 2 * p + 1,
+                                         fqcap, aq, ctx->nsm, st2);
+                    launch_fallback(M, fxs[p], qc + 2 * p + 1, (unsigned)maxq, ctx->nsm, st2);
                 });
-            } else {
-                kt.run(F_EXPAND, 1, [&] { launch_expand_plain(M, f0, f1, ctx->nsm, st); });
+                CK(cudaEventRecord(ctx->ovl_ev[1 + p], st2));
+                CK(cudaGetLastError());
+                if (pend) CK(cudaStreamWaitEvent(st, ctx->ovl_ev[1 + pend_par], 0));
+                CK(cudaMemcpyAsync(ctx->h_stat + 2, qc + 2 * p, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+                read_stat(ctx, dstat);
+                if (ctx->h_stat[1] & overflow_bits) { overflow = true; break; }
+                check_fatal(ctx->h_stat[1]);
+                if (ctx->h_stat[2] > (unsigned)overlap_rays_per_sm() * (unsigned)ctx->nsm) {  // work-bound: no overlap
+                    CK(cudaStreamWaitEvent(st, ctx->ovl_ev[1 + p], 0));
+                    read_stat(ctx, dstat);
+                    if (ctx->h_stat[1] & overflow_bits) { overflow = true; break; }
+                    check_fatal(ctx->h_stat[1]);
+                }
+                const unsigned e = std::min(ctx->h_stat[0], vcap);
+                kt.run(F_CENTERS, 1, [&] { launch_centers(M, f1, e, ctx->nsm, st); });
+                f0 = f1; f1 = e;
+                pend = true;
+                pend_par = p;
+                ++levels;
             }
+            CK(cudaStreamSynchronize(st2));
+        }
+        while (!fast && !overflow && f1 > f0) {
+            if (dedup) kt.run(F_OTHER, 1, [&] { launch_register_edges(M, f0, f1, ctx->nsm, st); });
+            kt.run(F_EXPAND, 1, [&] { launch_expand_plain(M, f0, f1, ctx->nsm, st); });
             CK(cudaGetLastError());
             read_stat(ctx, dstat);
             if (ctx->h_stat[1] & overflow_bits) { overflow = true; break; }
@@ -803,9 +886,16 @@ int hv_ctx_create(int device, hv_ctx** out) {
     c->device = device;
     if (cudaSetDevice(device) != cudaSuccess) { delete c; return HV_E_CUDA; }
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return HV_E_CUDA; }
+    if (cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return HV_E_CUDA;
+    }
+    for (auto& e : c->ovl_ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
     if (cudaMallocHost((void**)&c->h_stat, 4 * sizeof(unsigned)) != cudaSuccess) {
         cudaStreamDestroy(c->stream);
+        cudaStreamDestroy(c->stream2);
         delete c;
         return HV_E_CUDA;
     }
@@ -824,6 +914,10 @@ int hv_ctx_destroy(hv_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     cudaFreeHost(ctx->h_stat);
     for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->ovl_ev)
+        if (e) cudaEventDestroy(e);
+    cudaStreamSynchronize(ctx->stream2);
+    cudaStreamDestroy(ctx->stream2);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return HV_OK;
