@@ -33,7 +33,8 @@ struct hv_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;  // the fallback ladder of a level, beside the next level's expansion
-    cudaEvent_t ovl_ev[3] = {};      // expansion done, fallback done (two parities); no timing
+    cudaStream_t stream3 = nullptr;  // the edge registry of a frontier, beside its circumcentres
+    cudaEvent_t ovl_ev[4] = {};      // expansion done, fallback done (two parities), registry done; no timing
     int nsm = 1;
     std::string err;
     unsigned* h_stat = nullptr;  // pinned: vcount, status, queue length, pad
@@ -329,9 +330,12 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     // the second stream's kernels use the search scratch: drain it before that is freed
     // (also when an error unwinds the build)
     struct Drain {
-        cudaStream_t s;
-        ~Drain() { cudaStreamSynchronize(s); }
-    } drain{ctx->stream2};
+        cudaStream_t s2, s3;
+        ~Drain() {
+            cudaStreamSynchronize(s2);
+            cudaStreamSynchronize(s3);
+        }
+    } drain{ctx->stream2, ctx->stream3};
     unsigned V = 0;
     for (int attempt = 0;; ++attempt) {
         if (attempt > 4) throw HvError(HV_E_CAPACITY, "vertex capacity retries exhausted");
@@ -410,10 +414,27 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
             // Overlap pays while a ladder is latency-bound (a few rays per SM); a
             // ladder of more than 128 rays per SM (clustered data) is work-bound and
             // would only contend with the expansion, so the next level waits for it.
-            cudaStream_t st2 = ctx->stream2;
-            cudaEvent_t ev_exp = ctx->ovl_ev[0];
+            cudaStream_t st2 = ctx->stream2, st3 = ctx->stream3;
+            cudaEvent_t ev_exp = ctx->ovl_ev[0], ev_reg = ctx->ovl_ev[3];
             bool pend = false;
             int pend_par = 0;
+            // a new frontier [a, b): circumcentres on the main stream, the edge registry
+            // beside them (both read only the signatures); the expansion waits for both
+            static const bool side_registry = [] {
+                const char* e = std::getenv("HV_EDGE_STREAM");
+                return !(e && e[0] == '0');
+            }();
+            auto prepare = [&](unsigned a, unsigned b, bool centers) {
+                if (centers) kt.run(F_CENTERS, 1, [&] { launch_centers(M, a, b, ctx->nsm, st); });
+                if (dedup && !side_registry) {
+                    kt.run(F_OTHER, 1, [&] { launch_register_edges(M, a, b, ctx->nsm, st); });
+                } else if (dedup) {
+                    kt.run_on(st3, F_OTHER, 1, [&] { launch_register_edges(M, a, b, ctx->nsm, st3); });
+                    CK(cudaEventRecord(ev_reg, st3));
+                    CK(cudaStreamWaitEvent(st, ev_reg, 0));
+                }
+            };
+            if (!overflow) prepare(f0, f1, false);  // the seeds' centres are queued already
             for (int L = 0; !overflow; ++L) {
                 if (f1 == f0) {
                     if (!pend) break;
@@ -424,12 +445,11 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
                     check_fatal(ctx->h_stat[1]);
                     const unsigned e = std::min(ctx->h_stat[0], vcap);
                     if (e == f1) break;
-                    kt.run(F_CENTERS, 1, [&] { launch_centers(M, f1, e, ctx->nsm, st); });
+                    prepare(f1, e, true);
                     f0 = f1; f1 = e;
                     continue;
                 }
                 const int p = L & 1;
-                if (dedup) kt.run(F_OTHER, 1, [&] { launch_register_edges(M, f0, f1, ctx->nsm, st); });
                 CK(cudaMemsetAsync(qc + 2 * p, 0, 2 * sizeof(unsigned), st));
                 kt.run(F_EXPAND, 1, [&] {
                     launch_expand_fast(M, f0, f1, fqs[p], qc + 2 * p, fqcap, fxs[p], qc + 2 * p + 1, fqcap,
@@ -459,13 +479,14 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
                     check_fatal(ctx->h_stat[1]);
                 }
                 const unsigned e = std::min(ctx->h_stat[0], vcap);
-                kt.run(F_CENTERS, 1, [&] { launch_centers(M, f1, e, ctx->nsm, st); });
+                prepare(f1, e, true);
                 f0 = f1; f1 = e;
                 pend = true;
                 pend_par = p;
                 ++levels;
             }
             CK(cudaStreamSynchronize(st2));
+            CK(cudaStreamSynchronize(st3));
         }
         while (!fast && !overflow && f1 > f0) {
             if (dedup) kt.run(F_OTHER, 1, [&] { launch_register_edges(M, f0, f1, ctx->nsm, st); });
@@ -886,8 +907,10 @@ int hv_ctx_create(int device, hv_ctx** out) {
     c->device = device;
     if (cudaSetDevice(device) != cudaSuccess) { delete c; return HV_E_CUDA; }
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return HV_E_CUDA; }
-    if (cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream3, cudaStreamNonBlocking) != cudaSuccess) {
         cudaStreamDestroy(c->stream);
+        if (c->stream2) cudaStreamDestroy(c->stream2);
         delete c;
         return HV_E_CUDA;
     }
@@ -896,6 +919,7 @@ int hv_ctx_create(int device, hv_ctx** out) {
     if (cudaMallocHost((void**)&c->h_stat, 4 * sizeof(unsigned)) != cudaSuccess) {
         cudaStreamDestroy(c->stream);
         cudaStreamDestroy(c->stream2);
+        cudaStreamDestroy(c->stream3);
         delete c;
         return HV_E_CUDA;
     }
@@ -917,7 +941,9 @@ int hv_ctx_destroy(hv_ctx* ctx) {
     for (cudaEvent_t e : ctx->ovl_ev)
         if (e) cudaEventDestroy(e);
     cudaStreamSynchronize(ctx->stream2);
+    cudaStreamSynchronize(ctx->stream3);
     cudaStreamDestroy(ctx->stream2);
+    cudaStreamDestroy(ctx->stream3);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return HV_OK;
