@@ -33,6 +33,14 @@ constexpr double EPS64 = 1.1102230246251565e-16;
 // ---------------------------------------------------------------------------
 // vertex hash
 // ---------------------------------------------------------------------------
+// A slot read with acquire semantics: a published id orders the reads of its
+// record after it (the writer fences before publishing).
+__device__ __forceinline__ unsigned long long load_acquire(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
 template <int D>
 __device__ unsigned vertex_insert(const DevMesh& M, const int (&s)[D + 1], int newitem, bool& is_new) {
     is_new = false;
@@ -40,7 +48,7 @@ __device__ unsigned vertex_insert(const DevMesh& M, const int (&s)[D + 1], int n
     const unsigned fp = ((unsigned)(h >> 32) & 0x7FFFFFFFu) | 1u;
     unsigned long long slot = h & M.vhmask;
     for (unsigned long long probe = 0; probe <= M.vhmask; ++probe) {
-        unsigned long long e = *(volatile unsigned long long*)&M.vhash[slot];
+        unsigned long long e = load_acquire(&M.vhash[slot]);
         if (e == HASH_EMPTY) {
             unsigned long long prev = atomicCAS(&M.vhash[slot], HASH_EMPTY, HASH_BUSY);
             if (prev == HASH_EMPTY) {
@@ -58,18 +66,17 @@ __device__ unsigned vertex_insert(const DevMesh& M, const int (&s)[D + 1], int n
                 is_new = true;
                 return vid;
             }
-            e = prev;
+            e = load_acquire(&M.vhash[slot]);  // taken meanwhile: read it with acquire semantics
         }
         int spins = 0;
         while (e == HASH_BUSY) {
             if (++spins > SPIN_LIMIT) { set_status(M, ST_TIMEOUT); return INVALID_ID; }
             __nanosleep(32);
-            e = *(volatile unsigned long long*)&M.vhash[slot];
+            e = load_acquire(&M.vhash[slot]);
         }
         if ((unsigned)(e >> 32) == fp) {
             unsigned id = (unsigned)e;
             if (id != INVALID_ID) {
-                __threadfence();
                 bool eq = true;
 #pragma unroll
                 for (int k = 0; k <= D; ++k) eq &= (__ldcg(&M.vsig[(size_t)id * (D + 1) + k]) == s[k]);
