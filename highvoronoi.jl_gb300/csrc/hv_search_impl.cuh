@@ -40,6 +40,10 @@ __device__ __forceinline__ unsigned long long load_acquire(const unsigned long l
     asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
+// Publication of a slot this thread owns (BUSY): its record's writes before it.
+__device__ __forceinline__ void store_release(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 
 template <int D>
 __device__ unsigned vertex_insert(const DevMesh& M, const int (&s)[D + 1], int newitem, bool& is_new) {
@@ -61,8 +65,7 @@ __device__ unsigned vertex_insert(const DevMesh& M, const int (&s)[D + 1], int n
 #pragma unroll
                 for (int k = 0; k <= D; ++k) M.vsig[(size_t)vid * (D + 1) + k] = s[k];
                 M.vnew[vid] = newitem;
-                __threadfence();
-                atomicExch(&M.vhash[slot], ((unsigned long long)fp << 32) | vid);
+                store_release(&M.vhash[slot], ((unsigned long long)fp << 32) | vid);
                 is_new = true;
                 return vid;
             }
