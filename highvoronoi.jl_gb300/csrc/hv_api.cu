@@ -34,7 +34,7 @@ struct hv_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;  // the fallback ladder of a level, beside the next level's expansion
     cudaStream_t stream3 = nullptr;  // the edge registry of a frontier, beside its circumcentres
-    cudaEvent_t ovl_ev[4] = {};      // expansion done, fallback done (two parities), registry done; no timing
+    cudaEvent_t ovl_ev[6] = {};      // expansion, fallback (two parities), registry, lists of the non-seeds; no timing
     int nsm = 1;
     std::string err;
     unsigned* h_stat = nullptr;  // pinned: vcount, status, queue length, pad
@@ -248,6 +248,15 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         return;
     }
     Scratch prep(st);
+    // the side streams' kernels use this build's scratch: drain them before it is
+    // freed (also when an error unwinds the build)
+    struct Drain {
+        cudaStream_t s2, s3;
+        ~Drain() {
+            cudaStreamSynchronize(s2);
+            cudaStreamSynchronize(s3);
+        }
+    } drain{ctx->stream2, ctx->stream3};
     unsigned* dstat = prep.get<unsigned>(8);  // vcount, status, insecure queue, exact queue, ambiguous sets
     unsigned long long* dcnt = prep.get<unsigned long long>(C_NCOUNT);
     CK(cudaMemsetAsync(dstat, 0, 8 * sizeof(unsigned), st));
@@ -311,11 +320,22 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     K = std::min(K, std::max(n - 1, 0));
     K = std::min(K, 480);
     M.K = fast ? K : 0;
+    const int stride = mesh->prm.seed_stride > 0 ? mesh->prm.seed_stride : default_seed_stride(n);
+    bool knn_side = false;
     if (fast) {
         int* knn = prep.get<int>((size_t)n * std::max(K, 1));
         float* sec = prep.get<float>(n);
         M.knn = knn; M.sec = sec;
-        kt.run(F_KNN, 1, [&] { launch_knn(M, knn, sec, st); });
+        // the descent needs only the seeds' lists: the other generators' lists are
+        // computed on the second stream beside it and awaited before the first level
+        knn_side = stride > 1;
+        if (knn_side) {
+            CK(cudaEventRecord(ctx->ovl_ev[4], st));
+            CK(cudaStreamWaitEvent(ctx->stream2, ctx->ovl_ev[4], 0));
+            kt.run_on(ctx->stream2, F_KNN, 1, [&] { launch_knn(M, knn, sec, stride, 1, ctx->stream2); });
+            CK(cudaEventRecord(ctx->ovl_ev[5], ctx->stream2));
+        }
+        kt.run(F_KNN, 1, [&] { launch_knn(M, knn, sec, stride, 0, st); });
     }
     CK(cudaGetLastError());
     read_stat(ctx, dstat);
@@ -324,18 +344,8 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     // ---- search with capacity retry
     double factor = mesh->prm.capacity_factor > 0 ? mesh->prm.capacity_factor : 1.3;
     unsigned long long est = (unsigned long long)(vertices_per_point(d) * n) + (1ull << d) + 1024;
-    int stride = mesh->prm.seed_stride > 0 ? mesh->prm.seed_stride : default_seed_stride(n);
     const int nseeds = (n + stride - 1) / stride;
     std::unique_ptr<Scratch> srch;
-    // the second stream's kernels use the search scratch: drain it before that is freed
-    // (also when an error unwinds the build)
-    struct Drain {
-        cudaStream_t s2, s3;
-        ~Drain() {
-            cudaStreamSynchronize(s2);
-            cudaStreamSynchronize(s3);
-        }
-    } drain{ctx->stream2, ctx->stream3};
     unsigned V = 0;
     for (int attempt = 0;; ++attempt) {
         if (attempt > 4) throw HvError(HV_E_CAPACITY, "vertex capacity retries exhausted");
@@ -416,6 +426,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
             // would only contend with the expansion, so the next level waits for it.
             cudaStream_t st2 = ctx->stream2, st3 = ctx->stream3;
             cudaEvent_t ev_exp = ctx->ovl_ev[0], ev_reg = ctx->ovl_ev[3];
+            if (knn_side) CK(cudaStreamWaitEvent(st, ctx->ovl_ev[5], 0));  // every generator's list
             bool pend = false;
             int pend_par = 0;
             // a new frontier [a, b): circumcentres on the main stream, the edge registry

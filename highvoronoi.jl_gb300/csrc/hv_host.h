@@ -34,7 +34,8 @@ void launch_morton(int d, const double* in, int n, const double* lo, const doubl
 void launch_gather(int d, const double* in, const int* perm, int n, double* pts, float* pts32, float* pts32lo,
                    cudaStream_t st);
 void launch_bvh(const DevMesh& M, float* blo, float* bhi, unsigned* flags, cudaStream_t st);
-void launch_knn(const DevMesh& M, int* knn, float* sec, cudaStream_t st);
+// candidate lists: part 0 the generators 0, qs, 2 qs, ... (descent seeds), part 1 the rest (qs <= 1: all)
+void launch_knn(const DevMesh& M, int* knn, float* sec, int qs, int part, cudaStream_t st);
 size_t sort_pairs_u64_i32_temp(int n);
 void sort_pairs_u64_i32(void* temp, size_t temp_bytes, const unsigned long long* kin, unsigned long long* kout,
                         const int* vin, int* vout, int n, int end_bit, cudaStream_t st);

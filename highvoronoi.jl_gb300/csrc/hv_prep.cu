@@ -195,8 +195,10 @@ constexpr int KNN_LQ = 64;     // queued leaves per warp
 // coalesced) and keeps the K+1 nearest, which bounds the K+1-th distance.
 // Phase 2 walks the rest of the tree 32 nodes per step (one box test per
 // lane), queues the surviving leaves and scans them 32 points at a time.
+// part 0 takes the generators q = 0, qs, 2 qs, ... (the descent seeds), part 1
+// the others; qs <= 1: every generator.
 template <int D, int CAP>
-__global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float* sec) {
+__global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float* sec, int qs, int part) {
     constexpr int DP = (D <= 4) ? 4 : 8;
     __shared__ float sd[KNN_WPB][CAP];
     __shared__ int si[KNN_WPB][CAP];
@@ -211,7 +213,10 @@ __global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float
     int* ix = si[wib];
     int* stk = sstack[wib];
     int* lq = sleaf[wib];
-    for (int q = blockIdx.x * KNN_WPB + wib; q < M.n; q += gridDim.x * KNN_WPB) {
+    const int nseed = qs <= 1 ? M.n : (M.n + qs - 1) / qs;
+    const int nq = qs <= 1 ? M.n : (part == 0 ? nseed : M.n - nseed);
+    for (int w = blockIdx.x * KNN_WPB + wib; w < nq; w += gridDim.x * KNN_WPB) {
+        const int q = qs <= 1 ? w : (part == 0 ? w * qs : w + w / (qs - 1) + 1);
         float xq[DP];
         {
             const float4* p = reinterpret_cast<const float4*>(M.pts32 + (size_t)q * DP);
@@ -383,18 +388,21 @@ void launch_bvh(const DevMesh& M, float* blo, float* bhi, unsigned* flags, cudaS
 }
 
 template <int D>
-static void launch_knn_t(const DevMesh& M, int* knn, float* sec, cudaStream_t st) {
-    const int blocks = (M.n + KNN_WPB - 1) / KNN_WPB;
+static void launch_knn_t(const DevMesh& M, int* knn, float* sec, int qs, int part, cudaStream_t st) {
+    const int nseed = qs <= 1 ? M.n : (M.n + qs - 1) / qs;
+    const int nq = qs <= 1 ? M.n : (part == 0 ? nseed : M.n - nseed);
+    if (nq <= 0) return;
+    const int blocks = (nq + KNN_WPB - 1) / KNN_WPB;
     const int need = 2 * M.K + 64;
-    if (need <= 128) k_knn<D, 128><<<blocks, KNN_WPB * 32, 0, st>>>(M, knn, sec);
-    else if (need <= 256) k_knn<D, 256><<<blocks, KNN_WPB * 32, 0, st>>>(M, knn, sec);
-    else if (need <= 512) k_knn<D, 512><<<blocks, KNN_WPB * 32, 0, st>>>(M, knn, sec);
-    else k_knn<D, 1024><<<blocks, KNN_WPB * 32, 0, st>>>(M, knn, sec);
+    if (need <= 128) k_knn<D, 128><<<blocks, KNN_WPB * 32, 0, st>>>(M, knn, sec, qs, part);
+    else if (need <= 256) k_knn<D, 256><<<blocks, KNN_WPB * 32, 0, st>>>(M, knn, sec, qs, part);
+    else if (need <= 512) k_knn<D, 512><<<blocks, KNN_WPB * 32, 0, st>>>(M, knn, sec, qs, part);
+    else k_knn<D, 1024><<<blocks, KNN_WPB * 32, 0, st>>>(M, knn, sec, qs, part);
 }
 
-void launch_knn(const DevMesh& M, int* knn, float* sec, cudaStream_t st) {
+void launch_knn(const DevMesh& M, int* knn, float* sec, int qs, int part, cudaStream_t st) {
     if (M.n <= 0) return;
-    HV_DISPATCH(M.d, (launch_knn_t<DD>(M, knn, sec, st)));
+    HV_DISPATCH(M.d, (launch_knn_t<DD>(M, knn, sec, qs, part, st)));
 }
 
 size_t sort_pairs_u64_i32_temp(int n) {
