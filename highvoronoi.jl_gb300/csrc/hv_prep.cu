@@ -187,14 +187,74 @@ __device__ float warp_keep_smallest(float* sd, int* si, int n, int need, int lan
     return __uint_as_float(tb);
 }
 
+// Keeps every buffered entry with distance <= t for a t whose count lies in
+// [lo_need, hi_need] (lo_need <= n): interpolation on the volume law
+// count ~ t^(D/2) from the largest distance, guarded by bisection, then one
+// ordered compaction.  Typically one to three passes over the buffer instead of
+// the 31 of the exact selection, which remains the fallback when ties leave no
+// such t.  Returns t and sets `kept`.
+template <int D>
+__device__ float warp_keep_relaxed(float* sd, int* si, int n, int lo_need, int hi_need, int lane, int& kept) {
+    const unsigned FULL = 0xFFFFFFFFu;
+    unsigned bmin = 0xFFFFFFFFu, bmax = 0u;  // non-negative floats order as their bit patterns
+    for (int x = lane; x < n; x += 32) {
+        const unsigned b = __float_as_uint(sd[x]);
+        bmin = min(bmin, b);
+        bmax = max(bmax, b);
+    }
+    bmin = __reduce_min_sync(FULL, bmin);
+    bmax = __reduce_max_sync(FULL, bmax);
+    if (n <= hi_need) { kept = n; return __uint_as_float(bmax); }
+    float lo = __uint_as_float(bmin), hi = __uint_as_float(bmax);
+    const float target = 0.5f * (float)(lo_need + hi_need);
+    float t = hi * exp2f(log2f(target / (float)n) * (2.f / D));
+    int c = -1;
+#pragma unroll 1
+    for (int it = 0; it < 16; ++it) {
+        if (!(t > lo && t < hi)) t = 0.5f * (lo + hi);
+        if (!(t > lo && t < hi)) { c = -1; break; }  // adjacent values: ties
+        int cc = 0;
+        for (int x = lane; x < n; x += 32) cc += (sd[x] <= t);
+        cc = __reduce_add_sync(FULL, cc);
+        if (cc >= lo_need && cc <= hi_need) { c = cc; break; }
+        if (cc < lo_need) lo = t; else hi = t;
+        t *= exp2f(log2f(target / (float)max(cc, 1)) * (2.f / D));
+        c = -1;
+    }
+    if (c < 0) {
+        const float tb = warp_keep_smallest(sd, si, n, lo_need, lane);
+        kept = lo_need;
+        return tb;
+    }
+    int w = 0;
+    for (int base = 0; base < n; base += 32) {
+        const int x = base + lane;
+        float dv = 0.f;
+        int iv = 0;
+        if (x < n) { dv = sd[x]; iv = si[x]; }
+        const bool keep = x < n && dv <= t;
+        const unsigned bk = __ballot_sync(FULL, keep);
+        if (keep) { const int pos = w + __popc(bk & ((1u << lane) - 1u)); sd[pos] = dv; si[pos] = iv; }
+        w += __popc(bk);
+    }
+    __syncwarp();
+    kept = c;
+    return t;
+}
+
 constexpr int KNN_STK = 768;  // traversal stack entries per warp (bounded by 32 x tree depth + 64)
 constexpr int KNN_LQ = 64;     // queued leaves per warp
 
 // One warp per generator.  Phase 1 inserts the generator's smallest ancestor
 // subtree holding at least K+1+leaf points (a contiguous Morton range, read
-// coalesced) and keeps the K+1 nearest, which bounds the K+1-th distance.
-// Phase 2 walks the rest of the tree 32 nodes per step (one box test per
-// lane), queues the surviving leaves and scans them 32 points at a time.
+// coalesced) and keeps about the K+1 nearest, which bounds the K+1-th
+// distance.  Phase 2 walks the rest of the tree 32 nodes per step (one box test
+// per lane; the walk starts at the 32 nodes of depth 5), queues the surviving
+// leaves and scans them 64 points at a time.  The buffer is thinned to between
+// K+1 and 1.25 K entries whenever it fills (every entry beyond its threshold is
+// farther than the K+1 it keeps), and the final at most pow2(K+1) entries are
+// sorted by (distance, index): the list is the first K, its complete radius the
+// K+1-th distance.
 // part 0 takes the generators q = 0, qs, 2 qs, ... (the descent seeds), part 1
 // the others; qs <= 1: every generator.
 template <int D, int CAP>
@@ -206,9 +266,14 @@ __global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float
     __shared__ int sleaf[KNN_WPB][KNN_LQ];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int K = M.K;
+    const int W = max(K / 4, 8);                        // slack of a thinned buffer
+    int P1 = 32;                                         // final buffer bound (sorted)
+    while (P1 < K + 1) P1 <<= 1;
     const unsigned FULL = 0xFFFFFFFFu;
     const unsigned lt = (1u << lane) - 1u;
     const float ex = M.ulp32;
+    const int L = M.leaf;
+    const int lsh = (L & (L - 1)) == 0 ? __ffs(L) - 1 : -1;  // leaf size as a shift when a power of two
     float* d = sd[wib];
     int* ix = si[wib];
     int* stk = sstack[wib];
@@ -228,39 +293,42 @@ __global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float
         }
         int cnt = 0;
         float thr = INFINITY;
-        // the points pt(0..np-1) (except q) with d2 < thr into the buffer
+        auto dist2 = [&](int s) -> float {
+            if (s < 0 || s >= M.n || s == q) return INFINITY;
+            float xs[DP];
+            const float4* p = reinterpret_cast<const float4*>(M.pts32 + (size_t)s * DP);
+#pragma unroll
+            for (int h = 0; h < DP / 4; ++h) {
+                float4 f = __ldg(p + h);
+                xs[4 * h] = f.x; xs[4 * h + 1] = f.y; xs[4 * h + 2] = f.z; xs[4 * h + 3] = f.w;
+            }
+            float d2 = 0.f;
+#pragma unroll
+            for (int k = 0; k < D; ++k) { const float e = xs[k] - xq[k]; d2 = fmaf(e, e, d2); }
+            return d2;
+        };
+        // the points pt(0..np-1) (except q) with d2 < thr into the buffer, two
+        // rounds of 32 per step (both loads in flight together)
         auto scan = [&](int np, auto pt) {
-            for (int base = 0; base < np; base += 32) {
-                const int s = base + lane < np ? pt(base + lane) : -1;
-                float d2 = INFINITY;
-                if (s >= 0 && s < M.n && s != q) {
-                    float xs[DP];
-                    const float4* p = reinterpret_cast<const float4*>(M.pts32 + (size_t)s * DP);
-#pragma unroll
-                    for (int h = 0; h < DP / 4; ++h) {
-                        float4 f = __ldg(p + h);
-                        xs[4 * h] = f.x; xs[4 * h + 1] = f.y; xs[4 * h + 2] = f.z; xs[4 * h + 3] = f.w;
-                    }
-                    d2 = 0.f;
-#pragma unroll
-                    for (int k = 0; k < D; ++k) { const float e = xs[k] - xq[k]; d2 = fmaf(e, e, d2); }
-                }
-                const bool take = d2 < thr;
-                const unsigned bal = __ballot_sync(FULL, take);
-                if (take) { const int pos = cnt + __popc(bal & lt); d[pos] = d2; ix[pos] = s; }
-                cnt += __popc(bal);
+            for (int base = 0; base < np; base += 64) {
+                const int s0 = base + lane < np ? pt(base + lane) : -1;
+                const int s1 = base + 32 + lane < np ? pt(base + 32 + lane) : -1;
+                const float d0 = dist2(s0), d1 = dist2(s1);
+                const bool t0 = d0 < thr, t1 = d1 < thr;
+                const unsigned b0 = __ballot_sync(FULL, t0), b1 = __ballot_sync(FULL, t1);
+                if (t0) { const int pos = cnt + __popc(b0 & lt); d[pos] = d0; ix[pos] = s0; }
+                cnt += __popc(b0);
+                if (t1) { const int pos = cnt + __popc(b1 & lt); d[pos] = d1; ix[pos] = s1; }
+                cnt += __popc(b1);
                 __syncwarp();
-                if (cnt > CAP - 32) {  // keep the K+1 nearest so far; their largest bounds the rest
-                    thr = warp_keep_smallest(d, ix, cnt, K + 1, lane);
-                    cnt = K + 1;
-                }
+                if (cnt > CAP - 64) thr = warp_keep_relaxed<D>(d, ix, cnt, K + 1, K + 1 + W, lane, cnt);
             }
         };
         // ---- phase 1: the smallest ancestor subtree with at least K+1+leaf points
-        const int lq0 = q / M.leaf;
+        const int lq0 = q / L;
         int A = M.P + lq0, depthA = 0;  // node id and levels above the leaf
         int la0 = lq0, la1 = lq0 + 1;
-        while (A > 1 && (min(la1 * M.leaf, M.n) - la0 * M.leaf) < K + 1 + M.leaf) {
+        while (A > 1 && (min(la1 * L, M.n) - la0 * L) < K + 1 + L) {
             A >>= 1;
             ++depthA;
             la0 = (A << depthA) - M.P;
@@ -269,23 +337,21 @@ __global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float
             la1 = min(la1, M.nleaves);
         }
         {
-            const int s0 = la0 * M.leaf;
-            scan(min(la1 * M.leaf, M.n) - s0, [&](int x) { return s0 + x; });
+            const int s0 = la0 * L;
+            scan(min(la1 * L, M.n) - s0, [&](int x) { return s0 + x; });
         }
-        if (cnt >= K + 1) {
-            thr = warp_keep_smallest(d, ix, cnt, K + 1, lane);
-            cnt = K + 1;
-        }
-        // ---- phase 2: the rest of the tree
+        if (cnt >= K + 1) thr = warp_keep_relaxed<D>(d, ix, cnt, K + 1, K + 1 + W, lane, cnt);
+        // ---- phase 2: the rest of the tree, from the nodes of depth min(5, log2 P)
         if (A > 1) {
             const int lvA = 31 - __clz(A);
-            int sp = 1, nl = 0;
-            if (lane == 0) stk[0] = 1;
+            const int lv0 = min(5, 31 - __clz(M.P));
+            int sp = 1 << lv0, nl = 0;
+            if (lane < sp) stk[lane] = (1 << lv0) + lane;
             __syncwarp();
             while (sp > 0 || nl > 0) {
                 if (nl >= 2 || (sp == 0 && nl > 0)) {
-                    const int L = M.leaf;
-                    scan(nl * L, [&](int x) { return lq[x / L] * L + x % L; });
+                    if (lsh >= 0) scan(nl << lsh, [&](int x) { return (lq[x >> lsh] << lsh) + (x & (L - 1)); });
+                    else scan(nl * L, [&](int x) { return lq[x / L] * L + x % L; });
                     nl = 0;
                     continue;
                 }
@@ -330,10 +396,7 @@ __global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float
                 __syncwarp();
             }
         }
-        if (cnt > K + 1) {
-            warp_keep_smallest(d, ix, cnt, K + 1, lane);
-            cnt = K + 1;
-        }
+        if (cnt > P1) warp_keep_relaxed<D>(d, ix, cnt, K + 1, P1, lane, cnt);
         int n2 = 32;
         while (n2 < cnt) n2 <<= 1;
         for (int i = cnt + lane; i < n2; i += 32) { d[i] = INFINITY; ix[i] = 0x7FFFFFFF; }

@@ -1052,14 +1052,6 @@ __global__ void __launch_bounds__(128) k_centers(DevMesh M, unsigned v0, unsigne
         for (int k = 0; k < D; ++k) xa[k] = __ldg(pa + k);
 #pragma unroll
         for (int r = 0; r < D; ++r) con_row<D, double>(M, xa, s[r + 1], A[r], rho[r]);
-        double nrm = 0;
-#pragma unroll
-        for (int r = 0; r < D; ++r) {
-            double sr = 0;
-#pragma unroll
-            for (int k = 0; k < D; ++k) sr += fabs(A[r][k]);
-            nrm = fmax(nrm, sr);
-        }
         int piv[D];
         double rd[D];
         const bool ok = lu_factor_rcp<D>(A, piv, rd);
@@ -1082,26 +1074,93 @@ __global__ void __launch_bounds__(128) k_centers(DevMesh M, unsigned v0, unsigne
 #pragma unroll
         for (int h = 0; h < DP / 4; ++h) dst[h] = make_float4(r32[4 * h], r32[4 * h + 1], r32[4 * h + 2], r32[4 * h + 3]);
         if (M.vinv32) {
-            // FP64 inverse, rounded once to FP32: every ray direction of the vertex
-            double rows[D];
+            // FP64 inverse, rounded once to FP32: every ray direction of the vertex.
+            // A^-1 = U^-1 L^-1 P: column j of U^-1 L^-1 (L^-1 unit lower triangular,
+            // its column j zero above j) is column idx[j] of A^-1, idx = the row
+            // order after the pivoting swaps -- fewer FP64 operations than D full
+            // solves with unit vectors.
+            int idx[D];
 #pragma unroll
-            for (int k = 0; k < D; ++k) rows[k] = 0.0;
+            for (int k = 0; k < D; ++k) idx[k] = k;
 #pragma unroll
             for (int c = 0; c < D; ++c) {
-                double col[D];
 #pragma unroll
-                for (int k = 0; k < D; ++k) col[k] = (k == c) ? 1.0 : 0.0;
-                if (ok) lu_solve_rcp<D>(A, piv, rd, col);
+                for (int r = c + 1; r < D; ++r)
+                    if (piv[c] == r) { const int t = idx[c]; idx[c] = idx[r]; idx[r] = t; }
+            }
+            float rows[D];  // row sums of |A^-1| (condition estimate; FP32 suffices)
+#pragma unroll
+            for (int k = 0; k < D; ++k) rows[k] = 0.f;
+            float* out = M.vinv32 + (size_t)v * D * D;
+#pragma unroll
+            for (int j = 0; j < D; ++j) {
+                double x[D];
+#pragma unroll
+                for (int r = 0; r < D; ++r) {
+                    if (r < j) x[r] = 0.0;
+                    else if (r == j) x[r] = 1.0;
+                    else {
+                        double y = -A[r][j];
+#pragma unroll
+                        for (int k = j + 1; k < r; ++k) y = fma(-A[r][k], x[k], y);
+                        x[r] = y;
+                    }
+                }
+#pragma unroll
+                for (int r = D - 1; r >= 0; --r) {
+                    double y = x[r];
+#pragma unroll
+                    for (int k = r + 1; k < D; ++k) y = fma(-A[r][k], x[k], y);
+                    x[r] = y * rd[r];
+                }
+                const int c = idx[j];
 #pragma unroll
                 for (int k = 0; k < D; ++k) {
-                    M.vinv32[(size_t)v * D * D + k * D + c] = (float)col[k];
-                    rows[k] += fabs(col[k]);
+                    const float f = ok ? (float)x[k] : (k == c ? 1.f : 0.f);
+                    out[k * D + c] = f;
+                    rows[k] += fabsf(f);
                 }
             }
-            double ninv = 0;
+            float ninv = 0.f;
 #pragma unroll
-            for (int k = 0; k < D; ++k) ninv = fmax(ninv, rows[k]);
-            M.vcond[v] = ok ? (float)(nrm * ninv) : INFINITY;
+            for (int k = 0; k < D; ++k) ninv = fmaxf(ninv, rows[k]);
+            // infinity norm of A from the FP32 split coordinates (the estimate only)
+            float nrm = 0.f;
+            {
+                float xa32[DP], xal32[DP];
+                const float4* p = reinterpret_cast<const float4*>(M.pts32 + (size_t)s[0] * DP);
+                const float4* pl = reinterpret_cast<const float4*>(M.pts32lo + (size_t)s[0] * DP);
+#pragma unroll
+                for (int h = 0; h < DP / 4; ++h) {
+                    const float4 f = __ldg(p + h), g = __ldg(pl + h);
+                    xa32[4 * h] = f.x; xa32[4 * h + 1] = f.y; xa32[4 * h + 2] = f.z; xa32[4 * h + 3] = f.w;
+                    xal32[4 * h] = g.x; xal32[4 * h + 1] = g.y; xal32[4 * h + 2] = g.z; xal32[4 * h + 3] = g.w;
+                }
+#pragma unroll
+                for (int r = 0; r < D; ++r) {
+                    const int it = s[r + 1];
+                    float sr = 0.f;
+                    if (it < M.n) {
+                        const float4* q = reinterpret_cast<const float4*>(M.pts32 + (size_t)it * DP);
+                        const float4* ql = reinterpret_cast<const float4*>(M.pts32lo + (size_t)it * DP);
+                        float xg[DP], xgl[DP];
+#pragma unroll
+                        for (int h = 0; h < DP / 4; ++h) {
+                            const float4 f = __ldg(q + h), g = __ldg(ql + h);
+                            xg[4 * h] = f.x; xg[4 * h + 1] = f.y; xg[4 * h + 2] = f.z; xg[4 * h + 3] = f.w;
+                            xgl[4 * h] = g.x; xgl[4 * h + 1] = g.y; xgl[4 * h + 2] = g.z; xgl[4 * h + 3] = g.w;
+                        }
+#pragma unroll
+                        for (int k = 0; k < D; ++k) sr += fabsf((xg[k] - xa32[k]) + (xgl[k] - xal32[k]));
+                    } else {
+                        const DevPlane& P = M.planes[it - M.n];
+#pragma unroll
+                        for (int k = 0; k < D; ++k) sr += fabsf(P.n32[k]);
+                    }
+                    nrm = fmaxf(nrm, sr);
+                }
+            }
+            M.vcond[v] = ok ? nrm * ninv * 1.0001f : INFINITY;
         }
     }
 }
