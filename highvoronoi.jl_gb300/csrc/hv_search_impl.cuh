@@ -44,6 +44,14 @@ __device__ __forceinline__ unsigned long long load_acquire(const unsigned long l
 __device__ __forceinline__ void store_release(unsigned long long* p, unsigned long long v) {
     asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+// Compare-and-swap whose read has acquire semantics: one round trip claims an
+// empty slot or reads an occupied one as load_acquire would.
+__device__ __forceinline__ unsigned long long cas_acquire(unsigned long long* p, unsigned long long cmp,
+                                                          unsigned long long v) {
+    unsigned long long old;
+    asm volatile("atom.acquire.gpu.global.cas.b64 %0, [%1], %2, %3;" : "=l"(old) : "l"(p), "l"(cmp), "l"(v) : "memory");
+    return old;
+}
 
 template <int D>
 __device__ unsigned vertex_insert(const DevMesh& M, const int (&s)[D + 1], int newitem, bool& is_new) {
@@ -52,24 +60,20 @@ __device__ unsigned vertex_insert(const DevMesh& M, const int (&s)[D + 1], int n
     const unsigned fp = ((unsigned)(h >> 32) & 0x7FFFFFFFu) | 1u;
     unsigned long long slot = h & M.vhmask;
     for (unsigned long long probe = 0; probe <= M.vhmask; ++probe) {
-        unsigned long long e = load_acquire(&M.vhash[slot]);
+        unsigned long long e = cas_acquire(&M.vhash[slot], HASH_EMPTY, HASH_BUSY);
         if (e == HASH_EMPTY) {
-            unsigned long long prev = atomicCAS(&M.vhash[slot], HASH_EMPTY, HASH_BUSY);
-            if (prev == HASH_EMPTY) {
-                unsigned vid = atomicAdd(M.vcount, 1u);
-                if (vid >= M.vcap) {
-                    set_status(M, ST_VCAP);
-                    atomicExch(&M.vhash[slot], ((unsigned long long)fp << 32) | INVALID_ID);
-                    return INVALID_ID;
-                }
-#pragma unroll
-                for (int k = 0; k <= D; ++k) M.vsig[(size_t)vid * (D + 1) + k] = s[k];
-                M.vnew[vid] = newitem;
-                store_release(&M.vhash[slot], ((unsigned long long)fp << 32) | vid);
-                is_new = true;
-                return vid;
+            unsigned vid = atomicAdd(M.vcount, 1u);
+            if (vid >= M.vcap) {
+                set_status(M, ST_VCAP);
+                atomicExch(&M.vhash[slot], ((unsigned long long)fp << 32) | INVALID_ID);
+                return INVALID_ID;
             }
-            e = load_acquire(&M.vhash[slot]);  // taken meanwhile: read it with acquire semantics
+#pragma unroll
+            for (int k = 0; k <= D; ++k) M.vsig[(size_t)vid * (D + 1) + k] = s[k];
+            M.vnew[vid] = newitem;
+            store_release(&M.vhash[slot], ((unsigned long long)fp << 32) | vid);
+            is_new = true;
+            return vid;
         }
         int spins = 0;
         while (e == HASH_BUSY) {
@@ -1269,7 +1273,38 @@ __device__ __forceinline__ void planes32(const DevMesh& M, const float* xa, cons
     }
 }
 
+// Parameter interval [lo, hi] of a candidate's crossing t = num / den from the
+// error bounds of both; false if the ray moves away from the candidate.
+__device__ __forceinline__ bool cand_t32(float num, float e_num, float den, float e_den, float& lo, float& hi) {
+    const float S32 = 5.9604645e-08f;
+    if (den > e_den) {
+        const float r = __fdividef(1.f, den);
+        const float t = num * r;
+        float et;
+        if (e_den < 1e-3f * den) et = (e_num + fabsf(t) * e_den) * r * 1.0021f;
+        else et = __fdividef(e_num + fabsf(t) * e_den, den - e_den) * 1.00001f;
+        et += 8.f * S32 * fabsf(t);
+        lo = t - et; hi = t + et;
+        return true;
+    }
+    if (den < -e_den) return false;
+    if (num - e_num > 0.f) {
+        if (!(den + e_den > 0.f)) return false;
+        lo = __fdividef(num - e_num, den + e_den) * 0.99999f; hi = INFINITY;
+    } else {
+        lo = -INFINITY; hi = INFINITY;
+    }
+    return true;
+}
+
 constexpr int FAST_WPB = 4;  // warps per block
+// Candidate records in shared memory (D + 4 words per candidate and warp) for
+// d <= 5; in 6D (lists of 384) they would cost more resident warps than the
+// shared pass saves, and each ray rereads its candidates instead.
+__host__ __device__ constexpr bool fast_staged(int d) { return d <= 5; }
+inline size_t fast_smem_bytes(int d, int K) {
+    return fast_staged(d) ? (size_t)FAST_WPB * (d + 4) * (K > 0 ? K : 1) * sizeof(float) : 0;
+}
 
 template <int D>
 __device__ __forceinline__ void load_pt32(const DevMesh& M, int j, float (&x)[(D <= 4) ? 4 : 8]) {
@@ -1308,6 +1343,8 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 6) k_expand_fast(DevMesh M, uns
     __shared__ float sRlo1[FAST_WPB][R], sRhi1[FAST_WPB][R], sRlo2[FAST_WPB][R];
     __shared__ int sRj1[FAST_WPB][R];
     __shared__ float sCond[FAST_WPB];
+    extern __shared__ float sCand[];  // FAST_WPB x CW x K candidate records
+    constexpr int CW = D + 4;
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned FULL = 0xFFFFFFFFu;
     const unsigned nf = f1 - f0;
@@ -1398,8 +1435,7 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 6) k_expand_fast(DevMesh M, uns
 #pragma unroll
         for (int k = 0; k < D; ++k) { R1 += fabsf(rho[k]); rmax = fmaxf(rmax, fabsf(rho[k])); }
         const float erho = 2.f * S32 * rmax;  // rho is the rounded FP64 centre offset
-        // one pass over the candidate list per open ray: small per-lane state (more
-        // resident warps), the rays' directions read from shared memory
+        // |u|_1 of every open ray (error bound of its denominators)
         if (lane < R && ((rmask >> lane) & 1u)) {
             float a1 = 0.f;
 #pragma unroll
@@ -1430,6 +1466,47 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 6) k_expand_fast(DevMesh M, uns
             sec_own = sv;
         }
         const int* lst = M.knn + (size_t)own * K;
+        // ---- the candidates' ray-independent quantities, once per vertex, into this
+        // warp's records (structure of arrays; lane c owns entries c, c+32, ...):
+        // dl = x_j - x_a (split), A1 = |dl|_1, num = |dl|^2 - 2 dl.rho and its error
+        // bound; item -1 marks a generator of the vertex (on the sphere)
+        float* cr = sCand + (size_t)wib * CW * K;
+        if constexpr (fast_staged(D)) {
+            int jn = lane < K ? __ldg(lst + lane) : -1;
+            int jnn = lane + 32 < K ? __ldg(lst + lane + 32) : -1;
+            float xn[DP], xnl[DP];
+#pragma unroll
+            for (int k = 0; k < DP; ++k) { xn[k] = 0.f; xnl[k] = 0.f; }
+            if (jn >= 0) { load_pt32<D>(M, jn, xn); load_pt32lo<D>(M, jn, xnl); }
+            for (int c = lane; c < K; c += 32) {
+                int j = jn;
+                float xj[DP], xjl[DP];
+#pragma unroll
+                for (int k = 0; k < DP; ++k) { xj[k] = xn[k]; xjl[k] = xnl[k]; }
+                jn = jnn;
+                jnn = c + 64 < K ? __ldg(lst + c + 64) : -1;
+                if (jn >= 0) { load_pt32<D>(M, jn, xn); load_pt32lo<D>(M, jn, xnl); }
+                bool skip = j < 0;
+#pragma unroll
+                for (int q = 0; q < R; ++q) skip |= (j == sig[q]);
+                float A1 = 0.f, A2 = 0.f, A3 = 0.f, dr = 0.f;
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    const float dl = (xj[k] - xa[k]) + (xjl[k] - xal[k]);
+                    A1 += fabsf(dl);
+                    A2 = fmaf(dl, dl, A2);
+                    A3 = fmaf(fabsf(dl), fabsf(rho[k]), A3);
+                    dr = fmaf(dl, rho[k], dr);
+                    cr[k * K + c] = dl;
+                }
+                cr[D * K + c] = A1;
+                cr[(D + 1) * K + c] = fmaf(-2.f, dr, A2);
+                cr[(D + 2) * K + c] = CN * (A2 + 2.f * A3) + 2.f * A1 * erho + TINY * (A1 + R1);
+                cr[(D + 3) * K + c] = __int_as_float(skip ? -1 : j);
+            }
+        }
+        // ---- one pass over the records per open ray (the lane reads back only its own
+        // entries: no synchronisation needed)
         unsigned todo = rmask;
         while (todo) {
             const int m = __ffs(todo) - 1;
@@ -1438,64 +1515,67 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 6) k_expand_fast(DevMesh M, uns
 #pragma unroll
             for (int k = 0; k < D; ++k) um[k] = sU[wib][m][k];
             const float lm = sLam[wib][m], lbm = sLb[wib][m], u1m = sU1[wib][m];
+            const float eden0 = CD * fabsf(lm) + 2.f * relu * lbm + TINY * u1m;
             float lo1 = INFINITY, hi1 = INFINITY, lo2 = INFINITY;
             int j1 = -1;
-            // software pipeline: list entries two iterations ahead, coordinates one ahead
-            int jn = lane < K ? __ldg(lst + lane) : -1;
-            int jnn = lane + 32 < K ? __ldg(lst + lane + 32) : -1;
-            float xn[DP], xnl[DP];
+            if constexpr (!fast_staged(D)) {
+                // software pipeline: list entries two iterations ahead, coordinates one ahead
+                int jn = lane < K ? __ldg(lst + lane) : -1;
+                int jnn = lane + 32 < K ? __ldg(lst + lane + 32) : -1;
+                float xn[DP], xnl[DP];
 #pragma unroll
-            for (int k = 0; k < DP; ++k) { xn[k] = 0.f; xnl[k] = 0.f; }
-            if (jn >= 0) { load_pt32<D>(M, jn, xn); load_pt32lo<D>(M, jn, xnl); }
-            for (int c = lane; c < K; c += 32) {
-                const int j = jn;
-                float xj[DP], xjl[DP];
-#pragma unroll
-                for (int k = 0; k < DP; ++k) { xj[k] = xn[k]; xjl[k] = xnl[k]; }
-                jn = jnn;
-                jnn = c + 64 < K ? __ldg(lst + c + 64) : -1;
+                for (int k = 0; k < DP; ++k) { xn[k] = 0.f; xnl[k] = 0.f; }
                 if (jn >= 0) { load_pt32<D>(M, jn, xn); load_pt32lo<D>(M, jn, xnl); }
-                if (j < 0) continue;
-                bool insig = false;
+                for (int c = lane; c < K; c += 32) {
+                    const int j = jn;
+                    float xj[DP], xjl[DP];
 #pragma unroll
-                for (int q = 0; q < R; ++q) insig |= (j == sig[q]);
-                if (insig) continue;
-                float A1 = 0.f, A2 = 0.f, A3 = 0.f, dr = 0.f, du = 0.f, B = 0.f;
+                    for (int k = 0; k < DP; ++k) { xj[k] = xn[k]; xjl[k] = xnl[k]; }
+                    jn = jnn;
+                    jnn = c + 64 < K ? __ldg(lst + c + 64) : -1;
+                    if (jn >= 0) { load_pt32<D>(M, jn, xn); load_pt32lo<D>(M, jn, xnl); }
+                    if (j < 0) continue;
+                    bool insig = false;
 #pragma unroll
-                for (int k = 0; k < D; ++k) {
-                    const float dl = (xj[k] - xa[k]) + (xjl[k] - xal[k]);
-                    A1 += fabsf(dl);
-                    A2 = fmaf(dl, dl, A2);
-                    A3 = fmaf(fabsf(dl), fabsf(rho[k]), A3);
-                    dr = fmaf(dl, rho[k], dr);
-                    du = fmaf(dl, um[k], du);
-                    B = fmaf(fabsf(dl), fabsf(um[k]), B);
-                }
-                const float num = fmaf(-2.f, dr, A2);
-                const float e_num = CN * (A2 + 2.f * A3) + 2.f * A1 * erho + TINY * (A1 + R1);
-                const float den = 2.f * (du - lm);
-                const float e_den = CD * (B + fabsf(lm)) + 2.f * relu * (A1 + lbm) + TINY * u1m;
-                float lo, hi;
-                if (den > e_den) {
-                    const float r = __fdividef(1.f, den);
-                    const float t = num * r;
-                    float et;
-                    if (e_den < 1e-3f * den) et = (e_num + fabsf(t) * e_den) * r * 1.0021f;
-                    else et = __fdividef(e_num + fabsf(t) * e_den, den - e_den) * 1.00001f;
-                    et += 8.f * S32 * fabsf(t);
-                    lo = t - et; hi = t + et;
-                } else if (den < -e_den) {
-                    continue;
-                } else {
-                    if (num - e_num > 0.f) {
-                        if (!(den + e_den > 0.f)) continue;
-                        lo = __fdividef(num - e_num, den + e_den) * 0.99999f; hi = INFINITY;
-                    } else {
-                        lo = -INFINITY; hi = INFINITY;
+                    for (int q = 0; q < R; ++q) insig |= (j == sig[q]);
+                    if (insig) continue;
+                    float A1 = 0.f, A2 = 0.f, A3 = 0.f, dr = 0.f, du = 0.f, B = 0.f;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        const float dl = (xj[k] - xa[k]) + (xjl[k] - xal[k]);
+                        A1 += fabsf(dl);
+                        A2 = fmaf(dl, dl, A2);
+                        A3 = fmaf(fabsf(dl), fabsf(rho[k]), A3);
+                        dr = fmaf(dl, rho[k], dr);
+                        du = fmaf(dl, um[k], du);
+                        B = fmaf(fabsf(dl), fabsf(um[k]), B);
                     }
+                    const float num = fmaf(-2.f, dr, A2);
+                    const float e_num = CN * (A2 + 2.f * A3) + 2.f * A1 * erho + TINY * (A1 + R1);
+                    float lo, hi;
+                    if (!cand_t32(num, e_num, 2.f * (du - lm), CD * B + 2.f * relu * A1 + eden0, lo, hi)) continue;
+                    if (lo < lo1 || (lo == lo1 && j < j1)) { lo2 = lo1; lo1 = lo; hi1 = hi; j1 = j; }
+                    else if (lo < lo2) lo2 = lo;
                 }
-                if (lo < lo1 || (lo == lo1 && j < j1)) { lo2 = lo1; lo1 = lo; hi1 = hi; j1 = j; }
-                else if (lo < lo2) lo2 = lo;
+            } else {
+                for (int c = lane; c < K; c += 32) {
+                    const int j = __float_as_int(cr[(D + 3) * K + c]);
+                    if (j < 0) continue;
+                    float du = 0.f, B = 0.f;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        const float dl = cr[k * K + c];
+                        du = fmaf(dl, um[k], du);
+                        B = fmaf(fabsf(dl), fabsf(um[k]), B);
+                    }
+                    const float A1 = cr[D * K + c];
+                    const float num = cr[(D + 1) * K + c];
+                    const float e_num = cr[(D + 2) * K + c];
+                    float lo, hi;
+                    if (!cand_t32(num, e_num, 2.f * (du - lm), CD * B + 2.f * relu * A1 + eden0, lo, hi)) continue;
+                    if (lo < lo1 || (lo == lo1 && j < j1)) { lo2 = lo1; lo1 = lo; hi1 = hi; j1 = j; }
+                    else if (lo < lo2) lo2 = lo;
+                }
             }
             // warp reduction of the ray's top-2
 #pragma unroll
@@ -1872,12 +1952,15 @@ __global__ void __launch_bounds__(FB_WPB * 32, 4) k_fallback_warp(DevMesh M, con
         bool overflow = false;
         if (!complete || M.K == 0) {
             long long nnodes = 0, nleaves_seen = 0, npoints_in = 0;
-            int sp = 1, nl = 0;
-            if (lane == 0) stk[0] = 1;
+            // start at the (at most 32) nodes of depth min(5, log2 P): one step instead of five
+            const int lv0 = min(5, 31 - __clz(M.P));
+            int sp = 1 << lv0, nl = 0;
+            if (lane < sp) stk[lane] = (1 << lv0) + lane;
             __syncwarp();
+            const int L = M.leaf;
+            const int lsh = (L & (L - 1)) == 0 ? __ffs(L) - 1 : -1;  // leaf size as a shift when a power of two
             while (sp > 0 || nl > 0) {
                 if (nl >= 2 || (sp == 0 && nl > 0)) {
-                    const int L = M.leaf;
                     const int tot = nl * L;
                     nleaves_seen += nl;
                     // a point can beat the bound H only inside the ball of parameter H (the
@@ -1903,7 +1986,7 @@ __global__ void __launch_bounds__(FB_WPB * 32, 4) k_fallback_warp(DevMesh M, con
                         const int qq = base + lane;
                         int j = -1;
                         if (qq < tot) {
-                            j = lq[qq / L] * L + (qq % L);
+                            j = lsh >= 0 ? (lq[qq >> lsh] << lsh) + (qq & (L - 1)) : lq[qq / L] * L + (qq % L);
                             if (j >= M.n) j = -1;
                         }
                         if (j >= 0) {
@@ -2413,7 +2496,16 @@ static void launch_fast_t(const DevMesh& M, unsigned f0, unsigned f1, unsigned l
     if (!nf) return;
     unsigned blocks = (nf + FAST_WPB - 1) / FAST_WPB;
     if (blocks > (unsigned)nsm * 32) blocks = (unsigned)nsm * 32;
-    k_expand_fast<D><<<blocks, FAST_WPB * 32, 0, st>>>(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap);
+    const size_t sm = fast_smem_bytes(D, M.K);
+    if (sm > 48 * 1024) {
+        static bool set = false;  // once per instantiation (the largest list length)
+        if (!set) {
+            cudaFuncSetAttribute(k_expand_fast<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)fast_smem_bytes(D, 480));
+            set = true;
+        }
+    }
+    k_expand_fast<D><<<blocks, FAST_WPB * 32, sm, st>>>(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap);
 }
 template <int D>
 static void launch_fallback_warp_t(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq,
