@@ -386,6 +386,14 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
                 fxs[p] = srch->get<unsigned long long>(fqcap);
             }
         unsigned* qc = fast ? srch->get<unsigned>(4) : nullptr;  // nfq, nfx per parity
+        // rays the expansion decided, inserted into the vertex hash by their own kernel
+        // (a level decides fewer rays than the build has vertices)
+        M.dq = nullptr; M.ndq = nullptr; M.dqcap = 0;
+        if (fast) {
+            M.dqcap = vcap;
+            M.dq = srch->get<uint2>(M.dqcap);
+            M.ndq = srch->get<unsigned>(1);
+        }
         hv::AmbQueue aq{};  // ambiguous candidate sets of the FP32 tree search
         if (fast) {
             aq.cap = fqcap;
@@ -462,7 +470,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
                 }
                 const int p = L & 1;
                 CK(cudaMemsetAsync(qc + 2 * p, 0, 2 * sizeof(unsigned), st));
-                kt.run(F_EXPAND, 1, [&] {
+                kt.run(F_EXPAND, 2, [&] {
                     launch_expand_fast(M, f0, f1, fqs[p], qc + 2 * p, fqcap, fxs[p], qc + 2 * p + 1, fqcap,
                                        ctx->nsm, st);
                 });

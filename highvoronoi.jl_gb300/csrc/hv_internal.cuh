@@ -119,6 +119,10 @@ struct DevMesh {
     unsigned* ecnt;             // per-vertex bit mask of edges found twice
     unsigned* status;
     unsigned long long* cnt;
+    // rays the expansion decided, inserted by a separate kernel: (vertex << 3 | ray, winner)
+    uint2* dq;
+    unsigned* ndq;
+    unsigned dqcap;
 };
 
 __device__ __forceinline__ void set_status(const DevMesh& M, unsigned bits) { atomicOr(M.status, bits); }

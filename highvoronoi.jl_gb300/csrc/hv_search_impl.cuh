@@ -1329,7 +1329,7 @@ __device__ __forceinline__ void load_pt32lo(const DevMesh& M, int j, float (&x)[
 }
 
 template <int D>
-__global__ void __launch_bounds__(FAST_WPB * 32, 6) k_expand_fast(DevMesh M, unsigned f0, unsigned f1,
+__global__ void __launch_bounds__(FAST_WPB * 32, D <= 4 ? 8 : 6) k_expand_fast(DevMesh M, unsigned f0, unsigned f1,
                                                                unsigned long long* fq, unsigned* nfq,
                                                                unsigned fqcap, unsigned long long* fx,
                                                                unsigned* nfx, unsigned fxcap) {
@@ -1592,6 +1592,7 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 6) k_expand_fast(DevMesh M, uns
         }
         __syncwarp();
         // ---- per-ray decision on lane m
+        int dwin = -1;  // winner of this lane's ray when decided here
         if (lane < R && ((rmask >> lane) & 1u)) {
             const int m = lane;
             count_add(M.cnt + C_RAYS);
@@ -1659,25 +1660,49 @@ __global__ void __launch_bounds__(FAST_WPB * 32, 6) k_expand_fast(DevMesh M, uns
                 secure = (t > 0.f) && (lhs < sec_own * (1.f - 1e-5f));
             }
             if (certified && !secure) count_add(M.cnt + C_INSECURE);
-            const bool exact = false;
-            const bool queue = !(certified && secure);
-            if (exact) {
-                const unsigned slot = atomicAdd(nfx, 1u);
-                if (slot < fxcap) fx[slot] = ((unsigned long long)v << 4) | (unsigned)m;
-                else set_status(M, ST_QUEUE);
-            } else if (queue) {
+            if (!(certified && secure)) {
                 // bit 3: the list holds every possible winner (no tree pass needed)
                 const unsigned slot = atomicAdd(nfq, 1u);
                 if (slot < fqcap) fq[slot] = ((unsigned long long)v << 4) | ((unsigned)secure << 3) | (unsigned)m;
                 else set_status(M, ST_QUEUE);
             } else {
-                int ns[R];
-                make_sig<D>(sig, m, win, ns);
-                bool is_new;
-                vertex_insert<D>(M, ns, win, is_new);
+                dwin = win;
+            }
+        }
+        // decided rays: one range of the insert queue per warp, so the warp does not
+        // wait on the vertex hash (k_insert_decided inserts them; a full queue is a
+        // capacity retry like a full ray queue)
+        const unsigned dm = __ballot_sync(FULL, dwin >= 0);
+        if (dm) {
+            unsigned base = 0;
+            if (lane == 0) base = atomicAdd(M.ndq, (unsigned)__popc(dm));
+            base = __shfl_sync(FULL, base, 0);
+            if (dwin >= 0) {
+                const unsigned slot = base + __popc(dm & ((1u << lane) - 1u));
+                if (slot < M.dqcap) M.dq[slot] = make_uint2((v << 3) | (unsigned)lane, (unsigned)dwin);
+                else set_status(M, ST_QUEUE);
             }
         }
         __syncwarp();
+    }
+}
+
+// Vertex-hash inserts of the rays the expansion decided, one thread per ray:
+// many inserts in flight hide the round trips of the claim, the id and the
+// publication that a warp of the expansion would otherwise wait for.
+template <int D>
+__global__ void __launch_bounds__(256) k_insert_decided(DevMesh M) {
+    const unsigned n = min(*M.ndq, M.dqcap);  // past the capacity: a capacity retry follows
+    for (unsigned r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const uint2 e = M.dq[r];
+        const unsigned v = e.x >> 3;
+        int sig[D + 1];
+#pragma unroll
+        for (int k = 0; k <= D; ++k) sig[k] = M.vsig[(size_t)v * (D + 1) + k];
+        int ns[D + 1];
+        make_sig<D>(sig, (int)(e.x & 7u), (int)e.y, ns);
+        bool is_new;
+        vertex_insert<D>(M, ns, (int)e.y, is_new);
     }
 }
 
@@ -2505,7 +2530,9 @@ static void launch_fast_t(const DevMesh& M, unsigned f0, unsigned f1, unsigned l
             set = true;
         }
     }
+    cudaMemsetAsync(M.ndq, 0, sizeof(unsigned), st);
     k_expand_fast<D><<<blocks, FAST_WPB * 32, sm, st>>>(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap);
+    k_insert_decided<D><<<nsm * 8, 256, 0, st>>>(M);
 }
 template <int D>
 static void launch_fallback_warp_t(const DevMesh& M, const unsigned long long* fq, const unsigned* nfq,
