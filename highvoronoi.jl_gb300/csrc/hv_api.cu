@@ -530,6 +530,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     mesh->V = V;
     CK(cudaEventRecord(kt.next(), st));
     const int canon_ev = (int)kt.used - 1;
+    bool packed = false;  // canonical order from one packed sort (else d + 1 sorts)
     {
         Scratch cs(st);
         unsigned* keys = cs.get<unsigned>((size_t)V * (d + 1));
@@ -541,12 +542,27 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         if (V) k_iota<<<std::min<unsigned>((V + 255) / 256, 65535u), 256, 0, st>>>(order, V);
         int end_bit = 1;
         while ((1ull << end_bit) < (unsigned long long)(n + mesh->np + 1)) ++end_bit;
-        size_t tb = sort_pairs_u32_i32_temp((int)std::max(V, 1u));
-        void* tmp = cs.get<char>(tb);
-        for (int pos = d; pos >= 0; --pos) {
-            launch_gather_keys(keys + (size_t)pos * V, order, V, kt, st);
-            if (V) sort_pairs_u32_i32(tmp, tb, kt, kt2, order, order2, (int)V, end_bit, st);
+        if (d * end_bit <= 64) {
+            // one sort by the first d items packed in 64 bits; ties (the two end points
+            // of an edge) ordered by the last item
+            unsigned long long* k64 = cs.get<unsigned long long>(V);
+            unsigned long long* k64s = cs.get<unsigned long long>(V);
+            size_t tb = sort_pairs_u64_i32_temp((int)std::max(V, 1u));
+            void* tmp = cs.get<char>(tb);
+            launch_pack_keys(keys, V, d, end_bit, k64, st);
+            if (V) sort_pairs_u64_i32(tmp, tb, k64, k64s, order, order2, (int)V, d * end_bit, st);
             std::swap(order, order2);
+            launch_fix_runs(k64s, keys + (size_t)d * V, V, order, st);
+            packed = true;
+        } else {
+            // least significant item first, stable sorts
+            size_t tb = sort_pairs_u32_i32_temp((int)std::max(V, 1u));
+            void* tmp = cs.get<char>(tb);
+            for (int pos = d; pos >= 0; --pos) {
+                launch_gather_keys(keys + (size_t)pos * V, order, V, kt, st);
+                if (V) sort_pairs_u32_i32(tmp, tb, kt, kt2, order, order2, (int)V, end_bit, st);
+                std::swap(order, order2);
+            }
         }
         mesh->osig = dalloc<int>(st, (size_t)V * (d + 1));
         mesh->oc = dalloc<double>(st, (size_t)V * d);
@@ -555,7 +571,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     }
     CK(cudaEventRecord(kt.next(), st));
     kt.spans.emplace_back(F_CANON, canon_ev);
-    kt.launches += 3 + 2 * (d + 1);
+    kt.launches += packed ? 6 : 3 + 2 * (d + 1);
     CK(cudaEventRecord(ev.e[3], st));
     unsigned long long hc[C_NCOUNT];
     CK(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));

@@ -73,6 +73,8 @@ void launch_fallback(const DevMesh& M, const unsigned long long* fq, const unsig
 // canonical keys: original 0-based items of each vertex, sorted, SoA by position
 void launch_canon_keys(const DevMesh& M, unsigned V, unsigned* keys, cudaStream_t st);
 void launch_gather_keys(const unsigned* keys_pos, const int* order, unsigned V, unsigned* out, cudaStream_t st);
+void launch_pack_keys(const unsigned* keys, unsigned V, int d, int bits, unsigned long long* out, cudaStream_t st);
+void launch_fix_runs(const unsigned long long* sk, const unsigned* last, unsigned V, int* order, cudaStream_t st);
 void launch_canon_gather(const DevMesh& M, unsigned V, const unsigned* keys, const int* order, int* osig,
                          double* oc, cudaStream_t st);
 void launch_inc_pairs(int d, int n, unsigned V, const int* osig, unsigned long long* pairs, long long* cnt,

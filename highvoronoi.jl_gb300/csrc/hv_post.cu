@@ -186,6 +186,40 @@ void launch_gather_keys(const unsigned* keys_pos, const int* order, unsigned V, 
     if (!V) return;
     k_gather_keys<<<grid_for(V, 256), 256, 0, st>>>(keys_pos, order, V, out);
 }
+// The first d items of every canonical signature packed into one 64-bit key
+// (`bits` bits each, the first item most significant).
+__global__ void k_pack_keys(const unsigned* __restrict__ keys, unsigned V, int d, int bits, unsigned long long* out) {
+    for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        unsigned long long k = 0;
+        for (int q = 0; q < d; ++q) k = (k << bits) | keys[(size_t)q * V + v];
+        out[v] = k;
+    }
+}
+
+// After the stable sort by the packed first d items, a run of equal keys holds
+// the vertices sharing d generators -- the two end points of an edge -- and is
+// put in the order of the last item.
+__global__ void k_fix_runs(const unsigned long long* __restrict__ sk, const unsigned* __restrict__ last, unsigned V,
+                           int* order) {
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i + 1 < V; i += gridDim.x * blockDim.x) {
+        if (sk[i + 1] != sk[i] || (i > 0 && sk[i - 1] == sk[i])) continue;
+        unsigned j = i + 2;
+        while (j < V && sk[j] == sk[i]) ++j;
+        for (unsigned x = i + 1; x < j; ++x)
+            for (unsigned y = x; y > i && last[order[y]] < last[order[y - 1]]; --y) {
+                const int z = order[y]; order[y] = order[y - 1]; order[y - 1] = z;
+            }
+    }
+}
+
+void launch_pack_keys(const unsigned* keys, unsigned V, int d, int bits, unsigned long long* out, cudaStream_t st) {
+    if (!V) return;
+    k_pack_keys<<<grid_for(V, 256), 256, 0, st>>>(keys, V, d, bits, out);
+}
+void launch_fix_runs(const unsigned long long* sk, const unsigned* last, unsigned V, int* order, cudaStream_t st) {
+    if (V < 2) return;
+    k_fix_runs<<<grid_for(V, 256), 256, 0, st>>>(sk, last, V, order);
+}
 void launch_canon_gather(const DevMesh& M, unsigned V, const unsigned* keys, const int* order, int* osig,
                          double* oc, cudaStream_t st) {
     if (!V) return;
