@@ -741,11 +741,14 @@ __device__ void gauss_dir(unsigned long long seed, unsigned a, unsigned long lon
         philox4x32(c, (unsigned)seed, (unsigned)(seed >> 32));
 #pragma unroll
         for (int p = 0; p < 2; ++p) {
-            double u1 = ((double)c[2 * p] + 0.5) * 2.3283064365386963e-10;
-            double u2 = ((double)c[2 * p + 1] + 0.5) * 2.3283064365386963e-10;
-            double rr = sqrt(-2.0 * log(u1));
-            double sn, cs;
-            sincospi(2.0 * u2, &sn, &cs);
+            // Box-Muller in FP32: the descent needs random directions, not accurate
+            // ones, and FP64 transcendentals cost a lane-0 latency chain per step
+            const float u1 = ((float)(c[2 * p] >> 8) + 0.5f) * 5.9604645e-08f;  // (0, 1), 24 bits
+            const float u2 = ((float)(c[2 * p + 1] >> 8) + 0.5f) * 5.9604645e-08f;
+            const double rr = (double)sqrtf(-2.f * logf(u1));
+            float snf, csf;
+            sincospif(2.f * u2, &snf, &csf);
+            const double sn = snf, cs = csf;
 #pragma unroll
             for (int k = 0; k < D; ++k) {
                 if (k == got) g[k] = rr * cs;
@@ -2320,8 +2323,9 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_descent_warp(DevMesh M, int str
                     for (int k = 0; k < D; ++k) nn = fma(row[k], row[k], nn);
                     nn = sqrt(nn);
                     if (!(nn > 1e-300)) { good = false; break; }
+                    const double inn = 1.0 / nn;
 #pragma unroll
-                    for (int k = 0; k < D; ++k) B[nb][k] = row[k] / nn;
+                    for (int k = 0; k < D; ++k) B[nb][k] = row[k] * inn;
                     ++nb;
                 }
                 for (int rep = 0; rep < 2 && good; ++rep) {
@@ -2338,8 +2342,9 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_descent_warp(DevMesh M, int str
                 for (int k = 0; k < D; ++k) nn = fma(g[k], g[k], nn);
                 nn = sqrt(nn);
                 if (!(nn > 1e-12)) good = false;
+                const double inn = 1.0 / nn;
 #pragma unroll
-                for (int k = 0; k < D; ++k) sU[wib][k] = good ? g[k] / nn : 0.0;
+                for (int k = 0; k < D; ++k) sU[wib][k] = good ? g[k] * inn : 0.0;
                 sOk[wib] = good ? 1 : 0;
             }
             __syncwarp();
