@@ -271,7 +271,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     {
         size_t tb = sort_pairs_u64_i32_temp(n);
         void* tmp = prep.get<char>(tb);
-        sort_pairs_u64_i32(tmp, tb, codes, codes2, idx, perm, n, 64, st);
+        sort_pairs_u64_i32(tmp, tb, codes, codes2, idx, perm, n, d * morton_bits(d, n), st);
     }
     double* pts = prep.get<double>((size_t)n * d);
     float* pts32 = prep.get<float>((size_t)n * DP);

@@ -29,6 +29,7 @@ void box_planes(int d, const double* lo, const double* hi, DevPlane* out);
 std::string make_planes(int d, int np, const double* base, const double* normal, DevPlane* out);
 std::string planes_bbox(int d, int np, const DevPlane* P, double* lo, double* hi);
 
+int morton_bits(int d, int n);  // bits per axis of the Morton codes (the sort reads d times as many)
 void launch_morton(int d, const double* in, int n, const double* lo, const double* hi, const DevPlane* planes,
                    int np, unsigned long long* codes, int* idx, unsigned* status, cudaStream_t st);
 void launch_gather(int d, const double* in, const int* perm, int n, double* pts, float* pts32, float* pts32lo,

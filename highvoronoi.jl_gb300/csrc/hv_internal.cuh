@@ -298,6 +298,17 @@ __device__ __forceinline__ void con_row(const DevMesh& M, const double* xa, int 
     }
 }
 
+// DP (4 or 8) floats from a 16-byte aligned address as float4 loads.
+template <int DP>
+__device__ __forceinline__ void load_f4(const float* p, float (&x)[DP]) {
+    const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+    for (int h = 0; h < DP / 4; ++h) {
+        const float4 f = __ldg(q + h);
+        x[4 * h] = f.x; x[4 * h + 1] = f.y; x[4 * h + 2] = f.z; x[4 * h + 3] = f.w;
+    }
+}
+
 // Insertion of `item` into a sorted signature with one slot removed.
 template <int D>
 __device__ __forceinline__ void make_sig(const int (&sig)[D + 1], int drop, int item, int (&out)[D + 1]) {

@@ -13,6 +13,8 @@
 // distances) and a radius `sec` such that every generator closer than `sec`
 // is in the list.  The fast ray kernel accepts a decision only if the new
 // empty sphere lies inside that radius (the security test).
+#include <algorithm>
+
 #include <cub/cub.cuh>
 
 #include "hv_internal.cuh"
@@ -22,8 +24,7 @@ namespace hv {
 
 template <int D>
 __global__ void k_morton(const double* __restrict__ in, int n, DevBox box, const DevPlane* __restrict__ planes, int np,
-                         unsigned long long* codes, int* idx, unsigned* status) {
-    constexpr int B = (63 / D) > 21 ? 21 : (63 / D);
+                         int B, unsigned long long* codes, int* idx, unsigned* status) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         unsigned q[D];
         bool ok = true;
@@ -367,11 +368,12 @@ __global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float
                 }
                 if (keep && isfinite(thr)) {
                     float bd = 0.f;
-                    const float* lo = M.blo + (size_t)node * DP;
-                    const float* hi = M.bhi + (size_t)node * DP;
+                    float bl[DP], bh[DP];
+                    load_f4<DP>(M.blo + (size_t)node * DP, bl);
+                    load_f4<DP>(M.bhi + (size_t)node * DP, bh);
 #pragma unroll
                     for (int k = 0; k < D; ++k) {
-                        const float l = __ldg(lo + k), h = __ldg(hi + k);
+                        const float l = bl[k], h = bh[k];
                         const float e = xq[k] < l ? l - xq[k] : (xq[k] > h ? xq[k] - h : 0.f);
                         bd = fmaf(e, e, bd);
                     }
@@ -428,13 +430,23 @@ __global__ void __launch_bounds__(KNN_WPB * 32) k_knn(DevMesh M, int* knn, float
         default: break;                                \
     }
 
+int morton_bits(int d, int n) {
+    // at least 2^8 grid cells per point: ties are rare even in clusters, and the
+    // sort reads only these d * bits bits
+    int lg = 0;
+    while ((1ll << lg) < (long long)std::max(n, 1)) ++lg;
+    const int bmax = std::min(21, 63 / d);
+    return std::max(1, std::min(bmax, (lg + 8 + d - 1) / d));
+}
+
 void launch_morton(int d, const double* in, int n, const double* lo, const double* hi, const DevPlane* planes, int np,
                    unsigned long long* codes, int* idx, unsigned* status, cudaStream_t st) {
     if (n <= 0) return;
+    const int bits = morton_bits(d, n);
     DevBox box;
     for (int k = 0; k < d; ++k) { box.lo[k] = lo[k]; box.hi[k] = hi[k]; }
     const int blocks = (n + 255) / 256;
-    HV_DISPATCH(d, (k_morton<DD><<<blocks, 256, 0, st>>>(in, n, box, planes, np, codes, idx, status)));
+    HV_DISPATCH(d, (k_morton<DD><<<blocks, 256, 0, st>>>(in, n, box, planes, np, bits, codes, idx, status)));
 }
 
 void launch_gather(int d, const double* in, const int* perm, int n, double* pts, float* pts32, float* pts32lo,

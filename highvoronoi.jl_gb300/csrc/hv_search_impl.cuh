@@ -2064,15 +2064,16 @@ __global__ void __launch_bounds__(FB_WPB * 32, 4) k_fallback_warp(DevMesh M, con
                 const float tp = H;
                 if (keep && isfinite(tp)) {
                     float r2 = 0.f, bd2 = 0.f;
-                    const float* blo = M.blo + (size_t)node * DP;
-                    const float* bhi = M.bhi + (size_t)node * DP;
+                    float bl[DP], bh[DP];
+                    load_f4<DP>(M.blo + (size_t)node * DP, bl);
+                    load_f4<DP>(M.bhi + (size_t)node * DP, bh);
 #pragma unroll
                     for (int k = 0; k < D; ++k) {
                         const float off = fmaf(tp, u[k], rho[k]);
                         const float w2 = db[k] - off;
                         r2 = fmaf(w2, w2, r2);
                         const float ck = xa[k] + (xal[k] + off);
-                        const float l = __ldg(blo + k), h = __ldg(bhi + k);
+                        const float l = bl[k], h = bh[k];
                         const float ex = ck < l ? l - ck : (ck > h ? ck - h : 0.f);
                         bd2 = fmaf(ex, ex, bd2);
                     }
