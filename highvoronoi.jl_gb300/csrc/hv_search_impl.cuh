@@ -2529,12 +2529,12 @@ static void launch_fast_t(const DevMesh& M, unsigned f0, unsigned f1, unsigned l
     if (blocks > (unsigned)nsm * 32) blocks = (unsigned)nsm * 32;
     const size_t sm = fast_smem_bytes(D, M.K);
     if (sm > 48 * 1024) {
-        static bool set = false;  // once per instantiation (the largest list length)
-        if (!set) {
-            cudaFuncSetAttribute(k_expand_fast<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)fast_smem_bytes(D, 480));
-            set = true;
-        }
+        // once per instantiation, for the largest list length (thread-safe static init)
+        static const bool set = [] {
+            return cudaFuncSetAttribute(k_expand_fast<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)fast_smem_bytes(D, 480)) == cudaSuccess;
+        }();
+        (void)set;
     }
     cudaMemsetAsync(M.ndq, 0, sizeof(unsigned), st);
     k_expand_fast<D><<<blocks, FAST_WPB * 32, sm, st>>>(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap);
