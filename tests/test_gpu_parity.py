@@ -205,3 +205,17 @@ def test_near_lattice_points(gpu_lib, d, k, eps):
     m, st = _compare(hv, X, hv.HV_METHOD_FAST)
     v, _ = m.polygon()
     assert abs(v.sum() - 1.0) < 1e-11
+
+
+def test_canonical_order_both_sort_paths(gpu_lib):
+    """The canonical vertex order comes from one sort of the first d items
+    packed in 64 bits when they fit (4D, 2,000 generators: 4 x 11 bits) and
+    from d+1 stable passes otherwise (5D, 5,000 generators: 5 x 13 bits); either
+    way the vertices come out in lexicographic order of their 1-based generator
+    tuples, each once."""
+    for d, n, seed in ((4, 2000, 12), (5, 5000, 11)):
+        m = _build(gpu_lib, D.uniform_points(d, n, seed), gpu_lib.HV_METHOD_FAST)
+        s, _ = m.vertices()
+        assert len(s) > 0
+        assert np.array_equal(np.lexsort(s.T[::-1]), np.arange(len(s)))
+        assert (np.diff(s, axis=0) != 0).any(axis=1).all()
