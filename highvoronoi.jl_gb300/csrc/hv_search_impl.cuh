@@ -1331,6 +1331,9 @@ __device__ __forceinline__ void load_pt32lo(const DevMesh& M, int j, float (&x)[
     }
 }
 
+// 8 resident blocks (64 registers, 32 warps per SM) for d <= 4, whose records
+// leave room for them in shared memory; 6 for d >= 5 (5D records allow 5
+// blocks; the 6D kernel would spill at 64 registers).
 template <int D>
 __global__ void __launch_bounds__(FAST_WPB * 32, D <= 4 ? 8 : 6) k_expand_fast(DevMesh M, unsigned f0, unsigned f1,
                                                                unsigned long long* fq, unsigned* nfq,
