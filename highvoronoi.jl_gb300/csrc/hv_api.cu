@@ -380,10 +380,12 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         // parity: the ladder of level L drains its pair while level L+1 fills the other
         unsigned long long* fqs[2] = {nullptr, nullptr};
         unsigned long long* fxs[2] = {nullptr, nullptr};
+        float* fqhs[2] = {nullptr, nullptr};  // the expansion's bound of every insecure ray
         if (fast)
             for (int p = 0; p < 2; ++p) {
                 fqs[p] = srch->get<unsigned long long>(fqcap);
                 fxs[p] = srch->get<unsigned long long>(fqcap);
+                fqhs[p] = srch->get<float>(fqcap);
             }
         unsigned* qc = fast ? srch->get<unsigned>(4) : nullptr;  // nfq, nfx per parity
         // rays the expansion decided, inserted into the vertex hash by their own kernel
@@ -469,6 +471,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
                     continue;
                 }
                 const int p = L & 1;
+                M.fqh = fqhs[p];  // the expansion and the ladder of this level share the parity
                 CK(cudaMemsetAsync(qc + 2 * p, 0, 2 * sizeof(unsigned), st));
                 kt.run(F_EXPAND, 2, [&] {
                     launch_expand_fast(M, f0, f1, fqs[p], qc + 2 * p, fqcap, fxs[p], qc + 2 * p + 1, fqcap,

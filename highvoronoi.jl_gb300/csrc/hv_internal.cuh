@@ -123,6 +123,9 @@ struct DevMesh {
     uint2* dq;
     unsigned* ndq;
     unsigned dqcap;
+    // per queued insecure ray: the upper bound of the expansion's best candidate
+    // (+inf if none), the fallback's starting bound instead of a second list pass
+    float* fqh;
 };
 
 __device__ __forceinline__ void set_status(const DevMesh& M, unsigned bits) { atomicOr(M.status, bits); }

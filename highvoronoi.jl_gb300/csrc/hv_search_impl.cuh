@@ -1669,8 +1669,12 @@ __global__ void __launch_bounds__(FAST_WPB * 32, D <= 4 ? 8 : 6) k_expand_fast(D
             if (!(certified && secure)) {
                 // bit 3: the list holds every possible winner (no tree pass needed)
                 const unsigned slot = atomicAdd(nfq, 1u);
-                if (slot < fqcap) fq[slot] = ((unsigned long long)v << 4) | ((unsigned)secure << 3) | (unsigned)m;
-                else set_status(M, ST_QUEUE);
+                if (slot < fqcap) {
+                    fq[slot] = ((unsigned long long)v << 4) | ((unsigned)secure << 3) | (unsigned)m;
+                    if (M.fqh) M.fqh[slot] = win >= 0 ? bhi : INFINITY;
+                } else {
+                    set_status(M, ST_QUEUE);
+                }
             } else {
                 dwin = win;
             }
@@ -1958,8 +1962,13 @@ __global__ void __launch_bounds__(FB_WPB * 32, 4) k_fallback_warp(DevMesh M, con
                 },
                 [&](int it, float lo, float hi) { take(it, lo, hi); });
         }
-        // the candidate list
-        if (M.K > 0) {
+        // the candidate list -- unless a tree pass follows and the expansion left a
+        // finite bound: its best candidate's upper bound is then the starting bound,
+        // and the exhaustive tree pass meets every list candidate inside that ball
+        const float H0 = M.fqh ? M.fqh[w] : INFINITY;
+        const bool list_pass = M.K > 0 && (complete || !isfinite(H0));
+        if (!list_pass) H = fminf(H, H0);
+        if (list_pass) {
             const int* lst = M.knn + (size_t)own * M.K;
             for (int c = lane; c < M.K; c += 32) {
                 const int j = __ldg(lst + c);
