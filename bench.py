@@ -173,18 +173,11 @@ def cpu_baseline(pts, cells, threads):
 
 
 def serve_requests(count, seed=2000):
-    """The served stream: request r has d uniform in {2,3,4,5}, N log-uniform in
-    [200, 20000] and points uniform in the unit cube drawn with seed r; arrival
-    gaps are exponential with the requested mean rate."""
+    """The served stream (hvgpu.datasets.served_stream): request r has d uniform
+    in {2,3,4,5}, N log-uniform in [200, 20000] and points uniform in the unit
+    cube drawn with seed r; arrival gaps are exponential with unit mean."""
     from hvgpu import datasets as D
-    u = D.uniform01(seed, 0, 3 * count).reshape(count, 3)
-    reqs = []
-    for r in range(count):
-        d = 2 + min(int(u[r, 0] * 4), 3)
-        n = int(round(np.exp(np.log(200) + u[r, 1] * (np.log(20000) - np.log(200)))))
-        reqs.append((d, n, r))
-    gaps = -np.log(u[:, 2])
-    return reqs, gaps
+    return D.served_stream(count, seed)
 
 
 def run_serve(args, device):

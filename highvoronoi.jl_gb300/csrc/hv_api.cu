@@ -1351,7 +1351,8 @@ int mc_impl(hv_mesh* m, int ndir, uint64_t seed, double* vol, double* area, bool
             if (m->nnbr > 0) CK(cudaMemcpyAsync(area, outA, sizeof(double) * m->nnbr, cudaMemcpyDeviceToHost, st));
         }
         CK(cudaStreamSynchronize(st));
-        if (hs) throw HvError(HV_E_CAPACITY, "cell degree beyond the MC integrator's capacity");
+        if (hs & 4u) throw HvError(HV_E_CAPACITY, "cell degree beyond the MC integrator's capacity");
+        if (hs) throw HvError(HV_E_INTERNAL, "neighbour lists inconsistent (status " + std::to_string(hs) + ")");
     } catch (const HvError& e) {
         return fail(m->ctx, e);
     }

@@ -15,6 +15,7 @@ namespace hv {
 
 struct PolyArgs {
     int d, n;
+    int np;                  // boundary planes: valid items are 0 .. n+np-1
     const DevPlane* planes;  // boundary planes, generator ids n + p
     const double* pts;       // original order, n x d
     const int* osig;         // V x (d+1), original 0-based items
@@ -24,7 +25,8 @@ struct PolyArgs {
     const long long* nbr_off;
     const int* nbr;
     double* area;            // aligned with nbr
-    unsigned* status;        // bit 1: cell too large, bit 2: facet structure overflow
+    unsigned* status;        // 1: cell too large, 2: facet overflow, 4: degree over capacity,
+                             // 8: neighbour item out of range, 16: neighbour CSR not sorted/symmetric
     int capC, capV, capF, capE, capI;
 };
 
@@ -98,6 +100,16 @@ __global__ void __launch_bounds__(MC_WPB * 32) k_mc_cells(PolyArgs A, int ndir, 
         const int deg = (int)(A.nbr_off[i + 1] - b);
         if (deg > capN) {
             if (lane == 0) atomicOr(A.status, 4u);
+            continue;
+        }
+        // every item must be another generator or one of the np planes
+        bool bad = false;
+        for (int t = lane; t < deg; t += 32) {
+            const int k = A.nbr[b + t];
+            bad |= k < 0 || k >= A.n + A.np || k == i;
+        }
+        if (__any_sync(0xFFFFFFFFu, bad)) {
+            if (lane == 0) atomicOr(A.status, 8u);
             continue;
         }
         float xi[D];
@@ -198,6 +210,10 @@ __global__ void k_mc_pairs(PolyArgs A, const double* rawA, double* outA) {
             }
             long long lo = A.nbr_off[k], hi = A.nbr_off[k + 1] - 1;
             while (lo < hi) { const long long md = (lo + hi) >> 1; if (A.nbr[md] < i) lo = md + 1; else hi = md; }
+            if (lo > hi || A.nbr[lo] != i) {  // row k does not list i: not a sorted symmetric CSR
+                atomicOr(A.status, 16u);
+                continue;
+            }
             const double neigh = rawA[t], old = rawA[lo];
             const double na = fabs(neigh) < old * 1.0e-10 ? old : 0.5 * (old + neigh);
             outA[t] = na;
@@ -215,7 +231,7 @@ __global__ void k_mc_volumes(PolyArgs A, const double* rawV, const double* rawA,
         double v = rawV[i];
         for (long long t = A.nbr_off[i]; t < A.nbr_off[i + 1]; ++t) {
             const int k = A.nbr[t];
-            if (k >= A.n) continue;
+            if (k >= A.n || k < 0) continue;
             v += (outA[t] - rawA[t]) * facet_height<D>(A, xi, k) / D;
         }
         vol[i] = v;
@@ -235,7 +251,7 @@ __global__ void k_mc_volumes(PolyArgs A, const double* rawV, const double* rawA,
 
 static PolyArgs make_args(const IntegrateInput& in) {
     PolyArgs A;
-    A.d = in.d; A.n = in.n;
+    A.d = in.d; A.n = in.n; A.np = in.np;
     A.planes = in.planes;
     A.pts = in.pts; A.osig = in.osig; A.oc = in.oc;
     A.inc_off = in.inc_off; A.inc = in.inc; A.nbr_off = in.nbr_off; A.nbr = in.nbr;

@@ -5,8 +5,10 @@
 // allocator calls, or code handed fixed buffers by a framework).  The caller
 // passes every input and output in device memory; the integrator's scratch
 // (raw per-cell volumes and variances, raw interface areas, the cuboid's
-// boundary planes, a status word) lives in one file-scope static device array of HV_NOALLOC_SCRATCH_BYTES
-// (16 MiB), which every GPU that loads this library holds until exit.
+// box planes, a status word) lives in one file-scope static device array of HV_NOALLOC_SCRATCH_BYTES
+// (16 MiB), which every GPU that loads this library holds until exit.  The
+// domain is the cuboid [lo, hi]: its 2d faces are the planes n .. n+2d-1 in
+// the order of hv_mesh_build (n+2k: x_k = hi_k, n+2k+1: x_k = lo_k).
 //
 // The array's name is only a host-side stand-in for the symbol, so its device
 // address is fetched once per device with cudaGetSymbolAddress (at the first
@@ -30,6 +32,7 @@ constexpr size_t kScratchBytes = HV_NOALLOC_SCRATCH_BYTES;
 constexpr size_t kStatusBytes = 256;
 constexpr size_t kPlaneBytes = 2 * HV_MAXD * sizeof(hv::DevPlane) + 256 - (2 * HV_MAXD * sizeof(hv::DevPlane)) % 256;
 constexpr int kMaxDevices = 64;
+static_assert(kStatusBytes + kPlaneBytes == HV_NOALLOC_FIXED_BYTES, "fixed part of the scratch layout");
 
 static __device__ __align__(256) unsigned char g_mc_scratch[kScratchBytes];
 
@@ -95,5 +98,7 @@ extern "C" int hv_integrate_heuristic_mc_noalloc(int d, int64_t n, const double*
     unsigned hs = 0;
     if (cudaMemcpyAsync(&hs, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess) return HV_E_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return HV_E_CUDA;
-    return hs ? HV_E_INVALID_ARG : HV_OK;  // a cell's degree exceeded max_degree
+    // 4: a row longer than max_degree; 8: an item outside 0 .. n+2d-1 (or a cell
+    // listing itself); 16: a row k that does not list i although row i lists k
+    return hs ? HV_E_INVALID_ARG : HV_OK;
 }

@@ -163,8 +163,9 @@ def heuristic_mc_noalloc(d, n, d_pts, lo, hi, d_nbr_off, d_nbr, nnbr, max_degree
     rc = load().hv_integrate_heuristic_mc_noalloc(d, n, d_pts, dptr(lo), dptr(hi), d_nbr_off, d_nbr, nnbr,
                                                   max_degree, ndir, seed, d_vol, d_area, stream)
     if rc != HV_OK:
-        msg = {HV_E_CAPACITY: "2n + nnbr doubles exceed the static scratch",
-               HV_E_INVALID_ARG: "invalid argument or a row longer than max_degree"}.get(rc, "CUDA error")
+        msg = {HV_E_CAPACITY: "1536 bytes + 2n + nnbr doubles exceed the static scratch",
+               HV_E_INVALID_ARG: "invalid argument, a row longer than max_degree, an item outside "
+                                 "0..n+2d-1, or a neighbour relation that is not symmetric"}.get(rc, "CUDA error")
         raise HVError(rc, "hv_integrate_heuristic_mc_noalloc: " + msg)
 
 

@@ -77,6 +77,21 @@ def clustered_points(d: int, n: int, seed: int, n_clusters: int = 8, sigma: floa
     return np.ascontiguousarray(np.concatenate(out, axis=0)[:n])
 
 
+def served_stream(count: int, seed: int = 2000):
+    """The served stream of mesh requests: request r has d uniform in
+    {2,3,4,5}, N log-uniform in [200, 20000] and its points uniform in the unit
+    cube drawn with seed r (uniform_points(d, N, r)).  Returns the list of
+    (d, N, r) and the arrival gaps in units of the mean gap (exponential)."""
+    u = uniform01(seed, 0, 3 * count).reshape(count, 3)
+    reqs = []
+    for r in range(count):
+        d = 2 + min(int(u[r, 0] * 4), 3)
+        n = int(round(np.exp(np.log(200) + u[r, 1] * (np.log(20000) - np.log(200)))))
+        reqs.append((d, n, r))
+    gaps = -np.log(u[:, 2])
+    return reqs, gaps
+
+
 # The five workloads of the hot path (point cloud, boundary and integrator).
 WORKLOADS = {
     "2d_uniform_1k": dict(d=2, n=1000, seed=0, kind="uniform", integrator="polygon"),

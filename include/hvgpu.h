@@ -231,17 +231,26 @@ int hv_mesh_free(hv_mesh* mesh);
  * computes, but every input and output is a caller-owned device buffer and the
  * scratch lives in a static device array of HV_NOALLOC_SCRATCH_BYTES that this
  * library holds on every GPU that loads it.  No counterpart in the reference.
+ *   domain     the cuboid [lo, hi] only (host arrays of length d); its faces
+ *              are the items n .. n+2d-1 in hv_mesh_build's order: n+2k is
+ *              the upper face x_k = hi_k, n+2k+1 the lower face x_k = lo_k
  *   d_pts      n x d doubles (device), d_nbr_off n+1 int64 and d_nbr nnbr int32
- *              (device): neighbour CSR with 0-based generators, plane p as n+p
- *              (hv_mesh_neighbors' lists minus one), max_degree >= every row
+ *              (device): neighbour CSR with 0-based generators, every row
+ *              sorted ascending and the relation symmetric (j in row i iff i
+ *              in row j), as hv_mesh_neighbors returns it minus one for a box
+ *              mesh; max_degree >= every row length
  *   d_vol      n doubles (device), d_area nnbr doubles (device), stream a
  *              cudaStream_t (NULL: legacy default stream); returns synchronised
- * Limits: 256 + 8 (2 n + nnbr) bytes must fit the scratch (else
- * HV_E_CAPACITY); HV_E_INVALID_ARG if a row is longer than max_degree.
+ * Limits: HV_NOALLOC_FIXED_BYTES + 8 (2 n + nnbr) bytes must fit the scratch
+ * (else HV_E_CAPACITY, checked before any device work).  HV_E_INVALID_ARG if
+ * a row is longer than max_degree, an item lies outside 0 .. n+2d-1 (or a
+ * cell lists itself), or a row k does not list i while row i lists k.
  * The first call on a device looks up the scratch address on that device
  * (call it once before any stream capture).  Calls share the scratch: calls
  * that overlap on the GPU race. */
 #define HV_NOALLOC_SCRATCH_BYTES (16u << 20)
+/* Fixed part of the scratch: a 256-byte status block and the 2d box planes. */
+#define HV_NOALLOC_FIXED_BYTES 1536u
 int hv_integrate_heuristic_mc_noalloc(int d, int64_t n, const double* d_pts, const double* lo, const double* hi,
                                       const int64_t* d_nbr_off, const int32_t* d_nbr, int64_t nnbr, int max_degree,
                                       int ndir, uint64_t seed, double* d_vol, double* d_area, void* stream);

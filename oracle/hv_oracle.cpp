@@ -1376,6 +1376,281 @@ int hvo_sample_cells(int d, int64_t n, const double* pts, const double* lo, cons
     return fail ? -3 : 0;
 }
 
+
+/* Polygon volumes and areas of the listed cells, each computed from the cell's
+ * own polytope: every facet of cell i, towards lower and higher neighbours,
+ * by the flag decomposition (src/polyintegrator.jl:174-468), V_i = sum_k V_ik.
+ * (The mesh-wide pass copies the interface of a lower neighbour instead,
+ * src/cleanup_cell.jl:174-204; both are the same quantity.) */
+int hvo_polygon_cells(int d, int64_t n, const double* pts, const double* lo, const double* hi, uint64_t seed,
+                      int nthreads, int64_t ncells, const int64_t* cells, int64_t cap, double* vol, int64_t* offs,
+                      int64_t* items_out, double* area) {
+    if (d < 2 || d > MAXD || n <= 0 || ncells < 0) { set_err("invalid argument"); return -1; }
+    Problem P;
+    P.d = d; P.n = (int)n; P.seed = seed;
+    P.X.assign(pts, pts + (size_t)n * d);
+    set_box_planes(P, lo, hi);
+    for (int64_t i = 0; i < n; ++i)
+        if (!inside_planes(P, pts + i * d)) { set_err("point outside the open domain"); return -2; }
+    build_tree(P);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    std::vector<std::vector<int>> nb(ncells);
+    std::vector<std::vector<double>> ar(ncells);
+    std::vector<double> vv(ncells, 0.0);
+    int fail = 0;
+#pragma omp parallel reduction(+ : fail)
+    {
+        Explorer ex(P);
+        std::vector<CellVertex> cv;
+#pragma omp for schedule(dynamic, 1)
+        for (int64_t c = 0; c < ncells; ++c) {
+            const int i = (int)cells[c];
+            if (i < 0 || i >= n) { fail++; continue; }
+            ex.explore_cell(i, cv, false, nullptr);
+            if (cv.empty()) { fail++; continue; }
+            std::vector<int> its;
+            for (auto& v : cv) for (int s : v.sig) if (s != i) its.push_back(s);
+            std::sort(its.begin(), its.end());
+            its.erase(std::unique(its.begin(), its.end()), its.end());
+            PolyCell pc{P, i, cv};
+            double fact = 1;
+            for (int q = 2; q <= d; ++q) fact *= q;
+            std::vector<double> a(its.size(), 0.0);
+            double v = 0;
+            for (size_t t = 0; t < its.size(); ++t) {
+                const int k = its[t];
+                std::vector<int> L;
+                for (int w = 0; w < (int)cv.size(); ++w)
+                    if (std::find(cv[w].sig.begin(), cv[w].sig.end(), k) != cv[w].sig.end()) L.push_back(w);
+                std::vector<int> K{k};
+                const double Vik = pc.chain_sum(L, K) / fact;
+                a[t] = Vik * d / height(P, i, k);
+                v += Vik;
+            }
+            if (pc.bad) fail++;
+            nb[c] = std::move(its);
+            ar[c] = std::move(a);
+            vv[c] = v;
+        }
+    }
+    if (fail) { set_err("cell exploration or integration failed"); return -3; }
+    offs[0] = 0;
+    for (int64_t c = 0; c < ncells; ++c) offs[c + 1] = offs[c] + (int64_t)nb[c].size();
+    if (offs[ncells] > cap) { set_err("output capacity too small"); return -4; }
+    for (int64_t c = 0; c < ncells; ++c) {
+        vol[c] = vv[c];
+        for (size_t t = 0; t < nb[c].size(); ++t) {
+            items_out[offs[c] + (int64_t)t] = (int64_t)nb[c][t] + 1;
+            area[offs[c] + (int64_t)t] = ar[c][t];
+        }
+    }
+    return 0;
+}
+
+/* Certificate of a vertex list that does not use the oracle's own search.
+ *  out[0] vertices whose circumsphere holds a generator strictly inside, or
+ *         whose centre lies beyond a boundary plane that is not in the
+ *         signature
+ *  out[1] exact ties (a non-member on the sphere within binary128)
+ *  out[2] signatures that are not a valid vertex system (singular, no real
+ *         anchor, item out of range, unsorted)
+ *  out[3] edges (d-subsets with a real generator) that do not have exactly two
+ *         end points
+ *  out[4] duplicate signatures
+ *  out[5] candidates re-decided in binary128
+ *  maxdev largest |r_v - c_v| between the given coordinates and the FP64
+ *         circumcentre of the signature
+ * The circumsphere of each signature is solved in FP64; the generators near
+ * it come from a kd-tree ball query, and any decision within a margin of the
+ * FP64 error is redone with the centre solved in binary128.  With out[0..4]
+ * all zero, every listed vertex is a Voronoi vertex and every edge leads to
+ * another listed vertex: the list is the whole (connected) vertex graph of
+ * the bounded domain, i.e. the Voronoi mesh. */
+int hvo_certify_mesh(int d, int64_t n, const double* pts, const double* lo, const double* hi, int np,
+                     const double* base, const double* normal, int64_t nv, const int64_t* sig, const double* r,
+                     int nthreads, int64_t* out, double* maxdev) {
+    if (d < 2 || d > MAXD || n <= 0 || nv < 0 || !out) { set_err("invalid argument"); return -1; }
+    Problem P;
+    P.d = d; P.n = (int)n;
+    P.X.assign(pts, pts + (size_t)n * d);
+    if (np > 0) {
+        if (!set_planes(P, np, base, normal)) { set_err("invalid planes"); return -1; }
+    } else {
+        set_box_planes(P, lo, hi);
+    }
+    build_tree(P);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    const int64_t nitems = n + P.np;
+    int64_t bad_sphere = 0, ties = 0, bad_sys = 0, quad = 0;
+    double mdev = 0;
+#pragma omp parallel reduction(+ : bad_sphere, ties, bad_sys, quad) reduction(max : mdev)
+    {
+        std::vector<int> cand;
+#pragma omp for schedule(dynamic, 256)
+        for (int64_t v = 0; v < nv; ++v) {
+            const int64_t* s1 = sig + v * (d + 1);
+            int S[MAXD + 1];
+            bool ok = true;
+            for (int q = 0; q <= d; ++q) {
+                const int64_t it = s1[q] - 1;
+                if (it < 0 || it >= nitems || (q > 0 && s1[q] <= s1[q - 1])) ok = false;
+                S[q] = (int)it;
+            }
+            if (!ok || P.is_plane(S[0])) { bad_sys++; continue; }
+            VertexSys V = solve_vertex(P, S);
+            if (!V.ok) { bad_sys++; continue; }
+            const double* xa = P.x(S[0]);
+            double c[MAXD], r2 = 0;
+            for (int k = 0; k < d; ++k) { c[k] = xa[k] + V.rho[k]; r2 += V.rho[k] * V.rho[k]; }
+            for (int k = 0; k < d; ++k) mdev = std::max(mdev, std::fabs(c[k] - r[v * d + k]));
+            // binary128 centre, computed on demand
+            bool have_q = false;
+            qreal cq[MAXD], r2q = 0;
+            auto solve_q = [&]() {
+                if (have_q) return;
+                qreal M[MAXD][MAXD], rhs[MAXD];
+                for (int row = 0; row < d; ++row) constraint_row<qreal>(P, S[0], S[row + 1], M[row], rhs[row]);
+                int piv[MAXD] = {0};
+                lu_factor<qreal>(d, M, piv);
+                lu_solve<qreal>(d, M, piv, rhs);
+                r2q = 0;
+                for (int k = 0; k < d; ++k) { cq[k] = (qreal)xa[k] + rhs[k]; r2q += rhs[k] * rhs[k]; }
+                have_q = true;
+            };
+            const double margin = 1e-8 * std::max(1.0, V.cond / 1e5);
+            bool inside = false, tie = false;
+            // planes outside the signature: the centre must lie strictly inside
+            // them (a plane is the mirror of the cell's generator, which is
+            // nearer to the centre than the generator exactly when the centre
+            // lies beyond the plane)
+            const double R = std::sqrt(r2);
+            for (int p = 0; p < P.np && !inside; ++p) {
+                bool mem = false;
+                for (int q = 0; q <= d; ++q) mem |= S[q] == (int)n + p;
+                if (mem) continue;
+                const double h = plane_height(P, p, c);
+                if (h > margin * R) continue;
+                if (h < -margin * R) { inside = true; break; }
+                quad++;
+                solve_q();
+                qreal hq = (qreal)P.poff[p];
+                for (int k = 0; k < d; ++k) hq -= (qreal)P.pn[p][k] * cq[k];
+                const qreal tq = (qreal)1e-24 * (qreal)R;
+                if (hq < -tq) inside = true;
+                else if (!(hq > tq)) tie = true;
+            }
+            // generators in the ball of radius sqrt(r2 (1 + margin)) around c
+            cand.clear();
+            {
+                const double rr = r2 * (1.0 + margin) + 1e-300;
+                int stack[128]; int sp = 0;
+                if (!P.nodes.empty()) stack[sp++] = 0;
+                while (sp > 0) {
+                    const KdNode& nd = P.nodes[stack[--sp]];
+                    double dist2 = 0;
+                    for (int k = 0; k < d; ++k) {
+                        const double e = c[k] < nd.lo[k] ? nd.lo[k] - c[k] : (c[k] > nd.hi[k] ? c[k] - nd.hi[k] : 0);
+                        dist2 += e * e;
+                    }
+                    if (dist2 > rr) continue;
+                    if (nd.left < 0) {
+                        for (int t = nd.start; t < nd.end; ++t) cand.push_back(P.perm[t]);
+                    } else {
+                        if (sp + 2 > 128) { inside = true; break; }
+                        stack[sp++] = nd.left; stack[sp++] = nd.right;
+                    }
+                }
+            }
+            for (int j : cand) {
+                if (inside) break;
+                bool mem = false;
+                for (int q = 0; q <= d; ++q) mem |= S[q] == j;
+                if (mem) continue;
+                const double* xj = P.x(j);
+                double dd = 0;
+                for (int k = 0; k < d; ++k) { const double e = xj[k] - c[k]; dd += e * e; }
+                const double gap = dd - r2;
+                if (gap > margin * r2) continue;
+                if (gap < -margin * r2) { inside = true; break; }
+                quad++;
+                solve_q();
+                qreal ddq = 0;
+                for (int k = 0; k < d; ++k) { const qreal e = (qreal)xj[k] - cq[k]; ddq += e * e; }
+                const qreal g = ddq - r2q;
+                if (g < -(qreal)1e-24 * r2q) inside = true;
+                else if (!(g > (qreal)1e-24 * r2q)) tie = true;
+            }
+            if (inside) bad_sphere++;
+            else if (tie) ties++;
+        }
+    }
+    // edges and duplicates: every d-subset holding a real generator must belong
+    // to exactly two vertices, every signature must occur once
+    int bits = 1;
+    while ((1ll << bits) < nitems + 1) ++bits;
+    int64_t bad_edges = 0, dups = 0;
+    if ((d + 1) * bits <= 128) {
+        typedef unsigned __int128 u128;
+        std::vector<u128> keys;
+        keys.reserve((size_t)nv * (d + 1));
+        std::vector<u128> vkeys((size_t)nv);
+        for (int64_t v = 0; v < nv; ++v) {
+            const int64_t* s1 = sig + v * (d + 1);
+            u128 vk = 0;
+            for (int q = 0; q <= d; ++q) vk = (vk << bits) | (u128)(uint64_t)s1[q];
+            vkeys[v] = vk;
+            for (int m = 0; m <= d; ++m) {
+                u128 e = 0;
+                bool real = false;
+                for (int q = 0; q <= d; ++q) {
+                    if (q == m) continue;
+                    e = (e << bits) | (u128)(uint64_t)s1[q];
+                    real |= s1[q] <= n;
+                }
+                if (real) keys.push_back(e);
+            }
+        }
+        std::sort(keys.begin(), keys.end());
+        for (size_t a = 0; a < keys.size();) {
+            size_t b = a;
+            while (b < keys.size() && keys[b] == keys[a]) ++b;
+            if (b - a != 2) bad_edges++;
+            a = b;
+        }
+        std::sort(vkeys.begin(), vkeys.end());
+        for (size_t a = 1; a < vkeys.size(); ++a) dups += vkeys[a] == vkeys[a - 1];
+    } else {
+        std::vector<std::vector<int64_t>> keys;
+        std::vector<std::vector<int64_t>> vkeys;
+        for (int64_t v = 0; v < nv; ++v) {
+            const int64_t* s1 = sig + v * (d + 1);
+            vkeys.emplace_back(s1, s1 + d + 1);
+            for (int m = 0; m <= d; ++m) {
+                std::vector<int64_t> e;
+                bool real = false;
+                for (int q = 0; q <= d; ++q) if (q != m) { e.push_back(s1[q]); real |= s1[q] <= n; }
+                if (real) keys.push_back(std::move(e));
+            }
+        }
+        std::sort(keys.begin(), keys.end());
+        for (size_t a = 0; a < keys.size();) {
+            size_t b = a;
+            while (b < keys.size() && keys[b] == keys[a]) ++b;
+            if (b - a != 2) bad_edges++;
+            a = b;
+        }
+        std::sort(vkeys.begin(), vkeys.end());
+        for (size_t a = 1; a < vkeys.size(); ++a) dups += vkeys[a] == vkeys[a - 1];
+    }
+    out[0] = bad_sphere; out[1] = ties; out[2] = bad_sys; out[3] = bad_edges; out[4] = dups; out[5] = quad;
+    if (maxdev) *maxdev = mdev;
+    return 0;
+}
+
 static int64_t verify_vertices(const Problem& P, const double* pts, int64_t nv, const int64_t* sig,
                                const double* r, double rel_tol);
 

@@ -83,6 +83,24 @@ int64_t hvo_verify_vertices_planes(int d, int64_t n, const double* pts, int np, 
                                    const double* normal, int64_t nv, const int64_t* sig, const double* r,
                                    double rel_tol);
 
+/* VI_POLYGON volumes (ncells) and interface areas of the listed cells (0-based),
+ * each computed from the cell's own polytope, in a CSR of capacity cap:
+ * offs (ncells+1), items (1-based neighbours, sorted), area.  Returns -4 if
+ * cap is too small (offs[ncells] then holds the size needed). */
+int hvo_polygon_cells(int d, int64_t n, const double* pts, const double* lo, const double* hi, uint64_t seed,
+                      int nthreads, int64_t ncells, const int64_t* cells, int64_t cap, double* vol, int64_t* offs,
+                      int64_t* items, double* area);
+
+/* Certificate of a vertex list independent of the oracle's search (box
+ * [lo, hi] when np == 0, else the np planes base/normal): out[0] vertices with
+ * a generator strictly inside their circumsphere or a centre beyond a plane, out[1]
+ * exact ties, out[2] invalid signatures, out[3] edges without exactly two end
+ * points, out[4] duplicate signatures, out[5] binary128 re-decisions;
+ * *maxdev = largest coordinate deviation from the FP64 circumcentre. */
+int hvo_certify_mesh(int d, int64_t n, const double* pts, const double* lo, const double* hi, int np,
+                     const double* base, const double* normal, int64_t nv, const int64_t* sig, const double* r,
+                     int nthreads, int64_t* out, double* maxdev);
+
 /* Raw Philox4x32-10 block (for known-answer tests of the generator). */
 void hvo_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 

@@ -70,6 +70,10 @@ def lib():
             L.hvo_sample_cells.restype = I
             L.hvo_verify_vertices.argtypes = [I, I64, dp, dp, dp, I64, ip, dp, D]
             L.hvo_verify_vertices.restype = I64
+            L.hvo_polygon_cells.argtypes = [I, I64, dp, dp, dp, U64, I, I64, ip, I64, dp, ip, ip, dp]
+            L.hvo_polygon_cells.restype = I
+            L.hvo_certify_mesh.argtypes = [I, I64, dp, dp, dp, I, dp, dp, I64, ip, dp, I, ip, dp]
+            L.hvo_certify_mesh.restype = I
             u32p = ctypes.POINTER(ctypes.c_uint32)
             L.hvo_philox4x32.argtypes = [u32p, u32p, u32p]; L.hvo_philox4x32.restype = None
             L.hvo_mc_directions.argtypes = [I, I64, I, U64, dp]; L.hvo_mc_directions.restype = None
@@ -204,6 +208,62 @@ def sample_cells(pts, cells, seed=0, nthreads=0, lo=None, hi=None):
     if rc != 0:
         raise RuntimeError(lib().hvo_last_error().decode())
     return own.value, rays.value, sec.value
+
+
+def polygon_cells(pts, cells, lo=None, hi=None, seed=0, nthreads=0):
+    """VI_POLYGON of the listed cells (0-based), each from its own polytope:
+    (vol[ncells], offs[ncells+1], items (1-based neighbours), areas)."""
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    n, d = pts.shape
+    lo = np.ascontiguousarray(np.zeros(d) if lo is None else lo, dtype=np.float64)
+    hi = np.ascontiguousarray(np.ones(d) if hi is None else hi, dtype=np.float64)
+    cells = np.ascontiguousarray(cells, dtype=np.int64)
+    m = cells.shape[0]
+    cap = max(64, 8 * (d + 1) * 40 * m)
+    while True:
+        vol = np.zeros(m)
+        offs = np.zeros(m + 1, dtype=np.int64)
+        items = np.zeros(cap, dtype=np.int64)
+        area = np.zeros(cap)
+        rc = lib().hvo_polygon_cells(d, n, _dp(pts), _dp(lo), _dp(hi), seed, nthreads, m, _ip(cells), cap,
+                                     _dp(vol), _ip(offs), _ip(items), _dp(area))
+        if rc == -4:
+            cap = int(offs[-1])
+            continue
+        if rc != 0:
+            raise RuntimeError(lib().hvo_last_error().decode())
+        return vol, offs, items[:offs[-1]], area[:offs[-1]]
+
+
+def certify_mesh(pts, sig, r, lo=None, hi=None, planes=None, nthreads=0):
+    """Certificate of a vertex list that does not use the oracle's search: an
+    exact empty-sphere test of every vertex (kd-tree ball query, binary128 near
+    the sphere), exactly two end points per edge, no duplicate signature.
+    Returns a dict of violation counts (all zero for a Voronoi mesh), the
+    binary128 re-decisions and the largest coordinate deviation."""
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    n, d = pts.shape
+    sig = np.ascontiguousarray(sig, dtype=np.int64)
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    lo = np.ascontiguousarray(np.zeros(d) if lo is None else lo, dtype=np.float64)
+    hi = np.ascontiguousarray(np.ones(d) if hi is None else hi, dtype=np.float64)
+    if planes is not None:
+        base = np.ascontiguousarray(planes[0], dtype=np.float64)
+        normal = np.ascontiguousarray(planes[1], dtype=np.float64)
+        np_ = base.shape[0]
+    else:
+        base = normal = np.zeros(d)
+        np_ = 0
+    out = np.zeros(6, dtype=np.int64)
+    dev = ctypes.c_double()
+    rc = lib().hvo_certify_mesh(d, n, _dp(pts), _dp(lo), _dp(hi), np_, _dp(base), _dp(normal), sig.shape[0],
+                                _ip(sig), _dp(r), nthreads, _ip(out), ctypes.byref(dev))
+    if rc != 0:
+        raise RuntimeError(lib().hvo_last_error().decode())
+    keys = ("inside", "ties", "invalid", "open_edges", "duplicates", "quad_decisions")
+    res = {k: int(v) for k, v in zip(keys, out)}
+    res["max_coord_dev"] = dev.value
+    return res
 
 
 def philox4x32(ctr, key):

@@ -341,3 +341,57 @@ def test_reference_mc_directions_are_one_vector_per_batch():
     assert abs(r.sum() - 1.0) > 0.05
     again, _, _, _ = m.heuristic_mc(400, 3)   # the switch is off again
     np.testing.assert_array_equal(again, v)
+
+
+@pytest.mark.parametrize("d,n,seed", [(2, 800, 1), (3, 300, 2), (4, 200, 3), (5, 120, 4), (6, 50, 5)])
+def test_certificate_accepts_voronoi_meshes_and_catches_errors(d, n, seed):
+    """The search-independent certificate (empty spheres, two end points per
+    edge, unique signatures) passes on the oracle's meshes and flags a dropped
+    vertex, a duplicated one and a vertex whose signature lost a generator."""
+    X = D.uniform_points(d, n, seed)
+    s, r = O.OracleMesh(X).vertices()
+    c = O.certify_mesh(X, s, r)
+    assert all(c[k] == 0 for k in ("inside", "ties", "invalid", "open_edges", "duplicates"))
+    assert c["max_coord_dev"] < 1e-12
+    assert O.certify_mesh(X, s[1:], r[1:])["open_edges"] == d + 1
+    assert O.certify_mesh(X, np.vstack([s, s[:1]]), np.vstack([r, r[:1]]))["duplicates"] == 1
+    bad = s.copy()
+    other = next(j for j in range(1, n + 1) if j not in bad[0])
+    bad[0, 1] = other
+    bad[0] = np.sort(bad[0])
+    c = O.certify_mesh(X, bad, r)
+    assert c["inside"] + c["invalid"] >= 1 and c["open_edges"] > 0
+
+
+def test_certificate_on_plane_domains():
+    from _domains import simplex, simplex_points
+    base, normal, _ = simplex(3)
+    X = simplex_points(3, 200, 7)
+    s, r = O.OracleMesh(X, planes=(base, normal)).vertices()
+    c = O.certify_mesh(X, s, r, planes=(base, normal))
+    assert all(c[k] == 0 for k in ("inside", "ties", "invalid", "open_edges", "duplicates"))
+
+
+def test_certificate_reports_lattice_ties():
+    """More than d+1 co-spherical generators (a square lattice) are exact ties."""
+    g = (np.arange(4) + 0.5) / 4
+    X = np.array(np.meshgrid(g, g, indexing="ij")).reshape(2, -1).T.copy()
+    sig = np.array([[1, 2, 5]])   # three of the four corners around (0.25, 0.25)
+    c = O.certify_mesh(X, sig, np.array([[0.25, 0.25]]))
+    assert c["ties"] == 1 and c["inside"] == 0
+
+
+@pytest.mark.parametrize("d,n", [(2, 500), (3, 200), (4, 150), (5, 80)])
+def test_polygon_cells_match_the_mesh_pass(d, n):
+    """Cells integrated from their own polytope give the mesh pass's volumes and
+    areas (which copies the lower cell's interfaces) to rounding."""
+    X = D.uniform_points(d, n, 40 + d)
+    m = O.OracleMesh(X, integrate=True)
+    vol, area = m.polygon()
+    ro, rn = m.neighbors()
+    cells = np.arange(0, n, 3)
+    v, offs, items, a = O.polygon_cells(X, cells)
+    np.testing.assert_allclose(v, vol[cells], rtol=1e-12)
+    for c, i in enumerate(cells):
+        np.testing.assert_array_equal(items[offs[c]:offs[c + 1]], rn[ro[i]:ro[i + 1]])
+        np.testing.assert_allclose(a[offs[c]:offs[c + 1]], area[ro[i]:ro[i + 1]], rtol=1e-11, atol=1e-15)
