@@ -22,6 +22,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -55,12 +56,15 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-serve-capacity", action="store_true", help="skip the unbounded-rate serving run")
     ap.add_argument("--serve-integrator", choices=["polygon", "none"], default="polygon")
     ap.add_argument("--no-integrators", action="store_true")
     ap.add_argument("--knn", type=int, default=0, help="candidate list length (0 = library default)")
     ap.add_argument("--leaf-size", type=int, default=0, help="tree leaf size (0 = library default)")
     ap.add_argument("--seed-stride", type=int, default=0, help="one descent seed per this many generators (0 = default)")
     ap.add_argument("--mc-dirs", type=int, default=1000, help="directions per cell of VI_HEURISTIC_MC")
+    ap.add_argument("--no-c3", action="store_true", help="skip the 5D clustered 50k measurement")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 arm of the 5D measurement")
     return ap.parse_args()
 
 
@@ -181,40 +185,197 @@ def serve_requests(count, seed=2000):
 
 
 def run_serve(args, device):
-    import hvgpu
+    """The served stream twice: once at the offered Poisson rate (latency
+    percentiles of that load) and once with every request queued at the start
+    (the sustainable rate of the device, meshes per second)."""
     from hvgpu import datasets as D
     from hvgpu.serve import Server
     reqs, gaps = serve_requests(args.serve_requests)
     pts = [D.uniform_points(d, n, r) for d, n, r in reqs]
-    arrivals = np.cumsum(gaps / args.serve_rate)
     integ = None if args.serve_integrator == "none" else args.serve_integrator
-    with Server(device=device, slots=args.serve_slots) as srv:
-        # warm-up: one request per dimension
-        for d in (2, 3, 4, 5):
-            srv.result(srv.submit(D.uniform_points(d, 500, 10 ** 6 + d), integrator=integ))
+
+    def stream(arrivals):
+        with Server(device=device, slots=args.serve_slots) as srv:
+            for d in (2, 3, 4, 5):  # warm-up: one request per dimension
+                srv.result(srv.submit(D.uniform_points(d, 500, 10 ** 6 + d), integrator=integ))
+            t0 = time.perf_counter()
+            tickets = []
+            for p, ta in zip(pts, arrivals):
+                now = time.perf_counter() - t0
+                if ta > now:
+                    time.sleep(ta - now)
+                tickets.append(srv.submit(p, integrator=integ))
+            lat, svc, fails, verts = [], [], 0, 0
+            for t in tickets:
+                r = srv.result(t)
+                if r["status"] != 0:
+                    fails += 1
+                    continue
+                lat.append(r["latency_ms"])
+                svc.append(r["service_ms"])
+                verts += r["sig"].shape[0]
+            t_end = time.perf_counter() - t0
+        return np.array(lat), np.array(svc), fails, verts, t_end
+
+    lat, svc, fails, verts, t_end = stream(np.cumsum(gaps / args.serve_rate))
+    out = {"requests": len(reqs), "rate_per_s": args.serve_rate, "slots": args.serve_slots, "failures": fails,
+           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+           "mean_ms": float(lat.mean()), "meshes_per_s": len(lat) / t_end, "vertices": int(verts),
+           "service_p50_ms": float(np.percentile(svc, 50)), "service_p99_ms": float(np.percentile(svc, 99)),
+           "service_max_ms": float(svc.max()),
+           "config": "d uniform {2,3,4,5}, N log-uniform [200,20000], uniform points seed=request id, "
+                     "cuboid(d, periodic=[]), " + ("VI_POLYGON" if integ else "no integrator") +
+                     ", Poisson arrivals"}
+    if not args.no_serve_capacity:
+        clat, _, cfails, _, ct = stream(np.zeros(len(pts)))
+        out["capacity"] = {"meshes_per_s": len(clat) / ct, "failures": cfails, "seconds": ct,
+                           "note": "all requests queued at t=0: the sustainable rate"}
+    return out
+
+
+def fp32_peak_tflops(local, clocks):
+    """Nominal FP32 rate: SMs x 128 FP32 lanes x 2 flops x max SM clock."""
+    import torch
+    prop = torch.cuda.get_device_properties(local)
+    fmax = (clocks or {}).get("sm_max_mhz") or 2070.0
+    return prop.multi_processor_count * 128 * 2 * fmax * 1e6 / 1e12
+
+
+FP64_PEAK_TFLOPS = 1.25  # nominal GB300 FP64 rate; no measured FP64 peak exists for this pool
+
+
+def poly_flops(d, V):
+    """Algorithmic FP64 work of VI_POLYGON: sum over cells of E_cell (d-1)! 2 d^2
+    with E_cell = d V_cell / 2 and sum V_cell = (d+1) V (the flags of the
+    reference's decomposition)."""
+    return d * (d + 1) * V / 2.0 * math.factorial(d - 1) * 2 * d * d
+
+
+def run_c3(args, ctx, local, flush, clocks):
+    """The 5D clustered N=50,000 mesh (seed 2): the batched split-precision
+    search against the plain one-ray-per-thread FP64 search and the host CPU,
+    then VI_POLYGON and VI_HEURISTIC_MC (1,000 directions per cell) on the GPU
+    and the same phases in the CPU oracle."""
+    import torch
+    import hvgpu
+    from hvgpu import datasets as D
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    name = "5d_clustered_50k"
+    w = D.WORKLOADS[name]
+    pts = D.workload_points(name)
+    n, d = pts.shape
+    lo, hi = np.zeros(d), np.ones(d)
+    dev_pts = torch.from_numpy(np.ascontiguousarray(pts)).cuda()
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    out = {"workload": f"{d}d_clustered_{n}", "d": d, "n_points": n, "seed": w["seed"],
+           "boundary": "cuboid(d, periodic=[])", "l2": "flushed (256 MiB write) before every timed step"}
+
+    def timed(params, steps, warm):
+        for _ in range(warm):
+            hvgpu.Mesh(ctx, np.array([n, d]), lo, hi, params, device_ptr=dev_pts.data_ptr()).free()
+        tot, verts, sts = 0.0, 0, []
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            m = hvgpu.Mesh(ctx, np.array([n, d]), lo, hi, params, device_ptr=dev_pts.data_ptr())
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+            st = m.stats()
+            sts.append(st)
+            verts += st["vertices"]
+            m.free()
+        return verts / (tot / 1e3), tot / steps, sts
+
+    steps = max(1, min(args.steps, 5))
+    fv, fms, fst = timed(hvgpu.make_params(hvgpu.HV_METHOD_FAST), steps, max(args.warmup, 3))
+    st0 = fst[-1]
+    V = st0["vertices"]
+    out["fast"] = {"vertices_per_s": fv, "ms_per_step": fms, "steps": steps, "vertices": V,
+                   "rays_per_s": st0["rays"] / (fms / 1e3), "levels": st0["levels"],
+                   "breakdown_ms": {k: statistics.mean(s[k] for s in fst) for k in
+                                    ("ms_prepare", "ms_knn", "ms_descent", "ms_expand", "ms_fallback",
+                                     "ms_centers", "ms_canonical")}}
+    if not args.no_plain:
+        pv, pms, pst = timed(hvgpu.make_params(hvgpu.HV_METHOD_PLAIN), 1, 0)
+        assert pst[-1]["vertices"] == V
+        out["plain"] = {"vertices_per_s": pv, "ms_per_step": pms, "steps": 1,
+                        "method": "one ray per thread, FP64 shrinking-ball tree search from the root"}
+        out["fast_over_plain"] = fv / pv
+    # roofline: FP32 issue pipe for the candidate scan, FP64 pipe for the centres
+    m = hvgpu.Mesh(ctx, np.array([n, d]), lo, hi, hvgpu.make_params(hvgpu.HV_METHOD_FAST),
+                   device_ptr=dev_pts.data_ptr())
+    offs, nbr = m.neighbors()
+    nbar = len(nbr) / n
+    p32 = fp32_peak_tflops(local, clocks)
+    exp_ms = out["fast"]["breakdown_ms"]["ms_expand"]
+    f32 = V * nbar * (5 * d + 3)
+    cen_ms = out["fast"]["breakdown_ms"]["ms_centers"]
+    f64 = V * ((2.0 / 3.0) * d ** 3 + 4 * d * d)
+    out["roofline"] = {
+        "k_expand_fast": {"bound": "fp32", "unit": "TFLOP/s", "algorithmic_flops_per_vertex": nbar * (5 * d + 3),
+                          "achieved": f32 / (exp_ms / 1e3) / 1e12, "peak": p32,
+                          "frac": f32 / (exp_ms / 1e3) / 1e12 / p32, "peak_source": "nominal"},
+        "k_centers": {"bound": "fp64", "unit": "TFLOP/s", "algorithmic_flops_per_vertex": (2.0 / 3.0) * d ** 3 + 4 * d * d,
+                      "achieved": f64 / (cen_ms / 1e3) / 1e12, "peak": FP64_PEAK_TFLOPS,
+                      "frac": f64 / (cen_ms / 1e3) / 1e12 / FP64_PEAK_TFLOPS, "peak_source": "nominal"}}
+    # integrators on the same mesh, outputs in HBM (hv_integrate_*_device)
+    dvol = torch.empty(n, dtype=torch.float64, device="cuda")
+    darea = torch.empty(max(len(nbr), 1), dtype=torch.float64, device="cuda")
+    integ = {}
+    for key, fn in (("polygon", lambda: m.polygon_device(dvol.data_ptr(), darea.data_ptr())),
+                    ("heuristic_mc", lambda: m.heuristic_mc_device(args.mc_dirs, 7, dvol.data_ptr(),
+                                                                    darea.data_ptr()))):
+        fn()
+        ts = []
+        for _ in range(max(1, min(args.steps, 3))):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        integ[key] = {"ms": 1e3 * statistics.mean(ts), "cells_per_s": n / statistics.mean(ts)}
+    st = m.stats()
+    poly_dev_ms = st["ms_poly_incidence"] + st["ms_poly_facets"] + st["ms_poly_big"]
+    integ["polygon"].update({"device_ms": poly_dev_ms, "ms_poly_facets": st["ms_poly_facets"],
+                             "ms_poly_big": st["ms_poly_big"], "poly_big_facets": st["poly_big_facets"]})
+    pf = poly_flops(d, V)
+    out["roofline"]["k_poly_facets"] = {
+        "bound": "fp64", "unit": "TFLOP/s", "algorithmic_flops": pf,
+        "achieved": pf / (poly_dev_ms / 1e3) / 1e12, "peak": FP64_PEAK_TFLOPS,
+        "frac": pf / (poly_dev_ms / 1e3) / 1e12 / FP64_PEAK_TFLOPS, "peak_source": "nominal",
+        "note": "flags of the reference's decomposition; the GPU's pulling decomposition does fewer operations"}
+    integ["heuristic_mc"]["directions_per_cell"] = args.mc_dirs
+    m.free()
+    # the host CPU on the same phases (the oracle, OpenMP on every host core)
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        cells = np.arange(0, n, 20)
+        own, rays, sec = O.sample_cells(pts, cells, nthreads=threads)
+        out["cpu_baseline"] = {"value": own / sec, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"per-cell search of {len(cells)} of the {n} cells (every 20th), vertices "
+                                         f"owned per second (C++ restatement of the reference algorithm, OpenMP)"}
+        out["fast_over_cpu"] = fv / (own / sec)
+        pc = np.arange(0, n, 100)
         t0 = time.perf_counter()
-        tickets = []
-        for k, (p, ta) in enumerate(zip(pts, arrivals)):
-            now = time.perf_counter() - t0
-            if ta > now:
-                time.sleep(ta - now)
-            tickets.append(srv.submit(p, integrator=integ))
-        lat, fails, verts = [], 0, 0
-        for t in tickets:
-            r = srv.result(t)
-            if r["status"] != 0:
-                fails += 1
-                continue
-            lat.append(r["latency_ms"])
-            verts += r["sig"].shape[0]
-        t_end = time.perf_counter() - t0
-    lat = np.array(lat)
-    return {"requests": len(reqs), "rate_per_s": args.serve_rate, "slots": args.serve_slots, "failures": fails,
-            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "mean_ms": float(lat.mean()), "meshes_per_s": len(lat) / t_end, "vertices": int(verts),
-            "config": "d uniform {2,3,4,5}, N log-uniform [200,20000], uniform points seed=request id, "
-                      "cuboid(d, periodic=[]), " + ("VI_POLYGON" if integ else "no integrator") +
-                      ", Poisson arrivals"}
+        O.polygon_cells(pts, pc, nthreads=threads)
+        tp = time.perf_counter() - t0
+        integ["polygon"]["cpu"] = {"cells_per_s": len(pc) / tp, "cores": threads, "kind": "port",
+                                   "sample": f"{len(pc)} of the {n} cells (every 100th), each cell's search and "
+                                             f"flag-decomposition integral"}
+        ref = O.OracleMesh(pts, csr=(offs, nbr))
+        t0 = time.perf_counter()
+        ref.heuristic_mc(args.mc_dirs, 7, nthreads=threads)
+        tm = time.perf_counter() - t0
+        integ["heuristic_mc"]["cpu"] = {"cells_per_s": n / tm, "ms": 1e3 * tm, "cores": threads, "kind": "port",
+                                        "sample": f"all {n} cells on the GPU's neighbour lists, "
+                                                  f"{args.mc_dirs} directions per cell"}
+    out["integrators"] = integ
+    return out
 
 
 def run_reference(args):
@@ -362,36 +523,34 @@ def run_ours(args):
     traffic = None
     if tr and tr.get("d") == d:
         traffic = tr["dram_bytes_per_vertex"] * Vs / launches
-    roof = {"bound": "hbm", "kernel": "k_expand_fast" if method == hvgpu.HV_METHOD_FAST else "k_expand_plain",
-            "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-            "traffic": traffic, "peak_source": peak_kind,
-            "traffic_note": "ncu DRAM bytes with its default cache flush before every launch: the candidate lists "
-                            "are re-read from DRAM at every wavefront level, which L2 holds in an unprofiled run",
-            "alg_bytes_per_launch": alg_bytes / launches, "ms_per_launch": exp_ms / launches,
-            "launches_per_step": launches}
-    # FP32 view (the binding pipe of the candidate scan): n_bar (5d+3) flops per vertex, n_bar = mean
-    # neighbour count of the mesh; peak = SMs x 128 FP32 lanes x 2 x max SM clock (nominal)
-    try:
-        mm = build_dev()
-        _, nnbr = mm.counts(neighbors=True)
-        mm.free()
-        nbar = nnbr / n
-        prop = torch.cuda.get_device_properties(local)
-        fmax = (clocks or {}).get("sm_max_mhz") or 2070.0
-        fp32_peak = prop.multi_processor_count * 128 * 2 * fmax * 1e6 / 1e12
-        fl = Vs * nbar * (5 * d + 3)
-        ach = fl / (exp_ms / 1e3) / 1e12
-        roof["fp32"] = {"algorithmic_flops_per_vertex": nbar * (5 * d + 3), "mean_neighbours": nbar,
-                        "achieved_tflops": ach, "peak_tflops_nominal": fp32_peak, "frac": ach / fp32_peak}
-    except Exception as ex:  # noqa: BLE001
-        roof["fp32"] = {"error": str(ex)}
+    kernel = "k_expand_fast" if method == hvgpu.HV_METHOD_FAST else "k_expand_plain"
+    hbm = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+           "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
+           "traffic_note": "ncu DRAM bytes with its default cache flush before every launch: the candidate lists "
+                           "are re-read from DRAM at every wavefront level, which L2 holds in an unprofiled run",
+           "alg_bytes_per_launch": alg_bytes / launches, "ms_per_launch": exp_ms / launches,
+           "launches_per_step": launches}
+    # The binding roof of the candidate scan is the FP32 issue pipe (the working set lives in L2):
+    # n_bar (5d+3) flops per vertex, n_bar = mean neighbour count of the mesh; peak = SMs x 128 FP32
+    # lanes x 2 x max SM clock (nominal; no measured FP32 peak exists for this machine)
+    mm = build_dev()
+    _, nnbr = mm.counts(neighbors=True)
+    mm.free()
+    nbar = nnbr / n
+    fp32_peak = fp32_peak_tflops(local, clocks)
+    fl = Vs * nbar * (5 * d + 3)
+    ach = fl / (exp_ms / 1e3) / 1e12
+    roof = {"bound": "fp32", "kernel": kernel, "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": ach / fp32_peak, "traffic": traffic, "peak_source": "nominal",
+            "algorithmic_flops_per_vertex": nbar * (5 * d + 3), "mean_neighbours": nbar,
+            "ms_per_launch": exp_ms / launches, "launches_per_step": launches, "hbm": hbm}
     # FP64 view of the circumcentre solves: (2/3)d^3 + 4d^2 flops per vertex against the nominal
     # GB300 FP64 rate (1.25 TFLOP/s; no measured FP64 peak exists for this machine)
     cen_ms = statistics.mean(s["ms_centers"] for s in stats)
     f64 = Vs * ((2.0 / 3.0) * d ** 3 + 4 * d * d)
     roof["fp64"] = {"kernel": "k_centers", "algorithmic_flops_per_vertex": (2.0 / 3.0) * d ** 3 + 4 * d * d,
-                    "achieved_tflops": f64 / (cen_ms / 1e3) / 1e12, "peak_tflops_nominal": 1.25,
-                    "frac": f64 / (cen_ms / 1e3) / 1e12 / 1.25}
+                    "achieved_tflops": f64 / (cen_ms / 1e3) / 1e12, "peak_tflops_nominal": FP64_PEAK_TFLOPS,
+                    "frac": f64 / (cen_ms / 1e3) / 1e12 / FP64_PEAK_TFLOPS}
     # ---- CPU baseline on the host cores
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
@@ -402,6 +561,12 @@ def run_ours(args):
         cpu = {"value": own / sec, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"per-cell search of {len(cells)} of the {n} cells, vertices owned per second "
                          f"(C++ restatement of the reference algorithm, OpenMP)"}
+    c3 = None
+    if not args.no_c3 and ws == 1:
+        try:
+            c3 = run_c3(args, ctx, local, flush, clocks)
+        except Exception as e:  # the headline line must still print
+            c3 = {"error": repr(e)}
     serving = None
     if not args.no_serve and ws == 1:
         try:
@@ -423,7 +588,7 @@ def run_ours(args):
                                           "fallback_nodes", "fallback_leaves", "fallback_points",
                                           "ambiguous_sets")},
             "rays_per_s": st0["rays"] / (tot_ms / 1e3 / args.steps),
-            "breakdown_ms": breakdown, "serving": serving}
+            "breakdown_ms": breakdown, "c3_5d_clustered_50k": c3, "serving": serving}
     print(json.dumps(line), flush=True)
 
 

@@ -1333,6 +1333,24 @@ int hvo_heuristic_mc(const hvo_mesh* m, int ndir, uint64_t seed, int nthreads,
     return 0;
 }
 
+/* A mesh object holding only a given neighbour CSR (1-based items, planes
+ * n+p of the box [lo, hi]), for running the oracle's integrators on the
+ * neighbour lists of another mesh (phase timing). */
+int hvo_mesh_from_csr(int d, int64_t n, const double* pts, const double* lo, const double* hi,
+                      const int64_t* offs, const int64_t* nbr, hvo_mesh** out) {
+    if (d < 2 || d > MAXD || n <= 0 || !out) { set_err("invalid argument"); return -1; }
+    hvo_mesh* M = new hvo_mesh();
+    Problem& P = M->P;
+    P.d = d; P.n = (int)n;
+    P.X.assign(pts, pts + (size_t)n * d);
+    set_box_planes(P, lo, hi);
+    M->offs.assign(offs, offs + n + 1);
+    M->nbr.resize(offs[n]);
+    for (int64_t t = 0; t < offs[n]; ++t) M->nbr[t] = (int)(nbr[t] - 1);
+    *out = M;
+    return 0;
+}
+
 void hvo_get_stats(const hvo_mesh* m, hvo_stats* st) {
     st->rays = m->cnt.rays; st->descents = m->cnt.descents; st->descent_retries = m->cnt.descent_retries;
     st->quad_rescores = m->cnt.quad; st->degenerate = m->cnt.degenerate;

@@ -63,6 +63,10 @@ int hvo_heuristic_mc(const hvo_mesh* m, int ndir, uint64_t seed, int nthreads,
  * cells (new_directions! never resets its rejection flag,
  * src/mcintegrator.jl:82-95).  0 restores the i.i.d. estimator. */
 void hvo_set_mc_reference_directions(int recycle);
+/* A mesh holding only the given neighbour CSR (offs n+1, nbr 1-based, planes
+ * n+p of the box [lo, hi]): hvo_heuristic_mc runs on it (phase timing). */
+int hvo_mesh_from_csr(int d, int64_t n, const double* pts, const double* lo, const double* hi,
+                      const int64_t* offs, const int64_t* nbr, hvo_mesh** out);
 void hvo_get_stats(const hvo_mesh* m, hvo_stats* st);
 const char* hvo_last_error(void);
 void hvo_free(hvo_mesh* m);

@@ -70,6 +70,8 @@ def lib():
             L.hvo_sample_cells.restype = I
             L.hvo_verify_vertices.argtypes = [I, I64, dp, dp, dp, I64, ip, dp, D]
             L.hvo_verify_vertices.restype = I64
+            L.hvo_mesh_from_csr.argtypes = [I, I64, dp, dp, dp, ip, ip, ctypes.POINTER(P)]
+            L.hvo_mesh_from_csr.restype = I
             L.hvo_polygon_cells.argtypes = [I, I64, dp, dp, dp, U64, I, I64, ip, I64, dp, ip, ip, dp]
             L.hvo_polygon_cells.restype = I
             L.hvo_certify_mesh.argtypes = [I, I64, dp, dp, dp, I, dp, dp, I64, ip, dp, I, ip, dp]
@@ -93,15 +95,25 @@ def _ip(a):
 class OracleMesh:
     """Result of one oracle mesh build (1-based reference index conventions)."""
 
-    def __init__(self, pts, lo=None, hi=None, seed=0, nthreads=0, mode=0, integrate=False, planes=None):
+    def __init__(self, pts, lo=None, hi=None, seed=0, nthreads=0, mode=0, integrate=False, planes=None,
+                 csr=None):
         """Box [lo, hi] (default unit cube), or the convex domain of
-        ``planes = (base, normal)``, (P, d) arrays each."""
+        ``planes = (base, normal)``, (P, d) arrays each.  ``csr = (offs, nbr)``
+        (1-based neighbours) skips the search and holds only those neighbour
+        lists, for running the integrators on another mesh's lists."""
         L = lib()
         pts = np.ascontiguousarray(pts, dtype=np.float64)
         self.n, self.d = pts.shape
         self.pts = pts
         h = ctypes.c_void_p()
-        if planes is not None:
+        if csr is not None:
+            self.lo = np.ascontiguousarray(np.zeros(self.d) if lo is None else lo, dtype=np.float64)
+            self.hi = np.ascontiguousarray(np.ones(self.d) if hi is None else hi, dtype=np.float64)
+            offs = np.ascontiguousarray(csr[0], dtype=np.int64)
+            nbr = np.ascontiguousarray(csr[1], dtype=np.int64)
+            rc = L.hvo_mesh_from_csr(self.d, self.n, _dp(pts), _dp(self.lo), _dp(self.hi), _ip(offs), _ip(nbr),
+                                     ctypes.byref(h))
+        elif planes is not None:
             base = np.ascontiguousarray(planes[0], dtype=np.float64)
             normal = np.ascontiguousarray(planes[1], dtype=np.float64)
             self.lo = self.hi = None
