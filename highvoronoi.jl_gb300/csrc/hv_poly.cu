@@ -123,42 +123,11 @@ struct Grp {
     }
 };
 
-// Compare-exchange stages of distance j = 16 .. 1 of the bitonic merge of
-// width k on element e = 32 r + lane, held in a register: the partner e ^ j is
-// lane ^ j of the same warp.
-template <class K>
-__device__ __forceinline__ K bitonic_lanes(K v, int e, int k, int jtop) {
-    const int lane = e & 31;
-    const bool up = (e & k) == 0;
-    for (int j = jtop; j > 0; j >>= 1) {
-        const K p = __shfl_xor_sync(0xFFFFFFFFu, v, j);
-        const bool lower = (lane & j) == 0;
-        v = (lower == up) ? (p < v ? p : v) : (p < v ? v : p);
-    }
-    return v;
-}
-
-// Ascending bitonic sort of a[0 .. n2), n2 a power of two.  The stages of
-// distance below 32 run in registers with warp shuffles (one shared-memory
-// load and store per element for each run of them, no bank conflicts); the
-// wider ones in shared memory, where 32 consecutive threads touch 32
-// consecutive keys.  The compare-exchange network is the plain bitonic one.
 template <int NW, class K>
 __device__ void g_sort(K* a, int n2, const Grp<NW>& g) {
-    const int lane = g.rank & 31, w = g.rank >> 5;
-    const int nch = (n2 + 31) >> 5;
     g.sync();
-    // widths 2 .. 32 inside every chunk of 32 (a short array is padded with the
-    // largest key, which sorts to the unused end)
-    for (int r = w; r < nch; r += NW) {
-        const int e = (r << 5) | lane;
-        K v = e < n2 ? a[e] : ~(K)0;
-        for (int k = 2; k <= 32; k <<= 1) v = bitonic_lanes<K>(v, e, k, k >> 1);
-        if (e < n2) a[e] = v;
-    }
-    g.sync();
-    for (int k = 64; k <= n2; k <<= 1) {
-        for (int j = k >> 1; j >= 32; j >>= 1) {
+    for (int k = 2; k <= n2; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
             for (int q = g.rank; q < (n2 >> 1); q += g.size) {
                 const int x = ((q & ~(j - 1)) << 1) | (q & (j - 1));
                 const int y = x | j;
@@ -168,12 +137,6 @@ __device__ void g_sort(K* a, int n2, const Grp<NW>& g) {
             }
             g.sync();
         }
-        for (int r = w; r < nch; r += NW) {
-            const int e = (r << 5) | lane;
-            a[e] = bitonic_lanes<K>(a[e], e, k, 16);
-        }
-        g.sync();
-    }
 }
 
 // Stream compaction over x < n: write(x, rank of x among the kept) for
