@@ -71,6 +71,9 @@ struct hv_mesh {
     short* img_code = nullptr;         // nimg shift codes sum (s_k + 1) 3^k
     signed char* pshift = nullptr;     // nnbr x d lattice shifts of the neighbours
     int* pperm = nullptr;              // nnbr: position in the extended row
+    // shard of a mesh split over ranks: generators own0 .. own1-1 of the
+    // internal (Morton) order (-1: the whole mesh)
+    int own0 = -1, own1 = -1;
 };
 
 namespace {
@@ -281,6 +284,9 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     DevMesh M;
     std::memset(&M, 0, sizeof(M));
     M.d = d; M.n = n; M.dp = DP;
+    const bool shard = mesh->own0 >= 0;
+    M.own0 = shard ? mesh->own0 : 0;
+    M.own1 = shard ? mesh->own1 : n;
     double xs = 0;
     for (int k = 0; k < d; ++k) {
         M.lo[k] = mesh->lo[k]; M.hi[k] = mesh->hi[k];
@@ -320,7 +326,9 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     K = std::min(K, std::max(n - 1, 0));
     K = std::min(K, 480);
     M.K = fast ? K : 0;
-    const int stride = mesh->prm.seed_stride > 0 ? mesh->prm.seed_stride : default_seed_stride(n);
+    // a shard seeds every one of its generators: its cells need not be connected
+    // to each other through shared vertices
+    const int stride = shard ? 1 : (mesh->prm.seed_stride > 0 ? mesh->prm.seed_stride : default_seed_stride(n));
     bool knn_side = false;
     if (fast) {
         int* knn = prep.get<int>((size_t)n * std::max(K, 1));
@@ -344,7 +352,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     // ---- search with capacity retry
     double factor = mesh->prm.capacity_factor > 0 ? mesh->prm.capacity_factor : 1.3;
     unsigned long long est = (unsigned long long)(vertices_per_point(d) * n) + (1ull << d) + 1024;
-    const int nseeds = (n + stride - 1) / stride;
+    const int nseeds = (M.own1 - M.own0 + stride - 1) / stride;
     std::unique_ptr<Scratch> srch;
     unsigned V = 0;
     for (int attempt = 0;; ++attempt) {
@@ -414,8 +422,9 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         kt.run(F_DESCENT, 1, [&] { launch_descent(M, stride, nseeds, dseed, dfail, ndfail, ctx->nsm, st); });
         CK(cudaGetLastError());
         read_stat(ctx, dstat);
-        if (fast && ctx->h_stat[0] == 0 && !(ctx->h_stat[1] & (ST_VCAP | ST_HASH))) {
-            // no FP32 seed was decided: the exact descent on the undecided ones
+        if (fast && (ctx->h_stat[0] == 0 || shard) && !(ctx->h_stat[1] & (ST_VCAP | ST_HASH))) {
+            // no FP32 seed was decided (or a shard, whose every cell needs its
+            // seed): the exact descent on the undecided ones
             kt.run(F_DESCENT, 1, [&] { launch_descent_exact(M, nseeds, dseed, dfail, ndfail, ctx->nsm, st); });
             CK(cudaGetLastError());
             read_stat(ctx, dstat);
@@ -595,6 +604,10 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     S.fallback_leaves = (int64_t)hc[C_FBLEAVES];
     S.fallback_points = (int64_t)hc[C_FBPOINTS];
     S.ambiguous_sets = (int64_t)hc[C_AMBSET];
+    if (shard) {  // the vertices the shard owns sort first
+        mesh->V = (unsigned)hc[C_OWNED];
+        S.vertices = mesh->V;
+    }
     double fam[F_N];
     kt.totals(fam);
     S.ms_knn = fam[F_KNN];
@@ -758,6 +771,44 @@ int build_entry(hv_ctx* ctx, int d, int64_t n, const double* src, bool on_device
         ctx->err = "unknown method";
         return HV_E_INVALID_ARG;
     }
+    try {
+        CK(cudaSetDevice(ctx->device));
+        build_impl(ctx, m, src, on_device, src);
+    } catch (const HvError& e) {
+        hv_mesh_free(m);
+        return fail(ctx, e);
+    } catch (const std::bad_alloc&) {
+        hv_mesh_free(m);
+        ctx->err = "host allocation failed";
+        return HV_E_OOM;
+    }
+    *out = m;
+    return HV_OK;
+}
+
+// One shard of the box mesh split over nranks ranks: the generators of range
+// `rank` of the internal (Morton) order, the vertices whose smallest generator
+// lies in that range.
+int shard_entry(hv_ctx* ctx, int d, int64_t n, const double* src, bool on_device, const double* lo,
+                const double* hi, int rank, int nranks, const hv_params* params, hv_mesh** out) {
+    if (!ctx || !out) return HV_E_INVALID_ARG;
+    if (nranks < 1 || rank < 0 || rank >= nranks) { ctx->err = "rank outside 0 .. nranks-1"; return HV_E_INVALID_ARG; }
+    int rc = validate_common(ctx, d, n, lo, hi, out);
+    if (rc != HV_OK) return rc;
+    if (n > 0 && !src) { ctx->err = "null point array"; return HV_E_INVALID_ARG; }
+    hv_params p;
+    if (params) p = *params; else hv_params_default(&p);
+    if (p.method != HV_METHOD_FAST) { ctx->err = "shards use the fast method"; return HV_E_INVALID_ARG; }
+    std::unique_ptr<hv_mesh> mp(new hv_mesh());
+    hv_mesh* m = mp.get();
+    m->ctx = ctx; m->d = d; m->n = (int)n;
+    for (int k = 0; k < d; ++k) { m->lo[k] = lo[k]; m->hi[k] = hi[k]; }
+    m->np = 2 * d;
+    hv::box_planes(d, lo, hi, m->planes);
+    m->prm = p;
+    m->own0 = (int)((n * rank) / nranks);
+    m->own1 = (int)((n * (rank + 1)) / nranks);
+    mp.release();
     try {
         CK(cudaSetDevice(ctx->device));
         build_impl(ctx, m, src, on_device, src);
@@ -1175,6 +1226,10 @@ int periodic_integrate(hv_mesh* m, double* vol, double* area, bool dev_out, F&& 
 }
 
 int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out) {
+    if (m && m->own0 >= 0) {  // a shard holds only its own vertices
+        m->ctx->err = "integrate the merged mesh, not a shard";
+        return HV_E_INVALID_ARG;
+    }
     if (!m || (m->n > 0 && !vol)) return HV_E_INVALID_ARG;
     if (m->ext) {
         if (m->nnbr > 0 && !area) return HV_E_INVALID_ARG;
@@ -1306,6 +1361,10 @@ int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out) {
 }
 
 int mc_impl(hv_mesh* m, int ndir, uint64_t seed, double* vol, double* area, bool dev_out) {
+    if (m && m->own0 >= 0) {  // a shard holds only its own vertices
+        m->ctx->err = "integrate the merged mesh, not a shard";
+        return HV_E_INVALID_ARG;
+    }
     if (!m || ndir <= 0 || (m->n > 0 && !vol)) return HV_E_INVALID_ARG;
     if (m->ext) {
         if (m->nnbr > 0 && !area) return HV_E_INVALID_ARG;
@@ -1375,6 +1434,16 @@ int hv_integrate_heuristic_mc(hv_mesh* m, int ndir, uint64_t seed, double* vol, 
 
 int hv_integrate_heuristic_mc_device(hv_mesh* m, int ndir, uint64_t seed, double* d_vol, double* d_area) {
     return mc_impl(m, ndir, seed, d_vol, d_area, true);
+}
+
+int hv_mesh_build_shard(hv_ctx* ctx, int d, int64_t n, const double* pts, const double* lo, const double* hi,
+                        int rank, int nranks, const hv_params* params, hv_mesh** out) {
+    return shard_entry(ctx, d, n, pts, false, lo, hi, rank, nranks, params, out);
+}
+
+int hv_mesh_build_shard_device(hv_ctx* ctx, int d, int64_t n, const double* d_pts, const double* lo,
+                               const double* hi, int rank, int nranks, const hv_params* params, hv_mesh** out) {
+    return shard_entry(ctx, d, n, d_pts, true, lo, hi, rank, nranks, params, out);
 }
 
 int hv_mesh_build_periodic(hv_ctx* ctx, int d, int64_t n, const double* pts, const double* lo, const double* hi,

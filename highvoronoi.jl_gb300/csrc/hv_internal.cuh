@@ -45,7 +45,7 @@ enum : unsigned {
 
 enum {
     C_RAYS = 0, C_FALLBACK, C_UNCERT, C_INSECURE, C_DD, C_DEGEN, C_DESCENT, C_DRETRY, C_EDGECLOSED,
-    C_FBTREE, C_FBNODES, C_FBLEAVES, C_FBPOINTS, C_AMBSET,
+    C_FBTREE, C_FBNODES, C_FBLEAVES, C_FBPOINTS, C_AMBSET, C_OWNED,
     C_NCOUNT
 };
 
@@ -82,6 +82,10 @@ struct DevBox {
 
 struct DevMesh {
     int d, n;
+    // generators own0 .. own1-1 (internal order) belong to this build; a shard
+    // of a mesh split over ranks walks only edges that keep one of them and
+    // keeps the vertices whose smallest generator is one of them (0, n: all)
+    int own0, own1;
     int leaf, nleaves, P;
     int K, dp;
     unsigned vcap;

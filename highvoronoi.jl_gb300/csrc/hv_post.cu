@@ -15,7 +15,19 @@ namespace hv {
 
 template <int D>
 __global__ void k_canon_keys(DevMesh M, unsigned V, unsigned* keys) {
+    const bool shard = M.own0 > 0 || M.own1 < M.n;
     for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        if (shard) {
+            // a shard keeps the vertices whose smallest generator (internal order) it
+            // owns; the others get the largest key and sort behind them
+            const int s0 = M.vsig[(size_t)v * (D + 1)];
+            if (s0 < M.own0 || s0 >= M.own1) {
+#pragma unroll
+                for (int k = 0; k <= D; ++k) keys[(size_t)k * V + v] = 0xFFFFFFFFu;
+                continue;
+            }
+            count_add(M.cnt + C_OWNED);
+        }
         unsigned s[D + 1];
 #pragma unroll
         for (int k = 0; k <= D; ++k) {

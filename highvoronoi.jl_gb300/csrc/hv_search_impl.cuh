@@ -682,10 +682,17 @@ __device__ void exact_walk(const DevMesh& M, unsigned v, int m) {
 }
 
 // Edge sig \ {sig[m]} is walkable if it is not the edge the vertex was found
-// through and if it still contains a real generator.
+// through and if it still contains a real generator (in a shard: one of the
+// shard's own generators, so that only the shard's cells are explored).
 template <int D>
 __device__ __forceinline__ bool walkable(const DevMesh& M, const int (&sig)[D + 1], int vnew, int m) {
     if (sig[m] == vnew) return false;
+    if (M.own0 > 0 || M.own1 < M.n) {
+        bool own = false;
+#pragma unroll
+        for (int s = 0; s <= D; ++s) own |= (s != m && sig[s] >= M.own0 && sig[s] < M.own1);
+        return own;
+    }
     if (m == 0) return sig[1] < M.n;
     return true;
 }
@@ -765,8 +772,8 @@ __global__ void __launch_bounds__(128) k_descent(DevMesh M, int stride, int nsee
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (list && idx >= (int)*nlist) return;
     if (!list && idx >= nseeds) return;
-    const int i = list ? list[idx] : idx * stride;
-    if (i >= M.n) return;
+    const int i = list ? list[idx] : M.own0 + idx * stride;
+    if (i >= M.own1) return;
     count_add(M.cnt + C_DESCENT);
     for (int attempt = 0; attempt < 16; ++attempt) {
         Query<D> q;
@@ -2297,8 +2304,8 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_descent_warp(DevMesh M, int str
     const unsigned FULL = 0xFFFFFFFFu;
     const float S32 = 5.9604645e-08f;
     for (int w = blockIdx.x * FB_WPB + wib; w < nseeds; w += gridDim.x * FB_WPB) {
-        const int i = w * stride;
-        if (i >= M.n) continue;
+        const int i = M.own0 + w * stride;
+        if (i >= M.own1) continue;
         if (lane == 0) count_add(M.cnt + C_DESCENT);
         int T[D + 1];
 #pragma unroll

@@ -134,6 +134,11 @@ def load(path: str | None = None):
         L.hv_mesh_build_periodic_device.argtypes = [P, I, I64, P, dp, dp, i32p, ctypes.POINTER(Params),
                                                     ctypes.POINTER(P)]
         L.hv_mesh_build_periodic_device.restype = I
+        L.hv_mesh_build_shard.argtypes = [P, I, I64, P, dp, dp, I, I, ctypes.POINTER(Params), ctypes.POINTER(P)]
+        L.hv_mesh_build_shard.restype = I
+        L.hv_mesh_build_shard_device.argtypes = [P, I, I64, P, dp, dp, I, I, ctypes.POINTER(Params),
+                                                 ctypes.POINTER(P)]
+        L.hv_mesh_build_shard_device.restype = I
         L.hv_mesh_periodic_shifts.argtypes = [P, i8p]; L.hv_mesh_periodic_shifts.restype = I
         L.hv_mesh_periodic_images.argtypes = [P, ip, dp, ip, i8p]; L.hv_mesh_periodic_images.restype = I
         L.hv_mesh_device_views.argtypes = [P, ctypes.POINTER(DeviceViews)]; L.hv_mesh_device_views.restype = I
@@ -244,17 +249,34 @@ class Mesh:
     """A mesh built on the device (hv_mesh).  Results are copied out on demand."""
 
     def __init__(self, ctx: Context, pts: np.ndarray, lo, hi, params: Params, device_ptr: int | None = None,
-                 planes=None, periodic=None):
+                 planes=None, periodic=None, shard=None):
         """Box domain [lo, hi] (``periodic``: d flags of periodic axes), or
         (lo = hi = None) the convex domain of ``planes = (base, normal, bc)``:
         (P, d) base points, (P, d) outer normals and P boundary-condition codes
-        (or None)."""
+        (or None).  ``shard = (rank, nranks)``: one shard of the box mesh
+        split over ranks (hv_mesh_build_shard; merge with hvgpu.shard)."""
         L = load()
         self.ctx = ctx
         pts = np.ascontiguousarray(pts, dtype=np.float64)
         self.n, self.d = pts.shape if device_ptr is None else (int(pts[0]), int(pts[1]))
         h = ctypes.c_void_p()
         self.periodic = None
+        if shard is not None:
+            self.planes = None
+            self.lo = np.ascontiguousarray(lo, dtype=np.float64)
+            self.hi = np.ascontiguousarray(hi, dtype=np.float64)
+            rank, nranks = int(shard[0]), int(shard[1])
+            if device_ptr is None:
+                rc = L.hv_mesh_build_shard(ctx.handle, self.d, self.n, pts.ctypes.data_as(ctypes.c_void_p),
+                                           dptr(self.lo), dptr(self.hi), rank, nranks, ctypes.byref(params),
+                                           ctypes.byref(h))
+            else:
+                rc = L.hv_mesh_build_shard_device(ctx.handle, self.d, self.n, ctypes.c_void_p(device_ptr),
+                                                  dptr(self.lo), dptr(self.hi), rank, nranks, ctypes.byref(params),
+                                                  ctypes.byref(h))
+            ctx.check(rc, "hv_mesh_build_shard")
+            self._h = h
+            return
         if periodic is not None and any(periodic):
             flags = np.ascontiguousarray([1 if f else 0 for f in periodic], dtype=np.int32)
             if flags.shape[0] != self.d:

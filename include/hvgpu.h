@@ -181,6 +181,23 @@ int hv_mesh_build_periodic(hv_ctx* ctx, int d, int64_t n, const double* pts, con
                            const int* periodic, const hv_params* params, hv_mesh** out);
 int hv_mesh_build_periodic_device(hv_ctx* ctx, int d, int64_t n, const double* d_pts, const double* lo,
                                   const double* hi, const int* periodic, const hv_params* params, hv_mesh** out);
+/* One shard of the box mesh split over nranks GPUs (one rank each), the
+ * GPU form of the reference's cell split between threads
+ * (_voronoi(::MultiThread), src/sysvoronoi.jl:50-76).  Every rank passes all
+ * points; the generators are ordered along the library's Morton curve and
+ * rank r takes the r-th of nranks contiguous ranges of that order (sizes
+ * differ by at most one).  The shard searches the vertices of its own cells
+ * only and keeps those whose first generator in that order is its own, so
+ * every vertex of the mesh belongs to exactly one shard.  hv_mesh_counts /
+ * hv_mesh_vertices / hv_mesh_stats report the kept vertices (1-based
+ * original ids, sorted signatures, lexicographic order); all-gathering them
+ * and sorting the union gives hv_mesh_build's vertex records, from which the
+ * neighbour lists follow.  The integrators refuse a shard (HV_E_INVALID_ARG):
+ * they run on the merged mesh.  Fast method only. */
+int hv_mesh_build_shard(hv_ctx* ctx, int d, int64_t n, const double* pts, const double* lo, const double* hi,
+                        int rank, int nranks, const hv_params* params, hv_mesh** out);
+int hv_mesh_build_shard_device(hv_ctx* ctx, int d, int64_t n, const double* d_pts, const double* lo,
+                               const double* hi, int rank, int nranks, const hv_params* params, hv_mesh** out);
 /* Lattice shift s (nnbr x d, entries -1, 0, 1) of every neighbour entry: the
  * neighbour of cell i is the image x_j + s * (hi - lo).  Zeros for
  * non-periodic meshes. */
