@@ -74,6 +74,8 @@ struct hv_mesh {
     // shard of a mesh split over ranks: generators own0 .. own1-1 of the
     // internal (Morton) order (-1: the whole mesh)
     int own0 = -1, own1 = -1;
+    // incremental refinement: generators own_from .. n-1 are new (-1: none)
+    int own_from = -1;
 };
 
 namespace {
@@ -287,6 +289,8 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     const bool shard = mesh->own0 >= 0;
     M.own0 = shard ? mesh->own0 : 0;
     M.own1 = shard ? mesh->own1 : n;
+    M.own_from = mesh->own_from;
+    const bool restricted = shard || mesh->own_from >= 0;
     double xs = 0;
     for (int k = 0; k < d; ++k) {
         M.lo[k] = mesh->lo[k]; M.hi[k] = mesh->hi[k];
@@ -328,7 +332,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     M.K = fast ? K : 0;
     // a shard seeds every one of its generators: its cells need not be connected
     // to each other through shared vertices
-    const int stride = shard ? 1 : (mesh->prm.seed_stride > 0 ? mesh->prm.seed_stride : default_seed_stride(n));
+    const int stride = restricted ? 1 : (mesh->prm.seed_stride > 0 ? mesh->prm.seed_stride : default_seed_stride(n));
     bool knn_side = false;
     if (fast) {
         int* knn = prep.get<int>((size_t)n * std::max(K, 1));
@@ -352,6 +356,8 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     // ---- search with capacity retry
     double factor = mesh->prm.capacity_factor > 0 ? mesh->prm.capacity_factor : 1.3;
     unsigned long long est = (unsigned long long)(vertices_per_point(d) * n) + (1ull << d) + 1024;
+    if (mesh->own_from >= 0)  // refinement: only the vertices of the new cells (d+1 cells share a vertex)
+        est = std::min(est, (unsigned long long)(vertices_per_point(d) * (d + 1) * (n - mesh->own_from)) + 1024);
     const int nseeds = (M.own1 - M.own0 + stride - 1) / stride;
     std::unique_ptr<Scratch> srch;
     unsigned V = 0;
@@ -422,7 +428,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         kt.run(F_DESCENT, 1, [&] { launch_descent(M, stride, nseeds, dseed, dfail, ndfail, ctx->nsm, st); });
         CK(cudaGetLastError());
         read_stat(ctx, dstat);
-        if (fast && (ctx->h_stat[0] == 0 || shard) && !(ctx->h_stat[1] & (ST_VCAP | ST_HASH))) {
+        if (fast && (ctx->h_stat[0] == 0 || restricted) && !(ctx->h_stat[1] & (ST_VCAP | ST_HASH))) {
             // no FP32 seed was decided (or a shard, whose every cell needs its
             // seed): the exact descent on the undecided ones
             kt.run(F_DESCENT, 1, [&] { launch_descent_exact(M, nseeds, dseed, dfail, ndfail, ctx->nsm, st); });
@@ -812,6 +818,105 @@ int shard_entry(hv_ctx* ctx, int d, int64_t n, const double* src, bool on_device
     try {
         CK(cudaSetDevice(ctx->device));
         build_impl(ctx, m, src, on_device, src);
+    } catch (const HvError& e) {
+        hv_mesh_free(m);
+        return fail(ctx, e);
+    } catch (const std::bad_alloc&) {
+        hv_mesh_free(m);
+        ctx->err = "host allocation failed";
+        return HV_E_OOM;
+    }
+    *out = m;
+    return HV_OK;
+}
+
+// Incremental refinement (refine!, src/meshrefine.jl:183, src/geometry.jl:404-438):
+// the mesh of the old generators plus k new ones.  The search runs only over
+// the new generators' cells (every vertex holding a new generator); an old
+// vertex survives unless a new generator lies strictly inside its
+// circumsphere; both sorted lists merge into the canonical order.  A new
+// point within rounding of an old sphere makes the whole enlarged set be
+// searched again instead.
+int refine_entry(hv_mesh* old, int64_t k, const double* src, bool on_device, hv_mesh** out) {
+    using namespace hv;
+    if (!old || !out || k < 0 || (k > 0 && !src)) return HV_E_INVALID_ARG;
+    hv_ctx* ctx = old->ctx;
+    if (old->ext || old->pmask || old->own0 >= 0) {
+        ctx->err = "refinement takes a box or plane-domain mesh, not a periodic one or a shard";
+        return HV_E_INVALID_ARG;
+    }
+    if (old->prm.method != HV_METHOD_FAST) { ctx->err = "refinement uses the fast method"; return HV_E_INVALID_ARG; }
+    const int d = old->d, n_old = old->n;
+    if ((int64_t)n_old + k > (1ll << 30)) { ctx->err = "point count out of range"; return HV_E_INVALID_ARG; }
+    const int n = n_old + (int)k;
+    cudaStream_t st = ctx->stream;
+    std::unique_ptr<hv_mesh> mp(new hv_mesh());
+    hv_mesh* m = mp.get();
+    m->ctx = ctx; m->d = d; m->n = n;
+    for (int q = 0; q < d; ++q) { m->lo[q] = old->lo[q]; m->hi[q] = old->hi[q]; }
+    m->np = old->np;
+    std::memcpy(m->planes, old->planes, sizeof(DevPlane) * old->np);
+    m->prm = old->prm;
+    m->own_from = n_old;
+    const auto t0 = std::chrono::steady_clock::now();
+    try {
+        CK(cudaSetDevice(ctx->device));
+        double* all = dalloc<double>(st, (size_t)n * d);
+        struct Free { cudaStream_t s; double* p; ~Free() { dfree(s, p); } } fr{st, all};
+        if (n_old > 0) CK(cudaMemcpyAsync(all, old->d_in, sizeof(double) * n_old * d, cudaMemcpyDeviceToDevice, st));
+        if (k > 0)
+            CK(cudaMemcpyAsync(all + (size_t)n_old * d, src, sizeof(double) * k * d,
+                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+        mp.release();
+        build_impl(ctx, m, all, true, nullptr);  // the new generators' cells
+        // old vertices: kept unless a new point invades their sphere
+        const unsigned Vo = old->V, Vn = m->V;
+        Scratch sc(st);
+        long long* keep = sc.get<long long>((size_t)Vo + 1);
+        long long* rank = sc.get<long long>((size_t)Vo + 1);
+        unsigned* unsure = sc.get<unsigned>(1);
+        CK(cudaMemsetAsync(keep, 0, sizeof(long long) * (Vo + 1), st));
+        CK(cudaMemsetAsync(unsure, 0, sizeof(unsigned), st));
+        launch_refine_keep(d, n_old, (int)k, Vo, old->osig, old->oc, old->d_in, m->d_in + (size_t)n_old * d, keep,
+                           unsure, st);
+        const size_t tb = scan_temp((int)Vo + 1);
+        void* tmp = sc.get<char>(tb);
+        exclusive_scan_i64(tmp, tb, keep, rank, (int)Vo + 1, st);
+        long long kept = 0;
+        unsigned hu = 0;
+        CK(cudaMemcpyAsync(&kept, rank + Vo, sizeof(long long), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&hu, unsure, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (hu) {
+            // a new point within rounding of an old sphere: search the whole set
+            sc.release_all();
+            hv_mesh* fm = new hv_mesh();
+            fm->ctx = ctx; fm->d = d; fm->n = n;
+            for (int q = 0; q < d; ++q) { fm->lo[q] = old->lo[q]; fm->hi[q] = old->hi[q]; }
+            fm->np = old->np;
+            std::memcpy(fm->planes, old->planes, sizeof(DevPlane) * old->np);
+            fm->prm = old->prm;
+            fm->st = m->st;
+            hv_mesh_free(m);
+            m = fm;
+            build_impl(ctx, m, all, true, nullptr);
+            m->st.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            *out = m;
+            return HV_OK;
+        }
+        const unsigned V = (unsigned)kept + Vn;
+        int* osig = dalloc<int>(st, (size_t)std::max(V, 1u) * (d + 1));
+        double* oc = dalloc<double>(st, (size_t)std::max(V, 1u) * d);
+        launch_refine_merge(d, n_old, (int)k, Vo, old->osig, old->oc, keep, rank, Vn, m->osig, m->oc, osig, oc, st);
+        CK(cudaGetLastError());
+        dfree(st, m->osig);
+        dfree(st, m->oc);
+        m->osig = osig;
+        m->oc = oc;
+        m->V = V;
+        m->st.vertices = V;
+        CK(cudaStreamSynchronize(st));
+        m->st.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     } catch (const HvError& e) {
         hv_mesh_free(m);
         return fail(ctx, e);
@@ -1434,6 +1539,14 @@ int hv_integrate_heuristic_mc(hv_mesh* m, int ndir, uint64_t seed, double* vol, 
 
 int hv_integrate_heuristic_mc_device(hv_mesh* m, int ndir, uint64_t seed, double* d_vol, double* d_area) {
     return mc_impl(m, ndir, seed, d_vol, d_area, true);
+}
+
+int hv_mesh_refine(hv_mesh* old, int64_t k, const double* pts, hv_mesh** out) {
+    return refine_entry(old, k, pts, false, out);
+}
+
+int hv_mesh_refine_device(hv_mesh* old, int64_t k, const double* d_pts, hv_mesh** out) {
+    return refine_entry(old, k, d_pts, true, out);
 }
 
 int hv_mesh_build_shard(hv_ctx* ctx, int d, int64_t n, const double* pts, const double* lo, const double* hi,

@@ -72,6 +72,14 @@ void launch_fallback(const DevMesh& M, const unsigned long long* fq, const unsig
 
 // hv_post.cu
 // canonical keys: original 0-based items of each vertex, sorted, SoA by position
+// incremental refinement: keep[v] = 1 unless a new point lies strictly inside
+// old vertex v's circumsphere (uncertain: within the rounding margin), then
+// the merge of the kept old rows (plane items renumbered) with the new rows
+void launch_refine_keep(int d, int n_old, int k, unsigned V, const int* osig, const double* oc, const double* pts,
+                        const double* newp, long long* keep, unsigned* uncertain, cudaStream_t st);
+void launch_refine_merge(int d, int n_old, int k, unsigned V_old, const int* osig, const double* oc,
+                         const long long* keep, const long long* rank, unsigned V_new, const int* nsig,
+                         const double* nc, int* out_sig, double* out_c, cudaStream_t st);
 void launch_canon_keys(const DevMesh& M, unsigned V, unsigned* keys, cudaStream_t st);
 void launch_gather_keys(const unsigned* keys_pos, const int* order, unsigned V, unsigned* out, cudaStream_t st);
 void launch_pack_keys(const unsigned* keys, unsigned V, int d, int bits, unsigned long long* out, cudaStream_t st);

@@ -86,6 +86,9 @@ struct DevMesh {
     // of a mesh split over ranks walks only edges that keep one of them and
     // keeps the vertices whose smallest generator is one of them (0, n: all)
     int own0, own1;
+    // refinement: only the generators with original id >= own_from are new;
+    // the search walks only edges that keep one of them (-1: all generators)
+    int own_from;
     int leaf, nleaves, P;
     int K, dp;
     unsigned vcap;

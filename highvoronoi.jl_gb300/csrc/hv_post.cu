@@ -190,6 +190,120 @@ static unsigned grid_for(unsigned long long n, int bs) {
     return (unsigned)(b ? b : 1);
 }
 
+// ---------------------------------------------------------------------------
+// incremental refinement (hv_mesh_refine): old vertices whose circumsphere a
+// new generator invades disappear; the rest merge with the new vertices
+// ---------------------------------------------------------------------------
+constexpr int RK_TILE = 256;
+template <int D>
+__global__ void __launch_bounds__(RK_TILE) k_refine_keep(int n_old, int k, unsigned V, const int* __restrict__ osig,
+                                                         const double* __restrict__ oc, const double* __restrict__ pts,
+                                                         const double* __restrict__ newp, long long* keep,
+                                                         unsigned* uncertain) {
+    __shared__ double sq[RK_TILE][D];
+    const unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
+    double c[D], r2 = 0.0;
+    bool live = v < V, gone = false, unsure = false;
+    if (live) {
+        const int s0 = osig[(size_t)v * (D + 1)];  // the smallest item: a generator
+#pragma unroll
+        for (int q = 0; q < D; ++q) {
+            c[q] = oc[(size_t)v * D + q];
+            const double e = pts[(size_t)s0 * D + q] - c[q];
+            r2 = fma(e, e, r2);
+        }
+    }
+    for (int base = 0; base < k; base += RK_TILE) {
+        __syncthreads();
+        for (int x = threadIdx.x; x < RK_TILE && base + x < k; x += blockDim.x)
+#pragma unroll
+            for (int q = 0; q < D; ++q) sq[x][q] = newp[(size_t)(base + x) * D + q];
+        __syncthreads();
+        const int m = min(RK_TILE, k - base);
+        if (live && !gone)
+            for (int x = 0; x < m; ++x) {
+                double dd = 0.0;
+#pragma unroll
+                for (int q = 0; q < D; ++q) { const double e = sq[x][q] - c[q]; dd = fma(e, e, dd); }
+                // a margin far above the rounding of the stored centre and radius
+                if (dd < r2 * (1.0 - 1e-9)) { gone = true; break; }
+                if (dd <= r2 * (1.0 + 1e-9)) unsure = true;
+            }
+    }
+    if (live) {
+        keep[v] = gone ? 0 : 1;
+        if (unsure && !gone) atomicAdd(uncertain, 1u);
+    }
+}
+
+// Lexicographic comparison of a (d+1)-item row of the old mesh, with its
+// boundary items n_old+p renumbered to n_old+k+p, against a row of the new one.
+template <int D>
+__device__ __forceinline__ int cmp_rows(const int* a, int n_old, int k, const int* b) {
+#pragma unroll
+    for (int q = 0; q <= D; ++q) {
+        const int x = a[q] >= n_old ? a[q] + k : a[q];
+        if (x != b[q]) return x < b[q] ? -1 : 1;
+    }
+    return 0;
+}
+
+template <int D>
+__global__ void k_refine_merge_old(int n_old, int k, unsigned V_old, const int* __restrict__ osig,
+                                   const double* __restrict__ oc, const long long* __restrict__ keep,
+                                   const long long* __restrict__ rank, unsigned V_new, const int* __restrict__ nsig,
+                                   int* out_sig, double* out_c) {
+    for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < V_old; v += gridDim.x * blockDim.x) {
+        if (!keep[v]) continue;
+        const int* a = osig + (size_t)v * (D + 1);
+        unsigned lo = 0, hi = V_new;  // new rows below this one
+        while (lo < hi) {
+            const unsigned md = (lo + hi) >> 1;
+            if (cmp_rows<D>(a, n_old, k, nsig + (size_t)md * (D + 1)) > 0) lo = md + 1; else hi = md;
+        }
+        const size_t pos = (size_t)rank[v] + lo;
+#pragma unroll
+        for (int q = 0; q <= D; ++q) out_sig[pos * (D + 1) + q] = a[q] >= n_old ? a[q] + k : a[q];
+#pragma unroll
+        for (int q = 0; q < D; ++q) out_c[pos * D + q] = oc[(size_t)v * D + q];
+    }
+}
+
+template <int D>
+__global__ void k_refine_merge_new(int n_old, int k, unsigned V_old, const int* __restrict__ osig,
+                                   const long long* __restrict__ rank, unsigned V_new, const int* __restrict__ nsig,
+                                   const double* __restrict__ nc, int* out_sig, double* out_c) {
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < V_new; w += gridDim.x * blockDim.x) {
+        const int* b = nsig + (size_t)w * (D + 1);
+        unsigned lo = 0, hi = V_old;  // old rows below this one (kept or not)
+        while (lo < hi) {
+            const unsigned md = (lo + hi) >> 1;
+            if (cmp_rows<D>(osig + (size_t)md * (D + 1), n_old, k, b) < 0) lo = md + 1; else hi = md;
+        }
+        const size_t pos = (size_t)rank[lo] + w;  // rank: exclusive count of kept rows (V_old + 1 entries)
+#pragma unroll
+        for (int q = 0; q <= D; ++q) out_sig[pos * (D + 1) + q] = b[q];
+#pragma unroll
+        for (int q = 0; q < D; ++q) out_c[pos * D + q] = nc[(size_t)w * D + q];
+    }
+}
+
+void launch_refine_keep(int d, int n_old, int k, unsigned V, const int* osig, const double* oc, const double* pts,
+                        const double* newp, long long* keep, unsigned* uncertain, cudaStream_t st) {
+    if (!V) return;
+    HV_DISPATCH(d, (k_refine_keep<DD><<<(V + RK_TILE - 1) / RK_TILE, RK_TILE, 0, st>>>(n_old, k, V, osig, oc, pts,
+                                                                                       newp, keep, uncertain)));
+}
+
+void launch_refine_merge(int d, int n_old, int k, unsigned V_old, const int* osig, const double* oc,
+                         const long long* keep, const long long* rank, unsigned V_new, const int* nsig,
+                         const double* nc, int* out_sig, double* out_c, cudaStream_t st) {
+    HV_DISPATCH(d, (k_refine_merge_old<DD><<<grid_for(std::max(V_old, 1u), 256), 256, 0, st>>>(
+                        n_old, k, V_old, osig, oc, keep, rank, V_new, nsig, out_sig, out_c)));
+    HV_DISPATCH(d, (k_refine_merge_new<DD><<<grid_for(std::max(V_new, 1u), 256), 256, 0, st>>>(
+                        n_old, k, V_old, osig, rank, V_new, nsig, nc, out_sig, out_c)));
+}
+
 void launch_canon_keys(const DevMesh& M, unsigned V, unsigned* keys, cudaStream_t st) {
     if (!V) return;
     HV_DISPATCH(M.d, (k_canon_keys<DD><<<grid_for(V, 256), 256, 0, st>>>(M, V, keys)));

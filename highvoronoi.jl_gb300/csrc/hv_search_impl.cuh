@@ -687,6 +687,12 @@ __device__ void exact_walk(const DevMesh& M, unsigned v, int m) {
 template <int D>
 __device__ __forceinline__ bool walkable(const DevMesh& M, const int (&sig)[D + 1], int vnew, int m) {
     if (sig[m] == vnew) return false;
+    if (M.own_from >= 0) {
+        bool own = false;
+#pragma unroll
+        for (int s = 0; s <= D; ++s) own |= (s != m && sig[s] < M.n && __ldg(M.perm + sig[s]) >= M.own_from);
+        return own;
+    }
     if (M.own0 > 0 || M.own1 < M.n) {
         bool own = false;
 #pragma unroll
@@ -774,6 +780,7 @@ __global__ void __launch_bounds__(128) k_descent(DevMesh M, int stride, int nsee
     if (!list && idx >= nseeds) return;
     const int i = list ? list[idx] : M.own0 + idx * stride;
     if (i >= M.own1) return;
+    if (!list && M.own_from >= 0 && __ldg(M.perm + i) < M.own_from) return;  // refinement: new cells only
     count_add(M.cnt + C_DESCENT);
     for (int attempt = 0; attempt < 16; ++attempt) {
         Query<D> q;
@@ -2306,6 +2313,7 @@ __global__ void __launch_bounds__(FB_WPB * 32) k_descent_warp(DevMesh M, int str
     for (int w = blockIdx.x * FB_WPB + wib; w < nseeds; w += gridDim.x * FB_WPB) {
         const int i = M.own0 + w * stride;
         if (i >= M.own1) continue;
+        if (M.own_from >= 0 && __ldg(M.perm + i) < M.own_from) continue;  // refinement: new cells only
         if (lane == 0) count_add(M.cnt + C_DESCENT);
         int T[D + 1];
 #pragma unroll

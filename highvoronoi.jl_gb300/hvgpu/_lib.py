@@ -134,6 +134,8 @@ def load(path: str | None = None):
         L.hv_mesh_build_periodic_device.argtypes = [P, I, I64, P, dp, dp, i32p, ctypes.POINTER(Params),
                                                     ctypes.POINTER(P)]
         L.hv_mesh_build_periodic_device.restype = I
+        L.hv_mesh_refine.argtypes = [P, I64, P, ctypes.POINTER(P)]; L.hv_mesh_refine.restype = I
+        L.hv_mesh_refine_device.argtypes = [P, I64, P, ctypes.POINTER(P)]; L.hv_mesh_refine_device.restype = I
         L.hv_mesh_build_shard.argtypes = [P, I, I64, P, dp, dp, I, I, ctypes.POINTER(Params), ctypes.POINTER(P)]
         L.hv_mesh_build_shard.restype = I
         L.hv_mesh_build_shard_device.argtypes = [P, I, I64, P, dp, dp, I, I, ctypes.POINTER(Params),
@@ -327,6 +329,20 @@ class Mesh:
                                         dptr(self.hi), ctypes.byref(params), ctypes.byref(h))
         ctx.check(rc, "hv_mesh_build")
         self._h = h
+
+    def refined(self, xs) -> "Mesh":
+        """hv_mesh_refine: a new mesh of this mesh's generators plus the rows of
+        ``xs`` (numbered after them), searching only the new generators' cells.
+        This mesh stays valid."""
+        xs = np.ascontiguousarray(np.asarray(xs, dtype=np.float64).reshape(-1, self.d))
+        h = ctypes.c_void_p()
+        rc = load().hv_mesh_refine(self._h, xs.shape[0], xs.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h))
+        self.ctx.check(rc, "hv_mesh_refine")
+        m = Mesh.__new__(Mesh)
+        m.ctx, m.n, m.d, m.periodic, m.planes = self.ctx, self.n + xs.shape[0], self.d, None, self.planes
+        m.lo, m.hi = self.lo, self.hi
+        m._h = h
+        return m
 
     def counts(self, neighbors: bool = False):
         nv = ctypes.c_int64()

@@ -232,13 +232,19 @@ class VoronoiGeometry:
     def refine(self, xs, update: bool = True) -> "VoronoiGeometry":
         """refine!(VG, xs, update) (src/geometry.jl:404-433): appends the
         generators ``xs`` (numbered after the existing ones) and recomputes the
-        mesh, and with ``update`` the integrals.  The GPU search rebuilds the
-        whole tessellation of the enlarged set; the result is the one the
-        reference's cell-by-cell update reaches, since the tessellation is
-        unique."""
+        mesh, and with ``update`` the integrals.  On box and plane domains the
+        GPU searches only the new generators' cells and keeps the old vertices
+        whose circumspheres stay empty (hv_mesh_refine), the reference's
+        re-walk of the affected cells (src/meshrefine.jl:183); periodic
+        cuboids search the enlarged set again.  The tessellation is unique, so
+        both give the mesh of all points."""
         xs = np.asarray(xs, dtype=np.float64).reshape(-1, self.dimension)
         pts = np.ascontiguousarray(np.vstack([self.nodes, xs]))
-        mesh = self._build(pts)
+        b = self.boundary
+        if not (b.is_box and b.periodic) and self.method.code == _lib.HV_METHOD_FAST:
+            mesh = self.mesh.refined(xs)
+        else:
+            mesh = self._build(pts)
         self.mesh.free()
         self.mesh, self.nodes = mesh, pts
         if update:

@@ -181,6 +181,18 @@ int hv_mesh_build_periodic(hv_ctx* ctx, int d, int64_t n, const double* pts, con
                            const int* periodic, const hv_params* params, hv_mesh** out);
 int hv_mesh_build_periodic_device(hv_ctx* ctx, int d, int64_t n, const double* d_pts, const double* lo,
                                   const double* hi, const int* periodic, const hv_params* params, hv_mesh** out);
+/* Incremental refinement (refine!, src/meshrefine.jl:183,
+ * src/geometry.jl:404-438): the mesh of old's generators plus k new points
+ * (host array d x k; the _device form takes them in device memory), numbered
+ * n+1 .. n+k after the old ones, boundary plane p becoming generator n+k+p.
+ * Only the new generators' cells are searched; an old vertex stays unless a
+ * new point lies inside its circumsphere; the vertex records come out in the
+ * same canonical order as hv_mesh_build of all points gives (if a new point
+ * lies on an old circumsphere within rounding, the whole set is searched).
+ * old stays valid; box and plane domains, fast method; not periodic meshes
+ * or shards (HV_E_INVALID_ARG). */
+int hv_mesh_refine(hv_mesh* old, int64_t k, const double* pts, hv_mesh** out);
+int hv_mesh_refine_device(hv_mesh* old, int64_t k, const double* d_pts, hv_mesh** out);
 /* One shard of the box mesh split over nranks GPUs (one rank each), the
  * GPU form of the reference's cell split between threads
  * (_voronoi(::MultiThread), src/sysvoronoi.jl:50-76).  Every rank passes all

@@ -223,4 +223,56 @@ def test_refine_matches_a_fresh_build(gpu_lib):
         f = hv.VoronoiGeometry(pts, b, integrator=hv.VI_POLYGON)
         for x in (g, h):
             np.testing.assert_array_equal(x.mesh.vertices()[0], f.mesh.vertices()[0])
-            np.testing.assert_array_equal(hv.VoronoiData(x).volume, hv.VoronoiData(f).volume)
+            # a kept vertex's centre comes from the old mesh's solve: equal to rounding
+            np.testing.assert_allclose(x.mesh.vertices()[1], f.mesh.vertices()[1], rtol=0, atol=1e-13)
+            np.testing.assert_allclose(hv.VoronoiData(x).volume, hv.VoronoiData(f).volume, rtol=1e-12)
+
+
+@pytest.mark.parametrize("d,n,k,steps", [(4, 20000, 200, 3), (2, 3000, 1, 5), (5, 3000, 60, 2)])
+def test_incremental_refine_searches_only_the_new_cells(gpu_lib, d, n, k, steps):
+    """hv_mesh_refine: a few new generators at a time; after every step the
+    vertex records equal one build of all points, and the refinement walked
+    far fewer rays than that build."""
+    hv = gpu_lib
+    X = D.uniform_points(d, n + k * steps, 123 + d)
+    ctx = hv.default_context()
+    lo, hi = np.zeros(d), np.ones(d)
+    m = hv.Mesh(ctx, X[:n], lo, hi, hv.make_params(hv.HV_METHOD_FAST))
+    for st in range(steps):
+        m = m.refined(X[n + st * k:n + (st + 1) * k])
+        f = hv.Mesh(ctx, X[:n + (st + 1) * k], lo, hi, hv.make_params(hv.HV_METHOD_FAST))
+        s, r = m.vertices()
+        fs, fr = f.vertices()
+        np.testing.assert_array_equal(s, fs)
+        np.testing.assert_allclose(r, fr, rtol=0, atol=1e-13)
+        o, nb = m.neighbors()
+        fo, fnb = f.neighbors()
+        np.testing.assert_array_equal(o, fo)
+        np.testing.assert_array_equal(nb, fnb)
+        assert m.stats()["rays"] < 0.5 * f.stats()["rays"]
+    v, _ = m.polygon()
+    assert abs(v.sum() - 1.0) < 1e-11
+
+
+def test_refine_with_a_point_on_an_old_circumsphere(gpu_lib):
+    """A new point on an old vertex's circumsphere (within rounding) cannot be
+    placed by the kept-vertex test: the whole set is searched, and the result
+    is that of one build."""
+    hv = gpu_lib
+    X = D.uniform_points(2, 400, 5)
+    ctx = hv.default_context()
+    m = hv.Mesh(ctx, X, np.zeros(2), np.ones(2), hv.make_params(hv.HV_METHOD_FAST))
+    s, r = m.vertices()
+    v = int(np.argmin(np.sum((r - 0.5) ** 2, axis=1)))       # an interior vertex
+    R = np.linalg.norm(X[s[v, 0] - 1] - r[v])
+    q = r[v] + R * np.array([0.6, 0.8])
+    all_pts = np.vstack([X, q[None, :]])
+    try:
+        f = hv.Mesh(ctx, all_pts, np.zeros(2), np.ones(2), hv.make_params(hv.HV_METHOD_FAST))
+    except hv.HVError as e:  # co-circular within double-double: refused either way
+        with pytest.raises(hv.HVError) as e2:
+            m.refined(q)
+        assert e2.value.code == e.code
+        return
+    g = m.refined(q)
+    np.testing.assert_array_equal(g.vertices()[0], f.vertices()[0])
