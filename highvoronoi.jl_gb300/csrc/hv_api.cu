@@ -215,6 +215,14 @@ int overlap_rays_per_sm() {
     return v;
 }
 
+// HV_GRAPH=1 runs the wavefront's levels as one CUDA graph launch (device-side
+// level loop), HV_GRAPH=0 from the host (one synchronisation per level).
+bool use_graph(long long n) {
+    const char* e = std::getenv("HV_GRAPH");
+    (void)n;
+    return e && std::atoi(e) == 1;
+}
+
 void read_stat(hv_ctx* ctx, const unsigned* dstat) {
     CK(cudaMemcpyAsync(ctx->h_stat, dstat, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -471,7 +479,71 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
                 }
             };
             if (!overflow) prepare(f0, f1, false);  // the seeds' centres are queued already
-            for (int L = 0; !overflow; ++L) {
+            if (!overflow && use_graph(n)) {
+                // every level in one launch of a CUDA graph: a WHILE node whose body is
+                // [ladder of the previous level | expansion] -> advance -> [centres | edge
+                // registry]; the frontier and the level live in device memory
+                unsigned* lvl = srch->get<unsigned>(4);
+                const unsigned hl[4] = {f0, f1, 0, 0};
+                CK(cudaMemcpyAsync(lvl, hl, sizeof(hl), cudaMemcpyHostToDevice, st));
+                CK(cudaMemsetAsync(qc, 0, 4 * sizeof(unsigned), st));
+                DevMesh G = M;
+                G.G.lvl = lvl;
+                G.G.qc = qc;
+                for (int p = 0; p < 2; ++p) { G.G.fq[p] = fqs[p]; G.G.fx[p] = fxs[p]; G.G.fqh[p] = fqhs[p]; }
+                G.fqh = nullptr;
+                const unsigned stop_bits = overflow_bits | ST_BADINPUT | ST_TIMEOUT | ST_NUMERIC | ST_STACK |
+                                           ST_AMB | ST_DESCENT;
+                cudaGraph_t graph = nullptr;
+                cudaGraphExec_t exec = nullptr;
+                struct GraphFree {
+                    cudaGraph_t* g; cudaGraphExec_t* e;
+                    ~GraphFree() { if (*e) cudaGraphExecDestroy(*e); if (*g) cudaGraphDestroy(*g); }
+                } gfree{&graph, &exec};
+                launch_expand_fast(G, 0, 0, nullptr, nullptr, fqcap, nullptr, nullptr, fqcap, ctx->nsm, st);
+                CK(cudaGraphCreate(&graph, 0));
+                cudaGraphConditionalHandle handle;
+                CK(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+                cudaGraphNodeParams cp = {};
+                cp.type = cudaGraphNodeTypeConditional;
+                cp.conditional.handle = handle;
+                cp.conditional.type = cudaGraphCondTypeWhile;
+                cp.conditional.size = 1;
+                cudaGraphNode_t node;
+                CK(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp));
+                cudaGraph_t body = cp.conditional.phGraph_out[0];
+                CK(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+                const unsigned qmax = fqcap;
+                launch_level_begin(G, st);
+                CK(cudaEventRecord(ctx->ovl_ev[0], st));
+                CK(cudaStreamWaitEvent(st2, ctx->ovl_ev[0], 0));
+                CK(cudaMemsetAsync(aq.count, 0, sizeof(unsigned), st2));
+                launch_fallback_warp(G, nullptr, nullptr, fqcap, qmax, nullptr, nullptr, fqcap, aq, ctx->nsm, st2);
+                launch_fallback(G, nullptr, nullptr, qmax, ctx->nsm, st2);
+                CK(cudaEventRecord(ctx->ovl_ev[1], st2));
+                launch_expand_fast(G, 0, vcap, nullptr, nullptr, fqcap, nullptr, nullptr, fqcap, ctx->nsm, st);
+                CK(cudaStreamWaitEvent(st, ctx->ovl_ev[1], 0));
+                launch_level_advance(G, handle, stop_bits, st);
+                if (dedup) {
+                    CK(cudaEventRecord(ctx->ovl_ev[2], st));
+                    CK(cudaStreamWaitEvent(st3, ctx->ovl_ev[2], 0));
+                    launch_register_edges(G, 0, vcap, ctx->nsm, st3);
+                    CK(cudaEventRecord(ev_reg, st3));
+                }
+                launch_centers(G, 0, vcap, ctx->nsm, st);
+                if (dedup) CK(cudaStreamWaitEvent(st, ev_reg, 0));
+                CK(cudaStreamEndCapture(st, &body));
+                CK(cudaGraphInstantiate(&exec, graph, 0));
+                kt.run(F_EXPAND, 1, [&] { CK(cudaGraphLaunch(exec, st)); });
+                unsigned hl2[4];
+                CK(cudaMemcpyAsync(hl2, lvl, sizeof(hl2), cudaMemcpyDeviceToHost, st));
+                read_stat(ctx, dstat);
+                if (ctx->h_stat[1] & overflow_bits) overflow = true;
+                else check_fatal(ctx->h_stat[1]);
+                f0 = f1 = std::min(ctx->h_stat[0], vcap);
+                levels = hl2[2];
+            }
+            for (int L = 0; !overflow && !use_graph(n); ++L) {
                 if (f1 == f0) {
                     if (!pend) break;
                     CK(cudaStreamWaitEvent(st, ctx->ovl_ev[1 + pend_par], 0));

@@ -58,6 +58,8 @@ void launch_centers(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStr
 // residual correction of the ill-conditioned centres after the search (fast method)
 void launch_refine_centers(const DevMesh& M, unsigned V, int nsm, cudaStream_t st);
 void launch_register_edges(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st);
+void launch_level_begin(const DevMesh& M, cudaStream_t st);
+void launch_level_advance(const DevMesh& M, cudaGraphConditionalHandle h, unsigned stop_bits, cudaStream_t st);
 void launch_expand_plain(const DevMesh& M, unsigned f0, unsigned f1, int nsm, cudaStream_t st);
 void launch_expand_fast(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq,
                         unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm,

@@ -80,8 +80,22 @@ struct DevBox {
     double lo[HV_MAXD], hi[HV_MAXD];
 };
 
+// The wavefront as one CUDA graph launch (a conditional WHILE node runs the
+// levels): the frontier [lvl[0], lvl[1]) and the level index lvl[2] live in
+// device memory, and the kernels pick the ray queues of a level by its parity
+// (qc[2p], qc[2p+1]: queued and exact rays of parity p).  lvl == nullptr: the
+// host drives the levels and passes ranges and queues as arguments.
+struct LevelQueues {
+    unsigned* lvl;
+    unsigned long long* fq[2];
+    unsigned long long* fx[2];
+    float* fqh[2];
+    unsigned* qc;
+};
+
 struct DevMesh {
     int d, n;
+    LevelQueues G;
     // generators own0 .. own1-1 (internal order) belong to this build; a shard
     // of a mesh split over ranks walks only edges that keep one of them and
     // keeps the vertices whose smallest generator is one of them (0, n: all)

@@ -52,6 +52,36 @@ void launch_descent_exact_d4(const DevMesh& M, int maxn, unsigned long long seed
 void launch_descent_exact_d5(const DevMesh& M, int maxn, unsigned long long seed, int* failed, unsigned* nfailed, int nsm, cudaStream_t st);
 void launch_descent_exact_d6(const DevMesh& M, int maxn, unsigned long long seed, int* failed, unsigned* nfailed, int nsm, cudaStream_t st);
 
+// Graph-driven levels: the start of a level clears the ray counters of its
+// parity; the advance moves the frontier to the vertices found since, counts
+// the level and keeps the loop running while a frontier or queued rays remain
+// and no stop bit (capacity or a fatal error) is set.
+__global__ void k_level_begin(DevMesh M) {
+    if (threadIdx.x == 0) {
+        const unsigned p = M.G.lvl[2] & 1u;
+        M.G.qc[2 * p] = 0;
+        M.G.qc[2 * p + 1] = 0;
+    }
+}
+
+__global__ void k_level_advance(DevMesh M, cudaGraphConditionalHandle h, unsigned stop_bits) {
+    if (threadIdx.x != 0) return;
+    const unsigned L = M.G.lvl[2], p = L & 1u;
+    const unsigned f1 = M.G.lvl[1];
+    const unsigned e = min(*M.vcount, M.vcap);
+    const bool queued = M.G.qc[2 * p] + M.G.qc[2 * p + 1] > 0;
+    M.G.lvl[0] = f1;
+    M.G.lvl[1] = e;
+    M.G.lvl[2] = L + 1;
+    const bool stop = (*M.status & stop_bits) != 0;
+    cudaGraphSetConditional(h, (!stop && (e > f1 || queued)) ? 1u : 0u);
+}
+
+void launch_level_begin(const DevMesh& M, cudaStream_t st) { k_level_begin<<<1, 32, 0, st>>>(M); }
+void launch_level_advance(const DevMesh& M, cudaGraphConditionalHandle h, unsigned stop_bits, cudaStream_t st) {
+    k_level_advance<<<1, 32, 0, st>>>(M, h, stop_bits);
+}
+
 void launch_register_edges(const DevMesh& M, unsigned v0, unsigned v1, int nsm, cudaStream_t st) {
     switch (M.d) {
         case 2: launch_register_d2(M, v0, v1, nsm, st); break;

@@ -723,6 +723,10 @@ __global__ void __launch_bounds__(128) k_expand_plain(DevMesh M, unsigned f0, un
 template <int D>
 __global__ void __launch_bounds__(128) k_fallback(DevMesh M, const unsigned long long* fq, const unsigned* nfq,
                                                   unsigned fqcap) {
+    if (M.G.lvl) {  // graph-driven levels: the exact queue of the previous level
+        const int p = (M.G.lvl[2] + 1) & 1;
+        fq = M.G.fx[p]; nfq = M.G.qc + 2 * p + 1;
+    }
     const unsigned n = min(*nfq, fqcap);  // entries past the capacity were never written
     for (unsigned r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         const unsigned long long e = fq[r];
@@ -910,6 +914,7 @@ __global__ void __launch_bounds__(128) k_descent(DevMesh M, int stride, int nsee
 // ---------------------------------------------------------------------------
 template <int D>
 __global__ void __launch_bounds__(256) k_register_edges(DevMesh M, unsigned v0, unsigned v1) {
+    if (M.G.lvl) { v0 = M.G.lvl[0]; v1 = M.G.lvl[1]; }
     const unsigned long long total = (unsigned long long)(v1 - v0) * (D + 1);
     for (unsigned long long r = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; r < total;
          r += (unsigned long long)gridDim.x * blockDim.x) {
@@ -1063,6 +1068,7 @@ __global__ void __launch_bounds__(128) k_refine_centers(DevMesh M, unsigned V) {
 template <int D>
 __global__ void __launch_bounds__(128) k_centers(DevMesh M, unsigned v0, unsigned v1) {
     constexpr int DP = (D <= 4) ? 4 : 8;
+    if (M.G.lvl) { v0 = M.G.lvl[0]; v1 = M.G.lvl[1]; }
     for (unsigned v = v0 + blockIdx.x * blockDim.x + threadIdx.x; v < v1; v += gridDim.x * blockDim.x) {
         int s[D + 1];
 #pragma unroll
@@ -1367,6 +1373,15 @@ __global__ void __launch_bounds__(FAST_WPB * 32, D <= 4 ? 8 : 6) k_expand_fast(D
     constexpr int CW = D + 4;
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned FULL = 0xFFFFFFFFu;
+    float* fqh = M.fqh;
+    if (M.G.lvl) {  // graph-driven levels: this level's range and queues
+        f0 = M.G.lvl[0];
+        f1 = M.G.lvl[1];
+        const int p = M.G.lvl[2] & 1;
+        fq = M.G.fq[p]; nfq = M.G.qc + 2 * p;
+        fx = M.G.fx[p]; nfx = M.G.qc + 2 * p + 1;
+        fqh = M.G.fqh[p];
+    }
     const unsigned nf = f1 - f0;
     const float S32 = 5.9604645e-08f;                          // 2^-24
     for (unsigned w = blockIdx.x * FAST_WPB + wib; w < nf; w += gridDim.x * FAST_WPB) {
@@ -1685,7 +1700,7 @@ __global__ void __launch_bounds__(FAST_WPB * 32, D <= 4 ? 8 : 6) k_expand_fast(D
                 const unsigned slot = atomicAdd(nfq, 1u);
                 if (slot < fqcap) {
                     fq[slot] = ((unsigned long long)v << 4) | ((unsigned)secure << 3) | (unsigned)m;
-                    if (M.fqh) M.fqh[slot] = win >= 0 ? bhi : INFINITY;
+                    if (fqh) fqh[slot] = win >= 0 ? bhi : INFINITY;
                 } else {
                     set_status(M, ST_QUEUE);
                 }
@@ -1862,6 +1877,13 @@ __global__ void __launch_bounds__(FB_WPB * 32, 4) k_fallback_warp(DevMesh M, con
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned FULL = 0xFFFFFFFFu;
     const float S32 = 5.9604645e-08f;
+    const float* fqh = M.fqh;
+    if (M.G.lvl) {  // graph-driven levels: the queues of the previous level
+        const int p = (M.G.lvl[2] + 1) & 1;
+        fq = M.G.fq[p]; nfq = M.G.qc + 2 * p;
+        fx = M.G.fx[p]; nfx = M.G.qc + 2 * p + 1;
+        fqh = M.G.fqh[p];
+    }
     const unsigned nq = min(*nfq, fqcap);
     int* stk = sstack[wib];
     int* lq = sleaf[wib];
@@ -1979,7 +2001,7 @@ __global__ void __launch_bounds__(FB_WPB * 32, 4) k_fallback_warp(DevMesh M, con
         // the candidate list -- unless a tree pass follows and the expansion left a
         // finite bound: its best candidate's upper bound is then the starting bound,
         // and the exhaustive tree pass meets every list candidate inside that ball
-        const float H0 = M.fqh ? M.fqh[w] : INFINITY;
+        const float H0 = fqh ? fqh[w] : INFINITY;
         const bool list_pass = M.K > 0 && (complete || !isfinite(H0));
         if (!list_pass) H = fminf(H, H0);
         if (list_pass) {
@@ -2193,6 +2215,10 @@ __global__ void __launch_bounds__(DS_WPB * 32) k_decide_sets(DevMesh M, AmbQueue
     __shared__ int sok[DS_WPB];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned FULL = 0xFFFFFFFFu;
+    if (M.G.lvl) {  // graph-driven levels: the exact queue of the previous level
+        const int p = (M.G.lvl[2] + 1) & 1;
+        fx = M.G.fx[p]; nfx = M.G.qc + 2 * p + 1;
+    }
     const unsigned nq = min(*aq.count, aq.cap);
     if (nq > 2u * gridDim.x * DS_WPB) {  // many sets: one per thread (throughput)
         for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nq; w += gridDim.x * blockDim.x) {
@@ -2550,19 +2576,20 @@ template <int D>
 static void launch_fast_t(const DevMesh& M, unsigned f0, unsigned f1, unsigned long long* fq, unsigned* nfq,
                           unsigned fqcap, unsigned long long* fx, unsigned* nfx, unsigned fxcap, int nsm,
                           cudaStream_t st) {
-    unsigned nf = f1 - f0;
-    if (!nf) return;
-    unsigned blocks = (nf + FAST_WPB - 1) / FAST_WPB;
-    if (blocks > (unsigned)nsm * 32) blocks = (unsigned)nsm * 32;
     const size_t sm = fast_smem_bytes(D, M.K);
     if (sm > 48 * 1024) {
-        // once per instantiation, for the largest list length (thread-safe static init)
+        // once per instantiation, for the largest list length (thread-safe static
+        // init; an empty launch sets it up ahead of a stream capture)
         static const bool set = [] {
             return cudaFuncSetAttribute(k_expand_fast<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)fast_smem_bytes(D, 480)) == cudaSuccess;
         }();
         (void)set;
     }
+    unsigned nf = f1 - f0;
+    if (!nf) return;
+    unsigned blocks = (nf + FAST_WPB - 1) / FAST_WPB;
+    if (blocks > (unsigned)nsm * 32) blocks = (unsigned)nsm * 32;
     cudaMemsetAsync(M.ndq, 0, sizeof(unsigned), st);
     k_expand_fast<D><<<blocks, FAST_WPB * 32, sm, st>>>(M, f0, f1, fq, nfq, fqcap, fx, nfx, fxcap);
     k_insert_decided<D><<<nsm * 8, 256, 0, st>>>(M);

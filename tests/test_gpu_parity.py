@@ -219,3 +219,17 @@ def test_canonical_order_both_sort_paths(gpu_lib):
         assert len(s) > 0
         assert np.array_equal(np.lexsort(s.T[::-1]), np.arange(len(s)))
         assert (np.diff(s, axis=0) != 0).any(axis=1).all()
+
+
+@pytest.mark.parametrize("d,n,seed", [(2, 1000, 0), (3, 3000, 1), (4, 20000, 1), (5, 3000, 3)])
+def test_graph_driven_levels_give_the_same_mesh(gpu_lib, d, n, seed, monkeypatch):
+    """HV_GRAPH=1 runs all wavefront levels in one CUDA graph launch (a
+    conditional WHILE node reads the frontier on the device): the mesh is the
+    host-driven one, bit for bit."""
+    pts = D.uniform_points(d, n, seed)
+    a = _build(gpu_lib, pts, gpu_lib.HV_METHOD_FAST)
+    monkeypatch.setenv("HV_GRAPH", "1")
+    b = _build(gpu_lib, pts, gpu_lib.HV_METHOD_FAST)
+    for x, y in zip(a.vertices() + a.neighbors(), b.vertices() + b.neighbors()):
+        np.testing.assert_array_equal(x, y)
+    assert b.stats()["levels"] >= a.stats()["levels"] - 1
