@@ -1369,6 +1369,7 @@ __global__ void __launch_bounds__(FAST_WPB * 32, D <= 4 ? 8 : 6) k_expand_fast(D
     __shared__ float sRlo1[FAST_WPB][R], sRhi1[FAST_WPB][R], sRlo2[FAST_WPB][R];
     __shared__ int sRj1[FAST_WPB][R];
     __shared__ float sCond[FAST_WPB];
+    __shared__ float sDb[FAST_WPB][D];  // x_b - x_a of the edge that drops the anchor (ray 0)
     extern __shared__ float sCand[];  // FAST_WPB x CW x K candidate records
     constexpr int CW = D + 4;
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1437,7 +1438,7 @@ __global__ void __launch_bounds__(FAST_WPB * 32, D <= 4 ? 8 : 6) k_expand_fast(D
                     load_pt32<D>(M, b, xb);
                     load_pt32lo<D>(M, b, xbl);
 #pragma unroll
-                    for (int k = 0; k < D; ++k) db[k] = (xb[k] - xa[k]) + (xbl[k] - xal[k]);
+                    for (int k = 0; k < D; ++k) { db[k] = (xb[k] - xa[k]) + (xbl[k] - xal[k]); sDb[wib][k] = db[k]; }
                 }
                 float nu = 0.f;
 #pragma unroll
@@ -1501,6 +1502,14 @@ __global__ void __launch_bounds__(FAST_WPB * 32, D <= 4 ? 8 : 6) k_expand_fast(D
             sec_own = sv;
         }
         const int* lst = M.knn + (size_t)own * K;
+        float dow[D];  // x_own - x_a (split coordinates), for the security tests
+        {
+            float xo[DP], xol[DP];
+            load_pt32<D>(M, own, xo);
+            load_pt32lo<D>(M, own, xol);
+#pragma unroll
+            for (int k = 0; k < D; ++k) dow[k] = (xo[k] - xa[k]) + (xol[k] - xal[k]);
+        }
         // ---- the candidates' ray-independent quantities, once per vertex, into this
         // warp's records (structure of arrays; lane c owns entries c, c+32, ...):
         // dl = x_j - x_a (split), A1 = |dl|_1, num = |dl|^2 - 2 dl.rho and its error
@@ -1626,6 +1635,23 @@ __global__ void __launch_bounds__(FAST_WPB * 32, D <= 4 ? 8 : 6) k_expand_fast(D
             if (lane == 0) { sRlo1[wib][m] = lo1; sRhi1[wib][m] = hi1; sRlo2[wib][m] = lo2; sRj1[wib][m] = j1; }
         }
         __syncwarp();
+        // In a cuboid, every face is at least bdist (its rounding bound emax
+        // included) from the centre, so a crossing interval starts at t >=
+        // bdist (1 - 1e-5) - 1e-5 emax: a ray whose best candidate ends well
+        // below that cannot meet a face first, and neither its decision nor its
+        // certification depends on the faces
+        float bdist = -INFINITY, emax = 0.f;
+        if (M.box) {
+            bdist = INFINITY;
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                const float ck = xa[k] + (xal[k] + rho[k]);
+                const float hk = M.hi32[k], lk = M.lo32[k];
+                const float e = 4.f * S32 * (fabsf(hk) + fabsf(lk) + fabsf(xa[k]) + fabsf(rho[k])) + erho + TINY;
+                bdist = fminf(bdist, fminf(hk - ck, ck - lk) - e);
+                emax = fmaxf(emax, e);
+            }
+        }
         // ---- per-ray decision on lane m
         int dwin = -1;  // winner of this lane's ray when decided here
         if (lane < R && ((rmask >> lane) & 1u)) {
@@ -1639,7 +1665,7 @@ __global__ void __launch_bounds__(FAST_WPB * 32, D <= 4 ? 8 : 6) k_expand_fast(D
             // boundary planes in FP32 with the same error model
             float plo1 = INFINITY, phi1 = INFINITY, plo2 = INFINITY;
             int pj1 = -1;
-            planes32<D>(
+            if (!(cj1 >= 0 && fmaf(1.02f, chi1, emax) < 0.98f * bdist)) planes32<D>(
                 M, xa, xal, rho, u, erho, relu, TINY,
                 [&](int it) {
                     bool ex = false;
@@ -1664,29 +1690,14 @@ __global__ void __launch_bounds__(FAST_WPB * 32, D <= 4 ? 8 : 6) k_expand_fast(D
             if (win >= 0 && isfinite(bhi)) {
                 const float t = certified ? 0.5f * (blo + bhi) : bhi;
                 const float et = certified ? 0.5f * (bhi - blo) : 0.f;
-                float db[D];
-#pragma unroll
-                for (int k = 0; k < D; ++k) db[k] = 0.f;
-                if (m == 0) {
-                    int b = -1;
-#pragma unroll
-                    for (int s2 = 1; s2 <= D; ++s2) if (b < 0 && sig[s2] < M.n) b = sig[s2];
-                    float xb[DP], xbl[DP];
-                    load_pt32<D>(M, b, xb);
-                    load_pt32lo<D>(M, b, xbl);
-#pragma unroll
-                    for (int k = 0; k < D; ++k) db[k] = (xb[k] - xa[k]) + (xbl[k] - xal[k]);
-                }
-                float xo[DP], xol[DP];
-                load_pt32<D>(M, own, xo);
-                load_pt32lo<D>(M, own, xol);
                 float c2 = 0.f, r2 = 0.f, cm = 0.f;
 #pragma unroll
                 for (int k = 0; k < D; ++k) {
+                    const float db = m == 0 ? sDb[wib][k] : 0.f;
                     const float cc = fmaf(t, u[k], rho[k]);
-                    const float co = cc - ((xo[k] - xa[k]) + (xol[k] - xal[k]));
+                    const float co = cc - dow[k];
                     c2 = fmaf(co, co, c2);
-                    const float wv = db[k] - cc;
+                    const float wv = db - cc;
                     r2 = fmaf(wv, wv, r2);
                     cm = fmaxf(cm, fabsf(cc));
                 }
