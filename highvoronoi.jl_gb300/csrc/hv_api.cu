@@ -76,6 +76,14 @@ struct hv_mesh {
     int own0 = -1, own1 = -1;
     // incremental refinement: generators own_from .. n-1 are new (-1: none)
     int own_from = -1;
+    // integrand quadrature of VI_POLYGON (hv_quad.cu), built on first use
+    long long* q_foff = nullptr;  // nnbr + 1: incidence range of each facet slot (lower cells)
+    int* q_slot = nullptr;        // nnbr: cell of each slot
+    unsigned* q_v = nullptr;      // facet vertices in id order
+    double* q_w = nullptr;        // their flag weights
+    double* q_a = nullptr;        // nnbr: flag sums
+    double* q_c = nullptr;        // nnbr x d: facet centres
+    double* q_af = nullptr;       // nnbr: facet areas
 };
 
 namespace {
@@ -1537,6 +1545,85 @@ int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out) {
     return HV_OK;
 }
 
+// The quadrature of the integrand path: facet -> vertex lists (the polygon
+// integrator's incidence passes), then the flag weights and facet centres.
+hv::QuadRun quad_run(hv_mesh* m) {
+    hv::QuadRun Q{};
+    Q.d = m->d; Q.n = m->n; Q.planes = m->d_planes; Q.pts = m->d_in; Q.osig = m->osig; Q.oc = m->oc;
+    Q.nbr_off = m->nbr_off; Q.nbr = m->nbr; Q.nslots = m->nnbr; Q.foff = m->q_foff; Q.slot_cell = m->q_slot;
+    Q.qv = m->q_v; Q.qw = m->q_w; Q.qa = m->q_a; Q.qc = m->q_c; Q.af = m->q_af;
+    return Q;
+}
+
+void ensure_quad(hv_mesh* m) {
+    if (m->q_foff) return;
+    ensure_neighbors(m);
+    hv_ctx* ctx = m->ctx;
+    cudaStream_t st = ctx->stream;
+    const long long ns = m->nnbr;
+    Scratch s(st);
+    hv::PolyRun R{};
+    R.d = m->d; R.n = m->n; R.V = m->V; R.planes = m->d_planes;
+    R.pts = m->d_in; R.osig = m->osig; R.oc = m->oc; R.nbr_off = m->nbr_off; R.nbr = m->nbr;
+    R.nslots = ns; R.nsm = ctx->nsm; R.stream = st;
+    R.cnt = s.get<unsigned long long>((size_t)ns + 1);
+    m->q_foff = dalloc<long long>(st, (size_t)ns + 1);
+    m->q_slot = dalloc<int>(st, (size_t)std::max(ns, 1ll));
+    R.foff = m->q_foff;
+    R.slot_cell = m->q_slot;
+    CK(cudaMemsetAsync(R.cnt, 0, sizeof(unsigned long long) * (ns + 1), st));
+    auto run = [&](int pass) {
+        R.pass = pass;
+        if (hv::launch_poly(R) != 0) throw HvError(HV_E_CUDA, "quadrature incidence launch failed");
+        CK(cudaGetLastError());
+    };
+    run(0);
+    size_t tb = hv::scan_temp((int)(ns + 1));
+    void* tmp = s.get<char>(tb);
+    hv::exclusive_scan_i64(tmp, tb, (const long long*)R.cnt, m->q_foff, (int)(ns + 1), st);
+    long long ninc = 0;
+    CK(cudaMemcpyAsync(&ninc, m->q_foff + ns, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    unsigned* fvert = s.get<unsigned>((size_t)std::max(ninc, 1ll));
+    R.fvert = fvert;
+    CK(cudaMemsetAsync(R.cnt, 0, sizeof(unsigned long long) * (ns + 1), st));
+    run(1);
+    m->q_v = dalloc<unsigned>(st, (size_t)std::max(ninc, 1ll));
+    m->q_w = dalloc<double>(st, (size_t)std::max(ninc, 1ll));
+    m->q_a = dalloc<double>(st, (size_t)std::max(ns, 1ll));
+    m->q_c = dalloc<double>(st, (size_t)std::max(ns, 1ll) * m->d);
+    m->q_af = dalloc<double>(st, (size_t)std::max(ns, 1ll));
+    unsigned* dstat = s.get<unsigned>(1);
+    CK(cudaMemsetAsync(dstat, 0, sizeof(unsigned), st));
+    CK(cudaMemsetAsync(m->q_a, 0, sizeof(double) * std::max(ns, 1ll), st));
+    hv::QuadRun Q = quad_run(m);
+    Q.fvert = fvert;
+    Q.status = dstat;
+    hv::launch_poly_quad(Q, ctx->nsm, st);
+    hv::launch_quad_copy(Q, m->d, m->q_c, st);  // centres of the higher cells' slots
+    CK(cudaGetLastError());
+    unsigned hs = 0;
+    CK(cudaMemcpyAsync(&hs, dstat, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (hs) {
+        for (void* p : {(void*)m->q_foff, (void*)m->q_slot, (void*)m->q_v, (void*)m->q_w, (void*)m->q_a,
+                        (void*)m->q_c, (void*)m->q_af}) dfree(st, p);
+        m->q_foff = nullptr; m->q_slot = nullptr; m->q_v = nullptr; m->q_w = nullptr;
+        m->q_a = nullptr; m->q_c = nullptr; m->q_af = nullptr;
+        if (hs & 1u) throw HvError(HV_E_CAPACITY, "a facet has more vertices than the quadrature holds");
+        throw HvError(HV_E_INTERNAL, "a facet is not a simple polytope (degenerate vertex)");
+    }
+}
+
+int quad_check(hv_mesh* m) {
+    if (!m) return HV_E_INVALID_ARG;
+    if (m->ext || m->own0 >= 0) {
+        m->ctx->err = "the integrand quadrature takes box and plane-domain meshes";
+        return HV_E_INVALID_ARG;
+    }
+    return HV_OK;
+}
+
 int mc_impl(hv_mesh* m, int ndir, uint64_t seed, double* vol, double* area, bool dev_out) {
     if (m && m->own0 >= 0) {  // a shard holds only its own vertices
         m->ctx->err = "integrate the merged mesh, not a shard";
@@ -1600,6 +1687,55 @@ int mc_impl(hv_mesh* m, int ndir, uint64_t seed, double* vol, double* area, bool
 extern "C" {
 
 int hv_integrate_polygon(hv_mesh* m, double* vol, double* area) { return polygon_impl(m, vol, area, false); }
+
+int hv_mesh_facet_centers(hv_mesh* m, double* centers) {
+    int rc = quad_check(m);
+    if (rc != HV_OK) return rc;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        ensure_quad(m);
+        if (m->nnbr > 0) {
+            if (!centers) return HV_E_INVALID_ARG;
+            CK(cudaMemcpyAsync(centers, m->q_c, sizeof(double) * m->nnbr * m->d, cudaMemcpyDeviceToHost,
+                               m->ctx->stream));
+        }
+        CK(cudaStreamSynchronize(m->ctx->stream));
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
+int hv_integrate_polygon_functions(hv_mesh* m, int p, const double* fv, const double* fc, const double* fx,
+                                   double* iface, double* bulk) {
+    int rc = quad_check(m);
+    if (rc != HV_OK) return rc;
+    if (p < 1 || (m->V > 0 && !fv) || !fx) return HV_E_INVALID_ARG;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        ensure_quad(m);
+        const long long ns = m->nnbr;
+        if (ns > 0 && (!fc || !iface)) return HV_E_INVALID_ARG;
+        cudaStream_t st = m->ctx->stream;
+        Scratch s(st);
+        double* dfv = s.get<double>((size_t)std::max(m->V, 1u) * p);
+        double* dfc = s.get<double>((size_t)std::max(ns, 1ll) * p);
+        double* dfx = s.get<double>((size_t)m->n * p);
+        double* dif = s.get<double>((size_t)std::max(ns, 1ll) * p);
+        double* dbk = bulk ? s.get<double>((size_t)m->n * p) : nullptr;
+        if (m->V) CK(cudaMemcpyAsync(dfv, fv, sizeof(double) * m->V * p, cudaMemcpyHostToDevice, st));
+        if (ns) CK(cudaMemcpyAsync(dfc, fc, sizeof(double) * ns * p, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dfx, fx, sizeof(double) * m->n * p, cudaMemcpyHostToDevice, st));
+        hv::launch_quad_integrals(quad_run(m), p, dfv, dfc, dfx, dif, dbk, st);
+        CK(cudaGetLastError());
+        if (ns) CK(cudaMemcpyAsync(iface, dif, sizeof(double) * ns * p, cudaMemcpyDeviceToHost, st));
+        if (bulk) CK(cudaMemcpyAsync(bulk, dbk, sizeof(double) * m->n * p, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
 
 int hv_integrate_polygon_device(hv_mesh* m, double* d_vol, double* d_area) {
     return polygon_impl(m, d_vol, d_area, true);
@@ -1766,6 +1902,13 @@ int hv_mesh_free(hv_mesh* m) {
     dfree(st, m->img_code);
     dfree(st, m->pshift);
     dfree(st, m->pperm);
+    dfree(st, m->q_foff);
+    dfree(st, m->q_slot);
+    dfree(st, m->q_v);
+    dfree(st, m->q_w);
+    dfree(st, m->q_a);
+    dfree(st, m->q_c);
+    dfree(st, m->q_af);
     cudaStreamSynchronize(st);
     if (m->ext) hv_mesh_free(m->ext);
     delete m;

@@ -61,6 +61,35 @@ struct PolyRun {
     cudaStream_t stream;
 };
 int launch_poly(const PolyRun& R);
+
+// Integrand quadrature of VI_POLYGON (hv_quad.cu): per facet of a lower cell
+// (slot t with a non-empty incidence range foff[t] .. foff[t+1]) the facet's
+// vertices in id order (qv), their flag weights (qw), the flag sum (qa) and the
+// facet centre (qc, slots x d); af receives the facet areas of every slot.
+struct QuadRun {
+    int d, n;
+    const DevPlane* planes;
+    const double* pts;        // n x d, original order
+    const int* osig;          // V x (d+1), original items, planes n+p
+    const double* oc;         // V x d
+    const long long* nbr_off;
+    const int* nbr;
+    long long nslots;
+    const long long* foff;
+    const unsigned* fvert;
+    const int* slot_cell;
+    unsigned* qv;
+    double* qw;
+    double* qa;
+    double* qc;
+    double* af;
+    unsigned* status;         // 1: facet over QUAD_MAXV vertices, 8: facet not simple
+};
+void launch_poly_quad(const QuadRun& Q, int nsm, cudaStream_t st);
+// per-slot values a (slots x p) of the higher cells copied from the lower cell's slot
+void launch_quad_copy(const QuadRun& Q, int p, double* a, cudaStream_t st);
+void launch_quad_integrals(const QuadRun& Q, int p, const double* fv, const double* fc, const double* fx,
+                           double* iface, double* bulk, cudaStream_t st);
 // Work-area bytes: per block for tier A, per block (one group) for tier B.
 size_t poly_area_bytes(int d, int capV, int widen, bool tier_b);
 int launch_heuristic_mc(const IntegrateInput& in, int ndir, unsigned long long seed, int capN, double cvol,

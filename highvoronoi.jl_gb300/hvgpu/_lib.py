@@ -134,6 +134,9 @@ def load(path: str | None = None):
         L.hv_mesh_build_periodic_device.argtypes = [P, I, I64, P, dp, dp, i32p, ctypes.POINTER(Params),
                                                     ctypes.POINTER(P)]
         L.hv_mesh_build_periodic_device.restype = I
+        L.hv_mesh_facet_centers.argtypes = [P, dp]; L.hv_mesh_facet_centers.restype = I
+        L.hv_integrate_polygon_functions.argtypes = [P, I, dp, dp, dp, dp, dp]
+        L.hv_integrate_polygon_functions.restype = I
         L.hv_mesh_refine.argtypes = [P, I64, P, ctypes.POINTER(P)]; L.hv_mesh_refine.restype = I
         L.hv_mesh_refine_device.argtypes = [P, I64, P, ctypes.POINTER(P)]; L.hv_mesh_refine_device.restype = I
         L.hv_mesh_build_shard.argtypes = [P, I, I64, P, dp, dp, I, I, ctypes.POINTER(Params), ctypes.POINTER(P)]
@@ -261,6 +264,7 @@ class Mesh:
         self.ctx = ctx
         pts = np.ascontiguousarray(pts, dtype=np.float64)
         self.n, self.d = pts.shape if device_ptr is None else (int(pts[0]), int(pts[1]))
+        self._pts = pts if device_ptr is None else None
         h = ctypes.c_void_p()
         self.periodic = None
         if shard is not None:
@@ -341,6 +345,7 @@ class Mesh:
         m = Mesh.__new__(Mesh)
         m.ctx, m.n, m.d, m.periodic, m.planes = self.ctx, self.n + xs.shape[0], self.d, None, self.planes
         m.lo, m.hi = self.lo, self.hi
+        m._pts = None if getattr(self, "_pts", None) is None else np.vstack([self._pts, xs])
         m._h = h
         return m
 
@@ -371,6 +376,49 @@ class Mesh:
         area = np.zeros(max(E, 1))
         self.ctx.check(load().hv_integrate_polygon(self._h, dptr(vol), dptr(area)), "hv_integrate_polygon")
         return vol, area[:E]
+
+    def facet_centers(self) -> np.ndarray:
+        """(nnbr, d) centres of the facets (mean of their vertices), aligned
+        with neighbors(): the facet nodes of the integrand quadrature."""
+        _, E = self.counts(neighbors=True)
+        c = np.zeros((max(E, 1), self.d))
+        self.ctx.check(load().hv_mesh_facet_centers(self._h, dptr(c)), "hv_mesh_facet_centers")
+        return c[:E]
+
+    def polygon_functions(self, fv, fc, fx, bulk: bool = True):
+        """Interface (nnbr, p) and cell (n, p) integrals of a function given by
+        its values at the vertices (fv, rows of vertices()), the facet centres
+        (fc) and the generators (fx)."""
+        V, E = self.counts(neighbors=True)
+        fv = np.ascontiguousarray(np.asarray(fv, dtype=np.float64).reshape(V, -1))
+        p = fv.shape[1]
+        fc = np.ascontiguousarray(np.asarray(fc, dtype=np.float64).reshape(E, p))
+        fx = np.ascontiguousarray(np.asarray(fx, dtype=np.float64).reshape(self.n, p))
+        iface = np.zeros((max(E, 1), p))
+        blk = np.zeros((self.n, p)) if bulk else None
+        rc = load().hv_integrate_polygon_functions(self._h, p, dptr(fv), dptr(fc), dptr(fx), dptr(iface),
+                                                    dptr(blk) if bulk else None)
+        self.ctx.check(rc, "hv_integrate_polygon_functions")
+        return iface[:E], blk
+
+    def integrate_function(self, f, bulk: bool = True):
+        """Evaluates ``f`` ((m, d) points -> (m,) or (m, p) values) at the
+        quadrature nodes and returns the interface and cell integrals."""
+        _, r = self.vertices()
+        c = self.facet_centers()
+        x = self.points()
+
+        def ev(P):
+            y = np.asarray(f(P), dtype=np.float64)
+            return y.reshape(len(P), -1)
+        return self.polygon_functions(ev(r), ev(c), ev(x), bulk)
+
+    def points(self) -> np.ndarray:
+        """(n, d) generators in their original order (meshes built from host points)."""
+        pts = getattr(self, "_pts", None)
+        if pts is None:
+            raise HVError(HV_E_INVALID_ARG, "the generators of a mesh built from device memory stay on the device")
+        return pts
 
     def heuristic_mc(self, ndir: int, seed: int):
         _, E = self.counts(neighbors=True)

@@ -174,7 +174,7 @@ class VoronoiGeometry:
 
     def __init__(self, xs, b: Boundary | None = None, *, search_settings=None, integrator=VI_GEOMETRY,
                  mc_accurate=(1000, 1, 20), mc_seed: int = 0, context: _lib.Context | None = None,
-                 silence: bool = True):
+                 silence: bool = True, integrand=None, bulk: bool = True):
         pts = np.ascontiguousarray(np.asarray(xs, dtype=np.float64))
         if pts.ndim != 2:
             raise ValueError("xs must be an (n, d) array")
@@ -207,6 +207,10 @@ class VoronoiGeometry:
         self.integrator = integrator
         self.mc_accurate = mc_accurate
         self.mc_seed = mc_seed
+        # integrand=f (points (m, d) -> values (m,) or (m, p)): interface and, with
+        # bulk, cell integrals of f by VI_POLYGON's quadrature (src/polyintegrator.jl:80-123)
+        self.integrand = integrand
+        self.bulk = bulk
         if integrator not in (VI_GEOMETRY, VI_POLYGON, VI_FAST_POLYGON, VI_HEURISTIC_MC, VI_MONTECARLO):
             raise ValueError(f"unsupported integrator {integrator!r} on the GPU path")
         self._integrate()
@@ -224,8 +228,11 @@ class VoronoiGeometry:
     def _integrate(self):
         self._volumes = None
         self._areas = None
+        self._iface_int = self._bulk_int = None
         if self.integrator in (VI_POLYGON, VI_FAST_POLYGON):
             self._volumes, self._areas = self.mesh.polygon()
+            if self.integrand is not None:
+                self._iface_int, self._bulk_int = self.mesh.integrate_function(self.integrand, self.bulk)
         elif self.integrator in (VI_HEURISTIC_MC, VI_MONTECARLO):
             self._volumes, self._areas = self.mesh.heuristic_mc(int(self.mc_accurate[0]), int(self.mc_seed))
 
@@ -337,8 +344,10 @@ class VoronoiData:
     used by ``orientations``), ``offset`` counts the periodic images the search
     added, ``references`` (1-based originals) and ``reference_shifts`` (their
     translation vectors) describe them; otherwise ``offset`` is 0.  There are
-    no infinite edges (``boundary_vertices``).  Integrands (``bulk_integral``,
-    ``interface_integral``) are not computed on the GPU path.
+    no infinite edges (``boundary_vertices``).  With ``integrand=f`` and
+    VI_POLYGON, ``bulk_integral[i]`` (p values) and ``interface_integral[i]``
+    ((deg, p), aligned with ``neighbors[i]``) hold the integrals of f with the
+    reference's polygon quadrature (box and plane domains).
     """
 
     def __init__(self, geo: VoronoiGeometry, onboundary: bool = False):
@@ -371,6 +380,11 @@ class VoronoiData:
             self.reference_shifts = sh * (self.boundary.hi - self.boundary.lo)
         self.bulk_integral = None
         self.interface_integral = None
+        if getattr(geo, "_iface_int", None) is not None:
+            ii = geo._iface_int
+            self.interface_integral = [ii[offs[i]:offs[i + 1]] for i in range(len(offs) - 1)]
+            if geo._bulk_int is not None:
+                self.bulk_integral = [geo._bulk_int[i] for i in range(len(offs) - 1)]
         self.volume = geo._volumes
         self.area = None
         if geo._areas is not None:

@@ -164,6 +164,24 @@ int hv_mesh_vertices(hv_mesh* mesh, int64_t* sig, double* r);
 int hv_mesh_neighbors(hv_mesh* mesh, int64_t* offs, int64_t* nbr);
 /* Exact cell volumes (n) and interface areas aligned with hv_mesh_neighbors. */
 int hv_integrate_polygon(hv_mesh* mesh, double* vol, double* area);
+/* Integrals of a user function with VI_POLYGON's quadrature, the
+ * reference's Polygon_Integrator with an integrand (integrand= of
+ * VoronoiGeometry, src/polyintegrator.jl:80-123,174-330).  The library cannot
+ * call the function, so the caller evaluates it at the quadrature nodes:
+ *   the vertices (rows of hv_mesh_vertices), the facet centres (the mean of
+ *   each facet's vertices, nnbr x d aligned with hv_mesh_neighbors, from
+ *   hv_mesh_facet_centers) and the generators;
+ * and hv_integrate_polygon_functions forms, for p function components, the
+ * interface integrals (nnbr x p, aligned with the neighbour lists, the lower
+ * cell's value for both directions) and, if bulk is not NULL, the cell
+ * integrals (n x p) with the reference's rule: along each facet's flag
+ * simplices the edge average (f(r1)+f(r2))/2 with weight (d-1)/d and the
+ * facet centre with weight 1/d; bulk_i = sum_k V_ik f(x_i)/(d+1) +
+ * I_ik h_ik/(d+1).  A constant function gives the areas and volumes.  Box
+ * and plane-domain meshes; facets of up to 1024 vertices (HV_E_CAPACITY). */
+int hv_mesh_facet_centers(hv_mesh* m, double* centers);
+int hv_integrate_polygon_functions(hv_mesh* m, int p, const double* fv, const double* fc, const double* fx,
+                                   double* iface, double* bulk);
 /* Monte-Carlo volumes and areas, ndir Philox directions per cell. */
 int hv_integrate_heuristic_mc(hv_mesh* mesh, int ndir, uint64_t seed, double* vol, double* area);
 /* Periodic cuboid [lo, hi] (cuboid(d, periodic=...), src/boundary.jl:510-534):

@@ -840,6 +840,10 @@ struct PolyCell {
     int64_t chains = 0;
     int64_t bad = 0;
     std::vector<const double*> centers;
+    // optional: every flag simplex adds |det| / 2 to both end points of its edge
+    // (the reference averages the integrand over the edge's end points,
+    // src/polyintegrator.jl:88-95,176-194)
+    std::vector<double>* wv = nullptr;
 
     double det_cols(double cols[MAXD][MAXD]) {
         const int d = P.d;
@@ -862,7 +866,9 @@ struct PolyCell {
             for (const double* ce : centers) { for (int k = 0; k < d; ++k) cols[c][k] = ce[k] - xi[k]; ++c; }
             for (int v : L) { for (int k = 0; k < d; ++k) cols[c][k] = V[v].c[k] - xi[k]; ++c; }
             chains++;
-            return std::fabs(det_cols(cols));
+            const double w = std::fabs(det_cols(cols));
+            if (wv) { (*wv)[L[0]] += 0.5 * w; (*wv)[L[1]] += 0.5 * w; }
+            return w;
         }
         std::vector<double> cen(d, 0.0);
         for (int v : L) for (int k = 0; k < d; ++k) cen[k] += V[v].c[k];
@@ -995,6 +1001,13 @@ struct hvo_mesh {
     std::vector<int> nbr;
     std::vector<double> area;            // aligned with nbr (after symmetrisation)
     std::vector<double> vol;
+    // integrand quadrature of every facet computed by its lower cell, aligned
+    // with nbr: the facet's vertices (signatures, mapped to rows at the end),
+    // their edge weights sum |det| / 2 and the facet centre (mean of its vertices)
+    std::vector<std::vector<std::vector<int>>> qsig;
+    std::vector<std::vector<double>> qw;
+    std::vector<double> qc;              // nbr x d
+    std::vector<std::vector<int64_t>> qrow;
     bool integrated = false;
     Counters cnt;
     std::vector<int64_t> order;          // sorted vertex order
@@ -1011,6 +1024,14 @@ void finish_mesh(hvo_mesh* M) {
     M->order.resize(V);
     for (int64_t v = 0; v < V; ++v) M->order[v] = v;
     std::sort(M->order.begin(), M->order.end(), [&](int64_t a, int64_t b) { return M->vsig[a] < M->vsig[b]; });
+    if (!M->qsig.empty()) {
+        std::unordered_map<std::vector<int>, int64_t, SigHash> row;
+        for (int64_t o = 0; o < V; ++o) row.emplace(M->vsig[M->order[o]], o);
+        M->qrow.resize(M->qsig.size());
+        for (size_t t = 0; t < M->qsig.size(); ++t)
+            for (auto& sg : M->qsig[t]) M->qrow[t].push_back(row.at(sg));
+        M->qsig.clear();
+    }
     (void)d;
 }
 
@@ -1063,6 +1084,9 @@ static int build_mesh(hvo_mesh* M, int64_t n, const double* pts, int nthreads, i
     std::vector<std::vector<int>> nb(n);
     std::vector<std::vector<double>> ar(n);
     std::vector<std::vector<CellVertex>> owned(n);
+    std::vector<std::vector<std::vector<std::vector<int>>>> qs(integrate ? n : 0);
+    std::vector<std::vector<std::vector<double>>> qws(integrate ? n : 0);
+    std::vector<std::vector<double>> qcs(integrate ? n : 0);
     std::atomic<int> fail{0};
     auto per_cell = [&](Explorer& ex, int i, const std::vector<CellVertex>& cv, Counters& cnt) {
         std::vector<int> items;
@@ -1074,7 +1098,12 @@ static int build_mesh(hvo_mesh* M, int64_t n, const double* pts, int nthreads, i
         if (integrate) {
             PolyCell pc{P, i, cv};
             std::vector<double> a(items.size(), 0.0);
+            std::vector<double> wv(cv.size(), 0.0);
+            pc.wv = &wv;
             double fact = 1; for (int q = 2; q <= d; ++q) fact *= q;
+            qs[i].assign(items.size(), {});
+            qws[i].assign(items.size(), {});
+            qcs[i].assign(items.size() * d, 0.0);
             for (size_t t = 0; t < items.size(); ++t) {
                 int k = items[t];
                 if (!P.is_plane(k) && k < i) continue;
@@ -1082,9 +1111,16 @@ static int build_mesh(hvo_mesh* M, int64_t n, const double* pts, int nthreads, i
                 for (int v = 0; v < (int)cv.size(); ++v)
                     if (std::find(cv[v].sig.begin(), cv[v].sig.end(), k) != cv[v].sig.end()) L.push_back(v);
                 std::vector<int> K{k};
+                for (int v : L) wv[v] = 0.0;
                 double s = pc.chain_sum(L, K);
                 double Vik = s / fact;
                 a[t] = Vik * d / height(P, i, k);
+                for (int v : L) {
+                    qs[i][t].push_back(cv[v].sig);
+                    qws[i][t].push_back(wv[v]);
+                    for (int q = 0; q < d; ++q) qcs[i][t * d + q] += cv[v].c[q];
+                }
+                for (int q = 0; q < d; ++q) qcs[i][t * d + q] /= (double)L.size();
             }
             ar[i] = a;
             cnt.chains += pc.chains;
@@ -1137,6 +1173,15 @@ static int build_mesh(hvo_mesh* M, int64_t n, const double* pts, int nthreads, i
     M->nbr.resize(M->offs[n]);
     for (int64_t i = 0; i < n; ++i) std::copy(nb[i].begin(), nb[i].end(), M->nbr.begin() + M->offs[i]);
     if (integrate) {
+        M->qsig.resize(M->offs[n]);
+        M->qw.resize(M->offs[n]);
+        M->qc.assign((size_t)M->offs[n] * d, 0.0);
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t t = 0; t < M->offs[i + 1] - M->offs[i]; ++t) {
+                M->qsig[M->offs[i] + t] = std::move(qs[i][t]);
+                M->qw[M->offs[i] + t] = std::move(qws[i][t]);
+                std::copy(qcs[i].begin() + t * d, qcs[i].begin() + (t + 1) * d, M->qc.begin() + (M->offs[i] + t) * d);
+            }
         M->area.assign(M->offs[n], 0.0);
         M->vol.assign(n, 0.0);
         for (int64_t i = 0; i < n; ++i) std::copy(ar[i].begin(), ar[i].end(), M->area.begin() + M->offs[i]);
@@ -1183,6 +1228,77 @@ int hvo_polygon(const hvo_mesh* m, double* vol, double* area) {
     if (!m->integrated) { set_err("mesh built without integrate=1"); return -1; }
     std::copy(m->vol.begin(), m->vol.end(), vol);
     std::copy(m->area.begin(), m->area.end(), area);
+    return 0;
+}
+
+/* Integrals of tabulated functions, the reference's Polygon_Integrator with an
+ * integrand (src/polyintegrator.jl:80-123, 262-330): p components per node,
+ * fv at the vertices (rows of hvo_vertices), fc at the facet centres
+ * (hvo_facet_centers, aligned with hvo_neighbors), fx at the generators.
+ * Interface integral of facet (i, k), computed by the lower cell and copied:
+ *   I = (d-1)/d * sum_v W_v f(v) / ((d-1)! h) + A f(c_F) / d,
+ * W_v = sum over the flag simplices whose edge ends at v of |det| / 2;
+ * bulk of cell i (when bulk != 0): sum_k V_ik f(x_i)/(d+1) + I_ik h_ik/(d+1). */
+int hvo_polygon_functions(const hvo_mesh* m, int p, const double* fv, const double* fc, const double* fx, int bulk,
+                          double* iface, double* bulkint) {
+    if (!m->integrated || (m->qrow.empty() && !m->nbr.empty())) { set_err("mesh built without integrate=1"); return -1; }
+    const Problem& P = m->P;
+    const int d = P.d;
+    const int64_t n = P.n;
+    double fact1 = 1;  // (d-1)!
+    for (int q = 2; q < d; ++q) fact1 *= q;
+    std::fill(iface, iface + (size_t)m->nbr.size() * p, 0.0);
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t t = m->offs[i]; t < m->offs[i + 1]; ++t) {
+            const int k = m->nbr[t];
+            if (!P.is_plane(k) && k < i) continue;
+            const double h = height(P, (int)i, k);
+            for (int c = 0; c < p; ++c) {
+                double s = 0;
+                for (size_t x = 0; x < m->qrow[t].size(); ++x) s += m->qw[t][x] * fv[m->qrow[t][x] * p + c];
+                iface[t * p + c] = (d - 1.0) / d * s / (fact1 * h) + m->area[t] * fc[t * p + c] / d;
+            }
+        }
+    for (int64_t i = 0; i < n; ++i)  // interfaces to lower cells: copied
+        for (int64_t t = m->offs[i]; t < m->offs[i + 1]; ++t) {
+            const int k = m->nbr[t];
+            if (P.is_plane(k) || k > i) continue;
+            auto b = m->nbr.begin() + m->offs[k], e = m->nbr.begin() + m->offs[k + 1];
+            auto it = std::lower_bound(b, e, (int)i);
+            if (it != e && *it == (int)i)
+                for (int c = 0; c < p; ++c) iface[t * p + c] = iface[(m->offs[k] + (it - b)) * p + c];
+        }
+    if (bulk && bulkint) {
+        for (int64_t i = 0; i < n; ++i)
+            for (int c = 0; c < p; ++c) {
+                double s = 0;
+                for (int64_t t = m->offs[i]; t < m->offs[i + 1]; ++t) {
+                    const double h = height(P, (int)i, m->nbr[t]);
+                    const double vik = m->area[t] * h / d;
+                    s += fx[i * p + c] * vik / (d + 1.0) + iface[t * p + c] * h / (d + 1.0);
+                }
+                bulkint[i * p + c] = s;
+            }
+    }
+    return 0;
+}
+
+/* Facet centres (mean of the facet's vertices), nnbr x d aligned with
+ * hvo_neighbors (the lower cell's value for both directions). */
+int hvo_facet_centers(const hvo_mesh* m, double* centers) {
+    if (!m->integrated) { set_err("mesh built without integrate=1"); return -1; }
+    const Problem& P = m->P;
+    const int d = P.d;
+    for (int64_t i = 0; i < P.n; ++i)
+        for (int64_t t = m->offs[i]; t < m->offs[i + 1]; ++t) {
+            const int k = m->nbr[t];
+            int64_t src = t;
+            if (!P.is_plane(k) && k < i) {
+                auto b = m->nbr.begin() + m->offs[k], e = m->nbr.begin() + m->offs[k + 1];
+                src = m->offs[k] + (std::lower_bound(b, e, (int)i) - b);
+            }
+            for (int q = 0; q < d; ++q) centers[t * d + q] = m->qc[src * d + q];
+        }
     return 0;
 }
 

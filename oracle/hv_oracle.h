@@ -105,6 +105,15 @@ int hvo_certify_mesh(int d, int64_t n, const double* pts, const double* lo, cons
                      const double* base, const double* normal, int64_t nv, const int64_t* sig, const double* r,
                      int nthreads, int64_t* out, double* maxdev);
 
+/* Integrals of tabulated functions (p components) with the reference's
+ * polygon quadrature: fv at the vertices (hvo_vertices rows), fc at the facet
+ * centres (hvo_facet_centers), fx at the generators; interface integrals
+ * aligned with hvo_neighbors (nnbr x p) and, if bulk, cell integrals (n x p).
+ * Needs integrate=1. */
+int hvo_polygon_functions(const hvo_mesh* m, int p, const double* fv, const double* fc, const double* fx, int bulk,
+                          double* iface, double* bulkint);
+int hvo_facet_centers(const hvo_mesh* m, double* centers);
+
 /* Raw Philox4x32-10 block (for known-answer tests of the generator). */
 void hvo_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 

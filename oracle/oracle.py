@@ -70,6 +70,9 @@ def lib():
             L.hvo_sample_cells.restype = I
             L.hvo_verify_vertices.argtypes = [I, I64, dp, dp, dp, I64, ip, dp, D]
             L.hvo_verify_vertices.restype = I64
+            L.hvo_polygon_functions.argtypes = [P, I, dp, dp, dp, I, dp, dp]
+            L.hvo_polygon_functions.restype = I
+            L.hvo_facet_centers.argtypes = [P, dp]; L.hvo_facet_centers.restype = I
             L.hvo_mesh_from_csr.argtypes = [I, I64, dp, dp, dp, ip, ip, ctypes.POINTER(P)]
             L.hvo_mesh_from_csr.restype = I
             L.hvo_polygon_cells.argtypes = [I, I64, dp, dp, dp, U64, I, I64, ip, I64, dp, ip, ip, dp]
@@ -160,6 +163,31 @@ class OracleMesh:
         if L.hvo_polygon(self._h, _dp(vol), _dp(area)) != 0:
             raise RuntimeError(L.hvo_last_error().decode())
         return vol, area[:E]
+
+    def facet_centers(self):
+        """(nnbr, d) centres (vertex means) of the facets, aligned with neighbors()."""
+        L = lib()
+        E = L.hvo_num_neighbors(self._h)
+        c = np.zeros((max(E, 1), self.d))
+        if L.hvo_facet_centers(self._h, _dp(c)) != 0:
+            raise RuntimeError(L.hvo_last_error().decode())
+        return c[:E]
+
+    def polygon_functions(self, fv, fc, fx, bulk=True):
+        """Interface (nnbr, p) and cell (n, p) integrals of a function given by
+        its values fv at the vertices, fc at the facet centres and fx at the
+        generators (the reference's Polygon_Integrator with an integrand)."""
+        L = lib()
+        fv = np.ascontiguousarray(np.asarray(fv, dtype=np.float64).reshape(len(fv), -1))
+        p = fv.shape[1]
+        fc = np.ascontiguousarray(np.asarray(fc, dtype=np.float64).reshape(-1, p))
+        fx = np.ascontiguousarray(np.asarray(fx, dtype=np.float64).reshape(-1, p))
+        E = L.hvo_num_neighbors(self._h)
+        iface = np.zeros((max(E, 1), p))
+        blk = np.zeros((self.n, p))
+        if L.hvo_polygon_functions(self._h, p, _dp(fv), _dp(fc), _dp(fx), 1 if bulk else 0, _dp(iface), _dp(blk)) != 0:
+            raise RuntimeError(L.hvo_last_error().decode())
+        return iface[:E], blk
 
     def heuristic_mc(self, ndir, seed, nthreads=0, reference_directions=0):
         """i.i.d. directions per cell; ``reference_directions=r`` (> 0) instead

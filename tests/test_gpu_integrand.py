@@ -1,0 +1,62 @@
+"""Integrals of user functions with VI_POLYGON's quadrature on the GPU
+(hv_mesh_facet_centers / hv_integrate_polygon_functions) against the oracle's
+flag recursion, which follows the reference's Polygon_Integrator with an
+integrand (src/polyintegrator.jl:80-123,174-330).  The functions are the
+reference's own test integrands (test/basics.jl: x -> [1, x1, x2]) and x1^2.
+Bar: interface and cell integrals within RTOL relative; a constant function
+reproduces the areas and volumes; the linear one is exact in 2D and 3D."""
+import numpy as np
+import pytest
+
+import oracle as O
+from hvgpu import datasets as D
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+
+
+def _lin(P):
+    return np.stack([np.ones(len(P)), P[:, 0], P[:, 1]], axis=1)
+
+
+def _sq(P):
+    return P[:, :1] ** 2
+
+
+@pytest.mark.parametrize("d,n,seed", [(2, 400, 1), (3, 300, 2), (4, 150, 3), (5, 60, 4)])
+def test_integrands_match_the_oracle(gpu_lib, d, n, seed):
+    hv = gpu_lib
+    X = D.uniform_points(d, n, seed)
+    m = hv.Mesh(hv.default_context(), X, np.zeros(d), np.ones(d), hv.make_params(hv.HV_METHOD_FAST))
+    ref = O.OracleMesh(X, integrate=True)
+    s, r = m.vertices()
+    rs, rr = ref.vertices()
+    np.testing.assert_array_equal(s, rs)
+    c = m.facet_centers()
+    np.testing.assert_allclose(c, ref.facet_centers(), rtol=0, atol=1e-13)
+    vol, area = m.polygon()
+    for f in (_lin, _sq):
+        gi, gb = m.polygon_functions(f(r), f(c), f(X))
+        oi, ob = ref.polygon_functions(f(rr), f(c), f(X))
+        scale_i = np.abs(oi).max(axis=0)
+        assert np.all(np.abs(gi - oi) <= RTOL * scale_i + 1e-300)
+        np.testing.assert_allclose(gb, ob, rtol=RTOL, atol=RTOL * np.abs(ob).max())
+    gi, gb = m.polygon_functions(np.ones((len(r), 1)), np.ones((len(c), 1)), np.ones((n, 1)))
+    np.testing.assert_allclose(gi[:, 0], area, rtol=1e-11)
+    np.testing.assert_allclose(gb[:, 0], vol, rtol=1e-11)
+    if d <= 3:  # the reference's rule integrates linear functions exactly in 2D and 3D
+        _, gb = m.polygon_functions(_lin(r), _lin(c), _lin(X))
+        np.testing.assert_allclose(gb.sum(axis=0), [1.0, 0.5, 0.5], rtol=1e-12)
+
+
+def test_integrand_through_the_geometry_api(gpu_lib):
+    hv = gpu_lib
+    X = D.uniform_points(3, 200, 9)
+    geo = hv.VoronoiGeometry(X, hv.cuboid(3, periodic=[]), integrator=hv.VI_POLYGON, integrand=_lin)
+    vd = hv.VoronoiData(geo)
+    assert len(vd.bulk_integral) == 200 and vd.bulk_integral[0].shape == (3,)
+    np.testing.assert_allclose(sum(vd.bulk_integral), [1.0, 0.5, 0.5], rtol=1e-12)
+    np.testing.assert_allclose([b[0] for b in vd.bulk_integral], vd.volume, rtol=1e-11)
+    for i in (0, 17, 101):
+        np.testing.assert_allclose(vd.interface_integral[i][:, 0], vd.area[i], rtol=1e-11)

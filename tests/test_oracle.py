@@ -395,3 +395,25 @@ def test_polygon_cells_match_the_mesh_pass(d, n):
     for c, i in enumerate(cells):
         np.testing.assert_array_equal(items[offs[c]:offs[c + 1]], rn[ro[i]:ro[i + 1]])
         np.testing.assert_allclose(a[offs[c]:offs[c + 1]], area[ro[i]:ro[i + 1]], rtol=1e-11, atol=1e-15)
+
+
+@pytest.mark.parametrize("d,n", [(2, 300), (3, 150), (4, 80)])
+def test_oracle_integrand_quadrature(d, n):
+    """The polygon quadrature of an integrand: a constant gives the areas and
+    volumes; [1, x1, x2] integrates exactly over the cube in 2D and 3D (the
+    reference's rule is the centroid rule on the facet simplices there)."""
+    X = D.uniform_points(d, n, 50 + d)
+    m = O.OracleMesh(X, integrate=True)
+    vol, area = m.polygon()
+    s, r = m.vertices()
+    c = m.facet_centers()
+    one = lambda P: np.ones((len(P), 1))  # noqa: E731
+    I, B = m.polygon_functions(one(r), one(c), one(X))
+    np.testing.assert_allclose(I[:, 0], area, rtol=1e-12)
+    np.testing.assert_allclose(B[:, 0], vol, rtol=1e-12)
+    lin = lambda P: np.stack([np.ones(len(P)), P[:, 0], P[:, 1]], axis=1)  # noqa: E731
+    _, B = m.polygon_functions(lin(r), lin(c), lin(X))
+    if d <= 3:
+        np.testing.assert_allclose(B.sum(axis=0), [1.0, 0.5, 0.5], rtol=1e-12)
+    else:
+        assert abs(B.sum(axis=0)[1] - 0.5) < 0.01
