@@ -84,6 +84,7 @@ struct hv_mesh {
     double* q_a = nullptr;        // nnbr: flag sums
     double* q_c = nullptr;        // nnbr x d: facet centres
     double* q_af = nullptr;       // nnbr: facet areas
+    bool q_weights = false;       // the flag weights are in q_w (not only lists and centres)
 };
 
 namespace {
@@ -1555,8 +1556,14 @@ hv::QuadRun quad_run(hv_mesh* m) {
     return Q;
 }
 
-void ensure_quad(hv_mesh* m) {
-    if (m->q_foff) return;
+void ensure_quad(hv_mesh* m, bool weights) {
+    if (m->q_foff && (m->q_weights || !weights)) return;
+    if (m->q_foff) {  // lists and centres exist: the flag weights on top
+        for (void* p : {(void*)m->q_foff, (void*)m->q_slot, (void*)m->q_v, (void*)m->q_w, (void*)m->q_a,
+                        (void*)m->q_c, (void*)m->q_af}) dfree(m->ctx->stream, p);
+        m->q_foff = nullptr; m->q_slot = nullptr; m->q_v = nullptr; m->q_w = nullptr;
+        m->q_a = nullptr; m->q_c = nullptr; m->q_af = nullptr;
+    }
     ensure_neighbors(m);
     hv_ctx* ctx = m->ctx;
     cudaStream_t st = ctx->stream;
@@ -1599,7 +1606,8 @@ void ensure_quad(hv_mesh* m) {
     hv::QuadRun Q = quad_run(m);
     Q.fvert = fvert;
     Q.status = dstat;
-    hv::launch_poly_quad(Q, ctx->nsm, st);
+    hv::launch_poly_quad(Q, weights, ctx->nsm, st);
+    m->q_weights = weights;
     hv::launch_quad_copy(Q, m->d, m->q_c, st);  // centres of the higher cells' slots
     CK(cudaGetLastError());
     unsigned hs = 0;
@@ -1693,7 +1701,7 @@ int hv_mesh_facet_centers(hv_mesh* m, double* centers) {
     if (rc != HV_OK) return rc;
     try {
         CK(cudaSetDevice(m->ctx->device));
-        ensure_quad(m);
+        ensure_quad(m, false);
         if (m->nnbr > 0) {
             if (!centers) return HV_E_INVALID_ARG;
             CK(cudaMemcpyAsync(centers, m->q_c, sizeof(double) * m->nnbr * m->d, cudaMemcpyDeviceToHost,
@@ -1713,7 +1721,7 @@ int hv_integrate_polygon_functions(hv_mesh* m, int p, const double* fv, const do
     if (p < 1 || (m->V > 0 && !fv) || !fx) return HV_E_INVALID_ARG;
     try {
         CK(cudaSetDevice(m->ctx->device));
-        ensure_quad(m);
+        ensure_quad(m, true);
         const long long ns = m->nnbr;
         if (ns > 0 && (!fc || !iface)) return HV_E_INVALID_ARG;
         cudaStream_t st = m->ctx->stream;
@@ -1739,6 +1747,39 @@ int hv_integrate_polygon_functions(hv_mesh* m, int p, const double* fv, const do
 
 int hv_integrate_polygon_device(hv_mesh* m, double* d_vol, double* d_area) {
     return polygon_impl(m, d_vol, d_area, true);
+}
+
+int hv_integrate_heuristic_functions(hv_mesh* m, int p, const double* area, const double* fv, const double* fc,
+                                     const double* fx, double* iface, double* bulk) {
+    int rc = quad_check(m);
+    if (rc != HV_OK) return rc;
+    if (p < 1 || (m->V > 0 && !fv) || !fx) return HV_E_INVALID_ARG;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        ensure_quad(m, false);
+        const long long ns = m->nnbr;
+        if (ns > 0 && (!fc || !iface || !area)) return HV_E_INVALID_ARG;
+        cudaStream_t st = m->ctx->stream;
+        Scratch s(st);
+        double* dar = s.get<double>((size_t)std::max(ns, 1ll));
+        double* dfv = s.get<double>((size_t)std::max(m->V, 1u) * p);
+        double* dfc = s.get<double>((size_t)std::max(ns, 1ll) * p);
+        double* dfx = s.get<double>((size_t)m->n * p);
+        double* dif = s.get<double>((size_t)std::max(ns, 1ll) * p);
+        double* dbk = bulk ? s.get<double>((size_t)m->n * p) : nullptr;
+        if (ns) CK(cudaMemcpyAsync(dar, area, sizeof(double) * ns, cudaMemcpyHostToDevice, st));
+        if (m->V) CK(cudaMemcpyAsync(dfv, fv, sizeof(double) * m->V * p, cudaMemcpyHostToDevice, st));
+        if (ns) CK(cudaMemcpyAsync(dfc, fc, sizeof(double) * ns * p, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dfx, fx, sizeof(double) * m->n * p, cudaMemcpyHostToDevice, st));
+        hv::launch_heur_integrals(quad_run(m), p, dar, dfv, dfc, dfx, dif, dbk, st);
+        CK(cudaGetLastError());
+        if (ns) CK(cudaMemcpyAsync(iface, dif, sizeof(double) * ns * p, cudaMemcpyDeviceToHost, st));
+        if (bulk) CK(cudaMemcpyAsync(bulk, dbk, sizeof(double) * m->n * p, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
 }
 
 int hv_integrate_heuristic_mc(hv_mesh* m, int ndir, uint64_t seed, double* vol, double* area) {

@@ -85,7 +85,9 @@ struct QuadRun {
     double* af;
     unsigned* status;         // 1: facet over QUAD_MAXV vertices, 8: facet not simple
 };
-void launch_poly_quad(const QuadRun& Q, int nsm, cudaStream_t st);
+void launch_poly_quad(const QuadRun& Q, bool weights, int nsm, cudaStream_t st);
+void launch_heur_integrals(const QuadRun& Q, int p, const double* area, const double* fv, const double* fc,
+                           const double* fx, double* iface, double* bulk, cudaStream_t st);
 // per-slot values a (slots x p) of the higher cells copied from the lower cell's slot
 void launch_quad_copy(const QuadRun& Q, int p, double* a, cudaStream_t st);
 void launch_quad_integrals(const QuadRun& Q, int p, const double* fv, const double* fc, const double* fx,

@@ -40,7 +40,7 @@ __device__ __forceinline__ bool has_item(const int* osig, unsigned v, int it) {
     return h;
 }
 
-template <int D>
+template <int D, bool WEIGHTS>
 __global__ void __launch_bounds__(64) k_poly_quad(QuadRun Q) {
     constexpr int DEP = D > 2 ? D - 1 : 2;  // depths 1 .. D-1
     unsigned mask[DEP][QUAD_WORDS];
@@ -61,6 +61,17 @@ __global__ void __launch_bounds__(64) k_poly_quad(QuadRun Q) {
             int b = a - 1;
             while (b >= 0 && qv[b] > x) { qv[b + 1] = qv[b]; --b; }
             qv[b + 1] = x;
+        }
+        if (!WEIGHTS) {  // the vertex lists and the facet centres only
+            double c[D];
+#pragma unroll
+            for (int q = 0; q < D; ++q) c[q] = 0.0;
+            for (int a = 0; a < nv; ++a)
+#pragma unroll
+                for (int q = 0; q < D; ++q) c[q] += Q.oc[(size_t)qv[a] * D + q];
+#pragma unroll
+            for (int q = 0; q < D; ++q) Q.qc[(size_t)t * D + q] = c[q] / (double)nv;
+            continue;
         }
         for (int a = 0; a < nv; ++a) qw[a] = 0.0;
         const int i = Q.slot_cell[t], k = Q.nbr[t];
@@ -253,8 +264,56 @@ static unsigned grid_of(long long n, int bs, int cap) {
     return (unsigned)std::max(1ll, std::min(g, (long long)cap));
 }
 
-void launch_poly_quad(const QuadRun& Q, int nsm, cudaStream_t st) {
-    HV_DISPATCH(Q.d, (k_poly_quad<DD><<<grid_of(Q.nslots, 64, nsm * 16), 64, 0, st>>>(Q)));
+void launch_poly_quad(const QuadRun& Q, bool weights, int nsm, cudaStream_t st) {
+    if (weights) {
+        HV_DISPATCH(Q.d, (k_poly_quad<DD, true><<<grid_of(Q.nslots, 64, nsm * 16), 64, 0, st>>>(Q)));
+    } else {
+        HV_DISPATCH(Q.d, (k_poly_quad<DD, false><<<grid_of(Q.nslots, 64, nsm * 16), 64, 0, st>>>(Q)));
+    }
+}
+
+// The reference's heuristic integrand rule (src/heuristic.jl:105-166) on the
+// areas the caller passes (from the Monte-Carlo integrator): per facet, the
+// mean of f over its vertices with weight (d-1)/d and f at its centre with
+// weight 1/d, times the area; the cell integral adds h/d (A f(x_i)/(d+1) +
+// d/(d+1) I) over the facets.
+template <int D>
+__global__ void k_heur_iface(QuadRun Q, int p, const double* area, const double* fv, const double* fc, double* iface) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < Q.nslots;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long f0 = Q.foff[t], f1e = Q.foff[t + 1];
+        if (f1e == f0) continue;
+        for (int c = 0; c < p; ++c) {
+            double s = 0.0;
+            for (long long x = f0; x < f1e; ++x) s += fv[(size_t)Q.qv[x] * p + c];
+            iface[t * p + c] = area[t] * ((D - 1.0) / D * s / (double)(f1e - f0) + fc[t * p + c] / D);
+        }
+    }
+}
+
+template <int D>
+__global__ void k_heur_bulk(QuadRun Q, int p, const double* area, const double* fx, const double* iface, double* bulk) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < Q.n; i += gridDim.x * blockDim.x) {
+        double xi[D];
+#pragma unroll
+        for (int q = 0; q < D; ++q) xi[q] = Q.pts[(size_t)i * D + q];
+        for (int c = 0; c < p; ++c) {
+            double s = 0.0;
+            for (long long t = Q.nbr_off[i]; t < Q.nbr_off[i + 1]; ++t) {
+                const double h = facet_h<D>(Q, xi, Q.nbr[t]);
+                s += h / D * (area[t] * fx[(size_t)i * p + c] / (D + 1.0) + D / (D + 1.0) * iface[t * p + c]);
+            }
+            bulk[(size_t)i * p + c] = s;
+        }
+    }
+}
+
+void launch_heur_integrals(const QuadRun& Q, int p, const double* area, const double* fv, const double* fc,
+                           const double* fx, double* iface, double* bulk, cudaStream_t st) {
+    HV_DISPATCH(Q.d, (k_heur_iface<DD><<<grid_of(Q.nslots, 256, 1 << 20), 256, 0, st>>>(Q, p, area, fv, fc, iface)));
+    HV_DISPATCH(Q.d, (k_quad_copy<DD><<<grid_of(Q.n, 256, 1 << 20), 256, 0, st>>>(Q, p, iface)));
+    if (bulk)
+        HV_DISPATCH(Q.d, (k_heur_bulk<DD><<<grid_of(Q.n, 256, 1 << 20), 256, 0, st>>>(Q, p, area, fx, iface, bulk)));
 }
 
 void launch_quad_copy(const QuadRun& Q, int p, double* a, cudaStream_t st) {

@@ -137,6 +137,8 @@ def load(path: str | None = None):
         L.hv_mesh_facet_centers.argtypes = [P, dp]; L.hv_mesh_facet_centers.restype = I
         L.hv_integrate_polygon_functions.argtypes = [P, I, dp, dp, dp, dp, dp]
         L.hv_integrate_polygon_functions.restype = I
+        L.hv_integrate_heuristic_functions.argtypes = [P, I, dp, dp, dp, dp, dp, dp]
+        L.hv_integrate_heuristic_functions.restype = I
         L.hv_mesh_refine.argtypes = [P, I64, P, ctypes.POINTER(P)]; L.hv_mesh_refine.restype = I
         L.hv_mesh_refine_device.argtypes = [P, I64, P, ctypes.POINTER(P)]; L.hv_mesh_refine_device.restype = I
         L.hv_mesh_build_shard.argtypes = [P, I, I64, P, dp, dp, I, I, ctypes.POINTER(Params), ctypes.POINTER(P)]
@@ -401,9 +403,27 @@ class Mesh:
         self.ctx.check(rc, "hv_integrate_polygon_functions")
         return iface[:E], blk
 
-    def integrate_function(self, f, bulk: bool = True):
+    def heuristic_functions(self, area, fv, fc, fx, bulk: bool = True):
+        """The reference's heuristic integrand rule (hv_integrate_heuristic_functions)
+        on the interface areas ``area`` (e.g. from heuristic_mc)."""
+        V, E = self.counts(neighbors=True)
+        fv = np.ascontiguousarray(np.asarray(fv, dtype=np.float64).reshape(V, -1))
+        p = fv.shape[1]
+        fc = np.ascontiguousarray(np.asarray(fc, dtype=np.float64).reshape(E, p))
+        fx = np.ascontiguousarray(np.asarray(fx, dtype=np.float64).reshape(self.n, p))
+        area = np.ascontiguousarray(np.asarray(area, dtype=np.float64).reshape(E))
+        iface = np.zeros((max(E, 1), p))
+        blk = np.zeros((self.n, p)) if bulk else None
+        rc = load().hv_integrate_heuristic_functions(self._h, p, dptr(area), dptr(fv), dptr(fc), dptr(fx),
+                                                      dptr(iface), dptr(blk) if bulk else None)
+        self.ctx.check(rc, "hv_integrate_heuristic_functions")
+        return iface[:E], blk
+
+    def integrate_function(self, f, bulk: bool = True, heuristic_area=None):
         """Evaluates ``f`` ((m, d) points -> (m,) or (m, p) values) at the
-        quadrature nodes and returns the interface and cell integrals."""
+        quadrature nodes and returns the interface and cell integrals: the
+        polygon rule, or with ``heuristic_area`` (the interface areas of the
+        Monte-Carlo integrator) the heuristic rule."""
         _, r = self.vertices()
         c = self.facet_centers()
         x = self.points()
@@ -411,6 +431,8 @@ class Mesh:
         def ev(P):
             y = np.asarray(f(P), dtype=np.float64)
             return y.reshape(len(P), -1)
+        if heuristic_area is not None:
+            return self.heuristic_functions(heuristic_area, ev(r), ev(c), ev(x), bulk)
         return self.polygon_functions(ev(r), ev(c), ev(x), bulk)
 
     def points(self) -> np.ndarray:

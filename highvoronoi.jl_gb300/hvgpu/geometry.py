@@ -235,6 +235,9 @@ class VoronoiGeometry:
                 self._iface_int, self._bulk_int = self.mesh.integrate_function(self.integrand, self.bulk)
         elif self.integrator in (VI_HEURISTIC_MC, VI_MONTECARLO):
             self._volumes, self._areas = self.mesh.heuristic_mc(int(self.mc_accurate[0]), int(self.mc_seed))
+            if self.integrand is not None and self.integrator == VI_HEURISTIC_MC:
+                self._iface_int, self._bulk_int = self.mesh.integrate_function(self.integrand, self.bulk,
+                                                                               heuristic_area=self._areas)
 
     def refine(self, xs, update: bool = True) -> "VoronoiGeometry":
         """refine!(VG, xs, update) (src/geometry.jl:404-433): appends the
@@ -345,9 +348,10 @@ class VoronoiData:
     added, ``references`` (1-based originals) and ``reference_shifts`` (their
     translation vectors) describe them; otherwise ``offset`` is 0.  There are
     no infinite edges (``boundary_vertices``).  With ``integrand=f`` and
-    VI_POLYGON, ``bulk_integral[i]`` (p values) and ``interface_integral[i]``
-    ((deg, p), aligned with ``neighbors[i]``) hold the integrals of f with the
-    reference's polygon quadrature (box and plane domains).
+    VI_POLYGON or VI_HEURISTIC_MC, ``bulk_integral[i]`` (p values) and
+    ``interface_integral[i]`` ((deg, p), aligned with ``neighbors[i]``) hold the
+    integrals of f with the reference's polygon quadrature or its heuristic
+    rule on the Monte-Carlo areas (box and plane domains).
     """
 
     def __init__(self, geo: VoronoiGeometry, onboundary: bool = False):

@@ -182,6 +182,16 @@ int hv_integrate_polygon(hv_mesh* mesh, double* vol, double* area);
 int hv_mesh_facet_centers(hv_mesh* m, double* centers);
 int hv_integrate_polygon_functions(hv_mesh* m, int p, const double* fv, const double* fc, const double* fx,
                                    double* iface, double* bulk);
+/* Integrals of a user function with the reference's heuristic rule of
+ * VI_HEURISTIC_MC (Heuristic_Integrator, src/heuristic.jl:105-166) on given
+ * interface areas (nnbr, aligned with hv_mesh_neighbors; normally those of
+ * hv_integrate_heuristic_mc): I = A ((d-1)/d mean of f over the facet's
+ * vertices + f(c_F)/d), bulk_i = sum_k h_ik/d (A_ik f(x_i)/(d+1) +
+ * d/(d+1) I_ik).  Nodes and arguments as hv_integrate_polygon_functions.  Every
+ * facet uses all its vertices (the reference keeps a single vertex for facets
+ * toward lower-numbered neighbours, which depends on its storage order). */
+int hv_integrate_heuristic_functions(hv_mesh* m, int p, const double* area, const double* fv, const double* fc,
+                                     const double* fx, double* iface, double* bulk);
 /* Monte-Carlo volumes and areas, ndir Philox directions per cell. */
 int hv_integrate_heuristic_mc(hv_mesh* mesh, int ndir, uint64_t seed, double* vol, double* area);
 /* Periodic cuboid [lo, hi] (cuboid(d, periodic=...), src/boundary.jl:510-534):

@@ -1283,6 +1283,49 @@ int hvo_polygon_functions(const hvo_mesh* m, int p, const double* fv, const doub
     return 0;
 }
 
+/* The reference's heuristic integrand rule (Heuristic_Integrator,
+ * src/heuristic.jl:105-166) on given interface areas (aligned with
+ * hvo_neighbors): I = A ((d-1)/d mean_v f(v) + f(c_F)/d) over every vertex of
+ * the facet (computed by the lower cell and copied), bulk_i = sum_k h/d
+ * (A f(x_i)/(d+1) + d/(d+1) I).  Needs integrate=1 (the facet vertex lists). */
+int hvo_heuristic_functions(const hvo_mesh* m, int p, const double* area, const double* fv, const double* fc,
+                            const double* fx, int bulk, double* iface, double* bulkint) {
+    if (!m->integrated || (m->qrow.empty() && !m->nbr.empty())) { set_err("mesh built without integrate=1"); return -1; }
+    const Problem& P = m->P;
+    const int d = P.d;
+    const int64_t n = P.n;
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t t = m->offs[i]; t < m->offs[i + 1]; ++t) {
+            const int k = m->nbr[t];
+            if (!P.is_plane(k) && k < i) continue;
+            for (int c = 0; c < p; ++c) {
+                double s = 0;
+                for (int64_t row : m->qrow[t]) s += fv[row * p + c];
+                iface[t * p + c] = area[t] * ((d - 1.0) / d * s / (double)m->qrow[t].size() + fc[t * p + c] / d);
+            }
+        }
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t t = m->offs[i]; t < m->offs[i + 1]; ++t) {
+            const int k = m->nbr[t];
+            if (P.is_plane(k) || k > i) continue;
+            auto b = m->nbr.begin() + m->offs[k], e = m->nbr.begin() + m->offs[k + 1];
+            auto it = std::lower_bound(b, e, (int)i);
+            if (it != e && *it == (int)i)
+                for (int c = 0; c < p; ++c) iface[t * p + c] = iface[(m->offs[k] + (it - b)) * p + c];
+        }
+    if (bulk && bulkint)
+        for (int64_t i = 0; i < n; ++i)
+            for (int c = 0; c < p; ++c) {
+                double s = 0;
+                for (int64_t t = m->offs[i]; t < m->offs[i + 1]; ++t) {
+                    const double h = height(P, (int)i, m->nbr[t]);
+                    s += h / d * (area[t] * fx[i * p + c] / (d + 1.0) + d / (d + 1.0) * iface[t * p + c]);
+                }
+                bulkint[i * p + c] = s;
+            }
+    return 0;
+}
+
 /* Facet centres (mean of the facet's vertices), nnbr x d aligned with
  * hvo_neighbors (the lower cell's value for both directions). */
 int hvo_facet_centers(const hvo_mesh* m, double* centers) {

@@ -113,6 +113,10 @@ int hvo_certify_mesh(int d, int64_t n, const double* pts, const double* lo, cons
 int hvo_polygon_functions(const hvo_mesh* m, int p, const double* fv, const double* fc, const double* fx, int bulk,
                           double* iface, double* bulkint);
 int hvo_facet_centers(const hvo_mesh* m, double* centers);
+/* The heuristic integrand rule on given interface areas (aligned with
+ * hvo_neighbors); needs integrate=1. */
+int hvo_heuristic_functions(const hvo_mesh* m, int p, const double* area, const double* fv, const double* fc,
+                            const double* fx, int bulk, double* iface, double* bulkint);
 
 /* Raw Philox4x32-10 block (for known-answer tests of the generator). */
 void hvo_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

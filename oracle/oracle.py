@@ -73,6 +73,8 @@ def lib():
             L.hvo_polygon_functions.argtypes = [P, I, dp, dp, dp, I, dp, dp]
             L.hvo_polygon_functions.restype = I
             L.hvo_facet_centers.argtypes = [P, dp]; L.hvo_facet_centers.restype = I
+            L.hvo_heuristic_functions.argtypes = [P, I, dp, dp, dp, dp, I, dp, dp]
+            L.hvo_heuristic_functions.restype = I
             L.hvo_mesh_from_csr.argtypes = [I, I64, dp, dp, dp, ip, ip, ctypes.POINTER(P)]
             L.hvo_mesh_from_csr.restype = I
             L.hvo_polygon_cells.argtypes = [I, I64, dp, dp, dp, U64, I, I64, ip, I64, dp, ip, ip, dp]
@@ -186,6 +188,22 @@ class OracleMesh:
         iface = np.zeros((max(E, 1), p))
         blk = np.zeros((self.n, p))
         if L.hvo_polygon_functions(self._h, p, _dp(fv), _dp(fc), _dp(fx), 1 if bulk else 0, _dp(iface), _dp(blk)) != 0:
+            raise RuntimeError(L.hvo_last_error().decode())
+        return iface[:E], blk
+
+    def heuristic_functions(self, area, fv, fc, fx, bulk=True):
+        """The heuristic integrand rule on the interface areas ``area``."""
+        L = lib()
+        fv = np.ascontiguousarray(np.asarray(fv, dtype=np.float64).reshape(len(fv), -1))
+        p = fv.shape[1]
+        fc = np.ascontiguousarray(np.asarray(fc, dtype=np.float64).reshape(-1, p))
+        fx = np.ascontiguousarray(np.asarray(fx, dtype=np.float64).reshape(-1, p))
+        area = np.ascontiguousarray(area, dtype=np.float64)
+        E = L.hvo_num_neighbors(self._h)
+        iface = np.zeros((max(E, 1), p))
+        blk = np.zeros((self.n, p))
+        if L.hvo_heuristic_functions(self._h, p, _dp(area), _dp(fv), _dp(fc), _dp(fx), 1 if bulk else 0,
+                                     _dp(iface), _dp(blk)) != 0:
             raise RuntimeError(L.hvo_last_error().decode())
         return iface[:E], blk
 

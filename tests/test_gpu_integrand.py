@@ -60,3 +60,36 @@ def test_integrand_through_the_geometry_api(gpu_lib):
     np.testing.assert_allclose([b[0] for b in vd.bulk_integral], vd.volume, rtol=1e-11)
     for i in (0, 17, 101):
         np.testing.assert_allclose(vd.interface_integral[i][:, 0], vd.area[i], rtol=1e-11)
+
+
+@pytest.mark.parametrize("d,n,seed", [(3, 300, 5), (4, 150, 6), (6, 40, 7)])
+def test_heuristic_integrand_matches_the_oracle(gpu_lib, d, n, seed):
+    """VI_HEURISTIC_MC with an integrand (src/heuristic.jl:105-166) on the GPU's
+    Monte-Carlo areas: GPU and oracle apply the same rule to the same inputs."""
+    hv = gpu_lib
+    X = D.uniform_points(d, n, seed)
+    m = hv.Mesh(hv.default_context(), X, np.zeros(d), np.ones(d), hv.make_params(hv.HV_METHOD_FAST))
+    ref = O.OracleMesh(X, integrate=True)
+    _, area = m.heuristic_mc(500, 3)
+    s, r = m.vertices()
+    c = m.facet_centers()
+    for f in (_lin, _sq):
+        gi, gb = m.heuristic_functions(area, f(r), f(c), f(X))
+        oi, ob = ref.heuristic_functions(area, f(r), f(c), f(X))
+        np.testing.assert_allclose(gi, oi, rtol=1e-12, atol=1e-14 * np.abs(oi).max())
+        np.testing.assert_allclose(gb, ob, rtol=1e-12, atol=1e-14 * np.abs(ob).max())
+    geo = hv.VoronoiGeometry(X, hv.cuboid(d, periodic=[]), integrator=hv.VI_HEURISTIC_MC, integrand=_lin,
+                             mc_accurate=(500, 1, 20), mc_seed=3)
+    vd = hv.VoronoiData(geo)
+    # a constant integrand gives sum_k A_ik h_ik / d per cell (the cone volumes of the MC areas)
+    offs, nbr = geo.mesh.neighbors()
+    for i in (0, 7, n - 1):
+        h = []
+        for k in nbr[offs[i]:offs[i + 1]]:
+            if k <= n:
+                h.append(0.5 * np.linalg.norm(X[k - 1] - X[i]))
+            else:
+                p = k - n - 1
+                h.append(1.0 - X[i, p // 2] if p % 2 == 0 else X[i, p // 2])
+        expect = np.sum(vd.area[i] * np.array(h)) / d
+        assert abs(vd.bulk_integral[i][0] - expect) < 1e-12 * max(expect, 1e-300)
