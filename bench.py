@@ -228,8 +228,17 @@ def run_serve(args, device):
                      ", Poisson arrivals"}
     if not args.no_serve_capacity:
         clat, _, cfails, _, ct = stream(np.zeros(len(pts)))
-        out["capacity"] = {"meshes_per_s": len(clat) / ct, "failures": cfails, "seconds": ct,
+        cap = len(clat) / ct
+        out["capacity"] = {"meshes_per_s": cap, "failures": cfails, "seconds": ct,
                            "note": "all requests queued at t=0: the sustainable rate"}
+        # the same stream offered at 85% of that rate: latencies of the service, not of a growing queue
+        rate = 0.85 * cap
+        slat, ssvc, sfails, _, st_end = stream(np.cumsum(gaps / rate))
+        out["at_85pct_capacity"] = {"rate_per_s": rate, "p50_ms": float(np.percentile(slat, 50)),
+                                    "p99_ms": float(np.percentile(slat, 99)), "mean_ms": float(slat.mean()),
+                                    "meshes_per_s": len(slat) / st_end, "failures": sfails,
+                                    "service_p99_ms": float(np.percentile(ssvc, 99)),
+                                    "service_max_ms": float(ssvc.max())}
     return out
 
 
