@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "hv_host.h"
+#include "hv_degen.h"
 #include "hv_integrate.h"
 #include "hv_internal.cuh"
 #include "hv_periodic.h"
@@ -85,6 +86,16 @@ struct hv_mesh {
     double* q_c = nullptr;        // nnbr x d: facet centres
     double* q_af = nullptr;       // nnbr: facet areas
     bool q_weights = false;       // the flag weights are in q_w (not only lists and centres)
+    // vertices with more than d+1 generators (hv_degen.cu): every vertex's
+    // generator list as a CSR in canonical order; osig is then null
+    int g_max = 0;                // longest list (0: the fixed-width osig holds the vertices)
+    long long* g_off = nullptr;   // V + 1
+    int* g_sig = nullptr;         // g_off[V] original 0-based items, ascending per vertex
+    int* g_fcell = nullptr;       // nnbr: cell of each neighbour slot
+    long long* g_fbeg = nullptr;  // nnbr: the facet's vertices are g_fvert[g_fbeg .. g_fend)
+    long long* g_fend = nullptr;
+    int* g_fvert = nullptr;
+    bool allow_generic = false;   // a search that meets co-spherical generators walks them here
 };
 
 namespace {
@@ -245,6 +256,214 @@ void check_fatal(unsigned status) {
         throw HvError(HV_E_INTERNAL, "device search failed (status " + std::to_string(status) + ")");
 }
 
+// Vertices with more than d+1 generators: the search met co-spherical
+// generators (or HV_METHOD_GENERIC asked for this walk).  The vertex graph is
+// walked again from the search's first vertex with every vertex keeping all
+// generators on its sphere (hv_degen.cu); the result replaces the fixed-width
+// vertex list with a CSR of generator lists, and the neighbour lists keep the
+// pairs that share a full interface.  The device tree, points and planes of
+// the search (M) are reused.
+void generic_build(hv_ctx* ctx, hv_mesh* mesh, const hv::DevMesh& M) {
+    using namespace hv;
+    cudaStream_t st = ctx->stream;
+    const int d = mesh->d, n = mesh->n;
+    if (mesh->V == 0 || !mesh->osig) throw HvError(HV_E_INTERNAL, "no vertex to start the degenerate walk from");
+    int W = std::min(GMAX, std::max(2 * (d + 1), (1 << d) + 2 * d));
+    const unsigned long long vest = (unsigned long long)(vertices_per_point(d) * n) + (1ull << d) + 1024;
+    for (int attempt = 0;; ++attempt) {
+        if (attempt > 6) throw HvError(HV_E_CAPACITY, "degenerate walk: capacity retries exhausted");
+        const unsigned long long vcap64 = vest << std::min(attempt, 5);
+        if (vcap64 > 0x7FFFFFF0ull) throw HvError(HV_E_CAPACITY, "degenerate walk: vertex count beyond 31-bit ids");
+        Scratch s(st);
+        GenRun R{};
+        R.M = M;
+        R.x = mesh->d_in;
+        R.W = W;
+        R.vcap = (unsigned)vcap64;
+        R.vsig = s.get<int>((size_t)R.vcap * W);
+        R.vlen = s.get<int>(R.vcap);
+        R.vc = s.get<double>((size_t)R.vcap * d);
+        const unsigned long long hsize = next_pow2(2ull * R.vcap);
+        R.hmask = hsize - 1;
+        R.htab = s.get<unsigned long long>(hsize);
+        CK(cudaMemsetAsync(R.htab, 0xFF, sizeof(unsigned long long) * hsize, st));
+        unsigned* cnt = s.get<unsigned>(4);  // vertices, records, edges, status
+        CK(cudaMemsetAsync(cnt, 0, 4 * sizeof(unsigned), st));
+        R.vcnt = cnt; R.rcnt = cnt + 1; R.e_cnt = cnt + 2; R.status = cnt + 3;
+        unsigned hc[4] = {0, 0, 0, 0};
+        auto read = [&] {
+            CK(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+        };
+        launch_gen_seed(R, mesh->osig, mesh->oc, st);
+        CK(cudaGetLastError());
+        read();
+        std::unique_ptr<Scratch> es;
+        auto grow_edges = [&](unsigned need) {
+            es.reset(new Scratch(st));
+            R.e_cap = std::max(need, 4096u);
+            R.e_vert = es->get<unsigned>(R.e_cap);
+            R.e_F = es->get<unsigned long long>(R.e_cap);
+            R.e_u = es->get<double>((size_t)R.e_cap * d);
+            R.rcap = R.e_cap;
+            R.rsig = es->get<int>((size_t)R.rcap * W);
+            R.rlen = es->get<int>(R.rcap);
+            R.rc = es->get<double>((size_t)R.rcap * d);
+            R.rwin = es->get<unsigned>(R.rcap);
+        };
+        grow_edges(64u * (d + 1));
+        unsigned f0 = 0, f1 = hc[0];
+        long long levels = 0;
+        while (!hc[3] && f1 > f0) {
+            for (;;) {
+                CK(cudaMemsetAsync(R.e_cnt, 0, sizeof(unsigned), st));
+                CK(cudaMemsetAsync(R.rcnt, 0, sizeof(unsigned), st));
+                launch_gen_edges(R, f0, f1, ctx->nsm, st);
+                CK(cudaGetLastError());
+                read();
+                if (hc[2] <= R.e_cap || hc[3]) break;
+                grow_edges(hc[2] + hc[2] / 2);
+            }
+            if (hc[3]) break;
+            launch_gen_walk(R, hc[2], ctx->nsm, st);
+            CK(cudaGetLastError());
+            read();
+            if (hc[3]) break;
+            launch_gen_insert(R, hc[1], st);
+            launch_gen_commit(R, hc[1], st);
+            CK(cudaGetLastError());
+            read();
+            f0 = f1;
+            f1 = std::min(hc[0], R.vcap);
+            ++levels;
+        }
+        es.reset();
+        if (hc[3] & (GS_CAP | GS_HASH)) continue;
+        if (hc[3] & GS_WIDE) {
+            if (W == GMAX) throw HvError(HV_E_CAPACITY, "a degenerate vertex has more than 64 generators");
+            W = GMAX;
+            continue;
+        }
+        if (hc[3] & GS_SUBSETS)
+            throw HvError(HV_E_CAPACITY, "a degenerate vertex has too many generators to enumerate its edges");
+        if (hc[3]) throw HvError(HV_E_INTERNAL, "degenerate walk: singular vertex system or an edge without end");
+        // ---- canonical order and the generator-list CSR
+        const unsigned V = f1;
+        int* order = s.get<int>(std::max(V, 1u));
+        {
+            const size_t tb = gen_sort_temp(V);
+            void* tmp = s.get<char>(tb);
+            gen_sort(R, V, order, tmp, tb, st);
+        }
+        long long* lens = s.get<long long>((size_t)V + 1);
+        unsigned* dmax = s.get<unsigned>(1);
+        CK(cudaMemsetAsync(lens + V, 0, sizeof(long long), st));
+        CK(cudaMemsetAsync(dmax, 0, sizeof(unsigned), st));
+        launch_gen_lens(R, V, order, lens, dmax, st);
+        long long* goff = dalloc<long long>(st, (size_t)V + 1);
+        {
+            const size_t tb = scan_temp((int)V + 1);
+            void* tmp = s.get<char>(tb);
+            exclusive_scan_i64(tmp, tb, lens, goff, (int)V + 1, st);
+        }
+        long long total = 0;
+        unsigned gmax = 0;
+        CK(cudaMemcpyAsync(&total, goff + V, sizeof(long long), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&gmax, dmax, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        int* gsig = dalloc<int>(st, (size_t)std::max(total, 1ll));
+        double* oc = dalloc<double>(st, (size_t)std::max(V, 1u) * d);
+        launch_gen_fill(R, V, order, goff, gsig, oc, st);
+        dfree(st, mesh->osig);
+        dfree(st, mesh->oc);
+        mesh->osig = nullptr;
+        mesh->oc = oc;
+        mesh->g_off = goff;
+        mesh->g_sig = gsig;
+        mesh->g_max = (int)gmax;
+        mesh->V = V;
+        // ---- neighbours sharing a full interface, and each facet's vertices
+        long long* pc = s.get<long long>((size_t)V + 1);
+        long long* poff = s.get<long long>((size_t)V + 1);
+        CK(cudaMemsetAsync(pc + V, 0, sizeof(long long), st));
+        launch_gen_pair_count(n, V, goff, gsig, pc, st);
+        {
+            const size_t tb = scan_temp((int)V + 1);
+            void* tmp = s.get<char>(tb);
+            exclusive_scan_i64(tmp, tb, pc, poff, (int)V + 1, st);
+        }
+        long long np = 0;
+        CK(cudaMemcpyAsync(&np, poff + V, sizeof(long long), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (np > 0x7FFFFFF0ll) throw HvError(HV_E_CAPACITY, "degenerate walk: too many generator pairs");
+        unsigned long long* keys = s.get<unsigned long long>((size_t)std::max(np, 1ll));
+        unsigned long long* keys2 = s.get<unsigned long long>((size_t)std::max(np, 1ll));
+        int* vals = s.get<int>((size_t)std::max(np, 1ll));
+        int* vals2 = dalloc<int>(st, (size_t)std::max(np, 1ll));
+        mesh->g_fvert = vals2;
+        launch_gen_pair_emit(n, V, goff, gsig, poff, keys, vals, st);
+        if (np > 0) {
+            const size_t tb = sort_pairs_u64_i32_temp((int)np);
+            void* tmp = s.get<char>(tb);
+            sort_pairs_u64_i32(tmp, tb, keys, keys2, vals, vals2, (int)np, 64, st);
+        }
+        long long* keep = s.get<long long>((size_t)np + 1);
+        long long* kpos = s.get<long long>((size_t)np + 1);
+        long long* qend = s.get<long long>((size_t)std::max(np, 1ll));
+        CK(cudaMemsetAsync(keep + np, 0, sizeof(long long), st));
+        launch_gen_heads(d, np, keys2, vals2, goff, oc, keep, qend, st);
+        {
+            const size_t tb = scan_temp((int)np + 1);
+            void* tmp = s.get<char>(tb);
+            exclusive_scan_i64(tmp, tb, keep, kpos, (int)np + 1, st);
+        }
+        long long nn = 0;
+        CK(cudaMemcpyAsync(&nn, kpos + np, sizeof(long long), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        mesh->nbr = dalloc<int>(st, (size_t)std::max(nn, 1ll));
+        mesh->g_fcell = dalloc<int>(st, (size_t)std::max(nn, 1ll));
+        mesh->g_fbeg = dalloc<long long>(st, (size_t)std::max(nn, 1ll));
+        mesh->g_fend = dalloc<long long>(st, (size_t)std::max(nn, 1ll));
+        long long* ncnt = s.get<long long>((size_t)n + 1);
+        CK(cudaMemsetAsync(ncnt, 0, sizeof(long long) * (n + 1), st));
+        launch_gen_slots(np, keys2, keep, kpos, qend, mesh->nbr, mesh->g_fcell, mesh->g_fbeg, mesh->g_fend, ncnt, st);
+        mesh->nbr_off = dalloc<long long>(st, (size_t)n + 1);
+        {
+            const size_t tb = scan_temp(n + 1);
+            void* tmp = s.get<char>(tb);
+            exclusive_scan_i64(tmp, tb, ncnt, mesh->nbr_off, n + 1, st);
+        }
+        // ---- cell -> vertex incidence
+        unsigned long long* ik = s.get<unsigned long long>((size_t)std::max(total, 1ll));
+        unsigned long long* ik2 = s.get<unsigned long long>((size_t)std::max(total, 1ll));
+        long long* icnt = s.get<long long>((size_t)n + 1);
+        CK(cudaMemsetAsync(icnt, 0, sizeof(long long) * (n + 1), st));
+        launch_gen_inc_emit(n, V, goff, gsig, ik, icnt, st);
+        if (total > 0) {
+            const size_t tb = sort_keys_u64_temp(total);
+            void* tmp = s.get<char>(tb);
+            sort_keys_u64(tmp, tb, ik, ik2, total, st);
+        }
+        mesh->inc_off = dalloc<long long>(st, (size_t)n + 1);
+        {
+            const size_t tb = scan_temp(n + 1);
+            void* tmp = s.get<char>(tb);
+            exclusive_scan_i64(tmp, tb, icnt, mesh->inc_off, n + 1, st);
+        }
+        long long ninc = 0;
+        CK(cudaMemcpyAsync(&ninc, mesh->inc_off + n, sizeof(long long), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        mesh->inc = dalloc<int>(st, (size_t)std::max(ninc, 1ll));
+        launch_inc_split((unsigned long long)ninc, ik2, mesh->inc, st);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(st));
+        mesh->nnbr = nn;
+        mesh->st.vertices = V;
+        mesh->st.levels += levels;
+        return;
+    }
+}
+
 void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_device, const double* h_src) {
     using namespace hv;
     const int d = mesh->d, n = mesh->n;
@@ -342,7 +561,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     M.cnt = dcnt;
     kt.run(F_OTHER, 1, [&] { launch_bvh(M, blo, bhi, flags, st); });
     // ---- candidate lists
-    const bool fast = mesh->prm.method == HV_METHOD_FAST;
+    const bool fast = mesh->prm.method != HV_METHOD_PLAIN;  // the generic walk starts from the fast search
     int K = mesh->prm.knn > 0 ? mesh->prm.knn : default_knn(d);
     K = std::min(K, std::max(n - 1, 0));
     K = std::min(K, 480);
@@ -709,8 +928,14 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     S.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     // A tie that double-double cannot break means generators in degenerate
     // position (more than d+1 on one empty sphere, e.g. lattice points): the
-    // reference stores such a vertex with all of them; this search broke the tie
-    // by index, so the mesh is not the Voronoi diagram -- refuse it.
+    // reference stores such a vertex with all of them, and so does the generic
+    // walk of a box or plane-domain build.  This search broke the tie by index,
+    // so a periodic image set, a shard or a refinement refuses the mesh.
+    if (mesh->prm.method == HV_METHOD_GENERIC || (S.degenerate > 0 && mesh->allow_generic)) {
+        generic_build(ctx, mesh, M);
+        S.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return;
+    }
     if (S.degenerate > 0)
         throw HvError(HV_E_DEGENERATE, "generators in degenerate position (" + std::to_string(S.degenerate) +
                                            " exact ties, e.g. more than d+1 points on one empty sphere); "
@@ -806,6 +1031,7 @@ struct DomainSpec {
     const double* base = nullptr;
     const double* normal = nullptr;
     const int16_t* bc = nullptr;
+    bool generic_ok = true;  // co-spherical generators: walk vertices of any size (not for periodic images)
 };
 
 int build_entry(hv_ctx* ctx, int d, int64_t n, const double* src, bool on_device, const DomainSpec& dom,
@@ -853,9 +1079,15 @@ int build_entry(hv_ctx* ctx, int d, int64_t n, const double* src, bool on_device
             if (m->prm.rays_per_warp == 0) m->prm.rays_per_warp = it->second.rays_per_warp;
         }
     }
-    if (m->prm.method != HV_METHOD_FAST && m->prm.method != HV_METHOD_PLAIN) {
+    if (m->prm.method != HV_METHOD_FAST && m->prm.method != HV_METHOD_PLAIN && m->prm.method != HV_METHOD_GENERIC) {
         delete m;
         ctx->err = "unknown method";
+        return HV_E_INVALID_ARG;
+    }
+    m->allow_generic = dom.generic_ok;
+    if (m->prm.method == HV_METHOD_GENERIC && !dom.generic_ok) {
+        delete m;
+        ctx->err = "the generic walk takes box and plane-domain meshes";
         return HV_E_INVALID_ARG;
     }
     try {
@@ -927,6 +1159,7 @@ int refine_entry(hv_mesh* old, int64_t k, const double* src, bool on_device, hv_
         return HV_E_INVALID_ARG;
     }
     if (old->prm.method != HV_METHOD_FAST) { ctx->err = "refinement uses the fast method"; return HV_E_INVALID_ARG; }
+    if (old->g_max) { ctx->err = "refinement needs vertices of d+1 generators"; return HV_E_DEGENERATE; }
     const int d = old->d, n_old = old->n;
     if ((int64_t)n_old + k > (1ll << 30)) { ctx->err = "point count out of range"; return HV_E_INVALID_ARG; }
     const int n = n_old + (int)k;
@@ -1088,6 +1321,7 @@ int periodic_entry(hv_ctx* ctx, int d, int64_t n, const double* src, bool on_dev
             for (int k = 0; k < d; ++k) { elo[k] = lo[k] - B.delta[k]; ehi[k] = hi[k] + B.delta[k]; }
             DomainSpec dom;
             dom.lo = elo; dom.hi = ehi;
+            dom.generic_ok = false;
             hv_mesh* ext = nullptr;
             int r = build_entry(ctx, d, n_ext, ext_pts, true, dom, &m->prm, &ext);
             if (r != HV_OK) throw HvError(r, ctx->err);
@@ -1326,6 +1560,10 @@ int hv_mesh_counts(hv_mesh* m, int64_t* nverts, int64_t* nnbr_total) {
 
 int hv_mesh_vertices(hv_mesh* m, int64_t* sig, double* r) {
     if (!m || (m->V && (!sig || !r))) return HV_E_INVALID_ARG;
+    if (m->g_max > m->d + 1) {
+        m->ctx->err = "the mesh has vertices with more than d+1 generators: read them with hv_mesh_vertices_csr";
+        return HV_E_DEGENERATE;
+    }
     try {
         CK(cudaSetDevice(m->ctx->device));
         cudaStream_t st = m->ctx->stream;
@@ -1333,9 +1571,55 @@ int hv_mesh_vertices(hv_mesh* m, int64_t* sig, double* r) {
             Scratch s(st);
             const size_t ns = (size_t)m->V * (m->d + 1);
             int64_t* dsig = s.get<int64_t>(ns);
-            hv::launch_out_vertices(m->d, m->V, m->osig, dsig, st);
+            if (m->g_max) hv::launch_out_nbr((long long)ns, m->g_sig, dsig, st);  // every list has d+1 items
+            else hv::launch_out_vertices(m->d, m->V, m->osig, dsig, st);
             CK(cudaMemcpyAsync(sig, dsig, ns * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
             CK(cudaMemcpyAsync(r, m->oc, (size_t)m->V * m->d * sizeof(double), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+        }
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
+int hv_mesh_signature_total(hv_mesh* m, int64_t* total, int* max_len) {
+    if (!m || !total) return HV_E_INVALID_ARG;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        long long t = (long long)m->V * (m->d + 1);
+        if (m->g_max && m->V) {
+            CK(cudaMemcpyAsync(&t, m->g_off + m->V, sizeof(long long), cudaMemcpyDeviceToHost, m->ctx->stream));
+            CK(cudaStreamSynchronize(m->ctx->stream));
+        }
+        *total = t;
+        if (max_len) *max_len = m->g_max ? m->g_max : (m->V ? m->d + 1 : 0);
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
+int hv_mesh_vertices_csr(hv_mesh* m, int64_t* offs, int64_t* sig, double* r) {
+    if (!m || !offs || (m->V && (!sig || !r))) return HV_E_INVALID_ARG;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        cudaStream_t st = m->ctx->stream;
+        const unsigned V = m->V;
+        if (m->g_max) {
+            CK(cudaMemcpyAsync(offs, m->g_off, sizeof(int64_t) * (V + 1), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+        } else {
+            for (unsigned v = 0; v <= V; ++v) offs[v] = (int64_t)v * (m->d + 1);
+        }
+        const long long total = offs[V];
+        if (V) {
+            Scratch s(st);
+            int64_t* dsig = s.get<int64_t>((size_t)total);
+            if (m->g_max) hv::launch_out_nbr(total, m->g_sig, dsig, st);
+            else hv::launch_out_vertices(m->d, V, m->osig, dsig, st);
+            CK(cudaMemcpyAsync(sig, dsig, sizeof(int64_t) * total, cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(r, m->oc, sizeof(double) * V * m->d, cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
         }
     } catch (const HvError& e) {
@@ -1411,6 +1695,39 @@ int periodic_integrate(hv_mesh* m, double* vol, double* area, bool dev_out, F&& 
     return HV_OK;
 }
 
+// VI_POLYGON of a mesh with vertices of more than d+1 generators: the area of
+// every facet by the pulling decomposition over its faces (hv_degen.cu).
+int generic_polygon(hv_mesh* m, double* vol, double* area, bool dev_out) {
+    if (m->nnbr > 0 && !area) return HV_E_INVALID_ARG;
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        cudaStream_t st = m->ctx->stream;
+        Scratch s(st);
+        double* dvol = dev_out ? vol : s.get<double>((size_t)std::max(m->n, 1));
+        double* darea = dev_out ? area : s.get<double>((size_t)std::max(m->nnbr, 1ll));
+        unsigned* dst = s.get<unsigned>(1);
+        CK(cudaMemsetAsync(dst, 0, sizeof(unsigned), st));
+        hv::GenPoly P{};
+        P.d = m->d; P.n = m->n; P.planes = m->d_planes; P.pts = m->d_in;
+        P.off = m->g_off; P.sig = m->g_sig; P.oc = m->oc;
+        P.nbr_off = m->nbr_off; P.nbr = m->nbr; P.fcell = m->g_fcell; P.fbeg = m->g_fbeg; P.fend = m->g_fend;
+        P.fvert = m->g_fvert; P.nslots = m->nnbr; P.status = dst;
+        hv::launch_gen_polygon(P, darea, dvol, m->ctx->nsm, st);
+        CK(cudaGetLastError());
+        unsigned hs = 0;
+        CK(cudaMemcpyAsync(&hs, dst, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        if (!dev_out) {
+            if (m->n) CK(cudaMemcpyAsync(vol, dvol, sizeof(double) * m->n, cudaMemcpyDeviceToHost, st));
+            if (m->nnbr > 0) CK(cudaMemcpyAsync(area, darea, sizeof(double) * m->nnbr, cudaMemcpyDeviceToHost, st));
+        }
+        CK(cudaStreamSynchronize(st));
+        if (hs) throw HvError(HV_E_CAPACITY, "a facet has more than 64 vertices or faces (degenerate polygon)");
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
 int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out) {
     if (m && m->own0 >= 0) {  // a shard holds only its own vertices
         m->ctx->err = "integrate the merged mesh, not a shard";
@@ -1423,6 +1740,7 @@ int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out) {
             return polygon_impl(e, ev, ea, true);
         });
     }
+    if (m->g_max) return generic_polygon(m, vol, area, dev_out);
     try {
         CK(cudaSetDevice(m->ctx->device));
         ensure_neighbors(m);
@@ -1625,6 +1943,10 @@ void ensure_quad(hv_mesh* m, bool weights) {
 
 int quad_check(hv_mesh* m) {
     if (!m) return HV_E_INVALID_ARG;
+    if (m->g_max) {
+        m->ctx->err = "the integrand quadrature needs vertices of d+1 generators";
+        return HV_E_DEGENERATE;
+    }
     if (m->ext || m->own0 >= 0) {
         m->ctx->err = "the integrand quadrature takes box and plane-domain meshes";
         return HV_E_INVALID_ARG;
@@ -1907,7 +2229,7 @@ int hv_mesh_device_views(hv_mesh* m, hv_device_views* out) {
         out->nverts = m->V;
         out->nnbr = m->nnbr;
         out->ncell_vertices = ninc;
-        out->sig = m->osig;
+        out->sig = m->g_max ? (m->g_max == m->d + 1 ? m->g_sig : nullptr) : m->osig;
         out->r = m->oc;
         out->nbr_off = (const int64_t*)m->nbr_off;
         out->nbr = m->nbr;
@@ -1950,6 +2272,12 @@ int hv_mesh_free(hv_mesh* m) {
     dfree(st, m->q_a);
     dfree(st, m->q_c);
     dfree(st, m->q_af);
+    dfree(st, m->g_off);
+    dfree(st, m->g_sig);
+    dfree(st, m->g_fcell);
+    dfree(st, m->g_fbeg);
+    dfree(st, m->g_fend);
+    dfree(st, m->g_fvert);
     cudaStreamSynchronize(st);
     if (m->ext) hv_mesh_free(m->ext);
     delete m;

@@ -3,7 +3,7 @@
 The compute path is libhvgpu (C ABI, include/hvgpu.h); this package is the
 Python host side that mirrors the reference's VoronoiGeometry / VoronoiData API.
 """
-from ._lib import (HV_METHOD_FAST, HV_METHOD_PLAIN, Context, HVError, Mesh, default_context, load,  # noqa: F401
+from ._lib import (HV_METHOD_FAST, HV_METHOD_GENERIC, HV_METHOD_PLAIN, Context, HVError, Mesh, default_context, load,  # noqa: F401
                    make_params)
 from .geometry import (RCGPU, RCCombined, RCGPUPlain, RCNonGeneral, RCNonGeneralCutoff, RCNonGeneralFast,  # noqa: F401
                        RCNonGeneralHP, RCNonGeneralSkip, RCOriginal, RCOriginalHP, RCOriginalSafety, RCStandard,

@@ -24,6 +24,7 @@ HV_E_CUDA = -6
 HV_E_INTERNAL = -7
 HV_METHOD_FAST = 0
 HV_METHOD_PLAIN = 1
+HV_METHOD_GENERIC = 2  # vertices of any number of generators (lattices)
 
 _ERRNAMES = {
     HV_E_INVALID_ARG: "HV_E_INVALID_ARG", HV_E_OOM: "HV_E_OOM", HV_E_CAPACITY: "HV_E_CAPACITY",
@@ -121,6 +122,9 @@ def load(path: str | None = None):
         L.hv_mesh_counts.argtypes = [P, ip, ip]; L.hv_mesh_counts.restype = I
         L.hv_autotune.argtypes = [P, I, I64, P, dp, dp, ctypes.POINTER(Params)]; L.hv_autotune.restype = I
         L.hv_mesh_vertices.argtypes = [P, ip, dp]; L.hv_mesh_vertices.restype = I
+        L.hv_mesh_signature_total.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int)]
+        L.hv_mesh_signature_total.restype = I
+        L.hv_mesh_vertices_csr.argtypes = [P, ip, ip, dp]; L.hv_mesh_vertices_csr.restype = I
         L.hv_mesh_neighbors.argtypes = [P, ip, ip]; L.hv_mesh_neighbors.restype = I
         L.hv_integrate_polygon.argtypes = [P, dp, dp]; L.hv_integrate_polygon.restype = I
         L.hv_integrate_heuristic_mc.argtypes = [P, I, U64, dp, dp]; L.hv_integrate_heuristic_mc.restype = I
@@ -364,6 +368,29 @@ class Mesh:
         r = np.zeros((V, self.d), dtype=np.float64)
         self.ctx.check(load().hv_mesh_vertices(self._h, iptr(sig), dptr(r)), "hv_mesh_vertices")
         return sig, r
+
+    def vertices_csr(self):
+        """(offs (V+1), sig (1-based, ascending per vertex, back to back),
+        r (V, d)): vertices of any number of generators -- a lattice puts 2^d
+        points on one sphere -- in lexicographic order of their signatures."""
+        V, _ = self.counts()
+        tot = ctypes.c_int64()
+        mx = ctypes.c_int()
+        self.ctx.check(load().hv_mesh_signature_total(self._h, ctypes.byref(tot), ctypes.byref(mx)),
+                       "hv_mesh_signature_total")
+        offs = np.zeros(V + 1, dtype=np.int64)
+        sig = np.zeros(max(tot.value, 1), dtype=np.int64)
+        r = np.zeros((V, self.d), dtype=np.float64)
+        self.ctx.check(load().hv_mesh_vertices_csr(self._h, iptr(offs), iptr(sig), dptr(r)), "hv_mesh_vertices_csr")
+        return offs, sig[:tot.value], r
+
+    def max_signature(self) -> int:
+        """Longest vertex signature (d+1 unless generators are co-spherical)."""
+        tot = ctypes.c_int64()
+        mx = ctypes.c_int()
+        self.ctx.check(load().hv_mesh_signature_total(self._h, ctypes.byref(tot), ctypes.byref(mx)),
+                       "hv_mesh_signature_total")
+        return mx.value
 
     def neighbors(self):
         _, E = self.counts(neighbors=True)

@@ -251,9 +251,14 @@ class VoronoiGeometry:
         xs = np.asarray(xs, dtype=np.float64).reshape(-1, self.dimension)
         pts = np.ascontiguousarray(np.vstack([self.nodes, xs]))
         b = self.boundary
+        mesh = None
         if not (b.is_box and b.periodic) and self.method.code == _lib.HV_METHOD_FAST:
-            mesh = self.mesh.refined(xs)
-        else:
+            try:
+                mesh = self.mesh.refined(xs)
+            except _lib.HVError as e:  # co-spherical generators: a full build walks them
+                if e.code != _lib.HV_E_DEGENERATE:
+                    raise
+        if mesh is None:
             mesh = self._build(pts)
         self.mesh.free()
         self.mesh, self.nodes = mesh, pts
@@ -358,7 +363,12 @@ class VoronoiData:
         self.geometry = geo
         self.nodes = geo.nodes
         self.boundary = geo.boundary
-        self.vertex_sigs, self.vertex_coords = geo.mesh.vertices()
+        voff, vsig, self.vertex_coords = geo.mesh.vertices_csr()
+        width = np.diff(voff)
+        if width.size == 0 or np.all(width == geo.mesh.d + 1):
+            self.vertex_sigs = vsig.reshape(-1, geo.mesh.d + 1)
+        else:  # co-spherical generators (a lattice): every generator on the vertex's sphere
+            self.vertex_sigs = [vsig[voff[v]:voff[v + 1]] for v in range(width.size)]
         offs, nbr = geo.mesh.neighbors()
         self.neighbor_offsets = offs
         self.neighbor_flat = nbr

@@ -57,6 +57,11 @@ extern "C" {
  * (src/raycast-types.jl:244-285). */
 #define HV_METHOD_FAST 0  /* batched split-precision raycast (FP32 filter, FP64 verify) */
 #define HV_METHOD_PLAIN 1 /* one ray per thread, FP64, exact tree search */
+/* vertices of any number of generators (lattices): the fast search, then a
+ * walk of the vertex graph in which every vertex keeps all generators on its
+ * sphere.  A FAST build switches to it by itself when it meets co-spherical
+ * generators (box and plane domains). */
+#define HV_METHOD_GENERIC 2
 
 typedef struct hv_ctx hv_ctx;
 typedef struct hv_mesh hv_mesh;
@@ -64,7 +69,7 @@ typedef struct hv_mesh hv_mesh;
 /* Search settings (the GPU part of the reference's RaycastParameter,
  * src/raycast-types.jl:312-349).  Zero means "choose automatically". */
 typedef struct {
-    int method;           /* HV_METHOD_FAST or HV_METHOD_PLAIN */
+    int method;           /* HV_METHOD_FAST, HV_METHOD_PLAIN or HV_METHOD_GENERIC */
     int knn;              /* candidate-list length per generator */
     int leaf_size;        /* points per tree leaf */
     int rays_per_warp;    /* vertices expanded per warp in the fast kernel (1 or 2) */
@@ -157,8 +162,18 @@ int hv_autotune(hv_ctx* ctx, int d, int64_t n, const double* pts, const double* 
 /* Sizes of the caller's buffers: vertices, and the total neighbour count. */
 int hv_mesh_counts(hv_mesh* mesh, int64_t* nverts, int64_t* nnbr_total);
 /* Vertex records sorted lexicographically by signature: sig is (d+1) x V
- * (1-based, sorted), r is d x V. */
+ * (1-based, sorted), r is d x V.  HV_E_DEGENERATE if a vertex has more than
+ * d+1 generators (read those with hv_mesh_vertices_csr). */
 int hv_mesh_vertices(hv_mesh* mesh, int64_t* sig, double* r);
+/* Vertices of any number of generators -- the reference's vertex database
+ * holds every generator on a vertex's sphere (push!(mesh, sig => r),
+ * src/abstractmesh.jl:111-127; lattices put 2^d points on one sphere).
+ * hv_mesh_signature_total sizes the buffers: the summed signature length and
+ * the longest one.  hv_mesh_vertices_csr writes offs (V+1, 0-based), sig (the
+ * 1-based ascending signatures back to back) and r (d x V), in lexicographic
+ * order of the signatures (a shorter signature before its extensions). */
+int hv_mesh_signature_total(hv_mesh* mesh, int64_t* total, int* max_len);
+int hv_mesh_vertices_csr(hv_mesh* mesh, int64_t* offs, int64_t* sig, double* r);
 /* Neighbour CSR: offs[n+1] (0-based offsets), nbr (1-based, sorted per cell,
  * planes as n+p). */
 int hv_mesh_neighbors(hv_mesh* mesh, int64_t* offs, int64_t* nbr);
@@ -262,7 +277,7 @@ int hv_mesh_cell_vertices(hv_mesh* m, int64_t* offs, int64_t* vtx);
 typedef struct {
     int d;
     int64_t n, nverts, nnbr, ncell_vertices;
-    const int32_t* sig;       /* nverts x (d+1) */
+    const int32_t* sig;       /* nverts x (d+1); NULL if a vertex has more than d+1 generators */
     const double* r;          /* nverts x d */
     const int64_t* nbr_off;   /* n+1 */
     const int32_t* nbr;       /* nnbr, sorted per cell, planes last */

@@ -64,6 +64,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <unordered_map>
@@ -1884,6 +1885,442 @@ static int64_t verify_vertices(const Problem& P, const double* pts, int64_t nv, 
         if (!ok) bad++;
     }
     return bad;
+}
+
+}  // extern "C"
+
+/* ---------------- vertices with more than d+1 generators ----------------
+ * The reference stores a vertex with every generator on its sphere: the tie
+ * set of the ray's inrange search (NearestNeighborModified/kd_tree.jl:683-791,
+ * src/raycast.jl:794-970) joins the edge's generators, and such a vertex is
+ * left along the edges FastEdgeIterator finds (src/edgeiterate.jl:82-110).
+ * This restatement walks the vertex graph of a box from its corner lo in
+ * binary128.  A vertex is (G, c): G every generator with c on its sphere
+ * (points) or on its hyperplane (planes).  With h(x) = (x, 1) for a point
+ * and h(p) = (n_p, 0) for a plane, an edge is a direction (u, b) with
+ * (u, b).h(g) = 0 for the generators F that stay equidistant (points) or
+ * stay on their plane, and < 0 for the rest of G; F spans rank d (one free
+ * direction), and the d-subset of G that generates it is F's first basis in
+ * id order (every edge is found once).  Along the edge, the next vertex is at
+ * the smallest crossing parameter t over the generators outside G; every
+ * generator within a relative 1e-24 of it joins F.
+ * Neighbours follow neighbors_of_cell (src/neighbors.jl:219-258): cells i, j
+ * of a common vertex that share a full interface, i.e. a vertex with exactly
+ * d+1 generators or vertices of affine rank d-1.  Interface areas and volumes
+ * come from the pulling decomposition of each facet over its faces (the face
+ * cut by generator l is the facet's vertices that carry l). */
+namespace {
+
+constexpr double GEN_TOL = 1e-24;
+
+void hom_vec(const Problem& P, int it, qreal* h) {
+    const int d = P.d;
+    if (!P.is_plane(it)) {
+        const double* x = P.x(it);
+        for (int k = 0; k < d; ++k) h[k] = (qreal)x[k];
+        h[d] = 1;
+    } else {
+        for (int k = 0; k < d; ++k) h[k] = (qreal)P.pn[it - P.n][k];
+        h[d] = 0;
+    }
+}
+
+// Row echelon rank of m vectors of length w (partial pivoting), relative tolerance.
+int echelon_rank(std::vector<std::array<qreal, MAXD + 1>> rows, int w, qreal tol) {
+    const int m = (int)rows.size();
+    qreal scale = 0;
+    for (auto& r : rows) for (int k = 0; k < w; ++k) scale = std::max(scale, qabs(r[k]));
+    if (scale == 0) return 0;
+    int rank = 0;
+    for (int c = 0; c < w && rank < m; ++c) {
+        int p = rank;
+        for (int r = rank + 1; r < m; ++r) if (qabs(rows[r][c]) > qabs(rows[p][c])) p = r;
+        if (qabs(rows[p][c]) <= tol * scale) continue;
+        std::swap(rows[p], rows[rank]);
+        for (int r = rank + 1; r < m; ++r) {
+            const qreal f = rows[r][c] / rows[rank][c];
+            for (int k = c; k < w; ++k) rows[r][k] -= f * rows[rank][k];
+        }
+        ++rank;
+    }
+    return rank;
+}
+
+// Null vector of the d x (d+1) matrix H (rank d); false if the rank is lower.
+bool null_vector(int d, qreal H[MAXD][MAXD + 1], qreal* z) {
+    int col_of[MAXD];
+    qreal A[MAXD][MAXD + 1];
+    for (int r = 0; r < d; ++r) for (int k = 0; k <= d; ++k) A[r][k] = H[r][k];
+    qreal scale = 0;
+    for (int r = 0; r < d; ++r) for (int k = 0; k <= d; ++k) scale = std::max(scale, qabs(A[r][k]));
+    int rank = 0;
+    bool pivot_col[MAXD + 1] = {};
+    for (int c = 0; c <= d && rank < d; ++c) {
+        int p = rank;
+        for (int r = rank + 1; r < d; ++r) if (qabs(A[r][c]) > qabs(A[p][c])) p = r;
+        if (qabs(A[p][c]) <= (qreal)GEN_TOL * scale) continue;
+        for (int k = 0; k <= d; ++k) std::swap(A[p][k], A[rank][k]);
+        for (int r = 0; r < d; ++r) {
+            if (r == rank) continue;
+            const qreal f = A[r][c] / A[rank][c];
+            for (int k = 0; k <= d; ++k) A[r][k] -= f * A[rank][k];
+        }
+        col_of[rank] = c;
+        pivot_col[c] = true;
+        ++rank;
+    }
+    if (rank < d) return false;
+    int fc = 0;
+    while (pivot_col[fc]) ++fc;
+    for (int k = 0; k <= d; ++k) z[k] = 0;
+    z[fc] = 1;
+    for (int r = 0; r < d; ++r) z[col_of[r]] = -A[r][fc] / A[r][col_of[r]];
+    return true;
+}
+
+// Centre of the vertex with generators G: d independent rows of
+// 2 (x_g - x_a) . c = |x_g|^2 - |x_a|^2 (points) and n_p . c = off_p (planes).
+bool gen_centre(const Problem& P, const std::vector<int>& G, qreal* c) {
+    const int d = P.d;
+    int a = -1;
+    for (int g : G) if (!P.is_plane(g)) { a = g; break; }
+    if (a < 0) return false;
+    std::vector<std::array<qreal, MAXD + 1>> rows;
+    qreal A[MAXD][MAXD], rhs[MAXD];
+    int nr = 0;
+    const double* xa = P.x(a);
+    qreal na = 0;
+    for (int k = 0; k < d; ++k) na += (qreal)xa[k] * (qreal)xa[k];
+    for (int g : G) {
+        if (g == a || nr == d) continue;
+        std::array<qreal, MAXD + 1> row{};
+        qreal r;
+        if (!P.is_plane(g)) {
+            const double* xg = P.x(g);
+            qreal ng = 0;
+            for (int k = 0; k < d; ++k) { row[k] = 2 * ((qreal)xg[k] - (qreal)xa[k]); ng += (qreal)xg[k] * (qreal)xg[k]; }
+            r = ng - na;
+        } else {
+            for (int k = 0; k < d; ++k) row[k] = (qreal)P.pn[g - P.n][k];
+            r = (qreal)P.poff[g - P.n];
+        }
+        rows.push_back(row);
+        if (echelon_rank(rows, d, (qreal)GEN_TOL) < (int)rows.size()) { rows.pop_back(); continue; }
+        for (int k = 0; k < d; ++k) A[nr][k] = row[k];
+        rhs[nr++] = r;
+    }
+    if (nr < d) return false;
+    int piv[MAXD];
+    if (!lu_factor<qreal>(d, A, piv)) return false;
+    lu_solve<qreal>(d, A, piv, rhs);
+    for (int k = 0; k < d; ++k) c[k] = rhs[k];
+    return true;
+}
+
+struct GenEdge { std::vector<int> F; qreal u[MAXD]; };
+
+// The edges of vertex (G, c); false if G is too large to enumerate.
+bool gen_edges(const Problem& P, const std::vector<int>& G, std::vector<GenEdge>& out) {
+    const int d = P.d, m = (int)G.size();
+    out.clear();
+    double comb = 1;
+    for (int q = 0; q < d; ++q) comb = comb * (m - q) / (q + 1);
+    if (comb > 4e6) return false;
+    std::vector<std::array<qreal, MAXD + 1>> h(m);
+    for (int a = 0; a < m; ++a) hom_vec(P, G[a], h[a].data());
+    int idx[MAXD];
+    for (int q = 0; q < d; ++q) idx[q] = q;
+    for (;;) {
+        qreal H[MAXD][MAXD + 1], z[MAXD + 1];
+        for (int r = 0; r < d; ++r) for (int k = 0; k <= d; ++k) H[r][k] = h[idx[r]][k];
+        if (null_vector(d, H, z)) {
+            qreal zn = 0;
+            for (int k = 0; k <= d; ++k) zn = std::max(zn, qabs(z[k]));
+            int pos = 0, neg = 0;
+            std::vector<int> F;
+            for (int a = 0; a < m; ++a) {
+                qreal s = 0, hn = 0;
+                for (int k = 0; k <= d; ++k) { s += z[k] * h[a][k]; hn = std::max(hn, qabs(h[a][k])); }
+                if (qabs(s) <= (qreal)GEN_TOL * 16 * zn * hn) F.push_back(a);
+                else if (s > 0) ++pos;
+                else ++neg;
+            }
+            bool ok = !(pos > 0 && neg > 0) && (pos + neg > 0);
+            bool real = false;
+            for (int a : F) real |= !P.is_plane(G[a]);
+            ok = ok && real;
+            if (ok) {  // D must be F's first basis in id order
+                std::vector<std::array<qreal, MAXD + 1>> rows;
+                std::vector<int> basis;
+                for (int a : F) {
+                    rows.push_back(h[a]);
+                    if (echelon_rank(rows, d + 1, (qreal)GEN_TOL) < (int)rows.size()) { rows.pop_back(); continue; }
+                    basis.push_back(a);
+                    if ((int)basis.size() == d) break;
+                }
+                bool same = (int)basis.size() == d;
+                for (int q = 0; q < d && same; ++q) same = basis[q] == idx[q];
+                if (same) {
+                    GenEdge e;
+                    const qreal sg = pos > 0 ? -1 : 1;
+                    qreal un = 0;
+                    for (int k = 0; k < d; ++k) { e.u[k] = sg * z[k]; un += e.u[k] * e.u[k]; }
+                    un = (qreal)std::sqrt((double)un);
+                    for (int k = 0; k < d; ++k) e.u[k] /= un;
+                    for (int a : F) e.F.push_back(G[a]);
+                    out.push_back(e);
+                }
+            }
+        }
+        int q = d - 1;
+        while (q >= 0 && idx[q] == m - d + q) --q;
+        if (q < 0) break;
+        ++idx[q];
+        for (int r = q + 1; r < d; ++r) idx[r] = idx[r - 1] + 1;
+    }
+    return true;
+}
+
+// The vertex at the end of edge e of vertex (G, c); false if nothing is hit.
+bool gen_walk(const Problem& P, const std::vector<int>& G, const qreal* c, const GenEdge& e, std::vector<int>& G2) {
+    const int d = P.d;
+    int a = -1;
+    for (int g : e.F) if (!P.is_plane(g)) { a = g; break; }
+    const double* xa = P.x(a);
+    qreal ca = 0;
+    for (int k = 0; k < d; ++k) { const qreal w = c[k] - (qreal)xa[k]; ca += w * w; }
+    std::vector<std::pair<qreal, int>> ts;
+    auto in_G = [&](int it) { return std::binary_search(G.begin(), G.end(), it); };
+    for (int j = 0; j < P.n; ++j) {
+        if (in_G(j)) continue;
+        const double* xj = P.x(j);
+        qreal den = 0, cj = 0;
+        for (int k = 0; k < d; ++k) {
+            den += 2 * e.u[k] * ((qreal)xj[k] - (qreal)xa[k]);
+            const qreal w = c[k] - (qreal)xj[k];
+            cj += w * w;
+        }
+        if (!(den > 0)) continue;
+        ts.push_back({(cj - ca) / den, j});
+    }
+    for (int p = 0; p < P.np; ++p) {
+        const int it = P.n + p;
+        if (in_G(it)) continue;
+        qreal un = 0, nc = 0;
+        for (int k = 0; k < d; ++k) { un += (qreal)P.pn[p][k] * e.u[k]; nc += (qreal)P.pn[p][k] * c[k]; }
+        if (!(un > 0)) continue;
+        ts.push_back({((qreal)P.poff[p] - nc) / un, it});
+    }
+    if (ts.empty()) return false;
+    qreal tmin = ts[0].first;
+    for (auto& x : ts) tmin = std::min(tmin, x.first);
+    qreal scale = 0;
+    for (int k = 0; k < d; ++k) scale = std::max(scale, qabs(c[k]) + 1);
+    G2 = e.F;
+    for (auto& x : ts) if (x.first <= tmin + (qreal)GEN_TOL * (qabs(tmin) + scale)) G2.push_back(x.second);
+    std::sort(G2.begin(), G2.end());
+    return true;
+}
+
+// Modified Gram-Schmidt basis of the differences p - p0; returns the rank.
+int mgs_basis(int d, const std::vector<const qreal*>& pts, qreal Q[MAXD][MAXD], qreal tol) {
+    int r = 0;
+    for (size_t a = 1; a < pts.size() && r < d; ++a) {
+        qreal v[MAXD];
+        qreal n0 = 0;
+        for (int k = 0; k < d; ++k) { v[k] = pts[a][k] - pts[0][k]; n0 = std::max(n0, qabs(v[k])); }
+        for (int b = 0; b < r; ++b) {
+            qreal s = 0;
+            for (int k = 0; k < d; ++k) s += v[k] * Q[b][k];
+            for (int k = 0; k < d; ++k) v[k] -= s * Q[b][k];
+        }
+        qreal nn = 0;
+        for (int k = 0; k < d; ++k) nn += v[k] * v[k];
+        const qreal len = (qreal)std::sqrt((double)nn);
+        if (!(len > tol * (n0 + 1e-300))) continue;
+        for (int k = 0; k < d; ++k) Q[r][k] = v[k] / len;
+        ++r;
+    }
+    return r;
+}
+
+struct GenMesh {
+    const Problem& P;
+    std::vector<std::vector<int>> G;  // sorted generators per vertex
+    std::vector<std::array<qreal, MAXD>> C;
+    qreal face_volume(const std::vector<int>& S, const std::vector<int>& verts, int dim) const {
+        const int d = P.d;
+        if (dim == 0) return 1;
+        if (dim == 1) {
+            qreal best = 0;
+            for (size_t a = 0; a < verts.size(); ++a)
+                for (size_t b = a + 1; b < verts.size(); ++b) {
+                    qreal s = 0;
+                    for (int k = 0; k < d; ++k) { const qreal w = C[verts[a]][k] - C[verts[b]][k]; s += w * w; }
+                    best = std::max(best, s);
+                }
+            return (qreal)std::sqrt((double)best);
+        }
+        const int v0 = verts[0];
+        std::vector<int> items;
+        for (int v : verts) for (int g : G[v]) if (!std::binary_search(S.begin(), S.end(), g)) items.push_back(g);
+        std::sort(items.begin(), items.end());
+        items.erase(std::unique(items.begin(), items.end()), items.end());
+        std::vector<std::vector<int>> seen;
+        qreal total = 0;
+        for (int l : items) {
+            std::vector<int> sub;
+            for (int v : verts) if (std::binary_search(G[v].begin(), G[v].end(), l)) sub.push_back(v);
+            if ((int)sub.size() < dim || std::find(sub.begin(), sub.end(), v0) != sub.end()) continue;
+            if (std::find(seen.begin(), seen.end(), sub) != seen.end()) continue;
+            seen.push_back(sub);
+            std::vector<const qreal*> pp;
+            for (int v : sub) pp.push_back(C[v].data());
+            qreal Q[MAXD][MAXD];
+            if (mgs_basis(d, pp, Q, (qreal)1e-10) != dim - 1) continue;
+            qreal w[MAXD];
+            for (int k = 0; k < d; ++k) w[k] = C[v0][k] - C[sub[0]][k];
+            for (int b = 0; b < dim - 1; ++b) {
+                qreal s = 0;
+                for (int k = 0; k < d; ++k) s += w[k] * Q[b][k];
+                for (int k = 0; k < d; ++k) w[k] -= s * Q[b][k];
+            }
+            qreal hh = 0;
+            for (int k = 0; k < d; ++k) hh += w[k] * w[k];
+            std::vector<int> S2 = S;
+            S2.push_back(l);
+            std::sort(S2.begin(), S2.end());
+            total += (qreal)std::sqrt((double)hh) * face_volume(S2, sub, dim - 1) / dim;
+        }
+        return total;
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+int hvo_build_generic(int d, int64_t n, const double* pts, const double* lo, const double* hi, int integrate,
+                      hvo_mesh** out) {
+    if (d < 2 || d > MAXD || n < 1 || n > (1 << 20) || !out || !pts || !lo || !hi) {
+        set_err("invalid argument");
+        return -1;
+    }
+    hvo_mesh* M = new hvo_mesh();
+    Problem& P = M->P;
+    P.d = d; P.n = (int)n;
+    set_box_planes(P, lo, hi);
+    P.X.assign(pts, pts + (size_t)n * d);
+    for (int64_t i = 0; i < n; ++i)
+        if (!inside_planes(P, pts + i * d)) { set_err("point outside the open domain"); delete M; return -2; }
+    GenMesh GM{P, {}, {}};
+    // the corner lo: the lower planes and the nearest generators
+    std::vector<int> G0;
+    {
+        std::vector<qreal> dist(n);
+        qreal dmin = -1;
+        for (int64_t i = 0; i < n; ++i) {
+            qreal s = 0;
+            for (int k = 0; k < d; ++k) { const qreal w = (qreal)pts[i * d + k] - (qreal)lo[k]; s += w * w; }
+            dist[i] = s;
+            if (dmin < 0 || s < dmin) dmin = s;
+        }
+        for (int64_t i = 0; i < n; ++i) if (dist[i] <= dmin * (1 + (qreal)GEN_TOL)) G0.push_back((int)i);
+        for (int k = 0; k < d; ++k) G0.push_back((int)n + 2 * k + 1);
+        std::sort(G0.begin(), G0.end());
+    }
+    std::unordered_map<std::vector<int>, int, SigHash> index;
+    auto add = [&](const std::vector<int>& g) -> int {
+        auto it = index.find(g);
+        if (it != index.end()) return -1;
+        std::array<qreal, MAXD> c{};
+        if (!gen_centre(P, g, c.data())) return -2;
+        index.emplace(g, (int)GM.G.size());
+        GM.G.push_back(g);
+        GM.C.push_back(c);
+        return (int)GM.G.size() - 1;
+    };
+    if (add(G0) < 0) { set_err("corner vertex"); delete M; return -3; }
+    std::vector<GenEdge> edges;
+    for (size_t v = 0; v < GM.G.size(); ++v) {
+        const std::vector<int> g = GM.G[v];
+        const std::array<qreal, MAXD> c = GM.C[v];
+        if (!gen_edges(P, g, edges)) { set_err("a vertex has too many generators to enumerate"); delete M; return -4; }
+        for (auto& e : edges) {
+            std::vector<int> g2;
+            if (!gen_walk(P, g, c.data(), e, g2)) { set_err("an edge leaves the box"); delete M; return -3; }
+            if (add(g2) == -2) { set_err("singular vertex"); delete M; return -3; }
+        }
+    }
+    const int64_t V = (int64_t)GM.G.size();
+    for (int64_t v = 0; v < V; ++v) {
+        M->vsig.push_back(GM.G[v]);
+        for (int k = 0; k < d; ++k) M->vc.push_back((double)GM.C[v][k]);
+    }
+    // neighbours: pairs of a vertex that share a full interface
+    std::map<std::pair<int, int>, std::vector<int>> pairs;
+    for (int64_t v = 0; v < V; ++v)
+        for (int i : GM.G[v]) {
+            if (P.is_plane(i)) continue;
+            for (int j : GM.G[v]) if (j != i) pairs[{i, j}].push_back((int)v);
+        }
+    std::vector<std::vector<int>> nb(n);
+    std::vector<std::vector<std::vector<int>>> fv(n);
+    for (auto& kv : pairs) {
+        bool full = false;
+        for (int v : kv.second) full |= (int)GM.G[v].size() == d + 1;
+        if (!full) {
+            std::vector<const qreal*> pp;
+            for (int v : kv.second) pp.push_back(GM.C[v].data());
+            qreal Q[MAXD][MAXD];
+            full = mgs_basis(d, pp, Q, (qreal)1e-10) >= d - 1;
+        }
+        if (!full) continue;
+        nb[kv.first.first].push_back(kv.first.second);
+        fv[kv.first.first].push_back(kv.second);
+    }
+    M->offs.assign(n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) M->offs[i + 1] = M->offs[i] + (int64_t)nb[i].size();
+    M->nbr.resize(M->offs[n]);
+    for (int64_t i = 0; i < n; ++i) std::copy(nb[i].begin(), nb[i].end(), M->nbr.begin() + M->offs[i]);
+    if (integrate) {
+        M->area.assign(M->offs[n], 0.0);
+        M->vol.assign(n, 0.0);
+        for (int64_t i = 0; i < n; ++i)
+            for (size_t t = 0; t < nb[i].size(); ++t) {
+                const int k = nb[i][t];
+                std::vector<int> S{(int)i, k};
+                std::sort(S.begin(), S.end());
+                M->area[M->offs[i] + t] = (double)GM.face_volume(S, fv[i][t], d - 1);
+            }
+        for (int64_t i = 0; i < n; ++i) {
+            double v = 0;
+            for (int64_t t = M->offs[i]; t < M->offs[i + 1]; ++t) v += M->area[t] * height(P, (int)i, M->nbr[t]) / d;
+            M->vol[i] = v;
+        }
+        M->integrated = true;
+    }
+    finish_mesh(M);
+    *out = M;
+    return 0;
+}
+
+int64_t hvo_sig_total(const hvo_mesh* m) {
+    int64_t s = 0;
+    for (auto& g : m->vsig) s += (int64_t)g.size();
+    return s;
+}
+
+void hvo_vertices_csr(const hvo_mesh* m, int64_t* offs, int64_t* sig, double* r) {
+    const int d = m->P.d;
+    int64_t pos = 0;
+    offs[0] = 0;
+    for (size_t o = 0; o < m->order.size(); ++o) {
+        const int64_t v = m->order[o];
+        for (int g : m->vsig[v]) sig[pos++] = out_item(m->P, g);
+        offs[o + 1] = pos;
+        for (int k = 0; k < d; ++k) r[o * d + k] = m->vc[(size_t)v * d + k];
+    }
 }
 
 }  // extern "C"

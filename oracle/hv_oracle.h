@@ -124,6 +124,17 @@ void hvo_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4
 /* Philox4x32-10 unit directions shared with the GPU MC kernel (for tests). */
 void hvo_mc_directions(int d, int64_t cell, int ndir, uint64_t seed, double* dirs);
 
+/* Vertices with more than d+1 generators (lattices, co-spherical points): the
+ * vertex graph of the box [lo, hi] walked from the corner lo in binary128;
+ * every vertex keeps all generators on its sphere, neighbours share a full
+ * interface, integrate=1 adds the polygon volumes and areas. */
+int hvo_build_generic(int d, int64_t n, const double* pts, const double* lo, const double* hi, int integrate,
+                      hvo_mesh** out);
+/* Total signature length over the vertices, and the vertices as a CSR:
+ * offs (V+1), sig (1-based, sorted per vertex), r (V x d). */
+int64_t hvo_sig_total(const hvo_mesh* m);
+void hvo_vertices_csr(const hvo_mesh* m, int64_t* offs, int64_t* sig, double* r);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,10 @@ def lib():
             L.hvo_verify_vertices_planes.argtypes = [I, I64, dp, I, dp, dp, I64, ip, dp, D]
             L.hvo_verify_vertices_planes.restype = I64
             L.hvo_num_vertices.argtypes = [P]; L.hvo_num_vertices.restype = I64
+            L.hvo_build_generic.argtypes = [I, I64, dp, dp, dp, I, ctypes.POINTER(P)]
+            L.hvo_build_generic.restype = I
+            L.hvo_sig_total.argtypes = [P]; L.hvo_sig_total.restype = I64
+            L.hvo_vertices_csr.argtypes = [P, ip, ip, dp]; L.hvo_vertices_csr.restype = None
             L.hvo_num_neighbors.argtypes = [P]; L.hvo_num_neighbors.restype = I64
             L.hvo_vertices.argtypes = [P, ip, dp]; L.hvo_vertices.restype = None
             L.hvo_neighbors.argtypes = [P, ip, ip]; L.hvo_neighbors.restype = None
@@ -101,11 +105,13 @@ class OracleMesh:
     """Result of one oracle mesh build (1-based reference index conventions)."""
 
     def __init__(self, pts, lo=None, hi=None, seed=0, nthreads=0, mode=0, integrate=False, planes=None,
-                 csr=None):
+                 csr=None, generic=False):
         """Box [lo, hi] (default unit cube), or the convex domain of
         ``planes = (base, normal)``, (P, d) arrays each.  ``csr = (offs, nbr)``
         (1-based neighbours) skips the search and holds only those neighbour
-        lists, for running the integrators on another mesh's lists."""
+        lists, for running the integrators on another mesh's lists.
+        ``generic=True`` (box only) walks the vertex graph with vertices of any
+        number of generators (lattices); read them with vertices_csr()."""
         L = lib()
         pts = np.ascontiguousarray(pts, dtype=np.float64)
         self.n, self.d = pts.shape
@@ -117,6 +123,11 @@ class OracleMesh:
             offs = np.ascontiguousarray(csr[0], dtype=np.int64)
             nbr = np.ascontiguousarray(csr[1], dtype=np.int64)
             rc = L.hvo_mesh_from_csr(self.d, self.n, _dp(pts), _dp(self.lo), _dp(self.hi), _ip(offs), _ip(nbr),
+                                     ctypes.byref(h))
+        elif generic:
+            self.lo = np.ascontiguousarray(np.zeros(self.d) if lo is None else lo, dtype=np.float64)
+            self.hi = np.ascontiguousarray(np.ones(self.d) if hi is None else hi, dtype=np.float64)
+            rc = L.hvo_build_generic(self.d, self.n, _dp(pts), _dp(self.lo), _dp(self.hi), 1 if integrate else 0,
                                      ctypes.byref(h))
         elif planes is not None:
             base = np.ascontiguousarray(planes[0], dtype=np.float64)
@@ -148,6 +159,19 @@ class OracleMesh:
         if V:
             L.hvo_vertices(self._h, _ip(sig), _dp(r))
         return sig, r
+
+    def vertices_csr(self):
+        """(offs (V+1), sig (1-based, sorted per vertex), r (V, d)) for vertices
+        of any number of generators, in lexicographic order of their signatures."""
+        L = lib()
+        V = L.hvo_num_vertices(self._h)
+        S = L.hvo_sig_total(self._h)
+        offs = np.zeros(V + 1, dtype=np.int64)
+        sig = np.zeros(max(S, 1), dtype=np.int64)
+        r = np.zeros((V, self.d), dtype=np.float64)
+        if V:
+            L.hvo_vertices_csr(self._h, _ip(offs), _ip(sig), _dp(r))
+        return offs, sig[:S], r
 
     def neighbors(self):
         L = lib()

@@ -1,0 +1,123 @@
+"""Co-spherical generators (lattices): every vertex keeps all generators on its
+sphere, as the reference's vertex database does (push!(mesh, sig => r),
+src/abstractmesh.jl:111-127, with the tie sets of its inrange search and the
+edges of FastEdgeIterator, src/edgeiterate.jl:82-110).  The reference's own
+case is a 4 x 4 lattice of the unit square (test/fraud.jl:8-12); the 3D 4^3
+and 4D 3^4 lattices follow it.  Against the oracle's generic walk
+(binary128): signatures bit-exact, coordinates within 1e-13, neighbours
+bit-exact, VI_POLYGON volumes and areas within 1e-12; every cell of a k^d
+lattice has volume k^-d and the vertices are the grid points i/k.
+HV_METHOD_GENERIC on points in general position must give the fast mesh."""
+import numpy as np
+import pytest
+
+import oracle as O
+from hvgpu import datasets as D
+
+pytestmark = pytest.mark.gpu
+
+
+def lattice(d, k):
+    g = (np.arange(k) + 0.5) / k
+    return np.ascontiguousarray(np.stack(np.meshgrid(*([g] * d), indexing="ij"), -1).reshape(-1, d))
+
+
+def build(hv, X, method=None):
+    d = X.shape[1]
+    prm = hv.make_params(hv.HV_METHOD_FAST if method is None else method)
+    return hv.Mesh(hv.default_context(), X, np.zeros(d), np.ones(d), prm)
+
+
+@pytest.mark.parametrize("d,k", [(2, 4), (2, 7), (3, 4), (3, 5), (4, 3)])
+def test_lattice_matches_the_oracle(gpu_lib, d, k):
+    hv = gpu_lib
+    X = lattice(d, k)
+    m = build(hv, X)
+    ref = O.OracleMesh(X, integrate=True, generic=True)
+    offs, sig, r = m.vertices_csr()
+    ro, rs, rr = ref.vertices_csr()
+    np.testing.assert_array_equal(offs, ro)
+    np.testing.assert_array_equal(sig, rs)
+    np.testing.assert_allclose(r, rr, rtol=0, atol=1e-13)
+    assert len(offs) - 1 == (k + 1) ** d
+    assert m.max_signature() == 2 ** d
+    # the vertices are the grid points i/k
+    np.testing.assert_allclose(r * k, np.round(r * k), rtol=0, atol=1e-12)
+    no, nb = m.neighbors()
+    rno, rnb = ref.neighbors()
+    np.testing.assert_array_equal(no, rno)
+    np.testing.assert_array_equal(nb, rnb)
+    assert np.all(np.diff(no) == 2 * d)  # face neighbours only, no diagonal cells
+    vol, area = m.polygon()
+    rv, ra = ref.polygon()
+    np.testing.assert_allclose(vol, rv, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(area, ra, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(vol, np.full(len(X), float(k) ** -d), rtol=1e-12)
+    np.testing.assert_allclose(area, np.full(len(area), float(k) ** (1 - d)), rtol=1e-12)
+    assert abs(vol.sum() - 1.0) < 1e-12
+
+
+def test_fast_vertex_reads_refuse_long_signatures(gpu_lib):
+    hv = gpu_lib
+    m = build(hv, lattice(2, 4))
+    with pytest.raises(hv.HVError) as e:
+        m.vertices()
+    assert e.value.code == hv._lib.HV_E_DEGENERATE
+
+
+@pytest.mark.parametrize("d,n,seed", [(2, 300, 1), (3, 200, 2), (4, 100, 3)])
+def test_generic_walk_of_general_points_is_the_fast_mesh(gpu_lib, d, n, seed):
+    hv = gpu_lib
+    X = D.uniform_points(d, n, seed)
+    a = build(hv, X)
+    b = build(hv, X, hv.HV_METHOD_GENERIC)
+    sa, ra = a.vertices()
+    ob, sb, rb = b.vertices_csr()
+    assert np.all(np.diff(ob) == d + 1)
+    np.testing.assert_array_equal(sb.reshape(-1, d + 1), sa)
+    np.testing.assert_allclose(rb, ra, rtol=0, atol=1e-13)
+    for x, y in zip(a.neighbors(), b.neighbors()):
+        np.testing.assert_array_equal(x, y)
+    va, aa = a.polygon()
+    vb, ab = b.polygon()
+    np.testing.assert_allclose(vb, va, rtol=1e-10, atol=0)
+    np.testing.assert_allclose(ab, aa, rtol=1e-9, atol=1e-15)
+
+
+@pytest.mark.parametrize("d,k,seed", [(2, 6, 5), (3, 4, 6)])
+def test_lattice_with_moved_points(gpu_lib, d, k, seed):
+    """A lattice with a few points moved: degenerate and simple vertices mixed."""
+    hv = gpu_lib
+    X = lattice(d, k)
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(len(X), size=len(X) // 4, replace=False)
+    X[idx] += rng.uniform(-0.2, 0.2, size=(len(idx), d)) / k
+    m = build(hv, X)
+    ref = O.OracleMesh(X, integrate=True, generic=True)
+    offs, sig, r = m.vertices_csr()
+    ro, rs, rr = ref.vertices_csr()
+    np.testing.assert_array_equal(offs, ro)
+    np.testing.assert_array_equal(sig, rs)
+    np.testing.assert_allclose(r, rr, rtol=0, atol=1e-13)
+    for x, y in zip(m.neighbors(), ref.neighbors()):
+        np.testing.assert_array_equal(x, y)
+    vol, area = m.polygon()
+    rv, ra = ref.polygon()
+    np.testing.assert_allclose(vol, rv, rtol=1e-11, atol=0)
+    np.testing.assert_allclose(area, ra, rtol=1e-10, atol=1e-15)
+    assert abs(vol.sum() - 1.0) < 1e-12
+
+
+def test_lattice_monte_carlo_and_voronoi_data(gpu_lib):
+    hv = gpu_lib
+    d, k = 3, 4
+    X = lattice(d, k)
+    geo = hv.VoronoiGeometry(X, hv.cuboid(d, periodic=[]), integrator=hv.VI_POLYGON)
+    data = hv.VoronoiData(geo)
+    assert len(data.vertex_sigs) == (k + 1) ** d
+    assert max(len(s) for s in data.vertex_sigs) == 2 ** d
+    np.testing.assert_allclose(data.volume, np.full(len(X), k ** -3.0), rtol=1e-12)
+    m = build(hv, X)
+    vol, area = m.heuristic_mc(2000, 7)
+    assert abs(vol.sum() - 1.0) < 0.05
+    assert np.all(np.abs(vol * k ** 3 - 1.0) < 0.25)

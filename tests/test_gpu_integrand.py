@@ -33,6 +33,7 @@ def test_integrands_match_the_oracle(gpu_lib, d, n, seed):
     s, r = m.vertices()
     rs, rr = ref.vertices()
     np.testing.assert_array_equal(s, rs)
+    np.testing.assert_allclose(r, rr, rtol=0, atol=1e-13)
     c = m.facet_centers()
     np.testing.assert_allclose(c, ref.facet_centers(), rtol=0, atol=1e-13)
     vol, area = m.polygon()

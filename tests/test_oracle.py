@@ -417,3 +417,43 @@ def test_oracle_integrand_quadrature(d, n):
         np.testing.assert_allclose(B.sum(axis=0), [1.0, 0.5, 0.5], rtol=1e-12)
     else:
         assert abs(B.sum(axis=0)[1] - 0.5) < 0.01
+
+
+def _lattice(d, k):
+    g = (np.arange(k) + 0.5) / k
+    return np.ascontiguousarray(np.stack(np.meshgrid(*([g] * d), indexing="ij"), -1).reshape(-1, d))
+
+
+@pytest.mark.parametrize("d,k", [(2, 4), (3, 4), (4, 3)])
+def test_generic_walk_of_lattices(d, k):
+    """The reference's fraud case (test/fraud.jl:8-12, a 4 x 4 lattice) and
+    its 3D/4D analogues: (k+1)^d grid-point vertices, interior ones with 2^d
+    generators, 2d face neighbours per cell, cells of volume k^-d."""
+    m = O.OracleMesh(_lattice(d, k), integrate=True, generic=True)
+    offs, sig, r = m.vertices_csr()
+    assert len(offs) - 1 == (k + 1) ** d
+    assert np.diff(offs).max() == 2 ** d
+    np.testing.assert_allclose(r * k, np.round(r * k), rtol=0, atol=1e-13)
+    no, _ = m.neighbors()
+    assert np.all(np.diff(no) == 2 * d)
+    vol, area = m.polygon()
+    np.testing.assert_allclose(vol, np.full(k ** d, float(k) ** -d), rtol=1e-13)
+    np.testing.assert_allclose(area, np.full(len(area), float(k) ** (1 - d)), rtol=1e-13)
+
+
+@pytest.mark.parametrize("d,n,seed", [(2, 150, 1), (3, 80, 2)])
+def test_generic_walk_of_general_points_is_the_search(d, n, seed):
+    """On points in general position the generic walk gives the per-cell search's mesh."""
+    X = np.random.default_rng(seed).random((n, d))
+    a = O.OracleMesh(X, integrate=True)
+    b = O.OracleMesh(X, integrate=True, generic=True)
+    sa, ra = a.vertices()
+    ob, sb, rb = b.vertices_csr()
+    np.testing.assert_array_equal(sb.reshape(-1, d + 1), sa)
+    np.testing.assert_allclose(rb, ra, rtol=0, atol=1e-14)
+    for x, y in zip(a.neighbors(), b.neighbors()):
+        np.testing.assert_array_equal(x, y)
+    va, aa = a.polygon()
+    vb, ab = b.polygon()
+    np.testing.assert_allclose(vb, va, rtol=1e-12)
+    np.testing.assert_allclose(ab, aa, rtol=1e-11)
