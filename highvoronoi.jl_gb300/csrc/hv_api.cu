@@ -256,18 +256,69 @@ void check_fatal(unsigned status) {
         throw HvError(HV_E_INTERNAL, "device search failed (status " + std::to_string(status) + ")");
 }
 
+// A corner of the domain: the first d planes (in id order) whose hyperplanes
+// meet in one point inside all the others; the walk starts at its Voronoi
+// vertex (the corner, its planes and its nearest generators).
+bool domain_corner(const hv_mesh* mesh, double* v) {
+    const int d = mesh->d, np = mesh->np;
+    int idx[HV_MAXD];
+    for (int q = 0; q < d; ++q) idx[q] = q;
+    if (np < d) return false;
+    for (;;) {
+        double A[HV_MAXD][HV_MAXD], b[HV_MAXD];
+        for (int r = 0; r < d; ++r) {
+            for (int k = 0; k < d; ++k) A[r][k] = mesh->planes[idx[r]].n[k];
+            b[r] = mesh->planes[idx[r]].off;
+        }
+        bool ok = true;
+        for (int c = 0; c < d && ok; ++c) {  // Gaussian elimination, partial pivoting
+            int p = c;
+            for (int r = c + 1; r < d; ++r) if (std::fabs(A[r][c]) > std::fabs(A[p][c])) p = r;
+            if (!(std::fabs(A[p][c]) > 1e-12)) { ok = false; break; }
+            std::swap(A[p], A[c]);
+            std::swap(b[p], b[c]);
+            for (int r = c + 1; r < d; ++r) {
+                const double f = A[r][c] / A[c][c];
+                for (int k = c; k < d; ++k) A[r][k] -= f * A[c][k];
+                b[r] -= f * b[c];
+            }
+        }
+        if (ok) {
+            for (int r = d - 1; r >= 0; --r) {
+                double t = b[r];
+                for (int k = r + 1; k < d; ++k) t -= A[r][k] * v[k];
+                v[r] = t / A[r][r];
+            }
+            bool inside = true;
+            for (int p = 0; p < np && inside; ++p) {
+                double h = mesh->planes[p].off;
+                double sc = std::fabs(mesh->planes[p].off);
+                for (int k = 0; k < d; ++k) { h -= mesh->planes[p].n[k] * v[k]; sc += std::fabs(v[k]); }
+                inside = h >= -1e-12 * (sc + 1.0);
+            }
+            if (inside) return true;
+        }
+        int q = d - 1;
+        while (q >= 0 && idx[q] == np - d + q) --q;
+        if (q < 0) return false;
+        ++idx[q];
+        for (int r = q + 1; r < d; ++r) idx[r] = idx[r - 1] + 1;
+    }
+}
+
 // Vertices with more than d+1 generators: the search met co-spherical
 // generators (or HV_METHOD_GENERIC asked for this walk).  The vertex graph is
-// walked again from the search's first vertex with every vertex keeping all
-// generators on its sphere (hv_degen.cu); the result replaces the fixed-width
-// vertex list with a CSR of generator lists, and the neighbour lists keep the
-// pairs that share a full interface.  The device tree, points and planes of
-// the search (M) are reused.
+// walked from a corner of the domain with every vertex keeping all generators
+// on its sphere (hv_degen.cu); the result is a CSR of generator lists in place
+// of the fixed-width vertex list, and the neighbour lists keep the pairs that
+// share a full interface.  The device tree, points and planes of the search
+// (M) are reused.
 void generic_build(hv_ctx* ctx, hv_mesh* mesh, const hv::DevMesh& M) {
     using namespace hv;
     cudaStream_t st = ctx->stream;
     const int d = mesh->d, n = mesh->n;
-    if (mesh->V == 0 || !mesh->osig) throw HvError(HV_E_INTERNAL, "no vertex to start the degenerate walk from");
+    double corner[HV_MAXD];
+    if (!domain_corner(mesh, corner)) throw HvError(HV_E_INTERNAL, "degenerate walk: no corner of the domain found");
     int W = std::min(GMAX, std::max(2 * (d + 1), (1 << d) + 2 * d));
     const unsigned long long vest = (unsigned long long)(vertices_per_point(d) * n) + (1ull << d) + 1024;
     for (int attempt = 0;; ++attempt) {
@@ -295,7 +346,9 @@ void generic_build(hv_ctx* ctx, hv_mesh* mesh, const hv::DevMesh& M) {
             CK(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
         };
-        launch_gen_seed(R, mesh->osig, mesh->oc, st);
+        double* dcorner = s.get<double>(d);
+        CK(cudaMemcpyAsync(dcorner, corner, sizeof(double) * d, cudaMemcpyHostToDevice, st));
+        launch_gen_seed(R, dcorner, st);
         CK(cudaGetLastError());
         read();
         std::unique_ptr<Scratch> es;
@@ -561,7 +614,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     M.cnt = dcnt;
     kt.run(F_OTHER, 1, [&] { launch_bvh(M, blo, bhi, flags, st); });
     // ---- candidate lists
-    const bool fast = mesh->prm.method != HV_METHOD_PLAIN;  // the generic walk starts from the fast search
+    const bool fast = mesh->prm.method == HV_METHOD_FAST;
     int K = mesh->prm.knn > 0 ? mesh->prm.knn : default_knn(d);
     K = std::min(K, std::max(n - 1, 0));
     K = std::min(K, 480);
@@ -595,9 +648,21 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     if (mesh->own_from >= 0)  // refinement: only the vertices of the new cells (d+1 cells share a vertex)
         est = std::min(est, (unsigned long long)(vertices_per_point(d) * (d + 1) * (n - mesh->own_from)) + 1024);
     const int nseeds = (M.own1 - M.own0 + stride - 1) / stride;
+    // a tie that survives double-double: box and plane-domain builds stop the
+    // search and walk the vertex graph with vertices of any size instead
+    bool degen_abort = false;
+    auto fatal = [&](unsigned stt) -> bool {
+        if (mesh->allow_generic && (stt & ST_DEGEN) && !(stt & (ST_BADINPUT | ST_TIMEOUT))) {
+            degen_abort = true;
+            return true;
+        }
+        check_fatal(stt);
+        return false;
+    };
     std::unique_ptr<Scratch> srch;
     unsigned V = 0;
-    for (int attempt = 0;; ++attempt) {
+    if (mesh->prm.method == HV_METHOD_GENERIC) degen_abort = true;  // the walk needs only the tree
+    for (int attempt = 0; !degen_abort; ++attempt) {
         if (attempt > 4) throw HvError(HV_E_CAPACITY, "vertex capacity retries exhausted");
         unsigned long long vcap64 = (unsigned long long)(est * factor * (double)(1ull << attempt));
         if (vcap64 > 0xFFFFFFF0ull / 8) throw HvError(HV_E_CAPACITY, "vertex count beyond 32-bit ids");
@@ -673,9 +738,10 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         }
         const unsigned overflow_bits = ST_VCAP | ST_HASH | ST_QUEUE | ST_ECAP;
         bool overflow = (ctx->h_stat[1] & overflow_bits) != 0;
-        if (!overflow) check_fatal(ctx->h_stat[1]);
+        if (!overflow) fatal(ctx->h_stat[1]);
         unsigned f0 = 0, f1 = std::min(ctx->h_stat[0], vcap);
-        if (!overflow) kt.run(F_CENTERS, 1, [&] { launch_centers(M, 0, f1, ctx->nsm, st); });
+        if (degen_abort) f1 = 0;
+        if (!overflow && !degen_abort) kt.run(F_CENTERS, 1, [&] { launch_centers(M, 0, f1, ctx->nsm, st); });
         long long levels = 0;
         if (fast) {
             // Level L expands [f0, f1) on the context's stream; its fallback ladder
@@ -706,8 +772,8 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
                     CK(cudaStreamWaitEvent(st, ev_reg, 0));
                 }
             };
-            if (!overflow) prepare(f0, f1, false);  // the seeds' centres are queued already
-            if (!overflow && use_graph(n)) {
+            if (!overflow && !degen_abort) prepare(f0, f1, false);  // the seeds' centres are queued already
+            if (!overflow && !degen_abort && use_graph(n)) {
                 // every level in one launch of a CUDA graph: a WHILE node whose body is
                 // [ladder of the previous level | expansion] -> advance -> [centres | edge
                 // registry]; the frontier and the level live in device memory
@@ -767,18 +833,18 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
                 CK(cudaMemcpyAsync(hl2, lvl, sizeof(hl2), cudaMemcpyDeviceToHost, st));
                 read_stat(ctx, dstat);
                 if (ctx->h_stat[1] & overflow_bits) overflow = true;
-                else check_fatal(ctx->h_stat[1]);
+                else fatal(ctx->h_stat[1]);
                 f0 = f1 = std::min(ctx->h_stat[0], vcap);
                 levels = hl2[2];
             }
-            for (int L = 0; !overflow && !use_graph(n); ++L) {
+            for (int L = 0; !overflow && !degen_abort && !use_graph(n); ++L) {
                 if (f1 == f0) {
                     if (!pend) break;
                     CK(cudaStreamWaitEvent(st, ctx->ovl_ev[1 + pend_par], 0));
                     pend = false;
                     read_stat(ctx, dstat);
                     if (ctx->h_stat[1] & overflow_bits) { overflow = true; break; }
-                    check_fatal(ctx->h_stat[1]);
+                    if (fatal(ctx->h_stat[1])) break;
                     const unsigned e = std::min(ctx->h_stat[0], vcap);
                     if (e == f1) break;
                     prepare(f1, e, true);
@@ -808,12 +874,12 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
                 CK(cudaMemcpyAsync(ctx->h_stat + 2, qc + 2 * p, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
                 read_stat(ctx, dstat);
                 if (ctx->h_stat[1] & overflow_bits) { overflow = true; break; }
-                check_fatal(ctx->h_stat[1]);
+                if (fatal(ctx->h_stat[1])) break;
                 if (ctx->h_stat[2] > (unsigned)overlap_rays_per_sm() * (unsigned)ctx->nsm) {  // work-bound: no overlap
                     CK(cudaStreamWaitEvent(st, ctx->ovl_ev[1 + p], 0));
                     read_stat(ctx, dstat);
                     if (ctx->h_stat[1] & overflow_bits) { overflow = true; break; }
-                    check_fatal(ctx->h_stat[1]);
+                    if (fatal(ctx->h_stat[1])) break;
                 }
                 const unsigned e = std::min(ctx->h_stat[0], vcap);
                 prepare(f1, e, true);
@@ -825,18 +891,19 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
             CK(cudaStreamSynchronize(st2));
             CK(cudaStreamSynchronize(st3));
         }
-        while (!fast && !overflow && f1 > f0) {
+        while (!fast && !overflow && !degen_abort && f1 > f0) {
             if (dedup) kt.run(F_OTHER, 1, [&] { launch_register_edges(M, f0, f1, ctx->nsm, st); });
             kt.run(F_EXPAND, 1, [&] { launch_expand_plain(M, f0, f1, ctx->nsm, st); });
             CK(cudaGetLastError());
             read_stat(ctx, dstat);
             if (ctx->h_stat[1] & overflow_bits) { overflow = true; break; }
-            check_fatal(ctx->h_stat[1]);
+            if (fatal(ctx->h_stat[1])) break;
             const unsigned f2 = std::min(ctx->h_stat[0], vcap);
             kt.run(F_CENTERS, 1, [&] { launch_centers(M, f1, f2, ctx->nsm, st); });
             f0 = f1; f1 = f2;
             ++levels;
         }
+        if (degen_abort) break;
         if (overflow) { S.capacity_retries++; continue; }
         V = f1;
         S.levels = levels;
@@ -844,6 +911,19 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         break;
     }
     CK(cudaEventRecord(ev.e[2], st));
+    if (degen_abort || mesh->prm.method == HV_METHOD_GENERIC) {
+        srch.reset();
+        unsigned long long hc[C_NCOUNT];
+        CK(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        S.rays = (int64_t)hc[C_RAYS];
+        S.degenerate = (int64_t)hc[C_DEGEN];
+        S.descents = (int64_t)hc[C_DESCENT];
+        generic_build(ctx, mesh, M);
+        S.ms_prepare = ms_between(ev.e[0], ev.e[1]);
+        S.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return;
+    }
     // ---- canonical order
     mesh->V = V;
     CK(cudaEventRecord(kt.next(), st));
@@ -931,7 +1011,11 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     // reference stores such a vertex with all of them, and so does the generic
     // walk of a box or plane-domain build.  This search broke the tie by index,
     // so a periodic image set, a shard or a refinement refuses the mesh.
-    if (mesh->prm.method == HV_METHOD_GENERIC || (S.degenerate > 0 && mesh->allow_generic)) {
+    if (S.degenerate > 0 && mesh->allow_generic) {  // a tie the level checks did not see
+        dfree(st, mesh->osig);
+        dfree(st, mesh->oc);
+        mesh->osig = nullptr;
+        mesh->oc = nullptr;
         generic_build(ctx, mesh, M);
         S.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         return;

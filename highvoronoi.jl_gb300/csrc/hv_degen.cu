@@ -474,63 +474,60 @@ __global__ void k_gen_commit(GenRun R, unsigned nrec) {
     }
 }
 
-// Vertex 0: every generator on the sphere of the known vertex (sig0, c0).
+// Vertex 0: the domain corner v with the planes through it and its nearest
+// generators (all within 2e-9 relative of the smallest squared distance).
+constexpr int SEED_T = 256;
 template <int D>
-__global__ void k_gen_seed(GenRun R, const int* sig0, const double* c0) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    int a = -1;
-    for (int s = 0; s <= D; ++s)
-        if (sig0[s] < R.M.n && (a < 0 || sig0[s] < a)) a = sig0[s];
-    if (a < 0) { atomicOr(R.status, GS_NUMERIC); return; }
-    double c[D], ca = 0.0;
+__global__ void __launch_bounds__(SEED_T) k_gen_seed(GenRun R, const double* v) {
+    __shared__ double smin[SEED_T];
+    __shared__ int sG[GMAX];
+    __shared__ int sm;
+    __shared__ int sover;
+    double c[D];
 #pragma unroll
-    for (int k = 0; k < D; ++k) {
-        c[k] = c0[k];
-        const double w = c[k] - R.x[(size_t)a * D + k];
-        ca = fma(w, w, ca);
-    }
-    const double rad = sqrt(ca);
-    int G[GMAX] = {};
-    int m = 0;
-    bool over = false;
-    auto add = [&](int it) {
-        if (m == GMAX) { over = true; return; }
-        int x = m++;
-        while (x > 0 && G[x - 1] > it) { G[x] = G[x - 1]; --x; }
-        G[x] = it;
+    for (int k = 0; k < D; ++k) c[k] = v[k];
+    auto dist2 = [&](int j) {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) { const double w = R.x[(size_t)j * D + k] - c[k]; s = fma(w, w, s); }
+        return s;
     };
-    int stack[64];
-    int sp = 0;
-    stack[sp++] = 1;
-    while (sp > 0 && !over) {
-        const int node = stack[--sp];
-        if (gen_box_dist2<D>(R.M, node, c) > ca * (1.0 + 4.0 * GEN_REL) + 1e-300) continue;
-        if (node >= R.M.P) {
-            const int l = node - R.M.P;
-            if (l >= R.M.nleaves) continue;
-            const int s0 = l * R.M.leaf, s1 = min(s0 + R.M.leaf, R.M.n);
-            for (int j = s0; j < s1; ++j) {
-                double dj = 0.0;
-#pragma unroll
-                for (int k = 0; k < D; ++k) {
-                    const double w = c[k] - R.M.pts[(size_t)j * D + k];
-                    dj = fma(w, w, dj);
-                }
-                if (fabs(dj - ca) <= 2.0 * GEN_REL * ca) add(R.M.perm[j]);
-            }
-        } else {
-            if (sp + 2 > 64) { over = true; break; }
-            stack[sp++] = 2 * node + 1;
-            stack[sp++] = 2 * node;
-        }
+    double mn = INFINITY;
+    for (int j = threadIdx.x; j < R.M.n; j += SEED_T) mn = fmin(mn, dist2(j));
+    smin[threadIdx.x] = mn;
+    if (threadIdx.x == 0) { sm = 0; sover = 0; }
+    __syncthreads();
+    for (int w = SEED_T / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + w]);
+        __syncthreads();
     }
+    const double dmin = smin[0];
+    for (int j = threadIdx.x; j < R.M.n; j += SEED_T)
+        if (dist2(j) <= dmin * (1.0 + 2.0 * GEN_REL)) {
+            const int q = atomicAdd(&sm, 1);
+            if (q < GMAX) sG[q] = j;
+            else sover = 1;
+        }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const double rad = sqrt(dmin);
+    int m = min(sm, GMAX);
     for (int p = 0; p < R.M.np; ++p)
-        if (fabs(plane_height<D>(R.M.planes[p], c)) <= GEN_REL * (rad + 1e-300)) add(R.M.n + p);
-    if (over || m > R.W) { atomicOr(R.status, GS_WIDE); return; }
-    for (int s = 0; s < m; ++s) R.vsig[s] = G[s];
+        if (fabs(plane_height<D>(R.M.planes[p], c)) <= GEN_REL * (rad + 1e-300)) {
+            if (m < GMAX) sG[m++] = R.M.n + p;
+            else sover = 1;
+        }
+    if (sover || m > R.W) { atomicOr(R.status, GS_WIDE); return; }
+    for (int a = 1; a < m; ++a) {
+        const int x = sG[a];
+        int b = a - 1;
+        while (b >= 0 && sG[b] > x) { sG[b + 1] = sG[b]; --b; }
+        sG[b + 1] = x;
+    }
+    for (int q = 0; q < m; ++q) R.vsig[q] = sG[q];
     R.vlen[0] = m;
-    if (!gen_centre<D>(R, G, m, R.vc)) atomicOr(R.status, GS_NUMERIC);
-    R.htab[gen_hash(G, m) & R.hmask] = 0;
+    if (!gen_centre<D>(R, sG, m, R.vc)) atomicOr(R.status, GS_NUMERIC);
+    R.htab[gen_hash(sG, m) & R.hmask] = 0;
     *R.vcnt = 1;
 }
 
@@ -829,8 +826,8 @@ unsigned gen_grid(unsigned long long n, int bs, unsigned cap = 1u << 20) {
         default: break;                                \
     }
 
-void launch_gen_seed(const GenRun& R, const int* sig0, const double* c0, cudaStream_t st) {
-    HV_DISPATCH(R.M.d, (k_gen_seed<DD><<<1, 32, 0, st>>>(R, sig0, c0)));
+void launch_gen_seed(const GenRun& R, const double* corner, cudaStream_t st) {
+    HV_DISPATCH(R.M.d, (k_gen_seed<DD><<<1, SEED_T, 0, st>>>(R, corner)));
 }
 
 void launch_gen_edges(const GenRun& R, unsigned f0, unsigned f1, int nsm, cudaStream_t st) {

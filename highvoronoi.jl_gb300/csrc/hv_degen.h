@@ -49,9 +49,9 @@ struct GenRun {
     unsigned* status;
 };
 
-// The vertex at centre c0 (d doubles, device) through the generators sig0
-// (d+1 original ids, device): vertex 0 with every generator on its sphere.
-void launch_gen_seed(const GenRun& R, const int* sig0, const double* c0, cudaStream_t st);
+// Vertex 0: the domain corner (d doubles, device), the planes through it and
+// its nearest generators.
+void launch_gen_seed(const GenRun& R, const double* corner, cudaStream_t st);
 void launch_gen_edges(const GenRun& R, unsigned f0, unsigned f1, int nsm, cudaStream_t st);
 void launch_gen_walk(const GenRun& R, unsigned ne, int nsm, cudaStream_t st);
 void launch_gen_insert(const GenRun& R, unsigned nrec, cudaStream_t st);

@@ -184,13 +184,17 @@ def _grid(d, k):
 
 
 @pytest.mark.parametrize("d,k", [(2, 6), (3, 4)])
-def test_lattice_points_are_refused(gpu_lib, d, k):
-    """Lattice points put more than d+1 generators on one empty sphere; the
-    reference stores such vertices with all of them, this search would have to
-    break the ties by index -- it returns HV_E_DEGENERATE instead of a wrong mesh."""
+def test_lattice_points_in_periodic_cuboids_are_refused(gpu_lib, d, k):
+    """Lattice points put more than d+1 generators on one empty sphere.  A box
+    build walks such vertices with all their generators (test_gpu_degenerate);
+    the periodic reduction needs d+1 generators a vertex, so a periodic lattice
+    returns HV_E_DEGENERATE instead of a mesh whose ties were broken by index."""
     hv = gpu_lib
+    m = _build(hv, _grid(d, k), hv.HV_METHOD_FAST)
+    assert m.max_signature() == 2 ** d
     with pytest.raises(hv.HVError) as e:
-        _build(hv, _grid(d, k), hv.HV_METHOD_FAST)
+        hv.Mesh(hv.default_context(), _grid(d, k), np.zeros(d), np.ones(d), hv.make_params(hv.HV_METHOD_FAST),
+                periodic=list(range(d)))
     assert e.value.code == hv._lib.HV_E_DEGENERATE
     _compare(hv, D.uniform_points(2, 30, 3), hv.HV_METHOD_FAST)  # the context stays usable
 
