@@ -123,27 +123,17 @@ struct Grp {
     }
 };
 
-// Bitonic sort of a[0 .. n2) in shared memory.  In a stage with j below the
-// bank period (32 four-byte or 16 eight-byte words) a warp's pairs span 64
-// consecutive keys and its x (and y) keys would fall twice on the same bank;
-// the upper half of each bank group of lanes (lanes & SW) reads and writes y
-// before x, so every access of the warp hits distinct banks.
 template <int NW, class K>
 __device__ void g_sort(K* a, int n2, const Grp<NW>& g) {
-    constexpr int SW = sizeof(K) == 4 ? 16 : 8;
-    const bool hi_lane = (g.rank & SW) != 0;
     g.sync();
     for (int k = 2; k <= n2; k <<= 1)
         for (int j = k >> 1; j > 0; j >>= 1) {
-            const bool sw = hi_lane && j < 2 * SW;
             for (int q = g.rank; q < (n2 >> 1); q += g.size) {
                 const int x = ((q & ~(j - 1)) << 1) | (q & (j - 1));
                 const int y = x | j;
-                const int f = sw ? y : x, s = sw ? x : y;
-                const K pf = a[f], ps = a[s];
-                const K p = sw ? ps : pf, r = sw ? pf : ps;
+                const K p = a[x], r = a[y];
                 const bool up = (x & k) == 0;
-                if ((p > r) == up) { a[f] = sw ? p : r; a[s] = sw ? r : p; }
+                if ((p > r) == up) { a[x] = r; a[y] = p; }
             }
             g.sync();
         }
