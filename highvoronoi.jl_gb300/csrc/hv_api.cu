@@ -1812,6 +1812,14 @@ int generic_polygon(hv_mesh* m, double* vol, double* area, bool dev_out) {
     return HV_OK;
 }
 
+// VI_POLYGON areas from every vertex's signed flag terms (hv_polyflag.cu)
+// unless HV_POLY_FLAGS=0 selects the face-lattice kernels for every facet.
+bool use_poly_flags(int d) {
+    const char* e = std::getenv("HV_POLY_FLAGS");
+    if (e && e[0] == '0') return false;
+    return d >= 3;
+}
+
 int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out) {
     if (m && m->own0 >= 0) {  // a shard holds only its own vertices
         m->ctx->err = "integrate the merged mesh, not a shard";
@@ -1889,12 +1897,38 @@ int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out) {
                 cap_b = (int)next_pow2((unsigned)b);
             }
         }
-        R.capV = cap_a;
-        while (R.capV > 4 && hv::poly_area_bytes(d, R.capV, 1, false) > (size_t)smax) R.capV /= 2;
-        kt.run(1, 1, [&] { run(2); });
         unsigned hs[3] = {0, 0, 0};
-        CK(cudaMemcpyAsync(hs, dstat, sizeof(hs), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
+        bool flags = use_poly_flags(d);
+        if (flags) {
+            // every vertex's share of its facets, summed per cell in vertex order;
+            // facets whose signed terms cancel go to the face-lattice kernels
+            hv::FlagRun F{};
+            F.d = d; F.n = n; F.V = m->V; F.planes = m->d_planes; F.pts = m->d_in; F.osig = m->osig; F.oc = m->oc;
+            F.nbr_off = m->nbr_off; F.nbr = m->nbr; F.inc_off = m->inc_off; F.inc = m->inc; F.foff = foff;
+            const size_t nsh = (size_t)std::max(m->V, 1u) * hv::flag_pairs(d);
+            F.share = s.get<double>(nsh);
+            F.sabs = s.get<float>(nsh);
+            F.area = R.area; F.big = R.big; F.nbig = R.nbig; F.maxnv = R.maxnv; F.status = dstat;
+            kt.run(1, 2, [&] {
+                hv::launch_vertex_flags(F, ctx->nsm, st);
+                hv::launch_cell_flags(F, ctx->nsm, st);
+            });
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(hs, dstat, sizeof(hs), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (hs[0] & 2u) {  // a singular generator subset: the face lattice for every facet
+                flags = false;
+                CK(cudaMemsetAsync(dstat, 0, 8 * sizeof(unsigned), st));
+                CK(cudaMemsetAsync(R.area, 0, sizeof(double) * std::max(ns, 1ll), st));
+            }
+        }
+        if (!flags) {
+            R.capV = cap_a;
+            while (R.capV > 4 && hv::poly_area_bytes(d, R.capV, 1, false) > (size_t)smax) R.capV /= 2;
+            kt.run(1, 1, [&] { run(2); });
+            CK(cudaMemcpyAsync(hs, dstat, sizeof(hs), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+        }
         if (hs[0] & 8u) throw HvError(HV_E_INTERNAL, "a facet is not a simple polytope (degenerate vertex)");
         const unsigned nbig = hs[1];
         if (hs[1] > 0) {  // tier B: facets over the tier-A caps, one block each, shared memory

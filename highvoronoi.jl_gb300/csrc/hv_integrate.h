@@ -62,6 +62,35 @@ struct PolyRun {
 };
 int launch_poly(const PolyRun& R);
 
+// VI_POLYGON areas from the vertices alone (hv_polyflag.cu): every vertex's
+// share of the facets through it (signed flag terms over the circumcentres of
+// its generator subsets), then per cell the shares in vertex order.  Facets
+// whose terms cancel go to big (the exact tier-B kernels); status bit 2: a
+// singular generator subset (the host then runs the face-lattice kernels).
+struct FlagRun {
+    int d, n;
+    unsigned V;
+    const DevPlane* planes;
+    const double* pts;
+    const int* osig;
+    const double* oc;
+    const long long* nbr_off;
+    const int* nbr;
+    const long long* inc_off;  // cell -> vertex rows, ascending
+    const int* inc;
+    const long long* foff;     // facet slot -> its vertex range (the incidence passes)
+    double* share;             // V x d(d+1)/2
+    float* sabs;               // V x d(d+1)/2: sum of the shares' |terms|
+    double* area;
+    long long* big;
+    unsigned* nbig;
+    unsigned* maxnv;
+    unsigned* status;
+};
+int flag_pairs(int d);
+void launch_vertex_flags(const FlagRun& F, int nsm, cudaStream_t st);
+void launch_cell_flags(const FlagRun& F, int nsm, cudaStream_t st);
+
 // Integrand quadrature of VI_POLYGON (hv_quad.cu): per facet of a lower cell
 // (slot t with a non-empty incidence range foff[t] .. foff[t+1]) the facet's
 // vertices in id order (qv), their flag weights (qw), the flag sum (qa) and the
