@@ -1812,12 +1812,12 @@ int generic_polygon(hv_mesh* m, double* vol, double* area, bool dev_out) {
     return HV_OK;
 }
 
-// VI_POLYGON areas from every vertex's signed flag terms (hv_polyflag.cu)
-// unless HV_POLY_FLAGS=0 selects the face-lattice kernels for every facet.
+// HV_POLY_FLAGS=1: VI_POLYGON areas from every vertex's signed flag terms
+// (hv_polyflag.cu) instead of the face-lattice kernels (slower on this GPU:
+// the subset solves are latency-bound; kept as an independent second method).
 bool use_poly_flags(int d) {
     const char* e = std::getenv("HV_POLY_FLAGS");
-    if (e && e[0] == '0') return false;
-    return d >= 3;
+    return d >= 3 && e && e[0] == '1';
 }
 
 int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out) {

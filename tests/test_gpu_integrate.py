@@ -127,3 +127,20 @@ def test_reference_method_and_integrator_names(gpu_lib):
         vd = hv.VoronoiData(g)
         np.testing.assert_array_equal(vd.vertex_sigs, base.vertex_sigs)
         np.testing.assert_array_equal(vd.volume, base.volume)
+
+
+@pytest.mark.parametrize("d,n,seed", [(3, 400, 11), (4, 200, 12), (5, 80, 13)])
+def test_vertex_flag_areas_match_the_face_lattice(gpu_lib, d, n, seed, monkeypatch):
+    """HV_POLY_FLAGS=1: the areas from every vertex's signed flag terms (the
+    reference's flag decomposition with circumcentres of generator subsets as
+    reference points) agree with the face-lattice kernels and the oracle."""
+    hv = gpu_lib
+    X = D.uniform_points(d, n, seed)
+    m = hv.Mesh(hv.default_context(), X, np.zeros(d), np.ones(d), hv.make_params(hv.HV_METHOD_FAST))
+    v0, a0 = m.polygon()
+    monkeypatch.setenv("HV_POLY_FLAGS", "1")
+    v1, a1 = m.polygon()
+    np.testing.assert_allclose(v1, v0, rtol=1e-10, atol=0)
+    np.testing.assert_allclose(a1, a0, rtol=1e-9, atol=1e-14)
+    rv, ra = O.OracleMesh(X, integrate=True).polygon()
+    np.testing.assert_allclose(v1, rv, rtol=1e-10, atol=0)
