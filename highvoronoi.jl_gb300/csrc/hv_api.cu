@@ -96,6 +96,13 @@ struct hv_mesh {
     long long* g_fend = nullptr;
     int* g_fvert = nullptr;
     bool allow_generic = false;   // a search that meets co-spherical generators walks them here
+    // the search's kd-tree, kept for hv_mesh_verify: points in Morton order,
+    // internal -> original ids, node boxes (2P x DP floats each)
+    double* t_pts = nullptr;
+    int* t_perm = nullptr;
+    float* t_blo = nullptr;
+    float* t_bhi = nullptr;
+    int t_leaf = 0, t_nleaves = 0, t_P = 0;
 };
 
 namespace {
@@ -559,7 +566,10 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     unsigned long long* codes = prep.get<unsigned long long>(n);
     unsigned long long* codes2 = prep.get<unsigned long long>(n);
     int* idx = prep.get<int>(n);
-    int* perm = prep.get<int>(n);
+    // the tree (Morton-ordered points, permutation, boxes) stays with the mesh
+    // for hv_mesh_verify
+    int* perm = dalloc<int>(st, n);
+    mesh->t_perm = perm;
     KTimer kt(ctx);
     kt.run(F_OTHER, 1, [&] { launch_morton(d, mesh->d_in, n, mesh->lo, mesh->hi, mesh->d_planes, mesh->np, codes, idx, dstat + 1, st); });
     {
@@ -567,7 +577,8 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         void* tmp = prep.get<char>(tb);
         sort_pairs_u64_i32(tmp, tb, codes, codes2, idx, perm, n, d * morton_bits(d, n), st);
     }
-    double* pts = prep.get<double>((size_t)n * d);
+    double* pts = dalloc<double>(st, (size_t)n * d);
+    mesh->t_pts = pts;
     float* pts32 = prep.get<float>((size_t)n * DP);
     float* pts32lo = prep.get<float>((size_t)n * DP);
     kt.run(F_OTHER, 1, [&] { launch_gather(d, mesh->d_in, perm, n, pts, pts32, pts32lo, st); });
@@ -605,8 +616,13 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     M.nleaves = (n + M.leaf - 1) / M.leaf;
     M.P = (int)next_pow2((unsigned long long)M.nleaves);
     M.pts = pts; M.pts32 = pts32; M.pts32lo = pts32lo; M.perm = perm;
-    float* blo = prep.get<float>((size_t)2 * M.P * DP);
-    float* bhi = prep.get<float>((size_t)2 * M.P * DP);
+    float* blo = dalloc<float>(st, (size_t)2 * M.P * DP);
+    float* bhi = dalloc<float>(st, (size_t)2 * M.P * DP);
+    mesh->t_blo = blo;
+    mesh->t_bhi = bhi;
+    mesh->t_leaf = M.leaf;
+    mesh->t_nleaves = M.nleaves;
+    mesh->t_P = M.P;
     unsigned* flags = prep.get<unsigned>((size_t)2 * M.P);
     CK(cudaMemsetAsync(flags, 0, sizeof(unsigned) * 2 * M.P, st));
     M.blo = blo; M.bhi = bhi;
@@ -1712,6 +1728,40 @@ int hv_mesh_vertices_csr(hv_mesh* m, int64_t* offs, int64_t* sig, double* r) {
     return HV_OK;
 }
 
+int hv_mesh_verify(hv_mesh* m, int64_t* inside, int64_t* ties, double* max_dev) {
+    if (!m || !inside) return HV_E_INVALID_ARG;
+    if (!m->t_pts && m->n > 0) {
+        m->ctx->err = "verification needs the search tree (a box, plane-domain or refined mesh)";
+        return HV_E_INVALID_ARG;
+    }
+    try {
+        CK(cudaSetDevice(m->ctx->device));
+        cudaStream_t st = m->ctx->stream;
+        unsigned long long h[3] = {0, 0, 0};
+        if (m->V) {
+            Scratch s(st);
+            unsigned long long* dc = s.get<unsigned long long>(3);
+            CK(cudaMemsetAsync(dc, 0, 3 * sizeof(unsigned long long), st));
+            hv::DevMesh M;
+            std::memset(&M, 0, sizeof(M));
+            M.d = m->d; M.n = m->n; M.np = m->np; M.planes = m->d_planes;
+            M.pts = m->t_pts; M.perm = m->t_perm; M.blo = m->t_blo; M.bhi = m->t_bhi;
+            M.leaf = m->t_leaf; M.nleaves = m->t_nleaves; M.P = m->t_P; M.dp = m->d <= 4 ? 4 : 8;
+            hv::launch_verify(M, m->d_in, m->V, m->g_max ? m->g_off : nullptr, m->g_max ? m->g_sig : m->osig, m->oc,
+                              dc, dc + 2, st);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(h, dc, sizeof(h), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+        }
+        *inside = (int64_t)h[0];
+        if (ties) *ties = (int64_t)h[1];
+        if (max_dev) { double dv; std::memcpy(&dv, &h[2], sizeof(dv)); *max_dev = dv; }
+    } catch (const HvError& e) {
+        return fail(m->ctx, e);
+    }
+    return HV_OK;
+}
+
 int hv_mesh_neighbors(hv_mesh* m, int64_t* offs, int64_t* nbr) {
     if (!m || !offs) return HV_E_INVALID_ARG;
     try {
@@ -2396,6 +2446,10 @@ int hv_mesh_free(hv_mesh* m) {
     dfree(st, m->g_fbeg);
     dfree(st, m->g_fend);
     dfree(st, m->g_fvert);
+    dfree(st, m->t_pts);
+    dfree(st, m->t_perm);
+    dfree(st, m->t_blo);
+    dfree(st, m->t_bhi);
     cudaStreamSynchronize(st);
     if (m->ext) hv_mesh_free(m->ext);
     delete m;

@@ -808,6 +808,79 @@ __global__ void k_gen_volumes(GenPoly P, const double* area, double* vol) {
     }
 }
 
+// The reference's vertex verification (verify_vertex / fraud_vertex,
+// src/raycast.jl:477-502, src/sysvoronoi.jl:527-552): no generator strictly
+// inside a vertex's sphere.  One thread per vertex: the deviation of its
+// generators from the sphere (points) or of the centre from their planes, a
+// ball query of the kd-tree, and the planes it does not carry.
+template <int D>
+__global__ void k_verify(DevMesh M, const double* x, unsigned V, const long long* off, const int* sig,
+                         const double* oc, unsigned long long* cnt, unsigned long long* maxdev) {
+    for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        const long long s0 = off ? off[v] : (long long)v * (D + 1);
+        const long long s1 = off ? off[v + 1] : s0 + D + 1;
+        const int* G = sig + s0;
+        const int m = (int)(s1 - s0);
+        double c[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) c[k] = oc[(size_t)v * D + k];
+        int a = -1;
+        for (int q = 0; q < m; ++q)
+            if (G[q] < M.n) { a = G[q]; break; }
+        if (a < 0) { atomicAdd(cnt, 1ull); continue; }
+        double r2 = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) { const double w = c[k] - x[(size_t)a * D + k]; r2 = fma(w, w, r2); }
+        const double rad = sqrt(r2);
+        double dev = 0.0;
+        for (int q = 0; q < m; ++q) {
+            const int it = G[q];
+            if (it < M.n) {
+                double s = 0.0;
+#pragma unroll
+                for (int k = 0; k < D; ++k) { const double w = c[k] - x[(size_t)it * D + k]; s = fma(w, w, s); }
+                dev = fmax(dev, fabs(s - r2) / r2);
+            } else {
+                dev = fmax(dev, fabs(plane_height<D>(M.planes[it - M.n], c)) / rad);
+            }
+        }
+        bool inside = false, tie = false;
+        for (int p = 0; p < M.np; ++p) {
+            if (in_sorted(G, m, M.n + p)) continue;
+            const double h = plane_height<D>(M.planes[p], c);
+            if (h < -1e-10 * rad) inside = true;
+            else if (h <= 1e-10 * rad) tie = true;
+        }
+        int stack[64];
+        int sp = 0;
+        stack[sp++] = 1;
+        while (sp > 0 && !inside) {
+            const int node = stack[--sp];
+            if (gen_box_dist2<D>(M, node, c) > r2 * (1.0 + 1e-9)) continue;
+            if (node >= M.P) {
+                const int l = node - M.P;
+                if (l >= M.nleaves) continue;
+                const int j0 = l * M.leaf, j1 = min(j0 + M.leaf, M.n);
+                for (int j = j0; j < j1; ++j) {
+                    if (in_sorted(G, m, M.perm[j])) continue;
+                    double s = 0.0;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) { const double w = c[k] - M.pts[(size_t)j * D + k]; s = fma(w, w, s); }
+                    if (s < r2 * (1.0 - 1e-10)) inside = true;
+                    else if (s <= r2 * (1.0 + 1e-10)) tie = true;
+                }
+            } else {
+                if (sp + 2 > 64) { inside = true; break; }
+                stack[sp++] = 2 * node + 1;
+                stack[sp++] = 2 * node;
+            }
+        }
+        if (inside) atomicAdd(cnt, 1ull);
+        if (tie) atomicAdd(cnt + 1, 1ull);
+        atomicMax(maxdev, (unsigned long long)__double_as_longlong(dev));
+    }
+}
+
 unsigned gen_grid(unsigned long long n, int bs, unsigned cap = 1u << 20) {
     unsigned long long g = (n + bs - 1) / bs;
     if (g < 1) g = 1;
@@ -906,6 +979,12 @@ void launch_gen_inc_emit(int n, unsigned V, const long long* off, const int* sig
                          long long* cnt, cudaStream_t st) {
     if (!V) return;
     k_gen_inc_emit<<<gen_grid(V, 256), 256, 0, st>>>(n, V, off, sig, keys, cnt);
+}
+
+void launch_verify(const DevMesh& M, const double* x, unsigned V, const long long* off, const int* sig,
+                   const double* oc, unsigned long long* cnt, unsigned long long* maxdev, cudaStream_t st) {
+    if (!V) return;
+    HV_DISPATCH(M.d, (k_verify<DD><<<gen_grid(V, 128), 128, 0, st>>>(M, x, V, off, sig, oc, cnt, maxdev)));
 }
 
 void launch_gen_polygon(const GenPoly& P, double* area, double* vol, int nsm, cudaStream_t st) {

@@ -103,4 +103,12 @@ struct GenPoly {
 };
 void launch_gen_polygon(const GenPoly& P, double* area, double* vol, int nsm, cudaStream_t st);
 
+// Vertex verification: cnt[0] += vertices with a generator strictly inside
+// their sphere (or their centre beyond a plane), cnt[1] += vertices with a
+// generator outside their signature on the sphere (relative 1e-10); maxdev =
+// bits of the largest relative deviation of a vertex's own generators.  Rows
+// of sig: off (CSR) or d+1 wide when off is null.
+void launch_verify(const DevMesh& M, const double* x, unsigned V, const long long* off, const int* sig,
+                   const double* oc, unsigned long long* cnt, unsigned long long* maxdev, cudaStream_t st);
+
 }  // namespace hv

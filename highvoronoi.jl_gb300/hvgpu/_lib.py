@@ -125,6 +125,7 @@ def load(path: str | None = None):
         L.hv_mesh_signature_total.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int)]
         L.hv_mesh_signature_total.restype = I
         L.hv_mesh_vertices_csr.argtypes = [P, ip, ip, dp]; L.hv_mesh_vertices_csr.restype = I
+        L.hv_mesh_verify.argtypes = [P, ip, ip, dp]; L.hv_mesh_verify.restype = I
         L.hv_mesh_neighbors.argtypes = [P, ip, ip]; L.hv_mesh_neighbors.restype = I
         L.hv_integrate_polygon.argtypes = [P, dp, dp]; L.hv_integrate_polygon.restype = I
         L.hv_integrate_heuristic_mc.argtypes = [P, I, U64, dp, dp]; L.hv_integrate_heuristic_mc.restype = I
@@ -383,6 +384,17 @@ class Mesh:
         r = np.zeros((V, self.d), dtype=np.float64)
         self.ctx.check(load().hv_mesh_vertices_csr(self._h, iptr(offs), iptr(sig), dptr(r)), "hv_mesh_vertices_csr")
         return offs, sig[:tot.value], r
+
+    def verify(self) -> dict:
+        """The device check of the reference's verify_vertex: vertices with a
+        generator strictly inside their sphere (``inside``, 0 for a correct
+        mesh), with another generator on it (``ties``), and the largest relative
+        deviation of a vertex's own generators from its sphere (``max_dev``)."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        dv = ctypes.c_double()
+        self.ctx.check(load().hv_mesh_verify(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(dv)),
+                       "hv_mesh_verify")
+        return {"inside": a.value, "ties": b.value, "max_dev": dv.value}
 
     def max_signature(self) -> int:
         """Longest vertex signature (d+1 unless generators are co-spherical)."""

@@ -174,6 +174,17 @@ int hv_mesh_vertices(hv_mesh* mesh, int64_t* sig, double* r);
  * order of the signatures (a shorter signature before its extensions). */
 int hv_mesh_signature_total(hv_mesh* mesh, int64_t* total, int* max_len);
 int hv_mesh_vertices_csr(hv_mesh* mesh, int64_t* offs, int64_t* sig, double* r);
+/* Vertex verification on the device, the check of the reference's
+ * verify_vertex / fraud_vertex (src/raycast.jl:477-502,
+ * src/sysvoronoi.jl:527-552): *inside = vertices with a generator strictly
+ * inside their sphere or a centre beyond a boundary plane (0 for a correct
+ * mesh); *ties = vertices with a generator outside their signature on their
+ * sphere (relative 1e-10; 0 unless generators are co-spherical and the
+ * vertex list is fixed-width); *max_dev = largest relative deviation of a
+ * vertex's own generators from its sphere (and of its planes).  Box,
+ * plane-domain, refined and generic meshes (the search's tree stays with the
+ * mesh); periodic meshes are HV_E_INVALID_ARG. */
+int hv_mesh_verify(hv_mesh* mesh, int64_t* inside, int64_t* ties, double* max_dev);
 /* Neighbour CSR: offs[n+1] (0-based offsets), nbr (1-based, sorted per cell,
  * planes as n+p). */
 int hv_mesh_neighbors(hv_mesh* mesh, int64_t* offs, int64_t* nbr);

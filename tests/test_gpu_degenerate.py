@@ -121,3 +121,18 @@ def test_lattice_monte_carlo_and_voronoi_data(gpu_lib):
     vol, area = m.heuristic_mc(2000, 7)
     assert abs(vol.sum() - 1.0) < 0.05
     assert np.all(np.abs(vol * k ** 3 - 1.0) < 0.25)
+
+
+@pytest.mark.parametrize("d,n,seed", [(2, 2000, 1), (3, 3000, 2), (4, 3000, 3), (5, 1500, 4), (6, 600, 5)])
+def test_device_verification_of_the_vertices(gpu_lib, d, n, seed):
+    """hv_mesh_verify (verify_vertex / fraud_vertex, src/raycast.jl:477-502):
+    no generator strictly inside any vertex's sphere and no extra generator on
+    it, on uniform, clustered and lattice inputs; the vertex's own generators
+    lie on its sphere to 1e-12."""
+    hv = gpu_lib
+    for X in (D.uniform_points(d, n, seed), D.clustered_points(d, n, seed)):
+        v = build(hv, X).verify()
+        assert v["inside"] == 0 and v["ties"] == 0 and v["max_dev"] < 1e-12, v
+    if d <= 4:
+        v = build(hv, lattice(d, 4)).verify()
+        assert v["inside"] == 0 and v["ties"] == 0 and v["max_dev"] < 1e-12, v
