@@ -1421,13 +1421,14 @@ int periodic_entry(hv_ctx* ctx, int d, int64_t n, const double* src, bool on_dev
             for (int k = 0; k < d; ++k) { elo[k] = lo[k] - B.delta[k]; ehi[k] = hi[k] + B.delta[k]; }
             DomainSpec dom;
             dom.lo = elo; dom.hi = ehi;
-            dom.generic_ok = false;
+            dom.generic_ok = true;  // co-spherical images: the public view takes lists of any length
             hv_mesh* ext = nullptr;
             int r = build_entry(ctx, d, n_ext, ext_pts, true, dom, &m->prm, &ext);
             if (r != HV_OK) throw HvError(r, ctx->err);
             ensure_neighbors(ext);
             CK(cudaMemsetAsync(dbad, 0, sizeof(unsigned), st));
-            launch_per_validate(B, ext->osig, ext->oc, ext->V, (int)n, (int)n_ext, ext->d_in, dbad, st);
+            launch_per_validate(B, ext->g_max ? ext->g_off : nullptr, ext->g_max ? ext->g_sig : ext->osig, ext->oc,
+                                ext->V, (int)n, (int)n_ext, ext->d_in, dbad, st);
             CK(cudaMemcpyAsync(hb, dbad, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
             if (hb[0] == 0) {
@@ -1450,18 +1451,32 @@ int periodic_entry(hv_ctx* ctx, int d, int64_t n, const double* src, bool on_dev
             long long* flag = vs.get<long long>((size_t)Ve + 1);
             long long* pos = vs.get<long long>((size_t)Ve + 1);
             int* ext2pub = vs.get<int>((size_t)std::max(Ve, 1u));
-            launch_pub_flag(d, e->osig, Ve, (int)n, flag, st);
+            const bool gen = e->g_max > 0;  // vertices with more than d+1 generators: CSR rows
+            const long long* eoff = gen ? e->g_off : nullptr;
+            const int* esig = gen ? e->g_sig : e->osig;
+            long long* len = gen ? vs.get<long long>((size_t)Ve + 1) : nullptr;
+            long long* rowpos = gen ? vs.get<long long>((size_t)Ve + 1) : nullptr;
+            launch_pub_flag(d, eoff, esig, Ve, (int)n, flag, len, st);
             size_t tb = scan_temp((int)Ve + 1);
             void* tmp = vs.get<char>(tb);
             exclusive_scan_i64(tmp, tb, flag, pos, (int)Ve + 1, st);
-            long long Vp = 0;
+            if (gen) exclusive_scan_i64(tmp, tb, len, rowpos, (int)Ve + 1, st);
+            long long Vp = 0, Sp = 0;
             CK(cudaMemcpyAsync(&Vp, pos + Ve, sizeof(long long), cudaMemcpyDeviceToHost, st));
+            if (gen) CK(cudaMemcpyAsync(&Sp, rowpos + Ve, sizeof(long long), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
             m->V = (unsigned)Vp;
-            m->osig = dalloc<int>(st, (size_t)std::max(Vp, 1ll) * (d + 1));
+            if (gen) {
+                m->g_max = e->g_max;
+                m->g_off = dalloc<long long>(st, (size_t)Vp + 1);
+                m->g_sig = dalloc<int>(st, (size_t)std::max(Sp, 1ll));
+                CK(cudaMemcpyAsync(m->g_off + Vp, &Sp, sizeof(long long), cudaMemcpyHostToDevice, st));
+            } else {
+                m->osig = dalloc<int>(st, (size_t)std::max(Vp, 1ll) * (d + 1));
+            }
             m->oc = dalloc<double>(st, (size_t)std::max(Vp, 1ll) * d);
-            launch_pub_fill(d, e->osig, e->oc, Ve, (int)n, n_ext, m->img_ref, m->img_code, pos, m->osig, m->oc,
-                            ext2pub, st);
+            launch_pub_fill(d, eoff, esig, e->oc, Ve, (int)n, n_ext, m->img_ref, m->img_code, pos, rowpos,
+                            gen ? m->g_off : nullptr, gen ? m->g_sig : m->osig, m->oc, ext2pub, st);
             long long tot = 0, ninc = 0;
             CK(cudaMemcpyAsync(&tot, e->nbr_off + n, sizeof(long long), cudaMemcpyDeviceToHost, st));
             CK(cudaMemcpyAsync(&ninc, e->inc_off + n, sizeof(long long), cudaMemcpyDeviceToHost, st));

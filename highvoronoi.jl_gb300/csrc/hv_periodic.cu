@@ -102,16 +102,19 @@ __global__ void k_in_box(const double* __restrict__ pts, int n, PerBox B, unsign
 }
 
 // A vertex of an original cell is exact when its circumsphere lies inside the
-// widened box on every periodic axis and it holds no widened face.
+// widened box on every periodic axis and it holds no widened face.  Rows of
+// osig: off (a CSR, vertices of any number of generators) or d+1 wide.
 template <int D>
-__global__ void k_per_validate(const int* __restrict__ osig, const double* __restrict__ oc, unsigned V, int n,
-                               int n_ext, const double* __restrict__ ext, PerBox B, unsigned* bad) {
+__global__ void k_per_validate(const long long* __restrict__ off, const int* __restrict__ osig,
+                               const double* __restrict__ oc, unsigned V, int n, int n_ext,
+                               const double* __restrict__ ext, PerBox B, unsigned* bad) {
     for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        const int* s = osig + (size_t)v * (D + 1);
+        const long long s0 = off ? off[v] : (long long)v * (D + 1);
+        const int m = off ? (int)(off[v + 1] - s0) : D + 1;
+        const int* s = osig + s0;
         if (s[0] >= n) continue;  // sorted: s[0] is the smallest item
         bool ok = true;
-#pragma unroll
-        for (int k = 0; k <= D; ++k) {
+        for (int k = 0; k < m; ++k) {
             const int it = s[k];
             if (it >= n_ext && ((B.pmask >> ((it - n_ext) >> 1)) & 1)) ok = false;
         }
@@ -139,32 +142,51 @@ __device__ __forceinline__ void map_item(int e, int n, int n_ext, const int* ref
     else { id = n + (e - n_ext); code = center; }
 }
 
-__global__ void k_pub_flag(const int* __restrict__ osig, unsigned V, int dp1, int n, long long* flag) {
-    for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
-        flag[v] = osig[(size_t)v * dp1] < n ? 1 : 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) flag[V] = 0;
+// flag[v] = 1 for the vertices of original cells; len[v] their signature
+// length (0 for the others), so that a scan of len places the public rows
+template <int D>
+__global__ void k_pub_flag(const long long* __restrict__ off, const int* __restrict__ osig, unsigned V, int n,
+                           long long* flag, long long* len) {
+    for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        const long long s0 = off ? off[v] : (long long)v * (D + 1);
+        const bool pub = osig[s0] < n;
+        flag[v] = pub ? 1 : 0;
+        if (len) len[v] = pub ? (off ? off[v + 1] - s0 : D + 1) : 0;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        flag[V] = 0;
+        if (len) len[V] = 0;
+    }
 }
 
+constexpr int PUB_MAXSIG = 64;  // generators of one vertex
+
 template <int D>
-__global__ void k_pub_fill(const int* __restrict__ osig, const double* __restrict__ oc, unsigned V, int n, int n_ext,
-                           const int* __restrict__ ref, const short* __restrict__ icode,
-                           const long long* __restrict__ pos, int* psig, double* pc, int* ext2pub) {
+__global__ void k_pub_fill(const long long* __restrict__ off, const int* __restrict__ osig,
+                           const double* __restrict__ oc, unsigned V, int n, int n_ext, const int* __restrict__ ref,
+                           const short* __restrict__ icode, const long long* __restrict__ pos,
+                           const long long* __restrict__ rowpos, long long* poff, int* psig, double* pc,
+                           int* ext2pub) {
     const int center = (pow3(D) - 1) / 2;
     for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        const int* s = osig + (size_t)v * (D + 1);
+        const long long s0 = off ? off[v] : (long long)v * (D + 1);
+        const int m = off ? (int)(off[v + 1] - s0) : D + 1;
+        const int* s = osig + s0;
         if (s[0] >= n) { ext2pub[v] = -1; continue; }
         const long long p = pos[v];
         ext2pub[v] = (int)p;
-        int m[D + 1];
-#pragma unroll
-        for (int k = 0; k <= D; ++k) { int code; map_item(s[k], n, n_ext, ref, icode, center, m[k], code); }
-#pragma unroll
-        for (int a = 1; a <= D; ++a)
-#pragma unroll
-            for (int b = a; b > 0; --b)
-                if (m[b] < m[b - 1]) { const int t = m[b]; m[b] = m[b - 1]; m[b - 1] = t; }
-#pragma unroll
-        for (int k = 0; k <= D; ++k) psig[(size_t)p * (D + 1) + k] = m[k];
+        const long long dst = rowpos ? rowpos[v] : p * (D + 1);
+        if (poff) poff[p] = dst;
+        int mm[PUB_MAXSIG];
+        const int mc = m < PUB_MAXSIG ? m : PUB_MAXSIG;
+        for (int k = 0; k < mc; ++k) {
+            int code, id;
+            map_item(s[k], n, n_ext, ref, icode, center, id, code);
+            int b = k;
+            while (b > 0 && mm[b - 1] > id) { mm[b] = mm[b - 1]; --b; }
+            mm[b] = id;
+        }
+        for (int k = 0; k < mc; ++k) psig[dst + k] = mm[k];
 #pragma unroll
         for (int k = 0; k < D; ++k) pc[(size_t)p * D + k] = oc[(size_t)v * D + k];
     }
@@ -249,19 +271,21 @@ void launch_img_fill(const PerBox& B, const double* pts, int n, const long long*
     if (n <= 0) return;
     HV_DISPATCH(B.d, (k_img_fill<DD><<<grid_of(n, 128), 128, 0, st>>>(pts, n, B, off, ext, ref, icode)));
 }
-void launch_per_validate(const PerBox& B, const int* osig, const double* oc, unsigned V, int n, int n_ext,
-                         const double* ext, unsigned* bad, cudaStream_t st) {
+void launch_per_validate(const PerBox& B, const long long* off, const int* osig, const double* oc, unsigned V,
+                         int n, int n_ext, const double* ext, unsigned* bad, cudaStream_t st) {
     if (!V) return;
-    HV_DISPATCH(B.d, (k_per_validate<DD><<<grid_of(V, 256), 256, 0, st>>>(osig, oc, V, n, n_ext, ext, B, bad)));
+    HV_DISPATCH(B.d, (k_per_validate<DD><<<grid_of(V, 256), 256, 0, st>>>(off, osig, oc, V, n, n_ext, ext, B, bad)));
 }
-void launch_pub_flag(int d, const int* osig, unsigned V, int n, long long* flag, cudaStream_t st) {
-    k_pub_flag<<<grid_of(V, 256), 256, 0, st>>>(osig, V, d + 1, n, flag);
+void launch_pub_flag(int d, const long long* off, const int* osig, unsigned V, int n, long long* flag,
+                     long long* len, cudaStream_t st) {
+    HV_DISPATCH(d, (k_pub_flag<DD><<<grid_of(V, 256), 256, 0, st>>>(off, osig, V, n, flag, len)));
 }
-void launch_pub_fill(int d, const int* osig, const double* oc, unsigned V, int n, int n_ext, const int* ref,
-                     const short* icode, const long long* pos, int* psig, double* pc, int* ext2pub, cudaStream_t st) {
+void launch_pub_fill(int d, const long long* off, const int* osig, const double* oc, unsigned V, int n, int n_ext,
+                     const int* ref, const short* icode, const long long* pos, const long long* rowpos,
+                     long long* poff, int* psig, double* pc, int* ext2pub, cudaStream_t st) {
     if (!V) return;
-    HV_DISPATCH(d, (k_pub_fill<DD><<<grid_of(V, 256), 256, 0, st>>>(osig, oc, V, n, n_ext, ref, icode, pos, psig, pc,
-                                                                      ext2pub)));
+    HV_DISPATCH(d, (k_pub_fill<DD><<<grid_of(V, 256), 256, 0, st>>>(off, osig, oc, V, n, n_ext, ref, icode, pos,
+                                                                      rowpos, poff, psig, pc, ext2pub)));
 }
 void launch_pub_nbr(int d, int n, int n_ext, const long long* off, const int* nbr, const int* ref, const short* icode,
                     int* pnbr, signed char* pshift, int* perm, cudaStream_t st) {

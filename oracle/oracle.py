@@ -403,13 +403,31 @@ def periodic_margin_ok(ext_sig, ext_r, ext_pts, n, n_ext, lo, hi, periodic, delt
     return bool(np.all(inside[:, per]))
 
 
-def periodic_mesh(pts, lo, hi, periodic, delta=None, integrate=False, nthreads=0):
+def _margin_ok_csr(eoff, esig, er, ext_pts, n, n_ext, lo, hi, periodic, delta):
+    """periodic_margin_ok for vertices of any number of generators (CSR rows)."""
+    per = np.asarray(periodic, dtype=bool)
+    lo, hi, delta = (np.asarray(a, dtype=np.float64) for a in (lo, hi, delta))
+    for v in range(len(eoff) - 1):
+        s = esig[eoff[v]:eoff[v + 1]]
+        if s[0] > n:
+            continue
+        pl = s[s > n_ext]
+        if np.any(per[(pl - n_ext - 1) // 2]):
+            return False
+        R = np.linalg.norm(er[v] - ext_pts[s[0] - 1]) * (1 + 1e-12) + 1e-12
+        if not np.all(((er[v] - R > lo - delta) & (er[v] + R < hi + delta))[per]):
+            return False
+    return True
+
+
+def periodic_mesh(pts, lo, hi, periodic, delta=None, integrate=False, nthreads=0, generic=False):
     """The periodic tessellation of ``pts`` in the cuboid [lo, hi] (periodic
     axes flagged) from the oracle's mesh of the extended generator set.  With
     delta None the margin grows from 1.5 spacings by 1.5 until certified.
     Returns a dict: delta, sig (V, d+1) 1-based original ids (rows sorted),
     r, offs, nbr (1-based, sorted by (id, shift code)), shift (nnbr, d) and,
-    if integrate, vol and area."""
+    if integrate, vol and area.  generic=True meshes the extended set with the
+    generic walk (lattices): sig is then a CSR, sig_offs (V+1) and sig."""
     pts = np.ascontiguousarray(pts, dtype=np.float64)
     n, d = pts.shape
     lo = np.asarray(lo, dtype=np.float64)
@@ -423,9 +441,14 @@ def periodic_mesh(pts, lo, hi, periodic, delta=None, integrate=False, nthreads=0
         img, ref, sh = periodic_images(pts, lo, hi, per, dl)
         ext = np.vstack([pts, img])
         n_ext = len(ext)
-        M = OracleMesh(ext, lo=lo - dl, hi=hi + dl, integrate=integrate, nthreads=nthreads)
-        es, er = M.vertices()
-        if delta is not None or periodic_margin_ok(es, er, ext, n, n_ext, lo, hi, per, dl):
+        M = OracleMesh(ext, lo=lo - dl, hi=hi + dl, integrate=integrate, nthreads=nthreads, generic=generic)
+        if generic:
+            eoff, esig, er = M.vertices_csr()
+            ok = _margin_ok_csr(eoff, esig, er, ext, n, n_ext, lo, hi, per, dl)
+        else:
+            es, er = M.vertices()
+            ok = periodic_margin_ok(es, er, ext, n, n_ext, lo, hi, per, dl)
+        if delta is not None or ok:
             break
         if np.all(dl[per] >= 0.999 * L[per]):
             raise RuntimeError("too few generators for the periodic image margin")
@@ -437,9 +460,15 @@ def periodic_mesh(pts, lo, hi, periodic, delta=None, integrate=False, nthreads=0
     codes[n + 1:n_ext + 1] = (sh + 1) @ weights
     ids[n + 1:n_ext + 1] = ref + 1
     ids[n_ext + 1:] = n + np.arange(1, 2 * d + 1)
-    pub = es[:, 0] <= n
-    psig = np.sort(ids[es[pub]], axis=1)
-    pr = er[pub]
+    if generic:
+        rows = [np.sort(ids[esig[eoff[v]:eoff[v + 1]]]) for v in range(len(eoff) - 1) if esig[eoff[v]] <= n]
+        pr = er[np.array([esig[eoff[v]] <= n for v in range(len(eoff) - 1)], dtype=bool)]
+        psig_offs = np.concatenate([[0], np.cumsum([len(x) for x in rows])]).astype(np.int64)
+        psig = np.concatenate(rows) if rows else np.zeros(0, dtype=np.int64)
+    else:
+        pub = es[:, 0] <= n
+        psig = np.sort(ids[es[pub]], axis=1)
+        pr = er[pub]
     eo, en = M.neighbors()
     offs = eo[:n + 1].copy()
     tot = int(offs[-1])
@@ -450,6 +479,8 @@ def periodic_mesh(pts, lo, hi, periodic, delta=None, integrate=False, nthreads=0
     c = codes[en[:tot]][order]
     shift = np.stack([(c // 3 ** k) % 3 - 1 for k in range(d)], axis=1).astype(np.int8)
     out = dict(delta=dl, sig=psig, r=pr, offs=offs, nbr=nbr, shift=shift, nimages=len(img), ref=ref + 1, ref_shift=sh)
+    if generic:
+        out["sig_offs"] = psig_offs
     if integrate:
         vol, area = M.polygon()
         out["vol"] = vol[:n]

@@ -136,3 +136,29 @@ def test_device_verification_of_the_vertices(gpu_lib, d, n, seed):
     if d <= 4:
         v = build(hv, lattice(d, 4)).verify()
         assert v["inside"] == 0 and v["ties"] == 0 and v["max_dev"] < 1e-12, v
+
+
+@pytest.mark.parametrize("d,k,per", [(2, 4, [1, 1]), (2, 5, [1, 0]), (3, 3, [1, 1, 1]), (3, 4, [0, 1, 1])])
+def test_periodic_lattice_matches_the_oracle(gpu_lib, d, k, per):
+    """Periodic cuboids of lattice points (the reference's periodic_grid
+    geometry): the images are co-spherical too; the public view keeps every
+    generator of a vertex, against the oracle's generic walk of the same
+    extended set (the GPU's image margin)."""
+    hv = gpu_lib
+    X = lattice(d, k)
+    m = hv.Mesh(hv.default_context(), X, np.zeros(d), np.ones(d), hv.make_params(hv.HV_METHOD_FAST), periodic=per)
+    delta, ref, sh = m.periodic_images()
+    P = O.periodic_mesh(X, np.zeros(d), np.ones(d), per, delta=delta, integrate=True, generic=True)
+    offs, sig, r = m.vertices_csr()
+    np.testing.assert_array_equal(offs, P["sig_offs"])
+    np.testing.assert_array_equal(sig, P["sig"])
+    np.testing.assert_allclose(r, P["r"], rtol=0, atol=1e-13)
+    o, nb = m.neighbors()
+    np.testing.assert_array_equal(o, P["offs"])
+    np.testing.assert_array_equal(nb, P["nbr"])
+    np.testing.assert_array_equal(m.periodic_shifts(), P["shift"])
+    assert np.all(np.diff(o) == 2 * d)
+    v, a = m.polygon()
+    np.testing.assert_allclose(v, P["vol"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(a, P["area"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(v, np.full(len(X), float(k) ** -d), rtol=1e-12)

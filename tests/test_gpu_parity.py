@@ -184,19 +184,21 @@ def _grid(d, k):
 
 
 @pytest.mark.parametrize("d,k", [(2, 6), (3, 4)])
-def test_lattice_points_in_periodic_cuboids_are_refused(gpu_lib, d, k):
-    """Lattice points put more than d+1 generators on one empty sphere.  A box
-    build walks such vertices with all their generators (test_gpu_degenerate);
-    the periodic reduction needs d+1 generators a vertex, so a periodic lattice
-    returns HV_E_DEGENERATE instead of a mesh whose ties were broken by index."""
+def test_lattice_points_in_box_and_periodic_cuboids(gpu_lib, d, k):
+    """Lattice points put more than d+1 generators on one empty sphere: box and
+    periodic builds keep all of them (the generic walk; test_gpu_degenerate has
+    the oracle comparisons), every cell has volume k^-d, and the context stays
+    usable for a general-position build afterwards."""
     hv = gpu_lib
     m = _build(hv, _grid(d, k), hv.HV_METHOD_FAST)
     assert m.max_signature() == 2 ** d
-    with pytest.raises(hv.HVError) as e:
-        hv.Mesh(hv.default_context(), _grid(d, k), np.zeros(d), np.ones(d), hv.make_params(hv.HV_METHOD_FAST),
+    p = hv.Mesh(hv.default_context(), _grid(d, k), np.zeros(d), np.ones(d), hv.make_params(hv.HV_METHOD_FAST),
                 periodic=list(range(d)))
-    assert e.value.code == hv._lib.HV_E_DEGENERATE
-    _compare(hv, D.uniform_points(2, 30, 3), hv.HV_METHOD_FAST)  # the context stays usable
+    offs, sig, r = p.vertices_csr()
+    assert np.all(np.diff(offs) == 2 ** d)
+    v, _ = p.polygon()
+    np.testing.assert_allclose(v, np.full(k ** d, float(k) ** -d), rtol=1e-12)
+    _compare(hv, D.uniform_points(2, 30, 3), hv.HV_METHOD_FAST)
 
 
 @pytest.mark.parametrize("d,k,eps", [(2, 20, 1e-9), (3, 8, 1e-9), (4, 4, 1e-8), (3, 6, 1e-12)])
