@@ -549,7 +549,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         return;
     }
     Scratch prep(st);
-    // the side streams' kernels use this build's scratch: drain them before it is
+    // the side streams' kernels use the mesh build's scratch: drain them before it is
     // freed (also when an error unwinds the build)
     struct Drain {
         cudaStream_t s2, s3;

@@ -96,7 +96,7 @@ struct LevelQueues {
 struct DevMesh {
     int d, n;
     LevelQueues G;
-    // generators own0 .. own1-1 (internal order) belong to this build; a shard
+    // generators own0 .. own1-1 (internal order) belong to this mesh; a shard
     // of a mesh split over ranks walks only edges that keep one of them and
     // keeps the vertices whose smallest generator is one of them (0, n: all)
     int own0, own1;
