@@ -193,7 +193,7 @@ def test_lattice_points_in_box_and_periodic_cuboids(gpu_lib, d, k):
     m = _build(hv, _grid(d, k), hv.HV_METHOD_FAST)
     assert m.max_signature() == 2 ** d
     p = hv.Mesh(hv.default_context(), _grid(d, k), np.zeros(d), np.ones(d), hv.make_params(hv.HV_METHOD_FAST),
-                periodic=list(range(d)))
+                periodic=[1] * d)
     offs, sig, r = p.vertices_csr()
     assert np.all(np.diff(offs) == 2 ** d)
     v, _ = p.polygon()
