@@ -162,3 +162,25 @@ def test_periodic_lattice_matches_the_oracle(gpu_lib, d, k, per):
     np.testing.assert_allclose(v, P["vol"], rtol=1e-12, atol=0)
     np.testing.assert_allclose(a, P["area"], rtol=1e-12, atol=0)
     np.testing.assert_allclose(v, np.full(len(X), float(k) ** -d), rtol=1e-12)
+
+
+@pytest.mark.parametrize("d,k", [(2, 8), (3, 6)])
+def test_lattice_in_a_simplex_domain(gpu_lib, d, k):
+    """Lattice points in the simplex {x > 0, sum x < 1} (a plane domain): the
+    walk starts at a corner of the domain polytope; the cells tile the simplex,
+    every vertex's sphere is empty and carries all its generators."""
+    import math
+    hv = gpu_lib
+    X = lattice(d, k)
+    X = X[X.sum(axis=1) < 1.0 - 0.5 / k]
+    base = np.array([np.zeros(d) for _ in range(d)] + [np.full(d, 1.0 / d)])
+    normal = np.array([-np.eye(d)[q] for q in range(d)] + [np.ones(d)])
+    m = hv.Mesh(hv.default_context(), np.ascontiguousarray(X), None, None, hv.make_params(hv.HV_METHOD_FAST),
+                planes=(base, normal, None))
+    assert m.max_signature() == 2 ** d
+    v = m.verify()
+    assert v["inside"] == 0 and v["ties"] == 0 and v["max_dev"] < 1e-12, v
+    vol, _ = m.polygon()
+    assert abs(vol.sum() - 1.0 / math.factorial(d)) < 1e-12
+    inner = X.sum(axis=1) < 1.0 - 1.5 * d / k  # every face neighbour present, the square inside the simplex
+    np.testing.assert_allclose(vol[inner], float(k) ** -d, rtol=1e-12)
