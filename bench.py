@@ -65,6 +65,7 @@ def parse():
     ap.add_argument("--mc-dirs", type=int, default=1000, help="directions per cell of VI_HEURISTIC_MC")
     ap.add_argument("--no-c3", action="store_true", help="skip the 5D clustered 50k measurement")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 arm of the 5D measurement")
+    ap.add_argument("--no-lattice", action="store_true", help="skip the 3D lattice (co-spherical generators)")
     return ap.parse_args()
 
 
@@ -258,6 +259,38 @@ def poly_flops(d, V):
     with E_cell = d V_cell / 2 and sum V_cell = (d+1) V (the flags of the
     reference's decomposition)."""
     return d * (d + 1) * V / 2.0 * math.factorial(d - 1) * 2 * d * d
+
+
+def run_lattice(ctx, flush):
+    """Co-spherical generators: a 3D lattice of 32^3 points (8 on every interior
+    vertex's sphere) -- the search meets the ties and walks the vertex graph
+    with vertices of any size; build and VI_POLYGON times, CUDA events."""
+    import torch
+    import hvgpu
+    k, d = 32, 3
+    g = (np.arange(k) + 0.5) / k
+    pts = np.ascontiguousarray(np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, d))
+    lo, hi = np.zeros(d), np.ones(d)
+    prm = hvgpu.make_params(hvgpu.HV_METHOD_FAST)
+    hvgpu.Mesh(ctx, pts, lo, hi, prm).free()  # warm-up
+    times, ptimes = [], []
+    for _ in range(3):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m = hvgpu.Mesh(ctx, pts, lo, hi, prm)
+        times.append((time.perf_counter() - t0) * 1e3)
+        t1 = time.perf_counter()
+        vol, _ = m.polygon()
+        ptimes.append((time.perf_counter() - t1) * 1e3)
+        V = m.counts()[0]
+        mx = m.max_signature()
+        m.free()
+    ms = statistics.median(times)
+    return {"workload": "3d_lattice_32", "n_points": int(len(pts)), "vertices": int(V), "max_signature": int(mx),
+            "ms_build": ms, "vertices_per_s": V / (ms / 1e3), "ms_polygon": statistics.median(ptimes),
+            "volume_sum": float(vol.sum()), "timing": "host wall clock of hv_mesh_build (fast search until the "
+            "first tie, then the generic walk) and of hv_integrate_polygon"}
 
 
 def run_c3(args, ctx, local, flush, clocks):
@@ -576,6 +609,12 @@ def run_ours(args):
             c3 = run_c3(args, ctx, local, flush, clocks)
         except Exception as e:  # the headline line must still print
             c3 = {"error": repr(e)}
+    lattice = None
+    if not args.no_lattice and ws == 1:
+        try:
+            lattice = run_lattice(ctx, flush)
+        except Exception as e:  # the headline line must still print
+            lattice = {"error": repr(e)}
     serving = None
     if not args.no_serve and ws == 1:
         try:
@@ -597,7 +636,7 @@ def run_ours(args):
                                           "fallback_nodes", "fallback_leaves", "fallback_points",
                                           "ambiguous_sets")},
             "rays_per_s": st0["rays"] / (tot_ms / 1e3 / args.steps),
-            "breakdown_ms": breakdown, "c3_5d_clustered_50k": c3, "serving": serving}
+            "breakdown_ms": breakdown, "c3_5d_clustered_50k": c3, "lattice": lattice, "serving": serving}
     print(json.dumps(line), flush=True)
 
 
