@@ -214,7 +214,7 @@ def run_serve(args, device):
                     continue
                 lat.append(r["latency_ms"])
                 svc.append(r["service_ms"])
-                verts += r["sig"].shape[0]
+                verts += len(r["sig"])
             t_end = time.perf_counter() - t0
         return np.array(lat), np.array(svc), fails, verts, t_end
 

@@ -38,7 +38,7 @@ struct Job {
     int rc = HV_OK;
     std::string err;
     clk::time_point t_submit, t_start, t_end;
-    std::vector<int64_t> sig, offs, nbr;
+    std::vector<int64_t> sig, offs, nbr, sig_offs;
     std::vector<double> r, vol, area;
     int64_t nverts = 0, nnbr = 0;
     hv_stats stats;
@@ -89,13 +89,22 @@ void run_job(hv_ctx* ctx, Job& J) {
     if (rc == HV_OK) {
         int64_t nv = 0, nn = 0;
         rc = hv_mesh_counts(m, &nv, &nn);
+        int64_t tot = 0;
+        int maxlen = 0;
+        if (rc == HV_OK) rc = hv_mesh_signature_total(m, &tot, &maxlen);
         if (rc == HV_OK) {
             J.nverts = nv; J.nnbr = nn;
-            J.sig.resize((size_t)nv * (q.d + 1));
             J.r.resize((size_t)nv * q.d);
             J.offs.resize((size_t)q.n + 1);
             J.nbr.resize((size_t)std::max<int64_t>(nn, 1));
-            rc = hv_mesh_vertices(m, J.sig.data(), J.r.data());
+            if (maxlen > q.d + 1) {  // co-spherical generators: the signatures as a CSR
+                J.sig.resize((size_t)std::max<int64_t>(tot, 1));
+                J.sig_offs.resize((size_t)nv + 1);
+                rc = hv_mesh_vertices_csr(m, J.sig_offs.data(), J.sig.data(), J.r.data());
+            } else {
+                J.sig.resize((size_t)nv * (q.d + 1));
+                rc = hv_mesh_vertices(m, J.sig.data(), J.r.data());
+            }
         }
         if (rc == HV_OK) rc = hv_mesh_neighbors(m, J.offs.data(), J.nbr.data());
         if (rc == HV_OK && !J.periodic.empty()) {
@@ -262,6 +271,7 @@ int hv_server_wait(hv_server* S, int64_t ticket, double timeout_ms, hv_result* o
         out->area = J->area.empty() ? nullptr : J->area.data();
         out->stats = J->stats;
         out->shift = J->shift.empty() ? nullptr : J->shift.data();
+        out->sig_offs = J->sig_offs.empty() ? nullptr : J->sig_offs.data();
     }
     out->queue_ms = ms(J->t_submit, J->t_start);
     out->service_ms = ms(J->t_start, J->t_end);

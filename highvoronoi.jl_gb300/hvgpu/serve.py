@@ -35,7 +35,7 @@ class _Result(ctypes.Structure):
                 ("nbr", ctypes.POINTER(ctypes.c_int64)), ("vol", ctypes.POINTER(ctypes.c_double)),
                 ("area", ctypes.POINTER(ctypes.c_double)), ("queue_ms", ctypes.c_double),
                 ("service_ms", ctypes.c_double), ("latency_ms", ctypes.c_double), ("stats", _lib.Stats),
-                ("shift", ctypes.POINTER(ctypes.c_int8))]
+                ("shift", ctypes.POINTER(ctypes.c_int8)), ("sig_offs", ctypes.POINTER(ctypes.c_int64))]
 
 
 def _bind():
@@ -118,8 +118,14 @@ class Server:
         d, n, V, E = r.d, r.n, r.nverts, r.nnbr
         out = {"status": r.status, "queue_ms": r.queue_ms, "service_ms": r.service_ms, "latency_ms": r.latency_ms}
         if r.status == _lib.HV_OK:
+            if r.sig_offs:  # co-spherical generators: one array per vertex
+                so = _arr(r.sig_offs, V + 1, np.int64)
+                flat = _arr(r.sig, int(so[-1]), np.int64)
+                sig = [flat[so[v]:so[v + 1]] for v in range(V)]
+            else:
+                sig = _arr(r.sig, V * (d + 1), np.int64).reshape(V, d + 1)
             out.update({
-                "sig": _arr(r.sig, V * (d + 1), np.int64).reshape(V, d + 1),
+                "sig": sig,
                 "r": _arr(r.r, V * d, np.float64).reshape(V, d),
                 "offs": _arr(r.offs, n + 1, np.int64),
                 "nbr": _arr(r.nbr, E, np.int64),

@@ -396,6 +396,8 @@ typedef struct {
     double latency_ms;       /* submission -> result ready */
     hv_stats stats;
     const int8_t* shift;     /* d x nnbr lattice shifts of the neighbours (periodic requests), else NULL */
+    const int64_t* sig_offs; /* nverts+1 row offsets of sig when a vertex has more than d+1 generators
+                                (co-spherical generators, hv_mesh_vertices_csr); NULL: sig is (d+1) wide */
 } hv_result;
 
 int hv_server_start(const hv_server_config* cfg, hv_server** out);

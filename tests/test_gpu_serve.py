@@ -93,3 +93,26 @@ def test_served_periodic_and_plane_domains(gpu_lib):
     np.testing.assert_array_equal(rs["sig"], ms.vertices()[0])
     np.testing.assert_array_equal(rs["vol"], ms.polygon()[0])
     assert rs["shift"] is None and rb["shift"] is None
+
+
+def test_lattice_requests_return_every_generator(gpu_lib):
+    """A lattice request served next to general-position ones: its vertices
+    carry all their co-spherical generators (a CSR in the result), as a direct
+    build gives them."""
+    from hvgpu.serve import Server
+    hv = gpu_lib
+    g = (np.arange(5) + 0.5) / 5
+    lat = np.ascontiguousarray(np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3))
+    with Server(slots=4) as s:
+        tk = [s.submit(D.uniform_points(3, 300, 1), integrator="polygon"), s.submit(lat, integrator="polygon"),
+              s.submit(D.uniform_points(4, 200, 2), integrator="polygon")]
+        res = [s.result(t) for t in tk]
+    assert all(r["status"] == 0 for r in res)
+    m = hv.Mesh(hv.default_context(), lat, np.zeros(3), np.ones(3), hv.make_params(hv.HV_METHOD_FAST))
+    offs, sig, r = m.vertices_csr()
+    got = res[1]["sig"]
+    assert len(got) == len(offs) - 1 and max(len(x) for x in got) == 8
+    np.testing.assert_array_equal(np.concatenate(got), sig)
+    np.testing.assert_array_equal(res[1]["r"], r)
+    np.testing.assert_allclose(res[1]["vol"], np.full(len(lat), 0.2 ** 3), rtol=1e-12)
+    assert res[0]["sig"].shape[1] == 4 and res[2]["sig"].shape[1] == 5
