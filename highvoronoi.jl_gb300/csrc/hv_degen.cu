@@ -387,9 +387,13 @@ __global__ void __launch_bounds__(128) k_gen_walk(GenRun R, unsigned ne) {
                     consider((cj - ca) / den, jo);
                 }
             } else {
+                // the child nearer the vertex first: the generators met first along
+                // the edge lie near it, and the ball shrinks before the farther
+                // child is tested
                 if (sp + 2 > 64) { over = true; break; }
-                stack[sp++] = 2 * node + 1;
-                stack[sp++] = 2 * node;
+                const double dl = gen_box_dist2<D>(R.M, 2 * node, c), dr = gen_box_dist2<D>(R.M, 2 * node + 1, c);
+                if (dl <= dr) { stack[sp++] = 2 * node + 1; stack[sp++] = 2 * node; }
+                else { stack[sp++] = 2 * node; stack[sp++] = 2 * node + 1; }
             }
         }
         if (!isfinite(tb) || over) { atomicOr(R.status, over ? GS_WIDE : GS_NUMERIC); continue; }
