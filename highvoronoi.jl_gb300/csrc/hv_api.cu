@@ -319,13 +319,16 @@ bool domain_corner(const hv_mesh* mesh, double* v) {
 // on its sphere (hv_degen.cu); the result is a CSR of generator lists in place
 // of the fixed-width vertex list, and the neighbour lists keep the pairs that
 // share a full interface.  The device tree, points and planes of the search
-// (M) are reused.
-void generic_build(hv_ctx* ctx, hv_mesh* mesh, const hv::DevMesh& M) {
+// (M) are reused; the walk starts from the search's vertices (seed_sig,
+// nseed x (d+1) internal ids) when there are any, else from a domain corner.
+void generic_build(hv_ctx* ctx, hv_mesh* mesh, const hv::DevMesh& M, const int* seed_sig = nullptr,
+                   unsigned nseed = 0) {
     using namespace hv;
     cudaStream_t st = ctx->stream;
     const int d = mesh->d, n = mesh->n;
     double corner[HV_MAXD];
-    if (!domain_corner(mesh, corner)) throw HvError(HV_E_INTERNAL, "degenerate walk: no corner of the domain found");
+    if (nseed == 0 && !domain_corner(mesh, corner))
+        throw HvError(HV_E_INTERNAL, "degenerate walk: no corner of the domain found");
     int W = std::min(GMAX, std::max(2 * (d + 1), (1 << d) + 2 * d));
     const unsigned long long vest = (unsigned long long)(vertices_per_point(d) * n) + (1ull << d) + 1024;
     for (int attempt = 0;; ++attempt) {
@@ -353,11 +356,6 @@ void generic_build(hv_ctx* ctx, hv_mesh* mesh, const hv::DevMesh& M) {
             CK(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
         };
-        double* dcorner = s.get<double>(d);
-        CK(cudaMemcpyAsync(dcorner, corner, sizeof(double) * d, cudaMemcpyHostToDevice, st));
-        launch_gen_seed(R, dcorner, st);
-        CK(cudaGetLastError());
-        read();
         std::unique_ptr<Scratch> es;
         auto grow_edges = [&](unsigned need) {
             es.reset(new Scratch(st));
@@ -371,7 +369,20 @@ void generic_build(hv_ctx* ctx, hv_mesh* mesh, const hv::DevMesh& M) {
             R.rc = es->get<double>((size_t)R.rcap * d);
             R.rwin = es->get<unsigned>(R.rcap);
         };
-        grow_edges(64u * (d + 1));
+        grow_edges(std::max(64u * (d + 1), nseed));
+        if (nseed > 0) {  // many starting points: the levels span the gaps between them
+            launch_gen_seeds(R, seed_sig, nseed, ctx->nsm, st);
+            CK(cudaGetLastError());
+            read();
+            launch_gen_insert(R, hc[1], st);
+            launch_gen_commit(R, hc[1], st);
+        } else {
+            double* dcorner = s.get<double>(d);
+            CK(cudaMemcpyAsync(dcorner, corner, sizeof(double) * d, cudaMemcpyHostToDevice, st));
+            launch_gen_seed(R, dcorner, st);
+        }
+        CK(cudaGetLastError());
+        read();
         unsigned f0 = 0, f1 = hc[0];
         long long levels = 0;
         while (!hc[3] && f1 > f0) {
@@ -630,7 +641,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     M.cnt = dcnt;
     kt.run(F_OTHER, 1, [&] { launch_bvh(M, blo, bhi, flags, st); });
     // ---- candidate lists
-    const bool fast = mesh->prm.method == HV_METHOD_FAST;
+    const bool fast = mesh->prm.method != HV_METHOD_PLAIN;  // HV_METHOD_GENERIC: its walk starts from the descent
     int K = mesh->prm.knn > 0 ? mesh->prm.knn : default_knn(d);
     K = std::min(K, std::max(n - 1, 0));
     K = std::min(K, 480);
@@ -677,8 +688,8 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
     };
     std::unique_ptr<Scratch> srch;
     unsigned V = 0;
-    if (mesh->prm.method == HV_METHOD_GENERIC) degen_abort = true;  // the walk needs only the tree
-    for (int attempt = 0; !degen_abort; ++attempt) {
+    unsigned nseed = 0;  // vertices found before a hand-over to the generic walk
+    for (int attempt = 0;; ++attempt) {
         if (attempt > 4) throw HvError(HV_E_CAPACITY, "vertex capacity retries exhausted");
         unsigned long long vcap64 = (unsigned long long)(est * factor * (double)(1ull << attempt));
         if (vcap64 > 0xFFFFFFF0ull / 8) throw HvError(HV_E_CAPACITY, "vertex count beyond 32-bit ids");
@@ -767,6 +778,7 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         const unsigned overflow_bits = ST_VCAP | ST_HASH | ST_QUEUE | ST_ECAP;
         bool overflow = (ctx->h_stat[1] & overflow_bits) != 0;
         if (!overflow) fatal(ctx->h_stat[1]);
+        if (!overflow && mesh->prm.method == HV_METHOD_GENERIC) degen_abort = true;  // the walk from the seeds
         unsigned f0 = 0, f1 = std::min(ctx->h_stat[0], vcap);
         if (degen_abort) f1 = 0;
         if (!overflow && !degen_abort) kt.run(F_CENTERS, 1, [&] { launch_centers(M, 0, f1, ctx->nsm, st); });
@@ -931,7 +943,12 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
             f0 = f1; f1 = f2;
             ++levels;
         }
-        if (degen_abort) break;
+        if (degen_abort) {
+            // the vertices found so far start the generic walk (read at the last level check)
+            read_stat(ctx, dstat);
+            nseed = std::min(ctx->h_stat[0], vcap);
+            break;
+        }
         if (overflow) { S.capacity_retries++; continue; }
         V = f1;
         S.levels = levels;
@@ -939,15 +956,15 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         break;
     }
     CK(cudaEventRecord(ev.e[2], st));
-    if (degen_abort || mesh->prm.method == HV_METHOD_GENERIC) {
-        srch.reset();
+    if (degen_abort) {
         unsigned long long hc[C_NCOUNT];
         CK(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         S.rays = (int64_t)hc[C_RAYS];
         S.degenerate = (int64_t)hc[C_DEGEN];
         S.descents = (int64_t)hc[C_DESCENT];
-        generic_build(ctx, mesh, M);
+        generic_build(ctx, mesh, M, M.vsig, nseed);
+        srch.reset();
         S.ms_prepare = ms_between(ev.e[0], ev.e[1]);
         S.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         return;

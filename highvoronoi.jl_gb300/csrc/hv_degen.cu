@@ -535,6 +535,75 @@ __global__ void __launch_bounds__(SEED_T) k_gen_seed(GenRun R, const double* v) 
     *R.vcnt = 1;
 }
 
+// Records of the search's vertices (d+1 internal ids each; the search broke
+// the ties by index, but every sphere it found is empty): each completed with
+// every generator on its sphere, so that the walk starts from all of them.
+template <int D>
+__global__ void __launch_bounds__(128) k_gen_seeds(GenRun R, const int* vsig, unsigned nseed) {
+    for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < nseed; v += gridDim.x * blockDim.x) {
+        int sig[D + 1];
+#pragma unroll
+        for (int k = 0; k <= D; ++k) {
+            const int it = vsig[(size_t)v * (D + 1) + k];
+            sig[k] = it < R.M.n ? R.M.perm[it] : it;
+        }
+        for (int a = 1; a <= D; ++a) {
+            const int x = sig[a];
+            int b = a - 1;
+            while (b >= 0 && sig[b] > x) { sig[b + 1] = sig[b]; --b; }
+            sig[b + 1] = x;
+        }
+        double c[D];
+        if (!gen_centre<D>(R, sig, D + 1, c)) continue;  // a singular system: other seeds remain
+        double ca = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) { const double w = c[k] - R.x[(size_t)sig[0] * D + k]; ca = fma(w, w, ca); }
+        const double rad = sqrt(ca);
+        int G[GMAX];
+        int m = 0;
+        bool over = false;
+        auto add = [&](int it) {
+            if (m == GMAX) { over = true; return; }
+            int x = m++;
+            while (x > 0 && G[x - 1] > it) { G[x] = G[x - 1]; --x; }
+            G[x] = it;
+        };
+        int stack[64];
+        int sp = 0;
+        stack[sp++] = 1;
+        while (sp > 0 && !over) {
+            const int node = stack[--sp];
+            if (gen_box_dist2<D>(R.M, node, c) > ca * (1.0 + 4.0 * GEN_REL) + 1e-300) continue;
+            if (node >= R.M.P) {
+                const int l = node - R.M.P;
+                if (l >= R.M.nleaves) continue;
+                const int s0 = l * R.M.leaf, s1 = min(s0 + R.M.leaf, R.M.n);
+                for (int j = s0; j < s1; ++j) {
+                    double dj = 0.0;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        const double w = c[k] - R.M.pts[(size_t)j * D + k];
+                        dj = fma(w, w, dj);
+                    }
+                    if (fabs(dj - ca) <= 2.0 * GEN_REL * ca) add(R.M.perm[j]);
+                }
+            } else {
+                if (sp + 2 > 64) { over = true; break; }
+                stack[sp++] = 2 * node + 1;
+                stack[sp++] = 2 * node;
+            }
+        }
+        for (int p = 0; p < R.M.np; ++p)
+            if (fabs(plane_height<D>(R.M.planes[p], c)) <= GEN_REL * (rad + 1e-300)) add(R.M.n + p);
+        if (over || m > R.W) { atomicOr(R.status, GS_WIDE); continue; }
+        const unsigned r = atomicAdd(R.rcnt, 1u);  // rcap >= nseed
+        for (int q = 0; q < m; ++q) R.rsig[(size_t)r * R.W + q] = G[q];
+        R.rlen[r] = m;
+        R.rwin[r] = 0;
+        if (!gen_centre<D>(R, G, m, R.rc + (size_t)r * D)) atomicOr(R.status, GS_NUMERIC);
+    }
+}
+
 // ---- output
 struct GenLess {
     const int* vsig;
@@ -905,6 +974,11 @@ unsigned gen_grid(unsigned long long n, int bs, unsigned cap = 1u << 20) {
 
 void launch_gen_seed(const GenRun& R, const double* corner, cudaStream_t st) {
     HV_DISPATCH(R.M.d, (k_gen_seed<DD><<<1, SEED_T, 0, st>>>(R, corner)));
+}
+
+void launch_gen_seeds(const GenRun& R, const int* vsig, unsigned nseed, int nsm, cudaStream_t st) {
+    if (!nseed) return;
+    HV_DISPATCH(R.M.d, (k_gen_seeds<DD><<<gen_grid(nseed, 128, (unsigned)nsm * 16), 128, 0, st>>>(R, vsig, nseed)));
 }
 
 void launch_gen_edges(const GenRun& R, unsigned f0, unsigned f1, int nsm, cudaStream_t st) {

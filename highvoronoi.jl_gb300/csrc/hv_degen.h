@@ -52,6 +52,9 @@ struct GenRun {
 // Vertex 0: the domain corner (d doubles, device), the planes through it and
 // its nearest generators.
 void launch_gen_seed(const GenRun& R, const double* corner, cudaStream_t st);
+// Level-0 records from the search's vertices (vsig: nseed x (d+1) internal
+// ids), each completed with every generator on its sphere (rcap >= nseed).
+void launch_gen_seeds(const GenRun& R, const int* vsig, unsigned nseed, int nsm, cudaStream_t st);
 void launch_gen_edges(const GenRun& R, unsigned f0, unsigned f1, int nsm, cudaStream_t st);
 void launch_gen_walk(const GenRun& R, unsigned ne, int nsm, cudaStream_t st);
 void launch_gen_insert(const GenRun& R, unsigned nrec, cudaStream_t st);
