@@ -758,22 +758,11 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         read_stat(ctx, dstat);
         if (fast && (ctx->h_stat[0] == 0 || restricted) && !(ctx->h_stat[1] & (ST_VCAP | ST_HASH))) {
             // no FP32 seed was decided (or a shard, whose every cell needs its
-            // seed): the exact descent on the undecided ones.  Where co-spherical
-            // generators hand the build to the generic walk, a few seeds first:
-            // lattice points tie in every seed, and a tie there ends the search
-            bool probed_tie = false;
-            if (mesh->allow_generic && !restricted) {
-                kt.run(F_DESCENT, 1, [&] { launch_descent_exact(M, std::min(nseeds, 128), dseed, dfail, ndfail,
-                                                                ctx->nsm, st); });
-                CK(cudaGetLastError());
-                read_stat(ctx, dstat);
-                probed_tie = (ctx->h_stat[1] & ST_DEGEN) != 0;
-            }
-            if (!probed_tie) {
-                kt.run(F_DESCENT, 1, [&] { launch_descent_exact(M, nseeds, dseed, dfail, ndfail, ctx->nsm, st); });
-                CK(cudaGetLastError());
-                read_stat(ctx, dstat);
-            }
+            // seed): the exact descent on the undecided ones (on lattice points,
+            // every seed; the vertices it finds start the generic walk)
+            kt.run(F_DESCENT, 1, [&] { launch_descent_exact(M, nseeds, dseed, dfail, ndfail, ctx->nsm, st); });
+            CK(cudaGetLastError());
+            read_stat(ctx, dstat);
         }
         const unsigned overflow_bits = ST_VCAP | ST_HASH | ST_QUEUE | ST_ECAP;
         bool overflow = (ctx->h_stat[1] & overflow_bits) != 0;
