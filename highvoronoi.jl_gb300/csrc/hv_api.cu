@@ -756,10 +756,17 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         kt.run(F_DESCENT, 1, [&] { launch_descent(M, stride, nseeds, dseed, dfail, ndfail, ctx->nsm, st); });
         CK(cudaGetLastError());
         read_stat(ctx, dstat);
-        if (fast && (ctx->h_stat[0] == 0 || restricted) && !(ctx->h_stat[1] & (ST_VCAP | ST_HASH))) {
+        unsigned nundecided = 0;
+        if (fast && mesh->allow_generic && ctx->h_stat[0] != 0 && !restricted) {
+            CK(cudaMemcpyAsync(&nundecided, ndfail, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+        }
+        // a quarter of the seeds undecided in FP32: ties everywhere (lattice points),
+        // and the seeds' vertices will start the generic walk -- find them all
+        const bool tied = 4ull * nundecided > (unsigned long long)nseeds;
+        if (fast && (ctx->h_stat[0] == 0 || restricted || tied) && !(ctx->h_stat[1] & (ST_VCAP | ST_HASH))) {
             // no FP32 seed was decided (or a shard, whose every cell needs its
-            // seed): the exact descent on the undecided ones (on lattice points,
-            // every seed; the vertices it finds start the generic walk)
+            // seed): the exact descent on the undecided ones
             kt.run(F_DESCENT, 1, [&] { launch_descent_exact(M, nseeds, dseed, dfail, ndfail, ctx->nsm, st); });
             CK(cudaGetLastError());
             read_stat(ctx, dstat);
