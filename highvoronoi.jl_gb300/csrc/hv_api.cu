@@ -773,7 +773,10 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         }
         const unsigned overflow_bits = ST_VCAP | ST_HASH | ST_QUEUE | ST_ECAP;
         bool overflow = (ctx->h_stat[1] & overflow_bits) != 0;
-        if (!overflow) fatal(ctx->h_stat[1]);
+        // seeds that tie in every direction may find no vertex at all: with the
+        // generic walk ahead, the others start it
+        if (!overflow && tied && mesh->allow_generic && (ctx->h_stat[1] & ST_DESCENT)) degen_abort = true;
+        if (!overflow && !degen_abort) fatal(ctx->h_stat[1]);
         if (!overflow && mesh->prm.method == HV_METHOD_GENERIC) degen_abort = true;  // the walk from the seeds
         unsigned f0 = 0, f1 = std::min(ctx->h_stat[0], vcap);
         if (degen_abort) f1 = 0;
