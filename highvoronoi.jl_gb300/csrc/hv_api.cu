@@ -757,13 +757,16 @@ void build_impl(hv_ctx* ctx, hv_mesh* mesh, const double* d_src, bool src_on_dev
         CK(cudaGetLastError());
         read_stat(ctx, dstat);
         unsigned nundecided = 0;
-        if (fast && mesh->allow_generic && ctx->h_stat[0] != 0 && !restricted) {
+        if (fast && d == 2 && mesh->allow_generic && ctx->h_stat[0] != 0 && !restricted) {
             CK(cudaMemcpyAsync(&nundecided, ndfail, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
         }
         // a quarter of the seeds undecided in FP32: ties everywhere (lattice points),
-        // and the seeds' vertices will start the generic walk -- find them all
-        const bool tied = 4ull * nundecided > (unsigned long long)nseeds;
+        // and the seeds' vertices will start the generic walk -- find them all.
+        // In 2D only: there the exact descent of tied seeds is cheap (200^2
+        // lattice: 34 ms, walk levels 401 -> 5), in 3D and 4D each tied descent
+        // costs more than the levels it saves (32^3: 66 ms -> 1.9 s)
+        const bool tied = d == 2 && 4ull * nundecided > (unsigned long long)nseeds;
         if (fast && (ctx->h_stat[0] == 0 || restricted || tied) && !(ctx->h_stat[1] & (ST_VCAP | ST_HASH))) {
             // no FP32 seed was decided (or a shard, whose every cell needs its
             // seed): the exact descent on the undecided ones
