@@ -327,8 +327,8 @@ void generic_build(hv_ctx* ctx, hv_mesh* mesh, const hv::DevMesh& M, const int* 
     cudaStream_t st = ctx->stream;
     const int d = mesh->d, n = mesh->n;
     double corner[HV_MAXD];
-    if (nseed == 0 && !domain_corner(mesh, corner))
-        throw HvError(HV_E_INTERNAL, "degenerate walk: no corner of the domain found");
+    const bool have_corner = domain_corner(mesh, corner);
+    if (nseed == 0 && !have_corner) throw HvError(HV_E_INTERNAL, "degenerate walk: no corner of the domain found");
     int W = std::min(GMAX, std::max(2 * (d + 1), (1 << d) + 2 * d));
     const unsigned long long vest = (unsigned long long)(vertices_per_point(d) * n) + (1ull << d) + 1024;
     for (int attempt = 0;; ++attempt) {
@@ -376,7 +376,10 @@ void generic_build(hv_ctx* ctx, hv_mesh* mesh, const hv::DevMesh& M, const int* 
             read();
             launch_gen_insert(R, hc[1], st);
             launch_gen_commit(R, hc[1], st);
-        } else {
+            CK(cudaGetLastError());
+            read();
+        }
+        if (hc[0] == 0 && have_corner && !hc[3]) {  // no seed survived (or none given): the corner
             double* dcorner = s.get<double>(d);
             CK(cudaMemcpyAsync(dcorner, corner, sizeof(double) * d, cudaMemcpyHostToDevice, st));
             launch_gen_seed(R, dcorner, st);

@@ -596,11 +596,14 @@ __global__ void __launch_bounds__(128) k_gen_seeds(GenRun R, const int* vsig, un
         for (int p = 0; p < R.M.np; ++p)
             if (fabs(plane_height<D>(R.M.planes[p], c)) <= GEN_REL * (rad + 1e-300)) add(R.M.n + p);
         if (over || m > R.W) { atomicOr(R.status, GS_WIDE); continue; }
+        double cg[D];
+        if (!gen_centre<D>(R, G, m, cg)) continue;  // other seeds remain
         const unsigned r = atomicAdd(R.rcnt, 1u);  // rcap >= nseed
         for (int q = 0; q < m; ++q) R.rsig[(size_t)r * R.W + q] = G[q];
         R.rlen[r] = m;
         R.rwin[r] = 0;
-        if (!gen_centre<D>(R, G, m, R.rc + (size_t)r * D)) atomicOr(R.status, GS_NUMERIC);
+#pragma unroll
+        for (int k = 0; k < D; ++k) R.rc[(size_t)r * D + k] = cg[k];
     }
 }
 
