@@ -15,7 +15,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libhvgpu.so")
 SOURCES = ["hv_prep.cu", "hv_search.cu", "hv_search_d2.cu", "hv_search_d3.cu", "hv_search_d4.cu",
            "hv_search_d5.cu", "hv_search_d6.cu", "hv_post.cu", "hv_integrate.cu", "hv_poly.cu", "hv_api.cu", "hv_server.cpp", "hv_noalloc.cu",
-           "hv_domain.cu", "hv_periodic.cu", "hv_quad.cu", "hv_degen.cu", "hv_polyflag.cu"]
+           "hv_domain.cu", "hv_periodic.cu", "hv_quad.cu", "hv_degen.cu", "hv_polyflag.cu", "hv_polylat.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
 

@@ -1919,6 +1919,128 @@ bool use_poly_flags(int d) {
     return d >= 3 && e && e[0] == '1';
 }
 
+// VI_POLYGON over the face lattice of the whole mesh (hv_polylat.cu) from
+// d = 5 on (HV_POLY_LATTICE=0 / 1 turns it off / on for every d >= 3); its
+// tables are indexed by 32-bit entries, so larger meshes take the per-facet
+// kernels.
+bool use_poly_lattice(int d, unsigned V, long long nslots) {
+    int from = 5;
+    if (const char* e = std::getenv("HV_POLY_LATTICE")) from = e[0] == '0' ? 99 : e[0] == '1' ? 3 : from;
+    if (d < std::max(from, 3) || d > 6) return false;
+    long long emax = 0;
+    for (int c = 1; c < d; ++c) emax = std::max(emax, (long long)hv::lat_subsets(d, c));
+    return (long long)V * emax < (1ll << 31) - 2 && nslots < (1ll << 31) - 2;
+}
+
+// The interface areas of a mesh of simple vertices through the mesh-wide face
+// lattice into area (nslots, zeroed); build time in kt family 0, volumes in 1.
+void poly_lattice(hv_mesh* m, double* area, int* slot_cell, unsigned* dstat, Scratch& s, KTimer& kt) {
+    cudaStream_t st = m->ctx->stream;
+    const int d = m->d, n = m->n;
+    const unsigned V = m->V;
+    const long long ns = m->nnbr;
+    hv::LatIn L{};
+    L.d = d; L.n = n; L.V = V; L.planes = m->d_planes; L.pts = m->d_in; L.osig = m->osig; L.oc = m->oc;
+    L.nbr_off = m->nbr_off; L.nbr = m->nbr; L.status = dstat;
+    auto sync_read = [&](const void* dev, void* host, size_t b) {
+        CK(cudaMemcpyAsync(host, dev, b, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    };
+    int gbits = 1;
+    while ((1ll << gbits) <= (long long)n + m->np + 1) ++gbits;
+    std::vector<long long> nf(d + 1, 0);
+    std::vector<unsigned*> fref(d + 1, nullptr);
+    std::vector<unsigned char*> fmask(d + 1, nullptr);
+    std::vector<long long*> off(d + 1, nullptr);
+    std::vector<int*> child(d + 1, nullptr), lgen(d + 1, nullptr);
+    unsigned* fref2 = nullptr;
+    // level 1: facet slots
+    std::unique_ptr<Scratch> fprev(new Scratch(st));
+    int* Fp = fprev->get<int>((size_t)V * hv::lat_subsets(d, 1));
+    fref[1] = s.get<unsigned>((size_t)std::max(ns, 1ll));
+    nf[1] = ns;
+    CK(cudaMemsetAsync(fref[1], 0xFF, sizeof(unsigned) * std::max(ns, 1ll), st));
+    kt.run(0, 2, [&] { hv::launch_lat_facets(L, Fp, fref[1], slot_cell, st); });
+    CK(cudaGetLastError());
+    long long emax = 1;
+    for (int c = 2; c < d; ++c) emax = std::max(emax, (long long)V * hv::lat_subsets(d, c));
+    auto* keys = s.get<unsigned long long>((size_t)emax + 1);
+    auto* keys2 = s.get<unsigned long long>((size_t)emax + 1);
+    int* vals = s.get<int>((size_t)emax);
+    int* vals2 = s.get<int>((size_t)emax);
+    const size_t sort_tb = hv::sort_pairs_u64_i32_temp((int)emax);
+    void* sort_tmp = s.get<char>(sort_tb);
+    const size_t scan_tb = hv::scan_temp((int)std::max(emax, ns) + 1);
+    void* scan_tmp = s.get<char>(scan_tb);
+    auto* nvalid = s.get<unsigned long long>(1);
+    auto* cnt = s.get<unsigned long long>((size_t)std::max(emax, ns) + 1);
+    // the child lists of the parents at level c (children at level c + 1)
+    auto pairs = [&](int c, const int* Fc) {
+        const long long nG = nf[c];
+        CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (nG + 1), st));
+        off[c] = s.get<long long>((size_t)nG + 1);
+        kt.run(0, 2, [&] {
+            hv::launch_lat_pairs(L, c, nf[c + 1], fref[c + 1], fmask[c + 1], Fc, fref[c], cnt, nullptr, nullptr,
+                                 nullptr, false, st);
+            hv::exclusive_scan_i64(scan_tmp, scan_tb, (const long long*)cnt, off[c], (int)nG + 1, st);
+        });
+        long long np = 0;
+        sync_read(off[c] + nG, &np, sizeof(long long));
+        child[c] = s.get<int>((size_t)std::max(np, 1ll));
+        lgen[c] = s.get<int>((size_t)std::max(np, 1ll));
+        CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (nG + 1), st));
+        kt.run(0, 1, [&] {
+            hv::launch_lat_pairs(L, c, nf[c + 1], fref[c + 1], fmask[c + 1], Fc, fref[c], cnt, off[c], child[c],
+                                 lgen[c], true, st);
+        });
+        CK(cudaGetLastError());
+    };
+    for (int c = 2; c < d; ++c) {
+        const long long E = (long long)V * hv::lat_subsets(d, c);
+        std::unique_ptr<Scratch> fcur(new Scratch(st));
+        int* Fc = fcur->get<int>((size_t)std::max(E, 1ll));
+        int fbits = 1;
+        while ((1ll << fbits) < nf[c - 1]) ++fbits;
+        CK(cudaMemsetAsync(nvalid, 0, sizeof(unsigned long long), st));
+        kt.run(0, 2, [&] {
+            hv::launch_lat_entries(L, c, gbits, Fp, keys, vals, Fc, nvalid, st);
+            hv::sort_pairs_u64_i32(sort_tmp, sort_tb, keys, keys2, vals, vals2, (int)E, std::min(64, gbits + fbits), st);
+        });
+        CK(cudaGetLastError());
+        unsigned long long nval = 0;
+        sync_read(nvalid, &nval, sizeof(nval));
+        long long* heads = (long long*)keys;  // the unsorted keys are spent
+        long long* fidx = (long long*)keys2;  // and the sorted ones once the heads are marked
+        kt.run(0, 2, [&] {
+            hv::launch_lat_heads((long long)nval, keys2, heads, st);
+            hv::exclusive_scan_i64(scan_tmp, scan_tb, heads, fidx, (int)nval + 1, st);
+        });
+        sync_read(fidx + nval, &nf[c], sizeof(long long));
+        fref[c] = s.get<unsigned>((size_t)std::max(nf[c], 1ll));
+        fmask[c] = s.get<unsigned char>((size_t)std::max(nf[c], 1ll));
+        if (c == d - 1) fref2 = s.get<unsigned>((size_t)std::max(nf[c], 1ll));
+        kt.run(0, 1, [&] {
+            hv::launch_lat_scatter(L, c, (long long)nval, fidx, vals2, Fc, fref[c], fmask[c],
+                                   c == d - 1 ? fref2 : nullptr, st);
+        });
+        CK(cudaGetLastError());
+        pairs(c - 1, Fp);
+        fprev = std::move(fcur);
+        Fp = Fc;
+    }
+    fprev.reset();
+    // volumes, bottom-up
+    std::vector<double*> vol(d + 1, nullptr);
+    for (int c = d - 2; c >= 1; --c) {
+        vol[c] = c == 1 ? area : s.get<double>((size_t)std::max(nf[c], 1ll));
+        kt.run(1, 1, [&] {
+            hv::launch_lat_volumes(L, c, nf[c], off[c], child[c], lgen[c], fref[c], fmask[c], slot_cell, fref[c + 1],
+                                   c + 1 == d - 1 ? fref2 : nullptr, vol[c + 1], vol[c], st);
+        });
+        CK(cudaGetLastError());
+    }
+}
+
 int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out) {
     if (m && m->own0 >= 0) {  // a shard holds only its own vertices
         m->ctx->err = "integrate the merged mesh, not a shard";
@@ -1969,6 +2091,28 @@ int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out) {
             if (hv::launch_poly(R) != 0) throw HvError(HV_E_CUDA, "polygon integrator launch failed");
             CK(cudaGetLastError());
         };
+        if (use_poly_lattice(d, m->V, ns) && !use_poly_flags(d)) {
+            poly_lattice(m, R.area, R.slot_cell, dstat, s, kt);
+            unsigned h0 = 0;
+            CK(cudaMemcpyAsync(&h0, dstat, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (h0 & 8u) throw HvError(HV_E_INTERNAL, "a face is not a simple polytope (degenerate vertex)");
+            run(4);
+            if (!dev_out) {
+                CK(cudaMemcpyAsync(vol, R.vol, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+                if (ns > 0) CK(cudaMemcpyAsync(area, R.area, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+            }
+            CK(cudaStreamSynchronize(st));
+            double fam[F_N];
+            kt.totals(fam);
+            m->st.poly_big_facets = 0;
+            m->st.ms_poly_incidence = fam[0];
+            m->st.ms_poly_facets = fam[1];
+            m->st.ms_poly_big = 0;
+            m->st.ms_poly_total =
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            return HV_OK;
+        }
         // facet -> vertex incidences
         size_t scan_tb = hv::scan_temp((int)(ns + 1));
         void* scan_tmp = s.get<char>(scan_tb);

@@ -62,6 +62,43 @@ struct PolyRun {
 };
 int launch_poly(const PolyRun& R);
 
+// VI_POLYGON over the face lattice of the whole mesh (hv_polylat.cu), d >= 3.
+// Level 1: F1[rank * V + v] = the facet slot of each generator pair of vertex
+// v (-1 when its smaller generator is a plane), fref1[t] = the facet's smallest
+// vertex (0xFFFFFFFF: no vertex, a slot of the higher cell).  Level c >= 2:
+// entries (key, entry index rank * V + v) for every (c+1)-subset of every
+// signature (lat_subsets(d, c) per vertex), sorted over the key's low bits;
+// heads -> exclusive scan -> face index per entry (Fc), first vertex and mask
+// per face (fref, fmask; fref2 = the second vertex of an edge).  Pairs: the
+// child faces of level c+1 listed under their parents of level c.  Volumes:
+// bottom-up; level 1 writes A_ik into both slots.  status bit 8: a face that is
+// not simple or a signature pair that is not a neighbour pair.
+struct LatIn {
+    int d, n;
+    unsigned V;
+    const DevPlane* planes;
+    const double* pts;
+    const int* osig;
+    const double* oc;
+    const long long* nbr_off;
+    const int* nbr;
+    unsigned* status;
+};
+int lat_subsets(int d, int c);  // C(d+1, c+1): the (c+1)-subsets of a signature
+void launch_lat_facets(const LatIn& L, int* F1, unsigned* fref1, int* slot_cell, cudaStream_t st);
+void launch_lat_entries(const LatIn& L, int c, int gbits, const int* Fp, unsigned long long* keys, int* vals, int* Fc,
+                        unsigned long long* nvalid, cudaStream_t st);
+void launch_lat_heads(long long nval, const unsigned long long* sk, long long* flags, cudaStream_t st);
+void launch_lat_scatter(const LatIn& L, int c, long long nval, const long long* fidx, const int* sv, int* Fc,
+                        unsigned* fref, unsigned char* fmask, unsigned* fref2, cudaStream_t st);
+void launch_lat_pairs(const LatIn& L, int c, long long nH, const unsigned* frefH, const unsigned char* fmaskH,
+                      const int* Fc, const unsigned* frefG, unsigned long long* cnt, const long long* off, int* child,
+                      int* lgen, bool fill, cudaStream_t st);
+void launch_lat_volumes(const LatIn& L, int c, long long nG, const long long* off, int* child, int* lgen,
+                        const unsigned* frefG, const unsigned char* fmaskG, const int* slot_cell,
+                        const unsigned* frefH, const unsigned* fref2H, const double* volH, double* volG,
+                        cudaStream_t st);
+
 // VI_POLYGON areas from the vertices alone (hv_polyflag.cu): every vertex's
 // share of the facets through it (signed flag terms over the circumcentres of
 // its generator subsets), then per cell the shares in vertex order.  Facets

@@ -34,8 +34,9 @@
 #include <algorithm>
 #include <vector>
 
-#include "hv_internal.cuh"
 #include "hv_integrate.h"
+#include "hv_internal.cuh"
+#include "hv_polygeo.cuh"
 
 namespace hv {
 
@@ -230,69 +231,6 @@ template <int D>
 __device__ __forceinline__ void vload(const PolyIn& P, unsigned v, double* x) {
 #pragma unroll
     for (int q = 0; q < D; ++q) x[q] = P.oc[(size_t)v * D + q];
-}
-
-// |(p - a) ^ (b - a)| = dist(p, line ab) * |b - a| (twice the triangle's area),
-// by Lagrange's identity as the root of the sum of the squared 2x2 minors; each
-// minor is formed with one rounding (FMA), so there is no cancellation beyond it.
-template <int D>
-__device__ __forceinline__ double tri_area2(const double* p, const double* a, const double* b) {
-    double w[D], u[D];
-#pragma unroll
-    for (int q = 0; q < D; ++q) { w[q] = p[q] - a[q]; u[q] = b[q] - a[q]; }
-    double s2 = 0;
-#pragma unroll
-    for (int x = 0; x < D; ++x)
-#pragma unroll
-        for (int y = x + 1; y < D; ++y) {
-            const double m = fma(w[x], u[y], -(w[y] * u[x]));
-            s2 = fma(m, m, s2);
-        }
-    return sqrt(s2);
-}
-
-// Orthonormal basis (modified Gram-Schmidt) of the normals of a face's
-// defining generators; returns the count.
-template <int D>
-__device__ __forceinline__ int mgs_add(double (&Q)[D][D], int m, const double* nv) {
-    double r[D];
-#pragma unroll
-    for (int q = 0; q < D; ++q) r[q] = nv[q];
-    for (int s = 0; s < m; ++s) {
-        double dt = 0;
-#pragma unroll
-        for (int q = 0; q < D; ++q) dt = fma(Q[s][q], r[q], dt);
-#pragma unroll
-        for (int q = 0; q < D; ++q) r[q] = fma(-dt, Q[s][q], r[q]);
-    }
-    double nn = 0;
-#pragma unroll
-    for (int q = 0; q < D; ++q) nn = fma(r[q], r[q], nn);
-    const double inv = rsqrt(nn);
-#pragma unroll
-    for (int q = 0; q < D; ++q) Q[m][q] = r[q] * inv;
-    return m + 1;
-}
-
-// |n_x . (v - p)| / |component of n_x orthogonal to span(Q[0..m))|: the
-// distance from p to the hyperplane of aff(parent) cut out by generator x.
-template <int D>
-__device__ __forceinline__ double plane_dist(const double (&Q)[D][D], int m, const double* nx, const double* v,
-                                             const double* p) {
-    double r[D], num = 0;
-#pragma unroll
-    for (int q = 0; q < D; ++q) { r[q] = nx[q]; num = fma(nx[q], v[q] - p[q], num); }
-    for (int s = 0; s < m; ++s) {
-        double dt = 0;
-#pragma unroll
-        for (int q = 0; q < D; ++q) dt = fma(Q[s][q], r[q], dt);
-#pragma unroll
-        for (int q = 0; q < D; ++q) r[q] = fma(-dt, Q[s][q], r[q]);
-    }
-    double nn = 0;
-#pragma unroll
-    for (int q = 0; q < D; ++q) nn = fma(r[q], r[q], nn);
-    return fabs(num) * rsqrt(nn);
 }
 
 enum { F_OK = 0, F_CAP = 1, F_BAD = 2 };

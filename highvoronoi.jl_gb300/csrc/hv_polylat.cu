@@ -1,0 +1,385 @@
+// hv_polylat.cu -- VI_POLYGON over the face lattice of the whole mesh.
+//
+// A face of the tessellation is a set S of generators (|S| = c + 1 at
+// codimension c, S[0] a point generator); its vertices are the mesh vertices
+// whose signatures contain S.  The per-facet kernels (hv_poly.cu) build the face
+// lattice of every facet on its own, so a face of codimension c is built and
+// integrated once for each facet through it (a 2-face of a 6D mesh lies in 10
+// facets).  Here every face is built and integrated once:
+//   level 1 (facets): the pair (s_a, s_b) of a vertex's signature is the
+//     neighbour slot of s_b in the row of s_a (the lower cell's slot; the
+//     reference's interfaces are its neighbour pairs, src/polyintegrator.jl:174-316);
+//   level c >= 2: every (c+1)-subset S of a vertex's signature gets the key
+//     (face of S minus its largest generator, at level c-1) << gbits | max(S);
+//     a stable radix sort groups the entries of a face, so a face's index is the
+//     rank of its key; its reference vertex p_G is its first entry's vertex
+//     (entries are numbered subset rank * V + vertex, so that the key pass
+//     writes and reads whole lines);
+//   pairs: each face H of level c+1 lists itself under every parent G = H - {l}
+//     whose first vertex does not lie on H (sub-faces through the reference
+//     point have zero height and are skipped, as in the pulling decomposition);
+//   volumes, bottom-up: a 2-face from its edges (twice the triangle areas), a
+//     face of dimension m > 2 as vol(G) = 1/m * sum over H of dist(p_G, aff H) *
+//     vol(H), each parent's terms in the order of its children's indices (the
+//     sums are bitwise reproducible); a facet's value is the interface area A_ik.
+// Any vertex of G serves as p_G (every term is then a non-negative height
+// times a volume); the per-facet kernels take each face's smallest vertex id,
+// so the two paths sum the same decomposition with other reference points.
+#include <algorithm>
+
+#include "hv_integrate.h"
+#include "hv_internal.cuh"
+#include "hv_polygeo.cuh"
+
+namespace hv {
+
+__host__ __device__ constexpr int lat_binom(int n, int k) {
+    if (k < 0 || k > n) return 0;
+    int r = 1;
+    for (int q = 0; q < k; ++q) r = r * (n - q) / (q + 1);
+    return r;
+}
+
+int lat_subsets(int d, int c) { return lat_binom(d + 1, c + 1); }
+
+// Ranks of the bit masks over a signature (at most 7 generators) among the
+// masks of the same popcount in increasing numeric order (the combinatorial
+// number system, the same rank for every signature length), and the inverse.
+struct LatTabs {
+    unsigned char rank[128];
+    unsigned char mask[8][64];
+};
+__host__ __device__ constexpr LatTabs lat_tabs() {
+    LatTabs t{};
+    int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (unsigned m = 0; m < 128; ++m) {
+        int k = 0;
+        for (unsigned x = m; x; x &= x - 1) ++k;
+        t.rank[m] = (unsigned char)cnt[k];
+        t.mask[k][cnt[k]] = (unsigned char)m;
+        ++cnt[k];
+    }
+    return t;
+}
+__device__ const LatTabs g_lat = lat_tabs();
+
+__device__ __forceinline__ int lat_rank(unsigned m) { return __ldg(&g_lat.rank[m]); }
+__device__ __forceinline__ unsigned lat_unrank(int r, int k) { return __ldg(&g_lat.mask[k][r]); }
+
+__device__ __forceinline__ long long lat_find(const long long* off, const int* nbr, int row, int key) {
+    long long lo = off[row], hi = off[row + 1];
+    const long long end = hi;
+    while (lo < hi) {
+        const long long md = (lo + hi) >> 1;
+        if (nbr[md] < key) lo = md + 1; else hi = md;
+    }
+    return lo < end && nbr[lo] == key ? lo : -1;
+}
+
+static int lat_grid(long long n, int bs) {
+    const long long g = (n + bs - 1) / bs;
+    return (int)std::max(1ll, std::min(g, 1ll << 20));
+}
+
+// ---- level 1: facet slots of every vertex pair, and each facet's smallest vertex
+template <int D>
+__global__ void k_lat_facets(LatIn L, int* F1, unsigned* fref1) {
+    constexpr int G = D + 1;
+    for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < L.V; v += gridDim.x * blockDim.x) {
+        int s[G];
+#pragma unroll
+        for (int q = 0; q < G; ++q) s[q] = L.osig[(size_t)v * G + q];
+        int r = 0;  // masks (1 << a) | (1 << b), a < b, in increasing order
+#pragma unroll
+        for (int b = 1; b < G; ++b)
+#pragma unroll
+            for (int a = 0; a < b; ++a, ++r) {
+                long long t = -1;
+                if (s[a] < L.n) {
+                    t = lat_find(L.nbr_off, L.nbr, s[a], s[b]);
+                    if (t < 0) atomicOr(L.status, 8u);
+                    else atomicMin(fref1 + t, v);
+                }
+                F1[(size_t)r * L.V + v] = (int)t;
+            }
+    }
+}
+
+__global__ void k_lat_slot_cell(int n, const long long* nbr_off, int* slot_cell) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        for (long long t = nbr_off[i]; t < nbr_off[i + 1]; ++t) slot_cell[t] = i;
+}
+
+// ---- level c >= 2: one key per (vertex, (c+1)-subset); subsets whose smallest
+// generator is a plane get the sentinel (they bound no cell's facet)
+template <int D>
+__global__ void k_lat_entries(LatIn L, int c, int gbits, const int* Fp, unsigned long long* keys, int* vals, int* Fc,
+                              unsigned long long* nvalid) {
+    constexpr int G = D + 1;
+    unsigned long long cnt = 0;
+    for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < L.V; v += gridDim.x * blockDim.x) {
+        int s[G];
+#pragma unroll
+        for (int q = 0; q < G; ++q) s[q] = L.osig[(size_t)v * G + q];
+        int r = 0;
+        for (unsigned m = 1; m < (1u << G); ++m) {
+            if (__popc(m) != c + 1) continue;
+            const size_t e = (size_t)(r++) * L.V + v;
+            const int lo = __ffs(m) - 1, hi = 31 - __clz(m);
+            unsigned long long key = ~0ull;
+            if (s[lo] < L.n) {
+                const int pf = Fp[(size_t)lat_rank(m ^ (1u << hi)) * L.V + v];
+                if (pf >= 0) {
+                    key = ((unsigned long long)pf << gbits) | (unsigned long long)(unsigned)s[hi];
+                    ++cnt;
+                } else {
+                    atomicOr(L.status, 8u);
+                }
+            }
+            keys[e] = key;
+            vals[e] = (int)e;
+            if (key == ~0ull) Fc[e] = -1;
+        }
+    }
+    cnt = __reduce_add_sync(0xFFFFFFFFu, (unsigned)cnt);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(nvalid, cnt);
+}
+
+__global__ void k_lat_heads(long long nval, const unsigned long long* sk, long long* flags) {
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x <= nval;
+         x += (long long)gridDim.x * blockDim.x)
+        flags[x] = x < nval && (x == 0 || sk[x] != sk[x - 1]) ? 1 : 0;
+}
+
+// face index of every entry, and each face's first (smallest) vertex with the
+// face's generators as a mask over that vertex's signature; an edge must have
+// exactly two vertices
+template <int D>
+__global__ void k_lat_scatter(LatIn L, int c, long long nval, const long long* fidx, const int* sv, int* Fc,
+                              unsigned* fref, unsigned char* fmask, unsigned* fref2) {
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < nval;
+         x += (long long)gridDim.x * blockDim.x) {
+        const long long f = fidx[x + 1] - 1;
+        const int e = sv[x];
+        Fc[e] = (int)f;
+        if (fidx[x] == fidx[x + 1]) continue;
+        const unsigned v = (unsigned)e % L.V;
+        fref[f] = v;
+        fmask[f] = (unsigned char)lat_unrank((int)((unsigned)e / L.V), c + 1);
+        if (fref2) {
+            const bool two = x + 1 < nval && fidx[x + 2] == fidx[x + 1] && (x + 2 >= nval || fidx[x + 3] != fidx[x + 2]);
+            if (two) {
+                fref2[f] = (unsigned)sv[x + 1] % L.V;
+            } else {
+                fref2[f] = v;
+                atomicOr(L.status, 8u);
+            }
+        }
+    }
+}
+
+// ---- parent -> child lists between levels c and c+1 (count, then fill at
+// off[G] + a per-parent cursor; the volume kernel orders each list)
+template <int D, bool FILL>
+__global__ void k_lat_pairs(LatIn L, int c, long long nH, const unsigned* frefH, const unsigned char* fmaskH,
+                            const int* Fc, const unsigned* frefG, unsigned long long* cnt, const long long* off,
+                            int* child, int* lgen) {
+    constexpr int G = D + 1;
+    for (long long h = blockIdx.x * (long long)blockDim.x + threadIdx.x; h < nH;
+         h += (long long)gridDim.x * blockDim.x) {
+        const unsigned p = frefH[h];
+        const unsigned m = fmaskH[h];
+        int s[G];
+#pragma unroll
+        for (int q = 0; q < G; ++q) s[q] = L.osig[(size_t)p * G + q];
+#pragma unroll
+        for (int q = 0; q < G; ++q) {
+            if (!((m >> q) & 1u)) continue;
+            const unsigned pm = m ^ (1u << q);
+            if (s[__ffs(pm) - 1] >= L.n) continue;
+            const int g = Fc[(size_t)lat_rank(pm) * L.V + p];
+            if (g < 0) {
+                atomicOr(L.status, 8u);
+                continue;
+            }
+            const int l = s[q];
+            const unsigned pg = frefG[g];
+            bool through = false;
+#pragma unroll
+            for (int x = 0; x < G; ++x) through |= (L.osig[(size_t)pg * G + x] == l);
+            if (through) continue;
+            if (!FILL) {
+                atomicAdd(cnt + g, 1ull);
+            } else {
+                const long long pos = off[g] + (long long)atomicAdd(cnt + g, 1ull);
+                child[pos] = (int)h;
+                lgen[pos] = l;
+            }
+        }
+    }
+}
+
+// ---- volumes of the faces of level c from those of level c+1; level 1 writes
+// the interface areas of both slots
+
+// a parent's children in index order (its list is filled in arrival order)
+__device__ __forceinline__ void lat_order(long long a, long long b, int* child, int* lgen) {
+    for (long long x = a + 1; x < b; ++x) {
+        const int h = child[x], l = lgen[x];
+        long long y = x;
+        for (; y > a && child[y - 1] > h; --y) {
+            child[y] = child[y - 1];
+            lgen[y] = lgen[y - 1];
+        }
+        child[y] = h;
+        lgen[y] = l;
+    }
+}
+
+__device__ __forceinline__ void lat_store(const LatIn& L, long long g, bool facets, const int* slot_cell, double vol,
+                                          double* volG) {
+    volG[g] = vol;
+    if (facets) {  // the higher cell's slot of the same interface
+        const int k = L.nbr[g];
+        if (k < L.n) {
+            const long long t = lat_find(L.nbr_off, L.nbr, k, slot_cell[g]);
+            if (t >= 0) volG[t] = vol;
+        }
+    }
+}
+
+// 2-faces (level D-2) from their edges: 1/2 sum |(p - a) ^ (b - a)|
+template <int D>
+__global__ void __launch_bounds__(256) k_lat_area2(LatIn L, long long nG, const long long* off, int* child, int* lgen,
+                                                   const unsigned* frefG, const int* slot_cell, const unsigned* frefH,
+                                                   const unsigned* fref2H, double* volG) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nG;
+         g += (long long)gridDim.x * blockDim.x) {
+        const unsigned pg = frefG[g];
+        if (pg == 0xFFFFFFFFu) continue;  // a slot of the higher cell
+        const long long a = off[g], b = off[g + 1];
+        lat_order(a, b, child, lgen);
+        double p[D];
+#pragma unroll
+        for (int q = 0; q < D; ++q) p[q] = L.oc[(size_t)pg * D + q];
+        double sum = 0.0;
+        for (long long x = a; x < b; ++x) {
+            const int h = child[x];
+            double va[D], vb[D];
+            const unsigned ua = frefH[h], ub = fref2H[h];
+#pragma unroll
+            for (int q = 0; q < D; ++q) { va[q] = L.oc[(size_t)ua * D + q]; vb[q] = L.oc[(size_t)ub * D + q]; }
+            sum += tri_area2<D>(p, va, vb);
+        }
+        lat_store(L, g, D == 3, slot_cell, 0.5 * sum, volG);
+    }
+}
+
+// faces of dimension D - c >= 3: 1/(D-c) sum dist(p_G, aff H) vol(H)
+template <int D>
+__global__ void __launch_bounds__(256, 4) k_lat_volumes(LatIn L, int c, long long nG, const long long* off, int* child,
+                                                     int* lgen, const unsigned* frefG, const unsigned char* fmaskG,
+                                                     const int* slot_cell, const unsigned* frefH, const double* volH,
+                                                     double* volG) {
+    constexpr int G = D + 1;
+    constexpr int QR = D > 3 ? D - 3 : 1;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nG;
+         g += (long long)gridDim.x * blockDim.x) {
+        const unsigned pg = frefG[g];
+        if (pg == 0xFFFFFFFFu) continue;
+        const long long a = off[g], b = off[g + 1];
+        lat_order(a, b, child, lgen);
+        int sg[G];
+        int ns = 0;
+        if (c == 1) {
+            sg[0] = slot_cell[g];
+            sg[1] = L.nbr[g];
+            ns = 2;
+        } else {
+            const unsigned m = fmaskG[g];
+#pragma unroll
+            for (int q = 0; q < G; ++q)
+                if ((m >> q) & 1u) sg[ns++] = L.osig[(size_t)pg * G + q];
+        }
+        double x0[D], p[D];
+#pragma unroll
+        for (int q = 0; q < D; ++q) { x0[q] = L.pts[(size_t)sg[0] * D + q]; p[q] = L.oc[(size_t)pg * D + q]; }
+        double Q[QR][D];
+        int qm = 0;
+        for (int u = 1; u < ns && qm < QR; ++u) {
+            double nv[D];
+            gen_normal<D>(L.n, L.pts, L.planes, sg[u], x0, nv);
+            qm = mgs_add<D>(Q, qm, nv);
+        }
+        double sum = 0.0;
+        for (long long x = a; x < b; ++x) {
+            const int h = child[x];
+            double nl[D], vh[D];
+            gen_normal<D>(L.n, L.pts, L.planes, lgen[x], x0, nl);
+            const unsigned uh = frefH[h];
+#pragma unroll
+            for (int q = 0; q < D; ++q) vh[q] = L.oc[(size_t)uh * D + q];
+            sum += plane_dist<D>(Q, qm, nl, vh, p) * volH[h];
+        }
+        lat_store(L, g, c == 1, slot_cell, sum / (double)(D - c), volG);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+#define LAT_DISPATCH(d, CALL)                          \
+    switch (d) {                                       \
+        case 3: { constexpr int DD = 3; CALL; } break; \
+        case 4: { constexpr int DD = 4; CALL; } break; \
+        case 5: { constexpr int DD = 5; CALL; } break; \
+        case 6: { constexpr int DD = 6; CALL; } break; \
+        default: break;                                \
+    }
+
+void launch_lat_facets(const LatIn& L, int* F1, unsigned* fref1, int* slot_cell, cudaStream_t st) {
+    LAT_DISPATCH(L.d, (k_lat_facets<DD><<<lat_grid(L.V, 256), 256, 0, st>>>(L, F1, fref1)));
+    k_lat_slot_cell<<<lat_grid(L.n, 256), 256, 0, st>>>(L.n, L.nbr_off, slot_cell);
+}
+
+void launch_lat_entries(const LatIn& L, int c, int gbits, const int* Fp, unsigned long long* keys, int* vals, int* Fc,
+                        unsigned long long* nvalid, cudaStream_t st) {
+    LAT_DISPATCH(L.d, (k_lat_entries<DD><<<lat_grid(L.V, 256), 256, 0, st>>>(L, c, gbits, Fp, keys, vals, Fc, nvalid)));
+}
+
+void launch_lat_heads(long long nval, const unsigned long long* sk, long long* flags, cudaStream_t st) {
+    k_lat_heads<<<lat_grid(nval + 1, 256), 256, 0, st>>>(nval, sk, flags);
+}
+
+void launch_lat_scatter(const LatIn& L, int c, long long nval, const long long* fidx, const int* sv, int* Fc,
+                        unsigned* fref, unsigned char* fmask, unsigned* fref2, cudaStream_t st) {
+    LAT_DISPATCH(L.d, (k_lat_scatter<DD><<<lat_grid(nval, 256), 256, 0, st>>>(L, c, nval, fidx, sv, Fc, fref, fmask,
+                                                                           fref2)));
+}
+
+void launch_lat_pairs(const LatIn& L, int c, long long nH, const unsigned* frefH, const unsigned char* fmaskH,
+                      const int* Fc, const unsigned* frefG, unsigned long long* cnt, const long long* off, int* child,
+                      int* lgen, bool fill, cudaStream_t st) {
+    if (fill) {
+        LAT_DISPATCH(L.d, (k_lat_pairs<DD, true><<<lat_grid(nH, 256), 256, 0, st>>>(L, c, nH, frefH, fmaskH, Fc, frefG,
+                                                                                cnt, off, child, lgen)));
+    } else {
+        LAT_DISPATCH(L.d, (k_lat_pairs<DD, false><<<lat_grid(nH, 256), 256, 0, st>>>(L, c, nH, frefH, fmaskH, Fc,
+                                                                                 frefG, cnt, off, child, lgen)));
+    }
+}
+
+void launch_lat_volumes(const LatIn& L, int c, long long nG, const long long* off, int* child, int* lgen,
+                        const unsigned* frefG, const unsigned char* fmaskG, const int* slot_cell,
+                        const unsigned* frefH, const unsigned* fref2H, const double* volH, double* volG,
+                        cudaStream_t st) {
+    if (c == L.d - 2) {
+        LAT_DISPATCH(L.d, (k_lat_area2<DD><<<lat_grid(nG, 256), 256, 0, st>>>(L, nG, off, child, lgen, frefG, slot_cell,
+                                                                             frefH, fref2H, volG)));
+    } else {
+        LAT_DISPATCH(L.d, (k_lat_volumes<DD><<<lat_grid(nG, 256), 256, 0, st>>>(L, c, nG, off, child, lgen, frefG,
+                                                                               fmaskG, slot_cell, frefH, volH, volG)));
+    }
+}
+
+}  // namespace hv

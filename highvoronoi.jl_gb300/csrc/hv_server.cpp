@@ -46,9 +46,14 @@ struct Job {
 
 // Device bytes of one request: vertex records, tables, lists (same model as
 // the build's capacity estimate, src vertices-per-generator counts).
-double estimate_bytes(int d, int64_t n, int K) {
+double estimate_bytes(int d, int64_t n, int K, bool polygon) {
     static const double vpp[7] = {0, 0, 2.2, 7.0, 30.0, 150.0, 1400.0};
     const double V = 1.3 * (vpp[d] * (double)n + (double)(1 << d) + 1024);
+    // VI_POLYGON from d = 5 on: the mesh-wide face lattice's sort buffers (24
+    // bytes per entry, C(d+1, (d+1)/2) entries per vertex), two levels of its
+    // per-vertex face tables and the faces' lists
+    static const double lat[7] = {0, 0, 0, 0, 0, 24.0 * 20 + 8.0 * 20 + 200, 24.0 * 35 + 8.0 * 35 + 300};
+    if (polygon) return V * lat[d] + estimate_bytes(d, n, K, false);
     const int DP = d <= 4 ? 4 : 8;
     const double per_vertex = 4.0 * (d + 1) + 8.0 * d + 4.0 * DP + 4 + 4 + 16 + 8.0 * (d + 1) + 8.0 * (d + 1) * 2 +
                               4.0 * (d + 1) + 8.0 * d;
@@ -224,7 +229,8 @@ int hv_server_submit(hv_server* S, const hv_request* q, int64_t* ticket) {
     J->req.pts = nullptr; J->req.lo = nullptr; J->req.hi = nullptr;
     J->req.periodic = nullptr; J->req.base = nullptr; J->req.normal = nullptr; J->req.bc = nullptr;
     static const int kd[7] = {0, 0, 24, 64, 128, 256, 384};  // the library's default list lengths
-    J->est = estimate_bytes(q->d, (int64_t)n_eff, q->params.knn > 0 ? q->params.knn : kd[q->d]);
+    J->est = estimate_bytes(q->d, (int64_t)n_eff, q->params.knn > 0 ? q->params.knn : kd[q->d],
+                            q->integrator == HV_INTEGRATOR_POLYGON);
     if (J->est > S->budget) return HV_E_OOM;
     J->t_submit = clk::now();
     {

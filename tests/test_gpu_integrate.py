@@ -89,6 +89,7 @@ def test_polygon_tiers_agree(gpu_lib, d, n, seed, monkeypatch):
     """Tiny vertex caps push facets through the shared-memory and the global-memory
     tier-B kernels; every tier must give the same areas as the default run."""
     pts = D.uniform_points(d, n, seed)
+    monkeypatch.setenv("HV_POLY_LATTICE", "0")
     v0, a0 = _mesh(gpu_lib, pts).polygon()
     monkeypatch.setenv("HV_POLY_CAPS", "4,8")
     m = _mesh(gpu_lib, pts)
@@ -97,6 +98,50 @@ def test_polygon_tiers_agree(gpu_lib, d, n, seed, monkeypatch):
     assert st["poly_big_facets"] > 0 and st["ms_poly_big"] > 0
     np.testing.assert_allclose(v1, v0, rtol=1e-13, atol=0)
     np.testing.assert_allclose(a1, a0, rtol=1e-12, atol=1e-15 * max(1.0, a0.max()))
+
+
+def _domain_mesh(hv, kind, d, n, seed):
+    if kind == "box":
+        return _mesh(hv, D.uniform_points(d, n, seed))
+    if kind == "periodic":
+        X = D.uniform_points(d, n, seed)
+        return hv.Mesh(hv.default_context(), X, np.zeros(d), np.ones(d), hv.make_params(hv.HV_METHOD_FAST),
+                       periodic=[1] + [0] * (d - 1))
+    E = np.random.default_rng(seed).exponential(size=(n, d + 1))  # uniform in {x > 0, sum x < 1}
+    X = np.ascontiguousarray(E[:, :d] / E.sum(axis=1, keepdims=True))
+    base = np.array([np.zeros(d) for _ in range(d)] + [np.full(d, 1.0 / d)])
+    normal = np.array([-np.eye(d)[q] for q in range(d)] + [np.ones(d)])
+    return hv.Mesh(hv.default_context(), X, None, None, hv.make_params(hv.HV_METHOD_FAST), planes=(base, normal, None))
+
+
+@pytest.mark.parametrize("d,n,seed,kind", [(d, n, s, k) for d, n, s in [(3, 400, 21), (4, 300, 22), (5, 200, 23),
+                                                                         (6, 80, 24)]
+                                            for k in ("box", "simplex", "periodic") if d < 6 or k != "periodic"])
+def test_mesh_face_lattice_matches_the_facet_lattices(gpu_lib, d, n, seed, kind, monkeypatch):
+    """HV_POLY_LATTICE=1: every face of the mesh built and integrated once
+    (hv_polylat.cu) gives the per-facet face lattices' volumes and areas (the
+    same pulling decomposition, summed in another order) on box, plane and
+    periodic domains, bitwise the same on a second run."""
+    hv = gpu_lib
+    m = _domain_mesh(hv, kind, d, n, seed)
+    monkeypatch.setenv("HV_POLY_LATTICE", "0")
+    v0, a0 = m.polygon()
+    assert m.stats()["ms_poly_incidence"] > 0
+    monkeypatch.setenv("HV_POLY_LATTICE", "1")
+    v1, a1 = m.polygon()
+    assert m.stats()["ms_poly_big"] == 0 and m.stats()["poly_big_facets"] == 0
+    np.testing.assert_allclose(v1, v0, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(a1, a0, rtol=1e-11, atol=1e-15 * max(1.0, a0.max()))
+    v2, a2 = m.polygon()
+    np.testing.assert_array_equal(v2, v1)
+    np.testing.assert_array_equal(a2, a1)
+
+
+@pytest.mark.parametrize("d,n,seed", [(5, 300, 31), (6, 100, 32)])
+def test_mesh_face_lattice_against_the_oracle(gpu_lib, d, n, seed):
+    """The default VI_POLYGON path from d = 5 on against the oracle's flag
+    decomposition (src/polyintegrator.jl:174-468)."""
+    _poly_compare(gpu_lib, D.uniform_points(d, n, seed))
 
 
 def test_fast_polygon_integrator_is_the_polygon_integrator(gpu_lib):
