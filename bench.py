@@ -254,13 +254,6 @@ def fp32_peak_tflops(local, clocks):
 FP64_PEAK_TFLOPS = 1.25  # nominal GB300 FP64 rate; no measured FP64 peak exists for this machine
 
 
-def poly_flops(d, V):
-    """Algorithmic FP64 work of VI_POLYGON: sum over cells of E_cell (d-1)! 2 d^2
-    with E_cell = d V_cell / 2 and sum V_cell = (d+1) V (the flags of the
-    reference's decomposition)."""
-    return d * (d + 1) * V / 2.0 * math.factorial(d - 1) * 2 * d * d
-
-
 def run_lattice(ctx, flush):
     """Co-spherical generators: a 3D lattice of 32^3 points (8 on every interior
     vertex's sphere) -- the search meets the ties and walks the vertex graph
@@ -383,14 +376,16 @@ def run_c3(args, ctx, local, flush, clocks):
         integ[key] = {"ms": 1e3 * statistics.mean(ts), "cells_per_s": n / statistics.mean(ts)}
     st = m.stats()
     poly_dev_ms = st["ms_poly_incidence"] + st["ms_poly_facets"] + st["ms_poly_big"]
-    integ["polygon"].update({"device_ms": poly_dev_ms, "ms_poly_facets": st["ms_poly_facets"],
-                             "ms_poly_big": st["ms_poly_big"], "poly_big_facets": st["poly_big_facets"]})
-    pf = poly_flops(d, V)
-    out["roofline"]["k_poly_facets"] = {
-        "bound": "fp64", "unit": "TFLOP/s", "algorithmic_flops": pf,
-        "achieved": pf / (poly_dev_ms / 1e3) / 1e12, "peak": FP64_PEAK_TFLOPS,
-        "frac": pf / (poly_dev_ms / 1e3) / 1e12 / FP64_PEAK_TFLOPS, "peak_source": "nominal",
-        "note": "flags of the reference's decomposition; the GPU's pulling decomposition does fewer operations"}
+    integ["polygon"].update({"device_ms": poly_dev_ms, "ms_lattice_build": st["ms_poly_incidence"],
+                             "ms_terms": st["ms_poly_facets"], "faces": st["poly_faces"],
+                             "terms": st["poly_terms"]})
+    tf = st["poly_term_flops"]
+    out["roofline"]["k_lat_terms"] = {
+        "bound": "fp64", "unit": "TFLOP/s", "algorithmic_flops": tf,
+        "achieved": tf / (st["ms_poly_facets"] / 1e3) / 1e12, "peak": FP64_PEAK_TFLOPS,
+        "frac": tf / (st["ms_poly_facets"] / 1e3) / 1e12 / FP64_PEAK_TFLOPS, "peak_source": "nominal",
+        "note": "one term per face and sub-face of the mesh-wide face lattice (pulling decomposition), "
+                "FP64 operations counted per term, over the term kernels' device time"}
     integ["heuristic_mc"]["directions_per_cell"] = args.mc_dirs
     m.free()
     # the host CPU on the same phases (the oracle, OpenMP on every host core)
@@ -521,8 +516,8 @@ def run_ours(args):
             t = statistics.mean(ts)
             integ[name] = {"ms": 1e3 * t, "cells_per_s": n / t}
         st = m.stats()
-        integ["polygon"].update({k: st[k] for k in ("poly_big_facets", "ms_poly_incidence", "ms_poly_facets",
-                                                    "ms_poly_big")})
+        integ["polygon"].update({"ms_lattice_build": st["ms_poly_incidence"], "ms_terms": st["ms_poly_facets"],
+                                 "faces": st["poly_faces"], "terms": st["poly_terms"]})
         integ["heuristic_mc"]["directions_per_cell"] = args.mc_dirs
         m.free()
     # ---- end to end through the C ABI with host buffers

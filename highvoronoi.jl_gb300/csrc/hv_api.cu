@@ -1872,6 +1872,9 @@ int periodic_integrate(hv_mesh* m, double* vol, double* area, bool dev_out, F&& 
         m->st.ms_poly_facets = e->st.ms_poly_facets;
         m->st.ms_poly_big = e->st.ms_poly_big;
         m->st.ms_poly_total = e->st.ms_poly_total;
+        m->st.poly_faces = e->st.poly_faces;
+        m->st.poly_terms = e->st.poly_terms;
+        m->st.poly_term_flops = e->st.poly_term_flops;
     } catch (const HvError& e) {
         return fail(m->ctx, e);
     }
@@ -1919,13 +1922,13 @@ bool use_poly_flags(int d) {
     return d >= 3 && e && e[0] == '1';
 }
 
-// VI_POLYGON over the face lattice of the whole mesh (hv_polylat.cu) from
-// d = 5 on (HV_POLY_LATTICE=0 / 1 turns it off / on for every d >= 3); its
+// VI_POLYGON over the face lattice of the whole mesh (hv_polylat.cu) for
+// d >= 3 (HV_POLY_LATTICE=0 selects the per-facet kernels of hv_poly.cu); its
 // tables are indexed by 32-bit entries, so larger meshes take the per-facet
 // kernels.
 bool use_poly_lattice(int d, unsigned V, long long nslots) {
-    int from = 5;
-    if (const char* e = std::getenv("HV_POLY_LATTICE")) from = e[0] == '0' ? 99 : e[0] == '1' ? 3 : from;
+    int from = 3;
+    if (const char* e = std::getenv("HV_POLY_LATTICE")) from = e[0] == '0' ? 99 : from;
     if (d < std::max(from, 3) || d > 6) return false;
     long long emax = 0;
     for (int c = 1; c < d; ++c) emax = std::max(emax, (long long)hv::lat_subsets(d, c));
@@ -1952,7 +1955,8 @@ void poly_lattice(hv_mesh* m, double* area, int* slot_cell, unsigned* dstat, Scr
     std::vector<unsigned*> fref(d + 1, nullptr);
     std::vector<unsigned char*> fmask(d + 1, nullptr);
     std::vector<long long*> off(d + 1, nullptr);
-    std::vector<int*> child(d + 1, nullptr), lgen(d + 1, nullptr);
+    std::vector<int*> child(d + 1, nullptr), lgen(d + 1, nullptr), par(d + 1, nullptr);
+    std::vector<long long> npairs(d + 1, 0);
     unsigned* fref2 = nullptr;
     // level 1: facet slots
     std::unique_ptr<Scratch> fprev(new Scratch(st));
@@ -1981,17 +1985,19 @@ void poly_lattice(hv_mesh* m, double* area, int* slot_cell, unsigned* dstat, Scr
         off[c] = s.get<long long>((size_t)nG + 1);
         kt.run(0, 2, [&] {
             hv::launch_lat_pairs(L, c, nf[c + 1], fref[c + 1], fmask[c + 1], Fc, fref[c], cnt, nullptr, nullptr,
-                                 nullptr, false, st);
+                                 nullptr, nullptr, false, st);
             hv::exclusive_scan_i64(scan_tmp, scan_tb, (const long long*)cnt, off[c], (int)nG + 1, st);
         });
         long long np = 0;
         sync_read(off[c] + nG, &np, sizeof(long long));
+        npairs[c] = np;
         child[c] = s.get<int>((size_t)std::max(np, 1ll));
         lgen[c] = s.get<int>((size_t)std::max(np, 1ll));
+        par[c] = s.get<int>((size_t)std::max(np, 1ll));
         CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (nG + 1), st));
         kt.run(0, 1, [&] {
             hv::launch_lat_pairs(L, c, nf[c + 1], fref[c + 1], fmask[c + 1], Fc, fref[c], cnt, off[c], child[c],
-                                 lgen[c], true, st);
+                                 lgen[c], par[c], true, st);
         });
         CK(cudaGetLastError());
     };
@@ -2033,12 +2039,27 @@ void poly_lattice(hv_mesh* m, double* area, int* slot_cell, unsigned* dstat, Scr
     std::vector<double*> vol(d + 1, nullptr);
     for (int c = d - 2; c >= 1; --c) {
         vol[c] = c == 1 ? area : s.get<double>((size_t)std::max(nf[c], 1ll));
-        kt.run(1, 1, [&] {
-            hv::launch_lat_volumes(L, c, nf[c], off[c], child[c], lgen[c], fref[c], fmask[c], slot_cell, fref[c + 1],
-                                   c + 1 == d - 1 ? fref2 : nullptr, vol[c + 1], vol[c], st);
+        Scratch lv(st);  // this level's frames and terms
+        double* frame = c < d - 2 ? lv.get<double>((size_t)std::max(nf[c], 1ll) * (c + 1) * d) : nullptr;
+        double* term = lv.get<double>((size_t)std::max(npairs[c], 1ll));
+        kt.run(0, 1, [&] {
+            hv::launch_lat_prep(L, c, nf[c], off[c], child[c], lgen[c], fref[c], fmask[c], slot_cell, frame, st);
         });
+        kt.run(1, 1, [&] {
+            hv::launch_lat_terms(L, c, npairs[c], par[c], child[c], lgen[c], fref[c], frame, fref[c + 1],
+                                 c + 1 == d - 1 ? fref2 : nullptr, vol[c + 1], term, st);
+        });
+        kt.run(0, 1, [&] { hv::launch_lat_sum(L, c, nf[c], off[c], term, fref[c], slot_cell, vol[c], st); });
         CK(cudaGetLastError());
     }
+    m->st.poly_faces = 0;
+    m->st.poly_terms = 0;
+    m->st.poly_term_flops = 0;
+    for (int c = 1; c <= d - 2; ++c) {
+        m->st.poly_terms += npairs[c];
+        m->st.poly_term_flops += npairs[c] * hv::lat_term_flops(d, c);
+    }
+    for (int c = 2; c < d; ++c) m->st.poly_faces += nf[c];
 }
 
 int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out) {
@@ -2214,6 +2235,7 @@ int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out) {
         double fam[F_N];
         kt.totals(fam);
         m->st.poly_big_facets = nbig;
+        m->st.poly_faces = m->st.poly_terms = m->st.poly_term_flops = 0;
         m->st.ms_poly_incidence = fam[0];
         m->st.ms_poly_facets = fam[1];
         m->st.ms_poly_big = fam[2];

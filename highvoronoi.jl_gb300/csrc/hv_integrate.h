@@ -93,11 +93,19 @@ void launch_lat_scatter(const LatIn& L, int c, long long nval, const long long* 
                         unsigned* fref, unsigned char* fmask, unsigned* fref2, cudaStream_t st);
 void launch_lat_pairs(const LatIn& L, int c, long long nH, const unsigned* frefH, const unsigned char* fmaskH,
                       const int* Fc, const unsigned* frefG, unsigned long long* cnt, const long long* off, int* child,
-                      int* lgen, bool fill, cudaStream_t st);
-void launch_lat_volumes(const LatIn& L, int c, long long nG, const long long* off, int* child, int* lgen,
-                        const unsigned* frefG, const unsigned char* fmaskG, const int* slot_cell,
-                        const unsigned* frefH, const unsigned* fref2H, const double* volH, double* volG,
-                        cudaStream_t st);
+                      int* lgen, int* par, bool fill, cudaStream_t st);
+// volumes of level c from level c+1: prep (each parent's children in index
+// order and, for c < d - 2, its frame of (c + 1) * d doubles), one term per
+// pair, then each parent's sum (level 1: both slots of the interface)
+void launch_lat_prep(const LatIn& L, int c, long long nG, const long long* off, int* child, int* lgen,
+                     const unsigned* frefG, const unsigned char* fmaskG, const int* slot_cell, double* frame,
+                     cudaStream_t st);
+void launch_lat_terms(const LatIn& L, int c, long long npairs, const int* par, const int* child, const int* lgen,
+                      const unsigned* frefG, const double* frame, const unsigned* frefH, const unsigned* fref2H,
+                      const double* volH, double* term, cudaStream_t st);
+void launch_lat_sum(const LatIn& L, int c, long long nG, const long long* off, const double* term,
+                    const unsigned* frefG, const int* slot_cell, double* volG, cudaStream_t st);
+long long lat_term_flops(int d, int c);  // FP64 operations of one term at level c
 
 // VI_POLYGON areas from the vertices alone (hv_polyflag.cu): every vertex's
 // share of the facets through it (signed flag terms over the circumcentres of

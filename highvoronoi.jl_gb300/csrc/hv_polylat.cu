@@ -183,7 +183,7 @@ __global__ void k_lat_scatter(LatIn L, int c, long long nval, const long long* f
 template <int D, bool FILL>
 __global__ void k_lat_pairs(LatIn L, int c, long long nH, const unsigned* frefH, const unsigned char* fmaskH,
                             const int* Fc, const unsigned* frefG, unsigned long long* cnt, const long long* off,
-                            int* child, int* lgen) {
+                            int* child, int* lgen, int* par) {
     constexpr int G = D + 1;
     for (long long h = blockIdx.x * (long long)blockDim.x + threadIdx.x; h < nH;
          h += (long long)gridDim.x * blockDim.x) {
@@ -214,6 +214,7 @@ __global__ void k_lat_pairs(LatIn L, int c, long long nH, const unsigned* frefH,
                 const long long pos = off[g] + (long long)atomicAdd(cnt + g, 1ull);
                 child[pos] = (int)h;
                 lgen[pos] = l;
+                par[pos] = g;
             }
         }
     }
@@ -248,47 +249,20 @@ __device__ __forceinline__ void lat_store(const LatIn& L, long long g, bool face
     }
 }
 
-// 2-faces (level D-2) from their edges: 1/2 sum |(p - a) ^ (b - a)|
+// Per parent: its children in index order and, above the 2-faces, its frame:
+// the point generator x0 = S_G[0] and an orthonormal basis of the normals of
+// S_G's other generators (c rows), frame[g * (c + 1) * D ...] = x0, Q.
 template <int D>
-__global__ void __launch_bounds__(256) k_lat_area2(LatIn L, long long nG, const long long* off, int* child, int* lgen,
-                                                   const unsigned* frefG, const int* slot_cell, const unsigned* frefH,
-                                                   const unsigned* fref2H, double* volG) {
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nG;
-         g += (long long)gridDim.x * blockDim.x) {
-        const unsigned pg = frefG[g];
-        if (pg == 0xFFFFFFFFu) continue;  // a slot of the higher cell
-        const long long a = off[g], b = off[g + 1];
-        lat_order(a, b, child, lgen);
-        double p[D];
-#pragma unroll
-        for (int q = 0; q < D; ++q) p[q] = L.oc[(size_t)pg * D + q];
-        double sum = 0.0;
-        for (long long x = a; x < b; ++x) {
-            const int h = child[x];
-            double va[D], vb[D];
-            const unsigned ua = frefH[h], ub = fref2H[h];
-#pragma unroll
-            for (int q = 0; q < D; ++q) { va[q] = L.oc[(size_t)ua * D + q]; vb[q] = L.oc[(size_t)ub * D + q]; }
-            sum += tri_area2<D>(p, va, vb);
-        }
-        lat_store(L, g, D == 3, slot_cell, 0.5 * sum, volG);
-    }
-}
-
-// faces of dimension D - c >= 3: 1/(D-c) sum dist(p_G, aff H) vol(H)
-template <int D>
-__global__ void __launch_bounds__(256, 4) k_lat_volumes(LatIn L, int c, long long nG, const long long* off, int* child,
-                                                     int* lgen, const unsigned* frefG, const unsigned char* fmaskG,
-                                                     const int* slot_cell, const unsigned* frefH, const double* volH,
-                                                     double* volG) {
+__global__ void k_lat_prep(LatIn L, int c, long long nG, const long long* off, int* child, int* lgen,
+                           const unsigned* frefG, const unsigned char* fmaskG, const int* slot_cell, double* frame) {
     constexpr int G = D + 1;
     constexpr int QR = D > 3 ? D - 3 : 1;
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nG;
          g += (long long)gridDim.x * blockDim.x) {
         const unsigned pg = frefG[g];
-        if (pg == 0xFFFFFFFFu) continue;
-        const long long a = off[g], b = off[g + 1];
-        lat_order(a, b, child, lgen);
+        if (pg == 0xFFFFFFFFu) continue;  // a slot of the higher cell
+        lat_order(off[g], off[g + 1], child, lgen);
+        if (c >= D - 2) continue;
         int sg[G];
         int ns = 0;
         if (c == 1) {
@@ -301,9 +275,9 @@ __global__ void __launch_bounds__(256, 4) k_lat_volumes(LatIn L, int c, long lon
             for (int q = 0; q < G; ++q)
                 if ((m >> q) & 1u) sg[ns++] = L.osig[(size_t)pg * G + q];
         }
-        double x0[D], p[D];
+        double x0[D];
 #pragma unroll
-        for (int q = 0; q < D; ++q) { x0[q] = L.pts[(size_t)sg[0] * D + q]; p[q] = L.oc[(size_t)pg * D + q]; }
+        for (int q = 0; q < D; ++q) x0[q] = L.pts[(size_t)sg[0] * D + q];
         double Q[QR][D];
         int qm = 0;
         for (int u = 1; u < ns && qm < QR; ++u) {
@@ -311,16 +285,75 @@ __global__ void __launch_bounds__(256, 4) k_lat_volumes(LatIn L, int c, long lon
             gen_normal<D>(L.n, L.pts, L.planes, sg[u], x0, nv);
             qm = mgs_add<D>(Q, qm, nv);
         }
-        double sum = 0.0;
-        for (long long x = a; x < b; ++x) {
-            const int h = child[x];
-            double nl[D], vh[D];
-            gen_normal<D>(L.n, L.pts, L.planes, lgen[x], x0, nl);
-            const unsigned uh = frefH[h];
+        double* fr = frame + (size_t)g * (c + 1) * D;
 #pragma unroll
-            for (int q = 0; q < D; ++q) vh[q] = L.oc[(size_t)uh * D + q];
-            sum += plane_dist<D>(Q, qm, nl, vh, p) * volH[h];
+        for (int q = 0; q < D; ++q) fr[q] = x0[q];
+        for (int r = 0; r < qm; ++r)
+#pragma unroll
+            for (int q = 0; q < D; ++q) fr[(size_t)(r + 1) * D + q] = Q[r][q];
+    }
+}
+
+// One term per (parent, child) pair: 2-faces |(p - a) ^ (b - a)| over their
+// edges, higher faces dist(p_G, aff H) * vol(H) in the parent's frame.
+template <int D>
+__global__ void __launch_bounds__(256) k_lat_terms(LatIn L, int c, long long npairs, const int* par, const int* child,
+                                                   const int* lgen, const unsigned* frefG, const double* frame,
+                                                   const unsigned* frefH, const unsigned* fref2H, const double* volH,
+                                                   double* term) {
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < npairs;
+         x += (long long)gridDim.x * blockDim.x) {
+        const int g = par[x], h = child[x];
+        const unsigned pg = frefG[g];
+        double p[D];
+#pragma unroll
+        for (int q = 0; q < D; ++q) p[q] = L.oc[(size_t)pg * D + q];
+        if (c == D - 2) {
+            double va[D], vb[D];
+            const unsigned ua = frefH[h], ub = fref2H[h];
+#pragma unroll
+            for (int q = 0; q < D; ++q) { va[q] = L.oc[(size_t)ua * D + q]; vb[q] = L.oc[(size_t)ub * D + q]; }
+            term[x] = tri_area2<D>(p, va, vb);
+        } else {
+            const double* fr = frame + (size_t)g * (c + 1) * D;
+            const int l = lgen[x];
+            const unsigned uh = frefH[h];
+            double r[D], num = 0.0;
+            if (l < L.n) {
+#pragma unroll
+                for (int q = 0; q < D; ++q) r[q] = L.pts[(size_t)l * D + q] - fr[q];
+            } else {
+                const DevPlane& B = L.planes[l - L.n];
+#pragma unroll
+                for (int q = 0; q < D; ++q) r[q] = B.n[q];
+            }
+#pragma unroll
+            for (int q = 0; q < D; ++q) num = fma(r[q], L.oc[(size_t)uh * D + q] - p[q], num);
+            for (int s = 1; s <= c; ++s) {  // the component of n_l orthogonal to the frame
+                const double* qs = fr + (size_t)s * D;
+                double dt = 0;
+#pragma unroll
+                for (int q = 0; q < D; ++q) dt = fma(qs[q], r[q], dt);
+#pragma unroll
+                for (int q = 0; q < D; ++q) r[q] = fma(-dt, qs[q], r[q]);
+            }
+            double nn = 0;
+#pragma unroll
+            for (int q = 0; q < D; ++q) nn = fma(r[q], r[q], nn);
+            term[x] = fabs(num) * rsqrt(nn) * volH[h];
         }
+    }
+}
+
+// vol(G) = sum of its terms in child order / dim(G); level 1: both slots
+template <int D>
+__global__ void k_lat_sum(LatIn L, int c, long long nG, const long long* off, const double* term,
+                          const unsigned* frefG, const int* slot_cell, double* volG) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nG;
+         g += (long long)gridDim.x * blockDim.x) {
+        if (frefG[g] == 0xFFFFFFFFu) continue;
+        double sum = 0.0;
+        for (long long x = off[g]; x < off[g + 1]; ++x) sum += term[x];
         lat_store(L, g, c == 1, slot_cell, sum / (double)(D - c), volG);
     }
 }
@@ -359,27 +392,38 @@ void launch_lat_scatter(const LatIn& L, int c, long long nval, const long long* 
 
 void launch_lat_pairs(const LatIn& L, int c, long long nH, const unsigned* frefH, const unsigned char* fmaskH,
                       const int* Fc, const unsigned* frefG, unsigned long long* cnt, const long long* off, int* child,
-                      int* lgen, bool fill, cudaStream_t st) {
+                      int* lgen, int* par, bool fill, cudaStream_t st) {
     if (fill) {
         LAT_DISPATCH(L.d, (k_lat_pairs<DD, true><<<lat_grid(nH, 256), 256, 0, st>>>(L, c, nH, frefH, fmaskH, Fc, frefG,
-                                                                                cnt, off, child, lgen)));
+                                                                                cnt, off, child, lgen, par)));
     } else {
         LAT_DISPATCH(L.d, (k_lat_pairs<DD, false><<<lat_grid(nH, 256), 256, 0, st>>>(L, c, nH, frefH, fmaskH, Fc,
-                                                                                 frefG, cnt, off, child, lgen)));
+                                                                                 frefG, cnt, off, child, lgen, par)));
     }
 }
 
-void launch_lat_volumes(const LatIn& L, int c, long long nG, const long long* off, int* child, int* lgen,
-                        const unsigned* frefG, const unsigned char* fmaskG, const int* slot_cell,
-                        const unsigned* frefH, const unsigned* fref2H, const double* volH, double* volG,
-                        cudaStream_t st) {
-    if (c == L.d - 2) {
-        LAT_DISPATCH(L.d, (k_lat_area2<DD><<<lat_grid(nG, 256), 256, 0, st>>>(L, nG, off, child, lgen, frefG, slot_cell,
-                                                                             frefH, fref2H, volG)));
-    } else {
-        LAT_DISPATCH(L.d, (k_lat_volumes<DD><<<lat_grid(nG, 256), 256, 0, st>>>(L, c, nG, off, child, lgen, frefG,
-                                                                               fmaskG, slot_cell, frefH, volH, volG)));
-    }
+void launch_lat_prep(const LatIn& L, int c, long long nG, const long long* off, int* child, int* lgen,
+                     const unsigned* frefG, const unsigned char* fmaskG, const int* slot_cell, double* frame,
+                     cudaStream_t st) {
+    LAT_DISPATCH(L.d, (k_lat_prep<DD><<<lat_grid(nG, 256), 256, 0, st>>>(L, c, nG, off, child, lgen, frefG, fmaskG,
+                                                                        slot_cell, frame)));
+}
+
+void launch_lat_terms(const LatIn& L, int c, long long npairs, const int* par, const int* child, const int* lgen,
+                      const unsigned* frefG, const double* frame, const unsigned* frefH, const unsigned* fref2H,
+                      const double* volH, double* term, cudaStream_t st) {
+    LAT_DISPATCH(L.d, (k_lat_terms<DD><<<lat_grid(npairs, 256), 256, 0, st>>>(L, c, npairs, par, child, lgen, frefG,
+                                                                             frame, frefH, fref2H, volH, term)));
+}
+
+void launch_lat_sum(const LatIn& L, int c, long long nG, const long long* off, const double* term,
+                    const unsigned* frefG, const int* slot_cell, double* volG, cudaStream_t st) {
+    LAT_DISPATCH(L.d, (k_lat_sum<DD><<<lat_grid(nG, 256), 256, 0, st>>>(L, c, nG, off, term, frefG, slot_cell, volG)));
+}
+
+long long lat_term_flops(int d, int c) {
+    if (c == d - 2) return 2ll * d + 5ll * d * (d - 1) / 2 + 1;  // |(p - a) ^ (b - a)|
+    return 6ll * d + 4ll * c * d + 3;                           // dist(p, aff H) * vol(H)
 }
 
 }  // namespace hv

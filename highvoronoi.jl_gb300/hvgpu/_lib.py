@@ -51,12 +51,13 @@ TIME_FIELDS = ("ms_prepare", "ms_search", "ms_total", "ms_knn", "ms_descent", "m
                "ms_centers", "ms_canonical")
 POLY_FIELDS = ("ms_poly_incidence", "ms_poly_facets", "ms_poly_big", "ms_poly_total")
 FALLBACK_FIELDS = ("fallback_tree_rays", "fallback_nodes", "fallback_leaves", "fallback_points", "ambiguous_sets")
+LATTICE_FIELDS = ("poly_faces", "poly_terms", "poly_term_flops")
 
 
 class Stats(ctypes.Structure):
     _fields_ = ([(n, ctypes.c_int64) for n in STAT_FIELDS] + [(n, ctypes.c_double) for n in TIME_FIELDS] +
                 [("poly_big_facets", ctypes.c_int64)] + [(n, ctypes.c_double) for n in POLY_FIELDS] +
-                [(n, ctypes.c_int64) for n in FALLBACK_FIELDS])
+                [(n, ctypes.c_int64) for n in FALLBACK_FIELDS] + [(n, ctypes.c_int64) for n in LATTICE_FIELDS])
 
 
 class DeviceViews(ctypes.Structure):

@@ -105,8 +105,8 @@ typedef struct {
     double ms_canonical;    /* canonical renumbering */
     /* last hv_integrate_polygon on this mesh */
     int64_t poly_big_facets;   /* facets redone with global-memory work areas */
-    double ms_poly_incidence;  /* facet -> vertex lists (device) */
-    double ms_poly_facets;     /* shared-memory facet kernel (device) */
+    double ms_poly_incidence;  /* facet -> vertex lists (device; the face lattice: see below) */
+    double ms_poly_facets;     /* shared-memory facet kernel (device; the face lattice: its terms) */
     double ms_poly_big;        /* global-memory facet kernel (device) */
     double ms_poly_total;      /* whole call (host wall clock) */
     /* tree pass of the FP32 fallback (rays whose candidate list may miss the winner) */
@@ -115,6 +115,12 @@ typedef struct {
     int64_t fallback_leaves;   /* leaves scanned */
     int64_t fallback_points;   /* points inside the bounding ball (interval-evaluated) */
     int64_t ambiguous_sets;    /* candidate sets decided in FP64 after the FP32 tree search */
+    /* last hv_integrate_polygon through the mesh-wide face lattice (d >= 3; zero
+     * for the per-facet kernels): ms_poly_incidence is then the lattice build,
+     * the children's order, the frames and the sums, ms_poly_facets the terms */
+    int64_t poly_faces;        /* faces of codimension 2 .. d-1 */
+    int64_t poly_terms;        /* (face, sub-face) terms of the pulling decomposition */
+    int64_t poly_term_flops;   /* FP64 operations of those terms (algorithmic count, FMA = 2) */
 } hv_stats;
 
 int hv_version(void);

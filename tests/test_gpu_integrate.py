@@ -129,7 +129,9 @@ def test_mesh_face_lattice_matches_the_facet_lattices(gpu_lib, d, n, seed, kind,
     assert m.stats()["ms_poly_incidence"] > 0
     monkeypatch.setenv("HV_POLY_LATTICE", "1")
     v1, a1 = m.polygon()
-    assert m.stats()["ms_poly_big"] == 0 and m.stats()["poly_big_facets"] == 0
+    st = m.stats()
+    assert st["ms_poly_big"] == 0 and st["poly_big_facets"] == 0
+    assert st["poly_terms"] > 0 and st["poly_term_flops"] > st["poly_terms"] and st["poly_faces"] > 0
     np.testing.assert_allclose(v1, v0, rtol=1e-12, atol=0)
     np.testing.assert_allclose(a1, a0, rtol=1e-11, atol=1e-15 * max(1.0, a0.max()))
     v2, a2 = m.polygon()
