@@ -2004,7 +2004,7 @@ void poly_lattice(hv_mesh* m, double* area, int* slot_cell, unsigned* dstat, Scr
     for (int c = 2; c < d; ++c) {
         const long long E = (long long)V * hv::lat_subsets(d, c);
         std::unique_ptr<Scratch> fcur(new Scratch(st));
-        int* Fc = fcur->get<int>((size_t)std::max(E, 1ll));
+        int* Fc = c < d - 1 ? fcur->get<int>((size_t)std::max(E, 1ll)) : nullptr;  // no level reads the edges
         int fbits = 1;
         while ((1ll << fbits) < nf[c - 1]) ++fbits;
         CK(cudaMemsetAsync(nvalid, 0, sizeof(unsigned long long), st));

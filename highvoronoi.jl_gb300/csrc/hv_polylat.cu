@@ -138,7 +138,7 @@ __global__ void k_lat_entries(LatIn L, int c, int gbits, const int* Fp, unsigned
             }
             keys[e] = key;
             vals[e] = (int)e;
-            if (key == ~0ull) Fc[e] = -1;
+            if (key == ~0ull && Fc) Fc[e] = -1;
         }
     }
     cnt = __reduce_add_sync(0xFFFFFFFFu, (unsigned)cnt);
@@ -161,7 +161,7 @@ __global__ void k_lat_scatter(LatIn L, int c, long long nval, const long long* f
          x += (long long)gridDim.x * blockDim.x) {
         const long long f = fidx[x + 1] - 1;
         const int e = sv[x];
-        Fc[e] = (int)f;
+        if (Fc) Fc[e] = (int)f;  // (the edges' table is never read)
         if (fidx[x] == fidx[x + 1]) continue;
         const unsigned v = (unsigned)e % L.V;
         fref[f] = v;
