@@ -382,6 +382,12 @@ def run_c3(args, ctx, local, flush, clocks):
     integ["polygon"].update({"device_ms": poly_dev_ms, "ms_lattice_build": st["ms_poly_incidence"],
                              "ms_terms": st["ms_poly_facets"], "faces": st["poly_faces"],
                              "terms": st["poly_terms"]})
+    # the reference decomposition's flag count (sum over cells of E_cell (d-1)! 2 d^2,
+    # E_cell = d V_cell / 2, sum V_cell = (d+1) V): the work the reference's
+    # integrator would do, per second of this one
+    ref_flops = d * (d + 1) * V / 2.0 * math.factorial(d - 1) * 2 * d * d
+    integ["polygon"]["reference_flag_flops"] = ref_flops
+    integ["polygon"]["reference_equivalent_tflops"] = ref_flops / (poly_dev_ms / 1e3) / 1e12
     tf = st["poly_term_flops"]
     out["roofline"]["k_lat_terms"] = {
         "bound": "fp64", "unit": "TFLOP/s", "algorithmic_flops": tf,
