@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <functional>
 #include <memory>
 #include <new>
 #include <stdexcept>
@@ -1935,78 +1936,74 @@ bool use_poly_lattice(int d, unsigned V, long long nslots) {
     return (long long)V * emax < (1ll << 31) - 2 && nslots < (1ll << 31) - 2;
 }
 
-// The interface areas of a mesh of simple vertices through the mesh-wide face
-// lattice into area (nslots, zeroed); build time in kt family 0, volumes in 1.
-void poly_lattice(hv_mesh* m, double* area, int* slot_cell, unsigned* dstat, Scratch& s, KTimer& kt) {
+// The faces of levels 1 .. d-1 of a mesh of simple vertices (hv_polylat.cu):
+// counts, reference vertices and masks per level, the edges' second vertices,
+// and (when kept) the per-vertex face tables F[c][rank * V + v].
+struct Lattice {
+    std::vector<long long> nf;
+    std::vector<unsigned*> fref;
+    std::vector<unsigned char*> fmask;
+    unsigned* fref2 = nullptr;
+    std::vector<int*> F;
+};
+
+// on_level(c, F of level c-1, F of level c, entries, sorted entry ids, run starts)
+// runs after level c is numbered, while its sorted entries still exist.
+using LevelFn = std::function<void(int, const int*, const int*, long long, const int*, const long long*)>;
+
+hv::LatIn lat_input(hv_mesh* m, unsigned* dstat) {
+    hv::LatIn L{};
+    L.d = m->d; L.n = m->n; L.V = m->V; L.planes = m->d_planes; L.pts = m->d_in; L.osig = m->osig; L.oc = m->oc;
+    L.nbr_off = m->nbr_off; L.nbr = m->nbr; L.status = dstat;
+    return L;
+}
+
+void lattice_levels(hv_mesh* m, const hv::LatIn& L, int* slot_cell, Scratch& s, KTimer& kt, bool keep, bool starts,
+                    Lattice& T, const LevelFn& on_level) {
     cudaStream_t st = m->ctx->stream;
     const int d = m->d, n = m->n;
     const unsigned V = m->V;
     const long long ns = m->nnbr;
-    hv::LatIn L{};
-    L.d = d; L.n = n; L.V = V; L.planes = m->d_planes; L.pts = m->d_in; L.osig = m->osig; L.oc = m->oc;
-    L.nbr_off = m->nbr_off; L.nbr = m->nbr; L.status = dstat;
     auto sync_read = [&](const void* dev, void* host, size_t b) {
         CK(cudaMemcpyAsync(host, dev, b, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
     };
     int gbits = 1;
     while ((1ll << gbits) <= (long long)n + m->np + 1) ++gbits;
-    std::vector<long long> nf(d + 1, 0);
-    std::vector<unsigned*> fref(d + 1, nullptr);
-    std::vector<unsigned char*> fmask(d + 1, nullptr);
-    std::vector<long long*> off(d + 1, nullptr);
-    std::vector<int*> child(d + 1, nullptr), lgen(d + 1, nullptr), par(d + 1, nullptr);
-    std::vector<long long> npairs(d + 1, 0);
-    unsigned* fref2 = nullptr;
+    T.nf.assign(d + 1, 0);
+    T.fref.assign(d + 1, nullptr);
+    T.fmask.assign(d + 1, nullptr);
+    T.F.assign(d + 1, nullptr);
     // level 1: facet slots
     std::unique_ptr<Scratch> fprev(new Scratch(st));
-    int* Fp = fprev->get<int>((size_t)V * hv::lat_subsets(d, 1));
-    fref[1] = s.get<unsigned>((size_t)std::max(ns, 1ll));
-    nf[1] = ns;
-    CK(cudaMemsetAsync(fref[1], 0xFF, sizeof(unsigned) * std::max(ns, 1ll), st));
-    kt.run(0, 2, [&] { hv::launch_lat_facets(L, Fp, fref[1], slot_cell, st); });
+    int* Fp = (keep ? s : *fprev).get<int>((size_t)V * hv::lat_subsets(d, 1));
+    T.F[1] = keep ? Fp : nullptr;
+    T.fref[1] = s.get<unsigned>((size_t)std::max(ns, 1ll));
+    T.nf[1] = ns;
+    CK(cudaMemsetAsync(T.fref[1], 0xFF, sizeof(unsigned) * std::max(ns, 1ll), st));
+    kt.run(0, 2, [&] { hv::launch_lat_facets(L, Fp, T.fref[1], slot_cell, st); });
     CK(cudaGetLastError());
     long long emax = 1;
     for (int c = 2; c < d; ++c) emax = std::max(emax, (long long)V * hv::lat_subsets(d, c));
-    auto* keys = s.get<unsigned long long>((size_t)emax + 1);
-    auto* keys2 = s.get<unsigned long long>((size_t)emax + 1);
-    int* vals = s.get<int>((size_t)emax);
-    int* vals2 = s.get<int>((size_t)emax);
+    Scratch ws(st);  // the sort's buffers
+    auto* keys = ws.get<unsigned long long>((size_t)emax + 1);
+    auto* keys2 = ws.get<unsigned long long>((size_t)emax + 1);
+    int* vals = ws.get<int>((size_t)emax);
+    int* vals2 = ws.get<int>((size_t)emax);
     const size_t sort_tb = hv::sort_pairs_u64_i32_temp((int)emax);
-    void* sort_tmp = s.get<char>(sort_tb);
-    const size_t scan_tb = hv::scan_temp((int)std::max(emax, ns) + 1);
-    void* scan_tmp = s.get<char>(scan_tb);
-    auto* nvalid = s.get<unsigned long long>(1);
-    auto* cnt = s.get<unsigned long long>((size_t)std::max(emax, ns) + 1);
-    // the child lists of the parents at level c (children at level c + 1)
-    auto pairs = [&](int c, const int* Fc) {
-        const long long nG = nf[c];
-        CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (nG + 1), st));
-        off[c] = s.get<long long>((size_t)nG + 1);
-        kt.run(0, 2, [&] {
-            hv::launch_lat_pairs(L, c, nf[c + 1], fref[c + 1], fmask[c + 1], Fc, fref[c], cnt, nullptr, nullptr,
-                                 nullptr, nullptr, false, st);
-            hv::exclusive_scan_i64(scan_tmp, scan_tb, (const long long*)cnt, off[c], (int)nG + 1, st);
-        });
-        long long np = 0;
-        sync_read(off[c] + nG, &np, sizeof(long long));
-        npairs[c] = np;
-        child[c] = s.get<int>((size_t)std::max(np, 1ll));
-        lgen[c] = s.get<int>((size_t)std::max(np, 1ll));
-        par[c] = s.get<int>((size_t)std::max(np, 1ll));
-        CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (nG + 1), st));
-        kt.run(0, 1, [&] {
-            hv::launch_lat_pairs(L, c, nf[c + 1], fref[c + 1], fmask[c + 1], Fc, fref[c], cnt, off[c], child[c],
-                                 lgen[c], par[c], true, st);
-        });
-        CK(cudaGetLastError());
-    };
+    void* sort_tmp = ws.get<char>(sort_tb);
+    const size_t scan_tb = hv::scan_temp((int)emax + 1);
+    void* scan_tmp = ws.get<char>(scan_tb);
+    auto* nvalid = ws.get<unsigned long long>(1);
     for (int c = 2; c < d; ++c) {
         const long long E = (long long)V * hv::lat_subsets(d, c);
         std::unique_ptr<Scratch> fcur(new Scratch(st));
-        int* Fc = c < d - 1 ? fcur->get<int>((size_t)std::max(E, 1ll)) : nullptr;  // no level reads the edges
+        int* Fc = nullptr;  // no level reads the edges' table unless it is kept
+        if (keep) Fc = s.get<int>((size_t)std::max(E, 1ll));
+        else if (c < d - 1) Fc = fcur->get<int>((size_t)std::max(E, 1ll));
+        T.F[c] = keep ? Fc : nullptr;
         int fbits = 1;
-        while ((1ll << fbits) < nf[c - 1]) ++fbits;
+        while ((1ll << fbits) < T.nf[c - 1]) ++fbits;
         CK(cudaMemsetAsync(nvalid, 0, sizeof(unsigned long long), st));
         kt.run(0, 2, [&] {
             hv::launch_lat_entries(L, c, gbits, Fp, keys, vals, Fc, nvalid, st);
@@ -2021,35 +2018,83 @@ void poly_lattice(hv_mesh* m, double* area, int* slot_cell, unsigned* dstat, Scr
             hv::launch_lat_heads((long long)nval, keys2, heads, st);
             hv::exclusive_scan_i64(scan_tmp, scan_tb, heads, fidx, (int)nval + 1, st);
         });
-        sync_read(fidx + nval, &nf[c], sizeof(long long));
-        fref[c] = s.get<unsigned>((size_t)std::max(nf[c], 1ll));
-        fmask[c] = s.get<unsigned char>((size_t)std::max(nf[c], 1ll));
-        if (c == d - 1) fref2 = s.get<unsigned>((size_t)std::max(nf[c], 1ll));
+        sync_read(fidx + nval, &T.nf[c], sizeof(long long));
+        T.fref[c] = s.get<unsigned>((size_t)std::max(T.nf[c], 1ll));
+        T.fmask[c] = s.get<unsigned char>((size_t)std::max(T.nf[c], 1ll));
+        if (c == d - 1) T.fref2 = s.get<unsigned>((size_t)std::max(T.nf[c], 1ll));
+        long long* hstart = starts ? heads : nullptr;  // the head flags are spent once scanned
         kt.run(0, 1, [&] {
-            hv::launch_lat_scatter(L, c, (long long)nval, fidx, vals2, Fc, fref[c], fmask[c],
-                                   c == d - 1 ? fref2 : nullptr, st);
+            hv::launch_lat_scatter(L, c, (long long)nval, fidx, vals2, Fc, T.fref[c], T.fmask[c],
+                                   c == d - 1 ? T.fref2 : nullptr, hstart, st);
         });
         CK(cudaGetLastError());
-        pairs(c - 1, Fp);
-        fprev = std::move(fcur);
+        on_level(c, Fp, Fc, (long long)nval, vals2, hstart);
+        if (!keep) fprev = std::move(fcur);
         Fp = Fc;
     }
-    fprev.reset();
+}
+
+// The interface areas of a mesh of simple vertices through the mesh-wide face
+// lattice into area (nslots, zeroed); build time in kt family 0, terms in 1.
+void poly_lattice(hv_mesh* m, double* area, int* slot_cell, unsigned* dstat, Scratch& s, KTimer& kt) {
+    cudaStream_t st = m->ctx->stream;
+    const int d = m->d;
+    const long long ns = m->nnbr;
+    const hv::LatIn L = lat_input(m, dstat);
+    auto sync_read = [&](const void* dev, void* host, size_t b) {
+        CK(cudaMemcpyAsync(host, dev, b, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    };
+    Lattice T;
+    std::vector<long long*> off(d + 1, nullptr);
+    std::vector<int*> child(d + 1, nullptr), lgen(d + 1, nullptr), par(d + 1, nullptr);
+    std::vector<long long> npairs(d + 1, 0);
+    long long emax = 1;
+    for (int c = 2; c < d; ++c) emax = std::max(emax, (long long)m->V * hv::lat_subsets(d, c));
+    auto* cnt = s.get<unsigned long long>((size_t)std::max(emax, ns) + 1);
+    const size_t scan_tb = hv::scan_temp((int)std::max(emax, ns) + 1);
+    void* scan_tmp = s.get<char>(scan_tb);
+    // the child lists of the parents at level c - 1 (children at level c)
+    lattice_levels(m, L, slot_cell, s, kt, false, false, T,
+                   [&](int cc, const int* Fprev, const int*, long long, const int*, const long long*) {
+        const int c = cc - 1;
+        const long long nG = T.nf[c];
+        CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (nG + 1), st));
+        off[c] = s.get<long long>((size_t)nG + 1);
+        kt.run(0, 2, [&] {
+            hv::launch_lat_pairs(L, c, T.nf[c + 1], T.fref[c + 1], T.fmask[c + 1], Fprev, T.fref[c], cnt, nullptr,
+                                 nullptr, nullptr, nullptr, false, st);
+            hv::exclusive_scan_i64(scan_tmp, scan_tb, (const long long*)cnt, off[c], (int)nG + 1, st);
+        });
+        long long np = 0;
+        sync_read(off[c] + nG, &np, sizeof(long long));
+        npairs[c] = np;
+        child[c] = s.get<int>((size_t)std::max(np, 1ll));
+        lgen[c] = s.get<int>((size_t)std::max(np, 1ll));
+        par[c] = s.get<int>((size_t)std::max(np, 1ll));
+        CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (nG + 1), st));
+        kt.run(0, 1, [&] {
+            hv::launch_lat_pairs(L, c, T.nf[c + 1], T.fref[c + 1], T.fmask[c + 1], Fprev, T.fref[c], cnt, off[c],
+                                 child[c], lgen[c], par[c], true, st);
+        });
+        CK(cudaGetLastError());
+    });
     // volumes, bottom-up
     std::vector<double*> vol(d + 1, nullptr);
     for (int c = d - 2; c >= 1; --c) {
-        vol[c] = c == 1 ? area : s.get<double>((size_t)std::max(nf[c], 1ll));
+        vol[c] = c == 1 ? area : s.get<double>((size_t)std::max(T.nf[c], 1ll));
         Scratch lv(st);  // this level's frames and terms
-        double* frame = c < d - 2 ? lv.get<double>((size_t)std::max(nf[c], 1ll) * (c + 1) * d) : nullptr;
+        double* frame = c < d - 2 ? lv.get<double>((size_t)std::max(T.nf[c], 1ll) * (c + 1) * d) : nullptr;
         double* term = lv.get<double>((size_t)std::max(npairs[c], 1ll));
         kt.run(0, 1, [&] {
-            hv::launch_lat_prep(L, c, nf[c], off[c], child[c], lgen[c], fref[c], fmask[c], slot_cell, frame, st);
+            hv::launch_lat_prep(L, c, T.nf[c], off[c], child[c], lgen[c], T.fref[c], T.fmask[c], slot_cell, frame,
+                                st);
         });
         kt.run(1, 1, [&] {
-            hv::launch_lat_terms(L, c, npairs[c], par[c], child[c], lgen[c], fref[c], frame, fref[c + 1],
-                                 c + 1 == d - 1 ? fref2 : nullptr, vol[c + 1], term, st);
+            hv::launch_lat_terms(L, c, npairs[c], par[c], child[c], lgen[c], T.fref[c], frame, T.fref[c + 1],
+                                 c + 1 == d - 1 ? T.fref2 : nullptr, vol[c + 1], term, st);
         });
-        kt.run(0, 1, [&] { hv::launch_lat_sum(L, c, nf[c], off[c], term, fref[c], slot_cell, vol[c], st); });
+        kt.run(0, 1, [&] { hv::launch_lat_sum(L, c, T.nf[c], off[c], term, T.fref[c], slot_cell, vol[c], st); });
         CK(cudaGetLastError());
     }
     m->st.poly_faces = 0;
@@ -2059,7 +2104,61 @@ void poly_lattice(hv_mesh* m, double* area, int* slot_cell, unsigned* dstat, Scr
         m->st.poly_terms += npairs[c];
         m->st.poly_term_flops += npairs[c] * hv::lat_term_flops(d, c);
     }
-    for (int c = 2; c < d; ++c) m->st.poly_faces += nf[c];
+    for (int c = 2; c < d; ++c) m->st.poly_faces += T.nf[c];
+}
+
+// The integrand quadrature's flag weights through the face lattice: qw for the
+// facets' sorted vertex lists (qv, foff), the flag sums into qa; the facet
+// centres qc must exist.
+void quad_lattice(hv_mesh* m, const hv::QuadRun& Q, unsigned* dstat) {
+    hv_ctx* ctx = m->ctx;
+    cudaStream_t st = ctx->stream;
+    const int d = m->d;
+    KTimer kt(ctx);
+    Scratch s(st);
+    const hv::LatIn L = lat_input(m, dstat);
+    int* slot_cell = s.get<int>((size_t)std::max(m->nnbr, 1ll));
+    Lattice T;
+    std::vector<double*> cen(d + 1, nullptr);
+    cen[1] = Q.qc;  // the facet centres, by slot
+    lattice_levels(m, L, slot_cell, s, kt, true, true, T,
+                   [&](int c, const int*, const int*, long long nval, const int* sv, const long long* hstart) {
+        if (c > d - 2) return;
+        cen[c] = s.get<double>((size_t)std::max(T.nf[c], 1ll) * d);
+        hv::launch_lat_centroid(L, T.nf[c], nval, hstart, sv, cen[c], st);
+        CK(cudaGetLastError());
+    });
+    // frames of the levels 1 .. d-3 (the parents of the phi levels)
+    std::vector<double*> frame(d + 1, nullptr);
+    for (int c = 1; c <= d - 3; ++c) {
+        frame[c] = s.get<double>((size_t)std::max(T.nf[c], 1ll) * (c + 1) * d);
+        hv::launch_lat_prep(L, c, T.nf[c], nullptr, nullptr, nullptr, T.fref[c], T.fmask[c], slot_cell, frame[c], st);
+    }
+    // phi, top-down over the levels 2 .. d-2
+    std::vector<double*> phi(d + 1, nullptr);
+    for (int c = 2; c <= d - 2; ++c) {
+        phi[c] = s.get<double>((size_t)std::max(T.nf[c], 1ll) * hv::lat_subsets(c, 1));
+        hv::launch_lat_phi(L, c, T.nf[c], T.fref[c], T.fmask[c], T.F[c - 1], frame[c - 1], cen[c - 1], phi[c - 1],
+                           phi[c], st);
+    }
+    // the edges' sums per generator pair, then the (facet, vertex) weights
+    const long long nE = T.nf[d - 1];
+    double* pe = s.get<double>((size_t)std::max(nE, 1ll) * hv::lat_subsets(d - 1, 1));
+    hv::launch_lat_edgew(L, nE, T.fref[d - 1], T.fref2, T.fmask[d - 1], T.F[d - 2], cen[d - 2], phi[d - 2], pe, st);
+    hv::launch_lat_qweights(L, m->nnbr, Q.foff, Q.qv, slot_cell, T.F[d - 1], pe, Q.qw, Q.qa, st);
+    CK(cudaGetLastError());
+}
+
+// The integrand quadrature through the face lattice from d = 4 on
+// (HV_QUAD_LATTICE=1 / 0 turns it on for every d >= 3 / off); the flag walk of
+// hv_quad.cu otherwise (cheap in 3D: a facet's flags are its edges).
+bool use_quad_lattice(int d, unsigned V) {
+    int from = 4;
+    if (const char* e = std::getenv("HV_QUAD_LATTICE")) from = e[0] == '0' ? 99 : e[0] == '1' ? 3 : from;
+    if (d < std::max(from, 3) || d > 6) return false;
+    long long emax = 0;
+    for (int c = 1; c < d; ++c) emax = std::max(emax, (long long)V * hv::lat_subsets(d, c));
+    return emax < (1ll << 31) - 2;
 }
 
 int polygon_impl(hv_mesh* m, double* vol, double* area, bool dev_out) {
@@ -2307,7 +2406,9 @@ void ensure_quad(hv_mesh* m, bool weights) {
     hv::QuadRun Q = quad_run(m);
     Q.fvert = fvert;
     Q.status = dstat;
-    hv::launch_poly_quad(Q, weights, ctx->nsm, st);
+    const bool lat = weights && use_quad_lattice(m->d, m->V);
+    hv::launch_poly_quad(Q, weights && !lat, ctx->nsm, st);  // the sorted lists and the centres at least
+    if (lat) quad_lattice(m, Q, dstat);
     m->q_weights = weights;
     hv::launch_quad_copy(Q, m->d, m->q_c, st);  // centres of the higher cells' slots
     CK(cudaGetLastError());

@@ -89,8 +89,9 @@ void launch_lat_facets(const LatIn& L, int* F1, unsigned* fref1, int* slot_cell,
 void launch_lat_entries(const LatIn& L, int c, int gbits, const int* Fp, unsigned long long* keys, int* vals, int* Fc,
                         unsigned long long* nvalid, cudaStream_t st);
 void launch_lat_heads(long long nval, const unsigned long long* sk, long long* flags, cudaStream_t st);
+// hstart (optional): each face's first position in the sorted entries
 void launch_lat_scatter(const LatIn& L, int c, long long nval, const long long* fidx, const int* sv, int* Fc,
-                        unsigned* fref, unsigned char* fmask, unsigned* fref2, cudaStream_t st);
+                        unsigned* fref, unsigned char* fmask, unsigned* fref2, long long* hstart, cudaStream_t st);
 void launch_lat_pairs(const LatIn& L, int c, long long nH, const unsigned* frefH, const unsigned char* fmaskH,
                       const int* Fc, const unsigned* frefG, unsigned long long* cnt, const long long* off, int* child,
                       int* lgen, int* par, bool fill, cudaStream_t st);
@@ -106,6 +107,23 @@ void launch_lat_terms(const LatIn& L, int c, long long npairs, const int* par, c
 void launch_lat_sum(const LatIn& L, int c, long long nG, const long long* off, const double* term,
                     const unsigned* frefG, const int* slot_cell, double* volG, cudaStream_t st);
 long long lat_term_flops(int d, int c);  // FP64 operations of one term at level c
+// Integrand quadrature over the same lattice (the reference's flag |det| as a
+// product of centroid heights): face centroids of a level from its sorted
+// entries; phi (C(c+1, 2) chain sums per face of level c, from level c-1's
+// frames (launch_lat_prep with off = nullptr), centroids and phi); per edge
+// C(d, 2) sums over its 2-faces; the (facet, vertex) weights into qw and each
+// facet's flag sum into qa (foff / qv: the facets' sorted vertex lists).
+void launch_lat_centroid(const LatIn& L, long long nf, long long nval, const long long* hstart, const int* sv,
+                         double* cen, cudaStream_t st);
+void launch_lat_phi(const LatIn& L, int c, long long nQ, const unsigned* frefQ, const unsigned char* fmaskQ,
+                    const int* Fp, const double* frameP, const double* cenP, const double* phiP, double* phiQ,
+                    cudaStream_t st);
+void launch_lat_edgew(const LatIn& L, long long nE, const unsigned* frefE, const unsigned* fref2E,
+                      const unsigned char* fmaskE, const int* Fp, const double* cenP, const double* phiP, double* pe,
+                      cudaStream_t st);
+void launch_lat_qweights(const LatIn& L, long long ns, const long long* foff, const unsigned* qv,
+                         const int* slot_cell, const int* Fe, const double* pe, double* qw, double* qa,
+                         cudaStream_t st);
 
 // VI_POLYGON areas from the vertices alone (hv_polyflag.cu): every vertex's
 // share of the facets through it (signed flag terms over the circumcentres of

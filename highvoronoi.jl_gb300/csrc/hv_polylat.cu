@@ -156,7 +156,7 @@ __global__ void k_lat_heads(long long nval, const unsigned long long* sk, long l
 // exactly two vertices
 template <int D>
 __global__ void k_lat_scatter(LatIn L, int c, long long nval, const long long* fidx, const int* sv, int* Fc,
-                              unsigned* fref, unsigned char* fmask, unsigned* fref2) {
+                              unsigned* fref, unsigned char* fmask, unsigned* fref2, long long* hstart) {
     for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < nval;
          x += (long long)gridDim.x * blockDim.x) {
         const long long f = fidx[x + 1] - 1;
@@ -165,6 +165,7 @@ __global__ void k_lat_scatter(LatIn L, int c, long long nval, const long long* f
         if (fidx[x] == fidx[x + 1]) continue;
         const unsigned v = (unsigned)e % L.V;
         fref[f] = v;
+        if (hstart) hstart[f] = x;
         fmask[f] = (unsigned char)lat_unrank((int)((unsigned)e / L.V), c + 1);
         if (fref2) {
             const bool two = x + 1 < nval && fidx[x + 2] == fidx[x + 1] && (x + 2 >= nval || fidx[x + 3] != fidx[x + 2]);
@@ -261,7 +262,7 @@ __global__ void k_lat_prep(LatIn L, int c, long long nG, const long long* off, i
          g += (long long)gridDim.x * blockDim.x) {
         const unsigned pg = frefG[g];
         if (pg == 0xFFFFFFFFu) continue;  // a slot of the higher cell
-        lat_order(off[g], off[g + 1], child, lgen);
+        if (off) lat_order(off[g], off[g + 1], child, lgen);
         if (c >= D - 2) continue;
         int sg[G];
         int ns = 0;
@@ -359,6 +360,227 @@ __global__ void k_lat_sum(LatIn L, int c, long long nG, const long long* off, co
 }
 
 // ---------------------------------------------------------------------------
+// integrand quadrature (the reference's flag decomposition with face centroids)
+// ---------------------------------------------------------------------------
+// A flag F = L_1 > L_2 > ... > L_{D-2} > edge (r1, r2) of facet F of cell i has
+// |det(c_F - x_i, c(L_2) - x_i, ..., r1 - x_i, r2 - x_i)| = h_F * prod_{j < D-2}
+// dist(c(L_j), aff L_{j+1}) * |(c(L_{D-2}) - r1) ^ (r2 - r1)|, c(L) the mean of
+// L's vertices, h_F the distance of x_i to F: the product of the heights of the
+// successive centroids.  So for every face Q and every facet F containing it
+// (a generator pair of S_Q) phi_Q[F] = the sum over the chains from F down to Q
+// of the products of their heights, top-down over the face lattice; then each
+// edge's sums per facet, and each (facet, vertex) weight.
+
+// mean of each face's vertices: its entries from hstart[f] to the next face's
+// start, in the sorted order
+template <int D>
+__global__ void k_lat_centroid(LatIn L, long long nf, long long nval, const long long* hstart, const int* sv,
+                               double* cen) {
+    for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < nf;
+         f += (long long)gridDim.x * blockDim.x) {
+        const long long x0 = hstart[f], x1 = f + 1 < nf ? hstart[f + 1] : nval;
+        double sum[D];
+#pragma unroll
+        for (int q = 0; q < D; ++q) sum[q] = 0.0;
+        for (long long x = x0; x < x1; ++x) {
+            const unsigned v = (unsigned)sv[x] % L.V;
+#pragma unroll
+            for (int q = 0; q < D; ++q) sum[q] += L.oc[(size_t)v * D + q];
+        }
+        const double inv = 1.0 / (double)(x1 - x0);
+#pragma unroll
+        for (int q = 0; q < D; ++q) cen[(size_t)f * D + q] = sum[q] * inv;
+    }
+}
+
+// rank of the pair of positions (a, b) among the pairs of a set once position
+// j (j != a, b) is removed
+__device__ __forceinline__ int lat_pair_rank(int a, int b, int j) {
+    const int a2 = a - (j < a ? 1 : 0), b2 = b - (j < b ? 1 : 0);
+    return lat_rank((1u << a2) | (1u << b2));
+}
+
+// dist(p, aff Q) inside aff P for Q = P + {l}: the frame of P (x0, rows), a
+// vertex vq of Q
+template <int D>
+__device__ __forceinline__ double lat_height(const LatIn& L, const double* fr, int rows, int l, const double* vq,
+                                             const double* p) {
+    double r[D], num = 0.0;
+    if (l < L.n) {
+#pragma unroll
+        for (int q = 0; q < D; ++q) r[q] = L.pts[(size_t)l * D + q] - fr[q];
+    } else {
+        const DevPlane& B = L.planes[l - L.n];
+#pragma unroll
+        for (int q = 0; q < D; ++q) r[q] = B.n[q];
+    }
+#pragma unroll
+    for (int q = 0; q < D; ++q) num = fma(r[q], vq[q] - p[q], num);
+    for (int s = 1; s <= rows; ++s) {
+        const double* qs = fr + (size_t)s * D;
+        double dt = 0;
+#pragma unroll
+        for (int q = 0; q < D; ++q) dt = fma(qs[q], r[q], dt);
+#pragma unroll
+        for (int q = 0; q < D; ++q) r[q] = fma(-dt, qs[q], r[q]);
+    }
+    double nn = 0;
+#pragma unroll
+    for (int q = 0; q < D; ++q) nn = fma(r[q], r[q], nn);
+    return fabs(num) * rsqrt(nn);
+}
+
+// phi of the faces Q of level c (2 <= c <= D-2), C(c+1, 2) values per face (the
+// pairs of S_Q's positions in mask-rank order; 0 for a pair of two planes), from
+// the parents of level c-1: their frames, centroids and phi (1 for a facet)
+template <int D>
+__global__ void k_lat_phi(LatIn L, int c, long long nQ, const unsigned* frefQ, const unsigned char* fmaskQ,
+                          const int* Fp, const double* frameP, const double* cenP, const double* phiP, double* phiQ) {
+    constexpr int G = D + 1;
+    const int nq = lat_binom(c + 1, 2), npp = lat_binom(c, 2);
+    for (long long h = blockIdx.x * (long long)blockDim.x + threadIdx.x; h < nQ;
+         h += (long long)gridDim.x * blockDim.x) {
+        const unsigned p = frefQ[h];
+        const unsigned m = fmaskQ[h];
+        int pos[G], gen[G];
+        int k = 0;
+#pragma unroll
+        for (int q = 0; q < G; ++q)
+            if ((m >> q) & 1u) { pos[k] = q; gen[k] = L.osig[(size_t)p * G + q]; ++k; }
+        double vq[D];
+#pragma unroll
+        for (int q = 0; q < D; ++q) vq[q] = L.oc[(size_t)p * D + q];
+        for (int r = 0; r < nq; ++r) phiQ[(size_t)h * nq + r] = 0.0;
+        for (int j = 0; j <= c; ++j) {  // the parent P = Q - gen[j]
+            const unsigned pm = m ^ (1u << pos[j]);
+            if (L.osig[(size_t)p * G + __ffs(pm) - 1] >= L.n) continue;
+            const int g = Fp[(size_t)lat_rank(pm) * L.V + p];
+            if (g < 0) {
+                atomicOr(L.status, 8u);
+                continue;
+            }
+            const double* fr = frameP + (size_t)g * c * D;  // x0 and c - 1 rows
+            const double ht = lat_height<D>(L, fr, c - 1, gen[j], vq, cenP + (size_t)g * D);
+            for (int b = 1; b <= c; ++b)
+                for (int a = 0; a < b; ++a) {
+                    if (a == j || b == j || gen[a] >= L.n) continue;
+                    const double ph = c == 2 ? 1.0 : phiP[(size_t)g * npp + lat_pair_rank(a, b, j)];
+                    phiQ[(size_t)h * nq + lat_rank((1u << a) | (1u << b))] += ph * ht;
+                }
+        }
+    }
+}
+
+// per edge (level D-1) and pair of its D generators: the sum over its 2-faces L
+// of phi_L[pair] * |(c(L) - r1) ^ (r2 - r1)| (D = 3: the 2-faces are the facets,
+// phi = 1)
+template <int D>
+__global__ void k_lat_edgew(LatIn L, long long nE, const unsigned* frefE, const unsigned* fref2E,
+                            const unsigned char* fmaskE, const int* Fp, const double* cenP, const double* phiP,
+                            double* pe) {
+    constexpr int G = D + 1;
+    constexpr int NE = lat_binom(D, 2), NP = lat_binom(D - 1, 2);
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nE;
+         e += (long long)gridDim.x * blockDim.x) {
+        const unsigned p = frefE[e], p2 = fref2E[e];
+        const unsigned m = fmaskE[e];
+        int pos[D], gen[D];
+        int k = 0;
+#pragma unroll
+        for (int q = 0; q < G; ++q)
+            if (((m >> q) & 1u) && k < D) { pos[k] = q; gen[k] = L.osig[(size_t)p * G + q]; ++k; }
+        double va[D], vb[D], acc[NE];
+#pragma unroll
+        for (int q = 0; q < D; ++q) { va[q] = L.oc[(size_t)p * D + q]; vb[q] = L.oc[(size_t)p2 * D + q]; }
+#pragma unroll
+        for (int r = 0; r < NE; ++r) acc[r] = 0.0;
+#pragma unroll
+        for (int j = 0; j < D; ++j) {  // the 2-face L = e - gen[j]
+            const unsigned pm = m ^ (1u << pos[j]);
+            if (L.osig[(size_t)p * G + __ffs(pm) - 1] >= L.n) continue;
+            const int g = Fp[(size_t)lat_rank(pm) * L.V + p];
+            if (g < 0) {
+                atomicOr(L.status, 8u);
+                continue;
+            }
+            const double t = tri_area2<D>(cenP + (size_t)g * D, va, vb);
+#pragma unroll
+            for (int b = 1; b < D; ++b)
+#pragma unroll
+                for (int a = 0; a < b; ++a) {
+                    if (a == j || b == j || gen[a] >= L.n) continue;
+                    const double ph = D == 3 ? 1.0 : phiP[(size_t)g * NP + lat_pair_rank(a, b, j)];
+                    acc[lat_binom(b, 2) + a] += ph * t;
+                }
+        }
+#pragma unroll
+        for (int r = 0; r < NE; ++r) pe[(size_t)e * NE + r] = acc[r];
+    }
+}
+
+// the weight of the a-th vertex v of facet t (i, k): h_F / 2 * the sum over the
+// edges of v inside F (v's generators without one other than i and k) of the
+// edge's sum for (i, k); the facet's flag sum = the sum of its weights
+template <int D>
+__global__ void k_lat_qweights(LatIn L, long long ns, const long long* foff, const unsigned* qv, const int* slot_cell,
+                               const int* Fe, const double* pe, double* qw, double* qa) {
+    constexpr int G = D + 1;
+    constexpr int NE = lat_binom(D, 2);
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ns;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long f0 = foff[t], f1 = foff[t + 1];
+        if (f0 == f1) continue;  // a slot of the higher cell
+        const int i = slot_cell[t], k = L.nbr[t];
+        double h;
+        if (k >= L.n) {
+            double xi[D];
+#pragma unroll
+            for (int q = 0; q < D; ++q) xi[q] = L.pts[(size_t)i * D + q];
+            h = plane_height<D>(L.planes[k - L.n], xi);
+        } else {
+            double s2 = 0;
+#pragma unroll
+            for (int q = 0; q < D; ++q) {
+                const double e = L.pts[(size_t)k * D + q] - L.pts[(size_t)i * D + q];
+                s2 = fma(e, e, s2);
+            }
+            h = 0.5 * sqrt(s2);
+        }
+        double total = 0.0;
+        for (long long x = f0; x < f1; ++x) {
+            const unsigned v = qv[x];
+            int s[G], pi = -1, pk = -1;
+#pragma unroll
+            for (int q = 0; q < G; ++q) {
+                s[q] = L.osig[(size_t)v * G + q];
+                if (s[q] == i) pi = q;
+                if (s[q] == k) pk = q;
+            }
+            double w = 0.0;
+            if (pi < 0 || pk < 0) {
+                atomicOr(L.status, 8u);
+            } else {
+#pragma unroll
+                for (int j = 0; j < G; ++j) {
+                    if (j == pi || j == pk) continue;
+                    const unsigned em = ((1u << G) - 1u) ^ (1u << j);
+                    const int e = Fe[(size_t)lat_rank(em) * L.V + v];
+                    if (e < 0) {
+                        atomicOr(L.status, 8u);
+                        continue;
+                    }
+                    w += pe[(size_t)e * NE + lat_pair_rank(pi, pk, j)];
+                }
+            }
+            w *= 0.5 * h;
+            qw[x] = w;
+            total += w;
+        }
+        qa[t] = total;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 #define LAT_DISPATCH(d, CALL)                          \
@@ -385,9 +607,9 @@ void launch_lat_heads(long long nval, const unsigned long long* sk, long long* f
 }
 
 void launch_lat_scatter(const LatIn& L, int c, long long nval, const long long* fidx, const int* sv, int* Fc,
-                        unsigned* fref, unsigned char* fmask, unsigned* fref2, cudaStream_t st) {
+                        unsigned* fref, unsigned char* fmask, unsigned* fref2, long long* hstart, cudaStream_t st) {
     LAT_DISPATCH(L.d, (k_lat_scatter<DD><<<lat_grid(nval, 256), 256, 0, st>>>(L, c, nval, fidx, sv, Fc, fref, fmask,
-                                                                           fref2)));
+                                                                           fref2, hstart)));
 }
 
 void launch_lat_pairs(const LatIn& L, int c, long long nH, const unsigned* frefH, const unsigned char* fmaskH,
@@ -419,6 +641,32 @@ void launch_lat_terms(const LatIn& L, int c, long long npairs, const int* par, c
 void launch_lat_sum(const LatIn& L, int c, long long nG, const long long* off, const double* term,
                     const unsigned* frefG, const int* slot_cell, double* volG, cudaStream_t st) {
     LAT_DISPATCH(L.d, (k_lat_sum<DD><<<lat_grid(nG, 256), 256, 0, st>>>(L, c, nG, off, term, frefG, slot_cell, volG)));
+}
+
+void launch_lat_centroid(const LatIn& L, long long nf, long long nval, const long long* hstart, const int* sv,
+                         double* cen, cudaStream_t st) {
+    LAT_DISPATCH(L.d, (k_lat_centroid<DD><<<lat_grid(nf, 256), 256, 0, st>>>(L, nf, nval, hstart, sv, cen)));
+}
+
+void launch_lat_phi(const LatIn& L, int c, long long nQ, const unsigned* frefQ, const unsigned char* fmaskQ,
+                    const int* Fp, const double* frameP, const double* cenP, const double* phiP, double* phiQ,
+                    cudaStream_t st) {
+    LAT_DISPATCH(L.d, (k_lat_phi<DD><<<lat_grid(nQ, 128), 128, 0, st>>>(L, c, nQ, frefQ, fmaskQ, Fp, frameP, cenP,
+                                                                       phiP, phiQ)));
+}
+
+void launch_lat_edgew(const LatIn& L, long long nE, const unsigned* frefE, const unsigned* fref2E,
+                      const unsigned char* fmaskE, const int* Fp, const double* cenP, const double* phiP, double* pe,
+                      cudaStream_t st) {
+    LAT_DISPATCH(L.d, (k_lat_edgew<DD><<<lat_grid(nE, 128), 128, 0, st>>>(L, nE, frefE, fref2E, fmaskE, Fp, cenP,
+                                                                         phiP, pe)));
+}
+
+void launch_lat_qweights(const LatIn& L, long long ns, const long long* foff, const unsigned* qv,
+                         const int* slot_cell, const int* Fe, const double* pe, double* qw, double* qa,
+                         cudaStream_t st) {
+    LAT_DISPATCH(L.d, (k_lat_qweights<DD><<<lat_grid(ns, 128), 128, 0, st>>>(L, ns, foff, qv, slot_cell, Fe, pe, qw,
+                                                                            qa)));
 }
 
 long long lat_term_flops(int d, int c) {

@@ -21,7 +21,10 @@
 //
 // Weights: one thread per facet of its lower cell walks the chains with the
 // facet's vertex lists as bit masks (one mask per depth) and solves one d x d
-// determinant in FP64 per flag; facets of up to QUAD_MAXV vertices.
+// determinant in FP64 per flag; facets of up to QUAD_MAXV vertices.  From 4D on
+// the weights come from the mesh-wide face lattice instead (hv_polylat.cu: the
+// same |det| as products of centroid heights, summed once per face); this file
+// then gives the facets' sorted vertex lists and centres.
 #include <algorithm>
 
 #include "hv_integrate.h"
@@ -51,7 +54,7 @@ __global__ void __launch_bounds__(64) k_poly_quad(QuadRun Q) {
         const long long f0 = Q.foff[t];
         const int nv = (int)(Q.foff[t + 1] - f0);
         if (nv == 0) continue;  // a slot of the higher cell: its lower cell computes the facet
-        if (nv > QUAD_MAXV) { atomicOr(Q.status, 1u); continue; }
+        if (WEIGHTS && nv > QUAD_MAXV) { atomicOr(Q.status, 1u); continue; }
         unsigned* qv = Q.qv + f0;
         double* qw = Q.qw + f0;
         // the facet's vertices in id order (the incidence fill left them unordered)

@@ -94,3 +94,49 @@ def test_heuristic_integrand_matches_the_oracle(gpu_lib, d, n, seed):
                 h.append(1.0 - X[i, p // 2] if p % 2 == 0 else X[i, p // 2])
         expect = np.sum(vd.area[i] * np.array(h)) / d
         assert abs(vd.bulk_integral[i][0] - expect) < 1e-12 * max(expect, 1e-300)
+
+
+@pytest.mark.parametrize("d,n,seed", [(3, 300, 21), (4, 150, 22), (5, 80, 23)])
+def test_lattice_quadrature_matches_the_flag_walk(gpu_lib, d, n, seed, monkeypatch):
+    """HV_QUAD_LATTICE=1: the flag weights as products of centroid heights summed
+    over the mesh-wide face lattice (hv_polylat.cu) give the integrals of the
+    per-facet flag walk (hv_quad.cu) and the facet areas for a constant."""
+    hv = gpu_lib
+    X = D.uniform_points(d, n, seed)
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("HV_QUAD_LATTICE", mode)
+        m = hv.Mesh(hv.default_context(), X, np.zeros(d), np.ones(d), hv.make_params(hv.HV_METHOD_FAST))
+        s, r = m.vertices()
+        c = m.facet_centers()
+        res = [m.polygon_functions(f(r), f(c), f(X)) for f in (_lin, _sq)]
+        out[mode] = (c, res, m.polygon())
+    c0, r0, (v0, a0) = out["0"]
+    c1, r1, _ = out["1"]
+    np.testing.assert_array_equal(c1, c0)
+    for (gi0, gb0), (gi1, gb1) in zip(r0, r1):
+        np.testing.assert_allclose(gi1, gi0, rtol=1e-12, atol=1e-15 * np.abs(gi0).max())
+        np.testing.assert_allclose(gb1, gb0, rtol=1e-12, atol=1e-15 * np.abs(gb0).max())
+    np.testing.assert_allclose(r1[0][0][:, 0], a0, rtol=1e-11)
+    np.testing.assert_allclose(r1[0][1][:, 0], v0, rtol=1e-11)
+
+
+def test_lattice_quadrature_6d_against_the_oracle(gpu_lib):
+    """6D: facets beyond the flag walk's vertex cap are no limit for the face
+    lattice; the integrals against the oracle's flag recursion."""
+    hv = gpu_lib
+    d, n = 6, 50
+    X = D.uniform_points(d, n, 31)
+    m = hv.Mesh(hv.default_context(), X, np.zeros(d), np.ones(d), hv.make_params(hv.HV_METHOD_FAST))
+    ref = O.OracleMesh(X, integrate=True)
+    s, r = m.vertices()
+    c = m.facet_centers()
+    vol, area = m.polygon()
+    for f in (_lin, _sq):
+        gi, gb = m.polygon_functions(f(r), f(c), f(X))
+        oi, ob = ref.polygon_functions(f(r), f(c), f(X))
+        assert np.all(np.abs(gi - oi) <= RTOL * np.abs(oi).max(axis=0) + 1e-300)
+        np.testing.assert_allclose(gb, ob, rtol=RTOL, atol=RTOL * np.abs(ob).max())
+    gi, gb = m.polygon_functions(np.ones((len(r), 1)), np.ones((len(c), 1)), np.ones((n, 1)))
+    np.testing.assert_allclose(gi[:, 0], area, rtol=1e-11)
+    np.testing.assert_allclose(gb[:, 0], vol, rtol=1e-11)
