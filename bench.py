@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-serve-capacity", action="store_true", help="skip the unbounded-rate serving run")
+    ap.add_argument("--no-autotune", action="store_true", help="skip the autotuned 5D clustered build")
     ap.add_argument("--serve-integrator", choices=["polygon", "none"], default="polygon")
     ap.add_argument("--no-integrators", action="store_true")
     ap.add_argument("--knn", type=int, default=0, help="candidate list length (0 = library default)")
@@ -338,6 +339,15 @@ def run_c3(args, ctx, local, flush, clocks):
                    "breakdown_ms": {k: statistics.mean(s[k] for s in fst) for k in
                                     ("ms_prepare", "ms_knn", "ms_descent", "ms_expand", "ms_fallback",
                                      "ms_centers", "ms_canonical")}}
+    if not args.no_autotune:
+        # hv_autotune on these points (candidate-list length, leaf size, seed stride), then the
+        # same timed build with the winner; the vertex set does not depend on the knobs
+        tuned = ctx.autotune(d, n, pts=pts, lo=lo, hi=hi)
+        tv, tms, tst = timed(hvgpu.make_params(**tuned), steps, 2)
+        assert tst[-1]["vertices"] == V
+        out["autotuned"] = {"vertices_per_s": tv, "ms_per_step": tms, "steps": steps,
+                            "params": {k: tuned[k] for k in ("knn", "leaf_size", "seed_stride")},
+                            "over_defaults": tv / fv}
     if not args.no_plain:
         pv, pms, pst = timed(hvgpu.make_params(hvgpu.HV_METHOD_PLAIN), 1, 0)
         assert pst[-1]["vertices"] == V
