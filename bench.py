@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--leaf-size", type=int, default=0, help="tree leaf size (0 = library default)")
     ap.add_argument("--seed-stride", type=int, default=0, help="one descent seed per this many generators (0 = default)")
     ap.add_argument("--mc-dirs", type=int, default=1000, help="directions per cell of VI_HEURISTIC_MC")
-    ap.add_argument("--no-c3", action="store_true", help="skip the 5D clustered 50k measurement")
+    ap.add_argument("--no-c3", action="store_true", help="skip the 5D clustered 50k, 2D 1k and 6D 10k measurements")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 arm of the 5D measurement")
     ap.add_argument("--no-lattice", action="store_true", help="skip the 3D lattice (co-spherical generators)")
     return ap.parse_args()
@@ -434,6 +434,91 @@ def run_c3(args, ctx, local, flush, clocks):
     return out
 
 
+def run_small(args, ctx, flush, name, integrator):
+    """A contract workload beside the headline (2D uniform 1k with VI_POLYGON,
+    6D uniform 10k with VI_HEURISTIC_MC at --mc-dirs directions): the build
+    (CUDA events, L2 flushed), its integrator (host wall clock through the C
+    ABI, outputs copied) and the CPU oracle on bounded samples of both phases."""
+    import torch
+    import hvgpu
+    from hvgpu import datasets as D
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    w = D.WORKLOADS[name]
+    pts = D.workload_points(name)
+    n, d = pts.shape
+    lo, hi = np.zeros(d), np.ones(d)
+    dev_pts = torch.from_numpy(np.ascontiguousarray(pts)).cuda()
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    prm = hvgpu.make_params(hvgpu.HV_METHOD_FAST)
+    out = {"workload": name, "d": d, "n_points": n, "seed": w["seed"], "boundary": "cuboid(d, periodic=[])",
+           "l2": "flushed (256 MiB write) before every timed build"}
+    for _ in range(max(args.warmup, 3)):
+        hvgpu.Mesh(ctx, np.array([n, d]), lo, hi, prm, device_ptr=dev_pts.data_ptr()).free()
+    steps = max(1, min(args.steps, 10))
+    tot, V = 0.0, 0
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        m = hvgpu.Mesh(ctx, np.array([n, d]), lo, hi, prm, device_ptr=dev_pts.data_ptr())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1)
+        V = m.stats()["vertices"]
+        m.free()
+    gv = V * steps / (tot / 1e3)
+    out["build"] = {"vertices": V, "ms_per_step": tot / steps, "vertices_per_s": gv, "steps": steps}
+    m = hvgpu.Mesh(ctx, np.array([n, d]), lo, hi, prm, device_ptr=dev_pts.data_ptr())
+    fn = (lambda: m.polygon()) if integrator == "polygon" else (lambda: m.heuristic_mc(args.mc_dirs, 7))
+    for _ in range(3):
+        fn()
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        fn()
+        ts.append(time.perf_counter() - t0)
+    out[integrator] = {"ms": 1e3 * statistics.mean(ts), "cells_per_s": n / statistics.mean(ts)}
+    if integrator == "heuristic_mc":
+        out[integrator]["directions_per_cell"] = args.mc_dirs
+    offs, nbr = m.neighbors()
+    m.free()
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        every = max(1, n // 200)
+        cells = np.arange(0, n, every)
+        own, rays, sec = O.sample_cells(pts, cells, nthreads=threads)
+        out["build"]["cpu"] = {"value": own / sec, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"per-cell search of {len(cells)} of the {n} cells (every {every}th), "
+                                         f"vertices owned per second"}
+        out["build"]["gpu_over_cpu"] = gv / (own / sec)
+        if integrator == "polygon":
+            t0 = time.perf_counter()
+            O.polygon_cells(pts, cells, nthreads=threads)
+            tp = time.perf_counter() - t0
+            out[integrator]["cpu"] = {"cells_per_s": len(cells) / tp, "cores": threads, "kind": "port",
+                                      "sample": f"{len(cells)} of the {n} cells, each cell's search and "
+                                                f"flag-decomposition integral"}
+        else:
+            # the sampled cells keep their neighbour lists (the GPU's), the others none
+            keep = np.zeros(n, dtype=bool)
+            keep[cells] = True
+            cnt = np.where(keep, np.diff(offs), 0)
+            soffs = np.concatenate([[0], np.cumsum(cnt)]).astype(offs.dtype)
+            snbr = np.concatenate([nbr[offs[i]:offs[i + 1]] for i in cells]).astype(nbr.dtype)
+            ref = O.OracleMesh(pts, csr=(soffs, snbr))
+            t0 = time.perf_counter()
+            ref.heuristic_mc(args.mc_dirs, 7, nthreads=threads)
+            tm = time.perf_counter() - t0
+            out[integrator]["cpu"] = {"cells_per_s": len(cells) / tm, "cores": threads, "kind": "port",
+                                      "sample": f"{len(cells)} of the {n} cells (every {every}th) on the GPU's "
+                                                f"neighbour lists, {args.mc_dirs} directions per cell"}
+        out[integrator]["gpu_over_cpu"] = out[integrator]["cells_per_s"] / out[integrator]["cpu"]["cells_per_s"]
+    return out
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -623,6 +708,16 @@ def run_ours(args):
             c3 = run_c3(args, ctx, local, flush, clocks)
         except Exception as e:  # the headline line must still print
             c3 = {"error": repr(e)}
+    c1 = c4 = None
+    if not args.no_c3 and ws == 1:  # the other contract workloads, with their CPU baselines
+        try:
+            c1 = run_small(args, ctx, flush, "2d_uniform_1k", "polygon")
+        except Exception as e:  # the headline line must still print
+            c1 = {"error": repr(e)}
+        try:
+            c4 = run_small(args, ctx, flush, "6d_uniform_10k_mc", "heuristic_mc")
+        except Exception as e:
+            c4 = {"error": repr(e)}
     lattice = None
     if not args.no_lattice and ws == 1:
         try:
@@ -650,7 +745,8 @@ def run_ours(args):
                                           "fallback_nodes", "fallback_leaves", "fallback_points",
                                           "ambiguous_sets")},
             "rays_per_s": st0["rays"] / (tot_ms / 1e3 / args.steps),
-            "breakdown_ms": breakdown, "c3_5d_clustered_50k": c3, "lattice": lattice, "serving": serving}
+            "breakdown_ms": breakdown, "c1_2d_uniform_1k": c1, "c3_5d_clustered_50k": c3,
+            "c4_6d_uniform_10k": c4, "lattice": lattice, "serving": serving}
     print(json.dumps(line), flush=True)
 
 
