@@ -210,7 +210,9 @@ int hv_integrate_polygon(hv_mesh* mesh, double* vol, double* area);
  * simplices the edge average (f(r1)+f(r2))/2 with weight (d-1)/d and the
  * facet centre with weight 1/d; bulk_i = sum_k V_ik f(x_i)/(d+1) +
  * I_ik h_ik/(d+1).  A constant function gives the areas and volumes.  Box
- * and plane-domain meshes; facets of up to 1024 vertices (HV_E_CAPACITY). */
+ * and plane-domain meshes; in 2D and 3D facets of up to 1024 vertices
+ * (HV_E_CAPACITY; from 4D the weights come from the mesh's face lattice, with
+ * no per-facet cap). */
 int hv_mesh_facet_centers(hv_mesh* m, double* centers);
 int hv_integrate_polygon_functions(hv_mesh* m, int p, const double* fv, const double* fc, const double* fx,
                                    double* iface, double* bulk);
