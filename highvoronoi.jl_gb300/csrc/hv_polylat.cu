@@ -81,7 +81,8 @@ static int lat_grid(long long n, int bs) {
     return (int)std::max(1ll, std::min(g, 1ll << 20));
 }
 
-// ---- level 1: facet slots of every vertex pair, and each facet's smallest vertex
+// ---- level 1: facet slots of every vertex pair, and each facet's smallest
+// vertex (its reference vertex)
 template <int D>
 __global__ void k_lat_facets(LatIn L, int* F1, unsigned* fref1) {
     constexpr int G = D + 1;
@@ -151,9 +152,10 @@ __global__ void k_lat_heads(long long nval, const unsigned long long* sk, long l
         flags[x] = x < nval && (x == 0 || sk[x] != sk[x - 1]) ? 1 : 0;
 }
 
-// face index of every entry, and each face's first (smallest) vertex with the
-// face's generators as a mask over that vertex's signature; an edge must have
-// exactly two vertices
+// face index of every entry, and each face's reference vertex (its first
+// entry's) with the face's generators as a mask over that vertex's signature
+// and, if asked, the face's first position; an edge must have exactly two
+// vertices
 template <int D>
 __global__ void k_lat_scatter(LatIn L, int c, long long nval, const long long* fidx, const int* sv, int* Fc,
                               unsigned* fref, unsigned char* fmask, unsigned* fref2, long long* hstart) {
@@ -161,7 +163,7 @@ __global__ void k_lat_scatter(LatIn L, int c, long long nval, const long long* f
          x += (long long)gridDim.x * blockDim.x) {
         const long long f = fidx[x + 1] - 1;
         const int e = sv[x];
-        if (Fc) Fc[e] = (int)f;  // (the edges' table is never read)
+        if (Fc) Fc[e] = (int)f;  // (null for a table that no later pass reads)
         if (fidx[x] == fidx[x + 1]) continue;
         const unsigned v = (unsigned)e % L.V;
         fref[f] = v;
@@ -180,7 +182,7 @@ __global__ void k_lat_scatter(LatIn L, int c, long long nval, const long long* f
 }
 
 // ---- parent -> child lists between levels c and c+1 (count, then fill at
-// off[G] + a per-parent cursor; the volume kernel orders each list)
+// off[G] + a per-parent cursor; k_lat_prep orders each list)
 template <int D, bool FILL>
 __global__ void k_lat_pairs(LatIn L, int c, long long nH, const unsigned* frefH, const unsigned char* fmaskH,
                             const int* Fc, const unsigned* frefG, unsigned long long* cnt, const long long* off,
@@ -296,7 +298,8 @@ __global__ void k_lat_prep(LatIn L, int c, long long nG, const long long* off, i
 }
 
 // One term per (parent, child) pair: 2-faces |(p - a) ^ (b - a)| over their
-// edges, higher faces dist(p_G, aff H) * vol(H) in the parent's frame.
+// edges, higher faces dist(p_G, aff H) * vol(H) in the parent's frame (the
+// arithmetic of lat_height below, inlined: 48 instead of 56 registers in 6D).
 template <int D>
 __global__ void __launch_bounds__(256) k_lat_terms(LatIn L, int c, long long npairs, const int* par, const int* child,
                                                    const int* lgen, const unsigned* frefG, const double* frame,
