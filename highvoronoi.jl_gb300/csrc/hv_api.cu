@@ -2465,7 +2465,7 @@ int mc_impl(hv_mesh* m, int ndir, uint64_t seed, double* vol, double* area, bool
         const int capN = (int)((maxdeg + 7) / 8 * 8);
         int smax = 0;
         cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, m->ctx->device);
-        const size_t sm = (size_t)2 * capN * (d + 2) * sizeof(float) + (size_t)2 * 32 * capN * sizeof(double) + 16;
+        const size_t sm = hv::mc_smem_bytes(d, capN);
         if ((long long)sm > smax) throw HvError(HV_E_CAPACITY, "cell degree too large for the MC integrator");
         Scratch s(st);
         const size_t E = (size_t)std::max(m->nnbr, 1ll);

@@ -85,16 +85,28 @@ __device__ __forceinline__ void mc_direction(unsigned long long seed, unsigned s
     for (int k = 0; k < D; ++k) u[k] *= nn;
 }
 
-constexpr int MC_WPB = 2;
+constexpr int MC_WPB = 4;
+// neighbour records: D offsets, |delta|^2 (or -1 for a plane), 1/|delta| (or the
+// plane's distance), padded to whole float4s
+template <int D>
+__host__ __device__ constexpr int mc_ep() { return D <= 2 ? 4 : 8; }
 
+// One warp per cell, lane s % 32 casts direction s: the nearest bounding
+// hyperplane along u over the cell's neighbours (FP32; a candidate that cannot
+// beat the current minimum costs no division), t^d for the volume and
+// t^(d-1)/|cos| for the facet hit, accumulated in FP64.  The facet sums are
+// per warp: after every 32 directions the lanes that hit one facet add their
+// contributions in direction order, so the result does not depend on the
+// launch shape.
 template <int D>
 __global__ void __launch_bounds__(MC_WPB * 32) k_mc_cells(PolyArgs A, int ndir, unsigned long long seed, int capN,
                                                          double cvol, double* rawV, double* rawA, double* varV) {
+    constexpr int EP = mc_ep<D>();
     extern __shared__ __align__(16) unsigned char smem[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // per warp: capN x (D+1) floats (delta, |delta|^2 or plane code) + 32 x capN doubles
-    float* nb = (float*)(smem) + (size_t)wib * capN * (D + 2);
-    double* slab = (double*)((float*)smem + (size_t)MC_WPB * capN * (D + 2)) + (size_t)wib * 32 * capN;
+    // per warp: capN x EP floats (records) + capN doubles (facet sums)
+    float* nb = (float*)(smem) + (size_t)wib * capN * EP;
+    double* acc = (double*)((float*)smem + (size_t)MC_WPB * capN * EP) + (size_t)wib * capN;
     for (int i = blockIdx.x * MC_WPB + wib; i < A.n; i += gridDim.x * MC_WPB) {
         const long long b = A.nbr_off[i];
         const int deg = (int)(A.nbr_off[i + 1] - b);
@@ -112,12 +124,9 @@ __global__ void __launch_bounds__(MC_WPB * 32) k_mc_cells(PolyArgs A, int ndir, 
             if (lane == 0) atomicOr(A.status, 8u);
             continue;
         }
-        float xi[D];
-#pragma unroll
-        for (int c = 0; c < D; ++c) xi[c] = (float)A.pts[(size_t)i * D + c];
         for (int t = lane; t < deg; t += 32) {
             const int k = A.nbr[b + t];
-            float* e = nb + t * (D + 2);
+            float* e = nb + t * EP;
             if (k < A.n) {
                 float s = 0.f;
 #pragma unroll
@@ -136,44 +145,62 @@ __global__ void __launch_bounds__(MC_WPB * 32) k_mc_cells(PolyArgs A, int ndir, 
                 e[D] = -1.f;  // plane marker
                 e[D + 1] = (float)plane_height<D>(B, xd);
             }
-            for (int l = 0; l < 32; ++l) slab[l * capN + t] = 0.0;
+#pragma unroll
+            for (int c = D + 2; c < EP; ++c) e[c] = 0.f;
+            acc[t] = 0.0;
         }
         __syncwarp();
         double vs = 0.0, vs2 = 0.0;
-        for (int s = lane; s < ndir; s += 32) {
-            float u[D];
-            mc_direction<D>(seed, (unsigned)s, (unsigned long long)i, u);
-            float tb = INFINITY, cosb = 1.f;
+        for (int base = 0; base < ndir; base += 32) {
+            const int s = base + lane;
             int jb = -1;
-            for (int t = 0; t < deg; ++t) {
-                const float* e = nb + t * (D + 2);
-                float tt, cs;
-                if (e[D] >= 0.f) {
-                    float du = 0.f;
+            double val = 0.0;
+            if (s < ndir) {
+                float u[D];
+                mc_direction<D>(seed, (unsigned)s, (unsigned long long)i, u);
+                float tb = INFINITY, cosb = 1.f;
+                for (int t = 0; t < deg; ++t) {
+                    float e[EP];
+                    const float4* e4 = reinterpret_cast<const float4*>(nb + t * EP);
+#pragma unroll
+                    for (int h = 0; h < EP / 4; ++h) {
+                        const float4 f = e4[h];
+                        e[4 * h] = f.x; e[4 * h + 1] = f.y; e[4 * h + 2] = f.z; e[4 * h + 3] = f.w;
+                    }
+                    float du = 0.f;  // delta.u, or n.u (exactly +-u[axis] for axis planes)
 #pragma unroll
                     for (int c = 0; c < D; ++c) du = fmaf(e[c], u[c], du);
                     if (!(du > 0.f)) continue;
-                    tt = e[D] / (2.f * du);
-                    cs = du * e[D + 1];
-                } else {
-                    float uk = 0.f;  // n.u, exactly +-u[axis] for axis planes
-#pragma unroll
-                    for (int c = 0; c < D; ++c) uk = fmaf(e[c], u[c], uk);
-                    if (!(uk > 0.f)) continue;
-                    tt = e[D + 1] / uk;
-                    cs = uk;
+                    float tt, cs;
+                    if (e[D] >= 0.f) {
+                        if (!(e[D] < tb * (2.f * du))) continue;
+                        tt = e[D] / (2.f * du);
+                        cs = du * e[D + 1];
+                    } else {
+                        if (!(e[D + 1] < tb * du)) continue;
+                        tt = e[D + 1] / du;
+                        cs = du;
+                    }
+                    if (tt > 0.f && tt < tb) { tb = tt; jb = t; cosb = cs; }
                 }
-                if (tt > 0.f && tt < tb) { tb = tt; jb = t; cosb = cs; }
-            }
-            if (jb < 0) continue;
-            const double td = (double)tb;
-            double tpow = 1.0;
+                if (jb >= 0) {
+                    const double td = (double)tb;
+                    double tpow = 1.0;
 #pragma unroll
-            for (int c = 0; c < D - 1; ++c) tpow *= td;
-            const double tdd = tpow * td;
-            vs += tdd;
-            vs2 += tdd * tdd;
-            slab[lane * capN + jb] += tpow / fabs((double)cosb);
+                    for (int c = 0; c < D - 1; ++c) tpow *= td;
+                    const double tdd = tpow * td;
+                    vs += tdd;
+                    vs2 += tdd * tdd;
+                    val = tpow / fabs((double)cosb);
+                }
+            }
+            // this round's hits: the lanes that hit the same facet sum their values in
+            // lane (direction) order, the first of them adds the sum
+            const unsigned grp = __match_any_sync(0xFFFFFFFFu, jb);
+            double sum = 0.0;
+            for (unsigned g = grp; g; g &= g - 1) sum += __shfl_sync(grp, val, __ffs(g) - 1);
+            if (jb >= 0 && lane == __ffs(grp) - 1) acc[jb] += sum;
+            __syncwarp();
         }
         // fixed-order reductions
         for (int off = 16; off > 0; off >>= 1) {
@@ -182,11 +209,7 @@ __global__ void __launch_bounds__(MC_WPB * 32) k_mc_cells(PolyArgs A, int ndir, 
         }
         __syncwarp();
         const double carea = D * cvol;
-        for (int t = lane; t < deg; t += 32) {
-            double s = 0.0;
-            for (int l = 0; l < 32; ++l) s += slab[l * capN + t];
-            rawA[b + t] = s * carea / ndir;
-        }
+        for (int t = lane; t < deg; t += 32) rawA[b + t] = acc[t] * carea / ndir;
         if (lane == 0) {
             rawV[i] = vs * cvol / ndir;
             const double m = vs / ndir;
@@ -265,7 +288,7 @@ template <int D>
 static int mc_t(const IntegrateInput& in, int ndir, unsigned long long seed, int capN, double cvol, double* rawV,
                 double* rawA, double* varV, double* outA, double* vol, int nsm, cudaStream_t st) {
     PolyArgs A = make_args(in);
-    const size_t sm = (size_t)MC_WPB * capN * (D + 2) * sizeof(float) + (size_t)MC_WPB * 32 * capN * sizeof(double) + 16;
+    const size_t sm = mc_smem_bytes(D, capN);
     if (cudaFuncSetAttribute(k_mc_cells<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
         return -1;
     int blocks = (in.n + MC_WPB - 1) / MC_WPB;
@@ -275,6 +298,11 @@ static int mc_t(const IntegrateInput& in, int ndir, unsigned long long seed, int
     k_mc_pairs<D><<<(in.n + 255) / 256, 256, 0, st>>>(A, rawA, outA);
     k_mc_volumes<D><<<(in.n + 255) / 256, 256, 0, st>>>(A, rawV, rawA, outA, vol);
     return 0;
+}
+
+size_t mc_smem_bytes(int d, int capN) {
+    const int ep = d <= 2 ? 4 : 8;
+    return (size_t)MC_WPB * capN * ep * sizeof(float) + (size_t)MC_WPB * capN * sizeof(double) + 16;
 }
 
 int launch_heuristic_mc(const IntegrateInput& in, int ndir, unsigned long long seed, int capN, double cvol,

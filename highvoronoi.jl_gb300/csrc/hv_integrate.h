@@ -186,6 +186,8 @@ void launch_quad_integrals(const QuadRun& Q, int p, const double* fv, const doub
                            double* iface, double* bulk, cudaStream_t st);
 // Work-area bytes: per block for tier A, per block (one group) for tier B.
 size_t poly_area_bytes(int d, int capV, int widen, bool tier_b);
+// dynamic shared memory of the MC cell kernel for cells of up to capN neighbours
+size_t mc_smem_bytes(int d, int capN);
 int launch_heuristic_mc(const IntegrateInput& in, int ndir, unsigned long long seed, int capN, double cvol,
                         double* rawV, double* rawA, double* varV, double* outA, double* vol, int nsm,
                         cudaStream_t st);

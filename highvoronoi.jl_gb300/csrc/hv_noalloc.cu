@@ -75,7 +75,7 @@ extern "C" int hv_integrate_heuristic_mc_noalloc(int d, int64_t n, const double*
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     const int capN = (max_degree + 7) / 8 * 8;
-    const size_t sm = (size_t)2 * capN * (d + 2) * sizeof(float) + (size_t)2 * 32 * capN * sizeof(double) + 16;
+    const size_t sm = hv::mc_smem_bytes(d, capN);
     if ((long long)sm > smax) return HV_E_CAPACITY;
     cudaStream_t st = (cudaStream_t)stream;
     unsigned* status = (unsigned*)base;
