@@ -1323,7 +1323,8 @@ __device__ __forceinline__ bool cand_t32(float num, float e_num, float den, floa
 constexpr int FAST_WPB = 4;  // warps per block
 // Candidate records in shared memory (D + 4 words per candidate and warp) for
 // d <= 5; in 6D (lists of 384) they would cost more resident warps than the
-// shared pass saves, and each ray rereads its candidates instead.
+// shared pass saves: there each pass over the list meets two open rays (the
+// list read once per pass, not once per ray: 6D/10k expansion 59 -> 48 ms).
 __host__ __device__ constexpr bool fast_staged(int d) { return d <= 5; }
 inline size_t fast_smem_bytes(int d, int K) {
     return fast_staged(d) ? (size_t)FAST_WPB * (d + 4) * (K > 0 ? K : 1) * sizeof(float) : 0;
@@ -1549,6 +1550,98 @@ __global__ void __launch_bounds__(FAST_WPB * 32, D <= 4 ? 8 : 6) k_expand_fast(D
                 cr[(D + 3) * K + c] = __int_as_float(skip ? -1 : j);
             }
         }
+        if constexpr (!fast_staged(D)) {
+            // ---- 6D: passes over the candidate list, each for two open rays (the list is
+            // read once per pass instead of once per ray)
+            unsigned todo = rmask;
+            while (todo) {
+                int mr[2];
+                mr[0] = __ffs(todo) - 1;
+                todo &= todo - 1;
+                mr[1] = todo ? __ffs(todo) - 1 : -1;
+                if (todo) todo &= todo - 1;
+                const int nr = mr[1] >= 0 ? 2 : 1;
+                float eden[2], lmq[2];
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const int m = q < nr ? mr[q] : mr[0];
+                    lmq[q] = sLam[wib][m];
+                    eden[q] = CD * fabsf(lmq[q]) + 2.f * relu * sLb[wib][m] + TINY * sU1[wib][m];
+                }
+                float lo1[2], hi1[2], lo2[2];
+                int j1[2];
+#pragma unroll
+                for (int q = 0; q < 2; ++q) { lo1[q] = INFINITY; hi1[q] = INFINITY; lo2[q] = INFINITY; j1[q] = -1; }
+                int jn = lane < K ? __ldg(lst + lane) : -1;
+                int jnn = lane + 32 < K ? __ldg(lst + lane + 32) : -1;
+                float xn[DP], xnl[DP];
+#pragma unroll
+                for (int k = 0; k < DP; ++k) { xn[k] = 0.f; xnl[k] = 0.f; }
+                if (jn >= 0) { load_pt32<D>(M, jn, xn); load_pt32lo<D>(M, jn, xnl); }
+                for (int c = lane; c < K; c += 32) {
+                    const int j = jn;
+                    float xj[DP], xjl[DP];
+#pragma unroll
+                    for (int k = 0; k < DP; ++k) { xj[k] = xn[k]; xjl[k] = xnl[k]; }
+                    jn = jnn;
+                    jnn = c + 64 < K ? __ldg(lst + c + 64) : -1;
+                    if (jn >= 0) { load_pt32<D>(M, jn, xn); load_pt32lo<D>(M, jn, xnl); }
+                    if (j < 0) continue;
+                    bool insig = false;
+#pragma unroll
+                    for (int q = 0; q < R; ++q) insig |= (j == sig[q]);
+                    if (insig) continue;
+                    float dl[D], A1 = 0.f, A2 = 0.f, A3 = 0.f, dr = 0.f;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        dl[k] = (xj[k] - xa[k]) + (xjl[k] - xal[k]);
+                        A1 += fabsf(dl[k]);
+                        A2 = fmaf(dl[k], dl[k], A2);
+                        A3 = fmaf(fabsf(dl[k]), fabsf(rho[k]), A3);
+                        dr = fmaf(dl[k], rho[k], dr);
+                    }
+                    const float num = fmaf(-2.f, dr, A2);
+                    const float e_num = CN * (A2 + 2.f * A3) + 2.f * A1 * erho + TINY * (A1 + R1);
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        if (q >= nr) break;
+                        const int m = mr[q];
+                        float du = 0.f, B = 0.f;
+#pragma unroll
+                        for (int k = 0; k < D; ++k) {
+                            const float um = sU[wib][m][k];
+                            du = fmaf(dl[k], um, du);
+                            B = fmaf(fabsf(dl[k]), fabsf(um), B);
+                        }
+                        float lo, hi;
+                        if (!cand_t32(num, e_num, 2.f * (du - lmq[q]), CD * B + 2.f * relu * A1 + eden[q], lo, hi))
+                            continue;
+                        if (lo < lo1[q] || (lo == lo1[q] && j < j1[q])) { lo2[q] = lo1[q]; lo1[q] = lo; hi1[q] = hi; j1[q] = j; }
+                        else if (lo < lo2[q]) lo2[q] = lo;
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    if (q >= nr) break;
+                    float l1 = lo1[q], h1 = hi1[q], l2 = lo2[q];
+                    int jj = j1[q];
+#pragma unroll
+                    for (int off = 16; off > 0; off >>= 1) {
+                        const float olo1 = __shfl_xor_sync(FULL, l1, off);
+                        const float ohi1 = __shfl_xor_sync(FULL, h1, off);
+                        const float olo2 = __shfl_xor_sync(FULL, l2, off);
+                        const int oj1 = __shfl_xor_sync(FULL, jj, off);
+                        const bool take = (olo1 < l1) || (olo1 == l1 && oj1 >= 0 && (jj < 0 || oj1 < jj));
+                        if (take) { l2 = fminf(l1, olo2); l1 = olo1; h1 = ohi1; jj = oj1; }
+                        else { l2 = fminf(l2, olo1); }
+                    }
+                    if (lane == 0) {
+                        const int m = mr[q];
+                        sRlo1[wib][m] = l1; sRhi1[wib][m] = h1; sRlo2[wib][m] = l2; sRj1[wib][m] = jj;
+                    }
+                }
+            }
+        } else {
         // ---- one pass over the records per open ray (the lane reads back only its own
         // entries: no synchronisation needed)
         unsigned todo = rmask;
@@ -1633,6 +1726,7 @@ __global__ void __launch_bounds__(FAST_WPB * 32, D <= 4 ? 8 : 6) k_expand_fast(D
                 else { lo2 = fminf(lo2, olo1); }
             }
             if (lane == 0) { sRlo1[wib][m] = lo1; sRhi1[wib][m] = hi1; sRlo2[wib][m] = lo2; sRj1[wib][m] = j1; }
+        }
         }
         __syncwarp();
         // In a cuboid, every face is at least bdist (its rounding bound emax
