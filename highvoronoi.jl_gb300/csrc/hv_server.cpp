@@ -49,10 +49,11 @@ struct Job {
 double estimate_bytes(int d, int64_t n, int K, bool polygon) {
     static const double vpp[7] = {0, 0, 2.2, 7.0, 30.0, 150.0, 1400.0};
     const double V = 1.3 * (vpp[d] * (double)n + (double)(1 << d) + 1024);
-    // VI_POLYGON from d = 5 on: the mesh-wide face lattice's sort buffers (24
-    // bytes per entry, C(d+1, (d+1)/2) entries per vertex), two levels of its
-    // per-vertex face tables and the faces' lists
-    static const double lat[7] = {0, 0, 0, 0, 0, 24.0 * 20 + 8.0 * 20 + 200, 24.0 * 35 + 8.0 * 35 + 300};
+    // VI_POLYGON from d = 3 on: the mesh-wide face lattice's sort buffers (24
+    // bytes per entry, at most C(d+1, (d+1)/2) entries per vertex), two levels
+    // of its per-vertex face tables and the faces' lists
+    static const double lat[7] = {0, 0, 0, 24.0 * 4 + 8.0 * 6 + 100, 24.0 * 10 + 8.0 * 10 + 150,
+                                  24.0 * 20 + 8.0 * 20 + 200, 24.0 * 35 + 8.0 * 35 + 300};
     if (polygon) return V * lat[d] + estimate_bytes(d, n, K, false);
     const int DP = d <= 4 ? 4 : 8;
     const double per_vertex = 4.0 * (d + 1) + 8.0 * d + 4.0 * DP + 4 + 4 + 16 + 8.0 * (d + 1) + 8.0 * (d + 1) * 2 +
